@@ -1,0 +1,1320 @@
+// fs_api.cu -- host driver of the GB300 FLIP substep and the C ABI of
+// include/fs_gpu.h.
+//
+// One handle = one scene resident in HBM (fs_state.h) plus one CUDA stream.
+// FlipSolver::step() (flipsolver2d.cpp:412-462) becomes a fixed sequence of
+// kernel launches on that stream; the level-set extrapolation, whose result no
+// later stage of the substep reads, runs on a second stream and overlaps the
+// rest.  FlipSolver::stepFrame() keeps the reference's host-side CFL loop
+// (:464-500): one 32-byte device-to-host read per substep brings back the
+// maximum particle speed and the two solvers' iteration counts.
+//
+// Scene setup (frame 0) classifies cells on the GPU and seeds particles on the
+// host with std::mt19937 + std::uniform_real_distribution<float>, the same
+// generator and distribution the reference draws from
+// (flipsolver2d.cpp:71, 1013-1019), so initial particles are bit-identical.
+#include <algorithm>
+#include <atomic>
+#include <cfloat>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <random>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/fs_gpu.h"
+#include "fs_pcg.h"
+#include "fs_state.h"
+
+using namespace fsg;
+
+namespace fsg {
+std::atomic<long long> g_kernel_launches{0};
+}
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+static thread_local std::string t_last_error;
+
+static fs_status fail(fs_status st, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    t_last_error = buf;
+    return st;
+}
+
+#define CK(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t _e = (call);                                                                   \
+        if (_e != cudaSuccess) {                                                                   \
+            if (_e == cudaErrorMemoryAllocation)                                                   \
+                return fail(FS_ERR_OOM, "%s: %s (%s:%d)", #call, cudaGetErrorString(_e), __FILE__, \
+                            __LINE__);                                                             \
+            return fail(FS_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(_e), __FILE__,    \
+                        __LINE__);                                                                 \
+        }                                                                                          \
+    } while (0)
+
+#define TRY(expr)                                                                                  \
+    do {                                                                                           \
+        fs_status _s = (expr);                                                                     \
+        if (_s != FS_OK) return _s;                                                                \
+    } while (0)
+
+extern "C" const char *fs_status_string(fs_status s)
+{
+    switch (s) {
+    case FS_OK: return "ok";
+    case FS_ERR_BAD_ARG: return "bad argument";
+    case FS_ERR_CUDA: return "CUDA error";
+    case FS_ERR_OOM: return "out of device memory";
+    case FS_ERR_TIMEOUT: return "device wait timed out";
+    case FS_ERR_UNSUPPORTED: return "unsupported";
+    case FS_ERR_STATE: return "invalid state";
+    }
+    return "unknown";
+}
+
+extern "C" const char *fs_last_error(void) { return t_last_error.c_str(); }
+
+// ---------------------------------------------------------------------------
+// ThreadPool::splitRange (threadpool.cpp:41-76): the chunk ends of the
+// reference's max-abs residual test
+// ---------------------------------------------------------------------------
+static std::vector<int> split_range_ends(long long length, long long parts)
+{
+    std::vector<int> ends;
+    if (length == 0) return ends;
+    long long numParts = parts < 1 ? 1 : parts;
+    if (length < numParts) numParts = length;
+    long long partSize = length / numParts;
+    if (partSize < 1) partSize = 1;
+    long long remainder = 0;
+    if (partSize * numParts < length) remainder = length - partSize * numParts;
+    long long cs = 0, ce = std::min(partSize, length);
+    for (long long i = 0; i < numParts; i++) {
+        if (i < remainder) ce++;
+        ends.push_back((int)ce);
+        cs = ce;
+        ce = std::min(cs + partSize, length);
+        if (ce == cs) break;
+    }
+    return ends;
+}
+
+static int default_pool_threads()
+{
+    unsigned n = std::thread::hardware_concurrency();
+    return n ? (int)n : 1;
+}
+
+// ---------------------------------------------------------------------------
+// handle
+// ---------------------------------------------------------------------------
+struct Poly {
+    int kind; // 0 solid, 1 initial fluid, 2 sink
+    float value;
+    std::vector<float> xy;
+};
+
+__global__ void k_set_dt(Scalars *sc, float dt) { sc->dt = dt; }
+__global__ void k_fill_i32(int *p, int v, size_t n)
+{
+    size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) p[k] = v;
+}
+
+struct fs_solver {
+    fs_params p{};
+    fs_exec_params ex{};
+    GridDims d{};
+    SceneParams sp{};
+    Particles P;
+    Grids G;
+    Scalars *sc = nullptr;      // device
+    Scalars *sc_host = nullptr; // pinned mirror
+    int prec = FS_PCG_FP32;
+    size_t esz = 4;
+    size_t ncell = 0, nu = 0, nv = 0;
+    void *dens_rhs = nullptr, *dens_x = nullptr, *pres_rhs = nullptr, *pres_x = nullptr;
+    void *r0 = nullptr, *r1 = nullptr, *s0 = nullptr, *s1 = nullptr;
+    double *partials = nullptr;
+    int pcg_grid = 0;
+    int *chunk_end = nullptr, *chunk_last = nullptr;
+    int nchunks = 0;
+    GridBarrier *bar = nullptr;
+    void *rebin_scratch = nullptr;
+    size_t rebin_scratch_size = 0;
+    cudaStream_t st = nullptr, side = nullptr;
+    cudaEvent_t ev_p2g = nullptr, ev_levelset = nullptr;
+    bool levelset_pending = false;
+    std::vector<Poly> polys;
+    std::vector<float> obst_friction;
+    float *d_obst_friction = nullptr;
+    bool friction_dirty = true;
+    int frame = 0;
+    float step_dt = 0.f, frame_dt = 0.f;
+    bool initialized = false;
+    bool after_advect = false;
+    int density_iters_max = 0, pressure_iters_max = 0, substeps = 0;
+    bool timers = false;
+    double t_step_ms = 0.0, t_pcg_ms = 0.0, launches = 0.0;
+    cudaEvent_t e0 = nullptr, e1 = nullptr, p0 = nullptr, p1 = nullptr;
+    std::vector<void *> allocs;
+};
+
+template <typename T> static fs_status dalloc(fs_solver *s, T **p, size_t count)
+{
+    void *q = nullptr;
+    size_t bytes = count * sizeof(T);
+    if (bytes == 0) bytes = 16;
+    CK(cudaMalloc(&q, bytes));
+    s->allocs.push_back(q);
+    *p = (T *)q;
+    return FS_OK;
+}
+
+static void dfree(fs_solver *s, void *p)
+{
+    if (!p) return;
+    auto it = std::find(s->allocs.begin(), s->allocs.end(), p);
+    if (it != s->allocs.end()) s->allocs.erase(it);
+    cudaFree(p);
+}
+
+static fs_status set_device(const fs_solver *s)
+{
+    CK(cudaSetDevice(s->ex.device));
+    return FS_OK;
+}
+
+static fs_status alloc_particles(fs_solver *s, int cap)
+{
+    Particles &P = s->P;
+    void *old[] = {P.pos, P.vel, P.visc, P.slot_bin, P.pos2, P.vel2, P.visc2, P.slot_bin2,
+                   P.flag, P.dest, P.prune_slot, P.mkey, P.mval, P.mkey2, P.mval2};
+    for (void *q : old) dfree(s, q);
+    dfree(s, s->rebin_scratch);
+    P.cap = cap;
+    const size_t n = (size_t)std::max(cap, 1);
+    TRY(dalloc(s, &P.pos, n));
+    TRY(dalloc(s, &P.vel, n));
+    TRY(dalloc(s, &P.visc, n));
+    TRY(dalloc(s, &P.slot_bin, n));
+    TRY(dalloc(s, &P.pos2, n));
+    TRY(dalloc(s, &P.vel2, n));
+    TRY(dalloc(s, &P.visc2, n));
+    TRY(dalloc(s, &P.slot_bin2, n));
+    TRY(dalloc(s, &P.flag, n));
+    TRY(dalloc(s, &P.dest, n));
+    TRY(dalloc(s, &P.prune_slot, n));
+    TRY(dalloc(s, &P.mkey, n));
+    TRY(dalloc(s, &P.mval, n));
+    TRY(dalloc(s, &P.mkey2, n));
+    TRY(dalloc(s, &P.mval2, n));
+    s->rebin_scratch_size = rebin_scratch_bytes(P);
+    void *q = nullptr;
+    CK(cudaMalloc(&q, s->rebin_scratch_size));
+    s->allocs.push_back(q);
+    s->rebin_scratch = q;
+    return FS_OK;
+}
+
+static fs_status upload_particles(fs_solver *s, const std::vector<int> &counts,
+                                  const std::vector<float2> &pos, const std::vector<float2> &vel,
+                                  const std::vector<float> &visc)
+{
+    const int nb = s->P.nbins;
+    const int total = (int)pos.size();
+    if (total > s->P.cap || s->P.pos == nullptr) TRY(alloc_particles(s, total));
+    std::vector<int> start(nb + 1, 0), slot_bin(total);
+    for (int b = 0; b < nb; b++) start[b + 1] = start[b] + counts[b];
+    for (int b = 0; b < nb; b++)
+        for (int k = start[b]; k < start[b + 1]; k++) slot_bin[k] = b;
+    Particles &P = s->P;
+    CK(cudaMemcpyAsync(P.bin_start, start.data(), (nb + 1) * sizeof(int), cudaMemcpyHostToDevice, s->st));
+    CK(cudaMemcpyAsync(P.bin_count, counts.data(), nb * sizeof(int), cudaMemcpyHostToDevice, s->st));
+    if (total) {
+        CK(cudaMemcpyAsync(P.pos, pos.data(), total * sizeof(float2), cudaMemcpyHostToDevice, s->st));
+        CK(cudaMemcpyAsync(P.vel, vel.data(), total * sizeof(float2), cudaMemcpyHostToDevice, s->st));
+        CK(cudaMemcpyAsync(P.visc, visc.data(), total * sizeof(float), cudaMemcpyHostToDevice, s->st));
+        CK(cudaMemcpyAsync(P.slot_bin, slot_bin.data(), total * sizeof(int), cudaMemcpyHostToDevice, s->st));
+    }
+    CK(cudaStreamSynchronize(s->st));
+    s->after_advect = false;
+    return FS_OK;
+}
+
+// updateVelocityFromSolids factors depend on solid cells, solid ids and the
+// obstacles' friction; recompute them whenever one of those was replaced
+static fs_status ensure_friction(fs_solver *s)
+{
+    if (!s->friction_dirty) return FS_OK;
+    if (!s->d_obst_friction) TRY(dalloc(s, &s->d_obst_friction, s->obst_friction.size() + 1));
+    if (!s->obst_friction.empty())
+        CK(cudaMemcpyAsync(s->d_obst_friction, s->obst_friction.data(), s->obst_friction.size() * 4,
+                           cudaMemcpyHostToDevice, s->st));
+    launch_friction_factors(s->d, s->G, s->d_obst_friction, s->st);
+    g_kernel_launches += 1;
+    CK(cudaStreamSynchronize(s->st));
+    s->friction_dirty = false;
+    return FS_OK;
+}
+
+static fs_status wait_side(fs_solver *s)
+{
+    if (s->levelset_pending) {
+        CK(cudaStreamWaitEvent(s->st, s->ev_levelset, 0));
+        s->levelset_pending = false;
+    }
+    return FS_OK;
+}
+
+static fs_status sync_all(fs_solver *s)
+{
+    TRY(wait_side(s));
+    CK(cudaStreamSynchronize(s->st));
+    CK(cudaGetLastError());
+    return FS_OK;
+}
+
+extern "C" fs_status fs_create(const fs_params *p, const fs_exec_params *exec, fs_solver **out)
+{
+    if (!p || !out) return fail(FS_ERR_BAD_ARG, "fs_create: null argument");
+    *out = nullptr;
+    if (p->gridSizeI < 1 || p->gridSizeJ < 1 || p->dx <= 0 || p->fps <= 0 ||
+        p->particlesPerCell < 1 || p->pcgIterLimit < 0)
+        return fail(FS_ERR_BAD_ARG, "fs_create: invalid parameters");
+    if ((long long)p->gridSizeI * p->gridSizeJ > (1LL << 30))
+        return fail(FS_ERR_BAD_ARG, "fs_create: grid too large");
+    if (p->viscosityEnabled)
+        return fail(FS_ERR_UNSUPPORTED, "fs_create: viscosity is not part of this path");
+    if (p->simulationMethod != 0)
+        return fail(FS_ERR_UNSUPPORTED, "fs_create: only SIMULATION_LIQUID is supported");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(FS_ERR_CUDA, "fs_create: no CUDA device");
+    fs_solver *s = new fs_solver();
+    s->p = *p;
+    if (exec) s->ex = *exec;
+    if (s->ex.pool_threads <= 0) s->ex.pool_threads = default_pool_threads();
+    if (s->ex.pool_threads > 4096) s->ex.pool_threads = 4096;
+    if (s->ex.device < 0 || s->ex.device >= ndev) {
+        delete s;
+        return fail(FS_ERR_BAD_ARG, "fs_create: bad device ordinal");
+    }
+    s->prec = s->ex.pcg_precision == FS_PCG_FP64 ? FS_PCG_FP64 : FS_PCG_FP32;
+    s->esz = s->prec == FS_PCG_FP64 ? 8 : 4;
+    auto cleanup = [&](fs_status st) {
+        fs_destroy(s);
+        return st;
+    };
+    if (set_device(s) != FS_OK) return cleanup(FS_ERR_CUDA);
+    GridDims &d = s->d;
+    d.ni = p->gridSizeI;
+    d.nj = p->gridSizeJ;
+    d.bni = d.ni / 3 + (d.ni % 3 != 0);
+    d.bnj = d.nj / 3 + (d.nj % 3 != 0);
+    s->ncell = (size_t)d.ni * d.nj;
+    s->nu = (size_t)(d.ni + 1) * d.nj;
+    s->nv = (size_t)d.ni * (d.nj + 1);
+    SceneParams &sp = s->sp;
+    sp.fluidDensity = p->fluidDensity;
+    sp.dx = p->dx;
+    sp.particlesPerCell = p->particlesPerCell;
+    sp.gI = p->globalAccelerationI;
+    sp.gJ = p->globalAccelerationJ;
+    sp.picRatio = p->picRatio;
+    sp.particleScale = p->particleScale;
+    sp.pcgIterLimit = p->pcgIterLimit;
+    sp.parameterHandlingMethod = p->parameterHandlingMethod;
+    sp.viscosityEnabled = p->viscosityEnabled;
+    sp.projectTolerance = p->viscosityEnabled ? 1e-6 : 1e-2; // flipsolver2d.cpp:73
+    s->step_dt = 1.f / p->fps; // flipsolver2d.cpp:46-47
+    s->frame_dt = 1.f / p->fps;
+
+    fs_status st = FS_OK;
+#define A(expr)                                                                                    \
+    do {                                                                                           \
+        st = (expr);                                                                               \
+        if (st != FS_OK) return cleanup(st);                                                       \
+    } while (0)
+    if (cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->ev_p2g, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->ev_levelset, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreate(&s->e0) != cudaSuccess || cudaEventCreate(&s->e1) != cudaSuccess ||
+        cudaEventCreate(&s->p0) != cudaSuccess || cudaEventCreate(&s->p1) != cudaSuccess)
+        return cleanup(fail(FS_ERR_CUDA, "fs_create: stream/event creation failed"));
+    const size_t n = s->ncell;
+    Grids &G = s->G;
+    A(dalloc(s, &G.material, n));
+    A(dalloc(s, &G.solid_sdf, n));
+    A(dalloc(s, &G.solid_id, n));
+    A(dalloc(s, &G.fluid_sdf, n));
+    A(dalloc(s, &G.u, s->nu));
+    A(dalloc(s, &G.v, s->nv));
+    A(dalloc(s, &G.uvalid, s->nu));
+    A(dalloc(s, &G.vvalid, s->nv));
+    A(dalloc(s, &G.u2, s->nu));
+    A(dalloc(s, &G.v2, s->nv));
+    A(dalloc(s, &G.uvalid2, s->nu));
+    A(dalloc(s, &G.vvalid2, s->nv));
+    A(dalloc(s, &G.su, s->nu));
+    A(dalloc(s, &G.sv, s->nv));
+    A(dalloc(s, &G.suvalid, s->nu));
+    A(dalloc(s, &G.svvalid, s->nv));
+    A(dalloc(s, &G.visc, n));
+    A(dalloc(s, &G.known, n));
+    A(dalloc(s, &G.divc, n));
+    A(dalloc(s, &G.density, n));
+    A(dalloc(s, &G.counts, n));
+    A(dalloc(s, &G.cell_info, n));
+    A(dalloc(s, &G.ufric, n));
+    A(dalloc(s, &G.vfric, n));
+    A(dalloc(s, &G.emitter_id, n));
+    A(dalloc(s, &G.levelset_marker, n));
+    A(dalloc(s, &G.levelset_marker2, n));
+    A(dalloc(s, &G.levelset_val2, 2 * n));
+    A(dalloc(s, &G.levelset_active, (size_t)levelset_max_passes(d) + 1));
+    Particles &P = s->P;
+    P.nbins = d.bni * d.bnj;
+    A(dalloc(s, &P.bin_start, (size_t)P.nbins + 1));
+    A(dalloc(s, &P.bin_count, (size_t)P.nbins));
+    A(dalloc(s, &P.bin_start2, (size_t)P.nbins + 1));
+    A(dalloc(s, &P.bin_count2, (size_t)P.nbins));
+    A(dalloc(s, &P.survivors, (size_t)P.nbins));
+    A(dalloc(s, &P.incoming, (size_t)P.nbins + 1));
+    A(dalloc(s, &P.inc_off, (size_t)P.nbins + 1));
+    A(dalloc(s, &P.nmoved, 1));
+    A(dalloc(s, &s->sc, 1));
+    if (cudaMallocHost(&s->sc_host, sizeof(Scalars)) != cudaSuccess)
+        return cleanup(fail(FS_ERR_OOM, "fs_create: pinned allocation failed"));
+    // PCG vectors
+    const size_t vb = n * s->esz;
+    void **vecs[] = {&s->dens_rhs, &s->dens_x, &s->pres_rhs, &s->pres_x, &s->r0, &s->r1, &s->s0, &s->s1};
+    for (void **v : vecs) {
+        char *q = nullptr;
+        A(dalloc(s, &q, vb));
+        *v = q;
+    }
+    s->pcg_grid = s->prec == FS_PCG_FP64 ? pcg_grid_size<double>((long long)n)
+                                         : pcg_grid_size<float>((long long)n);
+    A(dalloc(s, &s->partials, (size_t)3 * s->pcg_grid + 8));
+    A(dalloc(s, &s->bar, 1));
+    std::vector<int> ends = split_range_ends((long long)n, s->ex.pool_threads);
+    s->nchunks = (int)ends.size();
+    A(dalloc(s, &s->chunk_end, ends.size() + 1));
+    A(dalloc(s, &s->chunk_last, ends.size() + 1));
+    if (!ends.empty() &&
+        cudaMemcpy(s->chunk_end, ends.data(), ends.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+        return cleanup(fail(FS_ERR_CUDA, "fs_create: upload failed"));
+
+    // initial grid state (FlipSolver ctor, flipsolver2d.cpp:27-45)
+    cudaStream_t q = s->st;
+    bool ok = cudaMemsetAsync(G.material, 0x10, n, q) == cudaSuccess; // EMPTY
+    k_fill_i32<<<(unsigned)((n + 255) / 256), 256, 0, q>>>(G.solid_id, -1, n);
+    k_fill_i32<<<(unsigned)((n + 255) / 256), 256, 0, q>>>(G.emitter_id, -1, n);
+    void *zero[] = {G.solid_sdf, G.fluid_sdf, G.visc, G.known, G.divc, G.density, G.counts,
+                    G.cell_info};
+    size_t zsz[] = {n * 4, n * 4, n * 4, n, n * 4, n * 4, n * 4, n};
+    for (int k = 0; k < 8; k++) ok = ok && cudaMemsetAsync(zero[k], 0, zsz[k], q) == cudaSuccess;
+    void *zu[] = {G.u, G.u2, G.su};
+    void *zv[] = {G.v, G.v2, G.sv};
+    for (int k = 0; k < 3; k++) {
+        ok = ok && cudaMemsetAsync(zu[k], 0, s->nu * 4, q) == cudaSuccess;
+        ok = ok && cudaMemsetAsync(zv[k], 0, s->nv * 4, q) == cudaSuccess;
+    }
+    void *zf[] = {G.uvalid, G.uvalid2, G.suvalid};
+    void *zg[] = {G.vvalid, G.vvalid2, G.svvalid};
+    for (int k = 0; k < 3; k++) {
+        ok = ok && cudaMemsetAsync(zf[k], 0, s->nu, q) == cudaSuccess;
+        ok = ok && cudaMemsetAsync(zg[k], 0, s->nv, q) == cudaSuccess;
+    }
+    for (void *v : {s->dens_rhs, s->dens_x, s->pres_rhs, s->pres_x})
+        ok = ok && cudaMemsetAsync(v, 0, vb, q) == cudaSuccess;
+    ok = ok && cudaMemsetAsync(P.bin_start, 0, (P.nbins + 1) * sizeof(int), q) == cudaSuccess;
+    ok = ok && cudaMemsetAsync(P.bin_count, 0, P.nbins * sizeof(int), q) == cudaSuccess;
+    ok = ok && cudaMemsetAsync(s->sc, 0, sizeof(Scalars), q) == cudaSuccess;
+    ok = ok && cudaStreamSynchronize(q) == cudaSuccess;
+    if (!ok) return cleanup(fail(FS_ERR_CUDA, "fs_create: initialisation failed"));
+    A(alloc_particles(s, 0));
+    *out = s;
+    return FS_OK;
+#undef A
+}
+
+extern "C" fs_status fs_destroy(fs_solver *s)
+{
+    if (!s) return FS_OK;
+    cudaSetDevice(s->ex.device);
+    if (s->st) cudaStreamSynchronize(s->st);
+    if (s->side) cudaStreamSynchronize(s->side);
+    for (void *q : s->allocs) cudaFree(q);
+    if (s->sc_host) cudaFreeHost(s->sc_host);
+    cudaEvent_t evs[] = {s->ev_p2g, s->ev_levelset, s->e0, s->e1, s->p0, s->p1};
+    for (cudaEvent_t e : evs)
+        if (e) cudaEventDestroy(e);
+    if (s->st) cudaStreamDestroy(s->st);
+    if (s->side) cudaStreamDestroy(s->side);
+    delete s;
+    return FS_OK;
+}
+
+static fs_status add_poly(fs_solver *s, int kind, float value, const float *xy, int n)
+{
+    if (!s || !xy || n < 1) return fail(FS_ERR_BAD_ARG, "polygon needs at least one vertex");
+    if (s->initialized) return fail(FS_ERR_STATE, "objects must be added before frame 0");
+    Poly g;
+    g.kind = kind;
+    g.value = value;
+    g.xy.assign(xy, xy + 2 * n);
+    s->polys.push_back(g);
+    if (kind == 0) s->obst_friction.push_back(value);
+    return FS_OK;
+}
+
+extern "C" fs_status fs_add_geometry(fs_solver *s, float friction, const float *xy, int n)
+{
+    return add_poly(s, 0, friction, xy, n);
+}
+extern "C" fs_status fs_add_initial_fluid(fs_solver *s, float viscosity, const float *xy, int n)
+{
+    return add_poly(s, 1, viscosity, xy, n);
+}
+extern "C" fs_status fs_add_sink(fs_solver *s, float divergence, const float *xy, int n)
+{
+    return add_poly(s, 2, divergence, xy, n);
+}
+
+// ---- host restatement of the sampler used for seeding (grid2d.h:187-216) --
+static inline float h_frac(float v) { return v - (float)(long long)v; }
+static inline float h_lerp(float a, float b, float f) { return (a * (1.0f - f)) + (b * f); }
+static inline float h_get(const std::vector<float> &g, int si, int sj, long long i, long long j)
+{
+    i = std::clamp<long long>(i, 0, si - 1);
+    j = std::clamp<long long>(j, 0, sj - 1);
+    return g[(size_t)i * sj + j];
+}
+static float h_grid_lerp(const std::vector<float> &g, int si, int sj, float ox, float oy, float i,
+                         float j)
+{
+    i += ox;
+    j += oy;
+    i = std::clamp(i, 0.f, (float)(si - 1));
+    j = std::clamp(j, 0.f, (float)(sj - 1));
+    long long ci = (long long)std::floor(i), cj = (long long)std::floor(j);
+    float fi = h_frac(i), fj = h_frac(j);
+    long long c2j = fj >= 0.5f ? cj + 1 : cj - 1;
+    long long c3i = fi >= 0.5f ? ci + 1 : ci - 1;
+    float il = fi < 0.5f ? 0.5f - fi : fi - 0.5f;
+    float jl = fj < 0.5f ? 0.5f - fj : fj - 0.5f;
+    float v1 = h_lerp(h_get(g, si, sj, ci, cj), h_get(g, si, sj, c3i, cj), il);
+    float v2 = h_lerp(h_get(g, si, sj, ci, c2j), h_get(g, si, sj, c3i, c2j), il);
+    return h_lerp(v1, v2, jl);
+}
+
+extern "C" fs_status fs_first_frame_init(fs_solver *s)
+{
+    if (!s) return fail(FS_ERR_BAD_ARG, "null handle");
+    if (s->initialized) return fail(FS_ERR_STATE, "frame 0 already initialised");
+    TRY(set_device(s));
+    const GridDims &d = s->d;
+    // polygons -> device
+    std::vector<float> xy;
+    std::vector<int> off(1, 0), kind;
+    std::vector<float> val;
+    for (const Poly &g : s->polys) {
+        xy.insert(xy.end(), g.xy.begin(), g.xy.end());
+        off.push_back(off.back() + (int)(g.xy.size() / 2));
+        kind.push_back(g.kind);
+        val.push_back(g.value);
+    }
+    float *dxy = nullptr, *dval = nullptr;
+    int *doff = nullptr, *dkind = nullptr;
+    TRY(dalloc(s, &dxy, xy.size() + 2));
+    TRY(dalloc(s, &doff, off.size()));
+    TRY(dalloc(s, &dkind, kind.size() + 1));
+    TRY(dalloc(s, &dval, val.size() + 1));
+    if (!xy.empty()) CK(cudaMemcpy(dxy, xy.data(), xy.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(doff, off.data(), off.size() * 4, cudaMemcpyHostToDevice));
+    if (!kind.empty()) {
+        CK(cudaMemcpy(dkind, kind.data(), kind.size() * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(dval, val.data(), val.size() * 4, cudaMemcpyHostToDevice));
+    }
+    // updateSinks, updateSources (none), updateSolids, updateInitialFluid
+    launch_scene_classify(d, s->G, (float)s->p.dx, dxy, doff, dkind, dval, (int)s->polys.size(), s->st);
+    g_kernel_launches += 1;
+    CK(cudaGetLastError());
+    s->friction_dirty = true;
+    TRY(ensure_friction(s));
+    // seedInitialFluid (flipsolver2d.cpp:682-707) on the host
+    std::vector<int8_t> mat(s->ncell);
+    std::vector<float> visc(s->ncell), u(s->nu), v(s->nv);
+    CK(cudaMemcpyAsync(mat.data(), s->G.material, s->ncell, cudaMemcpyDeviceToHost, s->st));
+    CK(cudaMemcpyAsync(visc.data(), s->G.visc, s->ncell * 4, cudaMemcpyDeviceToHost, s->st));
+    CK(cudaMemcpyAsync(u.data(), s->G.u, s->nu * 4, cudaMemcpyDeviceToHost, s->st));
+    CK(cudaMemcpyAsync(v.data(), s->G.v, s->nv * 4, cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    std::mt19937 rng(s->p.seed);
+    std::uniform_real_distribution<float> dist(0.f, 1.f);
+    const int nb = s->P.nbins;
+    std::vector<std::vector<float2>> bpos(nb), bvel(nb);
+    std::vector<std::vector<float>> bvisc(nb);
+    auto bin_of = [&](long long i, long long j) -> long long {
+        long long bi = i / 3, bj = j / 3;
+        if (bi < 0 || bi >= d.bni || bj < 0 || bj >= d.bnj) return -1;
+        return bi * d.bnj + bj;
+    };
+    for (long long i = 0; i < d.ni; i++)
+        for (long long j = 0; j < d.nj; j++) {
+            if (mat[(size_t)i * d.nj + j] != M_FLUID) continue;
+            const long long cellbin = bin_of(i, j);
+            for (int k = 0; k < s->p.particlesPerCell; k++) {
+                float x = (float)i + dist(rng);
+                float y = (float)j + dist(rng);
+                float vx = h_grid_lerp(u, d.ni + 1, d.nj, 0.5f, 0.f, x, y);
+                float vy = h_grid_lerp(v, d.ni, d.nj + 1, 0.f, 0.5f, x, y);
+                float vis = h_grid_lerp(visc, d.ni, d.nj, 0.5f, 0.5f, x, y);
+                const long long pb = bin_of((long long)x, (long long)y);
+                if (pb < 0) continue;
+                const size_t idx = bpos[pb].size();
+                bpos[pb].push_back(make_float2(x, y));
+                bvel[pb].push_back(make_float2(vx, vy));
+                bvisc[pb].push_back(0.f);
+                // the reference writes the viscosity through the cell's bin at
+                // the index returned by the position's bin (:692-702)
+                if (idx < bvisc[cellbin].size()) bvisc[cellbin][idx] = vis;
+            }
+        }
+    std::vector<int> counts(nb);
+    std::vector<float2> pos, vel;
+    std::vector<float> pv;
+    for (int b = 0; b < nb; b++) {
+        counts[b] = (int)bpos[b].size();
+        pos.insert(pos.end(), bpos[b].begin(), bpos[b].end());
+        vel.insert(vel.end(), bvel[b].begin(), bvel[b].end());
+        pv.insert(pv.end(), bvisc[b].begin(), bvisc[b].end());
+    }
+    TRY(upload_particles(s, counts, pos, vel, pv));
+    dfree(s, dxy);
+    dfree(s, doff);
+    dfree(s, dkind);
+    dfree(s, dval);
+    s->initialized = true;
+    return FS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// the substep
+// ---------------------------------------------------------------------------
+template <typename T> static PcgArgs<T> pcg_args(fs_solver *s, const void *b, void *x, int *iters)
+{
+    PcgArgs<T> a{};
+    a.ni = s->d.ni;
+    a.nj = s->d.nj;
+    a.N = (long long)s->ncell;
+    a.info = s->G.cell_info;
+    a.b = (const T *)b;
+    a.x = (T *)x;
+    a.r0 = (T *)s->r0;
+    a.r1 = (T *)s->r1;
+    a.s0 = (T *)s->s0;
+    a.s1 = (T *)s->s1;
+    a.partials = s->partials;
+    a.chunk_end = s->chunk_end;
+    a.chunk_last_unit = s->chunk_last;
+    a.nchunks = s->nchunks;
+    a.sc = s->sc;
+    a.density = s->sp.fluidDensity;
+    a.dx = s->sp.dx;
+    a.iter_limit = s->sp.pcgIterLimit;
+    a.tol = s->sp.projectTolerance;
+    a.iters_out = iters;
+    a.status = &s->sc->pcg_status;
+    a.bar = s->bar;
+    return a;
+}
+
+static fs_status run_pcg(fs_solver *s, const void *b, void *x, int *iters)
+{
+    if (s->timers) CK(cudaEventRecord(s->p0, s->st));
+    cudaError_t e;
+    if (s->prec == FS_PCG_FP64) e = launch_pcg<double>(pcg_args<double>(s, b, x, iters), s->pcg_grid, s->st);
+    else e = launch_pcg<float>(pcg_args<float>(s, b, x, iters), s->pcg_grid, s->st);
+    g_kernel_launches += 1;
+    if (e != cudaSuccess) return fail(FS_ERR_CUDA, "PCG launch: %s", cudaGetErrorString(e));
+    if (s->timers) {
+        CK(cudaEventRecord(s->p1, s->st));
+        CK(cudaEventSynchronize(s->p1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, s->p0, s->p1));
+        s->t_pcg_ms += ms;
+    }
+    return FS_OK;
+}
+
+static fs_status stage(fs_solver *s, int which, bool in_step)
+{
+    const GridDims &d = s->d;
+    const int dbl = s->prec == FS_PCG_FP64;
+    cudaStream_t q = s->st;
+    switch (which) {
+    case FS_STAGE_ADVECT:
+        launch_advect(d, s->P, s->G, s->sc, q);
+        g_kernel_launches += 1;
+        s->after_advect = true;
+        break;
+    case FS_STAGE_DECOMPOSITION:
+        launch_decomposition(d, s->G, q);
+        launch_chunk_last_unit(s->G.cell_info, s->chunk_end, s->nchunks, s->chunk_last, q);
+        g_kernel_launches += 2;
+        break;
+    case FS_STAGE_REBIN: {
+        long long before = g_kernel_launches;
+        launch_rebin(d, s->P, s->rebin_scratch, s->rebin_scratch_size, q);
+        int bits = 0;
+        while ((1 << bits) < s->P.nbins) bits++;
+        g_kernel_launches = before + 15 + 5 * ((bits + 7) / 8);
+        s->after_advect = false;
+        break;
+    }
+    case FS_STAGE_DENSITY:
+        if (s->sp.viscosityEnabled) break;
+        launch_density_grid(d, s->sp, s->P, s->G, s->dens_rhs, dbl, s->sc, q);
+        g_kernel_launches += 1;
+        TRY(run_pcg(s, s->dens_rhs, s->dens_x, &s->sc->density_iters));
+        launch_adjust(d, s->sp, s->P, s->G, s->dens_x, dbl, s->sc, q);
+        g_kernel_launches += 1;
+        break;
+    case FS_STAGE_DENSITY_GRID:
+        launch_density_grid(d, s->sp, s->P, s->G, s->dens_rhs, dbl, s->sc, q);
+        g_kernel_launches += 1;
+        break;
+    case FS_STAGE_P2G:
+        TRY(wait_side(s)); // the previous level-set pass writes the fluid SDF
+        launch_p2g_sdf_materials(d, s->sp, s->P, s->G, q);
+        g_kernel_launches += 1;
+        break;
+    case FS_STAGE_SDF:
+    case FS_STAGE_MATERIALS:
+    case FS_STAGE_AFTER_TRANSFER:
+    case FS_STAGE_RESEED:
+        break;
+    case FS_STAGE_LEVELSET:
+        if (in_step) {
+            CK(cudaEventRecord(s->ev_p2g, q));
+            CK(cudaStreamWaitEvent(s->side, s->ev_p2g, 0));
+            launch_levelset(d, s->G, s->side);
+            CK(cudaEventRecord(s->ev_levelset, s->side));
+            s->levelset_pending = true;
+        } else {
+            launch_levelset(d, s->G, q);
+        }
+        g_kernel_launches += 1 + levelset_max_passes(d);
+        break;
+    case FS_STAGE_VEL_EXTRAP:
+        launch_vel_extrapolate(d, s->G, s->sp, s->sc, false, q);
+        g_kernel_launches += 1;
+        break;
+    case FS_STAGE_SAVE_GRID:
+        launch_save_grid(d, s->G, q);
+        g_kernel_launches += 1;
+        break;
+    case FS_STAGE_BODY_FORCES:
+        launch_body_forces(d, s->sp, s->G, s->sc, q);
+        g_kernel_launches += 1;
+        break;
+    case FS_STAGE_PROJECT:
+        launch_pressure_rhs(d, s->G, s->pres_rhs, dbl, s->sp, q);
+        g_kernel_launches += 1;
+        TRY(run_pcg(s, s->pres_rhs, s->pres_x, &s->sc->pressure_iters));
+        launch_apply_pressure(d, s->sp, s->G, s->pres_x, dbl, s->sc, in_step, q);
+        g_kernel_launches += 1;
+        break;
+    case FS_STAGE_FRICTION:
+        if (!in_step) {
+            launch_friction(d, s->G, q);
+            g_kernel_launches += 1;
+        }
+        break;
+    case FS_STAGE_G2P:
+        launch_g2p(d, s->sp, s->P, s->G, q);
+        g_kernel_launches += 1;
+        break;
+    case FS_STAGE_COUNT:
+        launch_count_erase(d, s->sp, s->P, s->G, q);
+        g_kernel_launches += 1;
+        break;
+    default:
+        return fail(FS_ERR_BAD_ARG, "unknown stage %d", which);
+    }
+    CK(cudaGetLastError());
+    return FS_OK;
+}
+
+static fs_status step_impl(fs_solver *s)
+{
+    if (!s->initialized) return fail(FS_ERR_STATE, "call fs_first_frame_init or fs_step_frame first");
+    TRY(ensure_friction(s));
+    if (s->timers) CK(cudaEventRecord(s->e0, s->st));
+    k_set_dt<<<1, 1, 0, s->st>>>(s->sc, s->step_dt);
+    g_kernel_launches += 1;
+    TRY(stage(s, FS_STAGE_ADVECT, true));
+    TRY(stage(s, FS_STAGE_DECOMPOSITION, true));
+    TRY(stage(s, FS_STAGE_REBIN, true));
+    TRY(stage(s, FS_STAGE_DENSITY, true));
+    TRY(stage(s, FS_STAGE_P2G, true)); // + updateSdf + updateMaterials
+    TRY(stage(s, FS_STAGE_LEVELSET, true));
+    // extrapolate(10), saved copy and body forces in one pass (:437-440)
+    launch_vel_extrapolate(s->d, s->G, s->sp, s->sc, true, s->st);
+    g_kernel_launches += 1;
+    TRY(stage(s, FS_STAGE_PROJECT, true)); // + updateVelocityFromSolids
+    TRY(stage(s, FS_STAGE_VEL_EXTRAP, true));
+    TRY(stage(s, FS_STAGE_G2P, true));
+    TRY(stage(s, FS_STAGE_COUNT, true));
+    if (s->timers) {
+        TRY(wait_side(s));
+        CK(cudaEventRecord(s->e1, s->st));
+        CK(cudaEventSynchronize(s->e1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, s->e0, s->e1));
+        s->t_step_ms += ms;
+    }
+    return FS_OK;
+}
+
+// read back the device scalars (one small copy) and fold the iteration counts
+// into the frame statistics the way SolverStats does (max over the frame)
+static fs_status read_scalars(fs_solver *s)
+{
+    CK(cudaMemcpyAsync(s->sc_host, s->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    if (s->sc_host->pcg_status != 0)
+        return fail(FS_ERR_TIMEOUT, "a PCG grid barrier wait timed out");
+    return FS_OK;
+}
+
+static fs_status max_velocity(fs_solver *s, float *out)
+{
+    launch_max_velocity(s->P, s->sc, s->st);
+    g_kernel_launches += 2;
+    CK(cudaGetLastError());
+    TRY(read_scalars(s));
+    unsigned bits = s->sc_host->maxv2;
+    float v2;
+    memcpy(&v2, &bits, 4);
+    *out = std::sqrt(v2);
+    return FS_OK;
+}
+
+extern "C" fs_status fs_step(fs_solver *s)
+{
+    if (!s) return fail(FS_ERR_BAD_ARG, "null handle");
+    TRY(set_device(s));
+    CK(cudaMemsetAsync(&s->sc->density_iters, 0, 2 * sizeof(int), s->st));
+    s->substeps = 0;
+    TRY(step_impl(s));
+    TRY(read_scalars(s));
+    s->density_iters_max = s->sc_host->density_iters;
+    s->pressure_iters_max = s->sc_host->pressure_iters;
+    return FS_OK;
+}
+
+extern "C" fs_status fs_step_frame(fs_solver *s)
+{
+    if (!s) return fail(FS_ERR_BAD_ARG, "null handle");
+    TRY(set_device(s));
+    if (s->frame == 0 && !s->initialized) TRY(fs_first_frame_init(s));
+    float substepTime = 0.f;
+    bool finished = false;
+    int substepCount = 0;
+    s->density_iters_max = s->pressure_iters_max = s->substeps = 0;
+    while (!finished) {
+        float vel;
+        TRY(max_velocity(s, &vel));
+        if (substepCount > 0) {
+            s->density_iters_max = std::max(s->density_iters_max, s->sc_host->density_iters);
+            s->pressure_iters_max = std::max(s->pressure_iters_max, s->sc_host->pressure_iters);
+        }
+        float maxSubstepSize = s->p.cflNumber / (vel + 1e-15f);
+        if (substepTime + maxSubstepSize >= s->frame_dt || substepCount == (s->p.maxSubsteps - 1)) {
+            maxSubstepSize = s->frame_dt - substepTime;
+            finished = true;
+        } else if (substepTime + 2.f * maxSubstepSize >= s->frame_dt) {
+            maxSubstepSize = 0.5f * (s->frame_dt - substepTime);
+        }
+        s->step_dt = maxSubstepSize;
+        CK(cudaMemsetAsync(&s->sc->density_iters, 0, 2 * sizeof(int), s->st));
+        TRY(step_impl(s));
+        s->substeps++;
+        substepTime += maxSubstepSize;
+        substepCount++;
+        if (substepCount > 50) break;
+    }
+    TRY(read_scalars(s));
+    s->density_iters_max = std::max(s->density_iters_max, s->sc_host->density_iters);
+    s->pressure_iters_max = std::max(s->pressure_iters_max, s->sc_host->pressure_iters);
+    s->frame++;
+    return FS_OK;
+}
+
+extern "C" fs_status fs_set_step_dt(fs_solver *s, float dt)
+{
+    if (!s) return fail(FS_ERR_BAD_ARG, "null handle");
+    s->step_dt = dt;
+    TRY(set_device(s));
+    k_set_dt<<<1, 1, 0, s->st>>>(s->sc, dt);
+    CK(cudaGetLastError());
+    return FS_OK;
+}
+
+extern "C" fs_status fs_get_step_dt(fs_solver *s, float *dt)
+{
+    if (!s || !dt) return fail(FS_ERR_BAD_ARG, "null argument");
+    *dt = s->step_dt;
+    return FS_OK;
+}
+
+extern "C" fs_status fs_run_stage(fs_solver *s, int which)
+{
+    if (!s) return fail(FS_ERR_BAD_ARG, "null handle");
+    if (!s->initialized) return fail(FS_ERR_STATE, "scene not initialised");
+    TRY(set_device(s));
+    TRY(ensure_friction(s));
+    k_set_dt<<<1, 1, 0, s->st>>>(s->sc, s->step_dt);
+    if (which == FS_STAGE_DENSITY) CK(cudaMemsetAsync(&s->sc->density_iters, 0, sizeof(int), s->st));
+    if (which == FS_STAGE_PROJECT) CK(cudaMemsetAsync(&s->sc->pressure_iters, 0, sizeof(int), s->st));
+    TRY(stage(s, which, false));
+    TRY(sync_all(s));
+    TRY(read_scalars(s));
+    if (which == FS_STAGE_DENSITY) s->density_iters_max = s->sc_host->density_iters;
+    if (which == FS_STAGE_PROJECT) s->pressure_iters_max = s->sc_host->pressure_iters;
+    return FS_OK;
+}
+
+extern "C" fs_status fs_max_particle_velocity(fs_solver *s, float *out)
+{
+    if (!s || !out) return fail(FS_ERR_BAD_ARG, "null argument");
+    TRY(set_device(s));
+    return max_velocity(s, out);
+}
+
+// ---------------------------------------------------------------------------
+// state access
+// ---------------------------------------------------------------------------
+extern "C" fs_status fs_bin_count(fs_solver *s, size_t *n)
+{
+    if (!s || !n) return fail(FS_ERR_BAD_ARG, "null argument");
+    *n = (size_t)s->P.nbins;
+    return FS_OK;
+}
+
+static fs_status download_bins(fs_solver *s, std::vector<int> &start, std::vector<int> &count)
+{
+    start.resize(s->P.nbins + 1);
+    count.resize(s->P.nbins);
+    CK(cudaMemcpyAsync(start.data(), s->P.bin_start, start.size() * 4, cudaMemcpyDeviceToHost, s->st));
+    CK(cudaMemcpyAsync(count.data(), s->P.bin_count, count.size() * 4, cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    return FS_OK;
+}
+
+extern "C" fs_status fs_particle_count(fs_solver *s, size_t *n)
+{
+    if (!s || !n) return fail(FS_ERR_BAD_ARG, "null argument");
+    TRY(set_device(s));
+    TRY(sync_all(s));
+    std::vector<int> st, ct;
+    TRY(download_bins(s, st, ct));
+    size_t t = 0;
+    for (int c : ct) t += (size_t)c;
+    *n = t;
+    return FS_OK;
+}
+
+extern "C" fs_status fs_get_particles(fs_solver *s, int32_t *bin_counts, float *pos_xy,
+                                      float *vel_xy, float *visc, uint8_t *dead)
+{
+    if (!s) return fail(FS_ERR_BAD_ARG, "null handle");
+    TRY(set_device(s));
+    TRY(sync_all(s));
+    std::vector<int> st, ct;
+    TRY(download_bins(s, st, ct));
+    const int nslots = st[s->P.nbins];
+    std::vector<float2> p(nslots), v(nslots);
+    std::vector<float> vi(nslots);
+    std::vector<uint8_t> fl(nslots, 0);
+    if (nslots) {
+        CK(cudaMemcpy(p.data(), s->P.pos, nslots * sizeof(float2), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(v.data(), s->P.vel, nslots * sizeof(float2), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(vi.data(), s->P.visc, nslots * sizeof(float), cudaMemcpyDeviceToHost));
+        if (s->after_advect) CK(cudaMemcpy(fl.data(), s->P.flag, nslots, cudaMemcpyDeviceToHost));
+    }
+    size_t k = 0;
+    for (int b = 0; b < s->P.nbins; b++) {
+        if (bin_counts) bin_counts[b] = ct[b];
+        for (int q = st[b]; q < st[b] + ct[b]; q++, k++) {
+            if (pos_xy) {
+                pos_xy[2 * k] = p[q].x;
+                pos_xy[2 * k + 1] = p[q].y;
+            }
+            if (vel_xy) {
+                vel_xy[2 * k] = v[q].x;
+                vel_xy[2 * k + 1] = v[q].y;
+            }
+            if (visc) visc[k] = vi[q];
+            if (dead) dead[k] = (s->after_advect && fl[q] != P_STAY) ? 1 : 0;
+        }
+    }
+    return FS_OK;
+}
+
+extern "C" fs_status fs_set_particles(fs_solver *s, const int32_t *bin_counts, const float *pos_xy,
+                                      const float *vel_xy, const float *visc, const uint8_t *dead)
+{
+    if (!s || !bin_counts || !pos_xy || !vel_xy || !visc)
+        return fail(FS_ERR_BAD_ARG, "null argument");
+    TRY(set_device(s));
+    TRY(sync_all(s));
+    std::vector<int> counts(bin_counts, bin_counts + s->P.nbins);
+    size_t total = 0;
+    for (int c : counts) {
+        if (c < 0) return fail(FS_ERR_BAD_ARG, "negative bin count");
+        total += (size_t)c;
+    }
+    if (total > (size_t)INT32_MAX / 2) return fail(FS_ERR_BAD_ARG, "too many particles");
+    if (dead)
+        for (size_t k = 0; k < total; k++)
+            if (dead[k])
+                return fail(FS_ERR_UNSUPPORTED,
+                            "particles marked for death can only exist inside a substep");
+    std::vector<float2> p(total), v(total);
+    for (size_t k = 0; k < total; k++) {
+        p[k] = make_float2(pos_xy[2 * k], pos_xy[2 * k + 1]);
+        v[k] = make_float2(vel_xy[2 * k], vel_xy[2 * k + 1]);
+    }
+    std::vector<float> vi(visc, visc + total);
+    TRY(upload_particles(s, counts, p, v, vi));
+    s->initialized = true;
+    return FS_OK;
+}
+
+struct GridRef {
+    void *ptr;
+    size_t elems;
+    int elem_size;   // bytes on the device
+    int host_size;   // bytes in the API (double for the solver vectors)
+    bool solver_vec; // device element is the PCG precision
+};
+
+static bool grid_ref(fs_solver *s, int which, GridRef &g)
+{
+    const size_t n = s->ncell;
+    const int e = (int)s->esz;
+    switch (which) {
+    case FS_GRID_MATERIAL: g = {s->G.material, n, 1, 1, false}; return true;
+    case FS_GRID_SOLID_SDF: g = {s->G.solid_sdf, n, 4, 4, false}; return true;
+    case FS_GRID_FLUID_SDF: g = {s->G.fluid_sdf, n, 4, 4, false}; return true;
+    case FS_GRID_U: g = {s->G.u, s->nu, 4, 4, false}; return true;
+    case FS_GRID_V: g = {s->G.v, s->nv, 4, 4, false}; return true;
+    case FS_GRID_U_VALID: g = {s->G.uvalid, s->nu, 1, 1, false}; return true;
+    case FS_GRID_V_VALID: g = {s->G.vvalid, s->nv, 1, 1, false}; return true;
+    case FS_GRID_SAVED_U: g = {s->G.su, s->nu, 4, 4, false}; return true;
+    case FS_GRID_SAVED_V: g = {s->G.sv, s->nv, 4, 4, false}; return true;
+    case FS_GRID_VISCOSITY: g = {s->G.visc, n, 4, 4, false}; return true;
+    case FS_GRID_KNOWN_CENTERED: g = {s->G.known, n, 1, 1, false}; return true;
+    case FS_GRID_DENSITY: g = {s->G.density, n, 4, 4, false}; return true;
+    case FS_GRID_PARTICLE_COUNTS: g = {s->G.counts, n, 4, 4, false}; return true;
+    case FS_GRID_SOLID_ID: g = {s->G.solid_id, n, 4, 4, false}; return true;
+    case FS_GRID_DIV_CONTROL: g = {s->G.divc, n, 4, 4, false}; return true;
+    case FS_GRID_DENSITY_RHS: g = {s->dens_rhs, n, e, 8, true}; return true;
+    case FS_GRID_DENSITY_PRESSURE: g = {s->dens_x, n, e, 8, true}; return true;
+    case FS_GRID_PRESSURE: g = {s->pres_x, n, e, 8, true}; return true;
+    case FS_GRID_PRESSURE_RHS: g = {s->pres_rhs, n, e, 8, true}; return true;
+    case FS_GRID_EMITTER_ID: g = {s->G.emitter_id, n, 4, 4, false}; return true;
+    default: return false;
+    }
+}
+
+extern "C" fs_status fs_grid_bytes(fs_solver *s, int which, size_t *bytes)
+{
+    GridRef g;
+    if (!s || !bytes || !grid_ref(s, which, g)) return fail(FS_ERR_BAD_ARG, "bad grid id");
+    *bytes = g.elems * g.host_size;
+    return FS_OK;
+}
+
+extern "C" fs_status fs_get_grid(fs_solver *s, int which, void *out, size_t bytes)
+{
+    GridRef g;
+    if (!s || !out || !grid_ref(s, which, g)) return fail(FS_ERR_BAD_ARG, "bad grid id");
+    if (bytes != g.elems * g.host_size) return fail(FS_ERR_BAD_ARG, "grid size mismatch");
+    TRY(set_device(s));
+    TRY(sync_all(s));
+    if (g.solver_vec && g.elem_size == 4) {
+        std::vector<float> tmp(g.elems);
+        CK(cudaMemcpy(tmp.data(), g.ptr, g.elems * 4, cudaMemcpyDeviceToHost));
+        double *o = (double *)out;
+        for (size_t k = 0; k < g.elems; k++) o[k] = tmp[k];
+    } else {
+        CK(cudaMemcpy(out, g.ptr, bytes, cudaMemcpyDeviceToHost));
+    }
+    return FS_OK;
+}
+
+extern "C" fs_status fs_set_grid(fs_solver *s, int which, const void *in, size_t bytes)
+{
+    GridRef g;
+    if (!s || !in || !grid_ref(s, which, g)) return fail(FS_ERR_BAD_ARG, "bad grid id");
+    if (bytes != g.elems * g.host_size) return fail(FS_ERR_BAD_ARG, "grid size mismatch");
+    TRY(set_device(s));
+    TRY(sync_all(s));
+    if (g.solver_vec && g.elem_size == 4) {
+        std::vector<float> tmp(g.elems);
+        const double *src = (const double *)in;
+        for (size_t k = 0; k < g.elems; k++) tmp[k] = (float)src[k];
+        CK(cudaMemcpy(g.ptr, tmp.data(), g.elems * 4, cudaMemcpyHostToDevice));
+    } else {
+        CK(cudaMemcpy(g.ptr, in, bytes, cudaMemcpyHostToDevice));
+    }
+    if (which == FS_GRID_MATERIAL || which == FS_GRID_SOLID_ID) s->friction_dirty = true;
+    return FS_OK;
+}
+
+extern "C" fs_status fs_get_stat(fs_solver *s, int which, int *out)
+{
+    if (!s || !out) return fail(FS_ERR_BAD_ARG, "null argument");
+    switch (which) {
+    case FS_STAT_DENSITY_ITERS: *out = s->density_iters_max; return FS_OK;
+    case FS_STAT_PRESSURE_ITERS: *out = s->pressure_iters_max; return FS_OK;
+    case FS_STAT_SUBSTEPS: *out = s->substeps; return FS_OK;
+    case FS_STAT_FRAME: *out = s->frame; return FS_OK;
+    case FS_STAT_POOL_THREADS: *out = s->ex.pool_threads; return FS_OK;
+    default: return fail(FS_ERR_BAD_ARG, "bad stat id");
+    }
+}
+
+extern "C" fs_status fs_enable_timers(fs_solver *s, int enable)
+{
+    if (!s) return fail(FS_ERR_BAD_ARG, "null handle");
+    s->timers = enable != 0;
+    return FS_OK;
+}
+
+extern "C" fs_status fs_reset_timers(fs_solver *s)
+{
+    if (!s) return fail(FS_ERR_BAD_ARG, "null handle");
+    s->t_step_ms = s->t_pcg_ms = 0.0;
+    g_kernel_launches = 0;
+    return FS_OK;
+}
+
+extern "C" fs_status fs_get_timer(fs_solver *s, int which, double *value)
+{
+    if (!s || !value) return fail(FS_ERR_BAD_ARG, "null argument");
+    switch (which) {
+    case 0: *value = s->t_step_ms; return FS_OK;
+    case 1: *value = s->t_pcg_ms; return FS_OK;
+    case 2: *value = (double)g_kernel_launches.load(); return FS_OK;
+    default: return fail(FS_ERR_BAD_ARG, "bad timer id");
+    }
+}
+
+extern "C" fs_status fs_get_stream(fs_solver *s, void **stream)
+{
+    if (!s || !stream) return fail(FS_ERR_BAD_ARG, "null argument");
+    *stream = (void *)s->st;
+    return FS_OK;
+}
+
+extern "C" fs_status fs_synchronize(fs_solver *s)
+{
+    if (!s) return fail(FS_ERR_BAD_ARG, "null handle");
+    TRY(set_device(s));
+    return sync_all(s);
+}
+
+// ---------------------------------------------------------------------------
+// standalone LinearSolver::solve drop-in
+// ---------------------------------------------------------------------------
+namespace {
+struct PcgCache {
+    int device = -1;
+    size_t cap_cells = 0;
+    size_t esz = 0;
+    int grid = 0;
+    int8_t *material = nullptr;
+    uint8_t *info = nullptr;
+    void *b = nullptr, *x = nullptr, *r0 = nullptr, *r1 = nullptr, *s0 = nullptr, *s1 = nullptr;
+    double *partials = nullptr;
+    int *chunk_end = nullptr, *chunk_last = nullptr;
+    int chunk_cap = 0;
+    GridBarrier *bar = nullptr;
+    Scalars *sc = nullptr;
+    Scalars *sc_host = nullptr;
+    void release()
+    {
+        void *ps[] = {material, info, b, x, r0, r1, s0, s1, partials, chunk_end, chunk_last, bar, sc};
+        for (void *p : ps)
+            if (p) cudaFree(p);
+        if (sc_host) cudaFreeHost(sc_host);
+        *this = PcgCache();
+    }
+};
+std::mutex g_pcg_mu;
+PcgCache g_pcg[64];
+} // namespace
+
+static fs_status pcg_cache_get(int dev, size_t cells, size_t esz, int nchunks, PcgCache **out)
+{
+    if (dev < 0 || dev >= 64) return fail(FS_ERR_BAD_ARG, "bad device");
+    PcgCache &c = g_pcg[dev];
+    if (c.device == dev && c.cap_cells >= cells && c.esz == esz && c.chunk_cap >= nchunks) {
+        *out = &c;
+        return FS_OK;
+    }
+    c.release();
+    c.device = dev;
+    c.cap_cells = cells;
+    c.esz = esz;
+    c.chunk_cap = nchunks + 1;
+    c.grid = esz == 8 ? pcg_grid_size<double>((long long)cells) : pcg_grid_size<float>((long long)cells);
+    CK(cudaMalloc(&c.material, cells));
+    CK(cudaMalloc(&c.info, cells));
+    void **vs[] = {&c.b, &c.x, &c.r0, &c.r1, &c.s0, &c.s1};
+    for (void **v : vs) CK(cudaMalloc(v, cells * esz));
+    int maxgrid = std::max(pcg_grid_size<double>(1LL << 40), pcg_grid_size<float>(1LL << 40));
+    CK(cudaMalloc(&c.partials, (size_t)(3 * maxgrid + 8) * sizeof(double)));
+    CK(cudaMalloc(&c.chunk_end, (size_t)c.chunk_cap * sizeof(int)));
+    CK(cudaMalloc(&c.chunk_last, (size_t)c.chunk_cap * sizeof(int)));
+    CK(cudaMalloc(&c.bar, sizeof(GridBarrier)));
+    CK(cudaMalloc(&c.sc, sizeof(Scalars)));
+    CK(cudaMallocHost(&c.sc_host, sizeof(Scalars)));
+    *out = &c;
+    return FS_OK;
+}
+
+static bool valid_material(const int8_t *m, size_t n)
+{
+    for (size_t k = 0; k < n; k++) {
+        const int8_t v = m[k];
+        if (v != M_FLUID && v != M_SOURCE && v != M_SOLID && v != M_SINK && v != M_EMPTY) return false;
+    }
+    return true;
+}
+
+static fs_status pcg_solve_common(int ni, int nj, const int8_t *mat_dev, float dt, double density,
+                                  double dx, const void *rhs_dev, void *res_dev, int iter_limit,
+                                  double tol, const fs_exec_params *exec, int *iterations,
+                                  PcgCache *c, int prec)
+{
+    const size_t N = (size_t)ni * nj;
+    const int T = (exec && exec->pool_threads > 0) ? exec->pool_threads : default_pool_threads();
+    std::vector<int> ends = split_range_ends((long long)N, T);
+    cudaStream_t st = 0;
+    CK(cudaMemcpyAsync(c->chunk_end, ends.data(), ends.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    GridDims d{ni, nj, ni / 3 + (ni % 3 != 0), nj / 3 + (nj % 3 != 0)};
+    Grids G;
+    G.material = const_cast<int8_t *>(mat_dev);
+    G.cell_info = c->info;
+    launch_decomposition(d, G, st);
+    launch_chunk_last_unit(c->info, c->chunk_end, (int)ends.size(), c->chunk_last, st);
+    k_set_dt<<<1, 1, 0, st>>>(c->sc, dt);
+    CK(cudaMemsetAsync(&c->sc->pcg_status, 0, sizeof(int), st));
+    g_kernel_launches += 3;
+    cudaError_t e;
+    if (prec == FS_PCG_FP64) {
+        PcgArgs<double> a{};
+        a.ni = ni; a.nj = nj; a.N = (long long)N; a.info = c->info;
+        a.b = (const double *)rhs_dev; a.x = (double *)res_dev;
+        a.r0 = (double *)c->r0; a.r1 = (double *)c->r1; a.s0 = (double *)c->s0; a.s1 = (double *)c->s1;
+        a.partials = c->partials; a.chunk_end = c->chunk_end; a.chunk_last_unit = c->chunk_last;
+        a.nchunks = (int)ends.size(); a.sc = c->sc; a.density = density; a.dx = dx;
+        a.iter_limit = iter_limit; a.tol = tol; a.iters_out = &c->sc->density_iters;
+        a.status = &c->sc->pcg_status; a.bar = c->bar;
+        e = launch_pcg<double>(a, pcg_grid_size<double>((long long)N), st);
+    } else {
+        PcgArgs<float> a{};
+        a.ni = ni; a.nj = nj; a.N = (long long)N; a.info = c->info;
+        a.b = (const float *)rhs_dev; a.x = (float *)res_dev;
+        a.r0 = (float *)c->r0; a.r1 = (float *)c->r1; a.s0 = (float *)c->s0; a.s1 = (float *)c->s1;
+        a.partials = c->partials; a.chunk_end = c->chunk_end; a.chunk_last_unit = c->chunk_last;
+        a.nchunks = (int)ends.size(); a.sc = c->sc; a.density = density; a.dx = dx;
+        a.iter_limit = iter_limit; a.tol = tol; a.iters_out = &c->sc->density_iters;
+        a.status = &c->sc->pcg_status; a.bar = c->bar;
+        e = launch_pcg<float>(a, pcg_grid_size<float>((long long)N), st);
+    }
+    g_kernel_launches += 1;
+    if (e != cudaSuccess) return fail(FS_ERR_CUDA, "PCG launch: %s", cudaGetErrorString(e));
+    CK(cudaMemcpyAsync(c->sc_host, c->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (c->sc_host->pcg_status != 0) return fail(FS_ERR_TIMEOUT, "a PCG grid barrier wait timed out");
+    if (iterations) *iterations = c->sc_host->density_iters;
+    return FS_OK;
+}
+
+extern "C" fs_status fs_pcg_solve(int ni, int nj, const int8_t *material, float dt, double density,
+                                  double dx, const double *rhs, double *result, int iter_limit,
+                                  double tol, const fs_exec_params *exec, int *iterations)
+{
+    if (ni < 1 || nj < 1 || !material || !rhs || !result || iter_limit < 0)
+        return fail(FS_ERR_BAD_ARG, "fs_pcg_solve: invalid argument");
+    const size_t N = (size_t)ni * nj;
+    if (!valid_material(material, N)) return fail(FS_ERR_BAD_ARG, "fs_pcg_solve: unknown material code");
+    const int dev = exec ? exec->device : 0;
+    const int prec = (exec && exec->pcg_precision == FS_PCG_FP64) ? FS_PCG_FP64 : FS_PCG_FP32;
+    const size_t esz = prec == FS_PCG_FP64 ? 8 : 4;
+    std::lock_guard<std::mutex> lk(g_pcg_mu);
+    CK(cudaSetDevice(dev));
+    const int T = (exec && exec->pool_threads > 0) ? exec->pool_threads : default_pool_threads();
+    PcgCache *c = nullptr;
+    TRY(pcg_cache_get(dev, N, esz, std::min<long long>(T, (long long)N), &c));
+    CK(cudaMemcpy(c->material, material, N, cudaMemcpyHostToDevice));
+    if (prec == FS_PCG_FP64) {
+        CK(cudaMemcpy(c->b, rhs, N * 8, cudaMemcpyHostToDevice));
+    } else {
+        std::vector<float> tmp(N);
+        for (size_t k = 0; k < N; k++) tmp[k] = (float)rhs[k];
+        CK(cudaMemcpy(c->b, tmp.data(), N * 4, cudaMemcpyHostToDevice));
+    }
+    TRY(pcg_solve_common(ni, nj, c->material, dt, density, dx, c->b, c->x, iter_limit, tol, exec,
+                         iterations, c, prec));
+    if (prec == FS_PCG_FP64) {
+        CK(cudaMemcpy(result, c->x, N * 8, cudaMemcpyDeviceToHost));
+    } else {
+        std::vector<float> tmp(N);
+        CK(cudaMemcpy(tmp.data(), c->x, N * 4, cudaMemcpyDeviceToHost));
+        for (size_t k = 0; k < N; k++) result[k] = tmp[k];
+    }
+    return FS_OK;
+}
+
+extern "C" fs_status fs_pcg_solve_device(int ni, int nj, const int8_t *material_device, float dt,
+                                         double density, double dx, const void *rhs_device,
+                                         void *result_device, int iter_limit, double tol,
+                                         const fs_exec_params *exec, int *iterations)
+{
+    if (ni < 1 || nj < 1 || !material_device || !rhs_device || !result_device || iter_limit < 0)
+        return fail(FS_ERR_BAD_ARG, "fs_pcg_solve_device: invalid argument");
+    const size_t N = (size_t)ni * nj;
+    const int dev = exec ? exec->device : 0;
+    const int prec = (exec && exec->pcg_precision == FS_PCG_FP64) ? FS_PCG_FP64 : FS_PCG_FP32;
+    const size_t esz = prec == FS_PCG_FP64 ? 8 : 4;
+    std::lock_guard<std::mutex> lk(g_pcg_mu);
+    CK(cudaSetDevice(dev));
+    const int T = (exec && exec->pool_threads > 0) ? exec->pool_threads : default_pool_threads();
+    PcgCache *c = nullptr;
+    TRY(pcg_cache_get(dev, N, esz, std::min<long long>(T, (long long)N), &c));
+    return pcg_solve_common(ni, nj, material_device, dt, density, dx, rhs_device, result_device,
+                            iter_limit, tol, exec, iterations, c, prec);
+}

@@ -1,0 +1,756 @@
+// fs_grid.cu -- per-cell and per-face kernels of the FLIP substep.
+//
+//   scene classification   updateSinks / updateSolids / updateInitialFluid
+//   friction factors       updateVelocityFromSolids precomputation
+//   decomposition          getPressureProjectionMatrix + getIPPCoefficients,
+//                          matrix-free: one packed byte per cell
+//   density grid + RHS     updateDensityGrid + calcDensityCorrectionRhs
+//   P2G + SDF + materials  particleVelocityToGrid, centeredParamsToGrid,
+//                          updateSdf, updateMaterials fused into one gather
+//   level set / velocity   extrapolateLevelsetInside, breadthFirstExtrapolate:
+//   extrapolation          layer-synchronous, temporally blocked in shared memory
+//   pressure RHS / apply   calcPressureRhs, applyPressureThreadU/V fused with
+//                          the solid friction
+//
+// Compiled with -fmad=false so each float expression rounds exactly as the
+// reference's (-ffp-contract=off) build does.
+#include <cfloat>
+#include <climits>
+
+#include "fs_state.h"
+
+namespace fsg {
+
+constexpr int kThreads = 256;
+static inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
+
+// ---------------------------------------------------------------------------
+// scene classification (flipsolver2d.cpp:502-590), frame 0 only
+// ---------------------------------------------------------------------------
+// Geometry2d::signedDistance (geometry2d.cpp:54-73)
+__device__ float polygon_sdf(const float *__restrict__ xy, int n, float px, float py)
+{
+    float dx0 = px - xy[0], dy0 = py - xy[1];
+    float sq = dx0 * dx0 + dy0 * dy0 + 0.f * 0.f;
+    float sgn = 1.0f;
+    for (int i = 0, j = n - 1; i < n; j = i, i++) {
+        float ex = xy[2 * j] - xy[2 * i], ey = xy[2 * j + 1] - xy[2 * i + 1];
+        float wx = px - xy[2 * i], wy = py - xy[2 * i + 1];
+        float wde = wx * ex + wy * ey + 0.f * 0.f;
+        float ede = ex * ex + ey * ey + 0.f * 0.f;
+        float h = clampf(wde / ede, 0.0f, 1.0f);
+        float bx = wx - ex * h, by = wy - ey * h;
+        float bb = bx * bx + by * by + 0.f * 0.f;
+        sq = (bb < sq) ? bb : sq;
+        bool xf = py >= xy[2 * i + 1];
+        bool yf = py < xy[2 * j + 1];
+        bool zf = ex * wy > ey * wx;
+        if ((xf && yf && zf) || (!xf && !yf && !zf)) sgn = -sgn;
+    }
+    return (float)((double)sgn * sqrt((double)sq));
+}
+
+// kind: 0 solid (value = friction), 1 initial fluid (value = viscosity),
+// 2 sink (value = divergence)
+__global__ void k_scene_classify(GridDims d, Grids G, float dx, const float *__restrict__ xy,
+                                 const int *__restrict__ off, const int *__restrict__ kind,
+                                 const float *__restrict__ val, int npoly)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.ni * d.nj) return;
+    const int i = c / d.nj, j = c - i * d.nj;
+    int8_t m = G.material[c];
+    // updateSinks (:554-571)
+    for (int k = 0; k < npoly; k++) {
+        if (kind[k] != 2) continue;
+        if (polygon_sdf(xy + 2 * off[k], off[k + 1] - off[k], ((float)i + 0.5f) * dx,
+                        ((float)j + 0.5f) * dx) <= 0.f) {
+            m = M_SINK;
+            G.divc[c] = val[k];
+        }
+    }
+    // updateSolids (:502-530); (float(i)+0.5)*dx is evaluated in double
+    float dist = FLT_MAX;
+    int minIdx = 0, solidIdx = 0;
+    const float x = (float)(((double)(float)i + 0.5) * (double)dx);
+    const float y = (float)(((double)(float)j + 0.5) * (double)dx);
+    for (int k = 0; k < npoly; k++) {
+        if (kind[k] != 0) continue;
+        float sdf = polygon_sdf(xy + 2 * off[k], off[k + 1] - off[k], x, y) / dx;
+        if (sdf < dist) {
+            minIdx = solidIdx;
+            dist = sdf;
+        }
+        solidIdx++;
+    }
+    G.solid_sdf[c] = dist;
+    if (dist < 0) {
+        m = M_SOLID;
+        G.solid_id[c] = minIdx;
+    }
+    // updateInitialFluid (:573-590)
+    for (int k = 0; k < npoly; k++) {
+        if (kind[k] != 1) continue;
+        if (polygon_sdf(xy + 2 * off[k], off[k + 1] - off[k], ((float)i + 0.5f) * dx,
+                        ((float)j + 0.5f) * dx) <= 0.f) {
+            m = M_FLUID;
+            G.visc[c] = val[k];
+        }
+    }
+    G.material[c] = m;
+}
+
+void launch_scene_classify(const GridDims &d, const Grids &G, float dx, const float *poly_xy,
+                           const int *poly_off, const int *poly_kind, const float *poly_val,
+                           int npoly, cudaStream_t st)
+{
+    k_scene_classify<<<nblk((long long)d.ni * d.nj, kThreads), kThreads, 0, st>>>(
+        d, G, dx, poly_xy, poly_off, poly_kind, poly_val, npoly);
+}
+
+// updateVelocityFromSolids (flipsolver2d.cpp:1077-1104) depends only on solid
+// cells and solid ids, which never change after frame 0: precompute per face
+// the factor (1 - mean friction) or NaN where the face is not affected.
+__global__ void k_friction_factors(GridDims d, Grids G, const float *__restrict__ fric)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.ni * d.nj) return;
+    const int i = c / d.nj, j = c - i * d.nj;
+    float sum = 0;
+    int cnt = 0;
+    for (int io = -1; io < 2; io++)
+        for (int jo = -1; jo < 2; jo++) {
+            int a = i + io, b = j + jo;
+            if (a < 0 || a >= d.ni || b < 0 || b >= d.nj) continue;
+            int id = G.solid_id[(size_t)a * d.nj + b];
+            if (id != -1) {
+                sum += fric[id];
+                cnt++;
+            }
+        }
+    float fu = __int_as_float(0x7fc00000), fv = fu;
+    if (cnt > 0) {
+        float avg = sum / (float)cnt;
+        const int8_t *m = G.material;
+        bool uA = t_solid(mat_at(m, d, i, j + 1)) || t_solid(mat_at(m, d, i - 1, j + 1)) ||
+                  t_solid(mat_at(m, d, i, j)) || t_solid(mat_at(m, d, i - 1, j)) ||
+                  t_solid(mat_at(m, d, i, j - 1)) || t_solid(mat_at(m, d, i - 1, j - 1));
+        bool vA = t_solid(mat_at(m, d, i + 1, j)) || t_solid(mat_at(m, d, i + 1, j - 1)) ||
+                  t_solid(mat_at(m, d, i, j)) || t_solid(mat_at(m, d, i, j - 1)) ||
+                  t_solid(mat_at(m, d, i - 1, j)) || t_solid(mat_at(m, d, i - 1, j - 1));
+        if (uA) fu = 1 - avg;
+        if (vA) fv = 1 - avg;
+    }
+    G.ufric[c] = fu;
+    G.vfric[c] = fv;
+}
+
+void launch_friction_factors(const GridDims &d, const Grids &G, const float *obst_friction,
+                             cudaStream_t st)
+{
+    k_friction_factors<<<nblk((long long)d.ni * d.nj, kThreads), kThreads, 0, st>>>(
+        d, G, obst_friction);
+}
+
+__global__ void k_fill_u8(uint8_t *p, uint8_t v, size_t n)
+{
+    size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) p[k] = v;
+}
+void launch_fill_u8(uint8_t *p, uint8_t v, size_t n, cudaStream_t st)
+{
+    if (n) k_fill_u8<<<nblk((long long)n, kThreads), kThreads, 0, st>>>(p, v, n);
+}
+
+// ---------------------------------------------------------------------------
+// decomposition: one byte per cell, frozen for both solves of the substep.
+//   bit 7      the cell is a unit (fluid at this stage)
+//   bits 4..6  nonsolidNeighborCount of the cell (materialgrid.cpp:137-140);
+//              for a unit this equals its fluid-or-empty neighbour count
+//              (getPressureProjectionMatrix, flipsolver2d.cpp:832-869)
+//   bits 0..3  NeighborMask (pressuredata.h:87-95): fluid neighbour whose
+//              linear index lies inside the grid
+// IPP off-diagonals are 1/(nsc(neighbour) * scale) (flipsolver2d.cpp:924-927).
+// ---------------------------------------------------------------------------
+__global__ void k_decomposition(GridDims d, const int8_t *__restrict__ m, uint8_t *__restrict__ info)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const long long N = (long long)d.ni * d.nj;
+    if (c >= N) return;
+    const int i = c / d.nj, j = c - i * d.nj;
+    const int8_t mim = mat_at(m, d, i - 1, j), mip = mat_at(m, d, i + 1, j);
+    const int8_t mjm = mat_at(m, d, i, j - 1), mjp = mat_at(m, d, i, j + 1);
+    const int nsc = !t_solid(mim) + !t_solid(mip) + !t_solid(mjm) + !t_solid(mjp);
+    uint8_t b = (uint8_t)(nsc << 4);
+    if (t_fluid(m[c])) {
+        b |= 0x80;
+        if (t_fluid(mim) && c - d.nj >= 0) b |= 1;
+        if (t_fluid(mip) && c + d.nj < N) b |= 2;
+        if (t_fluid(mjm) && c - 1 >= 0) b |= 4;
+        if (t_fluid(mjp) && c + 1 < N) b |= 8;
+    }
+    info[c] = b;
+}
+
+void launch_decomposition(const GridDims &d, const Grids &G, cudaStream_t st)
+{
+    k_decomposition<<<nblk((long long)d.ni * d.nj, kThreads), kThreads, 0, st>>>(d, G.material,
+                                                                                G.cell_info);
+}
+
+// ---------------------------------------------------------------------------
+// density grid + RHS: updateDensityGridThread (flipsolver2d.cpp:201-249) and
+// calcDensityCorrectionRhs (:993-1011)
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_density_grid(GridDims d, Particles P, const int8_t *__restrict__ m,
+                               float *__restrict__ dens, T *__restrict__ rhs, double density,
+                               double dx, int ppc, const Scalars *__restrict__ sc)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.ni * d.nj) return;
+    const int ci = c / d.nj, cj = c - ci * d.nj;
+    const float cellVolume = (float)(dx * dx * dx);
+    const float particleMass = (float)((density * cellVolume) / ((float)ppc));
+    const int cbi = ci / 3, cbj = cj / 3;
+    float acc = 0.f;
+    for (int io = -1; io <= 1; io++) {
+        const int bi = cbi + io;
+        if (bi < 0 || bi >= d.bni) continue;
+        for (int jo = -1; jo <= 1; jo++) {
+            const int bj = cbj + jo;
+            if (bj < 0 || bj >= d.bnj) continue;
+            const int b = bi * d.bnj + bj;
+            const int st = P.bin_start[b], n = P.bin_count[b];
+            for (int k = 0; k < n; k++) {
+                const float2 p = P.pos[st + k];
+                const float w = sm_bilinear_hat(p.x - (float)ci - 0.5f, p.y - (float)cj - 0.5f);
+                if (fabsf(w) > 1e-6f) acc += w * particleMass;
+            }
+        }
+    }
+    acc /= cellVolume;
+    const int8_t mc = m[c];
+    if (t_fluid(mc) && (t_empty(mat_at(m, d, ci + 1, cj)) || t_empty(mat_at(m, d, ci - 1, cj)) ||
+                        t_empty(mat_at(m, d, ci, cj + 1)) || t_empty(mat_at(m, d, ci, cj - 1))))
+        acc = clampf(acc, (float)density, FLT_MAX);
+    dens[c] = acc;
+    const double scale = 1.0 / (double)sc->dt;
+    rhs[c] = t_fluid(mc) ? (T)(scale * (1.0 - clampd((double)acc / density, 0.5, 1.5))) : (T)0;
+}
+
+void launch_density_grid(const GridDims &d, const SceneParams &sp, const Particles &P,
+                         const Grids &G, void *rhs, int is_double, const Scalars *sc,
+                         cudaStream_t st)
+{
+    const int nb = nblk((long long)d.ni * d.nj, kThreads);
+    if (is_double)
+        k_density_grid<double><<<nb, kThreads, 0, st>>>(d, P, G.material, G.density,
+                                                        (double *)rhs, sp.fluidDensity, sp.dx,
+                                                        sp.particlesPerCell, sc);
+    else
+        k_density_grid<float><<<nb, kThreads, 0, st>>>(d, P, G.material, G.density, (float *)rhs,
+                                                       sp.fluidDensity, sp.dx,
+                                                       sp.particlesPerCell, sc);
+}
+
+// ---------------------------------------------------------------------------
+// P2G + centred parameters + fluid SDF + materials, one gather per cell:
+//   particleVelocityToGridThread (flipsolver2d.cpp:1329-1377)
+//   centeredParamsToGridThread   (:1394-1431)
+//   updateSdfThread              (:1276-1311)
+//   updateMaterials              (:1053-1075)
+// The U row i = NI and the V column j = NJ are never written by the
+// reference's loop over NI*NJ cells and stay at their fill values 0 / false.
+// ---------------------------------------------------------------------------
+__global__ void k_p2g_sdf_materials(GridDims d, Particles P, Grids G, float particleScale,
+                                    int handling)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.ni * d.nj) return;
+    const int ci = c / d.nj, cj = c - ci * d.nj;
+    const int cbi = ci / 3, cbj = cj / 3;
+    const float threshold = 1e-9f;
+    float uW = 1e-10f, vW = 1e-10f, uVel = 0.0f, vVel = 0.0f;
+    bool uValid = false, vValid = false;
+    float wT = (float)1e-10, vis = 0.0f;
+    bool visValid = false;
+    float d2 = FLT_MAX;
+    const float fi = (float)ci, fj = (float)cj;
+    const float cx = fi + 0.5f, cy = fj + 0.5f;
+    for (int io = -1; io <= 1; io++) {
+        const int bi = cbi + io;
+        if (bi < 0 || bi >= d.bni) continue;
+        for (int jo = -1; jo <= 1; jo++) {
+            const int bj = cbj + jo;
+            if (bj < 0 || bj >= d.bnj) continue;
+            const int b = bi * d.bnj + bj;
+            const int st = P.bin_start[b], n = P.bin_count[b];
+            for (int k = 0; k < n; k++) {
+                const float2 p = P.pos[st + k];
+                // SDF: min squared distance to the cell centre
+                const float ddx = p.x - cx, ddy = p.y - cy;
+                const float nd = ddx * ddx + ddy * ddy;
+                if (nd < d2) d2 = nd;
+                // velocity: weights at (i, j+0.5) for U and (i+0.5, j) for V
+                const float wU = sm_qbspline(p.x - fi, p.y - (fj + 0.5f));
+                const float wV = sm_qbspline(p.x - (fi + 0.5f), p.y - fj);
+                if (wU > threshold && wV > threshold) {
+                    const float2 v = P.vel[st + k];
+                    uW += wU;
+                    uVel += wU * v.x;
+                    uValid = true;
+                    vW += wV;
+                    vVel += wV * v.y;
+                    vValid = true;
+                }
+                if (handling != 2) {
+                    const float wc = sm_qbspline(p.x - fi, p.y - fj);
+                    if (wc > threshold) {
+                        wT += wc;
+                        vis += wc * P.visc[st + k];
+                        visValid = true;
+                    }
+                }
+            }
+        }
+    }
+    const int NV = d.nj + 1;
+    G.u[(size_t)ci * d.nj + cj] = uVel / uW;
+    G.uvalid[(size_t)ci * d.nj + cj] = uValid;
+    G.v[(size_t)ci * NV + cj] = vVel / vW;
+    G.vvalid[(size_t)ci * NV + cj] = vValid;
+    if (ci == d.ni - 1) { // U row NI stays at the fill value
+        G.u[(size_t)d.ni * d.nj + cj] = 0.f;
+        G.uvalid[(size_t)d.ni * d.nj + cj] = 0;
+    }
+    if (cj == d.nj - 1) { // V column NJ stays at the fill value
+        G.v[(size_t)ci * NV + d.nj] = 0.f;
+        G.vvalid[(size_t)ci * NV + d.nj] = 0;
+    }
+    if (handling != 2) {
+        G.visc[c] = vis / wT;
+        G.known[c] = visValid;
+        G.divc[c] = 0.f;
+    }
+    const float sdf = sqrtf(d2) - particleScale;
+    G.fluid_sdf[c] = sdf;
+    const int8_t mc = G.material[c];
+    if (sdf < 0.f) {
+        if (t_empty(mc)) G.material[c] = M_FLUID;
+    } else {
+        if (t_strict_fluid(mc)) G.material[c] = M_EMPTY;
+    }
+}
+
+void launch_p2g_sdf_materials(const GridDims &d, const SceneParams &sp, const Particles &P,
+                              const Grids &G, cudaStream_t st)
+{
+    k_p2g_sdf_materials<<<nblk((long long)d.ni * d.nj, kThreads), kThreads, 0, st>>>(
+        d, P, G, sp.particleScale, sp.parameterHandlingMethod);
+}
+
+// ---------------------------------------------------------------------------
+// Breadth-first extrapolation, layer-synchronous.
+// In the reference's FIFO BFS (mathfuncs.cpp:152-215, flipsolver2d.cpp:
+// 1433-1494) a cell's marker is its 8-neighbour graph distance to the seed
+// cells, every cell of layer k is finished before any cell of layer k+1, and
+// a layer-k cell reads only neighbours of layers < k.  Processing whole layers
+// at once therefore gives the same values.  A tile of TILE x TILE cells is
+// loaded with a halo of H cells; H layers are advanced in shared memory, after
+// which every interior cell is exact (each layer consumes one halo ring).
+// ---------------------------------------------------------------------------
+constexpr int kTile = 32;
+constexpr int kMarkInf = INT_MAX;
+constexpr int kMarkOut = INT_MIN; // outside the grid: not a neighbour
+
+template <int H>
+struct BfsTile {
+    static constexpr int W = kTile + 2 * H;
+    int mark[W * W];
+    float val[W * W];
+};
+
+// average over the 8-neighbourhood in the reference's order, neighbours with
+// a smaller marker only, summed in double
+template <int W>
+__device__ __forceinline__ double bfs_avg(const int *mark, const float *val, int r, int q, int k,
+                                          int &count)
+{
+    double avg = 0;
+    count = 0;
+#pragma unroll
+    for (int io = -1; io <= 1; io++)
+#pragma unroll
+        for (int jo = -1; jo <= 1; jo++) {
+            if (io == 0 && jo == 0) continue;
+            const int rr = r + io, qq = q + jo;
+            if (rr < 0 || rr >= W || qq < 0 || qq >= W) continue;
+            const int mk = mark[rr * W + qq];
+            if (mk == kMarkOut) continue;
+            if (mk < k) {
+                avg += (double)val[rr * W + qq];
+                count++;
+            }
+        }
+    return avg;
+}
+
+template <int W>
+__device__ __forceinline__ bool bfs_touches(const int *mark, int r, int q, int k)
+{
+#pragma unroll
+    for (int io = -1; io <= 1; io++)
+#pragma unroll
+        for (int jo = -1; jo <= 1; jo++) {
+            if (io == 0 && jo == 0) continue;
+            const int rr = r + io, qq = q + jo;
+            if (rr < 0 || rr >= W || qq < 0 || qq >= W) continue;
+            if (mark[rr * W + qq] == k) return true;
+        }
+    return false;
+}
+
+// Velocity extrapolation, breadthFirstExtrapolate(grid, flags, 10, ...):
+// layers 1..11 (a layer-k cell discovers layer k+1 while k <= 10).
+// With `save_gravity` the output also performs the two steps that follow the
+// first extrapolation in FlipSolver::step (:439-440): the saved copy receives
+// the extrapolated grid and the live grid gets + dt/dx * g.
+constexpr int kVelH = 11;
+
+__global__ void __launch_bounds__(1024) k_vel_extrap(GridDims d, Grids G, float gI, float gJ,
+                                                    double dx, const Scalars *__restrict__ sc,
+                                                    int save_gravity)
+{
+    __shared__ BfsTile<kVelH> t;
+    constexpr int W = BfsTile<kVelH>::W;
+    const bool isV = blockIdx.z == 1;
+    const int si = isV ? d.ni : d.ni + 1, sj = isV ? d.nj + 1 : d.nj;
+    const float *__restrict__ g = isV ? G.v : G.u;
+    const uint8_t *__restrict__ fl = isV ? G.vvalid : G.uvalid;
+    float *__restrict__ go = isV ? G.v2 : G.u2;
+    uint8_t *__restrict__ flo = isV ? G.vvalid2 : G.uvalid2;
+    const int ti0 = blockIdx.y * kTile, tj0 = blockIdx.x * kTile;
+    if (ti0 >= si || tj0 >= sj) return;
+    for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
+        const int r = e / W, q = e - r * W;
+        const int gi = ti0 - kVelH + r, gj = tj0 - kVelH + q;
+        if (gi < 0 || gi >= si || gj < 0 || gj >= sj) {
+            t.mark[e] = kMarkOut;
+            t.val[e] = 0.f;
+        } else {
+            const size_t idx = (size_t)gi * sj + gj;
+            t.mark[e] = fl[idx] ? 0 : kMarkInf;
+            t.val[e] = g[idx];
+        }
+    }
+    __syncthreads();
+    for (int k = 1; k <= kVelH; k++) {
+        for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
+            const int r = e / W, q = e - r * W;
+            if (t.mark[e] == kMarkInf && bfs_touches<W>(t.mark, r, q, k - 1)) t.mark[e] = k;
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
+            if (t.mark[e] != k) continue;
+            const int r = e / W, q = e - r * W;
+            int count;
+            const double avg = bfs_avg<W>(t.mark, t.val, r, q, k, count);
+            t.val[e] = (float)(avg / count);
+        }
+        __syncthreads();
+    }
+    const float factor = (float)((double)sc->dt / dx);
+    const float add = factor * (isV ? gJ : gI);
+    for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
+        const int r = e / kTile + kVelH, q = e % kTile + kVelH;
+        const int gi = ti0 - kVelH + r, gj = tj0 - kVelH + q;
+        if (gi >= si || gj >= sj) continue;
+        const size_t idx = (size_t)gi * sj + gj;
+        const int mk = t.mark[r * W + q];
+        const float vv = t.val[r * W + q];
+        const uint8_t valid = (mk != kMarkInf) ? 1 : 0;
+        if (save_gravity) {
+            (isV ? G.sv : G.su)[idx] = vv;
+            (isV ? G.svvalid : G.suvalid)[idx] = valid;
+            go[idx] = vv + add;
+        } else {
+            go[idx] = vv;
+        }
+        flo[idx] = valid;
+    }
+}
+
+void launch_vel_extrapolate(const GridDims &d, Grids &G, const SceneParams &sp,
+                            const Scalars *sc, bool save_and_gravity, cudaStream_t st)
+{
+    dim3 grid(nblk(d.nj + 1, kTile), nblk(d.ni + 1, kTile), 2);
+    k_vel_extrap<<<grid, 1024, 0, st>>>(d, G, sp.gI, sp.gJ, sp.dx, sc, save_and_gravity ? 1 : 0);
+    float *t = G.u; G.u = G.u2; G.u2 = t;
+    t = G.v; G.v = G.v2; G.v2 = t;
+    uint8_t *b = G.uvalid; G.uvalid = G.uvalid2; G.uvalid2 = b;
+    b = G.vvalid; G.vvalid = G.vvalid2; G.vvalid2 = b;
+}
+
+// Level set inside extrapolation (flipsolver2d.cpp:1433-1494): seeds are
+// cells with sdf > 0, depth unbounded, value = average - 1.  Pass p advances
+// layers p*H+1 .. (p+1)*H; markers and values ping-pong between two buffers,
+// and newly assigned values also go straight to the fluid SDF (which no pass
+// reads).  A pass that finds the previous pass assigned nothing returns.
+constexpr int kLsH = 16;
+
+__global__ void __launch_bounds__(1024) k_levelset_pass(GridDims d, float *__restrict__ sdf,
+                                                       const int *__restrict__ mark_in,
+                                                       const float *__restrict__ val_in,
+                                                       int *__restrict__ mark_out,
+                                                       float *__restrict__ val_out,
+                                                       int *__restrict__ active, int pass)
+{
+    __shared__ BfsTile<kLsH> t;
+    __shared__ int any_new;
+    constexpr int W = BfsTile<kLsH>::W;
+    if (pass > 0 && active[pass - 1] == 0) return;
+    const int si = d.ni, sj = d.nj;
+    const int ti0 = blockIdx.y * kTile, tj0 = blockIdx.x * kTile;
+    if (threadIdx.x == 0) any_new = 0;
+    for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
+        const int r = e / W, q = e - r * W;
+        const int gi = ti0 - kLsH + r, gj = tj0 - kLsH + q;
+        if (gi < 0 || gi >= si || gj < 0 || gj >= sj) {
+            t.mark[e] = kMarkOut;
+            t.val[e] = 0.f;
+        } else {
+            const size_t idx = (size_t)gi * sj + gj;
+            if (pass == 0) {
+                const float v = sdf[idx];
+                t.mark[e] = v > 0.f ? 0 : kMarkInf;
+                t.val[e] = v;
+            } else {
+                t.mark[e] = mark_in[idx];
+                t.val[e] = val_in[idx];
+            }
+        }
+    }
+    __syncthreads();
+    const int k0 = pass * kLsH;
+    bool assigned = false;
+    for (int k = k0 + 1; k <= k0 + kLsH; k++) {
+        for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
+            const int r = e / W, q = e - r * W;
+            if (t.mark[e] == kMarkInf && bfs_touches<W>(t.mark, r, q, k - 1)) t.mark[e] = k;
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
+            if (t.mark[e] != k) continue;
+            const int r = e / W, q = e - r * W;
+            int count;
+            const double avg = bfs_avg<W>(t.mark, t.val, r, q, k, count);
+            t.val[e] = (float)(avg / count - 1.f);
+        }
+        __syncthreads();
+    }
+    for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
+        const int r = e / kTile + kLsH, q = e % kTile + kLsH;
+        const int gi = ti0 - kLsH + r, gj = tj0 - kLsH + q;
+        if (gi >= si || gj >= sj) continue;
+        const size_t idx = (size_t)gi * sj + gj;
+        const int mk = t.mark[r * W + q];
+        mark_out[idx] = mk;
+        val_out[idx] = t.val[r * W + q];
+        if (mk > k0 && mk != kMarkInf) {
+            sdf[idx] = t.val[r * W + q];
+            assigned = true;
+        }
+    }
+    if (assigned) any_new = 1;
+    __syncthreads();
+    if (threadIdx.x == 0 && any_new) atomicExch(&active[pass], 1);
+}
+
+__global__ void k_zero_int(int *p, int n)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) p[k] = 0;
+}
+
+int levelset_max_passes(const GridDims &d)
+{
+    int m = d.ni > d.nj ? d.ni : d.nj;
+    return m / kLsH + 2;
+}
+
+void launch_levelset(const GridDims &d, Grids &G, cudaStream_t st)
+{
+    const int passes = levelset_max_passes(d);
+    k_zero_int<<<nblk(passes, kThreads), kThreads, 0, st>>>(G.levelset_active, passes);
+    dim3 grid(nblk(d.nj, kTile), nblk(d.ni, kTile));
+    int *mi = G.levelset_marker, *mo = G.levelset_marker2;
+    float *vi = G.levelset_val2 + (size_t)d.ni * d.nj, *vo = G.levelset_val2;
+    for (int p = 0; p < passes; p++) {
+        k_levelset_pass<<<grid, 1024, 0, st>>>(d, G.fluid_sdf, mi, vi, mo, vo, G.levelset_active, p);
+        int *ti = mi; mi = mo; mo = ti;
+        float *tf = vi; vi = vo; vo = tf;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// pressure RHS: calcPressureRhs (flipsolver2d.cpp:962-991) with divergenceAt
+// (:759-764), evaluated in double like the reference
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_pressure_rhs(GridDims d, const float *__restrict__ u, const float *__restrict__ v,
+                               const float *__restrict__ divc, const int8_t *__restrict__ m,
+                               T *__restrict__ rhs, double scale)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.ni * d.nj) return;
+    const int i = c / d.nj, j = c - i * d.nj;
+    if (!t_fluid(m[c])) {
+        rhs[c] = (T)0;
+        return;
+    }
+    const int NV = d.nj + 1;
+    const float u0 = u[(size_t)i * d.nj + j], u1 = u[(size_t)(i + 1) * d.nj + j];
+    const float v0 = v[(size_t)i * NV + j], v1 = v[(size_t)i * NV + j + 1];
+    const double div = (double)(u1 - u0 + v1 - v0 + divc[c]);
+    double val = -scale * div;
+    val -= (double)t_solid(mat_at(m, d, i - 1, j)) * scale * (double)(u0 - 0);
+    val += (double)t_solid(mat_at(m, d, i + 1, j)) * scale * (double)(u1 - 0);
+    val -= (double)t_solid(mat_at(m, d, i, j - 1)) * scale * (double)(v0 - 0);
+    val += (double)t_solid(mat_at(m, d, i, j + 1)) * scale * (double)(v1 - 0);
+    rhs[c] = (T)val;
+}
+
+void launch_pressure_rhs(const GridDims &d, const Grids &G, void *rhs, int is_double,
+                         const SceneParams &sp, cudaStream_t st)
+{
+    const double scale = 1.f / sp.dx;
+    const int nb = nblk((long long)d.ni * d.nj, kThreads);
+    if (is_double)
+        k_pressure_rhs<double><<<nb, kThreads, 0, st>>>(d, G.u, G.v, G.divc, G.material,
+                                                        (double *)rhs, scale);
+    else
+        k_pressure_rhs<float><<<nb, kThreads, 0, st>>>(d, G.u, G.v, G.divc, G.material,
+                                                       (float *)rhs, scale);
+}
+
+// ---------------------------------------------------------------------------
+// applyPressureThreadU/V (flipsolver2d.cpp:1133-1193) followed, per face, by
+// updateVelocityFromSolids (:1077-1104) through the precomputed factors
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_apply_pressure(GridDims d, Grids G, const T *__restrict__ p, double density,
+                                 double dx, const Scalars *__restrict__ sc, int with_friction)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.ni * d.nj) return;
+    const int i = c / d.nj, j = c - i * d.nj;
+    const double scale = (double)sc->dt / (density * dx);
+    const int8_t *m = G.material;
+    const double pc = (double)p[c];
+    // U face (i, j) between cells (i-1, j) and (i, j)
+    {
+        const double pim1 = i - 1 < 0 ? 0.0 : (double)p[c - d.nj];
+        const int8_t ma = mat_at(m, d, i - 1, j), mb = m[c];
+        const size_t f = (size_t)i * d.nj + j;
+        if (t_fluid(ma) || t_fluid(mb)) {
+            if (t_solid(ma) || t_solid(mb)) G.u[f] = 0.f;
+            else G.u[f] = (float)((double)G.u[f] - scale * (pc - pim1));
+        } else {
+            G.uvalid[f] = 0;
+        }
+        if (with_friction) {
+            const float fr = G.ufric[c];
+            if (fr == fr) G.u[f] = G.u[f] * fr;
+        }
+    }
+    // V face (i, j) between cells (i, j-1) and (i, j)
+    {
+        const double pjm1 = j - 1 < 0 ? 0.0 : (double)p[c - 1];
+        const int8_t ma = mat_at(m, d, i, j - 1), mb = m[c];
+        const size_t f = (size_t)i * (d.nj + 1) + j;
+        if (t_fluid(ma) || t_fluid(mb)) {
+            if (t_solid(ma) || t_solid(mb)) G.v[f] = 0.f;
+            else G.v[f] = (float)((double)G.v[f] - scale * (pc - pjm1));
+        } else {
+            G.vvalid[f] = 0;
+        }
+        if (with_friction) {
+            const float fr = G.vfric[c];
+            if (fr == fr) G.v[f] = G.v[f] * fr;
+        }
+    }
+}
+
+void launch_apply_pressure(const GridDims &d, const SceneParams &sp, const Grids &G,
+                           const void *pressure, int is_double, const Scalars *sc,
+                           bool with_friction, cudaStream_t st)
+{
+    const int nb = nblk((long long)d.ni * d.nj, kThreads);
+    if (is_double)
+        k_apply_pressure<double><<<nb, kThreads, 0, st>>>(d, G, (const double *)pressure,
+                                                          sp.fluidDensity, sp.dx, sc,
+                                                          with_friction ? 1 : 0);
+    else
+        k_apply_pressure<float><<<nb, kThreads, 0, st>>>(d, G, (const float *)pressure,
+                                                         sp.fluidDensity, sp.dx, sc,
+                                                         with_friction ? 1 : 0);
+}
+
+// updateVelocityFromSolids on its own (stage-level API)
+__global__ void k_friction(GridDims d, Grids G)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.ni * d.nj) return;
+    const int i = c / d.nj, j = c - i * d.nj;
+    const float fu = G.ufric[c], fv = G.vfric[c];
+    if (fu == fu) G.u[(size_t)i * d.nj + j] = G.u[(size_t)i * d.nj + j] * fu;
+    if (fv == fv) G.v[(size_t)i * (d.nj + 1) + j] = G.v[(size_t)i * (d.nj + 1) + j] * fv;
+}
+
+void launch_friction(const GridDims &d, const Grids &G, cudaStream_t st)
+{
+    k_friction<<<nblk((long long)d.ni * d.nj, kThreads), kThreads, 0, st>>>(d, G);
+}
+
+// m_savedFluidVelocityGrid = m_fluidVelocityGrid (flipsolver2d.cpp:439)
+__global__ void k_save_grid(Grids G, size_t nu, size_t nv)
+{
+    const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nu) {
+        G.su[k] = G.u[k];
+        G.suvalid[k] = G.uvalid[k];
+    }
+    if (k < nv) {
+        G.sv[k] = G.v[k];
+        G.svvalid[k] = G.vvalid[k];
+    }
+}
+
+void launch_save_grid(const GridDims &d, const Grids &G, cudaStream_t st)
+{
+    const size_t nu = (size_t)(d.ni + 1) * d.nj, nv = (size_t)d.ni * (d.nj + 1);
+    const size_t n = nu > nv ? nu : nv;
+    k_save_grid<<<nblk((long long)n, kThreads), kThreads, 0, st>>>(G, nu, nv);
+}
+
+// applyBodyForces (flipsolver2d.cpp:1222-1241): factor = dt / dx in float
+__global__ void k_body_forces(Grids G, size_t nu, size_t nv, float gI, float gJ, double dx,
+                              const Scalars *__restrict__ sc)
+{
+    const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const float factor = (float)((double)sc->dt / dx);
+    if (k < nu) G.u[k] += factor * gI;
+    if (k < nv) G.v[k] += factor * gJ;
+}
+
+void launch_body_forces(const GridDims &d, const SceneParams &sp, const Grids &G,
+                        const Scalars *sc, cudaStream_t st)
+{
+    const size_t nu = (size_t)(d.ni + 1) * d.nj, nv = (size_t)d.ni * (d.nj + 1);
+    const size_t n = nu > nv ? nu : nv;
+    k_body_forces<<<nblk((long long)n, kThreads), kThreads, 0, st>>>(G, nu, nv, sp.gI, sp.gJ,
+                                                                    sp.dx, sc);
+}
+
+} // namespace fsg

@@ -1,0 +1,138 @@
+// fs_state.h -- device-resident state of one FLIP scene and the launch
+// interface between the host driver (fs_api.cu) and the kernel files.
+//
+// HBM layout (all arrays row-major, linear index i*NJ + j as in
+// linearindexable2d.h:30-37):
+//   particles  bin-CSR: bin b owns slots [bin_start[b], bin_start[b] + bin_count[b]);
+//              slots past bin_count[b] up to bin_start[b+1] are gaps left by
+//              countParticles erasures.  pos/vel are float2 (the reference's
+//              Vec3 z component is always 0), visc float.  Within a bin the
+//              slots are in the reference's ParticleBin storage order.
+//   cell grids NI*NJ: material (int8), solid/fluid SDF, viscosity, density
+//              (float), known-centred / counts / solid id, cell_info (u8 packed
+//              pressure-operator row, see fs_grid.cu).
+//   face grids U (NI+1)*NJ and V NI*(NJ+1) float + u8 validity, current and
+//              saved copies.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "fs_common.cuh"
+
+namespace fsg {
+
+struct SceneParams {
+    double fluidDensity;
+    double dx;
+    int particlesPerCell;
+    float gI, gJ;
+    float picRatio;
+    float particleScale;
+    int pcgIterLimit;
+    int parameterHandlingMethod;
+    int viscosityEnabled;
+    double projectTolerance; // flipsolver2d.cpp:73
+};
+
+struct Particles {
+    float2 *pos = nullptr, *vel = nullptr;
+    float *visc = nullptr;
+    int *slot_bin = nullptr;
+    float2 *pos2 = nullptr, *vel2 = nullptr;
+    float *visc2 = nullptr;
+    int *slot_bin2 = nullptr;
+    uint8_t *flag = nullptr;   // P_STAY / P_MOVE / P_KILL / P_GAP after advection
+    int *dest = nullptr;       // destination bin of a moved particle
+    int *prune_slot = nullptr; // slot inside its bin after the swap-erase prune
+    int *bin_start = nullptr;  // nbins + 1
+    int *bin_count = nullptr;  // nbins
+    int *bin_start2 = nullptr, *bin_count2 = nullptr;
+    int *survivors = nullptr, *incoming = nullptr, *inc_off = nullptr; // nbins (+1)
+    int *mkey = nullptr, *mval = nullptr, *mkey2 = nullptr, *mval2 = nullptr; // moved list
+    int *nmoved = nullptr;     // device scalar
+    int cap = 0;               // slot capacity
+    int nbins = 0;
+};
+
+struct Grids {
+    int8_t *material = nullptr;
+    float *solid_sdf = nullptr;
+    int *solid_id = nullptr;
+    float *fluid_sdf = nullptr;
+    float *u = nullptr, *v = nullptr;
+    uint8_t *uvalid = nullptr, *vvalid = nullptr;
+    float *u2 = nullptr, *v2 = nullptr; // extrapolation output buffers
+    uint8_t *uvalid2 = nullptr, *vvalid2 = nullptr;
+    float *su = nullptr, *sv = nullptr; // saved grid (flipsolver2d.cpp:439)
+    uint8_t *suvalid = nullptr, *svvalid = nullptr;
+    float *visc = nullptr;
+    uint8_t *known = nullptr;
+    float *divc = nullptr;
+    float *density = nullptr;
+    int *counts = nullptr;
+    uint8_t *cell_info = nullptr; // pressure-operator rows frozen at DECOMPOSITION
+    float *ufric = nullptr, *vfric = nullptr; // 1 - mean friction, or NaN when not affected
+    int *emitter_id = nullptr;
+    int *levelset_marker = nullptr, *levelset_marker2 = nullptr;
+    float *levelset_val2 = nullptr;
+    int *levelset_active = nullptr; // device flag: a pass assigned new markers
+};
+
+// scratch scalars living in device memory
+struct Scalars {
+    float dt;              // m_stepDt of the running substep
+    unsigned int maxv2;    // float bits of max |v|^2 (atomicMax on bits)
+    int density_iters;     // LinearSolver::solve return values
+    int pressure_iters;
+    int pcg_status;        // 0 ok, 1 a grid-barrier wait timed out
+    int pad[3];
+};
+
+// launch helpers implemented in the kernel files
+void launch_advect(const GridDims &d, const Particles &P, const Grids &G, const Scalars *sc,
+                   cudaStream_t st);
+void launch_rebin(const GridDims &d, Particles &P, void *scratch, size_t scratch_bytes,
+                  cudaStream_t st);
+size_t rebin_scratch_bytes(const Particles &P);
+void launch_adjust(const GridDims &d, const SceneParams &sp, const Particles &P, const Grids &G,
+                   const void *pressure, int pressure_is_double, const Scalars *sc,
+                   cudaStream_t st);
+void launch_g2p(const GridDims &d, const SceneParams &sp, const Particles &P, const Grids &G,
+                cudaStream_t st);
+void launch_count_erase(const GridDims &d, const SceneParams &sp, Particles &P, const Grids &G,
+                        cudaStream_t st);
+void launch_max_velocity(const Particles &P, Scalars *sc, cudaStream_t st);
+
+void launch_decomposition(const GridDims &d, const Grids &G, cudaStream_t st);
+void launch_density_grid(const GridDims &d, const SceneParams &sp, const Particles &P,
+                         const Grids &G, void *rhs, int rhs_is_double, const Scalars *sc,
+                         cudaStream_t st);
+void launch_p2g_sdf_materials(const GridDims &d, const SceneParams &sp, const Particles &P,
+                              const Grids &G, cudaStream_t st);
+void launch_levelset(const GridDims &d, Grids &G, cudaStream_t st);
+void launch_vel_extrapolate(const GridDims &d, Grids &G, const SceneParams &sp,
+                            const Scalars *sc, bool save_and_gravity, cudaStream_t st);
+void launch_pressure_rhs(const GridDims &d, const Grids &G, void *rhs, int rhs_is_double,
+                         const SceneParams &sp, cudaStream_t st);
+void launch_apply_pressure(const GridDims &d, const SceneParams &sp, const Grids &G,
+                           const void *pressure, int pressure_is_double, const Scalars *sc,
+                           bool with_friction, cudaStream_t st);
+void launch_friction(const GridDims &d, const Grids &G, cudaStream_t st);
+void launch_save_grid(const GridDims &d, const Grids &G, cudaStream_t st);
+void launch_body_forces(const GridDims &d, const SceneParams &sp, const Grids &G,
+                        const Scalars *sc, cudaStream_t st);
+int levelset_max_passes(const GridDims &d);
+void launch_scene_classify(const GridDims &d, const Grids &G, float dx, const float *poly_xy,
+                           const int *poly_off, const int *poly_kind, const float *poly_val,
+                           int npoly, cudaStream_t st);
+void launch_friction_factors(const GridDims &d, const Grids &G, const float *obst_friction,
+                             cudaStream_t st);
+void launch_fill_u8(uint8_t *p, uint8_t v, size_t n, cudaStream_t st);
+
+// exclusive scan of n ints (out may alias nothing); writes the total to out[n]
+size_t scan_scratch_bytes(int n);
+void scan_exclusive(const int *in, int *out, int n, void *scratch, cudaStream_t st);
+
+} // namespace fsg

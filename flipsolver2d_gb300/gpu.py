@@ -1,0 +1,311 @@
+"""ctypes binding of libfsgpu.so (include/fs_gpu.h) and a Python mirror of the
+reference's FlipSolver / LinearSolver interface on top of it.
+
+The CUDA library is required: importing this module does not build it, and
+every call fails loudly (FsError / OSError) when it is missing or when no CUDA
+device is present.  There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+from typing import Dict, Optional
+
+import numpy as np
+
+from . import scenes as _scenes
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libfsgpu.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "fs_gpu.h")
+
+FS_OK = 0
+FS_PCG_FP32, FS_PCG_FP64 = 0, 1
+
+# stage ids (FS_STAGE_*), identical to the oracle's
+ADVECT, DECOMPOSITION, REBIN, DENSITY, P2G, SDF, MATERIALS, AFTER_TRANSFER, LEVELSET, \
+    VEL_EXTRAP, SAVE_GRID, BODY_FORCES, PROJECT, FRICTION, G2P, COUNT, RESEED, \
+    DENSITY_GRID = range(18)
+
+GRIDS: Dict[str, tuple] = {
+    "material": (0, np.int8, "c"), "solid_sdf": (1, np.float32, "c"),
+    "fluid_sdf": (2, np.float32, "c"), "u": (3, np.float32, "u"), "v": (4, np.float32, "v"),
+    "u_valid": (5, np.uint8, "u"), "v_valid": (6, np.uint8, "v"),
+    "saved_u": (7, np.float32, "u"), "saved_v": (8, np.float32, "v"),
+    "viscosity": (9, np.float32, "c"), "known_centered": (10, np.uint8, "c"),
+    "density": (11, np.float32, "c"), "particle_counts": (12, np.int32, "c"),
+    "solid_id": (13, np.int32, "c"), "div_control": (14, np.float32, "c"),
+    "density_rhs": (15, np.float64, "c"), "density_pressure": (16, np.float64, "c"),
+    "pressure": (17, np.float64, "c"), "pressure_rhs": (18, np.float64, "c"),
+    "emitter_id": (19, np.int32, "c"),
+}
+
+
+class FsError(RuntimeError):
+    def __init__(self, status: int, where: str, msg: str):
+        super().__init__(f"{where} failed with status {status}: {msg}")
+        self.status = status
+
+
+class ExecParams(ctypes.Structure):
+    _fields_ = [("pcg_precision", ctypes.c_int), ("pool_threads", ctypes.c_int),
+                ("device", ctypes.c_int), ("reserved", ctypes.c_int * 5)]
+
+
+_lib: Optional[ctypes.CDLL] = None
+
+_SIGS = {
+    "fs_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "fs_last_error": (ctypes.c_char_p, []),
+    "fs_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "fs_add_geometry": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p, ctypes.c_int]),
+    "fs_add_initial_fluid": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p, ctypes.c_int]),
+    "fs_add_sink": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p, ctypes.c_int]),
+    "fs_first_frame_init": (ctypes.c_int, [ctypes.c_void_p]),
+    "fs_step_frame": (ctypes.c_int, [ctypes.c_void_p]),
+    "fs_step": (ctypes.c_int, [ctypes.c_void_p]),
+    "fs_set_step_dt": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_float]),
+    "fs_get_step_dt": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_run_stage": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "fs_max_particle_velocity": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_particle_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_bin_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_get_particles": (ctypes.c_int, [ctypes.c_void_p] * 6),
+    "fs_set_particles": (ctypes.c_int, [ctypes.c_void_p] * 6),
+    "fs_grid_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "fs_get_grid": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]),
+    "fs_set_grid": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]),
+    "fs_get_stat": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "fs_enable_timers": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "fs_reset_timers": (ctypes.c_int, [ctypes.c_void_p]),
+    "fs_get_timer": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "fs_get_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
+    "fs_pcg_solve": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_float,
+                                    ctypes.c_double, ctypes.c_double, ctypes.c_void_p,
+                                    ctypes.c_void_p, ctypes.c_int, ctypes.c_double,
+                                    ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_pcg_solve_device": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                           ctypes.c_float, ctypes.c_double, ctypes.c_double,
+                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                           ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]),
+}
+
+
+def header_symbols() -> list:
+    """Function names declared in include/fs_gpu.h."""
+    with open(HEADER) as f:
+        text = f.read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(fs_\w+)\s*\(", text, re.M)))
+
+
+def load() -> ctypes.CDLL:
+    """Load the in-tree CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise OSError(f"{LIB_PATH} is missing: build it with "
+                      "`python -m flipsolver2d_gb300.build` (no CPU fallback exists)")
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in _SIGS.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _check(st: int, where: str):
+    if st != FS_OK:
+        lib = load()
+        raise FsError(st, where, lib.fs_last_error().decode(errors="replace"))
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def exec_params(precision: int = FS_PCG_FP32, pool_threads: int = 0, device: int = 0) -> ExecParams:
+    e = ExecParams()
+    e.pcg_precision = precision
+    e.pool_threads = pool_threads
+    e.device = device
+    return e
+
+
+class GpuFlipSolver:
+    """FlipSolver (flipsolver2d.h:183-432) with its substep on the GPU."""
+
+    def __init__(self, scene, precision: int = FS_PCG_FP32, pool_threads: int = 0,
+                 device: int = 0):
+        self.lib = load()
+        self.scene = scene
+        self._cp = scene.params.to_c()
+        self.ni, self.nj = self._cp.gridSizeI, self._cp.gridSizeJ
+        self._ex = exec_params(precision, pool_threads, device)
+        h = ctypes.c_void_p()
+        _check(self.lib.fs_create(ctypes.byref(self._cp), ctypes.byref(self._ex), ctypes.byref(h)),
+               "fs_create")
+        self.h = h
+        for o in scene.objects:
+            v = np.ascontiguousarray(o.verts, dtype=np.float32)
+            if o.kind == "solid":
+                _check(self.lib.fs_add_geometry(self.h, o.friction, _ptr(v), len(v)), "fs_add_geometry")
+            elif o.kind == "fluid":
+                _check(self.lib.fs_add_initial_fluid(self.h, o.viscosity, _ptr(v), len(v)),
+                       "fs_add_initial_fluid")
+            elif o.kind == "sink":
+                _check(self.lib.fs_add_sink(self.h, o.divergence, _ptr(v), len(v)), "fs_add_sink")
+            else:
+                raise ValueError(o.kind)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fs_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # driving (names follow the oracle driver so tests read alike)
+    def first_frame_init(self):
+        _check(self.lib.fs_first_frame_init(self.h), "fs_first_frame_init")
+
+    def step_frame(self):
+        _check(self.lib.fs_step_frame(self.h), "fs_step_frame")
+
+    def step(self):
+        _check(self.lib.fs_step(self.h), "fs_step")
+
+    def set_dt(self, dt: float):
+        _check(self.lib.fs_set_step_dt(self.h, float(dt)), "fs_set_step_dt")
+
+    @property
+    def dt(self) -> float:
+        x = ctypes.c_float()
+        _check(self.lib.fs_get_step_dt(self.h, ctypes.byref(x)), "fs_get_step_dt")
+        return float(x.value)
+
+    def stage(self, s: int):
+        _check(self.lib.fs_run_stage(self.h, int(s)), f"fs_run_stage({s})")
+
+    def max_particle_velocity(self) -> float:
+        x = ctypes.c_float()
+        _check(self.lib.fs_max_particle_velocity(self.h, ctypes.byref(x)), "fs_max_particle_velocity")
+        return float(x.value)
+
+    def stat(self, which: int) -> int:
+        x = ctypes.c_int()
+        _check(self.lib.fs_get_stat(self.h, which, ctypes.byref(x)), "fs_get_stat")
+        return int(x.value)
+
+    def particle_count(self) -> int:
+        x = ctypes.c_size_t()
+        _check(self.lib.fs_particle_count(self.h, ctypes.byref(x)), "fs_particle_count")
+        return int(x.value)
+
+    def bin_count(self) -> int:
+        x = ctypes.c_size_t()
+        _check(self.lib.fs_bin_count(self.h, ctypes.byref(x)), "fs_bin_count")
+        return int(x.value)
+
+    def get_particles(self) -> dict:
+        n = self.particle_count()
+        counts = np.zeros(self.bin_count(), np.int32)
+        pos = np.zeros((n, 2), np.float32)
+        vel = np.zeros((n, 2), np.float32)
+        visc = np.zeros(n, np.float32)
+        dead = np.zeros(n, np.uint8)
+        _check(self.lib.fs_get_particles(self.h, _ptr(counts), _ptr(pos), _ptr(vel), _ptr(visc),
+                                         _ptr(dead)), "fs_get_particles")
+        return {"bin_counts": counts, "pos": pos, "vel": vel, "visc": visc, "dead": dead}
+
+    def set_particles(self, p: dict):
+        c = np.ascontiguousarray(p["bin_counts"], np.int32)
+        pos = np.ascontiguousarray(p["pos"], np.float32)
+        vel = np.ascontiguousarray(p["vel"], np.float32)
+        visc = np.ascontiguousarray(p["visc"], np.float32)
+        dead = np.ascontiguousarray(p.get("dead", np.zeros(len(pos), np.uint8)), np.uint8)
+        _check(self.lib.fs_set_particles(self.h, _ptr(c), _ptr(pos), _ptr(vel), _ptr(visc),
+                                         _ptr(dead)), "fs_set_particles")
+
+    def grid_shape(self, name: str):
+        kind = GRIDS[name][2]
+        return {"c": (self.ni, self.nj), "u": (self.ni + 1, self.nj),
+                "v": (self.ni, self.nj + 1)}[kind]
+
+    def get_grid(self, name: str) -> np.ndarray:
+        gid, dt, _ = GRIDS[name]
+        out = np.zeros(self.grid_shape(name), dt)
+        _check(self.lib.fs_get_grid(self.h, gid, _ptr(out), out.nbytes), f"fs_get_grid({name})")
+        return out
+
+    def set_grid(self, name: str, a: np.ndarray):
+        gid, dt, _ = GRIDS[name]
+        a = np.ascontiguousarray(a, dtype=dt).reshape(self.grid_shape(name))
+        _check(self.lib.fs_set_grid(self.h, gid, _ptr(a), a.nbytes), f"fs_set_grid({name})")
+
+    def restore(self, snap: dict, grids=None):
+        """Load an oracle snapshot (particles + grids + dt)."""
+        self.set_particles(snap["particles"])
+        for g in (grids or [k for k in GRIDS if k in snap]):
+            self.set_grid(g, snap[g])
+        self.set_dt(snap["dt"])
+
+    # timing
+    def enable_timers(self, on: bool = True):
+        _check(self.lib.fs_enable_timers(self.h, int(on)), "fs_enable_timers")
+
+    def reset_timers(self):
+        _check(self.lib.fs_reset_timers(self.h), "fs_reset_timers")
+
+    def timer(self, which: int) -> float:
+        x = ctypes.c_double()
+        _check(self.lib.fs_get_timer(self.h, which, ctypes.byref(x)), "fs_get_timer")
+        return float(x.value)
+
+    def stream_ptr(self) -> int:
+        x = ctypes.c_void_p()
+        _check(self.lib.fs_get_stream(self.h, ctypes.byref(x)), "fs_get_stream")
+        return int(x.value or 0)
+
+    def synchronize(self):
+        _check(self.lib.fs_synchronize(self.h), "fs_synchronize")
+
+
+class GpuLinearSolver:
+    """LinearSolver (linearsolver.h:9-23): solve() keeps the reference's
+    arguments and return convention (iteration count; == iterLimit means the
+    solve failed)."""
+
+    def __init__(self, precision: int = FS_PCG_FP32, pool_threads: int = 0, device: int = 0):
+        self.lib = load()
+        self._ex = exec_params(precision, pool_threads, device)
+
+    def solve(self, material: np.ndarray, dt: float, density: float, dx: float,
+              result: np.ndarray, vec: np.ndarray, iter_limit: int = 20, tol: float = 1e-6) -> int:
+        ni, nj = material.shape
+        m = np.ascontiguousarray(material, np.int8)
+        b = np.ascontiguousarray(vec, np.float64).reshape(ni, nj)
+        x = np.zeros((ni, nj), np.float64)
+        it = ctypes.c_int()
+        _check(self.lib.fs_pcg_solve(ni, nj, _ptr(m), float(dt), float(density), float(dx), _ptr(b),
+                                     _ptr(x), int(iter_limit), float(tol), ctypes.byref(self._ex),
+                                     ctypes.byref(it)), "fs_pcg_solve")
+        result[...] = x.reshape(result.shape)
+        return int(it.value)
+
+
+def pcg_solve(material: np.ndarray, rhs: np.ndarray, dt: float, density: float, dx: float,
+              iter_limit: int, tol: float, precision: int = FS_PCG_FP32, pool_threads: int = 8):
+    """Functional form returning (iterations, solution)."""
+    x = np.zeros(material.shape, np.float64)
+    it = GpuLinearSolver(precision, pool_threads).solve(material, dt, density, dx, x, rhs,
+                                                        iter_limit, tol)
+    return it, x

@@ -1,0 +1,214 @@
+/*
+ * fs_gpu.h -- C ABI of the GB300 FLIP substep (libfsgpu.so).
+ *
+ * Drop-in boundary for FlipSolver2d's per-substep hot path.  The reference
+ * has no plugin system; its seams are the FlipSolver class
+ * (FlipSolver2dLib/flipsolver2d.h:183-432) and LinearSolver::solve
+ * (FlipSolver2dLib/linearsolver.h:15-20).  Every entry point below names the
+ * reference member it replaces.  Plain C types only; all pointers are host
+ * pointers unless the name says _device.  A handle owns its device memory and
+ * one CUDA stream; a handle is not re-entrant (neither is the reference:
+ * ThreadPool::i() and the static RNG distribution, flipsolver2d.cpp:1015).
+ *
+ * Errors: every call returns fs_status; FS_OK is 0.  fs_last_error() gives a
+ * message for the calling thread's last failure.  There is no CPU fallback:
+ * without a CUDA device fs_create fails with FS_ERR_CUDA.
+ */
+#ifndef FS_GPU_H
+#define FS_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum fs_status {
+    FS_OK = 0,
+    FS_ERR_BAD_ARG = 1,     /* invalid argument or size mismatch */
+    FS_ERR_CUDA = 2,        /* a CUDA runtime call failed / no device */
+    FS_ERR_OOM = 3,         /* device allocation failed */
+    FS_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up */
+    FS_ERR_UNSUPPORTED = 5, /* feature outside the supported path */
+    FS_ERR_STATE = 6        /* call not valid in the handle's current state */
+} fs_status;
+
+/* Field-for-field FlipSolverParameters (flipsolver2d.h:33-56); units and
+ * meaning as in the reference (dx in metres, gravity in m/s^2, fps, ...). */
+typedef struct fs_params {
+    double fluidDensity;
+    unsigned int seed;
+    double dx;
+    int particlesPerCell;
+    float globalAccelerationI;
+    float globalAccelerationJ;
+    float resolution;
+    int fps;
+    int maxSubsteps;
+    float picRatio;
+    float cflNumber;
+    float particleScale;
+    int pcgIterLimit;
+    float domainSizeI;
+    float domainSizeJ;
+    int gridSizeI;
+    int gridSizeJ;
+    float sceneScale;
+    int viscosityEnabled;        /* must be 0 (viscosity is not on this path) */
+    int useHeavyViscosity;
+    int simulationMethod;        /* must be 0 = SIMULATION_LIQUID */
+    int parameterHandlingMethod; /* 0 PARTICLE, 1 HYBRID, 2 GRID */
+} fs_params;
+
+enum { FS_PCG_FP32 = 0, FS_PCG_FP64 = 1 };
+
+/* Execution knobs with no counterpart in FlipSolverParameters. */
+typedef struct fs_exec_params {
+    int pcg_precision; /* FS_PCG_FP32 (default) or FS_PCG_FP64 vectors */
+    int pool_threads;  /* chunk count of the reference's max-abs residual test
+                          (ThreadPool size, threadpool.cpp:12); 0 = this host's
+                          std::thread::hardware_concurrency() like the reference */
+    int device;        /* CUDA device ordinal */
+    int reserved[5];
+} fs_exec_params;
+
+/* Stage ids: the calls FlipSolver::step() makes, in order
+ * (flipsolver2d.cpp:412-462).  Used by fs_run_stage for stage-level checks. */
+enum {
+    FS_STAGE_ADVECT = 0,         /* advect()                          :414 */
+    FS_STAGE_DECOMPOSITION = 1,  /* matrix + IPP coefficients         :417-418 */
+    FS_STAGE_REBIN = 2,          /* pruneParticles + rebinParticles   :421-422 */
+    FS_STAGE_DENSITY = 3,        /* densityCorrection()               :428 */
+    FS_STAGE_P2G = 4,            /* particleToGrid(); on the GPU fused with
+                                    updateSdf() and updateMaterials() */
+    FS_STAGE_SDF = 5,            /* no-op here: fused into FS_STAGE_P2G */
+    FS_STAGE_MATERIALS = 6,      /* no-op here: fused into FS_STAGE_P2G */
+    FS_STAGE_AFTER_TRANSFER = 7, /* afterTransfer(): sources only, no-op */
+    FS_STAGE_LEVELSET = 8,       /* extrapolateLevelsetInside         :436 */
+    FS_STAGE_VEL_EXTRAP = 9,     /* m_fluidVelocityGrid.extrapolate   :437,:455 */
+    FS_STAGE_SAVE_GRID = 10,     /* saved grid copy                   :439 */
+    FS_STAGE_BODY_FORCES = 11,   /* applyBodyForces()                 :440 */
+    FS_STAGE_PROJECT = 12,       /* project()                         :444 */
+    FS_STAGE_FRICTION = 13,      /* updateVelocityFromSolids()        :447 */
+    FS_STAGE_G2P = 14,           /* particleUpdate()                  :456 */
+    FS_STAGE_COUNT = 15,         /* countParticles()                  :459 */
+    FS_STAGE_RESEED = 16,        /* reseedParticles(): sources only, no-op */
+    FS_STAGE_DENSITY_GRID = 17   /* updateDensityGrid() alone (plus its RHS) */
+};
+
+/* Grid ids for fs_get_grid / fs_set_grid.  c = NI*NJ, u = (NI+1)*NJ,
+ * v = NI*(NJ+1) elements, row-major. */
+enum {
+    FS_GRID_MATERIAL = 0,         /* int8   c  MaterialGrid codes (materialgrid.h:6-13) */
+    FS_GRID_SOLID_SDF = 1,        /* float  c  m_solidSdf */
+    FS_GRID_FLUID_SDF = 2,        /* float  c  m_fluidSdf */
+    FS_GRID_U = 3,                /* float  u  velocityGridU */
+    FS_GRID_V = 4,                /* float  v  velocityGridV */
+    FS_GRID_U_VALID = 5,          /* uint8  u  */
+    FS_GRID_V_VALID = 6,          /* uint8  v  */
+    FS_GRID_SAVED_U = 7,          /* float  u  m_savedFluidVelocityGrid */
+    FS_GRID_SAVED_V = 8,          /* float  v  */
+    FS_GRID_VISCOSITY = 9,        /* float  c  m_viscosityGrid */
+    FS_GRID_KNOWN_CENTERED = 10,  /* uint8  c  m_knownCenteredParams */
+    FS_GRID_DENSITY = 11,         /* float  c  m_densityGrid */
+    FS_GRID_PARTICLE_COUNTS = 12, /* int32  c  m_fluidParticleCounts */
+    FS_GRID_SOLID_ID = 13,        /* int32  c  m_solidId */
+    FS_GRID_DIV_CONTROL = 14,     /* float  c  m_divergenceControl */
+    FS_GRID_DENSITY_RHS = 15,     /* double c  m_pressureRhs */
+    FS_GRID_DENSITY_PRESSURE = 16,/* double c  m_pressureSolverResult */
+    FS_GRID_PRESSURE = 17,        /* double c  projection pressure */
+    FS_GRID_PRESSURE_RHS = 18,    /* double c  projection right-hand side */
+    FS_GRID_EMITTER_ID = 19       /* int32  c  m_emitterId */
+};
+
+enum {
+    FS_STAT_DENSITY_ITERS = 0,  /* SolverStats::densityIterations()  */
+    FS_STAT_PRESSURE_ITERS = 1, /* SolverStats::pressureIterations() */
+    FS_STAT_SUBSTEPS = 2,       /* SolverStats::substepCount()       */
+    FS_STAT_FRAME = 3,          /* FlipSolver::frameNumber()         */
+    FS_STAT_POOL_THREADS = 4    /* chunk count of the residual test  */
+};
+
+typedef struct fs_solver fs_solver;
+
+const char *fs_status_string(fs_status s);
+const char *fs_last_error(void);
+
+/* FlipSolver::FlipSolver(const FlipSolverParameters*) (flipsolver2d.cpp:27-86)
+ * followed by initAdditionalParameters() (:1613-1616).  exec may be NULL. */
+fs_status fs_create(const fs_params *p, const fs_exec_params *exec, fs_solver **out);
+/* FlipSolver::~FlipSolver */
+fs_status fs_destroy(fs_solver *s);
+
+/* FlipSolver::addGeometry / addInitialFluid / addSink (flipsolver2d.cpp:602-620);
+ * xy holds n (x, y) vertex pairs in scene units. */
+fs_status fs_add_geometry(fs_solver *s, float friction, const float *xy, int n);
+fs_status fs_add_initial_fluid(fs_solver *s, float viscosity, const float *xy, int n);
+fs_status fs_add_sink(fs_solver *s, float divergence, const float *xy, int n);
+
+/* FlipSolver::firstFrameInit (flipsolver2d.cpp:788-795) */
+fs_status fs_first_frame_init(fs_solver *s);
+/* FlipSolver::stepFrame (flipsolver2d.cpp:464-500) */
+fs_status fs_step_frame(fs_solver *s);
+/* FlipSolver::step (flipsolver2d.cpp:412-462) with the current step dt */
+fs_status fs_step(fs_solver *s);
+/* m_stepDt, set by stepFrame's CFL loop in the reference (:490) */
+fs_status fs_set_step_dt(fs_solver *s, float dt);
+fs_status fs_get_step_dt(fs_solver *s, float *dt);
+/* one protected stage of step(), FS_STAGE_* */
+fs_status fs_run_stage(fs_solver *s, int stage);
+/* FlipSolver::maxParticleVelocity (flipsolver2d.cpp:1560-1574) */
+fs_status fs_max_particle_velocity(fs_solver *s, float *out);
+
+/* FlipSolver::particleCount / MarkerParticleSystem bins */
+fs_status fs_particle_count(fs_solver *s, size_t *n);
+fs_status fs_bin_count(fs_solver *s, size_t *n);
+/* particles bin by bin in the reference's storage order; dead is set for
+ * particles marked for death between FS_STAGE_ADVECT and FS_STAGE_REBIN */
+fs_status fs_get_particles(fs_solver *s, int32_t *bin_counts, float *pos_xy, float *vel_xy,
+                           float *visc, uint8_t *dead);
+fs_status fs_set_particles(fs_solver *s, const int32_t *bin_counts, const float *pos_xy,
+                           const float *vel_xy, const float *visc, const uint8_t *dead);
+
+fs_status fs_grid_bytes(fs_solver *s, int which, size_t *bytes);
+fs_status fs_get_grid(fs_solver *s, int which, void *out, size_t bytes);
+fs_status fs_set_grid(fs_solver *s, int which, const void *in, size_t bytes);
+fs_status fs_get_stat(fs_solver *s, int which, int *out);
+
+/* Device timing of the last fs_step / fs_step_frame calls, accumulated since
+ * fs_reset_timers: which = 0 whole substeps, 1 PCG kernels, 2 launches
+ * counted (as a float).  Times in milliseconds from CUDA events recorded on
+ * the handle's stream. */
+fs_status fs_enable_timers(fs_solver *s, int enable);
+fs_status fs_reset_timers(fs_solver *s);
+fs_status fs_get_timer(fs_solver *s, int which, double *value);
+/* the handle's cudaStream_t, as an opaque pointer */
+fs_status fs_get_stream(fs_solver *s, void **stream);
+fs_status fs_synchronize(fs_solver *s);
+
+/* LinearSolver::solve (linearsolver.cpp:25-73) on the operator and IPP
+ * coefficients that getPressureProjectionMatrix and getIPPCoefficients
+ * (flipsolver2d.cpp:797-945) build from `material` (MaterialGrid codes,
+ * ni*nj, row-major) with scale = dt / (density * dx * dx).  result is
+ * overwritten (the reference assigns zeros first); *iterations receives the
+ * reference's return value: the loop index at convergence, iter_limit on
+ * failure, 0 for a zero right-hand side.  exec may be NULL. */
+fs_status fs_pcg_solve(int ni, int nj, const int8_t *material, float dt, double density,
+                       double dx, const double *rhs, double *result, int iter_limit,
+                       double tol, const fs_exec_params *exec, int *iterations);
+
+/* Same solve with every array already in device memory: material (int8),
+ * rhs and result in FP32 (precision FS_PCG_FP32) or FP64 (FS_PCG_FP64).
+ * Scratch comes from a per-device cache that grows on demand.  Runs on the
+ * legacy default stream and returns after the solve completed. */
+fs_status fs_pcg_solve_device(int ni, int nj, const int8_t *material_device, float dt,
+                              double density, double dx, const void *rhs_device,
+                              void *result_device, int iter_limit, double tol,
+                              const fs_exec_params *exec, int *iterations);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FS_GPU_H */

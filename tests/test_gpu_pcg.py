@@ -1,0 +1,109 @@
+"""The LinearSolver::solve drop-in (fs_pcg_solve) against the oracle's
+restatement of linearsolver.cpp:25-73 on the same operator and IPP, and
+against the reference's own known-answer system (devDocs/matviz fixture)."""
+import os
+
+import numpy as np
+import pytest
+
+import fsoracle as fo
+from flipsolver2d_gb300 import gpu
+
+from conftest import POOL_THREADS
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def random_mask(n, seed, frac=0.55):
+    """1-cell solid border, a random blob of fluid, the rest empty."""
+    rng = np.random.default_rng(seed)
+    m = np.full((n, n), 0x10, np.int8)
+    yy, xx = np.mgrid[0:n, 0:n]
+    c = n / 2
+    ang = np.arctan2(yy - c, xx - c)
+    r = np.sqrt((yy - c) ** 2 + (xx - c) ** 2)
+    k = rng.integers(3, 7)
+    rad = n * (0.32 + 0.08 * np.sin(k * ang + rng.uniform(0, 6.28)))
+    m[r < rad] = 0x40
+    m[0, :] = m[-1, :] = m[:, 0] = m[:, -1] = 0x20
+    return m
+
+
+def rhs_for(m, seed):
+    rng = np.random.default_rng(seed)
+    b = rng.standard_normal(m.shape) * 100.0
+    b[(m & 0x40) == 0] = 0.0
+    return b
+
+
+@pytest.mark.parametrize("n,seed", [(24, 1), (64, 2), (101, 3), (128, 4)])
+def test_fp64_matches_reference_loop(port_lib, gpu_lib, n, seed):
+    m = random_mask(n, seed)
+    b = rhs_for(m, seed)
+    args = dict(dt=1.0 / 30, density=1000.0, dx=1.0 / n)
+    for limit, tol in [(200, 1e-2), (37, 1e-2), (500, 1e-6)]:
+        it_o, x_o = fo.pcg_solve(m, b, args["dt"], args["density"], args["dx"], limit, tol)
+        it_g, x_g = gpu.pcg_solve(m, b, args["dt"], args["density"], args["dx"], limit, tol,
+                                  precision=gpu.FS_PCG_FP64, pool_threads=POOL_THREADS)
+        assert it_g == it_o
+        err = np.linalg.norm(x_g - x_o) / max(np.linalg.norm(x_o), 1e-300)
+        assert err <= 1e-9, f"n={n} limit={limit}: {err}"
+
+
+@pytest.mark.parametrize("n,seed", [(64, 5), (128, 6), (256, 7)])
+def test_fp32_close_to_fp64(port_lib, gpu_lib, n, seed):
+    m = random_mask(n, seed)
+    b = rhs_for(m, seed)
+    it_o, x_o = fo.pcg_solve(m, b, 1.0 / 30, 1000.0, 1.0 / n, 200, 1e-2)
+    it_g, x_g = gpu.pcg_solve(m, b, 1.0 / 30, 1000.0, 1.0 / n, 200, 1e-2,
+                              precision=gpu.FS_PCG_FP32, pool_threads=POOL_THREADS)
+    err = np.linalg.norm(x_g - x_o) / np.linalg.norm(x_o)
+    assert err <= 2e-3, f"FP32 PCG relative-L2 error {err} (iters {it_g} vs {it_o})"
+
+
+def test_zero_rhs_returns_zero(gpu_lib):
+    m = random_mask(32, 1)
+    it, x = gpu.pcg_solve(m, np.zeros(m.shape), 0.01, 1000.0, 1.0 / 32, 50, 1e-2)
+    assert it == 0 and not np.any(x)
+
+
+def test_no_fluid_is_identity(port_lib, gpu_lib):
+    m = np.full((16, 16), 0x10, np.int8)
+    b = np.zeros((16, 16))
+    b[3, 4] = 1.0
+    it_o, x_o = fo.pcg_solve(m, b, 0.01, 1000.0, 1.0 / 16, 10, 1e-2)
+    it_g, x_g = gpu.pcg_solve(m, b, 0.01, 1000.0, 1.0 / 16, 10, 1e-2, precision=gpu.FS_PCG_FP64,
+                              pool_threads=POOL_THREADS)
+    assert it_g == it_o
+    assert np.allclose(x_g, x_o)
+
+
+def test_iteration_limit_reported(port_lib, gpu_lib):
+    m = random_mask(48, 9)
+    b = rhs_for(m, 9)
+    it, _ = gpu.pcg_solve(m, b, 1.0 / 30, 1000.0, 1.0 / 48, 3, 1e-12, precision=gpu.FS_PCG_FP64,
+                          pool_threads=POOL_THREADS)
+    assert it == 3
+
+
+def test_bad_material_rejected(gpu_lib):
+    m = random_mask(16, 1)
+    m[5, 5] = 0x7
+    with pytest.raises(gpu.FsError):
+        gpu.pcg_solve(m, np.ones(m.shape), 0.01, 1000.0, 1.0 / 16, 5, 1e-2)
+
+
+def test_matviz_known_answer(gpu_lib):
+    """devDocs/matviz: the reference's dumped 64x64 system (402 unknowns) and
+    its solve.  The GPU solve of the same operator must reproduce the
+    reference's solution to the fixture's own accuracy."""
+    f = np.load(os.path.join(GOLDEN, "matviz.npz"))
+    m, b, x_ref = f["material"], f["vin"], f["vout"]
+    scale = float(f["scale"])
+    it, x = gpu.pcg_solve(m, b, scale, 1.0, 1.0, 2000, 1e-9, precision=gpu.FS_PCG_FP64,
+                          pool_threads=POOL_THREADS)
+    fluid = (m & 0x40) != 0
+    err = np.linalg.norm(x[fluid] - x_ref[fluid]) / np.linalg.norm(x_ref[fluid])
+    assert err < 1e-4, f"relative-L2 vs the reference's vout: {err}"
