@@ -161,6 +161,7 @@ struct fs_solver {
     std::vector<float> obst_friction;
     float *d_obst_friction = nullptr;
     bool friction_dirty = true;
+    std::mt19937 rng; // m_randEngine (flipsolver2d.cpp:71), persists across calls
     int frame = 0;
     float step_dt = 0.f, frame_dt = 0.f;
     bool initialized = false;
@@ -341,6 +342,7 @@ extern "C" fs_status fs_create(const fs_params *p, const fs_exec_params *exec, f
     sp.projectTolerance = p->viscosityEnabled ? 1e-6 : 1e-2; // flipsolver2d.cpp:73
     s->step_dt = 1.f / p->fps; // flipsolver2d.cpp:46-47
     s->frame_dt = 1.f / p->fps;
+    s->rng = std::mt19937(p->seed);
 
     fs_status st = FS_OK;
 #define A(expr)                                                                                    \
@@ -473,7 +475,6 @@ extern "C" fs_status fs_destroy(fs_solver *s)
 static fs_status add_poly(fs_solver *s, int kind, float value, const float *xy, int n)
 {
     if (!s || !xy || n < 1) return fail(FS_ERR_BAD_ARG, "polygon needs at least one vertex");
-    if (s->initialized) return fail(FS_ERR_STATE, "objects must be added before frame 0");
     Poly g;
     g.kind = kind;
     g.value = value;
@@ -495,6 +496,8 @@ extern "C" fs_status fs_add_sink(fs_solver *s, float divergence, const float *xy
 {
     return add_poly(s, 2, divergence, xy, n);
 }
+
+static fs_status download_bins(fs_solver *s, std::vector<int> &start, std::vector<int> &count);
 
 // ---- host restatement of the sampler used for seeding (grid2d.h:187-216) --
 static inline float h_frac(float v) { return v - (float)(long long)v; }
@@ -526,8 +529,8 @@ static float h_grid_lerp(const std::vector<float> &g, int si, int sj, float ox, 
 extern "C" fs_status fs_first_frame_init(fs_solver *s)
 {
     if (!s) return fail(FS_ERR_BAD_ARG, "null handle");
-    if (s->initialized) return fail(FS_ERR_STATE, "frame 0 already initialised");
     TRY(set_device(s));
+    TRY(sync_all(s));
     const GridDims &d = s->d;
     // polygons -> device
     std::vector<float> xy;
@@ -565,11 +568,31 @@ extern "C" fs_status fs_first_frame_init(fs_solver *s)
     CK(cudaMemcpyAsync(u.data(), s->G.u, s->nu * 4, cudaMemcpyDeviceToHost, s->st));
     CK(cudaMemcpyAsync(v.data(), s->G.v, s->nv * 4, cudaMemcpyDeviceToHost, s->st));
     CK(cudaStreamSynchronize(s->st));
-    std::mt19937 rng(s->p.seed);
+    std::mt19937 &rng = s->rng;
     std::uniform_real_distribution<float> dist(0.f, 1.f);
     const int nb = s->P.nbins;
     std::vector<std::vector<float2>> bpos(nb), bvel(nb);
     std::vector<std::vector<float>> bvisc(nb);
+    {
+        // particles already present stay first in their bins; the seeds are
+        // appended (ParticleBin::addMarkerParticle pushes back)
+        std::vector<int> st, ct;
+        TRY(download_bins(s, st, ct));
+        const int nslots = st[nb];
+        if (nslots > 0) {
+            std::vector<float2> p(nslots), v(nslots);
+            std::vector<float> vi(nslots);
+            CK(cudaMemcpy(p.data(), s->P.pos, nslots * sizeof(float2), cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(v.data(), s->P.vel, nslots * sizeof(float2), cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(vi.data(), s->P.visc, nslots * sizeof(float), cudaMemcpyDeviceToHost));
+            for (int b = 0; b < nb; b++)
+                for (int q = st[b]; q < st[b] + ct[b]; q++) {
+                    bpos[b].push_back(p[q]);
+                    bvel[b].push_back(v[q]);
+                    bvisc[b].push_back(vi[q]);
+                }
+        }
+    }
     auto bin_of = [&](long long i, long long j) -> long long {
         long long bi = i / 3, bj = j / 3;
         if (bi < 0 || bi >= d.bni || bj < 0 || bj >= d.bnj) return -1;
@@ -764,7 +787,6 @@ static fs_status stage(fs_solver *s, int which, bool in_step)
 
 static fs_status step_impl(fs_solver *s)
 {
-    if (!s->initialized) return fail(FS_ERR_STATE, "call fs_first_frame_init or fs_step_frame first");
     TRY(ensure_friction(s));
     if (s->timers) CK(cudaEventRecord(s->e0, s->st));
     k_set_dt<<<1, 1, 0, s->st>>>(s->sc, s->step_dt);
@@ -834,7 +856,7 @@ extern "C" fs_status fs_step_frame(fs_solver *s)
 {
     if (!s) return fail(FS_ERR_BAD_ARG, "null handle");
     TRY(set_device(s));
-    if (s->frame == 0 && !s->initialized) TRY(fs_first_frame_init(s));
+    if (s->frame == 0) TRY(fs_first_frame_init(s)); // flipsolver2d.cpp:466-469
     float substepTime = 0.f;
     bool finished = false;
     int substepCount = 0;
@@ -888,7 +910,6 @@ extern "C" fs_status fs_get_step_dt(fs_solver *s, float *dt)
 extern "C" fs_status fs_run_stage(fs_solver *s, int which)
 {
     if (!s) return fail(FS_ERR_BAD_ARG, "null handle");
-    if (!s->initialized) return fail(FS_ERR_STATE, "scene not initialised");
     TRY(set_device(s));
     TRY(ensure_friction(s));
     k_set_dt<<<1, 1, 0, s->st>>>(s->sc, s->step_dt);

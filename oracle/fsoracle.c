@@ -1547,13 +1547,26 @@ static void count_particles(fso_solver *s)
 /* ------------------------------------------------------------------------ */
 /* driver                                                                   */
 /* ------------------------------------------------------------------------ */
+static int run_stage(fso_solver *s, int stage);
+
+/* Stage entry point: like SolverStats::reset before the stage, so the solve
+ * statistics report this stage's solve. */
 int fso_run_stage(fso_solver *s, int stage)
+{
+    if (stage == FSO_DENSITY) s->density_iters = 0;
+    if (stage == FSO_PROJECT) s->pressure_iters = 0;
+    return run_stage(s, stage);
+}
+
+static int run_stage(fso_solver *s, int stage)
 {
     switch (stage) {
     case FSO_ADVECT: advect(s); break;
     case FSO_DECOMPOSITION: build_matrix(s); break;
     case FSO_REBIN: prune(s); rebin(s); break;
-    case FSO_DENSITY: if (!s->p.viscosityEnabled) density_correction(s); break;
+    case FSO_DENSITY:
+        if (!s->p.viscosityEnabled) density_correction(s);
+        break;
     case FSO_P2G: particle_to_grid(s); break;
     case FSO_SDF: update_sdf(s); break;
     case FSO_MATERIALS: update_materials(s); break;
@@ -1584,7 +1597,7 @@ static void step(fso_solver *s) /* FlipSolver::step, flipsolver2d.cpp:412-462 */
                                 FSO_SDF, FSO_MATERIALS, FSO_AFTER_TRANSFER, FSO_LEVELSET,
                                 FSO_VEL_EXTRAP, FSO_SAVE_GRID, FSO_BODY_FORCES, FSO_PROJECT,
                                 FSO_FRICTION, FSO_VEL_EXTRAP, FSO_G2P, FSO_COUNT, FSO_RESEED};
-    for (size_t k = 0; k < sizeof(order) / sizeof(order[0]); k++) fso_run_stage(s, order[k]);
+    for (size_t k = 0; k < sizeof(order) / sizeof(order[0]); k++) run_stage(s, order[k]);
 }
 
 void fso_step(fso_solver *s)

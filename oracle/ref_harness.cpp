@@ -56,6 +56,7 @@ public:
             m_markerParticles.rebinParticles();
             break;
         case FSO_DENSITY:
+            m_stats.reset(); // report this stage's solve
             if (!m_viscosityEnabled) densityCorrection();
             break;
         case FSO_P2G: particleToGrid(); break;
@@ -66,7 +67,10 @@ public:
         case FSO_VEL_EXTRAP: m_fluidVelocityGrid.extrapolate(10); break;
         case FSO_SAVE_GRID: m_savedFluidVelocityGrid = m_fluidVelocityGrid; break;
         case FSO_BODY_FORCES: applyBodyForces(); break;
-        case FSO_PROJECT: project(); break;
+        case FSO_PROJECT:
+            m_stats.reset();
+            project();
+            break;
         case FSO_FRICTION: updateVelocityFromSolids(); break;
         case FSO_G2P: particleUpdate(); break;
         case FSO_COUNT: countParticles(); break;
