@@ -1,0 +1,342 @@
+"""Benchmark of the FLIP substep on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+
+Workload: the large plain-FLIP dam break -- 1x1 m at 1024^2 cells, 1-cell
+solid walls, fluid block I in [0.4, 1-dx], J in [dx, 0.4], 4 particles per
+cell jittered from seed 7 (~1.0 M particles), one convex 6-vertex solid
+(friction 0.1) drawn in the central 30 % from seed 7; density 1000, g = 9.81,
+30 fps, CFL 5, picRatio 0.03, pcgIterLimit 200 with the reference's absolute
+1e-2 max-abs stopping test, FP32 PCG with FP64 reductions.  Synthetic seeded
+data.  A step is one substep (FlipSolver::step) with the CFL dt the
+reference's frame loop would choose; the scene is first advanced by two
+frames so the fluid is moving.
+
+One JSON line is printed.  `value` is device-timed (CUDA events on the
+solver's stream, L2 flushed by a 256 MiB write between steps, outside the
+events); `e2e` goes through the C ABI with host-resident state uploaded and
+downloaded every step; `roofline` is for the PCG kernel, which dominates the
+substep; `cpu_baseline` is the CPU oracle on this host's cores on a bounded
+sample of the same workload.  With --impl reference only the CPU
+implementation is timed (the reference's sources are not present on GPU
+hosts, so its plain-C restatement, pinned bit for bit to it, stands in).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+RES = 1024
+SEED = 7
+WARM_FRAMES = 2
+METRIC = "particle-substeps/s"
+WORKLOAD = "dam_break_1024_obstacle"
+
+
+def scene():
+    from flipsolver2d_gb300 import scenes
+
+    return scenes.dam_break(RES, seed=SEED, obstacle=True)
+
+
+def cfl_dt(vel: float, p) -> float:
+    """First substep size of FlipSolver::stepFrame (flipsolver2d.cpp:478-489)."""
+    f32 = np.float32
+    frame_dt = f32(1.0) / f32(p.fps)
+    m = f32(p.cflNumber) / (f32(vel) + f32(1e-15))
+    if m >= frame_dt or p.maxSubsteps == 1:
+        return float(frame_dt)
+    if f32(2.0) * m >= frame_dt:
+        return float(f32(0.5) * frame_dt)
+    return float(m)
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sms, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sms.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sms) if sms else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sms)}
+
+
+def executed_iters(ret: int, limit: int) -> int:
+    """LinearSolver::solve returns the loop index on convergence."""
+    return limit if ret >= limit else ret + 1
+
+
+def run_cpu_sample(threads: int, substeps: int = 2):
+    """The CPU oracle on a bounded sample: frame-0 setup (untimed), then
+    `substeps` substeps of the same workload."""
+    os.environ["FSO_HOST_THREADS"] = str(threads)
+    os.environ.setdefault("FSO_REF_THREADS", str(threads))
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import build as oracle_build
+
+    oracle_build.build_port()
+    import fsoracle as fo
+
+    kind = "reference" if fo.available("ref") else "port"
+    sc = scene()
+    o = fo.OracleSolver(sc, "ref" if kind == "reference" else "port")
+    o.first_frame_init()
+    work, t_total, times = 0, 0.0, []
+    for _ in range(substeps):
+        n = o.particle_count()
+        o.set_dt(cfl_dt(o.max_particle_velocity(), sc.params))
+        t0 = time.perf_counter()
+        o.step()
+        dt = time.perf_counter() - t0
+        times.append(dt)
+        t_total += dt
+        work += n
+    o.close()
+    return {"value": work / t_total, "unit": METRIC, "cores": threads, "kind": kind,
+            "sample": f"{substeps} substeps of {WORKLOAD} from frame 0 ({work} particle-substeps, "
+                      f"{t_total:.1f} s)", "step_s": times}
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    steps = max(1, min(args.steps, 3))
+    cb = run_cpu_sample(threads, substeps=steps)
+    line = {"metric": METRIC, "value": cb["value"], "unit": METRIC, "n_gpus": args.gpus,
+            "steps": steps, "warmup": 0, "ms_per_step": 1e3 * float(np.mean(cb["step_s"])),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded dam-break scene)",
+            "config": {"workload": WORKLOAD, "grid": RES, "seed": SEED,
+                       "pcg": "reference PCG+IPP, FP64, limit 200, abs tol 1e-2"},
+            "impl": "reference",
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": cb["value"], "unit": METRIC, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def gpu_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(local)
+    from flipsolver2d_gb300 import build, gpu
+
+    build.build()
+    torch.cuda.set_device(local)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")
+
+    def l2_flush():
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+
+    sc = scene()
+    p = sc.params
+    s = gpu.GpuFlipSolver(sc, precision=gpu.FS_PCG_FP32, device=local)
+    for _ in range(WARM_FRAMES):
+        s.step_frame()
+    ncell = s.ni * s.nj
+    limit = p.pcgIterLimit
+
+    def one_step():
+        n = s.particle_count()
+        s.set_dt(cfl_dt(s.max_particle_velocity(), p))
+        s.step()
+        return n
+
+    for _ in range(args.warmup):
+        one_step()
+    s.enable_timers(True)
+    sampler = ClockSampler(local)
+    sampler.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    work, step_ms, pcg_ms, iters, bytes_pcg = 0, [], 0.0, [], 0.0
+    launches = 0.0
+    for _ in range(args.steps):
+        l2_flush()
+        s.reset_timers()
+        n = one_step()
+        work += n
+        step_ms.append(s.timer(0))
+        pcg_ms += s.timer(1)
+        launches += s.timer(2)
+        itd = executed_iters(s.stat(0), limit)
+        itp = executed_iters(s.stat(1), limit)
+        iters.append((itd, itp))
+        # algorithmic bytes of one solve: setup 16 B/cell (read b, write x, r, s)
+        # + 34 B per cell-iteration (FP32 x, r, s and the u8 operator row)
+        bytes_pcg += ncell * (2 * 16 + 34 * (itd + itp))
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    s.enable_timers(False)
+    total_ms = float(sum(step_ms))
+    if dist:
+        t = torch.tensor([total_ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * work / (total_ms / 1e3)
+
+    # end to end through the C ABI with host-resident state: upload particles
+    # and the carried grids, one substep, download them again
+    e2e_steps = max(1, min(args.steps, 5))
+    snap_p = s.get_particles()
+    carried = ["u", "v", "material"]
+    snap_g = {g: s.get_grid(g) for g in carried}
+    h2d = sum(v.nbytes for k, v in snap_p.items() if k != "dead") + snap_p["dead"].nbytes
+    h2d += sum(a.nbytes for a in snap_g.values())
+    d2h = h2d
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_work = 0
+    for _ in range(e2e_steps):
+        s.set_particles(snap_p)
+        for g, a in snap_g.items():
+            s.set_grid(g, a)
+        e2e_work += len(snap_p["pos"])
+        s.set_dt(cfl_dt(s.max_particle_velocity(), p))
+        s.step()
+        snap_p = s.get_particles()
+        snap_g = {g: s.get_grid(g) for g in carried}
+    e2e_s = time.perf_counter() - t0
+    e2e_value = world * e2e_work / e2e_s
+
+    peak, peak_kind = measured_peaks()
+    achieved = bytes_pcg / (pcg_ms / 1e3) / 1e9 if pcg_ms > 0 else None
+    n_pcg = 2 * args.steps
+    cell_iters = sum(ncell * (a + b) for a, b in iters)
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        try:
+            cpu = run_cpu_sample(os.cpu_count() or 1, substeps=2)
+            cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        except Exception as e:  # reported, never fatal for the GPU line
+            cpu = {"value": None, "unit": METRIC, "cores": 0, "kind": "port",
+                   "sample": f"failed: {e}"}
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded dam-break scene)",
+        "config": {"workload": WORKLOAD, "grid": RES, "seed": SEED, "particles": int(work / args.steps),
+                   "pcg": "PCG+IPP FP32 vectors, FP64 reductions, reference stopping "
+                          "(limit 200, abs tol 1e-2 max-abs)",
+                   "l2": "flushed between steps (256 MiB write)", "warm_frames": WARM_FRAMES,
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "pcg_cell_iter_per_s": cell_iters / (pcg_ms / 1e3) if pcg_ms > 0 else None,
+        "pcg_iterations_per_step": [list(x) for x in iters],
+        "step_latency_ms": {"p50": float(np.percentile(step_ms, 50)),
+                            "p99": float(np.percentile(step_ms, 99))},
+        "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
+                "path": "fs_set_particles + fs_set_grid(u, v, material) + fs_step + "
+                        "fs_get_particles + fs_get_grid, host buffers"},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": "k_pcg<float>",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": None,
+                     "peak_source": peak_kind,
+                     "bytes_model": "per solve 16 B/cell + 34 B/cell-iteration",
+                     "launches": n_pcg, "avg_launch_ms": pcg_ms / n_pcg},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    s.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return reference_arm(args)
+    return gpu_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -111,6 +111,17 @@ static std::vector<int> split_range_ends(long long length, long long parts)
     return ends;
 }
 
+static void split_range_params(long long length, long long parts, long long *ps, long long *rem)
+{
+    long long numParts = parts < 1 ? 1 : parts;
+    if (length < numParts) numParts = length;
+    if (numParts < 1) numParts = 1;
+    long long partSize = length / numParts;
+    if (partSize < 1) partSize = 1;
+    *ps = partSize;
+    *rem = partSize * numParts < length ? length - partSize * numParts : 0;
+}
+
 static int default_pool_threads()
 {
     unsigned n = std::thread::hardware_concurrency();
@@ -150,7 +161,9 @@ struct fs_solver {
     double *partials = nullptr;
     int pcg_grid = 0;
     int *chunk_end = nullptr, *chunk_last = nullptr;
+    double *chunk_val = nullptr;
     int nchunks = 0;
+    long long chunk_ps = 1, chunk_rem = 0; // splitRange part size and remainder
     GridBarrier *bar = nullptr;
     void *rebin_scratch = nullptr;
     size_t rebin_scratch_size = 0;
@@ -384,9 +397,8 @@ extern "C" fs_status fs_create(const fs_params *p, const fs_exec_params *exec, f
     A(dalloc(s, &G.ufric, n));
     A(dalloc(s, &G.vfric, n));
     A(dalloc(s, &G.emitter_id, n));
-    A(dalloc(s, &G.levelset_marker, n));
-    A(dalloc(s, &G.levelset_marker2, n));
-    A(dalloc(s, &G.levelset_val2, 2 * n));
+    A(dalloc(s, &G.levelset_cells, n));
+    A(dalloc(s, &G.levelset_act, 3 * ((size_t)(d.ni + 31) / 32) * ((d.nj + 31) / 32) + 8));
     A(dalloc(s, &G.levelset_active, (size_t)levelset_max_passes(d) + 1));
     Particles &P = s->P;
     P.nbins = d.bni * d.bnj;
@@ -415,8 +427,10 @@ extern "C" fs_status fs_create(const fs_params *p, const fs_exec_params *exec, f
     A(dalloc(s, &s->bar, 1));
     std::vector<int> ends = split_range_ends((long long)n, s->ex.pool_threads);
     s->nchunks = (int)ends.size();
+    split_range_params((long long)n, s->ex.pool_threads, &s->chunk_ps, &s->chunk_rem);
     A(dalloc(s, &s->chunk_end, ends.size() + 1));
     A(dalloc(s, &s->chunk_last, ends.size() + 1));
+    A(dalloc(s, &s->chunk_val, ends.size() + 1));
     if (!ends.empty() &&
         cudaMemcpy(s->chunk_end, ends.data(), ends.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
         return cleanup(fail(FS_ERR_CUDA, "fs_create: upload failed"));
@@ -656,6 +670,7 @@ template <typename T> static PcgArgs<T> pcg_args(fs_solver *s, const void *b, vo
     a.partials = s->partials;
     a.chunk_end = s->chunk_end;
     a.chunk_last_unit = s->chunk_last;
+    a.chunk_val = s->chunk_val;
     a.nchunks = s->nchunks;
     a.sc = s->sc;
     a.density = s->sp.fluidDensity;
@@ -665,6 +680,8 @@ template <typename T> static PcgArgs<T> pcg_args(fs_solver *s, const void *b, vo
     a.iters_out = iters;
     a.status = &s->sc->pcg_status;
     a.bar = s->bar;
+    a.wrap_flag = &s->sc->wrap_units;
+    a.mode = 0;
     return a;
 }
 
@@ -672,9 +689,10 @@ static fs_status run_pcg(fs_solver *s, const void *b, void *x, int *iters)
 {
     if (s->timers) CK(cudaEventRecord(s->p0, s->st));
     cudaError_t e;
-    if (s->prec == FS_PCG_FP64) e = launch_pcg<double>(pcg_args<double>(s, b, x, iters), s->pcg_grid, s->st);
-    else e = launch_pcg<float>(pcg_args<float>(s, b, x, iters), s->pcg_grid, s->st);
-    g_kernel_launches += 1;
+    int launched = 0;
+    if (s->prec == FS_PCG_FP64) e = launch_pcg<double>(pcg_args<double>(s, b, x, iters), s->st, &launched);
+    else e = launch_pcg<float>(pcg_args<float>(s, b, x, iters), s->st, &launched);
+    g_kernel_launches += launched;
     if (e != cudaSuccess) return fail(FS_ERR_CUDA, "PCG launch: %s", cudaGetErrorString(e));
     if (s->timers) {
         CK(cudaEventRecord(s->p1, s->st));
@@ -698,9 +716,8 @@ static fs_status stage(fs_solver *s, int which, bool in_step)
         s->after_advect = true;
         break;
     case FS_STAGE_DECOMPOSITION:
-        launch_decomposition(d, s->G, q);
-        launch_chunk_last_unit(s->G.cell_info, s->chunk_end, s->nchunks, s->chunk_last, q);
-        g_kernel_launches += 2;
+        launch_decomposition(d, s->G, s->chunk_last, s->nchunks, s->chunk_ps, s->chunk_rem, s->sc, q);
+        g_kernel_launches += 1;
         break;
     case FS_STAGE_REBIN: {
         long long before = g_kernel_launches;
@@ -1179,13 +1196,14 @@ struct PcgCache {
     void *b = nullptr, *x = nullptr, *r0 = nullptr, *r1 = nullptr, *s0 = nullptr, *s1 = nullptr;
     double *partials = nullptr;
     int *chunk_end = nullptr, *chunk_last = nullptr;
+    double *chunk_val = nullptr;
     int chunk_cap = 0;
     GridBarrier *bar = nullptr;
     Scalars *sc = nullptr;
     Scalars *sc_host = nullptr;
     void release()
     {
-        void *ps[] = {material, info, b, x, r0, r1, s0, s1, partials, chunk_end, chunk_last, bar, sc};
+        void *ps[] = {material, info, b, x, r0, r1, s0, s1, partials, chunk_end, chunk_last, chunk_val, bar, sc};
         for (void *p : ps)
             if (p) cudaFree(p);
         if (sc_host) cudaFreeHost(sc_host);
@@ -1218,6 +1236,7 @@ static fs_status pcg_cache_get(int dev, size_t cells, size_t esz, int nchunks, P
     CK(cudaMalloc(&c.partials, (size_t)(3 * maxgrid + 8) * sizeof(double)));
     CK(cudaMalloc(&c.chunk_end, (size_t)c.chunk_cap * sizeof(int)));
     CK(cudaMalloc(&c.chunk_last, (size_t)c.chunk_cap * sizeof(int)));
+    CK(cudaMalloc(&c.chunk_val, (size_t)c.chunk_cap * sizeof(double)));
     CK(cudaMalloc(&c.bar, sizeof(GridBarrier)));
     CK(cudaMalloc(&c.sc, sizeof(Scalars)));
     CK(cudaMallocHost(&c.sc_host, sizeof(Scalars)));
@@ -1248,34 +1267,40 @@ static fs_status pcg_solve_common(int ni, int nj, const int8_t *mat_dev, float d
     Grids G;
     G.material = const_cast<int8_t *>(mat_dev);
     G.cell_info = c->info;
-    launch_decomposition(d, G, st);
-    launch_chunk_last_unit(c->info, c->chunk_end, (int)ends.size(), c->chunk_last, st);
+    long long ps = 1, rem = 0;
+    split_range_params((long long)N, T, &ps, &rem);
+    launch_decomposition(d, G, c->chunk_last, (int)ends.size(), ps, rem, c->sc, st);
     k_set_dt<<<1, 1, 0, st>>>(c->sc, dt);
     CK(cudaMemsetAsync(&c->sc->pcg_status, 0, sizeof(int), st));
-    g_kernel_launches += 3;
+    g_kernel_launches += 2;
     cudaError_t e;
+    int launched = 0;
     if (prec == FS_PCG_FP64) {
         PcgArgs<double> a{};
         a.ni = ni; a.nj = nj; a.N = (long long)N; a.info = c->info;
         a.b = (const double *)rhs_dev; a.x = (double *)res_dev;
         a.r0 = (double *)c->r0; a.r1 = (double *)c->r1; a.s0 = (double *)c->s0; a.s1 = (double *)c->s1;
         a.partials = c->partials; a.chunk_end = c->chunk_end; a.chunk_last_unit = c->chunk_last;
+        a.chunk_val = c->chunk_val;
         a.nchunks = (int)ends.size(); a.sc = c->sc; a.density = density; a.dx = dx;
         a.iter_limit = iter_limit; a.tol = tol; a.iters_out = &c->sc->density_iters;
         a.status = &c->sc->pcg_status; a.bar = c->bar;
-        e = launch_pcg<double>(a, pcg_grid_size<double>((long long)N), st);
+        a.wrap_flag = &c->sc->wrap_units; a.mode = 0;
+        e = launch_pcg<double>(a, st, &launched);
     } else {
         PcgArgs<float> a{};
         a.ni = ni; a.nj = nj; a.N = (long long)N; a.info = c->info;
         a.b = (const float *)rhs_dev; a.x = (float *)res_dev;
         a.r0 = (float *)c->r0; a.r1 = (float *)c->r1; a.s0 = (float *)c->s0; a.s1 = (float *)c->s1;
         a.partials = c->partials; a.chunk_end = c->chunk_end; a.chunk_last_unit = c->chunk_last;
+        a.chunk_val = c->chunk_val;
         a.nchunks = (int)ends.size(); a.sc = c->sc; a.density = density; a.dx = dx;
         a.iter_limit = iter_limit; a.tol = tol; a.iters_out = &c->sc->density_iters;
         a.status = &c->sc->pcg_status; a.bar = c->bar;
-        e = launch_pcg<float>(a, pcg_grid_size<float>((long long)N), st);
+        a.wrap_flag = &c->sc->wrap_units; a.mode = 0;
+        e = launch_pcg<float>(a, st, &launched);
     }
-    g_kernel_launches += 1;
+    g_kernel_launches += launched;
     if (e != cudaSuccess) return fail(FS_ERR_CUDA, "PCG launch: %s", cudaGetErrorString(e));
     CK(cudaMemcpyAsync(c->sc_host, c->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));

@@ -172,30 +172,59 @@ void launch_fill_u8(uint8_t *p, uint8_t v, size_t n, cudaStream_t st)
 //              linear index lies inside the grid
 // IPP off-diagonals are 1/(nsc(neighbour) * scale) (flipsolver2d.cpp:924-927).
 // ---------------------------------------------------------------------------
-__global__ void k_decomposition(GridDims d, const int8_t *__restrict__ m, uint8_t *__restrict__ info)
+__device__ __forceinline__ int chunk_of(long long c, long long ps, long long rem)
 {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    const long long N = (long long)d.ni * d.nj;
-    if (c >= N) return;
-    const int i = c / d.nj, j = c - i * d.nj;
-    const int8_t mim = mat_at(m, d, i - 1, j), mip = mat_at(m, d, i + 1, j);
-    const int8_t mjm = mat_at(m, d, i, j - 1), mjp = mat_at(m, d, i, j + 1);
-    const int nsc = !t_solid(mim) + !t_solid(mip) + !t_solid(mjm) + !t_solid(mjp);
-    uint8_t b = (uint8_t)(nsc << 4);
-    if (t_fluid(m[c])) {
-        b |= 0x80;
-        if (t_fluid(mim) && c - d.nj >= 0) b |= 1;
-        if (t_fluid(mip) && c + d.nj < N) b |= 2;
-        if (t_fluid(mjm) && c - 1 >= 0) b |= 4;
-        if (t_fluid(mjp) && c + 1 < N) b |= 8;
-    }
-    info[c] = b;
+    // ThreadPool::splitRange: the first `rem` chunks hold ps + 1 cells
+    const long long big = rem * (ps + 1);
+    return (int)(c < big ? c / (ps + 1) : rem + (c - big) / ps);
 }
 
-void launch_decomposition(const GridDims &d, const Grids &G, cudaStream_t st)
+__global__ void k_decomposition(GridDims d, const int8_t *__restrict__ m, uint8_t *__restrict__ info,
+                                int *__restrict__ chunk_last, int nchunks, long long ps,
+                                long long rem, int *__restrict__ wrap)
 {
-    k_decomposition<<<nblk((long long)d.ni * d.nj, kThreads), kThreads, 0, st>>>(d, G.material,
-                                                                                G.cell_info);
+    __shared__ int last_sm[8];
+    __shared__ int k0_sm;
+    const long long N = (long long)d.ni * d.nj;
+    const long long blo = (long long)blockIdx.x * blockDim.x;
+    const long long bhi = (blo + blockDim.x < N ? blo + blockDim.x : N) - 1;
+    if (threadIdx.x == 0) k0_sm = chunk_of(blo, ps, rem);
+    if (threadIdx.x < 8) last_sm[threadIdx.x] = -1;
+    __syncthreads();
+    const int k0 = k0_sm;
+    const bool few = chunk_of(bhi, ps, rem) - k0 < 8;
+    const long long c = blo + threadIdx.x;
+    if (c < N) {
+        const int i = (int)(c / d.nj), j = (int)(c - (long long)i * d.nj);
+        const int8_t mim = mat_at(m, d, i - 1, j), mip = mat_at(m, d, i + 1, j);
+        const int8_t mjm = mat_at(m, d, i, j - 1), mjp = mat_at(m, d, i, j + 1);
+        const int nsc = !t_solid(mim) + !t_solid(mip) + !t_solid(mjm) + !t_solid(mjp);
+        uint8_t b = (uint8_t)(nsc << 4);
+        if (t_fluid(m[c])) {
+            b |= 0x80;
+            if (t_fluid(mim) && c - d.nj >= 0) b |= 1;
+            if (t_fluid(mip) && c + d.nj < N) b |= 2;
+            if (t_fluid(mjm) && c - 1 >= 0) b |= 4;
+            if (t_fluid(mjp) && c + 1 < N) b |= 8;
+            if (j == 0 || j == d.nj - 1) atomicOr(wrap, 1);
+            const int k = chunk_of(c, ps, rem);
+            if (few) atomicMax(&last_sm[k - k0], (int)c);
+            else atomicMax(&chunk_last[k], (int)c);
+        }
+        info[c] = b;
+    }
+    __syncthreads();
+    if (few && threadIdx.x < 8 && last_sm[threadIdx.x] >= 0 && k0 + (int)threadIdx.x < nchunks)
+        atomicMax(&chunk_last[k0 + threadIdx.x], last_sm[threadIdx.x]);
+}
+
+void launch_decomposition(const GridDims &d, const Grids &G, int *chunk_last, int nchunks,
+                          long long ps, long long rem, Scalars *sc, cudaStream_t st)
+{
+    cudaMemsetAsync(chunk_last, 0xff, (size_t)nchunks * sizeof(int), st);
+    cudaMemsetAsync(&sc->wrap_units, 0, sizeof(int), st);
+    k_decomposition<<<nblk((long long)d.ni * d.nj, kThreads), kThreads, 0, st>>>(
+        d, G.material, G.cell_info, chunk_last, nchunks, ps, rem, &sc->wrap_units);
 }
 
 // ---------------------------------------------------------------------------
@@ -411,6 +440,61 @@ __device__ __forceinline__ bool bfs_touches(const int *mark, int r, int q, int k
     return false;
 }
 
+// Advance layers k0+1 .. k0+H of the breadth-first extrapolation inside a
+// loaded tile.  The frontier of each layer is kept as a list in shared memory:
+// cells of layer k are the unmarked neighbours of layer k-1 cells (claimed
+// with a compare-and-swap, so each is listed once); their values are then
+// computed from neighbours of smaller layers, in the reference's neighbour
+// order.  The set of cells per layer, hence every value, is deterministic.
+// `minus_one` selects the level-set form (average - 1).
+template <int H>
+__device__ __forceinline__ void bfs_layers(BfsTile<H> &t, short *fa, short *fb, int *cnt, int k0,
+                                           bool minus_one)
+{
+    constexpr int W = BfsTile<H>::W;
+    if (threadIdx.x == 0) cnt[0] = 0;
+    __syncthreads();
+    for (int e = threadIdx.x; e < W * W; e += blockDim.x)
+        if (t.mark[e] == k0) fa[atomicAdd(&cnt[0], 1)] = (short)e;
+    __syncthreads();
+    short *cur = fa, *nxt = fb;
+    int ncur = cnt[0];
+    for (int k = k0 + 1; k <= k0 + H; k++) {
+        if (ncur == 0) break;
+        if (threadIdx.x == 0) cnt[1] = 0;
+        __syncthreads();
+        for (int f = threadIdx.x; f < ncur; f += blockDim.x) {
+            const int e = cur[f];
+            const int r = e / W, q = e - r * W;
+#pragma unroll
+            for (int io = -1; io <= 1; io++)
+#pragma unroll
+                for (int jo = -1; jo <= 1; jo++) {
+                    if (io == 0 && jo == 0) continue;
+                    const int rr = r + io, qq = q + jo;
+                    if (rr < 0 || rr >= W || qq < 0 || qq >= W) continue;
+                    const int n = rr * W + qq;
+                    if (t.mark[n] == kMarkInf && atomicCAS(&t.mark[n], kMarkInf, k) == kMarkInf)
+                        nxt[atomicAdd(&cnt[1], 1)] = (short)n;
+                }
+        }
+        __syncthreads();
+        const int nnext = cnt[1];
+        for (int f = threadIdx.x; f < nnext; f += blockDim.x) {
+            const int e = nxt[f];
+            const int r = e / W, q = e - r * W;
+            int count;
+            const double avg = bfs_avg<W>(t.mark, t.val, r, q, k, count);
+            t.val[e] = minus_one ? (float)(avg / count - 1.f) : (float)(avg / count);
+        }
+        __syncthreads();
+        short *tmp = cur;
+        cur = nxt;
+        nxt = tmp;
+        ncur = nnext;
+    }
+}
+
 // Velocity extrapolation, breadthFirstExtrapolate(grid, flags, 10, ...):
 // layers 1..11 (a layer-k cell discovers layer k+1 while k <= 10).
 // With `save_gravity` the output also performs the two steps that follow the
@@ -423,6 +507,9 @@ __global__ void __launch_bounds__(1024) k_vel_extrap(GridDims d, Grids G, float 
                                                     int save_gravity)
 {
     __shared__ BfsTile<kVelH> t;
+    __shared__ short fa[BfsTile<kVelH>::W * BfsTile<kVelH>::W];
+    __shared__ short fb[BfsTile<kVelH>::W * BfsTile<kVelH>::W];
+    __shared__ int cnt[2];
     constexpr int W = BfsTile<kVelH>::W;
     const bool isV = blockIdx.z == 1;
     const int si = isV ? d.ni : d.ni + 1, sj = isV ? d.nj + 1 : d.nj;
@@ -444,22 +531,15 @@ __global__ void __launch_bounds__(1024) k_vel_extrap(GridDims d, Grids G, float 
             t.val[e] = g[idx];
         }
     }
-    __syncthreads();
-    for (int k = 1; k <= kVelH; k++) {
-        for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
-            const int r = e / W, q = e - r * W;
-            if (t.mark[e] == kMarkInf && bfs_touches<W>(t.mark, r, q, k - 1)) t.mark[e] = k;
-        }
-        __syncthreads();
-        for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
-            if (t.mark[e] != k) continue;
-            const int r = e / W, q = e - r * W;
-            int count;
-            const double avg = bfs_avg<W>(t.mark, t.val, r, q, k, count);
-            t.val[e] = (float)(avg / count);
-        }
-        __syncthreads();
+    bool has_seed = false, has_inf = false;
+    for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
+        has_seed |= t.mark[e] == 0;
+        has_inf |= t.mark[e] == kMarkInf;
     }
+    // a tile whose loaded region lacks either seeds or unknown cells assigns
+    // nothing and only copies its interior through
+    const bool work = __syncthreads_or(has_seed) && __syncthreads_or(has_inf);
+    if (work) bfs_layers<kVelH>(t, fa, fb, cnt, 0, false);
     const float factor = (float)((double)sc->dt / dx);
     const float add = factor * (isV ? gJ : gI);
     for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
@@ -494,25 +574,65 @@ void launch_vel_extrapolate(const GridDims &d, Grids &G, const SceneParams &sp,
 
 // Level set inside extrapolation (flipsolver2d.cpp:1433-1494): seeds are
 // cells with sdf > 0, depth unbounded, value = average - 1.  Pass p advances
-// layers p*H+1 .. (p+1)*H; markers and values ping-pong between two buffers,
-// and newly assigned values also go straight to the fluid SDF (which no pass
-// reads).  A pass that finds the previous pass assigned nothing returns.
-constexpr int kLsH = 16;
+// layers p*H+1 .. (p+1)*H.  Each cell's (marker, value) pair lives in one
+// 64-bit word that is read and written whole, so a concurrently finished
+// neighbour tile is seen either untouched or final -- both consistent with
+// the exact layered solution, which is all a tile needs from its halo.  Only
+// newly assigned cells are written (and copied to the fluid SDF).  A tile
+// works in pass p only if a tile within one tile of it assigned cells in pass
+// p-1: the frontier of layer p*H is otherwise out of its reach.  Once a pass
+// assigns nothing, the remaining passes return immediately.
+constexpr int kLsH = 15; // keeps the tile's static shared memory under 48 KiB
+
+__device__ __forceinline__ unsigned long long ls_pack(int mark, float v)
+{
+    return ((unsigned long long)(unsigned)mark << 32) | (unsigned long long)__float_as_uint(v);
+}
+
+__global__ void k_levelset_init(GridDims d, const float *__restrict__ sdf,
+                                unsigned long long *__restrict__ cells, uint8_t *__restrict__ act,
+                                int ntiles, int *__restrict__ active, int passes)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long N = (long long)d.ni * d.nj;
+    if (c < N) {
+        const float v = sdf[c];
+        cells[c] = ls_pack(v > 0.f ? 0 : kMarkInf, v);
+    }
+    if (c < 3LL * ntiles) act[c] = 0;
+    if (c < passes) active[c] = 0;
+}
 
 __global__ void __launch_bounds__(1024) k_levelset_pass(GridDims d, float *__restrict__ sdf,
-                                                       const int *__restrict__ mark_in,
-                                                       const float *__restrict__ val_in,
-                                                       int *__restrict__ mark_out,
-                                                       float *__restrict__ val_out,
+                                                       unsigned long long *__restrict__ cells,
+                                                       uint8_t *__restrict__ act,
                                                        int *__restrict__ active, int pass)
 {
     __shared__ BfsTile<kLsH> t;
-    __shared__ int any_new;
+    __shared__ short fa[BfsTile<kLsH>::W * BfsTile<kLsH>::W];
+    __shared__ short fb[BfsTile<kLsH>::W * BfsTile<kLsH>::W];
+    __shared__ int cnt[2];
     constexpr int W = BfsTile<kLsH>::W;
-    if (pass > 0 && active[pass - 1] == 0) return;
+    if (pass > 0 && ((volatile int *)active)[pass - 1] == 0) return;
     const int si = d.ni, sj = d.nj;
+    const int tiles_i = gridDim.y, tiles_j = gridDim.x;
+    const int ntiles = tiles_i * tiles_j;
+    const int tile = blockIdx.y * tiles_j + blockIdx.x;
+    uint8_t *act_prev = act + (size_t)((pass + 2) % 3) * ntiles;
+    uint8_t *act_cur = act + (size_t)(pass % 3) * ntiles;
+    uint8_t *act_next = act + (size_t)((pass + 1) % 3) * ntiles;
+    if (threadIdx.x == 0) act_next[tile] = 0;
+    if (pass > 0) {
+        bool near = false;
+        for (int a = -1; a <= 1; a++)
+            for (int b = -1; b <= 1; b++) {
+                const int ti = (int)blockIdx.y + a, tj = (int)blockIdx.x + b;
+                if (ti >= 0 && ti < tiles_i && tj >= 0 && tj < tiles_j)
+                    near |= ((volatile uint8_t *)act_prev)[ti * tiles_j + tj] != 0;
+            }
+        if (!near) return;
+    }
     const int ti0 = blockIdx.y * kTile, tj0 = blockIdx.x * kTile;
-    if (threadIdx.x == 0) any_new = 0;
     for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
         const int r = e / W, q = e - r * W;
         const int gi = ti0 - kLsH + r, gj = tj0 - kLsH + q;
@@ -520,57 +640,32 @@ __global__ void __launch_bounds__(1024) k_levelset_pass(GridDims d, float *__res
             t.mark[e] = kMarkOut;
             t.val[e] = 0.f;
         } else {
-            const size_t idx = (size_t)gi * sj + gj;
-            if (pass == 0) {
-                const float v = sdf[idx];
-                t.mark[e] = v > 0.f ? 0 : kMarkInf;
-                t.val[e] = v;
-            } else {
-                t.mark[e] = mark_in[idx];
-                t.val[e] = val_in[idx];
-            }
+            const unsigned long long w = ((volatile unsigned long long *)cells)[(size_t)gi * sj + gj];
+            t.mark[e] = (int)(w >> 32);
+            t.val[e] = __uint_as_float((unsigned)(w & 0xffffffffu));
         }
     }
     __syncthreads();
     const int k0 = pass * kLsH;
+    bfs_layers<kLsH>(t, fa, fb, cnt, k0, true);
     bool assigned = false;
-    for (int k = k0 + 1; k <= k0 + kLsH; k++) {
-        for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
-            const int r = e / W, q = e - r * W;
-            if (t.mark[e] == kMarkInf && bfs_touches<W>(t.mark, r, q, k - 1)) t.mark[e] = k;
-        }
-        __syncthreads();
-        for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
-            if (t.mark[e] != k) continue;
-            const int r = e / W, q = e - r * W;
-            int count;
-            const double avg = bfs_avg<W>(t.mark, t.val, r, q, k, count);
-            t.val[e] = (float)(avg / count - 1.f);
-        }
-        __syncthreads();
-    }
     for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
         const int r = e / kTile + kLsH, q = e % kTile + kLsH;
         const int gi = ti0 - kLsH + r, gj = tj0 - kLsH + q;
         if (gi >= si || gj >= sj) continue;
-        const size_t idx = (size_t)gi * sj + gj;
         const int mk = t.mark[r * W + q];
-        mark_out[idx] = mk;
-        val_out[idx] = t.val[r * W + q];
         if (mk > k0 && mk != kMarkInf) {
-            sdf[idx] = t.val[r * W + q];
+            const size_t idx = (size_t)gi * sj + gj;
+            const float v = t.val[r * W + q];
+            cells[idx] = ls_pack(mk, v);
+            sdf[idx] = v;
             assigned = true;
         }
     }
-    if (assigned) any_new = 1;
-    __syncthreads();
-    if (threadIdx.x == 0 && any_new) atomicExch(&active[pass], 1);
-}
-
-__global__ void k_zero_int(int *p, int n)
-{
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < n) p[k] = 0;
+    if (__syncthreads_or(assigned) && threadIdx.x == 0) {
+        act_cur[tile] = 1;
+        atomicExch(&active[pass], 1);
+    }
 }
 
 int levelset_max_passes(const GridDims &d)
@@ -582,15 +677,18 @@ int levelset_max_passes(const GridDims &d)
 void launch_levelset(const GridDims &d, Grids &G, cudaStream_t st)
 {
     const int passes = levelset_max_passes(d);
-    k_zero_int<<<nblk(passes, kThreads), kThreads, 0, st>>>(G.levelset_active, passes);
     dim3 grid(nblk(d.nj, kTile), nblk(d.ni, kTile));
-    int *mi = G.levelset_marker, *mo = G.levelset_marker2;
-    float *vi = G.levelset_val2 + (size_t)d.ni * d.nj, *vo = G.levelset_val2;
-    for (int p = 0; p < passes; p++) {
-        k_levelset_pass<<<grid, 1024, 0, st>>>(d, G.fluid_sdf, mi, vi, mo, vo, G.levelset_active, p);
-        int *ti = mi; mi = mo; mo = ti;
-        float *tf = vi; vi = vo; vo = tf;
-    }
+    const int ntiles = grid.x * grid.y;
+    const long long n = (long long)d.ni * d.nj;
+    long long init_n = n > 3LL * ntiles ? n : 3LL * ntiles;
+    if (init_n < passes) init_n = passes;
+    unsigned long long *cells = reinterpret_cast<unsigned long long *>(G.levelset_cells);
+    k_levelset_init<<<nblk(init_n, kThreads), kThreads, 0, st>>>(d, G.fluid_sdf, cells,
+                                                               G.levelset_act, ntiles,
+                                                               G.levelset_active, passes);
+    for (int p = 0; p < passes; p++)
+        k_levelset_pass<<<grid, 1024, 0, st>>>(d, G.fluid_sdf, cells, G.levelset_act,
+                                                G.levelset_active, p);
 }
 
 // ---------------------------------------------------------------------------

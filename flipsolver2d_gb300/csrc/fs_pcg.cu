@@ -107,6 +107,70 @@ __device__ __forceinline__ double grid_sum(const double *partials, int nblocks, 
     return r;
 }
 
+// Barrier that also reduces one or two FP64 values per block.  Every block
+// publishes its partials and arrives; the last block to arrive sums all
+// partials with its whole thread block in a fixed order (so every run and
+// every block sees the same totals), optionally evaluates the reference's
+// chunked max-abs residual test, publishes the results in the barrier
+// record and releases the others.  Waits are bounded like grid_barrier.
+template <typename R>
+__device__ __forceinline__ bool grid_reduce(GridBarrier *gb, double *partials, unsigned nblocks,
+                                            double v0, double v1, int nvals, int *status,
+                                            double *sm, double out[3], R last_block_extra)
+{
+    __shared__ int s_last;
+    __shared__ unsigned s_gen;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = v0;
+        if (nvals > 1) partials[nblocks + blockIdx.x] = v1;
+        cuda::atomic_ref<unsigned, cuda::thread_scope_device> gen(gb->gen);
+        cuda::atomic_ref<unsigned, cuda::thread_scope_device> cnt(gb->count);
+        s_gen = gen.load(cuda::memory_order_acquire);
+        __threadfence();
+        const unsigned arrived = cnt.fetch_add(1u, cuda::memory_order_acq_rel);
+        s_last = arrived == nblocks - 1;
+    }
+    __syncthreads();
+    if (s_last) {
+        __threadfence();
+        double a = 0.0, b = 0.0;
+        for (unsigned k = threadIdx.x; k < nblocks; k += blockDim.x) {
+            a += ((volatile double *)partials)[k];
+            if (nvals > 1) b += ((volatile double *)partials)[nblocks + k];
+        }
+        a = block_sum(a, sm);
+        if (nvals > 1) b = block_sum(b, sm);
+        const double extra = last_block_extra();
+        if (threadIdx.x == 0) {
+            gb->result[0] = a;
+            gb->result[1] = b;
+            gb->result[2] = extra;
+            __threadfence();
+            cuda::atomic_ref<unsigned, cuda::thread_scope_device> gen(gb->gen);
+            cuda::atomic_ref<unsigned, cuda::thread_scope_device> cnt(gb->count);
+            cnt.store(0u, cuda::memory_order_relaxed);
+            gen.fetch_add(1u, cuda::memory_order_release);
+        }
+    } else if (threadIdx.x == 0) {
+        cuda::atomic_ref<unsigned, cuda::thread_scope_device> gen(gb->gen);
+        long long spins = 0;
+        while (gen.load(cuda::memory_order_acquire) == s_gen) {
+            if (++spins > kBarrierSpinLimit) {
+                atomicExch(status, 1);
+                break;
+            }
+            __nanosleep(32);
+        }
+    }
+    __syncthreads();
+    if (*((volatile int *)status) != 0) return false;
+    out[0] = ((volatile double *)gb->result)[0];
+    out[1] = ((volatile double *)gb->result)[1];
+    out[2] = ((volatile double *)gb->result)[2];
+    return true;
+}
+
 // ---- element arithmetic --------------------------------------------------
 template <typename T> struct Ops;
 
@@ -202,6 +266,8 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgArgs<T> a)
 {
     __shared__ double sm[40];
     __shared__ double bcast[4];
+    if (a.mode == 1 && *a.wrap_flag == 0) return;
+    if (a.mode == 2 && *a.wrap_flag != 0) return;
     const long long N = a.N;
     const int nj = a.nj;
     const int G = gridDim.x;
@@ -343,65 +409,489 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgArgs<T> a)
     if (blockIdx.x == 0 && threadIdx.x == 0) *a.iters_out = result;
 }
 
-// last unit row of each splitRange chunk (or -1); one warp per chunk
-__global__ void k_chunk_last_unit(const uint8_t *__restrict__ info, const int *__restrict__ chunk_end,
-                                  int nchunks, int *__restrict__ last)
+// ---------------------------------------------------------------------------
+// Shared-memory tiled FP32 kernel.  The grid is cut into tiles of TI x TJ
+// cells sized at launch so that each block owns about one tile per sweep
+// (large tiles keep many loads in flight and amortise the halo).  A sweep
+// stages its inputs with a halo of two cells, computes the recomputed
+// intermediate (M r, then s; or A s, then r) once per halo-1 cell in shared
+// memory and the final stencil on the tile.  Neighbours are the 2-D
+// neighbours, equal to the reference's linear-index neighbours except across
+// the j = 0 / j = NJ-1 edges; a decomposition flag routes grids with unit rows
+// on those edges to the linear kernel above.
+// ---------------------------------------------------------------------------
+constexpr int kTiledThreads = 1024;
+constexpr int kMaxTileCells = 12288;
+
+struct TileShape {
+    int ti, tj; // tile rows / columns
+};
+
+__device__ __forceinline__ float ipp_tile(const float *__restrict__ R, const uint8_t *__restrict__ I,
+                                          int c2, int w2, const float inv[5])
 {
-    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (w >= nchunks) return;
-    const long long start = w == 0 ? 0 : chunk_end[w - 1];
-    long long hiIdx = chunk_end[w] - 1;
-    long long found = -1;
-    while (hiIdx >= start) {
-        const long long k = hiIdx - lane;
-        const bool u = k >= start && (info[k] & 0x80);
-        const unsigned bal = __ballot_sync(0xffffffffu, u);
-        if (bal) {
-            found = hiIdx - (__ffs(bal) - 1);
+    const uint8_t ic = I[c2];
+    const float rc = R[c2];
+    if (!(ic & 0x80)) return rc;
+    const float iNeg = inv[(I[c2 - w2] >> 4) & 7];
+    const float iPos = inv[(I[c2 + w2] >> 4) & 7];
+    const float jNeg = inv[(I[c2 - 1] >> 4) & 7];
+    const float jPos = inv[(I[c2 + 1] >> 4) & 7];
+    const float diag = (1.f + iNeg * iNeg) + jNeg * jNeg;
+    float acc = diag * rc;
+    acc = fmaf(jNeg, R[c2 - 1], acc);
+    acc = fmaf(jPos, R[c2 + 1], acc);
+    acc = fmaf(iNeg, R[c2 - w2], acc);
+    acc = fmaf(iPos, R[c2 + w2], acc);
+    return acc;
+}
+
+// A row from array S (row stride `stride`) at index c
+__device__ __forceinline__ float a_tile(const float *__restrict__ S, uint8_t ic, int c, int stride,
+                                        float scale)
+{
+    const float sc_ = S[c];
+    if (!(ic & 0x80)) return sc_;
+    float nb = 0.f;
+    if (ic & 1) nb += S[c - stride];
+    if (ic & 2) nb += S[c + stride];
+    if (ic & 4) nb += S[c - 1];
+    if (ic & 8) nb += S[c + 1];
+    return scale * ((float)((ic >> 4) & 7) * sc_ - nb);
+}
+
+// ---- reductions that keep FP64 arithmetic off the 1024-thread paths --------
+// GB300's FP64 pipe runs at a small fraction of FP32, so a block-wide FP64
+// shuffle tree costs microseconds.  Inside a warp the partial sums travel as
+// compensated FP32 pairs (Knuth's two-sum keeps the rounding error of every
+// addition in the low word, ~48 significant bits); FP64 arithmetic starts at
+// the 32 per-warp pairs (one warp) and at the per-block partials (one warp).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+    s = a + b;
+    const float bv = s - a;
+    e = (a - (s - bv)) + (b - bv);
+}
+
+// block-wide sum of per-thread FP32 partials; FP64 result in every thread
+__device__ __forceinline__ double block_sum_ff(float v, double *sm)
+{
+    float hi = v, lo = 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float h2 = __shfl_down_sync(0xffffffffu, hi, o);
+        const float l2 = __shfl_down_sync(0xffffffffu, lo, o);
+        float s, e;
+        two_sum(hi, h2, s, e);
+        hi = s;
+        lo = lo + l2 + e;
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) sm[w] = (double)hi + (double)lo;
+    __syncthreads();
+    if (w == 0) {
+        double x = lane < (int)(blockDim.x >> 5) ? sm[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) sm[32] = x;
+    }
+    __syncthreads();
+    const double r = sm[32];
+    __syncthreads();
+    return r;
+}
+
+// sum of the per-block partials after a barrier, by one warp in a fixed order
+__device__ __forceinline__ double sum_partials_w(const double *partials, int nblocks, double *sm)
+{
+    if (threadIdx.x < 32) {
+        double a = 0.0;
+        for (int k = threadIdx.x; k < nblocks; k += 32) a += ((volatile const double *)partials)[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+        if (threadIdx.x == 0) sm[34] = a;
+    }
+    __syncthreads();
+    const double r = sm[34];
+    __syncthreads();
+    return r;
+}
+
+// Tight-spin grid barrier (bounded like grid_barrier; spins without sleeping
+// first, since a barrier here normally completes within microseconds).
+__device__ __forceinline__ bool grid_sync_fast(GridBarrier *gb, unsigned nblocks, int *status)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *vgen = &gb->gen;
+        const unsigned g = *vgen;
+        __threadfence();
+        const unsigned arrived = atomicAdd(&gb->count, 1u);
+        if (arrived == nblocks - 1) {
+            gb->count = 0;
+            __threadfence();
+            atomicAdd(&gb->gen, 1u);
+        } else {
+            long long spins = 0;
+            while (*vgen == g) {
+                if (++spins > (kBarrierSpinLimit << 4)) {
+                    atomicExch(status, 1);
+                    break;
+                }
+                if (spins > 4096) __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return *((volatile int *)status) == 0;
+}
+
+// sum of the per-block partials after a barrier: one load per thread, then a
+// fixed-order block reduction (identical in every block)
+__device__ __forceinline__ double sum_partials(const double *partials, int nblocks, double *sm)
+{
+    double v = 0.0;
+    for (int k = threadIdx.x; k < nblocks; k += blockDim.x) v += ((volatile const double *)partials)[k];
+    return block_sum(v, sm);
+}
+
+// Batched halo load: every thread issues all of its global loads before any
+// shared-memory store, so up to kLoadBatch loads are in flight per thread.
+constexpr int kLoadBatch = 16;
+
+template <typename V>
+__device__ __forceinline__ void load_region(V *__restrict__ dst, const V *__restrict__ src, int ti0,
+                                            int tj0, int halo, int h, int w, int NI, int NJ)
+{
+    const int n = h * w;
+    for (int base = 0; base < n; base += kLoadBatch * (int)blockDim.x) {
+        V v[kLoadBatch];
+#pragma unroll
+        for (int k = 0; k < kLoadBatch; k++) {
+            const int e = base + k * (int)blockDim.x + (int)threadIdx.x;
+            v[k] = (V)0;
+            if (e < n) {
+                const int gi = ti0 - halo + e / w, gj = tj0 - halo + e % w;
+                if (gi >= 0 && gi < NI && gj >= 0 && gj < NJ) v[k] = src[(size_t)gi * NJ + gj];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kLoadBatch; k++) {
+            const int e = base + k * (int)blockDim.x + (int)threadIdx.x;
+            if (e < n) dst[e] = v[k];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kTiledThreads) k_pcg_tiled(PcgArgs<float> a, TileShape ts)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ double sm[40];
+    __shared__ double s_err;
+    if (a.mode == 1 && *a.wrap_flag == 0) return;
+    if (a.mode == 2 && *a.wrap_flag != 0) return;
+    const int NI = a.ni, NJ = a.nj;
+    const long long N = a.N;
+    const int G = gridDim.x;
+    const int TI = ts.ti, TJ = ts.tj;
+    const int W2 = TJ + 4, H2 = TI + 4, W1 = TJ + 2, H1 = TI + 2;
+    float *A2 = reinterpret_cast<float *>(smem_raw);
+    float *B1 = A2 + H2 * W2;
+    uint8_t *I2 = reinterpret_cast<uint8_t *>(B1 + H1 * W1);
+    const int tiles_j = (NJ + TJ - 1) / TJ, tiles_i = (NI + TI - 1) / TI;
+    const int ntiles = tiles_i * tiles_j;
+    double *pA = a.partials, *pB = a.partials + G, *pC = a.partials + 2 * G;
+    double *chunk_val = a.chunk_val;
+
+    const double scale_d = (double)a.sc->dt / (a.density * a.dx * a.dx);
+    const float scale = (float)scale_d;
+    float inv[5];
+    inv[0] = 0.f; // only outside the grid
+#pragma unroll
+    for (int n = 1; n < 5; n++) inv[n] = (float)(1.0 / (n * scale_d));
+
+    // phase 0 (contiguous ranges): x = 0, r = s = b, sigma = b.b, zero test
+    const long long per = ((N + G - 1) / G + blockDim.x - 1) / blockDim.x * blockDim.x;
+    const long long lo = (long long)blockIdx.x * per;
+    const long long hi = lo + per < N ? lo + per : N;
+    float bb = 0.f;
+    int nz = 0;
+    for (long long c = lo + threadIdx.x; c < hi; c += blockDim.x) {
+        const float bv = a.b[c];
+        a.x[c] = 0.f;
+        a.r0[c] = bv;
+        a.s0[c] = bv;
+        bb = fmaf(bv, bv, bb);
+        nz |= fabsf(bv) > 1.0e-15f;
+    }
+    {
+        const double part = block_sum_ff(bb, sm);
+        const int anynz = __syncthreads_or(nz);
+        if (threadIdx.x == 0) {
+            pA[blockIdx.x] = part;
+            pC[blockIdx.x] = anynz ? 1.0 : 0.0;
+        }
+    }
+    if (!grid_sync_fast(a.bar, G, a.status)) return;
+    double sigma = sum_partials_w(pA, G, sm);
+    if (sum_partials_w(pC, G, sm) == 0.0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) *a.iters_out = 0;
+        return;
+    }
+
+    double beta = 0.0;
+    int result = a.iter_limit;
+    for (int it = 0; it < a.iter_limit; it++) {
+        float *rc = (it & 1) ? a.r1 : a.r0;
+        float *rn = (it & 1) ? a.r0 : a.r1;
+        float *scur = (it & 1) ? a.s1 : a.s0;
+        const float *sprev = (it & 1) ? a.s0 : a.s1;
+        const bool first = it == 0;
+        const float fb = (float)beta;
+
+        // ---- sweep 1: s = M r + beta s_prev on the halo, q = A s, q.s ----
+        float qs = 0.f;
+        for (int t = blockIdx.x; t < ntiles; t += G) {
+            const int ti0 = (t / tiles_j) * TI, tj0 = (t % tiles_j) * TJ;
+            load_region<uint8_t>(I2, a.info, ti0, tj0, 2, H2, W2, NI, NJ);
+            if (!first) load_region<float>(A2, rc, ti0, tj0, 2, H2, W2, NI, NJ);
+            load_region<float>(B1, first ? scur : sprev, ti0, tj0, 1, H1, W1, NI, NJ);
+            __syncthreads();
+            if (!first) {
+                for (int e = threadIdx.x; e < H1 * W1; e += blockDim.x) {
+                    const int r = e / W1, q = e - r * W1;
+                    const int c2 = (r + 1) * W2 + (q + 1);
+                    B1[e] = fmaf(B1[e], fb, ipp_tile(A2, I2, c2, W2, inv));
+                }
+                __syncthreads();
+            }
+            for (int e = threadIdx.x; e < TI * TJ; e += blockDim.x) {
+                const int r = e / TJ, q = e - r * TJ;
+                const int gi = ti0 + r, gj = tj0 + q;
+                if (gi >= NI || gj >= NJ) continue;
+                const int c1 = (r + 1) * W1 + (q + 1);
+                const uint8_t ic = I2[(r + 2) * W2 + (q + 2)];
+                const float s_c = B1[c1];
+                const float qv = a_tile(B1, ic, c1, W1, scale);
+                qs = fmaf(qv, s_c, qs);
+                if (!first) scur[(size_t)gi * NJ + gj] = s_c;
+            }
+            __syncthreads();
+        }
+        {
+            const double part = block_sum_ff(qs, sm);
+            if (threadIdx.x == 0) pA[blockIdx.x] = part;
+        }
+        if (!grid_sync_fast(a.bar, G, a.status)) return;
+        const double alpha = sigma / (sum_partials_w(pA, G, sm) + 1e-8);
+        const float fa = (float)alpha;
+
+        // ---- sweep 2: r' = r - alpha A s on the halo, z = M r', x += alpha s
+        float zr = 0.f;
+        for (int t = blockIdx.x; t < ntiles; t += G) {
+            const int ti0 = (t / tiles_j) * TI, tj0 = (t % tiles_j) * TJ;
+            load_region<uint8_t>(I2, a.info, ti0, tj0, 2, H2, W2, NI, NJ);
+            load_region<float>(A2, scur, ti0, tj0, 2, H2, W2, NI, NJ);
+            load_region<float>(B1, rc, ti0, tj0, 1, H1, W1, NI, NJ);
+            __syncthreads();
+            for (int e = threadIdx.x; e < H1 * W1; e += blockDim.x) {
+                const int r = e / W1, q = e - r * W1;
+                const int c2 = (r + 1) * W2 + (q + 1);
+                B1[e] = fmaf(-a_tile(A2, I2[c2], c2, W2, scale), fa, B1[e]);
+            }
+            __syncthreads();
+            for (int e = threadIdx.x; e < TI * TJ; e += blockDim.x) {
+                const int r = e / TJ, q = e - r * TJ;
+                const int gi = ti0 + r, gj = tj0 + q;
+                if (gi >= NI || gj >= NJ) continue;
+                const int c1 = (r + 1) * W1 + (q + 1);
+                const int c2 = (r + 2) * W2 + (q + 2);
+                const uint8_t ic = I2[c2];
+                const float r_c = B1[c1];
+                float z = r_c;
+                if (ic & 0x80) {
+                    const float iNeg = inv[(I2[c2 - W2] >> 4) & 7];
+                    const float iPos = inv[(I2[c2 + W2] >> 4) & 7];
+                    const float jNeg = inv[(I2[c2 - 1] >> 4) & 7];
+                    const float jPos = inv[(I2[c2 + 1] >> 4) & 7];
+                    const float diag = (1.f + iNeg * iNeg) + jNeg * jNeg;
+                    z = diag * r_c;
+                    z = fmaf(jNeg, B1[c1 - 1], z);
+                    z = fmaf(jPos, B1[c1 + 1], z);
+                    z = fmaf(iNeg, B1[c1 - W1], z);
+                    z = fmaf(iPos, B1[c1 + W1], z);
+                }
+                zr = fmaf(z, r_c, zr);
+                const size_t g = (size_t)gi * NJ + gj;
+                a.x[g] = fmaf(A2[c2], fa, a.x[g]);
+                rn[g] = r_c;
+            }
+            __syncthreads();
+        }
+        // VOps::maxAbs (vmath.cpp:100-136): each chunk's value is |r| at the
+        // chunk's last unit row, read here by the block that wrote it; -1
+        // marks the rare case r == 0 there, resolved after the barrier.
+        for (int k = threadIdx.x; k < a.nchunks; k += blockDim.x) {
+            const int idx = a.chunk_last_unit[k];
+            if (idx < 0) continue;
+            const int gi = idx / NJ, gj = idx - gi * NJ;
+            const int owner = ((gi / TI) * tiles_j + gj / TJ) % G;
+            if (owner != (int)blockIdx.x) continue;
+            const float v = rn[idx];
+            chunk_val[k] = v != 0.f ? fabs((double)v) : -1.0;
+        }
+        {
+            const double part = block_sum_ff(zr, sm);
+            if (threadIdx.x == 0) pB[blockIdx.x] = part;
+        }
+        if (!grid_sync_fast(a.bar, G, a.status)) return;
+        if (threadIdx.x < 32) {
+            double m = 0.0;
+            for (int k = threadIdx.x; k < a.nchunks; k += 32) {
+                const long long start = k == 0 ? 0 : a.chunk_end[k - 1];
+                const int last = a.chunk_last_unit[k];
+                double v;
+                if (last < 0) {
+                    v = DBL_MIN;
+                } else {
+                    v = ((volatile double *)chunk_val)[k];
+                    if (v < 0.0) {
+                        long long idx = last - 1;
+                        while (idx >= start && ((volatile float *)rn)[idx] == 0.f) idx--;
+                        v = idx >= start ? fabs((double)((volatile float *)rn)[idx]) : DBL_MIN;
+                    }
+                }
+                if (v > m) m = v;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double t = __shfl_down_sync(0xffffffffu, m, o);
+                if (t > m) m = t;
+            }
+            if (threadIdx.x == 0) s_err = m;
+        }
+        __syncthreads();
+        const double err = s_err;
+        const double newSigma = sum_partials_w(pB, G, sm);
+        if (err <= a.tol) {
+            result = it;
             break;
         }
-        hiIdx -= 32;
+        beta = newSigma / sigma;
+        sigma = newSigma;
     }
-    if (lane == 0) last[w] = (int)found;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.iters_out = result;
 }
 
-void launch_chunk_last_unit(const uint8_t *info, const int *chunk_end, int nchunks, int *last,
-                            cudaStream_t st)
+static size_t tiled_smem(TileShape ts)
 {
-    const int threads = 256;
-    const int blocks = (nchunks * 32 + threads - 1) / threads;
-    k_chunk_last_unit<<<blocks, threads, 0, st>>>(info, chunk_end, nchunks, last);
+    return (size_t)(ts.ti + 4) * (ts.tj + 4) * 4 + (size_t)(ts.ti + 2) * (ts.tj + 2) * 4 +
+           (size_t)(ts.ti + 4) * (ts.tj + 4) + 16;
 }
 
+// Tiles of up to 128 columns; rows chosen so that the tile count is at most
+// `blocks` x k for the smallest k whose tiles fit in shared memory, i.e. every
+// block owns k tiles per sweep (k = 1 whenever the grid allows).
+static TileShape tile_shape(int ni, int nj, int blocks)
+{
+    TileShape ts;
+    ts.tj = nj < 128 ? ((nj + 31) / 32) * 32 : 128;
+    const long long tiles_j = (nj + ts.tj - 1) / ts.tj;
+    const long long cap = kMaxTileCells / ts.tj;
+    for (long long k = 1;; k++) {
+        long long max_ti = (long long)blocks * k / tiles_j;
+        if (max_ti < 1) continue;
+        long long ti = (ni + max_ti - 1) / max_ti;
+        // at least 8 rows: thinner tiles would mostly load halo
+        if (ti < 8) ti = ni < 8 ? ni : 8;
+        if (ti <= cap || k > 4096) {
+            ts.ti = (int)(ti < cap ? ti : cap);
+            return ts;
+        }
+    }
+}
+
+static int occupancy_grid(const void *fn, int threads, int max_per_sm)
+{
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, threads, 0);
+    if (per < 1) per = 1;
+    if (per > max_per_sm) per = max_per_sm;
+    return sms * per;
+}
+
+// largest grid any PCG launch may use (sizes the partial-sum buffer)
 template <typename T> int pcg_grid_size(long long N)
 {
-    static int cached = 0;
-    if (!cached) {
-        int dev = 0, sms = 0, per = 0;
+    static int lin = 0, sms = 0;
+    if (!lin) lin = occupancy_grid((const void *)k_pcg<T>, kPcgThreads, 64);
+    if (!sms) {
+        int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pcg<T>, kPcgThreads, 0);
-        cached = sms * (per > 0 ? per : 1);
     }
-    long long want = (N + kPcgThreads * 4 - 1) / (kPcgThreads * 4);
-    if (want < 1) want = 1;
-    return (int)(want < cached ? want : cached);
+    (void)N;
+    return lin > sms ? lin : sms;
 }
 
-template <typename T> cudaError_t launch_pcg(const PcgArgs<T> &a, int grid, cudaStream_t st)
+template <typename T>
+static cudaError_t coop(const void *fn, PcgArgs<T> args, int grid, int threads, cudaStream_t st)
 {
-    PcgArgs<T> args = a;
     void *kargs[] = {&args};
-    cudaMemsetAsync(a.bar, 0, sizeof(GridBarrier), st);
-    return cudaLaunchCooperativeKernel((const void *)k_pcg<T>, dim3(grid), dim3(kPcgThreads),
-                                       kargs, 0, st);
+    cudaError_t e = cudaMemsetAsync(args.bar, 0, sizeof(GridBarrier), st);
+    if (e != cudaSuccess) return e;
+    return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(threads), kargs, 0, st);
+}
+
+template <typename T> cudaError_t launch_pcg(const PcgArgs<T> &a, cudaStream_t st, int *launched)
+{
+    static int lin = 0;
+    if (!lin) lin = occupancy_grid((const void *)k_pcg<T>, kPcgThreads, 64);
+    long long want = (a.N + kPcgThreads * 4 - 1) / (kPcgThreads * 4);
+    int glin = (int)(want < 1 ? 1 : (want < lin ? want : lin));
+    if (sizeof(T) == 8) {
+        PcgArgs<T> b = a;
+        b.mode = 0;
+        *launched = 1;
+        return coop((const void *)k_pcg<T>, b, glin, kPcgThreads, st);
+    }
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const TileShape big{kMaxTileCells / 128, 128};
+        cudaFuncSetAttribute((const void *)k_pcg_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)tiled_smem(big));
+    }
+    const TileShape ts = tile_shape(a.ni, a.nj, sms);
+    const long long ntiles = (long long)((a.ni + ts.ti - 1) / ts.ti) * ((a.nj + ts.tj - 1) / ts.tj);
+    // equal tile counts per block
+    const long long tpb = (ntiles + sms - 1) / sms;
+    const int gtil = (int)((ntiles + tpb - 1) / tpb);
+    PcgArgs<T> b = a;
+    b.mode = 2; // tiled unless a unit row touches the j edges
+    {
+        PcgArgs<float> fa = *reinterpret_cast<PcgArgs<float> *>(&b);
+        TileShape tsv = ts;
+        void *kargs[] = {&fa, &tsv};
+        cudaError_t e = cudaMemsetAsync(fa.bar, 0, sizeof(GridBarrier), st);
+        if (e != cudaSuccess) return e;
+        e = cudaLaunchCooperativeKernel((const void *)k_pcg_tiled, dim3(gtil), dim3(kTiledThreads),
+                                        kargs, tiled_smem(ts), st);
+        if (e != cudaSuccess) return e;
+    }
+    b.mode = 1;
+    *launched = 2;
+    return coop((const void *)k_pcg<T>, b, glin, kPcgThreads, st);
 }
 
 template int pcg_grid_size<float>(long long);
 template int pcg_grid_size<double>(long long);
-template cudaError_t launch_pcg<float>(const PcgArgs<float> &, int, cudaStream_t);
-template cudaError_t launch_pcg<double>(const PcgArgs<double> &, int, cudaStream_t);
-
-int pcg_partials_per_block() { return 4; }
+template cudaError_t launch_pcg<float>(const PcgArgs<float> &, cudaStream_t, int *);
+template cudaError_t launch_pcg<double>(const PcgArgs<double> &, cudaStream_t, int *);
 
 } // namespace fsg

@@ -11,6 +11,7 @@ namespace fsg {
 struct GridBarrier {
     unsigned int count;
     unsigned int gen;
+    double result[4]; // scalars published by the last block to arrive
 };
 
 template <typename T> struct PcgArgs {
@@ -23,6 +24,7 @@ template <typename T> struct PcgArgs {
     double *partials;          // 3 * grid doubles
     const int *chunk_end;      // splitRange chunk ends (exclusive)
     const int *chunk_last_unit;// last unit row per chunk or -1
+    double *chunk_val;         // per chunk |r| at its last unit row (scratch)
     int nchunks;
     const Scalars *sc;         // dt of the substep
     double density, dx;
@@ -31,11 +33,15 @@ template <typename T> struct PcgArgs {
     int *iters_out;
     int *status;               // set to 1 when a barrier wait times out
     GridBarrier *bar;
+    const int *wrap_flag;      // set by the decomposition when a unit row sits on
+                               // the j = 0 or j = NJ-1 edge (linear-index wrap)
+    int mode;                  // 0 run, 1 run only if *wrap_flag, 2 only if !*wrap_flag
 };
 
 template <typename T> int pcg_grid_size(long long N);
-template <typename T> cudaError_t launch_pcg(const PcgArgs<T> &a, int grid, cudaStream_t st);
-void launch_chunk_last_unit(const uint8_t *info, const int *chunk_end, int nchunks, int *last,
-                            cudaStream_t st);
+// Runs the solve: FP32 uses the shared-memory tiled kernel, falling back to
+// the linear-index kernel when a unit row touches the j edges; FP64 always
+// uses the linear-index kernel.  Returns the number of kernels launched.
+template <typename T> cudaError_t launch_pcg(const PcgArgs<T> &a, cudaStream_t st, int *launched);
 
 } // namespace fsg

@@ -75,9 +75,9 @@ struct Grids {
     uint8_t *cell_info = nullptr; // pressure-operator rows frozen at DECOMPOSITION
     float *ufric = nullptr, *vfric = nullptr; // 1 - mean friction, or NaN when not affected
     int *emitter_id = nullptr;
-    int *levelset_marker = nullptr, *levelset_marker2 = nullptr;
-    float *levelset_val2 = nullptr;
-    int *levelset_active = nullptr; // device flag: a pass assigned new markers
+    unsigned long long *levelset_cells = nullptr; // packed (marker, value) per cell
+    uint8_t *levelset_act = nullptr;  // 3 x tiles activity flags (pass ring)
+    int *levelset_active = nullptr;   // per pass: any cell assigned
 };
 
 // scratch scalars living in device memory
@@ -87,7 +87,8 @@ struct Scalars {
     int density_iters;     // LinearSolver::solve return values
     int pressure_iters;
     int pcg_status;        // 0 ok, 1 a grid-barrier wait timed out
-    int pad[3];
+    int wrap_units;        // a unit row lies on the j = 0 or j = NJ-1 edge
+    int pad[2];
 };
 
 // launch helpers implemented in the kernel files
@@ -105,7 +106,11 @@ void launch_count_erase(const GridDims &d, const SceneParams &sp, Particles &P, 
                         cudaStream_t st);
 void launch_max_velocity(const Particles &P, Scalars *sc, cudaStream_t st);
 
-void launch_decomposition(const GridDims &d, const Grids &G, cudaStream_t st);
+// the pressure-operator rows plus, per splitRange chunk of the reference's
+// max-abs test (ps cells per chunk, the first `rem` chunks one more), the
+// last unit row of the chunk
+void launch_decomposition(const GridDims &d, const Grids &G, int *chunk_last, int nchunks,
+                          long long ps, long long rem, Scalars *sc, cudaStream_t st);
 void launch_density_grid(const GridDims &d, const SceneParams &sp, const Particles &P,
                          const Grids &G, void *rhs, int rhs_is_double, const Scalars *sc,
                          cudaStream_t st);
