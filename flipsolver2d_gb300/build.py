@@ -28,6 +28,7 @@ UNITS = {
     "fs_grid.cu": ["-fmad=false"],
     "fs_api.cu": ["-fmad=false"],
     "fs_pcg.cu": ["-fmad=true"],
+    "fs_pcg_tma.cu": ["-fmad=true"],
 }
 
 

@@ -28,6 +28,7 @@
 
 #include "../../include/fs_gpu.h"
 #include "fs_pcg.h"
+#include "fs_pcg_tma.h"
 #include "fs_state.h"
 
 using namespace fsg;
@@ -165,6 +166,9 @@ struct fs_solver {
     int nchunks = 0;
     long long chunk_ps = 1, chunk_rem = 0; // splitRange part size and remainder
     GridBarrier *bar = nullptr;
+    bool tma = false;          // TMA-staged FP32 PCG available for this grid
+    int tma_ti = 0, tma_tj = 0;
+    TmaMaps maps_dens{}, maps_pres{};
     void *rebin_scratch = nullptr;
     size_t rebin_scratch_size = 0;
     cudaStream_t st = nullptr, side = nullptr;
@@ -425,6 +429,22 @@ extern "C" fs_status fs_create(const fs_params *p, const fs_exec_params *exec, f
                                          : pcg_grid_size<float>((long long)n);
     A(dalloc(s, &s->partials, (size_t)3 * s->pcg_grid + 8));
     A(dalloc(s, &s->bar, 1));
+    if (s->prec == FS_PCG_FP32 && tma_tile_shape(d.ni, d.nj, &s->tma_ti, &s->tma_tj)) {
+        s->tma = tma_maps(&s->maps_dens, d.ni, d.nj, s->tma_ti, s->tma_tj, G.cell_info,
+                          (const float *)s->dens_rhs, (const float *)s->dens_x,
+                          (const float *)s->r0, (const float *)s->r1, (const float *)s->s0,
+                          (const float *)s->s1) &&
+                 tma_store_maps(&s->maps_dens, d.ni, d.nj, s->tma_ti, s->tma_tj,
+                                (const float *)s->r0, (const float *)s->r1, (const float *)s->s0,
+                                (const float *)s->s1) &&
+                 tma_maps(&s->maps_pres, d.ni, d.nj, s->tma_ti, s->tma_tj, G.cell_info,
+                          (const float *)s->pres_rhs, (const float *)s->pres_x,
+                          (const float *)s->r0, (const float *)s->r1, (const float *)s->s0,
+                          (const float *)s->s1) &&
+                 tma_store_maps(&s->maps_pres, d.ni, d.nj, s->tma_ti, s->tma_tj,
+                                (const float *)s->r0, (const float *)s->r1, (const float *)s->s0,
+                                (const float *)s->s1);
+    }
     std::vector<int> ends = split_range_ends((long long)n, s->ex.pool_threads);
     s->nchunks = (int)ends.size();
     split_range_params((long long)n, s->ex.pool_threads, &s->chunk_ps, &s->chunk_rem);
@@ -690,8 +710,18 @@ static fs_status run_pcg(fs_solver *s, const void *b, void *x, int *iters)
     if (s->timers) CK(cudaEventRecord(s->p0, s->st));
     cudaError_t e;
     int launched = 0;
-    if (s->prec == FS_PCG_FP64) e = launch_pcg<double>(pcg_args<double>(s, b, x, iters), s->st, &launched);
-    else e = launch_pcg<float>(pcg_args<float>(s, b, x, iters), s->st, &launched);
+    if (s->prec == FS_PCG_FP64) {
+        e = launch_pcg<double>(pcg_args<double>(s, b, x, iters), s->st, &launched);
+    } else if (s->tma) {
+        PcgArgs<float> pa = pcg_args<float>(s, b, x, iters);
+        pa.mode = 2; // unless a unit row sits on a j edge
+        e = launch_pcg_tma(pa, b == s->dens_rhs ? s->maps_dens : s->maps_pres, s->tma_ti,
+                           s->tma_tj, s->st);
+        if (e == cudaSuccess) e = launch_pcg_linear_if_wrap(pa, s->st);
+        launched = 2;
+    } else {
+        e = launch_pcg<float>(pcg_args<float>(s, b, x, iters), s->st, &launched);
+    }
     g_kernel_launches += launched;
     if (e != cudaSuccess) return fail(FS_ERR_CUDA, "PCG launch: %s", cudaGetErrorString(e));
     if (s->timers) {
@@ -1298,7 +1328,21 @@ static fs_status pcg_solve_common(int ni, int nj, const int8_t *mat_dev, float d
         a.iter_limit = iter_limit; a.tol = tol; a.iters_out = &c->sc->density_iters;
         a.status = &c->sc->pcg_status; a.bar = c->bar;
         a.wrap_flag = &c->sc->wrap_units; a.mode = 0;
-        e = launch_pcg<float>(a, st, &launched);
+        int ti = 0, tj = 0;
+        TmaMaps maps;
+        if (tma_tile_shape(ni, nj, &ti, &tj) &&
+            tma_maps(&maps, ni, nj, ti, tj, c->info, (const float *)rhs_dev, (const float *)res_dev,
+                     (const float *)c->r0, (const float *)c->r1, (const float *)c->s0,
+                     (const float *)c->s1) &&
+            tma_store_maps(&maps, ni, nj, ti, tj, (const float *)c->r0, (const float *)c->r1,
+                           (const float *)c->s0, (const float *)c->s1)) {
+            a.mode = 2;
+            e = launch_pcg_tma(a, maps, ti, tj, st);
+            if (e == cudaSuccess) e = launch_pcg_linear_if_wrap(a, st);
+            launched = 2;
+        } else {
+            e = launch_pcg<float>(a, st, &launched);
+        }
     }
     g_kernel_launches += launched;
     if (e != cudaSuccess) return fail(FS_ERR_CUDA, "PCG launch: %s", cudaGetErrorString(e));

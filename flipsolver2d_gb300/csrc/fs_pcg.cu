@@ -889,6 +889,19 @@ template <typename T> cudaError_t launch_pcg(const PcgArgs<T> &a, cudaStream_t s
     return coop((const void *)k_pcg<T>, b, glin, kPcgThreads, st);
 }
 
+// the linear-index FP32 kernel, run only when the decomposition flagged unit
+// rows on the j edges (the TMA kernel runs otherwise)
+cudaError_t launch_pcg_linear_if_wrap(const PcgArgs<float> &a, cudaStream_t st)
+{
+    static int lin = 0;
+    if (!lin) lin = occupancy_grid((const void *)k_pcg<float>, kPcgThreads, 64);
+    long long want = (a.N + kPcgThreads * 4 - 1) / (kPcgThreads * 4);
+    int glin = (int)(want < 1 ? 1 : (want < lin ? want : lin));
+    PcgArgs<float> b = a;
+    b.mode = 1;
+    return coop((const void *)k_pcg<float>, b, glin, kPcgThreads, st);
+}
+
 template int pcg_grid_size<float>(long long);
 template int pcg_grid_size<double>(long long);
 template cudaError_t launch_pcg<float>(const PcgArgs<float> &, cudaStream_t, int *);

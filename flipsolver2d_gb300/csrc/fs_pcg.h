@@ -43,5 +43,6 @@ template <typename T> int pcg_grid_size(long long N);
 // the linear-index kernel when a unit row touches the j edges; FP64 always
 // uses the linear-index kernel.  Returns the number of kernels launched.
 template <typename T> cudaError_t launch_pcg(const PcgArgs<T> &a, cudaStream_t st, int *launched);
+cudaError_t launch_pcg_linear_if_wrap(const PcgArgs<float> &a, cudaStream_t st);
 
 } // namespace fsg

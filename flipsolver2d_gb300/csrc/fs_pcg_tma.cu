@@ -1,0 +1,996 @@
+// fs_pcg_tma.cu -- the FP32 pressure / density solve with TMA-staged tiles.
+//
+// Same algorithm and semantics as fs_pcg.cu (LinearSolver::solve,
+// linearsolver.cpp:25-73, with the reference's operator and IPP rows), but
+// every tile moves through the Tensor Memory Accelerator: one thread issues
+// 2-D box copies global -> shared (cp.async.bulk.tensor, completion on an
+// mbarrier), the boxes start two rows / four columns before the tile and
+// the hardware fills cells outside the grid with zeros -- exactly the
+// reference's treatment of indices outside the vector.  Tile results (s, r,
+// x) are staged in shared memory and written back with TMA stores.  The
+// threads only compute, mapped warp-per-row and lane-per-column.
+//
+// TMA rules respected here: boxes start at a column that is a multiple of
+// 16 bytes (columns tj0 - 4 for floats, tj0 - 16 for the u8 operator rows,
+// tj0 a multiple of 32), stores start inside the grid, row pitches are
+// multiples of 16 bytes (NJ % 16 == 0, checked by the host, else the
+// non-TMA kernel runs), shared destinations are 128-byte aligned.
+//
+// Cross-block visibility: a block's TMA stores are complete
+// (cp.async.bulk.wait_group 0) and ordered for the generic and async proxies
+// (fence.proxy.async) before it arrives at the grid barrier; after the barrier
+// the loading thread fences again before issuing the next TMA loads.
+#include <cfloat>
+#include <cstdio>
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include "fs_pcg.h"
+#include "fs_pcg_tma.h"
+
+namespace fsg {
+
+constexpr int kThreads = 1024;
+constexpr long long kSpinLimit = 1LL << 25; // a few seconds with the sleeps
+
+__device__ __forceinline__ unsigned smem_u32(const void *p)
+{
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(smem_u32(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y,
+                                            unsigned long long *bar)
+{
+    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+                 "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, int x, int y, const void *src)
+{
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(map),
+                 "r"(x), "r"(y), "r"(smem_u32(src))
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_shared() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_all() { asm volatile("fence.proxy.async;" ::: "memory"); }
+
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+    s = a + b;
+    const float bv = s - a;
+    e = (a - (s - bv)) + (b - bv);
+}
+
+// block sum of FP32 partials: compensated FP32 pairs inside warps, FP64 for
+// the 32 warp results; same value in every thread
+__device__ __forceinline__ double bsum(float v, double *sm)
+{
+    float hi = v, lo = 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float h2 = __shfl_down_sync(0xffffffffu, hi, o);
+        const float l2 = __shfl_down_sync(0xffffffffu, lo, o);
+        float s, e;
+        two_sum(hi, h2, s, e);
+        hi = s;
+        lo = lo + l2 + e;
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) sm[w] = (double)hi + (double)lo;
+    __syncthreads();
+    if (w == 0) {
+        double x = lane < (int)(blockDim.x >> 5) ? sm[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) sm[32] = x;
+    }
+    __syncthreads();
+    const double r = sm[32];
+    __syncthreads();
+    return r;
+}
+
+__device__ __forceinline__ double psum(const double *partials, int nblocks, double *sm)
+{
+    if (threadIdx.x < 32) {
+        double a = 0.0;
+        for (int k = threadIdx.x; k < nblocks; k += 32) a += ((volatile const double *)partials)[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+        if (threadIdx.x == 0) sm[34] = a;
+    }
+    __syncthreads();
+    const double r = sm[34];
+    __syncthreads();
+    return r;
+}
+
+// grid barrier with bounded spins; the calling block's TMA stores are
+// complete and proxy-fenced before it arrives
+__device__ __forceinline__ bool gsync(GridBarrier *gb, unsigned nblocks, int *status)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        bulk_wait_all();
+        fence_async_all();
+        volatile unsigned *vgen = &gb->gen;
+        const unsigned g = *vgen;
+        __threadfence();
+        const unsigned arrived = atomicAdd(&gb->count, 1u);
+        if (arrived == nblocks - 1) {
+            gb->count = 0;
+            __threadfence();
+            atomicAdd(&gb->gen, 1u);
+        } else {
+            long long spins = 0;
+            while (*vgen == g) {
+                if (++spins > kSpinLimit || *((volatile int *)status) != 0) {
+                    atomicExch(status, 1);
+                    break;
+                }
+                if (spins > 4096) __nanosleep(64);
+            }
+        }
+        __threadfence();
+        fence_async_all();
+    }
+    __syncthreads();
+    return *((volatile int *)status) == 0;
+}
+
+// wait for the current TMA load batch (bounded)
+__device__ __forceinline__ bool load_wait(unsigned long long *bar, unsigned &phase, int *status)
+{
+    long long spins = 0;
+    while (!mbar_try_wait(bar, phase & 1)) {
+        if (++spins > kSpinLimit || *((volatile int *)status) != 0) {
+            atomicExch(status, 1);
+            return false;
+        }
+    }
+    phase++;
+    return true;
+}
+
+struct SmemLayout {
+    int ti, tj;
+    int wr;  // columns of a float box: tj + 8
+    int wi;  // columns of the u8 box: tj + 32
+    int h2;  // rows of a box: ti + 4
+    int w1, h1;
+    size_t off_ib, off_rb, off_sb, off_b1, off_st, off_xb, bytes;
+};
+
+__host__ __device__ inline size_t a128(size_t x) { return (x + 127) & ~(size_t)127; }
+
+__host__ __device__ inline SmemLayout smem_layout(int ti, int tj)
+{
+    SmemLayout L;
+    L.ti = ti;
+    L.tj = tj;
+    L.wr = tj + 8;
+    L.wi = tj + 32;
+    L.h2 = ti + 4;
+    L.w1 = tj + 2;
+    L.h1 = ti + 2;
+    size_t o = 0;
+    L.off_ib = o;
+    o = a128(o + (size_t)L.h2 * L.wi);
+    L.off_rb = o;
+    o = a128(o + (size_t)L.h2 * L.wr * 4);
+    L.off_sb = o;
+    o = a128(o + (size_t)L.h2 * L.wr * 4);
+    L.off_b1 = o;
+    o = a128(o + (size_t)L.h1 * L.w1 * 4);
+    L.off_st = o;
+    o = a128(o + (size_t)ti * tj * 4);
+    L.off_xb = o;
+    o = a128(o + (size_t)ti * tj * 4);
+    L.bytes = o + 128; // + alignment slack
+    return L;
+}
+
+// indices: a float box element (row r, col q) of the tile's halo coordinates
+// (r in [-2, ti+2), q in [-4, tj+4)) lives at (r + 2) * wr + (q + 4); the u8
+// box uses (r + 2) * wi + (q + 16)
+
+__global__ void __launch_bounds__(kThreads, 1)
+k_pcg_tma(PcgArgs<float> a, const __grid_constant__ TmaMaps m, int ti, int tj)
+{
+    extern __shared__ unsigned char smem_dyn[];
+    __shared__ double sm[40];
+    __shared__ double s_err;
+    __shared__ __align__(8) unsigned long long bar;
+    if (a.mode == 1 && *a.wrap_flag == 0) return;
+    if (a.mode == 2 && *a.wrap_flag != 0) return;
+    unsigned char *base = reinterpret_cast<unsigned char *>(
+        ((size_t)smem_dyn + 127) & ~(size_t)127);
+    const SmemLayout L = smem_layout(ti, tj);
+    uint8_t *IB = base + L.off_ib;
+    float *RB = reinterpret_cast<float *>(base + L.off_rb);
+    float *SB = reinterpret_cast<float *>(base + L.off_sb);
+    float *B1 = reinterpret_cast<float *>(base + L.off_b1);
+    float *ST = reinterpret_cast<float *>(base + L.off_st);
+    float *XB = reinterpret_cast<float *>(base + L.off_xb);
+    const int NI = a.ni, NJ = a.nj;
+    const int G = gridDim.x;
+    const int tiles_j = (NJ + tj - 1) / tj, tiles_i = (NI + ti - 1) / ti;
+    const int ntiles = tiles_i * tiles_j;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    double *pA = a.partials, *pB = a.partials + G, *pC = a.partials + 2 * G;
+    const unsigned box_f = (unsigned)(L.h2 * L.wr * 4), box_i = (unsigned)(L.h2 * L.wi);
+    const unsigned box_x = (unsigned)(ti * tj * 4);
+
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    unsigned phase = 0;
+
+    const double scale_d = (double)a.sc->dt / (a.density * a.dx * a.dx);
+    const float scale = (float)scale_d;
+    __shared__ float inv[8];
+    if (threadIdx.x < 8) inv[threadIdx.x] = (threadIdx.x >= 1 && threadIdx.x <= 4)
+                                                ? (float)(1.0 / (threadIdx.x * scale_d)) : 0.f;
+
+    // phase 0: sigma = b.b and the zero test (VOps::isZero, 1e-15)
+    {
+        const long long N = a.N;
+        const long long per = ((N + G - 1) / G + blockDim.x - 1) / blockDim.x * blockDim.x;
+        const long long lo = (long long)blockIdx.x * per;
+        const long long hi = lo + per < N ? lo + per : N;
+        float bb = 0.f;
+        int nz = 0;
+        for (long long c = lo + threadIdx.x; c < hi; c += blockDim.x) {
+            const float bv = a.b[c];
+            bb = fmaf(bv, bv, bb);
+            nz |= fabsf(bv) > 1.0e-15f;
+        }
+        const double part = bsum(bb, sm);
+        const int anynz = __syncthreads_or(nz);
+        if (threadIdx.x == 0) {
+            pA[blockIdx.x] = part;
+            pC[blockIdx.x] = anynz ? 1.0 : 0.0;
+        }
+    }
+    if (!gsync(a.bar, G, a.status)) return;
+    double sigma = psum(pA, G, sm);
+    if (psum(pC, G, sm) == 0.0) {
+        // the reference leaves result at zero
+        for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < a.N;
+             c += (long long)G * blockDim.x)
+            a.x[c] = 0.f;
+        if (blockIdx.x == 0 && threadIdx.x == 0) *a.iters_out = 0;
+        return;
+    }
+
+    double beta = 0.0;
+    int result = a.iter_limit;
+    for (int it = 0; it < a.iter_limit; it++) {
+        const bool first = it == 0;
+        // r_it: b on the first iteration, then the ping-pong buffers
+        const CUtensorMap *mr_cur = first ? &m.b : ((it & 1) ? &m.r1 : &m.r0);
+        const CUtensorMap *ms_cur = first ? &m.b : ((it & 1) ? &m.s1 : &m.s0);
+        // s_0 = b is never stored, so iteration 1 reads it from b
+        const CUtensorMap *ms_prev = it == 1 ? &m.b : ((it & 1) ? &m.s0 : &m.s1);
+        const CUtensorMap *ms_cur_st = (it & 1) ? &m.s1_st : &m.s0_st;
+        const CUtensorMap *mr_next_st = (it & 1) ? &m.r0_st : &m.r1_st;
+        const float fb = (float)beta;
+
+        // ---- sweep 1: s = M r + beta s_prev on the halo, q = A s, q.s ----
+        float qs = 0.f;
+        for (int t = blockIdx.x; t < ntiles; t += G) {
+            const int ti0 = (t / tiles_j) * ti, tj0 = (t % tiles_j) * tj;
+            if (threadIdx.x == 0) {
+                bulk_wait_read(); // staging of an earlier store may still be read
+                mbar_expect_tx(&bar, box_i + (first ? 0u : box_f) + box_f);
+                tma_load_2d(IB, &m.info, tj0 - 16, ti0 - 2, &bar);
+                if (!first) tma_load_2d(RB, mr_cur, tj0 - 4, ti0 - 2, &bar);
+                tma_load_2d(SB, first ? ms_cur : ms_prev, tj0 - 4, ti0 - 2, &bar);
+            }
+            if (!load_wait(&bar, phase, a.status)) return;
+            // s on the tile and its 1-halo
+            for (int r = warp; r < L.h1; r += nw) {
+                const int rr = r - 1;
+                for (int q = lane; q < L.w1; q += 32) {
+                    const int qq = q - 1;
+                    const int cf = (rr + 2) * L.wr + (qq + 4);
+                    float s = SB[cf];
+                    if (!first) {
+                        const int ci = (rr + 2) * L.wi + (qq + 16);
+                        const uint8_t ic = IB[ci];
+                        float z = RB[cf];
+                        if (ic & 0x80) {
+                            const float iNeg = inv[(IB[ci - L.wi] >> 4) & 7];
+                            const float iPos = inv[(IB[ci + L.wi] >> 4) & 7];
+                            const float jNeg = inv[(IB[ci - 1] >> 4) & 7];
+                            const float jPos = inv[(IB[ci + 1] >> 4) & 7];
+                            const float diag = (1.f + iNeg * iNeg) + jNeg * jNeg;
+                            float acc = diag * z;
+                            acc = fmaf(jNeg, RB[cf - 1], acc);
+                            acc = fmaf(jPos, RB[cf + 1], acc);
+                            acc = fmaf(iNeg, RB[cf - L.wr], acc);
+                            acc = fmaf(iPos, RB[cf + L.wr], acc);
+                            z = acc;
+                        }
+                        s = fmaf(s, fb, z);
+                    }
+                    B1[r * L.w1 + q] = s;
+                }
+            }
+            __syncthreads();
+            // q = A s on the tile
+            for (int r = warp; r < ti; r += nw) {
+                for (int q = lane; q < tj; q += 32) {
+                    const int c1 = (r + 1) * L.w1 + (q + 1);
+                    const uint8_t ic = IB[(r + 2) * L.wi + (q + 16)];
+                    const float s_c = B1[c1];
+                    float qv = s_c;
+                    if (ic & 0x80) {
+                        float nb = 0.f;
+                        if (ic & 1) nb += B1[c1 - L.w1];
+                        if (ic & 2) nb += B1[c1 + L.w1];
+                        if (ic & 4) nb += B1[c1 - 1];
+                        if (ic & 8) nb += B1[c1 + 1];
+                        qv = scale * ((float)((ic >> 4) & 7) * s_c - nb);
+                    }
+                    if (ti0 + r < NI && tj0 + q < NJ) qs = fmaf(qv, s_c, qs);
+                    ST[r * tj + q] = s_c;
+                }
+            }
+            if (!first) {
+                fence_async_shared();
+                __syncthreads();
+                if (threadIdx.x == 0) {
+                    tma_store_2d(ms_cur_st, tj0, ti0, ST);
+                    bulk_commit();
+                }
+            }
+            __syncthreads();
+        }
+        {
+            const double part = bsum(qs, sm);
+            if (threadIdx.x == 0) pA[blockIdx.x] = part;
+        }
+        if (!gsync(a.bar, G, a.status)) return;
+        const double alpha = sigma / (psum(pA, G, sm) + 1e-8);
+        const float fa = (float)alpha;
+
+        // ---- sweep 2: r' = r - alpha A s on the halo, z = M r', x += alpha s
+        float zr = 0.f;
+        for (int t = blockIdx.x; t < ntiles; t += G) {
+            const int ti0 = (t / tiles_j) * ti, tj0 = (t % tiles_j) * tj;
+            if (threadIdx.x == 0) {
+                bulk_wait_read();
+                mbar_expect_tx(&bar, box_i + 2 * box_f + (first ? 0u : box_x));
+                tma_load_2d(IB, &m.info, tj0 - 16, ti0 - 2, &bar);
+                tma_load_2d(SB, ms_cur, tj0 - 4, ti0 - 2, &bar);
+                tma_load_2d(RB, mr_cur, tj0 - 4, ti0 - 2, &bar);
+                if (!first) tma_load_2d(XB, &m.x, tj0, ti0, &bar);
+            }
+            if (!load_wait(&bar, phase, a.status)) return;
+            // r' on the tile and its 1-halo
+            for (int r = warp; r < L.h1; r += nw) {
+                const int rr = r - 1;
+                for (int q = lane; q < L.w1; q += 32) {
+                    const int qq = q - 1;
+                    const int cf = (rr + 2) * L.wr + (qq + 4);
+                    const uint8_t ic = IB[(rr + 2) * L.wi + (qq + 16)];
+                    const float s_c = SB[cf];
+                    float qv = s_c;
+                    if (ic & 0x80) {
+                        float nb = 0.f;
+                        if (ic & 1) nb += SB[cf - L.wr];
+                        if (ic & 2) nb += SB[cf + L.wr];
+                        if (ic & 4) nb += SB[cf - 1];
+                        if (ic & 8) nb += SB[cf + 1];
+                        qv = scale * ((float)((ic >> 4) & 7) * s_c - nb);
+                    }
+                    B1[r * L.w1 + q] = fmaf(-qv, fa, RB[cf]);
+                }
+            }
+            __syncthreads();
+            // z = M r', x += alpha s on the tile
+            for (int r = warp; r < ti; r += nw) {
+                for (int q = lane; q < tj; q += 32) {
+                    const int c1 = (r + 1) * L.w1 + (q + 1);
+                    const int ci = (r + 2) * L.wi + (q + 16);
+                    const uint8_t ic = IB[ci];
+                    const float r_c = B1[c1];
+                    float z = r_c;
+                    if (ic & 0x80) {
+                        const float iNeg = inv[(IB[ci - L.wi] >> 4) & 7];
+                        const float iPos = inv[(IB[ci + L.wi] >> 4) & 7];
+                        const float jNeg = inv[(IB[ci - 1] >> 4) & 7];
+                        const float jPos = inv[(IB[ci + 1] >> 4) & 7];
+                        const float diag = (1.f + iNeg * iNeg) + jNeg * jNeg;
+                        z = diag * r_c;
+                        z = fmaf(jNeg, B1[c1 - 1], z);
+                        z = fmaf(jPos, B1[c1 + 1], z);
+                        z = fmaf(iNeg, B1[c1 - L.w1], z);
+                        z = fmaf(iPos, B1[c1 + L.w1], z);
+                    }
+                    if (ti0 + r < NI && tj0 + q < NJ) zr = fmaf(z, r_c, zr);
+                    const float s_c = SB[(r + 2) * L.wr + (q + 4)];
+                    const float x_old = first ? 0.f : XB[r * tj + q];
+                    XB[r * tj + q] = fmaf(s_c, fa, x_old);
+                    ST[r * tj + q] = r_c;
+                }
+            }
+            fence_async_shared();
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                tma_store_2d(&m.x, tj0, ti0, XB);
+                tma_store_2d(mr_next_st, tj0, ti0, ST);
+                bulk_commit();
+            }
+            // VOps::maxAbs (vmath.cpp:100-136): |r'| at each chunk's last unit
+            // row, taken from the tile that computed it; -1 marks r' == 0
+            for (int k = threadIdx.x; k < a.nchunks; k += blockDim.x) {
+                const int idx = a.chunk_last_unit[k];
+                if (idx < 0) continue;
+                const int gi = idx / NJ, gj = idx - gi * NJ;
+                if (gi < ti0 || gi >= ti0 + ti || gj < tj0 || gj >= tj0 + tj) continue;
+                const float v = ST[(gi - ti0) * tj + (gj - tj0)];
+                a.chunk_val[k] = v != 0.f ? fabs((double)v) : -1.0;
+            }
+            __syncthreads();
+        }
+        {
+            const double part = bsum(zr, sm);
+            if (threadIdx.x == 0) pB[blockIdx.x] = part;
+        }
+        if (!gsync(a.bar, G, a.status)) return;
+        const float *rn = (it & 1) ? a.r0 : a.r1;
+        if (threadIdx.x < 32) {
+            double mx = 0.0;
+            for (int k = threadIdx.x; k < a.nchunks; k += 32) {
+                const long long start = k == 0 ? 0 : a.chunk_end[k - 1];
+                const int last = a.chunk_last_unit[k];
+                double v;
+                if (last < 0) {
+                    v = DBL_MIN;
+                } else {
+                    v = ((volatile double *)a.chunk_val)[k];
+                    if (v < 0.0) {
+                        long long idx = last - 1;
+                        while (idx >= start && ((volatile const float *)rn)[idx] == 0.f) idx--;
+                        v = idx >= start ? fabs((double)((volatile const float *)rn)[idx]) : DBL_MIN;
+                    }
+                }
+                if (v > mx) mx = v;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double t = __shfl_down_sync(0xffffffffu, mx, o);
+                if (t > mx) mx = t;
+            }
+            if (threadIdx.x == 0) s_err = mx;
+        }
+        __syncthreads();
+        const double err = s_err;
+        const double newSigma = psum(pB, G, sm);
+        if (err <= a.tol) {
+            result = it;
+            break;
+        }
+        beta = newSigma / sigma;
+        sigma = newSigma;
+    }
+    if (threadIdx.x == 0) bulk_wait_all();
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.iters_out = result;
+}
+
+// ---------------------------------------------------------------------------
+// Shared-memory-resident variant: one tile per block for the whole solve.
+// r, s (with a 2-cell halo), x and the operator rows live in shared memory;
+// per sweep a block publishes its tile of the vector it just updated (plain
+// stores, ping-pong buffers by iteration parity so a neighbour still reading
+// the previous value is never overwritten) and, after the grid barrier,
+// reads back only the 2-deep ring of neighbour cells around its tile.  Used
+// when every tile fits one block and the tile count does not exceed the SMs.
+// ---------------------------------------------------------------------------
+struct ResLayout {
+    int ti, tj, w2, h2, w1, h1;
+    size_t off_rb, off_sb, off_ib, off_b1, off_xt, bytes;
+};
+
+__host__ __device__ inline ResLayout res_layout(int ti, int tj)
+{
+    ResLayout L;
+    L.ti = ti;
+    L.tj = tj;
+    L.w2 = tj + 4;
+    L.h2 = ti + 4;
+    L.w1 = tj + 2;
+    L.h1 = ti + 2;
+    size_t o = 0;
+    L.off_rb = o;
+    o = a128(o + (size_t)L.h2 * L.w2 * 4);
+    L.off_sb = o;
+    o = a128(o + (size_t)L.h2 * L.w2 * 4);
+    L.off_b1 = o;
+    o = a128(o + (size_t)L.h1 * L.w1 * 4);
+    L.off_xt = o;
+    o = a128(o + (size_t)ti * tj * 4);
+    L.off_ib = o;
+    o = a128(o + (size_t)L.h2 * L.w2);
+    L.bytes = o + 128;
+    return L;
+}
+
+// the k-th cell of the 2-deep ring around a tile, in halo coordinates
+__device__ __forceinline__ void ring_cell(int k, int ti, int tj, int &r, int &q)
+{
+    const int w2 = tj + 4;
+    if (k < 2 * w2) { // two rows above
+        r = k / w2 - 2;
+        q = k % w2 - 2;
+        return;
+    }
+    k -= 2 * w2;
+    if (k < 2 * w2) { // two rows below
+        r = ti + k / w2;
+        q = k % w2 - 2;
+        return;
+    }
+    k -= 2 * w2;
+    r = k >> 2; // ti rows x 4 side cells
+    const int s = k & 3;
+    q = s < 2 ? s - 2 : tj + (s - 2);
+}
+
+__device__ __forceinline__ void load_ring(float *dst, const float *__restrict__ src, int ti0,
+                                          int tj0, int ti, int tj, int NI, int NJ)
+{
+    const int w2 = tj + 4;
+    const int n = 4 * w2 + 4 * ti;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        int r, q;
+        ring_cell(k, ti, tj, r, q);
+        const int gi = ti0 + r, gj = tj0 + q;
+        float v = 0.f;
+        if (gi >= 0 && gi < NI && gj >= 0 && gj < NJ) v = ((volatile const float *)src)[(size_t)gi * NJ + gj];
+        dst[(r + 2) * w2 + (q + 2)] = v;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+k_pcg_resident(PcgArgs<float> a, int ti, int tj)
+{
+    extern __shared__ unsigned char smem_dyn[];
+    __shared__ double sm[40];
+    __shared__ double s_err;
+    __shared__ float inv[8];
+    if (a.mode == 1 && *a.wrap_flag == 0) return;
+    if (a.mode == 2 && *a.wrap_flag != 0) return;
+    unsigned char *base = reinterpret_cast<unsigned char *>(((size_t)smem_dyn + 127) & ~(size_t)127);
+    const ResLayout L = res_layout(ti, tj);
+    float *Rb = reinterpret_cast<float *>(base + L.off_rb);
+    float *Sb = reinterpret_cast<float *>(base + L.off_sb);
+    float *B1 = reinterpret_cast<float *>(base + L.off_b1);
+    float *Xt = reinterpret_cast<float *>(base + L.off_xt);
+    uint8_t *Ib = base + L.off_ib;
+    const int NI = a.ni, NJ = a.nj;
+    const int G = gridDim.x;
+    const int tiles_j = (NJ + tj - 1) / tj;
+    const int ti0 = ((int)blockIdx.x / tiles_j) * ti, tj0 = ((int)blockIdx.x % tiles_j) * tj;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int w2 = L.w2, w1 = L.w1;
+    double *pA = a.partials, *pB = a.partials + G, *pC = a.partials + 2 * G;
+
+    const double scale_d = (double)a.sc->dt / (a.density * a.dx * a.dx);
+    const float scale = (float)scale_d;
+    if (threadIdx.x < 8)
+        inv[threadIdx.x] = (threadIdx.x >= 1 && threadIdx.x <= 4) ? (float)(1.0 / (threadIdx.x * scale_d)) : 0.f;
+
+    // load the operator rows and r_0 = s_0 = b with their halo; x = 0
+    float bb = 0.f;
+    int nz = 0;
+    for (int r = warp; r < L.h2; r += nw) {
+        const int gi = ti0 - 2 + r;
+        for (int q = lane; q < w2; q += 32) {
+            const int gj = tj0 - 2 + q;
+            const bool inb = gi >= 0 && gi < NI && gj >= 0 && gj < NJ;
+            const size_t g = (size_t)gi * NJ + gj;
+            const float bv = inb ? a.b[g] : 0.f;
+            Rb[r * w2 + q] = bv;
+            Sb[r * w2 + q] = bv;
+            Ib[r * w2 + q] = inb ? a.info[g] : (uint8_t)0;
+            const bool own = r >= 2 && r < ti + 2 && q >= 2 && q < tj + 2 && inb;
+            if (own) {
+                bb = fmaf(bv, bv, bb);
+                nz |= fabsf(bv) > 1.0e-15f;
+            }
+        }
+    }
+    for (int e = threadIdx.x; e < ti * tj; e += blockDim.x) Xt[e] = 0.f;
+    {
+        const double part = bsum(bb, sm);
+        const int anynz = __syncthreads_or(nz);
+        if (threadIdx.x == 0) {
+            pA[blockIdx.x] = part;
+            pC[blockIdx.x] = anynz ? 1.0 : 0.0;
+        }
+    }
+    if (!gsync(a.bar, G, a.status)) return;
+    double sigma = psum(pA, G, sm);
+    const bool zero = psum(pC, G, sm) == 0.0;
+
+    double beta = 0.0;
+    int result = zero ? 0 : a.iter_limit;
+    for (int it = 0; !zero && it < a.iter_limit; it++) {
+        const bool first = it == 0;
+        float *s_pub = (it & 1) ? a.s1 : a.s0;       // s_it published here
+        float *r_pub = (it & 1) ? a.r0 : a.r1;       // r_{it+1} published here
+        const float fb = (float)beta;
+
+        // ---- sweep 1 -------------------------------------------------------
+        if (!first) {
+            // neighbours' r_it (published last sweep 2) around the tile
+            load_ring(Rb, (it & 1) ? a.r1 : a.r0, ti0, tj0, ti, tj, NI, NJ);
+            __syncthreads();
+        }
+        // s_it on the tile and its 1-halo into B1
+        for (int r = warp; r < L.h1; r += nw) {
+            for (int q = lane; q < w1; q += 32) {
+                const int c2 = (r + 1) * w2 + (q + 1);
+                float s = Sb[c2];
+                if (!first) {
+                    const uint8_t ic = Ib[c2];
+                    float z = Rb[c2];
+                    if (ic & 0x80) {
+                        const float iNeg = inv[(Ib[c2 - w2] >> 4) & 7];
+                        const float iPos = inv[(Ib[c2 + w2] >> 4) & 7];
+                        const float jNeg = inv[(Ib[c2 - 1] >> 4) & 7];
+                        const float jPos = inv[(Ib[c2 + 1] >> 4) & 7];
+                        const float diag = (1.f + iNeg * iNeg) + jNeg * jNeg;
+                        float acc = diag * z;
+                        acc = fmaf(jNeg, Rb[c2 - 1], acc);
+                        acc = fmaf(jPos, Rb[c2 + 1], acc);
+                        acc = fmaf(iNeg, Rb[c2 - w2], acc);
+                        acc = fmaf(iPos, Rb[c2 + w2], acc);
+                        z = acc;
+                    }
+                    s = fmaf(s, fb, z);
+                }
+                B1[r * w1 + q] = s;
+            }
+        }
+        __syncthreads();
+        float qs = 0.f;
+        for (int r = warp; r < ti; r += nw) {
+            const int gi = ti0 + r;
+            for (int q = lane; q < tj; q += 32) {
+                const int gj = tj0 + q;
+                const int c1 = (r + 1) * w1 + (q + 1);
+                const uint8_t ic = Ib[(r + 2) * w2 + (q + 2)];
+                const float s_c = B1[c1];
+                float qv = s_c;
+                if (ic & 0x80) {
+                    float nb = 0.f;
+                    if (ic & 1) nb += B1[c1 - w1];
+                    if (ic & 2) nb += B1[c1 + w1];
+                    if (ic & 4) nb += B1[c1 - 1];
+                    if (ic & 8) nb += B1[c1 + 1];
+                    qv = scale * ((float)((ic >> 4) & 7) * s_c - nb);
+                }
+                qs = fmaf(qv, s_c, qs);
+                if (!first) {
+                    Sb[(r + 2) * w2 + (q + 2)] = s_c;
+                    if (gi < NI && gj < NJ) s_pub[(size_t)gi * NJ + gj] = s_c;
+                }
+            }
+        }
+        {
+            const double part = bsum(qs, sm);
+            if (threadIdx.x == 0) pA[blockIdx.x] = part;
+        }
+        if (!gsync(a.bar, G, a.status)) return;
+        const double alpha = sigma / (psum(pA, G, sm) + 1e-8);
+        const float fa = (float)alpha;
+
+        // ---- sweep 2 -------------------------------------------------------
+        if (!first) {
+            load_ring(Sb, s_pub, ti0, tj0, ti, tj, NI, NJ); // neighbours' s_it
+            __syncthreads();
+        }
+        for (int r = warp; r < L.h1; r += nw) {
+            for (int q = lane; q < w1; q += 32) {
+                const int c2 = (r + 1) * w2 + (q + 1);
+                const uint8_t ic = Ib[c2];
+                const float s_c = Sb[c2];
+                float qv = s_c;
+                if (ic & 0x80) {
+                    float nb = 0.f;
+                    if (ic & 1) nb += Sb[c2 - w2];
+                    if (ic & 2) nb += Sb[c2 + w2];
+                    if (ic & 4) nb += Sb[c2 - 1];
+                    if (ic & 8) nb += Sb[c2 + 1];
+                    qv = scale * ((float)((ic >> 4) & 7) * s_c - nb);
+                }
+                B1[r * w1 + q] = fmaf(-qv, fa, Rb[c2]);
+            }
+        }
+        __syncthreads();
+        float zr = 0.f;
+        for (int r = warp; r < ti; r += nw) {
+            const int gi = ti0 + r;
+            for (int q = lane; q < tj; q += 32) {
+                const int gj = tj0 + q;
+                const int c1 = (r + 1) * w1 + (q + 1);
+                const int c2 = (r + 2) * w2 + (q + 2);
+                const uint8_t ic = Ib[c2];
+                const float r_c = B1[c1];
+                float z = r_c;
+                if (ic & 0x80) {
+                    const float iNeg = inv[(Ib[c2 - w2] >> 4) & 7];
+                    const float iPos = inv[(Ib[c2 + w2] >> 4) & 7];
+                    const float jNeg = inv[(Ib[c2 - 1] >> 4) & 7];
+                    const float jPos = inv[(Ib[c2 + 1] >> 4) & 7];
+                    const float diag = (1.f + iNeg * iNeg) + jNeg * jNeg;
+                    z = diag * r_c;
+                    z = fmaf(jNeg, B1[c1 - 1], z);
+                    z = fmaf(jPos, B1[c1 + 1], z);
+                    z = fmaf(iNeg, B1[c1 - w1], z);
+                    z = fmaf(iPos, B1[c1 + w1], z);
+                }
+                zr = fmaf(z, r_c, zr);
+                Xt[r * tj + q] = fmaf(Sb[c2], fa, Xt[r * tj + q]);
+                Rb[c2] = r_c;
+                if (gi < NI && gj < NJ) r_pub[(size_t)gi * NJ + gj] = r_c;
+            }
+        }
+        __syncthreads();
+        // VOps::maxAbs (vmath.cpp:100-136) from the tile that owns each
+        // chunk's last unit row; -1 marks r' == 0 there
+        for (int k = threadIdx.x; k < a.nchunks; k += blockDim.x) {
+            const int idx = a.chunk_last_unit[k];
+            if (idx < 0) continue;
+            const int gi = idx / NJ, gj = idx - gi * NJ;
+            if (gi < ti0 || gi >= ti0 + ti || gj < tj0 || gj >= tj0 + tj) continue;
+            const float v = Rb[(gi - ti0 + 2) * w2 + (gj - tj0 + 2)];
+            a.chunk_val[k] = v != 0.f ? fabs((double)v) : -1.0;
+        }
+        {
+            const double part = bsum(zr, sm);
+            if (threadIdx.x == 0) pB[blockIdx.x] = part;
+        }
+        if (!gsync(a.bar, G, a.status)) return;
+        if (threadIdx.x < 32) {
+            double mx = 0.0;
+            for (int k = threadIdx.x; k < a.nchunks; k += 32) {
+                const long long start = k == 0 ? 0 : a.chunk_end[k - 1];
+                const int last = a.chunk_last_unit[k];
+                double v;
+                if (last < 0) {
+                    v = DBL_MIN;
+                } else {
+                    v = ((volatile double *)a.chunk_val)[k];
+                    if (v < 0.0) {
+                        long long idx = last - 1;
+                        while (idx >= start && ((volatile const float *)r_pub)[idx] == 0.f) idx--;
+                        v = idx >= start ? fabs((double)((volatile const float *)r_pub)[idx]) : DBL_MIN;
+                    }
+                }
+                if (v > mx) mx = v;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double t2 = __shfl_down_sync(0xffffffffu, mx, o);
+                if (t2 > mx) mx = t2;
+            }
+            if (threadIdx.x == 0) s_err = mx;
+        }
+        __syncthreads();
+        const double err = s_err;
+        const double newSigma = psum(pB, G, sm);
+        if (err <= a.tol) {
+            result = it;
+            break;
+        }
+        beta = newSigma / sigma;
+        sigma = newSigma;
+    }
+    // the solution leaves shared memory once
+    for (int r = warp; r < ti; r += nw) {
+        const int gi = ti0 + r;
+        if (gi >= NI) break;
+        for (int q = lane; q < tj; q += 32) {
+            const int gj = tj0 + q;
+            if (gj < NJ) a.x[(size_t)gi * NJ + gj] = Xt[r * tj + q];
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.iters_out = result;
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+static bool encode(CUtensorMap *map, const void *ptr, CUtensorMapDataType dt, int esz, int ni,
+                   int nj, int box_w, int box_h)
+{
+    auto fn = encode_fn();
+    if (!fn || ((size_t)ptr & 15)) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)nj, (cuuint64_t)ni};
+    cuuint64_t strides[1] = {(cuuint64_t)nj * esz};
+    cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)box_h};
+    cuuint32_t es[2] = {1, 1};
+    return fn(map, dt, 2, const_cast<void *>(ptr), dims, strides, box, es,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+           CUDA_SUCCESS;
+}
+
+static int sm_count()
+{
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    return sms;
+}
+
+constexpr int kMaxTmaCells = 54 * 128;
+
+bool tma_tile_shape(int ni, int nj, int *ti, int *tj)
+{
+    if (nj % 16 != 0) return false;
+    const int blocks = sm_count();
+    int w = nj < 128 ? nj : 128;
+    if (w % 32 != 0) w = ((w + 31) / 32) * 32;
+    const long long tiles_j = (nj + w - 1) / w;
+    const long long cap = kMaxTmaCells / w;
+    for (long long k = 1; k <= 4096; k++) {
+        long long max_ti = (long long)blocks * k / tiles_j;
+        if (max_ti < 1) continue;
+        long long h = (ni + max_ti - 1) / max_ti;
+        if (h < 8) h = ni < 8 ? ni : 8;
+        if (h <= cap) {
+            *ti = (int)h;
+            *tj = w;
+            return h + 4 <= 256;
+        }
+    }
+    return false;
+}
+
+bool tma_maps(TmaMaps *m, int ni, int nj, int ti, int tj, const uint8_t *info, const float *b,
+              const float *x, const float *r0, const float *r1, const float *s0, const float *s1)
+{
+    const CUtensorMapDataType F = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    const CUtensorMapDataType U = CU_TENSOR_MAP_DATA_TYPE_UINT8;
+    return encode(&m->info, info, U, 1, ni, nj, tj + 32, ti + 4) &&
+           encode(&m->b, b, F, 4, ni, nj, tj + 8, ti + 4) &&
+           encode(&m->x, x, F, 4, ni, nj, tj, ti) &&
+           encode(&m->r0, r0, F, 4, ni, nj, tj + 8, ti + 4) &&
+           encode(&m->r1, r1, F, 4, ni, nj, tj + 8, ti + 4) &&
+           encode(&m->s0, s0, F, 4, ni, nj, tj + 8, ti + 4) &&
+           encode(&m->s1, s1, F, 4, ni, nj, tj + 8, ti + 4);
+}
+
+// r and s are loaded with halo boxes and stored with tile boxes, so each has
+// a second map encoded with the tile box for the stores
+bool tma_store_maps(TmaMaps *m, int ni, int nj, int ti, int tj, const float *r0, const float *r1,
+                    const float *s0, const float *s1)
+{
+    const CUtensorMapDataType F = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    return encode(&m->r0_st, r0, F, 4, ni, nj, tj, ti) &&
+           encode(&m->r1_st, r1, F, 4, ni, nj, tj, ti) &&
+           encode(&m->s0_st, s0, F, 4, ni, nj, tj, ti) &&
+           encode(&m->s1_st, s1, F, 4, ni, nj, tj, ti);
+}
+
+constexpr size_t kMaxResidentSmem = 200 * 1024;
+
+bool resident_tile_shape(int ni, int nj, int *ti, int *tj)
+{
+    const int blocks = sm_count();
+    for (int w = 32; w <= 256; w *= 2) {
+        const long long tiles_j = (nj + w - 1) / w;
+        if (tiles_j > blocks) continue;
+        const long long max_ti = blocks / tiles_j;
+        long long h = (ni + max_ti - 1) / max_ti;
+        if (h < 1) h = 1;
+        const long long ntiles = ((ni + h - 1) / h) * tiles_j;
+        if (ntiles > blocks) continue;
+        if (res_layout((int)h, w).bytes > kMaxResidentSmem) continue;
+        // prefer the first width whose tiles fit; narrower tiles waste less
+        // on ragged right edges
+        *ti = (int)h;
+        *tj = w;
+        return true;
+    }
+    return false;
+}
+
+cudaError_t launch_pcg_resident(const PcgArgs<float> &a, int ti, int tj, cudaStream_t st)
+{
+    const ResLayout L = res_layout(ti, tj);
+    static size_t configured = 0;
+    if (L.bytes > configured) {
+        cudaError_t e = cudaFuncSetAttribute((const void *)k_pcg_resident,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)kMaxResidentSmem + 256);
+        if (e != cudaSuccess) return e;
+        configured = kMaxResidentSmem + 256;
+    }
+    const int grid = ((a.ni + ti - 1) / ti) * ((a.nj + tj - 1) / tj);
+    PcgArgs<float> args = a;
+    int vti = ti, vtj = tj;
+    void *kargs[] = {&args, &vti, &vtj};
+    cudaError_t e = cudaMemsetAsync(args.bar, 0, sizeof(GridBarrier), st);
+    if (e != cudaSuccess) return e;
+    return cudaLaunchCooperativeKernel((const void *)k_pcg_resident, dim3(grid), dim3(kThreads),
+                                       kargs, L.bytes, st);
+}
+
+cudaError_t launch_pcg_tma(const PcgArgs<float> &a, const TmaMaps &maps, int ti, int tj,
+                           cudaStream_t st)
+{
+    const SmemLayout L = smem_layout(ti, tj);
+    static size_t configured = 0;
+    if (L.bytes > configured) {
+        cudaError_t e = cudaFuncSetAttribute((const void *)k_pcg_tma,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)L.bytes);
+        if (e != cudaSuccess) return e;
+        configured = L.bytes;
+    }
+    const long long ntiles = (long long)((a.ni + ti - 1) / ti) * ((a.nj + tj - 1) / tj);
+    const long long tpb = (ntiles + sm_count() - 1) / sm_count();
+    const int grid = (int)((ntiles + tpb - 1) / tpb);
+    PcgArgs<float> args = a;
+    TmaMaps mm = maps;
+    int vti = ti, vtj = tj;
+    void *kargs[] = {&args, &mm, &vti, &vtj};
+    cudaError_t e = cudaMemsetAsync(args.bar, 0, sizeof(GridBarrier), st);
+    if (e != cudaSuccess) return e;
+    return cudaLaunchCooperativeKernel((const void *)k_pcg_tma, dim3(grid), dim3(kThreads), kargs,
+                                       L.bytes, st);
+}
+
+} // namespace fsg
