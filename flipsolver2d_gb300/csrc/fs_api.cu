@@ -168,6 +168,8 @@ struct fs_solver {
     GridBarrier *bar = nullptr;
     bool tma = false;          // TMA-staged FP32 PCG available for this grid
     int tma_ti = 0, tma_tj = 0;
+    bool resident = false;     // FP32 PCG with every tile resident in shared memory
+    int res_ti = 0, res_tj = 0;
     TmaMaps maps_dens{}, maps_pres{};
     void *rebin_scratch = nullptr;
     size_t rebin_scratch_size = 0;
@@ -429,6 +431,8 @@ extern "C" fs_status fs_create(const fs_params *p, const fs_exec_params *exec, f
                                          : pcg_grid_size<float>((long long)n);
     A(dalloc(s, &s->partials, (size_t)3 * s->pcg_grid + 8));
     A(dalloc(s, &s->bar, 1));
+    if (s->prec == FS_PCG_FP32)
+        s->resident = resident_tile_shape(d.ni, d.nj, &s->res_ti, &s->res_tj);
     if (s->prec == FS_PCG_FP32 && tma_tile_shape(d.ni, d.nj, &s->tma_ti, &s->tma_tj)) {
         s->tma = tma_maps(&s->maps_dens, d.ni, d.nj, s->tma_ti, s->tma_tj, G.cell_info,
                           (const float *)s->dens_rhs, (const float *)s->dens_x,
@@ -712,6 +716,12 @@ static fs_status run_pcg(fs_solver *s, const void *b, void *x, int *iters)
     int launched = 0;
     if (s->prec == FS_PCG_FP64) {
         e = launch_pcg<double>(pcg_args<double>(s, b, x, iters), s->st, &launched);
+    } else if (s->resident) {
+        PcgArgs<float> pa = pcg_args<float>(s, b, x, iters);
+        pa.mode = 2; // unless a unit row sits on a j edge
+        e = launch_pcg_resident(pa, s->res_ti, s->res_tj, s->st);
+        if (e == cudaSuccess) e = launch_pcg_linear_if_wrap(pa, s->st);
+        launched = 2;
     } else if (s->tma) {
         PcgArgs<float> pa = pcg_args<float>(s, b, x, iters);
         pa.mode = 2; // unless a unit row sits on a j edge
@@ -1330,7 +1340,12 @@ static fs_status pcg_solve_common(int ni, int nj, const int8_t *mat_dev, float d
         a.wrap_flag = &c->sc->wrap_units; a.mode = 0;
         int ti = 0, tj = 0;
         TmaMaps maps;
-        if (tma_tile_shape(ni, nj, &ti, &tj) &&
+        if (resident_tile_shape(ni, nj, &ti, &tj)) {
+            a.mode = 2;
+            e = launch_pcg_resident(a, ti, tj, st);
+            if (e == cudaSuccess) e = launch_pcg_linear_if_wrap(a, st);
+            launched = 2;
+        } else if (tma_tile_shape(ni, nj, &ti, &tj) &&
             tma_maps(&maps, ni, nj, ti, tj, c->info, (const float *)rhs_dev, (const float *)res_dev,
                      (const float *)c->r0, (const float *)c->r1, (const float *)c->s0,
                      (const float *)c->s1) &&

@@ -85,81 +85,191 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
     e = (a - (s - bv)) + (b - bv);
 }
 
-// block sum of FP32 partials: compensated FP32 pairs inside warps, FP64 for
-// the 32 warp results; same value in every thread
-__device__ __forceinline__ double bsum(float v, double *sm)
+// Scalars of the iteration (dot products, alpha, beta) are carried as
+// unevaluated float pairs (hi + lo, about 48 significant bits).  Double
+// arithmetic would be simpler, but on this part every FP64 operation has a
+// latency of a few hundred cycles, and the reductions and two divisions of
+// an iteration sit on the critical path between grid barriers.
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b)
 {
-    float hi = v, lo = 0.f;
+    float s, e;
+    two_sum(a.x, b.x, s, e);
+    e += a.y + b.y;
+    const float h = s + e;
+    return make_float2(h, e - (h - s));
+}
+
+__device__ __forceinline__ float2 ff_shfl_down(float2 v, int o)
+{
+    return make_float2(__shfl_down_sync(0xffffffffu, v.x, o), __shfl_down_sync(0xffffffffu, v.y, o));
+}
+
+// a / b rounded to float (error within about one float ulp)
+__device__ __forceinline__ float ff_div(float2 a, float2 b)
+{
+    const float q = __fdiv_rn(a.x, b.x);
+    const float r = (fmaf(-q, b.x, a.x) + a.y) - q * b.y;
+    return q + __fdiv_rn(r, b.x);
+}
+
+// block sum of per-thread FP32 partials as a float pair; same value in every
+// thread.  sm holds at least 36 float2.
+__device__ __forceinline__ float2 bsum(float v, float2 *sm)
+{
+    float2 a = make_float2(v, 0.f);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const float h2 = __shfl_down_sync(0xffffffffu, hi, o);
-        const float l2 = __shfl_down_sync(0xffffffffu, lo, o);
-        float s, e;
-        two_sum(hi, h2, s, e);
-        hi = s;
-        lo = lo + l2 + e;
-    }
+    for (int o = 16; o > 0; o >>= 1) a = ff_add(a, ff_shfl_down(a, o));
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (lane == 0) sm[w] = (double)hi + (double)lo;
+    if (lane == 0) sm[w] = a;
     __syncthreads();
     if (w == 0) {
-        double x = lane < (int)(blockDim.x >> 5) ? sm[lane] : 0.0;
+        float2 x = lane < (int)(blockDim.x >> 5) ? sm[lane] : make_float2(0.f, 0.f);
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        for (int o = 16; o > 0; o >>= 1) x = ff_add(x, ff_shfl_down(x, o));
         if (lane == 0) sm[32] = x;
     }
     __syncthreads();
-    const double r = sm[32];
+    const float2 r = sm[32];
     __syncthreads();
     return r;
 }
 
-__device__ __forceinline__ double psum(const double *partials, int nblocks, double *sm)
+// sum of the blocks' partials in a fixed order, so every block obtains the
+// same value; read through L2 (other blocks wrote them)
+__device__ __forceinline__ float2 psum(const float2 *partials, int nblocks, float2 *sm)
 {
     if (threadIdx.x < 32) {
-        double a = 0.0;
-        for (int k = threadIdx.x; k < nblocks; k += 32) a += ((volatile const double *)partials)[k];
+        float2 a = make_float2(0.f, 0.f);
+        for (int k = threadIdx.x; k < nblocks; k += 32) a = ff_add(a, __ldcg(partials + k));
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+        for (int o = 16; o > 0; o >>= 1) a = ff_add(a, ff_shfl_down(a, o));
         if (threadIdx.x == 0) sm[34] = a;
     }
     __syncthreads();
-    const double r = sm[34];
+    const float2 r = sm[34];
     __syncthreads();
     return r;
 }
 
-// grid barrier with bounded spins; the calling block's TMA stores are
-// complete and proxy-fenced before it arrives
-__device__ __forceinline__ bool gsync(GridBarrier *gb, unsigned nblocks, int *status)
+// The stopping test err <= tol of the reference (double) evaluated on float
+// magnitudes: err is either the largest |r| found (a float) or, when no
+// chunk holds a nonzero, DBL_MIN (VOps::maxAbs) or 0 (no chunks).
+struct TolTest {
+    float tf;     // largest float f with (double)f <= tol
+    int min_ok;   // DBL_MIN <= tol
+    int zero_ok;  // 0 <= tol
+};
+
+__device__ __forceinline__ TolTest tol_test(double tol)
+{
+    TolTest t;
+    float f = (float)tol;
+    if ((double)f > tol) f = nextafterf(f, -INFINITY);
+    t.tf = f;
+    t.min_ok = DBL_MIN <= tol;
+    t.zero_ok = 0.0 <= tol;
+    return t;
+}
+
+__device__ __forceinline__ bool tol_met(const TolTest &t, float mx, int has_min)
+{
+    if (mx > 0.f) return mx <= t.tf;
+    return has_min ? t.min_ok : t.zero_ok;
+}
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned atom_add_acq_rel(unsigned *p, unsigned v)
+{
+    unsigned old;
+    asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+__device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v)
+{
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Grid barrier with bounded spins.  Arrival is an acquire-release add on the
+// counter (it publishes the block's writes, ordered before it by the block
+// barrier); the last block resets the counter and releases the next
+// generation, which the others acquire.  With async_proxy the block's TMA
+// stores are complete and fenced for the generic proxy before it arrives.
+__device__ __forceinline__ bool gsync(GridBarrier *gb, unsigned nblocks, int *status,
+                                      bool async_proxy = true)
 {
     __syncthreads();
     if (threadIdx.x == 0) {
-        bulk_wait_all();
-        fence_async_all();
-        volatile unsigned *vgen = &gb->gen;
-        const unsigned g = *vgen;
-        __threadfence();
-        const unsigned arrived = atomicAdd(&gb->count, 1u);
+        if (async_proxy) {
+            bulk_wait_all();
+            fence_async_all();
+        }
+        const unsigned g = ld_acquire_u32(&gb->gen);
+        const unsigned arrived = atom_add_acq_rel(&gb->count, 1u);
         if (arrived == nblocks - 1) {
             gb->count = 0;
-            __threadfence();
-            atomicAdd(&gb->gen, 1u);
+            st_release_u32(&gb->gen, g + 1);
         } else {
             long long spins = 0;
-            while (*vgen == g) {
-                if (++spins > kSpinLimit || *((volatile int *)status) != 0) {
+            while (ld_acquire_u32(&gb->gen) == g) {
+                ++spins;
+                if (spins > kSpinLimit ||
+                    ((spins & 1023) == 0 && *((volatile int *)status) != 0)) {
                     atomicExch(status, 1);
                     break;
                 }
-                if (spins > 4096) __nanosleep(64);
             }
         }
-        __threadfence();
-        fence_async_all();
+        if (async_proxy) fence_async_all();
     }
     __syncthreads();
     return *((volatile int *)status) == 0;
+}
+
+// VOps::maxAbs (vmath.cpp:100-136) with the reference's chunking, then the
+// stopping test: the value of a chunk is |r| at its last nonzero entry.  The
+// owner tile of each chunk's last unit row stored |r| there in chunk_val (or
+// -1 when it is zero, then the chunk is scanned backwards here).
+__device__ __forceinline__ bool chunk_converged(const PcgArgs<float> &a, const float *rn,
+                                                const TolTest &tt, int *s_flag)
+{
+    if (threadIdx.x < 32) {
+        const float *cv = reinterpret_cast<const float *>(a.chunk_val);
+        float mx = 0.f;
+        int has_min = 0;
+        for (int k = threadIdx.x; k < a.nchunks; k += 32) {
+            const long long start = k == 0 ? 0 : a.chunk_end[k - 1];
+            const int last = a.chunk_last_unit[k];
+            if (last < 0) {
+                has_min = 1;
+                continue;
+            }
+            float v = __ldcg(cv + k);
+            if (v < 0.f) {
+                long long idx = last - 1;
+                while (idx >= start && __ldcg(rn + idx) == 0.f) idx--;
+                if (idx >= start) {
+                    v = fabsf(__ldcg(rn + idx));
+                } else {
+                    has_min = 1;
+                    v = 0.f;
+                }
+            }
+            mx = fmaxf(mx, v);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
+        has_min = __any_sync(0xffffffffu, has_min);
+        if (threadIdx.x == 0) *s_flag = tol_met(tt, mx, has_min) ? 1 : 0;
+    }
+    __syncthreads();
+    const int f = *s_flag;
+    __syncthreads();
+    return f != 0;
 }
 
 // wait for the current TMA load batch (bounded)
@@ -222,8 +332,8 @@ __global__ void __launch_bounds__(kThreads, 1)
 k_pcg_tma(PcgArgs<float> a, const __grid_constant__ TmaMaps m, int ti, int tj)
 {
     extern __shared__ unsigned char smem_dyn[];
-    __shared__ double sm[40];
-    __shared__ double s_err;
+    __shared__ float2 sm[40];
+    __shared__ int s_flag;
     __shared__ __align__(8) unsigned long long bar;
     if (a.mode == 1 && *a.wrap_flag == 0) return;
     if (a.mode == 2 && *a.wrap_flag != 0) return;
@@ -241,7 +351,10 @@ k_pcg_tma(PcgArgs<float> a, const __grid_constant__ TmaMaps m, int ti, int tj)
     const int tiles_j = (NJ + tj - 1) / tj, tiles_i = (NI + ti - 1) / ti;
     const int ntiles = tiles_i * tiles_j;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    double *pA = a.partials, *pB = a.partials + G, *pC = a.partials + 2 * G;
+    float2 *pA = reinterpret_cast<float2 *>(a.partials), *pB = pA + G, *pC = pA + 2 * G;
+    const TolTest tt = tol_test(a.tol);
+    // 1e-8 added to the denominator of alpha, as a float pair
+    const float2 eps8 = make_float2((float)1e-8, (float)(1e-8 - (double)(float)1e-8));
     const unsigned box_f = (unsigned)(L.h2 * L.wr * 4), box_i = (unsigned)(L.h2 * L.wi);
     const unsigned box_x = (unsigned)(ti * tj * 4);
 
@@ -271,16 +384,16 @@ k_pcg_tma(PcgArgs<float> a, const __grid_constant__ TmaMaps m, int ti, int tj)
             bb = fmaf(bv, bv, bb);
             nz |= fabsf(bv) > 1.0e-15f;
         }
-        const double part = bsum(bb, sm);
+        const float2 part = bsum(bb, sm);
         const int anynz = __syncthreads_or(nz);
         if (threadIdx.x == 0) {
             pA[blockIdx.x] = part;
-            pC[blockIdx.x] = anynz ? 1.0 : 0.0;
+            pC[blockIdx.x] = make_float2(anynz ? 1.f : 0.f, 0.f);
         }
     }
     if (!gsync(a.bar, G, a.status)) return;
-    double sigma = psum(pA, G, sm);
-    if (psum(pC, G, sm) == 0.0) {
+    float2 sigma = psum(pA, G, sm);
+    if (psum(pC, G, sm).x == 0.f) {
         // the reference leaves result at zero
         for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < a.N;
              c += (long long)G * blockDim.x)
@@ -289,7 +402,7 @@ k_pcg_tma(PcgArgs<float> a, const __grid_constant__ TmaMaps m, int ti, int tj)
         return;
     }
 
-    double beta = 0.0;
+    float fb = 0.f;
     int result = a.iter_limit;
     for (int it = 0; it < a.iter_limit; it++) {
         const bool first = it == 0;
@@ -300,7 +413,6 @@ k_pcg_tma(PcgArgs<float> a, const __grid_constant__ TmaMaps m, int ti, int tj)
         const CUtensorMap *ms_prev = it == 1 ? &m.b : ((it & 1) ? &m.s0 : &m.s1);
         const CUtensorMap *ms_cur_st = (it & 1) ? &m.s1_st : &m.s0_st;
         const CUtensorMap *mr_next_st = (it & 1) ? &m.r0_st : &m.r1_st;
-        const float fb = (float)beta;
 
         // ---- sweep 1: s = M r + beta s_prev on the halo, q = A s, q.s ----
         float qs = 0.f;
@@ -374,12 +486,11 @@ k_pcg_tma(PcgArgs<float> a, const __grid_constant__ TmaMaps m, int ti, int tj)
             __syncthreads();
         }
         {
-            const double part = bsum(qs, sm);
+            const float2 part = bsum(qs, sm);
             if (threadIdx.x == 0) pA[blockIdx.x] = part;
         }
         if (!gsync(a.bar, G, a.status)) return;
-        const double alpha = sigma / (psum(pA, G, sm) + 1e-8);
-        const float fa = (float)alpha;
+        const float fa = ff_div(sigma, ff_add(psum(pA, G, sm), eps8));
 
         // ---- sweep 2: r' = r - alpha A s on the halo, z = M r', x += alpha s
         float zr = 0.f;
@@ -457,49 +568,22 @@ k_pcg_tma(PcgArgs<float> a, const __grid_constant__ TmaMaps m, int ti, int tj)
                 const int gi = idx / NJ, gj = idx - gi * NJ;
                 if (gi < ti0 || gi >= ti0 + ti || gj < tj0 || gj >= tj0 + tj) continue;
                 const float v = ST[(gi - ti0) * tj + (gj - tj0)];
-                a.chunk_val[k] = v != 0.f ? fabs((double)v) : -1.0;
+                reinterpret_cast<float *>(a.chunk_val)[k] = v != 0.f ? fabsf(v) : -1.f;
             }
             __syncthreads();
         }
         {
-            const double part = bsum(zr, sm);
+            const float2 part = bsum(zr, sm);
             if (threadIdx.x == 0) pB[blockIdx.x] = part;
         }
         if (!gsync(a.bar, G, a.status)) return;
         const float *rn = (it & 1) ? a.r0 : a.r1;
-        if (threadIdx.x < 32) {
-            double mx = 0.0;
-            for (int k = threadIdx.x; k < a.nchunks; k += 32) {
-                const long long start = k == 0 ? 0 : a.chunk_end[k - 1];
-                const int last = a.chunk_last_unit[k];
-                double v;
-                if (last < 0) {
-                    v = DBL_MIN;
-                } else {
-                    v = ((volatile double *)a.chunk_val)[k];
-                    if (v < 0.0) {
-                        long long idx = last - 1;
-                        while (idx >= start && ((volatile const float *)rn)[idx] == 0.f) idx--;
-                        v = idx >= start ? fabs((double)((volatile const float *)rn)[idx]) : DBL_MIN;
-                    }
-                }
-                if (v > mx) mx = v;
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const double t = __shfl_down_sync(0xffffffffu, mx, o);
-                if (t > mx) mx = t;
-            }
-            if (threadIdx.x == 0) s_err = mx;
-        }
-        __syncthreads();
-        const double err = s_err;
-        const double newSigma = psum(pB, G, sm);
-        if (err <= a.tol) {
+        const float2 newSigma = psum(pB, G, sm);
+        if (chunk_converged(a, rn, tt, &s_flag)) {
             result = it;
             break;
         }
-        beta = newSigma / sigma;
+        fb = ff_div(newSigma, sigma);
         sigma = newSigma;
     }
     if (threadIdx.x == 0) bulk_wait_all();
@@ -584,8 +668,8 @@ __global__ void __launch_bounds__(kThreads, 1)
 k_pcg_resident(PcgArgs<float> a, int ti, int tj)
 {
     extern __shared__ unsigned char smem_dyn[];
-    __shared__ double sm[40];
-    __shared__ double s_err;
+    __shared__ float2 sm[40];
+    __shared__ int s_flag;
     __shared__ float inv[8];
     if (a.mode == 1 && *a.wrap_flag == 0) return;
     if (a.mode == 2 && *a.wrap_flag != 0) return;
@@ -602,7 +686,10 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     const int ti0 = ((int)blockIdx.x / tiles_j) * ti, tj0 = ((int)blockIdx.x % tiles_j) * tj;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int w2 = L.w2, w1 = L.w1;
-    double *pA = a.partials, *pB = a.partials + G, *pC = a.partials + 2 * G;
+    float2 *pA = reinterpret_cast<float2 *>(a.partials), *pB = pA + G, *pC = pA + 2 * G;
+    const TolTest tt = tol_test(a.tol);
+    // 1e-8 added to the denominator of alpha, as a float pair
+    const float2 eps8 = make_float2((float)1e-8, (float)(1e-8 - (double)(float)1e-8));
 
     const double scale_d = (double)a.sc->dt / (a.density * a.dx * a.dx);
     const float scale = (float)scale_d;
@@ -631,24 +718,23 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     }
     for (int e = threadIdx.x; e < ti * tj; e += blockDim.x) Xt[e] = 0.f;
     {
-        const double part = bsum(bb, sm);
+        const float2 part = bsum(bb, sm);
         const int anynz = __syncthreads_or(nz);
         if (threadIdx.x == 0) {
             pA[blockIdx.x] = part;
-            pC[blockIdx.x] = anynz ? 1.0 : 0.0;
+            pC[blockIdx.x] = make_float2(anynz ? 1.f : 0.f, 0.f);
         }
     }
-    if (!gsync(a.bar, G, a.status)) return;
-    double sigma = psum(pA, G, sm);
-    const bool zero = psum(pC, G, sm) == 0.0;
+    if (!gsync(a.bar, G, a.status, false)) return;
+    float2 sigma = psum(pA, G, sm);
+    const bool zero = psum(pC, G, sm).x == 0.f;
 
-    double beta = 0.0;
+    float fb = 0.f;
     int result = zero ? 0 : a.iter_limit;
     for (int it = 0; !zero && it < a.iter_limit; it++) {
         const bool first = it == 0;
         float *s_pub = (it & 1) ? a.s1 : a.s0;       // s_it published here
         float *r_pub = (it & 1) ? a.r0 : a.r1;       // r_{it+1} published here
-        const float fb = (float)beta;
 
         // ---- sweep 1 -------------------------------------------------------
         if (!first) {
@@ -708,12 +794,11 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
             }
         }
         {
-            const double part = bsum(qs, sm);
+            const float2 part = bsum(qs, sm);
             if (threadIdx.x == 0) pA[blockIdx.x] = part;
         }
-        if (!gsync(a.bar, G, a.status)) return;
-        const double alpha = sigma / (psum(pA, G, sm) + 1e-8);
-        const float fa = (float)alpha;
+        if (!gsync(a.bar, G, a.status, false)) return;
+        const float fa = ff_div(sigma, ff_add(psum(pA, G, sm), eps8));
 
         // ---- sweep 2 -------------------------------------------------------
         if (!first) {
@@ -775,46 +860,19 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
             const int gi = idx / NJ, gj = idx - gi * NJ;
             if (gi < ti0 || gi >= ti0 + ti || gj < tj0 || gj >= tj0 + tj) continue;
             const float v = Rb[(gi - ti0 + 2) * w2 + (gj - tj0 + 2)];
-            a.chunk_val[k] = v != 0.f ? fabs((double)v) : -1.0;
+            reinterpret_cast<float *>(a.chunk_val)[k] = v != 0.f ? fabsf(v) : -1.f;
         }
         {
-            const double part = bsum(zr, sm);
+            const float2 part = bsum(zr, sm);
             if (threadIdx.x == 0) pB[blockIdx.x] = part;
         }
-        if (!gsync(a.bar, G, a.status)) return;
-        if (threadIdx.x < 32) {
-            double mx = 0.0;
-            for (int k = threadIdx.x; k < a.nchunks; k += 32) {
-                const long long start = k == 0 ? 0 : a.chunk_end[k - 1];
-                const int last = a.chunk_last_unit[k];
-                double v;
-                if (last < 0) {
-                    v = DBL_MIN;
-                } else {
-                    v = ((volatile double *)a.chunk_val)[k];
-                    if (v < 0.0) {
-                        long long idx = last - 1;
-                        while (idx >= start && ((volatile const float *)r_pub)[idx] == 0.f) idx--;
-                        v = idx >= start ? fabs((double)((volatile const float *)r_pub)[idx]) : DBL_MIN;
-                    }
-                }
-                if (v > mx) mx = v;
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const double t2 = __shfl_down_sync(0xffffffffu, mx, o);
-                if (t2 > mx) mx = t2;
-            }
-            if (threadIdx.x == 0) s_err = mx;
-        }
-        __syncthreads();
-        const double err = s_err;
-        const double newSigma = psum(pB, G, sm);
-        if (err <= a.tol) {
+        if (!gsync(a.bar, G, a.status, false)) return;
+        const float2 newSigma = psum(pB, G, sm);
+        if (chunk_converged(a, r_pub, tt, &s_flag)) {
             result = it;
             break;
         }
-        beta = newSigma / sigma;
+        fb = ff_div(newSigma, sigma);
         sigma = newSigma;
     }
     // the solution leaves shared memory once
@@ -865,13 +923,10 @@ static bool encode(CUtensorMap *map, const void *ptr, CUtensorMapDataType dt, in
 
 static int sm_count()
 {
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    }
-    return sms;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms > 0 ? sms : 1;
 }
 
 constexpr int kMaxTmaCells = 54 * 128;
@@ -950,19 +1005,16 @@ bool resident_tile_shape(int ni, int nj, int *ti, int *tj)
 cudaError_t launch_pcg_resident(const PcgArgs<float> &a, int ti, int tj, cudaStream_t st)
 {
     const ResLayout L = res_layout(ti, tj);
-    static size_t configured = 0;
-    if (L.bytes > configured) {
-        cudaError_t e = cudaFuncSetAttribute((const void *)k_pcg_resident,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)kMaxResidentSmem + 256);
-        if (e != cudaSuccess) return e;
-        configured = kMaxResidentSmem + 256;
-    }
+    // the attribute is per device; setting it costs a few microseconds
+    cudaError_t e = cudaFuncSetAttribute((const void *)k_pcg_resident,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)L.bytes);
+    if (e != cudaSuccess) return e;
     const int grid = ((a.ni + ti - 1) / ti) * ((a.nj + tj - 1) / tj);
     PcgArgs<float> args = a;
     int vti = ti, vtj = tj;
     void *kargs[] = {&args, &vti, &vtj};
-    cudaError_t e = cudaMemsetAsync(args.bar, 0, sizeof(GridBarrier), st);
+    e = cudaMemsetAsync(args.bar, 0, sizeof(GridBarrier), st);
     if (e != cudaSuccess) return e;
     return cudaLaunchCooperativeKernel((const void *)k_pcg_resident, dim3(grid), dim3(kThreads),
                                        kargs, L.bytes, st);
@@ -972,14 +1024,10 @@ cudaError_t launch_pcg_tma(const PcgArgs<float> &a, const TmaMaps &maps, int ti,
                            cudaStream_t st)
 {
     const SmemLayout L = smem_layout(ti, tj);
-    static size_t configured = 0;
-    if (L.bytes > configured) {
-        cudaError_t e = cudaFuncSetAttribute((const void *)k_pcg_tma,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)L.bytes);
-        if (e != cudaSuccess) return e;
-        configured = L.bytes;
-    }
+    cudaError_t e = cudaFuncSetAttribute((const void *)k_pcg_tma,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)L.bytes);
+    if (e != cudaSuccess) return e;
     const long long ntiles = (long long)((a.ni + ti - 1) / ti) * ((a.nj + tj - 1) / tj);
     const long long tpb = (ntiles + sm_count() - 1) / sm_count();
     const int grid = (int)((ntiles + tpb - 1) / tpb);
@@ -987,7 +1035,7 @@ cudaError_t launch_pcg_tma(const PcgArgs<float> &a, const TmaMaps &maps, int ti,
     TmaMaps mm = maps;
     int vti = ti, vtj = tj;
     void *kargs[] = {&args, &mm, &vti, &vtj};
-    cudaError_t e = cudaMemsetAsync(args.bar, 0, sizeof(GridBarrier), st);
+    e = cudaMemsetAsync(args.bar, 0, sizeof(GridBarrier), st);
     if (e != cudaSuccess) return e;
     return cudaLaunchCooperativeKernel((const void *)k_pcg_tma, dim3(grid), dim3(kThreads), kargs,
                                        L.bytes, st);
