@@ -188,7 +188,11 @@ struct fs_solver {
     int density_iters_max = 0, pressure_iters_max = 0, substeps = 0;
     bool timers = false;
     double t_step_ms = 0.0, t_pcg_ms = 0.0, launches = 0.0;
-    cudaEvent_t e0 = nullptr, e1 = nullptr, p0 = nullptr, p1 = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    // PCG timing events per solve of a substep (0 density, 1 pressure); read
+    // after the substep so that timing adds no host wait inside it
+    cudaEvent_t p0[2] = {nullptr, nullptr}, p1[2] = {nullptr, nullptr};
+    bool pcg_timed[2] = {false, false};
     std::vector<void *> allocs;
 };
 
@@ -374,7 +378,8 @@ extern "C" fs_status fs_create(const fs_params *p, const fs_exec_params *exec, f
         cudaEventCreateWithFlags(&s->ev_p2g, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&s->ev_levelset, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreate(&s->e0) != cudaSuccess || cudaEventCreate(&s->e1) != cudaSuccess ||
-        cudaEventCreate(&s->p0) != cudaSuccess || cudaEventCreate(&s->p1) != cudaSuccess)
+        cudaEventCreate(&s->p0[0]) != cudaSuccess || cudaEventCreate(&s->p1[0]) != cudaSuccess ||
+        cudaEventCreate(&s->p0[1]) != cudaSuccess || cudaEventCreate(&s->p1[1]) != cudaSuccess)
         return cleanup(fail(FS_ERR_CUDA, "fs_create: stream/event creation failed"));
     const size_t n = s->ncell;
     Grids &G = s->G;
@@ -429,7 +434,7 @@ extern "C" fs_status fs_create(const fs_params *p, const fs_exec_params *exec, f
     }
     s->pcg_grid = s->prec == FS_PCG_FP64 ? pcg_grid_size<double>((long long)n)
                                          : pcg_grid_size<float>((long long)n);
-    A(dalloc(s, &s->partials, (size_t)3 * s->pcg_grid + 8));
+    A(dalloc(s, &s->partials, (size_t)8 * s->pcg_grid + 16));
     A(dalloc(s, &s->bar, 1));
     if (s->prec == FS_PCG_FP32)
         s->resident = resident_tile_shape(d.ni, d.nj, &s->res_ti, &s->res_tj);
@@ -501,7 +506,7 @@ extern "C" fs_status fs_destroy(fs_solver *s)
     if (s->side) cudaStreamSynchronize(s->side);
     for (void *q : s->allocs) cudaFree(q);
     if (s->sc_host) cudaFreeHost(s->sc_host);
-    cudaEvent_t evs[] = {s->ev_p2g, s->ev_levelset, s->e0, s->e1, s->p0, s->p1};
+    cudaEvent_t evs[] = {s->ev_p2g, s->ev_levelset, s->e0, s->e1, s->p0[0], s->p1[0], s->p0[1], s->p1[1]};
     for (cudaEvent_t e : evs)
         if (e) cudaEventDestroy(e);
     if (s->st) cudaStreamDestroy(s->st);
@@ -711,7 +716,8 @@ template <typename T> static PcgArgs<T> pcg_args(fs_solver *s, const void *b, vo
 
 static fs_status run_pcg(fs_solver *s, const void *b, void *x, int *iters)
 {
-    if (s->timers) CK(cudaEventRecord(s->p0, s->st));
+    const int slot = b == s->dens_rhs ? 0 : 1;
+    if (s->timers) CK(cudaEventRecord(s->p0[slot], s->st));
     cudaError_t e;
     int launched = 0;
     if (s->prec == FS_PCG_FP64) {
@@ -735,11 +741,22 @@ static fs_status run_pcg(fs_solver *s, const void *b, void *x, int *iters)
     g_kernel_launches += launched;
     if (e != cudaSuccess) return fail(FS_ERR_CUDA, "PCG launch: %s", cudaGetErrorString(e));
     if (s->timers) {
-        CK(cudaEventRecord(s->p1, s->st));
-        CK(cudaEventSynchronize(s->p1));
+        CK(cudaEventRecord(s->p1[slot], s->st));
+        s->pcg_timed[slot] = true;
+    }
+    return FS_OK;
+}
+
+// adds the PCG times recorded since the last call (waits for them)
+static fs_status collect_pcg_timers(fs_solver *s)
+{
+    for (int k = 0; k < 2; k++) {
+        if (!s->pcg_timed[k]) continue;
+        CK(cudaEventSynchronize(s->p1[k]));
         float ms = 0.f;
-        CK(cudaEventElapsedTime(&ms, s->p0, s->p1));
+        CK(cudaEventElapsedTime(&ms, s->p0[k], s->p1[k]));
         s->t_pcg_ms += ms;
+        s->pcg_timed[k] = false;
     }
     return FS_OK;
 }
@@ -868,6 +885,7 @@ static fs_status step_impl(fs_solver *s)
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, s->e0, s->e1));
         s->t_step_ms += ms;
+        TRY(collect_pcg_timers(s));
     }
     return FS_OK;
 }
@@ -974,6 +992,7 @@ extern "C" fs_status fs_run_stage(fs_solver *s, int which)
     if (which == FS_STAGE_PROJECT) CK(cudaMemsetAsync(&s->sc->pressure_iters, 0, sizeof(int), s->st));
     TRY(stage(s, which, false));
     TRY(sync_all(s));
+    TRY(collect_pcg_timers(s));
     TRY(read_scalars(s));
     if (which == FS_STAGE_DENSITY) s->density_iters_max = s->sc_host->density_iters;
     if (which == FS_STAGE_PROJECT) s->pressure_iters_max = s->sc_host->pressure_iters;
@@ -1273,7 +1292,7 @@ static fs_status pcg_cache_get(int dev, size_t cells, size_t esz, int nchunks, P
     void **vs[] = {&c.b, &c.x, &c.r0, &c.r1, &c.s0, &c.s1};
     for (void **v : vs) CK(cudaMalloc(v, cells * esz));
     int maxgrid = std::max(pcg_grid_size<double>(1LL << 40), pcg_grid_size<float>(1LL << 40));
-    CK(cudaMalloc(&c.partials, (size_t)(3 * maxgrid + 8) * sizeof(double)));
+    CK(cudaMalloc(&c.partials, (size_t)(8 * maxgrid + 16) * sizeof(double)));
     CK(cudaMalloc(&c.chunk_end, (size_t)c.chunk_cap * sizeof(int)));
     CK(cudaMalloc(&c.chunk_last, (size_t)c.chunk_cap * sizeof(int)));
     CK(cudaMalloc(&c.chunk_val, (size_t)c.chunk_cap * sizeof(double)));

@@ -21,7 +21,7 @@ template <typename T> struct PcgArgs {
     const T *b;                // right-hand side
     T *x;                      // solution
     T *r0, *r1, *s0, *s1;      // ping-pong work vectors
-    double *partials;          // 3 * grid doubles
+    double *partials;          // 8 * grid + 16 doubles (per-block partials, epoch flags)
     const int *chunk_end;      // splitRange chunk ends (exclusive)
     const int *chunk_last_unit;// last unit row per chunk or -1
     double *chunk_val;         // per chunk |r| at its last unit row (scratch)

@@ -601,9 +601,12 @@ k_pcg_tma(PcgArgs<float> a, const __grid_constant__ TmaMaps m, int ti, int tj)
 // ---------------------------------------------------------------------------
 struct ResLayout {
     int ti, tj, w2, h2, w1, h1;
-    size_t off_rb, off_sb, off_ib, off_b1, off_xt, bytes;
+    size_t off_rb, off_sb, off_b1, off_xt, off_op, bytes;
 };
 
+// r and s with a 2-cell halo (h2 x w2), the sweep results on the tile and a
+// 1-cell halo (h1 x w1), x on the tile, and a packed operator word per
+// tile-plus-1-halo cell
 __host__ __device__ inline ResLayout res_layout(int ti, int tj)
 {
     ResLayout L;
@@ -622,8 +625,8 @@ __host__ __device__ inline ResLayout res_layout(int ti, int tj)
     o = a128(o + (size_t)L.h1 * L.w1 * 4);
     L.off_xt = o;
     o = a128(o + (size_t)ti * tj * 4);
-    L.off_ib = o;
-    o = a128(o + (size_t)L.h2 * L.w2);
+    L.off_op = o;
+    o = a128(o + (size_t)L.h1 * L.w1 * 4);
     L.bytes = o + 128;
     return L;
 }
@@ -659,18 +662,122 @@ __device__ __forceinline__ void load_ring(float *dst, const float *__restrict__ 
         ring_cell(k, ti, tj, r, q);
         const int gi = ti0 + r, gj = tj0 + q;
         float v = 0.f;
-        if (gi >= 0 && gi < NI && gj >= 0 && gj < NJ) v = ((volatile const float *)src)[(size_t)gi * NJ + gj];
+        if (gi >= 0 && gi < NI && gj >= 0 && gj < NJ) v = __ldcg(src + (size_t)gi * NJ + gj);
         dst[(r + 2) * w2 + (q + 2)] = v;
     }
 }
 
+// byte offset of the per-block epoch flags inside the partials buffer of the
+// resident kernel: after G float4 records and G float2 pairs, 32-byte aligned
+__host__ __device__ inline size_t res_flags_offset(int G)
+{
+    return ((size_t)G * 24 + 31) & ~(size_t)31;
+}
+
+// float-pair accumulation without renormalising: hi carries the running
+// sum, lo the rounding errors of the additions and the low parts
+__device__ __forceinline__ float2 ff_acc(float2 a, float2 b)
+{
+    float s, e;
+    two_sum(a.x, b.x, s, e);
+    return make_float2(s, (a.y + b.y) + e);
+}
+__device__ __forceinline__ float2 ff_norm(float2 a)
+{
+    const float h = a.x + a.y;
+    return make_float2(h, a.y - (h - a.x));
+}
+
+// Block sum of per-thread FP32 partials as a float pair, valid in thread 0
+// only.  The caller orders the next use of sm (64 floats) with a block
+// barrier.  (Plain float sums inside the warps were measured to let the
+// unconverged 200-iteration solves drift visibly further from FP64.)
+__device__ __forceinline__ float2 bsum0(float v, float *sm)
+{
+    float2 a0 = make_float2(v, 0.f);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a0 = ff_acc(a0, ff_shfl_down(a0, o));
+    a0 = ff_norm(a0);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) {
+        sm[2 * w] = a0.x;
+        sm[2 * w + 1] = a0.y;
+    }
+    __syncthreads();
+    float2 x = make_float2(0.f, 0.f);
+    if (w == 0) {
+        x = lane < (int)(blockDim.x >> 5) ? make_float2(sm[2 * lane], sm[2 * lane + 1])
+                                          : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x = ff_acc(x, ff_shfl_down(x, o));
+        x = ff_norm(x);
+    }
+    return x;
+}
+
+__device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned *p)
+{
+    unsigned v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed_u32(unsigned *p, unsigned v)
+{
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void red_relaxed_add(unsigned *p, unsigned v)
+{
+    asm volatile("red.relaxed.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+
+// Bounded spin of one thread until *p >= target (acquire); false on timeout
+// or when another block reported one.
+__device__ __forceinline__ bool spin_until(const unsigned *p, unsigned target, int *status)
+{
+    long long spins = 0;
+    while ((int)(ld_acquire_u32(p) - target) < 0) {
+        ++spins;
+        if (spins > kSpinLimit || ((spins & 1023) == 0 && *((volatile int *)status) != 0)) {
+            atomicExch(status, 1);
+            return false;
+        }
+    }
+    return true;
+}
+
+// Runs f(r, q) over the h1 x w1 tile-plus-1-halo region: warps take rows and
+// lanes the interior columns, then the two halo columns of every row go out
+// to all threads in one pass (instead of a nearly idle extra pass per row).
+template <typename F>
+__device__ __forceinline__ void for_halo1(int h1, int w1, F f)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int r = warp; r < h1; r += nw)
+        for (int q = lane + 1; q < w1 - 1; q += 32) f(r, q);
+    for (int k = threadIdx.x; k < 2 * h1; k += blockDim.x) f(k >> 1, (k & 1) ? w1 - 1 : 0);
+}
+
+// ---------------------------------------------------------------------------
+// The resident kernel.  Synchronisation, all by thread 0 of a block after a
+// block barrier:
+//  * a grid barrier is a monotonic arrival counter: fence.acq_rel, then a
+//    relaxed reduction-add (fire and forget); barrier k is complete when the
+//    counter reads G k (acquire).  The counter is zeroed at launch.
+//  * a block publishes each vector it stores with an epoch flag (relaxed
+//    store after the same fence); neighbours whose halo ring reads that
+//    vector wait for the flag instead of the grid barrier.
+// Iteration it publishes s_it as epoch 2 it + 1 and r_{it+1} as 2 it + 2.
+// ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kThreads, 1)
 k_pcg_resident(PcgArgs<float> a, int ti, int tj)
 {
     extern __shared__ unsigned char smem_dyn[];
-    __shared__ float2 sm[40];
+    __shared__ float smf[64];
+    __shared__ float4 s_bcast;
     __shared__ int s_flag;
     __shared__ float inv[8];
+    __shared__ int s_cmax, s_cscan;
     if (a.mode == 1 && *a.wrap_flag == 0) return;
     if (a.mode == 2 && *a.wrap_flag != 0) return;
     unsigned char *base = reinterpret_cast<unsigned char *>(((size_t)smem_dyn + 127) & ~(size_t)127);
@@ -679,16 +786,26 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     float *Sb = reinterpret_cast<float *>(base + L.off_sb);
     float *B1 = reinterpret_cast<float *>(base + L.off_b1);
     float *Xt = reinterpret_cast<float *>(base + L.off_xt);
-    uint8_t *Ib = base + L.off_ib;
+    unsigned *Op = reinterpret_cast<unsigned *>(base + L.off_op);
     const int NI = a.ni, NJ = a.nj;
     const int G = gridDim.x;
-    const int tiles_j = (NJ + tj - 1) / tj;
+    const int tiles_j = (NJ + tj - 1) / tj, tiles_i = (NI + ti - 1) / ti;
     const int ti0 = ((int)blockIdx.x / tiles_j) * ti, tj0 = ((int)blockIdx.x % tiles_j) * tj;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int w2 = L.w2, w1 = L.w1;
-    float2 *pA = reinterpret_cast<float2 *>(a.partials), *pB = pA + G, *pC = pA + 2 * G;
+    const int w2 = L.w2, w1 = L.w1, h1 = L.h1;
+    // partials: z.r records (float4), then the s.As pairs (float2); the
+    // zero test of b uses the record area before the first iteration; then
+    // the epoch flags, one 32-byte sector per block (zeroed at launch)
+    float4 *pB = reinterpret_cast<float4 *>(a.partials);
+    float2 *pA = reinterpret_cast<float2 *>(pB + G), *pC = reinterpret_cast<float2 *>(pB);
+    unsigned *flags =
+        reinterpret_cast<unsigned *>(reinterpret_cast<unsigned char *>(a.partials) + res_flags_offset(G));
+    unsigned *count = &a.bar->count;
+    unsigned barriers = 0; // grid barriers arrived at so far
+    // chunks without a unit row report DBL_MIN (VOps::maxAbs) on every iteration
+    int has_min_static = 0;
+    for (int k = 0; k < a.nchunks; k++) has_min_static |= a.chunk_last_unit[k] < 0;
     const TolTest tt = tol_test(a.tol);
-    // 1e-8 added to the denominator of alpha, as a float pair
     const float2 eps8 = make_float2((float)1e-8, (float)(1e-8 - (double)(float)1e-8));
 
     const double scale_d = (double)a.sc->dt / (a.density * a.dx * a.dx);
@@ -696,7 +813,57 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     if (threadIdx.x < 8)
         inv[threadIdx.x] = (threadIdx.x >= 1 && threadIdx.x <= 4) ? (float)(1.0 / (threadIdx.x * scale_d)) : 0.f;
 
-    // load the operator rows and r_0 = s_0 = b with their halo; x = 0
+    // thread 0, after the block barrier: publish an epoch (0: none) and
+    // arrive at the next grid barrier
+    auto arrive = [&](unsigned epoch) {
+        barriers++;
+        if (threadIdx.x == 0) {
+            fence_acq_rel_gpu();
+            if (epoch) st_relaxed_u32(flags + 8 * blockIdx.x, epoch);
+            red_relaxed_add(count, 1u);
+        }
+    };
+    // completes the last grid barrier and sums the blocks' float2 partials
+    // (or float4 records: pair sum, max, max) in a fixed order, so every
+    // block obtains the same scalars; the result is in every thread
+    auto wait_sum = [&](const void *parts, bool rec4) -> float4 {
+        if (warp == 0) {
+            bool ok = true;
+            if (lane == 0) ok = spin_until(count, barriers * (unsigned)G, a.status);
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            float2 acc = make_float2(0.f, 0.f);
+            float mx = 0.f, sc = 0.f;
+            if (ok) {
+                for (int k = lane; k < G; k += 32) {
+                    if (rec4) {
+                        const float4 v = __ldcg(reinterpret_cast<const float4 *>(parts) + k);
+                        acc = ff_acc(acc, make_float2(v.x, v.y));
+                        mx = fmaxf(mx, v.z);
+                        sc = fmaxf(sc, v.w);
+                    } else {
+                        acc = ff_acc(acc, __ldcg(reinterpret_cast<const float2 *>(parts) + k));
+                    }
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                acc = ff_acc(acc, ff_shfl_down(acc, o));
+                mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
+                sc = fmaxf(sc, __shfl_down_sync(0xffffffffu, sc, o));
+            }
+            if (lane == 0) {
+                acc = ff_norm(acc);
+                s_bcast = make_float4(acc.x, acc.y, mx, sc);
+            }
+        }
+        __syncthreads();
+        return s_bcast;
+    };
+    auto ok = [&]() { return *((volatile int *)a.status) == 0; };
+
+    // load the operator rows (bytes, into B1 for now) and r_0 = s_0 = b with
+    // their halo; x = 0
+    uint8_t *Ib = reinterpret_cast<uint8_t *>(B1); // h2*w2 bytes fit in h1*w1 floats
     float bb = 0.f;
     int nz = 0;
     for (int r = warp; r < L.h2; r += nw) {
@@ -717,56 +884,126 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
         }
     }
     for (int e = threadIdx.x; e < ti * tj; e += blockDim.x) Xt[e] = 0.f;
+    __syncthreads();
+    // packed operator word of each tile-plus-1-halo cell: its own row byte
+    // (bits 0-7) and the cell counts of its four neighbours (3 bits each:
+    // i-1 at 8, i+1 at 11, j-1 at 14, j+1 at 17), which select the IPP
+    // coefficients
+    for (int e = threadIdx.x; e < h1 * w1; e += blockDim.x) {
+        const int r = e / w1, q = e - r * w1;
+        const int c2 = (r + 1) * w2 + (q + 1);
+        Op[e] = (unsigned)Ib[c2] | ((unsigned)((Ib[c2 - w2] >> 4) & 7) << 8) |
+                ((unsigned)((Ib[c2 + w2] >> 4) & 7) << 11) |
+                ((unsigned)((Ib[c2 - 1] >> 4) & 7) << 14) | ((unsigned)((Ib[c2 + 1] >> 4) & 7) << 17);
+    }
+    float sigma_hi, sigma_lo;
+    bool zero;
     {
-        const float2 part = bsum(bb, sm);
+        const float2 part = bsum0(bb, smf); // its block barrier also retires Ib
         const int anynz = __syncthreads_or(nz);
         if (threadIdx.x == 0) {
             pA[blockIdx.x] = part;
             pC[blockIdx.x] = make_float2(anynz ? 1.f : 0.f, 0.f);
         }
+        __syncthreads();
+        arrive(0u);
+        const float4 s0 = wait_sum(pA, false);
+        if (!ok()) return;
+        sigma_hi = s0.x;
+        sigma_lo = s0.y;
+        __syncthreads(); // everyone has read the broadcast slot
+        zero = wait_sum(pC, false).x == 0.f; // same barrier, already complete
     }
-    if (!gsync(a.bar, G, a.status, false)) return;
-    float2 sigma = psum(pA, G, sm);
-    const bool zero = psum(pC, G, sm).x == 0.f;
+    float2 sigma = make_float2(sigma_hi, sigma_lo);
+
+    // neighbour tiles whose cells the 2-deep ring reads: threads 0..nn-1
+    // each watch one of them (at most 5 rows x 3 columns of tiles)
+    const int bi_lo = ti0 - 2 < 0 ? 0 : (ti0 - 2) / ti;
+    const int bi_hi = min(tiles_i - 1, (ti0 + ti + 1) / ti);
+    const int bj_lo = tj0 - 2 < 0 ? 0 : (tj0 - 2) / tj;
+    const int bj_hi = min(tiles_j - 1, (tj0 + tj + 1) / tj);
+    const int ncols = bj_hi - bj_lo + 1;
+    const int nn = (bi_hi - bi_lo + 1) * ncols;
+    const unsigned *watch = nullptr;
+    if ((int)threadIdx.x < nn)
+        watch = flags + 8 * ((bi_lo + (int)threadIdx.x / ncols) * tiles_j + bj_lo + (int)threadIdx.x % ncols);
+    auto wait_neighbours = [&](unsigned epoch) -> bool {
+        if (watch) spin_until(watch, epoch, a.status);
+        __syncthreads();
+        return ok();
+    };
+
+    // z = M v at a cell with operator word p, v centred at c in a row-major
+    // array of pitch w (IncompletePoissonPreconditioner, the reference's
+    // asymmetric rows); branch-free so that tiles cost the same whatever
+    // their fluid fraction
+    auto precond = [&](unsigned p, const float *v, int c, int w) -> float {
+        const float iNeg = inv[(p >> 8) & 7];
+        const float iPos = inv[(p >> 11) & 7];
+        const float jNeg = inv[(p >> 14) & 7];
+        const float jPos = inv[(p >> 17) & 7];
+        const float vc = v[c];
+        const float diag = (1.f + iNeg * iNeg) + jNeg * jNeg;
+        float acc = diag * vc;
+        acc = fmaf(jNeg, v[c - 1], acc);
+        acc = fmaf(jPos, v[c + 1], acc);
+        acc = fmaf(iNeg, v[c - w], acc);
+        acc = fmaf(iPos, v[c + w], acc);
+        return (p & 0x80) ? acc : vc;
+    };
+    // (A v) at a cell with operator word p (the pressure matrix row)
+    auto apply_a = [&](unsigned p, const float *v, int c, int w) -> float {
+        const float vc = v[c];
+        float nb = (p & 1) ? v[c - w] : 0.f;
+        nb += (p & 2) ? v[c + w] : 0.f;
+        nb += (p & 4) ? v[c - 1] : 0.f;
+        nb += (p & 8) ? v[c + 1] : 0.f;
+        const float av = scale * ((float)((p >> 4) & 7) * vc - nb);
+        return (p & 0x80) ? av : vc;
+    };
 
     float fb = 0.f;
     int result = zero ? 0 : a.iter_limit;
-    for (int it = 0; !zero && it < a.iter_limit; it++) {
+    for (int it = 0; !zero && a.iter_limit > 0; it++) {
         const bool first = it == 0;
-        float *s_pub = (it & 1) ? a.s1 : a.s0;       // s_it published here
-        float *r_pub = (it & 1) ? a.r0 : a.r1;       // r_{it+1} published here
+        float *s_pub = (it & 1) ? a.s1 : a.s0; // s_it published here
+        float *r_pub = (it & 1) ? a.r0 : a.r1; // r_{it+1} published here
 
         // ---- sweep 1 -------------------------------------------------------
         if (!first) {
-            // neighbours' r_it (published last sweep 2) around the tile
-            load_ring(Rb, (it & 1) ? a.r1 : a.r0, ti0, tj0, ti, tj, NI, NJ);
-            __syncthreads();
-        }
-        // s_it on the tile and its 1-halo into B1
-        for (int r = warp; r < L.h1; r += nw) {
-            for (int q = lane; q < w1; q += 32) {
-                const int c2 = (r + 1) * w2 + (q + 1);
-                float s = Sb[c2];
-                if (!first) {
-                    const uint8_t ic = Ib[c2];
-                    float z = Rb[c2];
-                    if (ic & 0x80) {
-                        const float iNeg = inv[(Ib[c2 - w2] >> 4) & 7];
-                        const float iPos = inv[(Ib[c2 + w2] >> 4) & 7];
-                        const float jNeg = inv[(Ib[c2 - 1] >> 4) & 7];
-                        const float jPos = inv[(Ib[c2 + 1] >> 4) & 7];
-                        const float diag = (1.f + iNeg * iNeg) + jNeg * jNeg;
-                        float acc = diag * z;
-                        acc = fmaf(jNeg, Rb[c2 - 1], acc);
-                        acc = fmaf(jPos, Rb[c2 + 1], acc);
-                        acc = fmaf(iNeg, Rb[c2 - w2], acc);
-                        acc = fmaf(iPos, Rb[c2 + w2], acc);
-                        z = acc;
-                    }
-                    s = fmaf(s, fb, z);
-                }
-                B1[r * w1 + q] = s;
+            const bool more = it < a.iter_limit;
+            if (more) {
+                // z_it = M r_it on the tile and its 1-halo while the grid
+                // barrier of the last sweep completes
+                if (!wait_neighbours(2u * it)) return;
+                load_ring(Rb, (it & 1) ? a.r1 : a.r0, ti0, tj0, ti, tj, NI, NJ);
+                __syncthreads();
+                for_halo1(h1, w1, [&](int r, int q) {
+                    B1[r * w1 + q] = precond(Op[r * w1 + q], Rb, (r + 1) * w2 + (q + 1), w2);
+                });
             }
+            // end of iteration it - 1: beta and the stopping test
+            const float4 rec = wait_sum(pB, true);
+            if (!ok()) return;
+            const float2 newSigma = make_float2(rec.x, rec.y);
+            // a zero at a chunk-end unit row needs the backward scan; otherwise
+            // the largest |r| over the blocks decides
+            const bool done = rec.w != 0.f
+                                  ? chunk_converged(a, (it & 1) ? a.r1 : a.r0, tt, &s_flag)
+                                  : tol_met(tt, rec.z, has_min_static);
+            if (done) {
+                result = it - 1;
+                break;
+            }
+            if (!more) break;
+            fb = ff_div(newSigma, sigma);
+            sigma = newSigma;
+            // s_it = z_it + beta s_{it-1}
+            for_halo1(h1, w1, [&](int r, int q) {
+                B1[r * w1 + q] = fmaf(Sb[(r + 1) * w2 + (q + 1)], fb, B1[r * w1 + q]);
+            });
+        } else {
+            for_halo1(h1, w1, [&](int r, int q) { B1[r * w1 + q] = Sb[(r + 1) * w2 + (q + 1)]; });
         }
         __syncthreads();
         float qs = 0.f;
@@ -775,18 +1012,8 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
             for (int q = lane; q < tj; q += 32) {
                 const int gj = tj0 + q;
                 const int c1 = (r + 1) * w1 + (q + 1);
-                const uint8_t ic = Ib[(r + 2) * w2 + (q + 2)];
                 const float s_c = B1[c1];
-                float qv = s_c;
-                if (ic & 0x80) {
-                    float nb = 0.f;
-                    if (ic & 1) nb += B1[c1 - w1];
-                    if (ic & 2) nb += B1[c1 + w1];
-                    if (ic & 4) nb += B1[c1 - 1];
-                    if (ic & 8) nb += B1[c1 + 1];
-                    qv = scale * ((float)((ic >> 4) & 7) * s_c - nb);
-                }
-                qs = fmaf(qv, s_c, qs);
+                qs = fmaf(apply_a(Op[c1], B1, c1, w1), s_c, qs);
                 if (!first) {
                     Sb[(r + 2) * w2 + (q + 2)] = s_c;
                     if (gi < NI && gj < NJ) s_pub[(size_t)gi * NJ + gj] = s_c;
@@ -794,34 +1021,33 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
             }
         }
         {
-            const float2 part = bsum(qs, sm);
-            if (threadIdx.x == 0) pA[blockIdx.x] = part;
+            const float2 part = bsum0(qs, smf);
+            if (threadIdx.x == 0) {
+                pA[blockIdx.x] = part;
+                s_cmax = 0;
+                s_cscan = 0;
+            }
         }
-        if (!gsync(a.bar, G, a.status, false)) return;
-        const float fa = ff_div(sigma, ff_add(psum(pA, G, sm), eps8));
+        __syncthreads();
+        arrive(first ? 0u : 2u * it + 1u);
 
         // ---- sweep 2 -------------------------------------------------------
         if (!first) {
+            if (!wait_neighbours(2u * it + 1u)) return;
             load_ring(Sb, s_pub, ti0, tj0, ti, tj, NI, NJ); // neighbours' s_it
             __syncthreads();
         }
-        for (int r = warp; r < L.h1; r += nw) {
-            for (int q = lane; q < w1; q += 32) {
-                const int c2 = (r + 1) * w2 + (q + 1);
-                const uint8_t ic = Ib[c2];
-                const float s_c = Sb[c2];
-                float qv = s_c;
-                if (ic & 0x80) {
-                    float nb = 0.f;
-                    if (ic & 1) nb += Sb[c2 - w2];
-                    if (ic & 2) nb += Sb[c2 + w2];
-                    if (ic & 4) nb += Sb[c2 - 1];
-                    if (ic & 8) nb += Sb[c2 + 1];
-                    qv = scale * ((float)((ic >> 4) & 7) * s_c - nb);
-                }
-                B1[r * w1 + q] = fmaf(-qv, fa, Rb[c2]);
-            }
-        }
+        // A s_it on the tile and its 1-halo while the grid barrier completes
+        for_halo1(h1, w1, [&](int r, int q) {
+            B1[r * w1 + q] = apply_a(Op[r * w1 + q], Sb, (r + 1) * w2 + (q + 1), w2);
+        });
+        const float4 qsum = wait_sum(pA, false);
+        if (!ok()) return;
+        const float fa = ff_div(sigma, ff_add(make_float2(qsum.x, qsum.y), eps8));
+        // r_{it+1} = r_it - alpha A s_it
+        for_halo1(h1, w1, [&](int r, int q) {
+            B1[r * w1 + q] = fmaf(-B1[r * w1 + q], fa, Rb[(r + 1) * w2 + (q + 1)]);
+        });
         __syncthreads();
         float zr = 0.f;
         for (int r = warp; r < ti; r += nw) {
@@ -830,30 +1056,15 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
                 const int gj = tj0 + q;
                 const int c1 = (r + 1) * w1 + (q + 1);
                 const int c2 = (r + 2) * w2 + (q + 2);
-                const uint8_t ic = Ib[c2];
                 const float r_c = B1[c1];
-                float z = r_c;
-                if (ic & 0x80) {
-                    const float iNeg = inv[(Ib[c2 - w2] >> 4) & 7];
-                    const float iPos = inv[(Ib[c2 + w2] >> 4) & 7];
-                    const float jNeg = inv[(Ib[c2 - 1] >> 4) & 7];
-                    const float jPos = inv[(Ib[c2 + 1] >> 4) & 7];
-                    const float diag = (1.f + iNeg * iNeg) + jNeg * jNeg;
-                    z = diag * r_c;
-                    z = fmaf(jNeg, B1[c1 - 1], z);
-                    z = fmaf(jPos, B1[c1 + 1], z);
-                    z = fmaf(iNeg, B1[c1 - w1], z);
-                    z = fmaf(iPos, B1[c1 + w1], z);
-                }
-                zr = fmaf(z, r_c, zr);
+                zr = fmaf(precond(Op[c1], B1, c1, w1), r_c, zr);
                 Xt[r * tj + q] = fmaf(Sb[c2], fa, Xt[r * tj + q]);
                 Rb[c2] = r_c;
                 if (gi < NI && gj < NJ) r_pub[(size_t)gi * NJ + gj] = r_c;
             }
         }
         __syncthreads();
-        // VOps::maxAbs (vmath.cpp:100-136) from the tile that owns each
-        // chunk's last unit row; -1 marks r' == 0 there
+        // |r_{it+1}| at each chunk's last unit row, from the tile holding it
         for (int k = threadIdx.x; k < a.nchunks; k += blockDim.x) {
             const int idx = a.chunk_last_unit[k];
             if (idx < 0) continue;
@@ -861,19 +1072,16 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
             if (gi < ti0 || gi >= ti0 + ti || gj < tj0 || gj >= tj0 + tj) continue;
             const float v = Rb[(gi - ti0 + 2) * w2 + (gj - tj0 + 2)];
             reinterpret_cast<float *>(a.chunk_val)[k] = v != 0.f ? fabsf(v) : -1.f;
+            if (v != 0.f) atomicMax(&s_cmax, __float_as_int(fabsf(v))); // order of non-negative floats
+            else s_cscan = 1;
         }
         {
-            const float2 part = bsum(zr, sm);
-            if (threadIdx.x == 0) pB[blockIdx.x] = part;
+            const float2 part = bsum0(zr, smf); // its barrier also orders s_cmax / s_cscan
+            if (threadIdx.x == 0)
+                pB[blockIdx.x] = make_float4(part.x, part.y, __int_as_float(s_cmax), s_cscan ? 1.f : 0.f);
         }
-        if (!gsync(a.bar, G, a.status, false)) return;
-        const float2 newSigma = psum(pB, G, sm);
-        if (chunk_converged(a, r_pub, tt, &s_flag)) {
-            result = it;
-            break;
-        }
-        fb = ff_div(newSigma, sigma);
-        sigma = newSigma;
+        __syncthreads();
+        arrive(2u * it + 2u);
     }
     // the solution leaves shared memory once
     for (int r = warp; r < ti; r += nw) {
@@ -979,11 +1187,14 @@ bool tma_store_maps(TmaMaps *m, int ni, int nj, int ti, int tj, const float *r0,
            encode(&m->s1_st, s1, F, 4, ni, nj, tj, ti);
 }
 
-constexpr size_t kMaxResidentSmem = 200 * 1024;
+constexpr size_t kMaxResidentSmem = 220 * 1024;
 
 bool resident_tile_shape(int ni, int nj, int *ti, int *tj)
 {
+    // among tile widths 32..256, the shape with the fewest cells per block
+    // including the 1-halo it recomputes, with at most one tile per SM
     const int blocks = sm_count();
+    long long best = -1;
     for (int w = 32; w <= 256; w *= 2) {
         const long long tiles_j = (nj + w - 1) / w;
         if (tiles_j > blocks) continue;
@@ -993,13 +1204,15 @@ bool resident_tile_shape(int ni, int nj, int *ti, int *tj)
         const long long ntiles = ((ni + h - 1) / h) * tiles_j;
         if (ntiles > blocks) continue;
         if (res_layout((int)h, w).bytes > kMaxResidentSmem) continue;
-        // prefer the first width whose tiles fit; narrower tiles waste less
-        // on ragged right edges
-        *ti = (int)h;
-        *tj = w;
-        return true;
+        const long long cost = (h + 2) * (w + 2);
+        if (best < 0 || cost < best) {
+            best = cost;
+            *ti = (int)h;
+            *tj = w;
+        }
+        if (w >= nj) break; // wider tiles only add empty columns
     }
-    return false;
+    return best >= 0;
 }
 
 cudaError_t launch_pcg_resident(const PcgArgs<float> &a, int ti, int tj, cudaStream_t st)
@@ -1015,6 +1228,9 @@ cudaError_t launch_pcg_resident(const PcgArgs<float> &a, int ti, int tj, cudaStr
     int vti = ti, vtj = tj;
     void *kargs[] = {&args, &vti, &vtj};
     e = cudaMemsetAsync(args.bar, 0, sizeof(GridBarrier), st);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(reinterpret_cast<unsigned char *>(args.partials) + res_flags_offset(grid), 0,
+                        (size_t)grid * 32, st);
     if (e != cudaSuccess) return e;
     return cudaLaunchCooperativeKernel((const void *)k_pcg_resident, dim3(grid), dim3(kThreads),
                                        kargs, L.bytes, st);
