@@ -1442,3 +1442,166 @@ extern "C" fs_status fs_pcg_solve_device(int ni, int nj, const int8_t *material_
     return pcg_solve_common(ni, nj, material_device, dt, density, dx, rhs_device, result_device,
                             iter_limit, tol, exec, iterations, c, prec);
 }
+
+// ---------------------------------------------------------------------------
+// fs_pcg_solve_device_noalloc: the FP32 device-pointer solve with all of its
+// scratch in one fixed device array (no counterpart in the reference).
+//
+// Some callers cannot allocate device memory once they are running: a
+// simulation or serving loop that reserved its whole device budget when it
+// started (a cudaMalloc there can fail), or one that cannot afford the device
+// synchronisation cudaMalloc and cudaFree may imply while its other streams
+// are busy.  This path calls neither, nor any other allocating routine; it
+// uses only the array below, which is part of the library's device image and
+// so exists, on every device the library is loaded on, before the first call.
+// Its cost for everyone is kNaBytes (about 4.7 MB) of device memory.
+//
+// Limit: ni * nj <= kNoAllocMaxCells (512 x 512 = 262144 cells), FP32 only,
+// at most kNoAllocMaxParts pool threads.  Larger requests are rejected before
+// any device work.
+//
+// The first call on a device looks up the array's address there
+// (cudaGetSymbolAddress, with that device current); make that first call
+// before any stream capture begins.  All calls use the same array and it keeps
+// whatever the last call left in it, so each call clears the words that must
+// start at zero (scalars, barrier counter, epoch flags) itself.  Two calls that
+// overlapped on the GPU would race on the array; this function holds a
+// process-wide lock and returns only after its solve has finished, so its own
+// calls never overlap.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr size_t kNoAllocMaxCells = 512 * 512;
+constexpr int kNoAllocMaxGrid = 4096;  // cooperative blocks the solve may use
+constexpr int kNoAllocMaxParts = 4096; // splitRange parts (pool threads)
+constexpr size_t na_up(size_t x) { return (x + 255) & ~(size_t)255; }
+constexpr size_t kNaInfo = 0;
+constexpr size_t kNaR0 = na_up(kNaInfo + kNoAllocMaxCells);
+constexpr size_t kNaR1 = na_up(kNaR0 + 4 * kNoAllocMaxCells);
+constexpr size_t kNaS0 = na_up(kNaR1 + 4 * kNoAllocMaxCells);
+constexpr size_t kNaS1 = na_up(kNaS0 + 4 * kNoAllocMaxCells);
+constexpr size_t kNaPartials = na_up(kNaS1 + 4 * kNoAllocMaxCells);
+constexpr size_t kNaChunkEnd = na_up(kNaPartials + 8 * (8 * (size_t)kNoAllocMaxGrid + 16));
+constexpr size_t kNaChunkLast = na_up(kNaChunkEnd + 4 * ((size_t)kNoAllocMaxParts + 1));
+constexpr size_t kNaChunkVal = na_up(kNaChunkLast + 4 * ((size_t)kNoAllocMaxParts + 1));
+constexpr size_t kNaBar = na_up(kNaChunkVal + 8 * ((size_t)kNoAllocMaxParts + 1));
+constexpr size_t kNaScalars = na_up(kNaBar + sizeof(GridBarrier));
+constexpr size_t kNaBytes = na_up(kNaScalars + sizeof(Scalars));
+} // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
+
+static std::mutex g_noalloc_mu;
+static unsigned char *g_noalloc_base[64]; // the array's address per device
+
+// splitRange chunk ends (the reference's partition of [0, N) into parts)
+__global__ void k_na_chunk_ends(int *ends, int parts, long long ps, long long rem)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < parts) ends[i] = (int)((long long)(i + 1) * ps + min((long long)(i + 1), rem));
+}
+
+extern "C" fs_status fs_pcg_solve_device_noalloc(int ni, int nj, const int8_t *material_device,
+                                                 float dt, double density, double dx,
+                                                 const float *rhs_device, float *result_device,
+                                                 int iter_limit, double tol,
+                                                 const fs_exec_params *exec, int *iterations)
+{
+    if (ni < 1 || nj < 1 || !material_device || !rhs_device || !result_device || iter_limit < 0)
+        return fail(FS_ERR_BAD_ARG, "fs_pcg_solve_device_noalloc: invalid argument");
+    const long long N = (long long)ni * nj;
+    if (N > (long long)kNoAllocMaxCells)
+        return fail(FS_ERR_BAD_ARG,
+                    "fs_pcg_solve_device_noalloc: %d x %d = %lld cells exceeds the fixed scratch "
+                    "maximum of %zu cells",
+                    ni, nj, N, kNoAllocMaxCells);
+    if (exec && exec->pcg_precision == FS_PCG_FP64)
+        return fail(FS_ERR_UNSUPPORTED, "fs_pcg_solve_device_noalloc: FP32 only");
+    const int dev = exec ? exec->device : 0;
+    if (dev < 0 || dev >= 64) return fail(FS_ERR_BAD_ARG, "fs_pcg_solve_device_noalloc: bad device");
+    const int T = (exec && exec->pool_threads > 0) ? exec->pool_threads : default_pool_threads();
+    const long long parts = std::max<long long>(1, std::min<long long>(T, N));
+    if (parts > kNoAllocMaxParts)
+        return fail(FS_ERR_BAD_ARG, "fs_pcg_solve_device_noalloc: %lld pool threads exceed %d", parts,
+                    kNoAllocMaxParts);
+
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    CK(cudaSetDevice(dev));
+    if (!g_noalloc_base[dev]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(FS_ERR_CUDA, "fs_pcg_solve_device_noalloc: cudaGetSymbolAddress: %s",
+                        cudaGetErrorString(e));
+        g_noalloc_base[dev] = static_cast<unsigned char *>(p);
+    }
+    if (pcg_grid_size<float>(N) > kNoAllocMaxGrid)
+        return fail(FS_ERR_UNSUPPORTED, "fs_pcg_solve_device_noalloc: device needs more than %d blocks",
+                    kNoAllocMaxGrid);
+    unsigned char *base = g_noalloc_base[dev];
+    uint8_t *info = base + kNaInfo;
+    int *chunk_end = reinterpret_cast<int *>(base + kNaChunkEnd);
+    int *chunk_last = reinterpret_cast<int *>(base + kNaChunkLast);
+    Scalars *sc = reinterpret_cast<Scalars *>(base + kNaScalars);
+    cudaStream_t st = 0;
+
+    long long ps = 1, rem = 0;
+    split_range_params(N, T, &ps, &rem);
+    // status, iteration count and wrap flag start at zero; the barrier words
+    // and epoch flags are zeroed by the PCG launchers
+    CK(cudaMemsetAsync(sc, 0, sizeof(Scalars), st));
+    k_na_chunk_ends<<<(unsigned)((parts + 255) / 256), 256, 0, st>>>(chunk_end, (int)parts, ps, rem);
+    k_set_dt<<<1, 1, 0, st>>>(sc, dt);
+    GridDims d{ni, nj, ni / 3 + (ni % 3 != 0), nj / 3 + (nj % 3 != 0)};
+    Grids G;
+    G.material = const_cast<int8_t *>(material_device);
+    G.cell_info = info;
+    launch_decomposition(d, G, chunk_last, (int)parts, ps, rem, sc, st);
+    g_kernel_launches += 3;
+
+    PcgArgs<float> a{};
+    a.ni = ni;
+    a.nj = nj;
+    a.N = N;
+    a.info = info;
+    a.b = rhs_device;
+    a.x = result_device;
+    a.r0 = reinterpret_cast<float *>(base + kNaR0);
+    a.r1 = reinterpret_cast<float *>(base + kNaR1);
+    a.s0 = reinterpret_cast<float *>(base + kNaS0);
+    a.s1 = reinterpret_cast<float *>(base + kNaS1);
+    a.partials = reinterpret_cast<double *>(base + kNaPartials);
+    a.chunk_end = chunk_end;
+    a.chunk_last_unit = chunk_last;
+    a.chunk_val = reinterpret_cast<double *>(base + kNaChunkVal);
+    a.nchunks = (int)parts;
+    a.sc = sc;
+    a.density = density;
+    a.dx = dx;
+    a.iter_limit = iter_limit;
+    a.tol = tol;
+    a.iters_out = &sc->density_iters;
+    a.status = &sc->pcg_status;
+    a.bar = reinterpret_cast<GridBarrier *>(base + kNaBar);
+    a.wrap_flag = &sc->wrap_units;
+    a.mode = 0;
+    cudaError_t e;
+    int launched = 0, ti = 0, tj = 0;
+    if (resident_tile_shape(ni, nj, &ti, &tj)) {
+        a.mode = 2; // the linear-index kernel takes over when a unit row wraps
+        e = launch_pcg_resident(a, ti, tj, st);
+        if (e == cudaSuccess) e = launch_pcg_linear_if_wrap(a, st);
+        launched = 2;
+    } else {
+        e = launch_pcg<float>(a, st, &launched);
+    }
+    g_kernel_launches += launched;
+    if (e != cudaSuccess)
+        return fail(FS_ERR_CUDA, "fs_pcg_solve_device_noalloc: PCG launch: %s", cudaGetErrorString(e));
+    Scalars h{};
+    CK(cudaMemcpyAsync(&h, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (h.pcg_status != 0)
+        return fail(FS_ERR_TIMEOUT, "fs_pcg_solve_device_noalloc: a PCG grid barrier wait timed out");
+    if (iterations) *iterations = h.density_iters;
+    return FS_OK;
+}

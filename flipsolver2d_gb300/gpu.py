@@ -21,6 +21,9 @@ LIB_PATH = os.path.join(HERE, "_build", "libfsgpu.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "fs_gpu.h")
 
 FS_OK = 0
+# fs_status codes (include/fs_gpu.h)
+FS_ERR_BAD_ARG, FS_ERR_CUDA, FS_ERR_OOM, FS_ERR_TIMEOUT, FS_ERR_UNSUPPORTED, FS_ERR_STATE = \
+    range(1, 7)
 FS_PCG_FP32, FS_PCG_FP64 = 0, 1
 
 # stage ids (FS_STAGE_*), identical to the oracle's
@@ -91,6 +94,11 @@ _SIGS = {
                                            ctypes.c_float, ctypes.c_double, ctypes.c_double,
                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                            ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_pcg_solve_device_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                                   ctypes.c_float, ctypes.c_double, ctypes.c_double,
+                                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                                   ctypes.c_double, ctypes.c_void_p,
+                                                   ctypes.c_void_p]),
 }
 
 

@@ -207,6 +207,28 @@ fs_status fs_pcg_solve_device(int ni, int nj, const int8_t *material_device, flo
                               void *result_device, int iter_limit, double tol,
                               const fs_exec_params *exec, int *iterations);
 
+/* fs_pcg_solve_device without any device allocation.  This entry point has
+ * no counterpart in the reference.  It is for callers that cannot allocate
+ * device memory while they run: a loop that reserved its whole device budget
+ * at start-up, or one that cannot take the device synchronisation that
+ * cudaMalloc / cudaFree may cause while its other streams are busy.  The
+ * solve (FP32 only; rhs and result are float arrays) uses one fixed scratch
+ * array compiled into the library instead of the growing cache.
+ * Limits: ni * nj <= 262144 cells (512 x 512) and at most 4096 pool threads;
+ * larger requests fail with FS_ERR_BAD_ARG before any device work, and
+ * pcg_precision FS_PCG_FP64 fails with FS_ERR_UNSUPPORTED.
+ * The first call on a device looks up the scratch array's address on that
+ * device; make that first call before any stream capture begins.  All calls
+ * share the array and it keeps what the last call left in it (each call
+ * clears what must start at zero).  Calls that overlapped on the GPU would
+ * race on it: the function holds a process-wide lock, runs on the legacy
+ * default stream and returns after its solve finished, so its own calls do
+ * not overlap. */
+fs_status fs_pcg_solve_device_noalloc(int ni, int nj, const int8_t *material_device, float dt,
+                                      double density, double dx, const float *rhs_device,
+                                      float *result_device, int iter_limit, double tol,
+                                      const fs_exec_params *exec, int *iterations);
+
 #ifdef __cplusplus
 }
 #endif
