@@ -31,6 +31,7 @@
 namespace fsg {
 
 constexpr int kThreads = 1024;
+constexpr int kStripThreads = 512; // resident kernel with register strips: 128 registers a thread
 constexpr long long kSpinLimit = 1LL << 25; // a few seconds with the sleeps
 
 __device__ __forceinline__ unsigned smem_u32(const void *p)
@@ -600,33 +601,37 @@ k_pcg_tma(PcgArgs<float> a, const __grid_constant__ TmaMaps m, int ti, int tj)
 // when every tile fits one block and the tile count does not exceed the SMs.
 // ---------------------------------------------------------------------------
 struct ResLayout {
-    int ti, tj, w2, h2, w1, h1;
+    int ti, tj, w2, h2, w1, h1, hp;
     size_t off_rb, off_sb, off_b1, off_xt, off_op, bytes;
 };
 
 // r and s with a 2-cell halo (h2 x w2), the sweep results on the tile and a
 // 1-cell halo (h1 x w1), x on the tile, and a packed operator word per
-// tile-plus-1-halo cell
-__host__ __device__ inline ResLayout res_layout(int ti, int tj)
+// tile-plus-1-halo cell.  hp >= h1 pads the tile-plus-1-halo rows to whole
+// register strips: rows h1 .. hp - 1 exist in Rb, Sb and the operator words
+// so that strip loads need no bounds test.
+__host__ __device__ inline ResLayout res_layout(int ti, int tj, int hp = 0)
 {
     ResLayout L;
     L.ti = ti;
     L.tj = tj;
     L.w2 = tj + 4;
-    L.h2 = ti + 4;
     L.w1 = tj + 2;
     L.h1 = ti + 2;
+    L.hp = hp > L.h1 ? hp : L.h1;
+    L.h2 = L.hp + 2;
     size_t o = 0;
     L.off_rb = o;
     o = a128(o + (size_t)L.h2 * L.w2 * 4);
     L.off_sb = o;
     o = a128(o + (size_t)L.h2 * L.w2 * 4);
-    L.off_b1 = o;
-    o = a128(o + (size_t)L.h1 * L.w1 * 4);
+    L.off_b1 = o; // also holds the operator bytes (h2 x w2) during set-up
+    const size_t b1 = (size_t)L.h1 * L.w1 * 4, ib = (size_t)L.h2 * L.w2;
+    o = a128(o + (b1 > ib ? b1 : ib));
     L.off_xt = o;
     o = a128(o + (size_t)ti * tj * 4);
     L.off_op = o;
-    o = a128(o + (size_t)L.h1 * L.w1 * 4);
+    o = a128(o + (size_t)L.hp * L.w1 * 4);
     L.bytes = o + 128;
     return L;
 }
@@ -758,6 +763,38 @@ __device__ __forceinline__ void for_halo1(int h1, int w1, F f)
     for (int k = threadIdx.x; k < 2 * h1; k += blockDim.x) f(k >> 1, (k & 1) ? w1 - 1 : 0);
 }
 
+// z = M v at one cell from its value and its four neighbours' values, for
+// operator word p (IncompletePoissonPreconditioner with the reference's
+// asymmetric rows); branch-free so that every tile costs the same whatever
+// its fluid fraction.  inv[n] = 1 / (n scale) for n = 1..4, else 0.
+__device__ __forceinline__ float ipp_apply(unsigned p, const float *inv, float vc, float up, float dn,
+                                           float lf, float rt)
+{
+    const float iNeg = inv[(p >> 8) & 7];
+    const float iPos = inv[(p >> 11) & 7];
+    const float jNeg = inv[(p >> 14) & 7];
+    const float jPos = inv[(p >> 17) & 7];
+    const float diag = (1.f + iNeg * iNeg) + jNeg * jNeg;
+    float acc = diag * vc;
+    acc = fmaf(jNeg, lf, acc);
+    acc = fmaf(jPos, rt, acc);
+    acc = fmaf(iNeg, up, acc);
+    acc = fmaf(iPos, dn, acc);
+    return (p & 0x80) ? acc : vc;
+}
+
+// (A v) at one cell (the pressure matrix row; identity on non-unit rows)
+__device__ __forceinline__ float op_apply(unsigned p, float scale, float vc, float up, float dn,
+                                          float lf, float rt)
+{
+    float nb = (p & 1) ? up : 0.f;
+    nb += (p & 2) ? dn : 0.f;
+    nb += (p & 4) ? lf : 0.f;
+    nb += (p & 8) ? rt : 0.f;
+    const float av = scale * ((float)((p >> 4) & 7) * vc - nb);
+    return (p & 0x80) ? av : vc;
+}
+
 // ---------------------------------------------------------------------------
 // The resident kernel.  Synchronisation, all by thread 0 of a block after a
 // block barrier:
@@ -768,8 +805,19 @@ __device__ __forceinline__ void for_halo1(int h1, int w1, F f)
 //    store after the same fence); neighbours whose halo ring reads that
 //    vector wait for the flag instead of the grid barrier.
 // Iteration it publishes s_it as epoch 2 it + 1 and r_{it+1} as 2 it + 2.
+//
+// RPS = 0: every sweep reads and writes the shared-memory arrays.
+// RPS > 0 (register strips): warp w owns columns 32 (w % G) .. +31 of the
+// tile (G = tj / 32 column groups) and a strip of at most RPS consecutive rows
+// of the tile-plus-1-halo region; each thread keeps r, s and the operator
+// words of its strip in registers, so only horizontal neighbours and the rows
+// just outside its strip come from shared memory.  The two halo columns are
+// computed from shared memory by a few threads per warp.  Every cell, strip
+// or halo, goes through the same ipp_apply / op_apply, so values that two
+// tiles both compute agree bit for bit.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads, 1)
+template <int RPS>
+__global__ void __launch_bounds__(RPS > 0 ? kStripThreads : kThreads, 1)
 k_pcg_resident(PcgArgs<float> a, int ti, int tj)
 {
     extern __shared__ unsigned char smem_dyn[];
@@ -780,8 +828,15 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     __shared__ int s_cmax, s_cscan;
     if (a.mode == 1 && *a.wrap_flag == 0) return;
     if (a.mode == 2 && *a.wrap_flag != 0) return;
-    unsigned char *base = reinterpret_cast<unsigned char *>(((size_t)smem_dyn + 127) & ~(size_t)127);
-    const ResLayout L = res_layout(ti, tj);
+    // no TMA here, so the 16-byte alignment of dynamic shared memory is
+    // enough; indexing smem_dyn directly keeps the accesses in the shared
+    // window (32-bit addresses, LDS/STS)
+    unsigned char *base = smem_dyn;
+    // register strips: warp w owns column group w % ngrp and strip w / ngrp
+    constexpr int kR = RPS > 0 ? RPS : 1;
+    const int ngrp = tj >> 5;
+    const int nstrips = (int)(blockDim.x >> 5) / ngrp;
+    const ResLayout L = res_layout(ti, tj, RPS > 0 ? nstrips * RPS : 0);
     float *Rb = reinterpret_cast<float *>(base + L.off_rb);
     float *Sb = reinterpret_cast<float *>(base + L.off_sb);
     float *B1 = reinterpret_cast<float *>(base + L.off_b1);
@@ -889,7 +944,7 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     // (bits 0-7) and the cell counts of its four neighbours (3 bits each:
     // i-1 at 8, i+1 at 11, j-1 at 14, j+1 at 17), which select the IPP
     // coefficients
-    for (int e = threadIdx.x; e < h1 * w1; e += blockDim.x) {
+    for (int e = threadIdx.x; e < L.hp * w1; e += blockDim.x) {
         const int r = e / w1, q = e - r * w1;
         const int c2 = (r + 1) * w2 + (q + 1);
         Op[e] = (unsigned)Ib[c2] | ((unsigned)((Ib[c2 - w2] >> 4) & 7) << 8) |
@@ -933,34 +988,55 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
         return ok();
     };
 
-    // z = M v at a cell with operator word p, v centred at c in a row-major
-    // array of pitch w (IncompletePoissonPreconditioner, the reference's
-    // asymmetric rows); branch-free so that tiles cost the same whatever
-    // their fluid fraction
+    // the stencils on a row-major shared array of pitch w, centred at c
     auto precond = [&](unsigned p, const float *v, int c, int w) -> float {
-        const float iNeg = inv[(p >> 8) & 7];
-        const float iPos = inv[(p >> 11) & 7];
-        const float jNeg = inv[(p >> 14) & 7];
-        const float jPos = inv[(p >> 17) & 7];
-        const float vc = v[c];
-        const float diag = (1.f + iNeg * iNeg) + jNeg * jNeg;
-        float acc = diag * vc;
-        acc = fmaf(jNeg, v[c - 1], acc);
-        acc = fmaf(jPos, v[c + 1], acc);
-        acc = fmaf(iNeg, v[c - w], acc);
-        acc = fmaf(iPos, v[c + w], acc);
-        return (p & 0x80) ? acc : vc;
+        return ipp_apply(p, inv, v[c], v[c - w], v[c + w], v[c - 1], v[c + 1]);
     };
-    // (A v) at a cell with operator word p (the pressure matrix row)
     auto apply_a = [&](unsigned p, const float *v, int c, int w) -> float {
-        const float vc = v[c];
-        float nb = (p & 1) ? v[c - w] : 0.f;
-        nb += (p & 2) ? v[c + w] : 0.f;
-        nb += (p & 4) ? v[c - 1] : 0.f;
-        nb += (p & 8) ? v[c + 1] : 0.f;
-        const float av = scale * ((float)((p >> 4) & 7) * vc - nb);
-        return (p & 0x80) ? av : vc;
+        return op_apply(p, scale, v[c], v[c - w], v[c + w], v[c - 1], v[c + 1]);
     };
+
+    // register strips (RPS > 0): this thread's strip is rows row0 ..
+    // row0 + RPS - 1 of the (padded) tile-plus-1-halo region in column qb.
+    // Rows >= h1 are padding: computed, never stored.  Row h1 itself is the
+    // outer ring row below the tile; its registers are refreshed from the
+    // ring so that row h1 - 1 can take its lower neighbour from a register.
+    const int row0 = (warp / ngrp) * kR;
+    const int qb = 1 + 32 * (warp % ngrp) + lane; // column in the 1-halo region
+    const int cbase = (row0 + 1) * w2 + (qb + 1); // its first cell in Rb / Sb
+    // Rr: r; Sr: s, or between a sweep's two halves the value that does not
+    // need the new scalar yet (z = M r, then A s) -- s itself is in Sb then
+    float Rr[kR], Sr[kR];
+    const unsigned *Ost = Op + row0 * w1 + qb; // operator words of the strip, pitch w1
+    if constexpr (RPS > 0) {
+#pragma unroll
+        for (int rr = 0; rr < kR; rr++) {
+            Rr[rr] = Rb[cbase + rr * w2];
+            Sr[rr] = Rr[rr];
+        }
+    }
+    auto live = [&](int rr) { return row0 + rr < h1; };                     // stored rows
+    auto on_tile = [&](int rr) { return row0 + rr >= 1 && row0 + rr <= ti; }; // tile rows
+    // lower neighbour of strip row rr: a register inside the strip, shared
+    // memory below its last row
+    auto dn_of = [&](const float *reg, const float *arr, int rr, int c) -> float {
+        return rr + 1 < kR ? reg[rr + 1 < kR ? rr + 1 : 0] : arr[c + w2];
+    };
+    auto up_of = [&](const float *reg, const float *arr, int rr, int c) -> float {
+        return rr > 0 ? reg[rr > 0 ? rr - 1 : 0] : arr[c - w2];
+    };
+    // after a ring load: the register copy of row h1 (the outer ring row)
+    auto refresh_ring_row = [&](float *reg, const float *arr) {
+#pragma unroll
+        for (int rr = 0; rr < kR; rr++)
+            if (row0 + rr == h1) reg[rr] = arr[cbase + rr * w2];
+    };
+    // halo-column cells (1-halo columns 0 and w1 - 1), spread over the warps
+    float *Ze = B1; // 2 h1 floats of scratch (B1 is unused with strips)
+    const int edge0 = (threadIdx.x & 7) == 0 ? (int)(threadIdx.x >> 3) : 1 << 30;
+    const int edge_step = (int)(blockDim.x >> 3);
+    auto edge_cell = [&](int e) { return ((e >> 1) + 1) * w2 + ((e & 1) ? w1 : 1); };
+    auto edge_op = [&](int e) { return Op[(e >> 1) * w1 + ((e & 1) ? w1 - 1 : 0)]; };
 
     float fb = 0.f;
     int result = zero ? 0 : a.iter_limit;
@@ -978,9 +1054,21 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
                 if (!wait_neighbours(2u * it)) return;
                 load_ring(Rb, (it & 1) ? a.r1 : a.r0, ti0, tj0, ti, tj, NI, NJ);
                 __syncthreads();
-                for_halo1(h1, w1, [&](int r, int q) {
-                    B1[r * w1 + q] = precond(Op[r * w1 + q], Rb, (r + 1) * w2 + (q + 1), w2);
-                });
+                if constexpr (RPS > 0) {
+                    refresh_ring_row(Rr, Rb);
+#pragma unroll
+                    for (int rr = 0; rr < kR; rr++) {
+                        const int c = cbase + rr * w2;
+                        Sr[rr] = ipp_apply(Ost[rr * w1], inv, Rr[rr], up_of(Rr, Rb, rr, c),
+                                           dn_of(Rr, Rb, rr, c), Rb[c - 1], Rb[c + 1]);
+                    }
+                    for (int ed = edge0; ed < 2 * h1; ed += edge_step)
+                        Ze[ed] = precond(edge_op(ed), Rb, edge_cell(ed), w2);
+                } else {
+                    for_halo1(h1, w1, [&](int r, int q) {
+                        B1[r * w1 + q] = precond(Op[r * w1 + q], Rb, (r + 1) * w2 + (q + 1), w2);
+                    });
+                }
             }
             // end of iteration it - 1: beta and the stopping test
             const float4 rec = wait_sum(pB, true);
@@ -999,24 +1087,58 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
             fb = ff_div(newSigma, sigma);
             sigma = newSigma;
             // s_it = z_it + beta s_{it-1}
-            for_halo1(h1, w1, [&](int r, int q) {
-                B1[r * w1 + q] = fmaf(Sb[(r + 1) * w2 + (q + 1)], fb, B1[r * w1 + q]);
-            });
-        } else {
+            if constexpr (RPS > 0) {
+#pragma unroll
+                for (int rr = 0; rr < kR; rr++) {
+                    const int c = cbase + rr * w2;
+                    Sr[rr] = fmaf(Sb[c], fb, Sr[rr]);
+                }
+#pragma unroll
+                for (int rr = 0; rr < kR; rr++)
+                    if (live(rr)) Sb[cbase + rr * w2] = Sr[rr];
+                for (int ed = edge0; ed < 2 * h1; ed += edge_step) {
+                    const int c = edge_cell(ed);
+                    Sb[c] = fmaf(Sb[c], fb, Ze[ed]);
+                }
+            } else {
+                for_halo1(h1, w1, [&](int r, int q) {
+                    B1[r * w1 + q] = fmaf(Sb[(r + 1) * w2 + (q + 1)], fb, B1[r * w1 + q]);
+                });
+            }
+        } else if constexpr (RPS == 0) {
             for_halo1(h1, w1, [&](int r, int q) { B1[r * w1 + q] = Sb[(r + 1) * w2 + (q + 1)]; });
         }
         __syncthreads();
         float qs = 0.f;
-        for (int r = warp; r < ti; r += nw) {
-            const int gi = ti0 + r;
-            for (int q = lane; q < tj; q += 32) {
-                const int gj = tj0 + q;
-                const int c1 = (r + 1) * w1 + (q + 1);
-                const float s_c = B1[c1];
-                qs = fmaf(apply_a(Op[c1], B1, c1, w1), s_c, qs);
-                if (!first) {
-                    Sb[(r + 2) * w2 + (q + 2)] = s_c;
-                    if (gi < NI && gj < NJ) s_pub[(size_t)gi * NJ + gj] = s_c;
+        if constexpr (RPS > 0) {
+            const int gj = tj0 + qb - 1;
+#pragma unroll
+            for (int rr = 0; rr < kR; rr++) {
+                const int c = cbase + rr * w2;
+                const float q = op_apply(Ost[rr * w1], scale, Sr[rr], up_of(Sr, Sb, rr, c),
+                                         dn_of(Sr, Sb, rr, c), Sb[c - 1], Sb[c + 1]);
+                // padding rows may hold anything, even inf: select, do not scale
+                qs = on_tile(rr) ? fmaf(q, Sr[rr], qs) : qs;
+            }
+            if (!first && gj < NJ) {
+#pragma unroll
+                for (int rr = 0; rr < kR; rr++) {
+                    const int gi = ti0 + row0 + rr - 1;
+                    if (on_tile(rr) && gi < NI) s_pub[(size_t)gi * NJ + gj] = Sr[rr];
+                }
+            }
+        } else {
+            for (int r = warp; r < ti; r += nw) {
+                const int gi = ti0 + r;
+                for (int q = lane; q < tj; q += 32) {
+                    const int gj = tj0 + q;
+                    const int c1 = (r + 1) * w1 + (q + 1);
+                    const float s_c = B1[c1];
+                    qs = fmaf(apply_a(Op[c1], B1, c1, w1), s_c, qs);
+                    if (!first) {
+                        Sb[(r + 2) * w2 + (q + 2)] = s_c;
+                        if (gi < NI && gj < NJ) s_pub[(size_t)gi * NJ + gj] = s_c;
+                    }
                 }
             }
         }
@@ -1038,29 +1160,79 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
             __syncthreads();
         }
         // A s_it on the tile and its 1-halo while the grid barrier completes
-        for_halo1(h1, w1, [&](int r, int q) {
-            B1[r * w1 + q] = apply_a(Op[r * w1 + q], Sb, (r + 1) * w2 + (q + 1), w2);
-        });
+        if constexpr (RPS > 0) {
+            if (!first) refresh_ring_row(Sr, Sb);
+            float prev = 0.f; // s of the row above, before it was overwritten
+#pragma unroll
+            for (int rr = 0; rr < kR; rr++) {
+                const int c = cbase + rr * w2;
+                const float cur = Sr[rr];
+                const float up = rr > 0 ? prev : Sb[c - w2];
+                Sr[rr] = op_apply(Ost[rr * w1], scale, cur, up, dn_of(Sr, Sb, rr, c), Sb[c - 1], Sb[c + 1]);
+                prev = cur; // s_it itself stays in Sb
+            }
+            for (int ed = edge0; ed < 2 * h1; ed += edge_step) Ze[ed] = apply_a(edge_op(ed), Sb, edge_cell(ed), w2);
+        } else {
+            for_halo1(h1, w1, [&](int r, int q) {
+                B1[r * w1 + q] = apply_a(Op[r * w1 + q], Sb, (r + 1) * w2 + (q + 1), w2);
+            });
+        }
         const float4 qsum = wait_sum(pA, false);
         if (!ok()) return;
         const float fa = ff_div(sigma, ff_add(make_float2(qsum.x, qsum.y), eps8));
-        // r_{it+1} = r_it - alpha A s_it
-        for_halo1(h1, w1, [&](int r, int q) {
-            B1[r * w1 + q] = fmaf(-B1[r * w1 + q], fa, Rb[(r + 1) * w2 + (q + 1)]);
-        });
+        // r_{it+1} = r_it - alpha A s_it (and x += alpha s_it on the tile)
+        if constexpr (RPS > 0) {
+#pragma unroll
+            for (int rr = 0; rr < kR; rr++) Rr[rr] = fmaf(-Sr[rr], fa, Rr[rr]);
+#pragma unroll
+            for (int rr = 0; rr < kR; rr++) {
+                const int c = cbase + rr * w2;
+                if (live(rr)) Rb[c] = Rr[rr];
+                if (on_tile(rr)) {
+                    float *xp = Xt + (row0 + rr - 1) * tj + (qb - 1);
+                    *xp = fmaf(Sb[c], fa, *xp);
+                }
+            }
+            for (int ed = edge0; ed < 2 * h1; ed += edge_step) {
+                const int c = edge_cell(ed);
+                Rb[c] = fmaf(-Ze[ed], fa, Rb[c]);
+            }
+        } else {
+            for_halo1(h1, w1, [&](int r, int q) {
+                B1[r * w1 + q] = fmaf(-B1[r * w1 + q], fa, Rb[(r + 1) * w2 + (q + 1)]);
+            });
+        }
         __syncthreads();
         float zr = 0.f;
-        for (int r = warp; r < ti; r += nw) {
-            const int gi = ti0 + r;
-            for (int q = lane; q < tj; q += 32) {
-                const int gj = tj0 + q;
-                const int c1 = (r + 1) * w1 + (q + 1);
-                const int c2 = (r + 2) * w2 + (q + 2);
-                const float r_c = B1[c1];
-                zr = fmaf(precond(Op[c1], B1, c1, w1), r_c, zr);
-                Xt[r * tj + q] = fmaf(Sb[c2], fa, Xt[r * tj + q]);
-                Rb[c2] = r_c;
-                if (gi < NI && gj < NJ) r_pub[(size_t)gi * NJ + gj] = r_c;
+        if constexpr (RPS > 0) {
+            const int gj = tj0 + qb - 1;
+#pragma unroll
+            for (int rr = 0; rr < kR; rr++) {
+                const int c = cbase + rr * w2;
+                const float z = ipp_apply(Ost[rr * w1], inv, Rr[rr], up_of(Rr, Rb, rr, c), dn_of(Rr, Rb, rr, c),
+                                          Rb[c - 1], Rb[c + 1]);
+                zr = on_tile(rr) ? fmaf(z, Rr[rr], zr) : zr;
+            }
+            if (gj < NJ) {
+#pragma unroll
+                for (int rr = 0; rr < kR; rr++) {
+                    const int gi = ti0 + row0 + rr - 1;
+                    if (on_tile(rr) && gi < NI) r_pub[(size_t)gi * NJ + gj] = Rr[rr];
+                }
+            }
+        } else {
+            for (int r = warp; r < ti; r += nw) {
+                const int gi = ti0 + r;
+                for (int q = lane; q < tj; q += 32) {
+                    const int gj = tj0 + q;
+                    const int c1 = (r + 1) * w1 + (q + 1);
+                    const int c2 = (r + 2) * w2 + (q + 2);
+                    const float r_c = B1[c1];
+                    zr = fmaf(precond(Op[c1], B1, c1, w1), r_c, zr);
+                    Xt[r * tj + q] = fmaf(Sb[c2], fa, Xt[r * tj + q]);
+                    Rb[c2] = r_c;
+                    if (gi < NI && gj < NJ) r_pub[(size_t)gi * NJ + gj] = r_c;
+                }
             }
         }
         __syncthreads();
@@ -1189,6 +1361,29 @@ bool tma_store_maps(TmaMaps *m, int ni, int nj, int ti, int tj, const float *r0,
 
 constexpr size_t kMaxResidentSmem = 220 * 1024;
 
+// rows per register strip for a tile shape (0: strips do not apply)
+static int strip_rows(int ti, int tj)
+{
+    const int warps = kStripThreads / 32;
+    if (tj % 32 != 0 || tj / 32 > warps || warps % (tj / 32) != 0) return 0;
+    const int nstrips = warps / (tj / 32);
+    const int rps = (ti + 2 + nstrips - 1) / nstrips;
+    if (rps <= 1) return 1;
+    if (rps <= 2) return 2;
+    if (rps <= 4) return 4;
+    if (rps <= 8) return 8;
+    if (rps <= 16) return 16;
+    return 0;
+}
+
+// shared memory of the resident kernel for a tile shape (strips pad rows)
+static size_t resident_smem(int ti, int tj)
+{
+    const int rps = strip_rows(ti, tj);
+    const int nstrips = rps > 0 ? kStripThreads / 32 / (tj / 32) : 0;
+    return res_layout(ti, tj, nstrips * rps).bytes;
+}
+
 bool resident_tile_shape(int ni, int nj, int *ti, int *tj)
 {
     // among tile widths 32..256, the shape with the fewest cells per block
@@ -1203,7 +1398,7 @@ bool resident_tile_shape(int ni, int nj, int *ti, int *tj)
         if (h < 1) h = 1;
         const long long ntiles = ((ni + h - 1) / h) * tiles_j;
         if (ntiles > blocks) continue;
-        if (res_layout((int)h, w).bytes > kMaxResidentSmem) continue;
+        if (resident_smem((int)h, w) > kMaxResidentSmem) continue;
         const long long cost = (h + 2) * (w + 2);
         if (best < 0 || cost < best) {
             best = cost;
@@ -1215,25 +1410,38 @@ bool resident_tile_shape(int ni, int nj, int *ti, int *tj)
     return best >= 0;
 }
 
-cudaError_t launch_pcg_resident(const PcgArgs<float> &a, int ti, int tj, cudaStream_t st)
+template <int RPS>
+static cudaError_t launch_resident_rps(const PcgArgs<float> &a, int ti, int tj, int grid,
+                                       cudaStream_t st)
 {
-    const ResLayout L = res_layout(ti, tj);
-    // the attribute is per device; setting it costs a few microseconds
-    cudaError_t e = cudaFuncSetAttribute((const void *)k_pcg_resident,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)L.bytes);
+    const int nstrips = (RPS > 0 ? kStripThreads : kThreads) / 32 / (tj / 32);
+    const size_t smem = res_layout(ti, tj, RPS > 0 ? nstrips * RPS : 0).bytes;
+    cudaError_t e = cudaFuncSetAttribute((const void *)k_pcg_resident<RPS>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    const int grid = ((a.ni + ti - 1) / ti) * ((a.nj + tj - 1) / tj);
     PcgArgs<float> args = a;
     int vti = ti, vtj = tj;
     void *kargs[] = {&args, &vti, &vtj};
-    e = cudaMemsetAsync(args.bar, 0, sizeof(GridBarrier), st);
+    return cudaLaunchCooperativeKernel((const void *)k_pcg_resident<RPS>, dim3(grid),
+                                       dim3(RPS > 0 ? kStripThreads : kThreads), kargs, smem, st);
+}
+
+cudaError_t launch_pcg_resident(const PcgArgs<float> &a, int ti, int tj, cudaStream_t st)
+{
+    const int grid = ((a.ni + ti - 1) / ti) * ((a.nj + tj - 1) / tj);
+    cudaError_t e = cudaMemsetAsync(a.bar, 0, sizeof(GridBarrier), st);
     if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(reinterpret_cast<unsigned char *>(args.partials) + res_flags_offset(grid), 0,
+    e = cudaMemsetAsync(reinterpret_cast<unsigned char *>(a.partials) + res_flags_offset(grid), 0,
                         (size_t)grid * 32, st);
     if (e != cudaSuccess) return e;
-    return cudaLaunchCooperativeKernel((const void *)k_pcg_resident, dim3(grid), dim3(kThreads),
-                                       kargs, L.bytes, st);
+    switch (strip_rows(ti, tj)) {
+    case 1: return launch_resident_rps<1>(a, ti, tj, grid, st);
+    case 2: return launch_resident_rps<2>(a, ti, tj, grid, st);
+    case 4: return launch_resident_rps<4>(a, ti, tj, grid, st);
+    case 8: return launch_resident_rps<8>(a, ti, tj, grid, st);
+    case 16: return launch_resident_rps<16>(a, ti, tj, grid, st);
+    default: return launch_resident_rps<0>(a, ti, tj, grid, st);
+    }
 }
 
 cudaError_t launch_pcg_tma(const PcgArgs<float> &a, const TmaMaps &maps, int ti, int tj,
