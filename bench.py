@@ -7,8 +7,9 @@ solid walls, fluid block I in [0.4, 1-dx], J in [dx, 0.4], 4 particles per
 cell jittered from seed 7 (~1.0 M particles), one convex 6-vertex solid
 (friction 0.1) drawn in the central 30 % from seed 7; density 1000, g = 9.81,
 30 fps, CFL 5, picRatio 0.03, pcgIterLimit 200 with the reference's absolute
-1e-2 max-abs stopping test, FP32 PCG with FP64 reductions.  Synthetic seeded
-data.  A step is one substep (FlipSolver::step) with the CFL dt the
+1e-2 max-abs stopping test, FP32 PCG vectors with float-pair (hi + lo)
+reductions and scalars.  Synthetic seeded data.  --res picks a smaller grid
+of the same scene (parity-size runs and profiler captures).  A step is one substep (FlipSolver::step) with the CFL dt the
 reference's frame loop would choose; the scene is first advanced by two
 frames so the fluid is moving.
 
@@ -42,6 +43,16 @@ SEED = 7
 WARM_FRAMES = 2
 METRIC = "particle-substeps/s"
 WORKLOAD = "dam_break_1024_obstacle"
+# DRAM bytes (read + write) of one k_pcg_resident launch, from the ncu
+# capture summarised in profiles/k_pcg_resident_dam_break_1024.md; the solve
+# keeps its vectors on chip, so this is b and the operator in, x out
+PCG_TRAFFIC_BYTES = None
+
+
+def set_resolution(res: int):
+    global RES, WORKLOAD
+    RES = res
+    WORKLOAD = f"dam_break_{res}_obstacle"
 
 
 def scene():
@@ -293,8 +304,8 @@ def gpu_arm(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded dam-break scene)",
         "config": {"workload": WORKLOAD, "grid": RES, "seed": SEED, "particles": int(work / args.steps),
-                   "pcg": "PCG+IPP FP32 vectors, FP64 reductions, reference stopping "
-                          "(limit 200, abs tol 1e-2 max-abs)",
+                   "pcg": "PCG+IPP FP32 vectors, float-pair reductions and scalars, reference "
+                          "stopping (limit 200, abs tol 1e-2 max-abs)",
                    "l2": "flushed between steps (256 MiB write)", "warm_frames": WARM_FRAMES,
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "pcg_cell_iter_per_s": cell_iters / (pcg_ms / 1e3) if pcg_ms > 0 else None,
@@ -306,9 +317,10 @@ def gpu_arm(args):
                 "path": "fs_set_particles + fs_set_grid(u, v, material) + fs_step + "
                         "fs_get_particles + fs_get_grid, host buffers"},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": "k_pcg<float>",
+        "roofline": {"bound": "hbm", "kernel": "k_pcg_resident",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None, "traffic": None,
+                     "frac": (achieved / peak) if achieved else None,
+                     "traffic": PCG_TRAFFIC_BYTES if RES == 1024 else None,
                      "peak_source": peak_kind,
                      "bytes_model": "per solve 16 B/cell + 34 B/cell-iteration",
                      "launches": n_pcg, "avg_launch_ms": pcg_ms / n_pcg},
@@ -330,7 +342,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--res", type=int, default=RES, help="grid side of the dam break (default 1024)")
     args = ap.parse_args()
+    set_resolution(args.res)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

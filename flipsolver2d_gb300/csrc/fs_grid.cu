@@ -321,6 +321,9 @@ __global__ void k_p2g_sdf_materials(GridDims d, Particles P, Grids G, float part
                 const float ddx = p.x - cx, ddy = p.y - cy;
                 const float nd = ddx * ddx + ddy * ddy;
                 if (nd < d2) d2 = nd;
+                // every B-spline below is zero unless the particle is within
+                // 2 cells of (i, j) in both axes: skip the rest of the far ones
+                if (!(fabsf(p.x - fi) < 2.f && fabsf(p.y - fj) < 2.f)) continue;
                 // velocity: weights at (i, j+0.5) for U and (i+0.5, j) for V
                 const float wU = sm_qbspline(p.x - fi, p.y - (fj + 0.5f));
                 const float wV = sm_qbspline(p.x - (fi + 0.5f), p.y - fj);
@@ -425,6 +428,79 @@ __device__ __forceinline__ double bfs_avg(const int *mark, const float *val, int
     return avg;
 }
 
+__device__ __forceinline__ void ls_two_sum(float a, float b, float &s, float &e)
+{
+    s = a + b;
+    const float bv = s - a;
+    e = (a - (s - bv)) + (b - bv);
+}
+
+// The value of a BFS cell: avg / count (velocity extrapolation,
+// mathfuncs.cpp:152-215) or avg / count - 1 (level set, flipsolver2d.cpp:
+// 1433-1494), with avg the double sum of the smaller-marker neighbours in the
+// reference's order, rounded to float at the end.  FP64 operations have a
+// latency of hundreds of cycles here and every BFS layer waits for its
+// slowest cell, so the value is first formed in float-pair arithmetic: the
+// sum and its rounding errors are carried exactly enough (s + eh + el), the
+// quotient keeps its remainder.  Its distance from the reference's double
+// result is below 2^-44 (sum |v| + 1); when that bound cannot place the value
+// strictly inside one float's rounding interval, the cell is recomputed in
+// double exactly like the reference.  Either way the result is the
+// reference's float.
+template <int W>
+__device__ __forceinline__ float bfs_layer_value(const int *mark, const float *val, int r, int q, int k,
+                                                 bool minus_one)
+{
+    float s = 0.f, eh = 0.f, el = 0.f, m = 0.f;
+    int count = 0;
+#pragma unroll
+    for (int io = -1; io <= 1; io++)
+#pragma unroll
+        for (int jo = -1; jo <= 1; jo++) {
+            if (io == 0 && jo == 0) continue;
+            const int rr = r + io, qq = q + jo;
+            if (rr < 0 || rr >= W || qq < 0 || qq >= W) continue;
+            const int mk = mark[rr * W + qq];
+            if (mk == kMarkOut || mk >= k) continue;
+            const float x = val[rr * W + qq];
+            float t2, er, t3, er2;
+            ls_two_sum(s, x, t2, er);
+            s = t2;
+            ls_two_sum(eh, er, t3, er2);
+            eh = t3;
+            el += er2;
+            m += fabsf(x);
+            count++;
+        }
+    const float cf = (float)count;
+    const float qh = __fdiv_rn(s, cf);
+    const float rem = fmaf(-qh, cf, s); // exact
+    float t1, t2;
+    ls_two_sum(rem, eh, t1, t2);
+    const float ql = __fdiv_rn(t1 + (t2 + el), cf);
+    float h, l;
+    if (minus_one) {
+        ls_two_sum(qh, -1.f, h, l);
+        l += ql;
+    } else {
+        h = qh;
+        l = ql;
+    }
+    const float f = h + l;
+    const float d = (h - f) + l;
+    const float bound = (m + 1.f) * 0x1p-44f;
+    const float gap = 0.5f * fminf(nextafterf(f, INFINITY) - f, f - nextafterf(f, -INFINITY));
+    if (count > 0 && isfinite(f) && isfinite(m) && fabsf(f) >= 0x1p-100f &&
+        fabsf(d) + bound < 0.99f * gap)
+        return f;
+    const double avg = bfs_avg<W>(mark, val, r, q, k, count);
+    // dividing by 1, 2, 4 or 8 is an exact scaling, the same as multiplying
+    // by the reciprocal -- and a multiply has a fraction of the latency
+    const double inv2 = count == 1 ? 1.0 : count == 2 ? 0.5 : count == 4 ? 0.25 : 0.125;
+    const double a = (count & (count - 1)) == 0 ? avg * inv2 : avg / count;
+    return minus_one ? (float)(a - 1.f) : (float)a;
+}
+
 template <int W>
 __device__ __forceinline__ bool bfs_touches(const int *mark, int r, int q, int k)
 {
@@ -447,15 +523,41 @@ __device__ __forceinline__ bool bfs_touches(const int *mark, int r, int q, int k
 // computed from neighbours of smaller layers, in the reference's neighbour
 // order.  The set of cells per layer, hence every value, is deterministic.
 // `minus_one` selects the level-set form (average - 1).
-template <int H>
-__device__ __forceinline__ void bfs_layers(BfsTile<H> &t, short *fa, short *fb, int *cnt, int k0,
-                                           bool minus_one)
+// Appends `cnt_mine` entries per thread to a shared list with one atomic per
+// warp; returns this thread's first slot.  All threads of the warp call it.
+__device__ __forceinline__ int warp_append(int *counter, int cnt_mine)
 {
-    constexpr int W = BfsTile<H>::W;
+    const int lane = threadIdx.x & 31;
+    int incl = cnt_mine;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    int base = 0;
+    if (lane == 31 && incl > 0) base = atomicAdd(counter, incl);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    return base + incl - cnt_mine;
+}
+
+template <int W, int H>
+__device__ __forceinline__ void bfs_layers(int *mark, float *val, short *fa, short *fb, int *cnt,
+                                           int k0, bool minus_one)
+{
+    struct {
+        int *mark;
+        float *val;
+    } t{mark, val};
     if (threadIdx.x == 0) cnt[0] = 0;
     __syncthreads();
-    for (int e = threadIdx.x; e < W * W; e += blockDim.x)
-        if (t.mark[e] == k0) fa[atomicAdd(&cnt[0], 1)] = (short)e;
+    // the frontier: cells of layer k0 (blockDim.x is a multiple of 32, so
+    // whole warps run every round)
+    for (int e0 = 0; e0 < W * W; e0 += blockDim.x) {
+        const int e = e0 + (int)threadIdx.x;
+        const int mine = (e < W * W && t.mark[e] == k0) ? 1 : 0;
+        const int slot = warp_append(&cnt[0], mine);
+        if (mine) fa[slot] = (short)e;
+    }
     __syncthreads();
     short *cur = fa, *nxt = fb;
     int ncur = cnt[0];
@@ -463,29 +565,37 @@ __device__ __forceinline__ void bfs_layers(BfsTile<H> &t, short *fa, short *fb, 
         if (ncur == 0) break;
         if (threadIdx.x == 0) cnt[1] = 0;
         __syncthreads();
-        for (int f = threadIdx.x; f < ncur; f += blockDim.x) {
-            const int e = cur[f];
-            const int r = e / W, q = e - r * W;
+        for (int f0 = 0; f0 < ncur; f0 += blockDim.x) {
+            const int f = f0 + (int)threadIdx.x;
+            int r = 0, q = 0;
+            unsigned got = 0; // neighbours this cell claimed, bit (io+1)*3+(jo+1)
+            if (f < ncur) {
+                const int e = cur[f];
+                r = e / W;
+                q = e - r * W;
 #pragma unroll
-            for (int io = -1; io <= 1; io++)
+                for (int io = -1; io <= 1; io++)
 #pragma unroll
-                for (int jo = -1; jo <= 1; jo++) {
-                    if (io == 0 && jo == 0) continue;
-                    const int rr = r + io, qq = q + jo;
-                    if (rr < 0 || rr >= W || qq < 0 || qq >= W) continue;
-                    const int n = rr * W + qq;
-                    if (t.mark[n] == kMarkInf && atomicCAS(&t.mark[n], kMarkInf, k) == kMarkInf)
-                        nxt[atomicAdd(&cnt[1], 1)] = (short)n;
-                }
+                    for (int jo = -1; jo <= 1; jo++) {
+                        if (io == 0 && jo == 0) continue;
+                        const int rr = r + io, qq = q + jo;
+                        if (rr < 0 || rr >= W || qq < 0 || qq >= W) continue;
+                        const int n = rr * W + qq;
+                        if (t.mark[n] == kMarkInf && atomicCAS(&t.mark[n], kMarkInf, k) == kMarkInf)
+                            got |= 1u << ((io + 1) * 3 + (jo + 1));
+                    }
+            }
+            int slot = warp_append(&cnt[1], __popc(got));
+#pragma unroll
+            for (int b = 0; b < 9; b++)
+                if (got & (1u << b)) nxt[slot++] = (short)((r + b / 3 - 1) * W + (q + b % 3 - 1));
         }
         __syncthreads();
         const int nnext = cnt[1];
         for (int f = threadIdx.x; f < nnext; f += blockDim.x) {
             const int e = nxt[f];
             const int r = e / W, q = e - r * W;
-            int count;
-            const double avg = bfs_avg<W>(t.mark, t.val, r, q, k, count);
-            t.val[e] = minus_one ? (float)(avg / count - 1.f) : (float)(avg / count);
+            t.val[e] = bfs_layer_value<W>(t.mark, t.val, r, q, k, minus_one);
         }
         __syncthreads();
         short *tmp = cur;
@@ -539,7 +649,7 @@ __global__ void __launch_bounds__(1024) k_vel_extrap(GridDims d, Grids G, float 
     // a tile whose loaded region lacks either seeds or unknown cells assigns
     // nothing and only copies its interior through
     const bool work = __syncthreads_or(has_seed) && __syncthreads_or(has_inf);
-    if (work) bfs_layers<kVelH>(t, fa, fb, cnt, 0, false);
+    if (work) bfs_layers<W, kVelH>(t.mark, t.val, fa, fb, cnt, 0, false);
     const float factor = (float)((double)sc->dt / dx);
     const float add = factor * (isV ? gJ : gI);
     for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
@@ -575,14 +685,23 @@ void launch_vel_extrapolate(const GridDims &d, Grids &G, const SceneParams &sp,
 // Level set inside extrapolation (flipsolver2d.cpp:1433-1494): seeds are
 // cells with sdf > 0, depth unbounded, value = average - 1.  Pass p advances
 // layers p*H+1 .. (p+1)*H.  Each cell's (marker, value) pair lives in one
-// 64-bit word that is read and written whole, so a concurrently finished
-// neighbour tile is seen either untouched or final -- both consistent with
-// the exact layered solution, which is all a tile needs from its halo.  Only
-// newly assigned cells are written (and copied to the fluid SDF).  A tile
+// 64-bit word that is read and written whole.  A tile only trusts halo cells
+// of earlier passes (markers <= p*H, final since the previous launch); cells
+// a concurrently running neighbour tile assigned in this pass are reset and
+// recomputed, giving the same values.  Only newly assigned interior cells are
+// written (and copied to the fluid SDF).  A tile
 // works in pass p only if a tile within one tile of it assigned cells in pass
 // p-1: the frontier of layer p*H is otherwise out of its reach.  Once a pass
 // assigns nothing, the remaining passes return immediately.
-constexpr int kLsH = 15; // keeps the tile's static shared memory under 48 KiB
+// 64 x 64 tiles with a 32-cell halo: (64 + 64)^2 cells of (marker, value)
+// plus two frontier lists, 192 KiB of dynamic shared memory; 32 layers a
+// pass.  Larger tiles than the velocity extrapolation's cut the halo cells a
+// tile reloads per interior cell (4x against 14x for 32 x 32 with 15) and the
+// number of passes.
+constexpr int kLsTile = 64;
+constexpr int kLsH = 32;
+constexpr int kLsW = kLsTile + 2 * kLsH;
+constexpr size_t kLsSmem = (size_t)kLsW * kLsW * (4 + 4 + 2 + 2) + 16;
 
 __device__ __forceinline__ unsigned long long ls_pack(int mark, float v)
 {
@@ -603,16 +722,20 @@ __global__ void k_levelset_init(GridDims d, const float *__restrict__ sdf,
     if (c < passes) active[c] = 0;
 }
 
-__global__ void __launch_bounds__(1024) k_levelset_pass(GridDims d, float *__restrict__ sdf,
+__global__ void __launch_bounds__(1024, 1) k_levelset_pass(GridDims d, float *__restrict__ sdf,
                                                        unsigned long long *__restrict__ cells,
                                                        uint8_t *__restrict__ act,
                                                        int *__restrict__ active, int pass)
 {
-    __shared__ BfsTile<kLsH> t;
-    __shared__ short fa[BfsTile<kLsH>::W * BfsTile<kLsH>::W];
-    __shared__ short fb[BfsTile<kLsH>::W * BfsTile<kLsH>::W];
-    __shared__ int cnt[2];
-    constexpr int W = BfsTile<kLsH>::W;
+    extern __shared__ int ls_smem[];
+    constexpr int W = kLsW;
+    struct {
+        int *mark;
+        float *val;
+    } t{ls_smem, reinterpret_cast<float *>(ls_smem + W * W)};
+    short *fa = reinterpret_cast<short *>(ls_smem + 2 * W * W);
+    short *fb = fa + W * W;
+    int *cnt = reinterpret_cast<int *>(fb + W * W);
     if (pass > 0 && ((volatile int *)active)[pass - 1] == 0) return;
     const int si = d.ni, sj = d.nj;
     const int tiles_i = gridDim.y, tiles_j = gridDim.x;
@@ -632,7 +755,9 @@ __global__ void __launch_bounds__(1024) k_levelset_pass(GridDims d, float *__res
             }
         if (!near) return;
     }
-    const int ti0 = blockIdx.y * kTile, tj0 = blockIdx.x * kTile;
+    const int ti0 = blockIdx.y * kLsTile, tj0 = blockIdx.x * kLsTile;
+    const int k0 = pass * kLsH;
+    int open = 0;
     for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
         const int r = e / W, q = e - r * W;
         const int gi = ti0 - kLsH + r, gj = tj0 - kLsH + q;
@@ -641,16 +766,22 @@ __global__ void __launch_bounds__(1024) k_levelset_pass(GridDims d, float *__res
             t.val[e] = 0.f;
         } else {
             const unsigned long long w = ((volatile unsigned long long *)cells)[(size_t)gi * sj + gj];
-            t.mark[e] = (int)(w >> 32);
+            int mk = (int)(w >> 32);
+            // a halo cell a neighbour tile already assigned in this same pass
+            // is recomputed here: the frontier of every layer must come from
+            // this tile's own BFS, or cells next to it could be missed
+            if (mk > k0 && mk != kMarkInf) mk = kMarkInf;
+            t.mark[e] = mk;
             t.val[e] = __uint_as_float((unsigned)(w & 0xffffffffu));
+            open |= mk == kMarkInf;
         }
     }
-    __syncthreads();
-    const int k0 = pass * kLsH;
-    bfs_layers<kLsH>(t, fa, fb, cnt, k0, true);
+    // a tile whose cells are all assigned already has nothing to do
+    if (!__syncthreads_or(open)) return;
+    bfs_layers<W, kLsH>(t.mark, t.val, fa, fb, cnt, k0, true);
     bool assigned = false;
-    for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
-        const int r = e / kTile + kLsH, q = e % kTile + kLsH;
+    for (int e = threadIdx.x; e < kLsTile * kLsTile; e += blockDim.x) {
+        const int r = e / kLsTile + kLsH, q = e % kLsTile + kLsH;
         const int gi = ti0 - kLsH + r, gj = tj0 - kLsH + q;
         if (gi >= si || gj >= sj) continue;
         const int mk = t.mark[r * W + q];
@@ -677,7 +808,7 @@ int levelset_max_passes(const GridDims &d)
 void launch_levelset(const GridDims &d, Grids &G, cudaStream_t st)
 {
     const int passes = levelset_max_passes(d);
-    dim3 grid(nblk(d.nj, kTile), nblk(d.ni, kTile));
+    dim3 grid(nblk(d.nj, kLsTile), nblk(d.ni, kLsTile));
     const int ntiles = grid.x * grid.y;
     const long long n = (long long)d.ni * d.nj;
     long long init_n = n > 3LL * ntiles ? n : 3LL * ntiles;
@@ -686,9 +817,11 @@ void launch_levelset(const GridDims &d, Grids &G, cudaStream_t st)
     k_levelset_init<<<nblk(init_n, kThreads), kThreads, 0, st>>>(d, G.fluid_sdf, cells,
                                                                G.levelset_act, ntiles,
                                                                G.levelset_active, passes);
+    cudaFuncSetAttribute((const void *)k_levelset_pass, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kLsSmem);
     for (int p = 0; p < passes; p++)
-        k_levelset_pass<<<grid, 1024, 0, st>>>(d, G.fluid_sdf, cells, G.levelset_act,
-                                                G.levelset_active, p);
+        k_levelset_pass<<<grid, 1024, kLsSmem, st>>>(d, G.fluid_sdf, cells, G.levelset_act,
+                                                      G.levelset_active, p);
 }
 
 // ---------------------------------------------------------------------------

@@ -31,7 +31,8 @@
 namespace fsg {
 
 constexpr int kThreads = 1024;
-constexpr int kStripThreads = 512; // resident kernel with register strips: 128 registers a thread
+constexpr int kStripThreads = 512;
+constexpr int kMaxOwnedChunks = 64; // chunk ends a resident tile lists in shared memory // resident kernel with register strips: 128 registers a thread
 constexpr long long kSpinLimit = 1LL << 25; // a few seconds with the sleeps
 
 __device__ __forceinline__ unsigned smem_u32(const void *p)
@@ -826,8 +827,11 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     __shared__ int s_flag;
     __shared__ float inv[8];
     __shared__ int s_cmax, s_cscan;
+    __shared__ int s_nown;           // chunks whose last unit row is in this tile
+    __shared__ int2 s_own[kMaxOwnedChunks]; // (chunk, Rb index)
     if (a.mode == 1 && *a.wrap_flag == 0) return;
     if (a.mode == 2 && *a.wrap_flag != 0) return;
+    if (threadIdx.x == 0) s_nown = 0; // ordered before its use by the set-up barriers
     // no TMA here, so the 16-byte alignment of dynamic shared memory is
     // enough; indexing smem_dyn directly keeps the accesses in the shared
     // window (32-bit addresses, LDS/STS)
@@ -940,6 +944,16 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     }
     for (int e = threadIdx.x; e < ti * tj; e += blockDim.x) Xt[e] = 0.f;
     __syncthreads();
+    // the chunk ends this tile owns, listed once (more than kMaxOwnedChunks,
+    // possible only with tiny chunks, falls back to a scan of all chunks)
+    for (int k = threadIdx.x; k < a.nchunks; k += blockDim.x) {
+        const int idx = a.chunk_last_unit[k];
+        if (idx < 0) continue;
+        const int gi = idx / NJ, gj = idx - gi * NJ;
+        if (gi < ti0 || gi >= ti0 + ti || gj < tj0 || gj >= tj0 + tj) continue;
+        const int slot = atomicAdd(&s_nown, 1);
+        if (slot < kMaxOwnedChunks) s_own[slot] = make_int2(k, (gi - ti0 + 2) * w2 + (gj - tj0 + 2));
+    }
     // packed operator word of each tile-plus-1-halo cell: its own row byte
     // (bits 0-7) and the cell counts of its four neighbours (3 bits each:
     // i-1 at 8, i+1 at 11, j-1 at 14, j+1 at 17), which select the IPP
@@ -1025,6 +1039,23 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     auto up_of = [&](const float *reg, const float *arr, int rr, int c) -> float {
         return rr > 0 ? reg[rr > 0 ? rr - 1 : 0] : arr[c - w2];
     };
+    // tile cells within two of the tile border (what a neighbour's ring reads)
+    const int tcol = qb - 1;
+    const bool col_band = tcol < 2 || tcol >= tj - 2;
+    auto in_band = [&](int rr) {
+        const int tr = row0 + rr - 1;
+        return col_band || tr < 2 || tr >= ti - 2;
+    };
+    auto publish_tile_r = [&](float *dst) {
+        for (int r = warp; r < ti; r += nw) {
+            const int gi = ti0 + r;
+            if (gi >= NI) break;
+            for (int q = lane; q < tj; q += 32) {
+                const int gj = tj0 + q;
+                if (gj < NJ) dst[(size_t)gi * NJ + gj] = Rb[(r + 2) * w2 + (q + 2)];
+            }
+        }
+    };
     // after a ring load: the register copy of row h1 (the outer ring row)
     auto refresh_ring_row = [&](float *reg, const float *arr) {
 #pragma unroll
@@ -1076,6 +1107,15 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
             const float2 newSigma = make_float2(rec.x, rec.y);
             // a zero at a chunk-end unit row needs the backward scan; otherwise
             // the largest |r| over the blocks decides
+            if (RPS > 0 && rec.w != 0.f) {
+                // the scan reads r anywhere in a chunk: every tile publishes
+                // all of r_it (still intact in Rb) and the grid waits for it
+                publish_tile_r((it & 1) ? a.r1 : a.r0);
+                __syncthreads();
+                arrive(0u);
+                wait_sum(pA, false); // completes the barrier (the sum is unused)
+                if (!ok()) return;
+            }
             const bool done = rec.w != 0.f
                                   ? chunk_converged(a, (it & 1) ? a.r1 : a.r0, tt, &s_flag)
                                   : tol_met(tt, rec.z, has_min_static);
@@ -1120,11 +1160,13 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
                 // padding rows may hold anything, even inf: select, do not scale
                 qs = on_tile(rr) ? fmaf(q, Sr[rr], qs) : qs;
             }
+            // only the 2-cell band along the tile's border is published: it
+            // is all that neighbours' rings read
             if (!first && gj < NJ) {
 #pragma unroll
                 for (int rr = 0; rr < kR; rr++) {
                     const int gi = ti0 + row0 + rr - 1;
-                    if (on_tile(rr) && gi < NI) s_pub[(size_t)gi * NJ + gj] = Sr[rr];
+                    if (on_tile(rr) && in_band(rr) && gi < NI) s_pub[(size_t)gi * NJ + gj] = Sr[rr];
                 }
             }
         } else {
@@ -1213,11 +1255,13 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
                                           Rb[c - 1], Rb[c + 1]);
                 zr = on_tile(rr) ? fmaf(z, Rr[rr], zr) : zr;
             }
+            // the band only, as for s; the rare backward max-abs scan gets the
+            // whole tile published on demand (publish_tile_r)
             if (gj < NJ) {
 #pragma unroll
                 for (int rr = 0; rr < kR; rr++) {
                     const int gi = ti0 + row0 + rr - 1;
-                    if (on_tile(rr) && gi < NI) r_pub[(size_t)gi * NJ + gj] = Rr[rr];
+                    if (on_tile(rr) && in_band(rr) && gi < NI) r_pub[(size_t)gi * NJ + gj] = Rr[rr];
                 }
             }
         } else {
@@ -1237,15 +1281,22 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
         }
         __syncthreads();
         // |r_{it+1}| at each chunk's last unit row, from the tile holding it
-        for (int k = threadIdx.x; k < a.nchunks; k += blockDim.x) {
-            const int idx = a.chunk_last_unit[k];
-            if (idx < 0) continue;
-            const int gi = idx / NJ, gj = idx - gi * NJ;
-            if (gi < ti0 || gi >= ti0 + ti || gj < tj0 || gj >= tj0 + tj) continue;
-            const float v = Rb[(gi - ti0 + 2) * w2 + (gj - tj0 + 2)];
+        auto chunk_end_value = [&](int k, float v) {
             reinterpret_cast<float *>(a.chunk_val)[k] = v != 0.f ? fabsf(v) : -1.f;
             if (v != 0.f) atomicMax(&s_cmax, __float_as_int(fabsf(v))); // order of non-negative floats
             else s_cscan = 1;
+        };
+        if (s_nown <= kMaxOwnedChunks) {
+            for (int j = threadIdx.x; j < s_nown; j += blockDim.x)
+                chunk_end_value(s_own[j].x, Rb[s_own[j].y]);
+        } else {
+            for (int k = threadIdx.x; k < a.nchunks; k += blockDim.x) {
+                const int idx = a.chunk_last_unit[k];
+                if (idx < 0) continue;
+                const int gi = idx / NJ, gj = idx - gi * NJ;
+                if (gi < ti0 || gi >= ti0 + ti || gj < tj0 || gj >= tj0 + tj) continue;
+                chunk_end_value(k, Rb[(gi - ti0 + 2) * w2 + (gj - tj0 + 2)]);
+            }
         }
         {
             const float2 part = bsum0(zr, smf); // its barrier also orders s_cmax / s_cscan
