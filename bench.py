@@ -43,10 +43,11 @@ SEED = 7
 WARM_FRAMES = 2
 METRIC = "particle-substeps/s"
 WORKLOAD = "dam_break_1024_obstacle"
-# DRAM bytes (read + write) of one k_pcg_resident launch, from the ncu
-# capture summarised in profiles/k_pcg_resident_dam_break_1024.md; the solve
-# keeps its vectors on chip, so this is b and the operator in, x out
-PCG_TRAFFIC_BYTES = None
+# DRAM bytes (read + write) of one k_pcg_resident launch at 1024^2, from the
+# ncu capture summarised in profiles/k_pcg_resident_dam_break.md; the solve
+# keeps its vectors on chip, so this is little more than b and the operator
+# in, x out
+PCG_TRAFFIC_BYTES = 12966400
 
 
 def set_resolution(res: int):
@@ -133,6 +134,21 @@ class ClockSampler:
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sms) if sms else None, "sm_max_mhz": mx,
                 "reasons": sorted(reasons), "samples": len(sms)}
+
+
+def combine_replicas(ms: float, work: float, dist=None, device: str = "cpu"):
+    """Whole-job figures of independent replicas (one scene per rank, no
+    collective on the data path): the slowest rank's time and the sum of the
+    particle-substeps all ranks processed."""
+    if dist is None:
+        return ms, work
+    import torch
+
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    w = torch.tensor([float(work)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(w, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(w.item())
 
 
 def executed_iters(ret: int, limit: int) -> int:
@@ -255,12 +271,8 @@ def gpu_arm(args):
     torch.cuda.synchronize()
     clocks = sampler.stop()
     s.enable_timers(False)
-    total_ms = float(sum(step_ms))
-    if dist:
-        t = torch.tensor([total_ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * work / (total_ms / 1e3)
+    total_ms, work = combine_replicas(float(sum(step_ms)), work, dist, f"cuda:{local}")
+    value = work / (total_ms / 1e3)
 
     # end to end through the C ABI with host-resident state: upload particles
     # and the carried grids, one substep, download them again
@@ -284,7 +296,8 @@ def gpu_arm(args):
         snap_p = s.get_particles()
         snap_g = {g: s.get_grid(g) for g in carried}
     e2e_s = time.perf_counter() - t0
-    e2e_value = world * e2e_work / e2e_s
+    e2e_ms, e2e_work = combine_replicas(1e3 * e2e_s, e2e_work, dist, f"cuda:{local}")
+    e2e_value = e2e_work / (e2e_ms / 1e3)
 
     peak, peak_kind = measured_peaks()
     achieved = bytes_pcg / (pcg_ms / 1e3) / 1e9 if pcg_ms > 0 else None

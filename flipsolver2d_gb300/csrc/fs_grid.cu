@@ -452,7 +452,8 @@ __device__ __forceinline__ float bfs_layer_value(const int *mark, const float *v
                                                  bool minus_one)
 {
     float s = 0.f, eh = 0.f, el = 0.f, m = 0.f;
-    int count = 0;
+    int count = 0, mine = INT_MAX;
+    bool el_exact = true;
 #pragma unroll
     for (int io = -1; io <= 1; io++)
 #pragma unroll
@@ -468,25 +469,53 @@ __device__ __forceinline__ float bfs_layer_value(const int *mark, const float *v
             s = t2;
             ls_two_sum(eh, er, t3, er2);
             eh = t3;
+            el_exact &= er2 == 0.f;
             el += er2;
             m += fabsf(x);
+            if (x != 0.f) mine = min(mine, ilogbf(x));
             count++;
         }
     const float cf = (float)count;
     const float qh = __fdiv_rn(s, cf);
     const float rem = fmaf(-qh, cf, s); // exact
-    float t1, t2;
+    float t1, t2, v, ev, u, eu;
     ls_two_sum(rem, eh, t1, t2);
-    const float ql = __fdiv_rn(t1 + (t2 + el), cf);
-    float h, l;
+    ls_two_sum(t2, el, v, ev);
+    ls_two_sum(t1, v, u, eu);
+    const float ql = __fdiv_rn(u, cf);
+    // the quotient qh + ql is exact when the remainder terms added exactly
+    // and ql times the count gives them back
+    const bool q_exact = ev == 0.f && eu == 0.f && fmaf(ql, cf, -u) == 0.f;
+    float h, l, err3 = 0.f;
     if (minus_one) {
         ls_two_sum(qh, -1.f, h, l);
-        l += ql;
+        float l2;
+        ls_two_sum(l, ql, l2, err3);
+        l = l2;
     } else {
         h = qh;
         l = ql;
     }
     const float f = h + l;
+    // Exact case, which covers the frequent exact ties (a value exactly half
+    // way between two floats): when every error term above was captured
+    // exactly (el_exact, q_exact, err3 == 0), h + l is the exact value.  When
+    // the inputs also span few enough binades (27 for the sum; 52 bits for the
+    // quotient minus one) every double operation of the reference is exact as
+    // well, and both round the same exact value to float, ties to even.
+    if (count > 0 && el_exact && q_exact && err3 == 0.f && mine >= -100 && m < 0x1p100f) {
+        const int em = m > 0.f ? ilogbf(m) : -1000;
+        const bool sum_exact = m == 0.f || em - mine <= 27;
+        const int ea = qh != 0.f ? ilogbf(qh) : -1000;
+        const int lsb = min(qh != 0.f ? ilogbf(qh) - 23 : INT_MAX, ql != 0.f ? ilogbf(ql) - 23 : INT_MAX);
+        // qh + ql (the quotient) must fit a double, and so must it minus one
+        const bool sub_exact = minus_one ? (max(ea, 0) + 1 - min(lsb, 0) <= 52) : (ea - lsb <= 51);
+        if (sum_exact && sub_exact) {
+            if (f != 0.f && isfinite(f)) return f;
+            // an exact zero sum: the reference's double sum is +0 as well
+            if (!minus_one && s == 0.f && eh == 0.f && el == 0.f) return 0.f;
+        }
+    }
     const float d = (h - f) + l;
     const float bound = (m + 1.f) * 0x1p-44f;
     const float gap = 0.5f * fminf(nextafterf(f, INFINITY) - f, f - nextafterf(f, -INFINITY));

@@ -32,7 +32,8 @@ namespace fsg {
 
 constexpr int kThreads = 1024;
 constexpr int kStripThreads = 512;
-constexpr int kMaxOwnedChunks = 64; // chunk ends a resident tile lists in shared memory // resident kernel with register strips: 128 registers a thread
+constexpr int kMaxOwnedChunks = 64; // chunk ends a resident tile lists in shared memory
+constexpr int kPartRounds = 8;      // per-lane partial loads: up to 256 resident blocks // resident kernel with register strips: 128 registers a thread
 constexpr long long kSpinLimit = 1LL << 25; // a few seconds with the sleeps
 
 __device__ __forceinline__ unsigned smem_u32(const void *p)
@@ -142,7 +143,19 @@ __device__ __forceinline__ float2 psum(const float2 *partials, int nblocks, floa
 {
     if (threadIdx.x < 32) {
         float2 a = make_float2(0.f, 0.f);
-        for (int k = threadIdx.x; k < nblocks; k += 32) a = ff_add(a, __ldcg(partials + k));
+        if (nblocks <= 32 * kPartRounds) {
+            // issue every load before consuming any: one L2 round trip
+            float2 v[kPartRounds];
+#pragma unroll
+            for (int i = 0; i < kPartRounds; i++) {
+                const int k = (int)threadIdx.x + 32 * i;
+                v[i] = k < nblocks ? __ldcg(partials + k) : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int i = 0; i < kPartRounds; i++) a = ff_add(a, v[i]);
+        } else {
+            for (int k = threadIdx.x; k < nblocks; k += 32) a = ff_add(a, __ldcg(partials + k));
+        }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) a = ff_add(a, ff_shfl_down(a, o));
         if (threadIdx.x == 0) sm[34] = a;
@@ -893,15 +906,32 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
             float2 acc = make_float2(0.f, 0.f);
             float mx = 0.f, sc = 0.f;
             if (ok) {
-                for (int k = lane; k < G; k += 32) {
-                    if (rec4) {
-                        const float4 v = __ldcg(reinterpret_cast<const float4 *>(parts) + k);
-                        acc = ff_acc(acc, make_float2(v.x, v.y));
-                        mx = fmaxf(mx, v.z);
-                        sc = fmaxf(sc, v.w);
-                    } else {
-                        acc = ff_acc(acc, __ldcg(reinterpret_cast<const float2 *>(parts) + k));
+                // all of a lane's loads are issued before any is consumed:
+                // one L2 round trip instead of one per partial (G <= 32 kPartRounds)
+                if (rec4) {
+                    float4 v[kPartRounds];
+#pragma unroll
+                    for (int i = 0; i < kPartRounds; i++) {
+                        const int k = lane + 32 * i;
+                        v[i] = k < G ? __ldcg(reinterpret_cast<const float4 *>(parts) + k)
+                                     : make_float4(0.f, 0.f, 0.f, 0.f);
                     }
+#pragma unroll
+                    for (int i = 0; i < kPartRounds; i++) {
+                        acc = ff_acc(acc, make_float2(v[i].x, v[i].y));
+                        mx = fmaxf(mx, v[i].z);
+                        sc = fmaxf(sc, v[i].w);
+                    }
+                } else {
+                    float2 v[kPartRounds];
+#pragma unroll
+                    for (int i = 0; i < kPartRounds; i++) {
+                        const int k = lane + 32 * i;
+                        v[i] = k < G ? __ldcg(reinterpret_cast<const float2 *>(parts) + k)
+                                     : make_float2(0.f, 0.f);
+                    }
+#pragma unroll
+                    for (int i = 0; i < kPartRounds; i++) acc = ff_acc(acc, v[i]);
                 }
             }
 #pragma unroll
@@ -1438,8 +1468,9 @@ static size_t resident_smem(int ti, int tj)
 bool resident_tile_shape(int ni, int nj, int *ti, int *tj)
 {
     // among tile widths 32..256, the shape with the fewest cells per block
-    // including the 1-halo it recomputes, with at most one tile per SM
-    const int blocks = sm_count();
+    // including the 1-halo it recomputes, with at most one tile per SM (and
+    // no more tiles than the grid reduction reads partials for)
+    const int blocks = min(sm_count(), 32 * kPartRounds);
     long long best = -1;
     for (int w = 32; w <= 256; w *= 2) {
         const long long tiles_j = (nj + w - 1) / w;
