@@ -573,64 +573,66 @@ template <int W, int H>
 __device__ __forceinline__ void bfs_layers(int *mark, float *val, short *fa, short *fb, int *cnt,
                                            int k0, bool minus_one)
 {
-    struct {
-        int *mark;
-        float *val;
-    } t{mark, val};
-    if (threadIdx.x == 0) cnt[0] = 0;
+    // cnt[0..2]: rotating list lengths (the list of layer k is counted in
+    // cnt[k % 3]; cnt[(k + 2) % 3] is free while layer k is processed)
+    if (threadIdx.x < 3) cnt[threadIdx.x] = 0;
     __syncthreads();
-    // the frontier: cells of layer k0 (blockDim.x is a multiple of 32, so
-    // whole warps run every round)
+    // claims the unmarked neighbours of cell e for layer k + 1 and lists them
+    // (all threads of a warp call it; `live` says whether e is a real cell)
+    auto expand = [&](bool live, int e, int k, short *out, int *counter) {
+        int r = 0, q = 0;
+        unsigned got = 0; // bit (io+1)*3+(jo+1) for each neighbour claimed
+        if (live) {
+            r = e / W;
+            q = e - r * W;
+#pragma unroll
+            for (int io = -1; io <= 1; io++)
+#pragma unroll
+                for (int jo = -1; jo <= 1; jo++) {
+                    if (io == 0 && jo == 0) continue;
+                    const int rr = r + io, qq = q + jo;
+                    if (rr < 0 || rr >= W || qq < 0 || qq >= W) continue;
+                    const int n = rr * W + qq;
+                    if (mark[n] == kMarkInf && atomicCAS(&mark[n], kMarkInf, k + 1) == kMarkInf)
+                        got |= 1u << ((io + 1) * 3 + (jo + 1));
+                }
+        }
+        int slot = warp_append(counter, __popc(got));
+#pragma unroll
+        for (int b = 0; b < 9; b++)
+            if (got & (1u << b)) out[slot++] = (short)((r + b / 3 - 1) * W + (q + b % 3 - 1));
+    };
+    // layer k0 (final from earlier passes) discovers layer k0 + 1
     for (int e0 = 0; e0 < W * W; e0 += blockDim.x) {
         const int e = e0 + (int)threadIdx.x;
-        const int mine = (e < W * W && t.mark[e] == k0) ? 1 : 0;
-        const int slot = warp_append(&cnt[0], mine);
-        if (mine) fa[slot] = (short)e;
+        expand(e < W * W && mark[e] == k0, e, k0, fa, &cnt[(k0 + 1) % 3]);
     }
     __syncthreads();
     short *cur = fa, *nxt = fb;
-    int ncur = cnt[0];
+    // One phase per layer k: the values of layer-k cells (they read only
+    // layers < k, all final) and the discovery of layer k + 1 from them
+    // (claiming cells that are unmarked; a value never counts a neighbour of
+    // layer k or above, so the two do not interfere).
     for (int k = k0 + 1; k <= k0 + H; k++) {
+        const int ncur = cnt[k % 3];
         if (ncur == 0) break;
-        if (threadIdx.x == 0) cnt[1] = 0;
-        __syncthreads();
+        if (threadIdx.x == 0) cnt[(k + 2) % 3] = 0;
+        const bool more = k < k0 + H;
         for (int f0 = 0; f0 < ncur; f0 += blockDim.x) {
             const int f = f0 + (int)threadIdx.x;
-            int r = 0, q = 0;
-            unsigned got = 0; // neighbours this cell claimed, bit (io+1)*3+(jo+1)
-            if (f < ncur) {
-                const int e = cur[f];
-                r = e / W;
-                q = e - r * W;
-#pragma unroll
-                for (int io = -1; io <= 1; io++)
-#pragma unroll
-                    for (int jo = -1; jo <= 1; jo++) {
-                        if (io == 0 && jo == 0) continue;
-                        const int rr = r + io, qq = q + jo;
-                        if (rr < 0 || rr >= W || qq < 0 || qq >= W) continue;
-                        const int n = rr * W + qq;
-                        if (t.mark[n] == kMarkInf && atomicCAS(&t.mark[n], kMarkInf, k) == kMarkInf)
-                            got |= 1u << ((io + 1) * 3 + (jo + 1));
-                    }
+            const bool live = f < ncur;
+            int e = 0;
+            if (live) {
+                e = cur[f];
+                const int r = e / W, q = e - r * W;
+                val[e] = bfs_layer_value<W>(mark, val, r, q, k, minus_one);
             }
-            int slot = warp_append(&cnt[1], __popc(got));
-#pragma unroll
-            for (int b = 0; b < 9; b++)
-                if (got & (1u << b)) nxt[slot++] = (short)((r + b / 3 - 1) * W + (q + b % 3 - 1));
-        }
-        __syncthreads();
-        const int nnext = cnt[1];
-        for (int f = threadIdx.x; f < nnext; f += blockDim.x) {
-            const int e = nxt[f];
-            const int r = e / W, q = e - r * W;
-            t.val[e] = bfs_layer_value<W>(t.mark, t.val, r, q, k, minus_one);
+            if (more) expand(live, e, k, nxt, &cnt[(k + 1) % 3]);
         }
         __syncthreads();
         short *tmp = cur;
         cur = nxt;
         nxt = tmp;
-        ncur = nnext;
     }
 }
 
@@ -648,7 +650,7 @@ __global__ void __launch_bounds__(1024) k_vel_extrap(GridDims d, Grids G, float 
     __shared__ BfsTile<kVelH> t;
     __shared__ short fa[BfsTile<kVelH>::W * BfsTile<kVelH>::W];
     __shared__ short fb[BfsTile<kVelH>::W * BfsTile<kVelH>::W];
-    __shared__ int cnt[2];
+    __shared__ int cnt[3];
     constexpr int W = BfsTile<kVelH>::W;
     const bool isV = blockIdx.z == 1;
     const int si = isV ? d.ni : d.ni + 1, sj = isV ? d.nj + 1 : d.nj;
