@@ -348,6 +348,41 @@ def gpu_arm(args):
     return 0
 
 
+def poisson_arm(args):
+    """Standalone mixed-precision pressure solves (--poisson N): the spec-mode
+    solve to a 1e-6 true relative residual on a seeded 55 %-fluid star mask
+    with the divergence of N(0, 1) face velocities as right-hand side.  Each
+    step is one whole solve through fs_pcg_solve_spec with host arrays, so the
+    time includes the uploads and the download."""
+    from flipsolver2d_gb300 import build, gpu, scenes
+
+    build.build()
+    n = args.poisson
+    m, b, dx = scenes.poisson_case(n, seed=0)
+    for _ in range(args.warmup):
+        gpu.pcg_solve_spec(m, b, 1.0 / 30, 1000.0, dx, 1e-6)
+    times, iters, rr = [], [], 0.0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        it, x, rr = gpu.pcg_solve_spec(m, b, 1.0 / 30, 1000.0, dx, 1e-6)
+        times.append(time.perf_counter() - t0)
+        iters.append(it)
+    total = sum(times)
+    cells = n * n
+    line = {"metric": "pcg-cell-iter/s", "value": cells * sum(iters) / total, "unit": "cell-iter/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic (seeded star mask, N(0,1) face velocities)",
+            "config": {"workload": f"poisson_{n}_spec", "grid": n, "rel_tol": 1e-6,
+                       "solver": "FP32 PCG, textbook IPP, FP64 refinement"},
+            "inner_iterations": iters, "rel_residual": rr,
+            "e2e": {"value": cells * sum(iters) / total, "unit": "cell-iter/s",
+                    "h2d_bytes_per_step": int(m.nbytes + b.nbytes), "d2h_bytes_per_step": int(b.nbytes)}}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -356,10 +391,14 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--res", type=int, default=RES, help="grid side of the dam break (default 1024)")
+    ap.add_argument("--poisson", type=int, default=0,
+                    help="time standalone spec-mode pressure solves on an N x N grid instead")
     args = ap.parse_args()
     set_resolution(args.res)
     if args.warmup < 3:
         args.warmup = 3
+    if args.poisson:
+        return poisson_arm(args)
     if args.impl == "reference":
         return reference_arm(args)
     return gpu_arm(args)

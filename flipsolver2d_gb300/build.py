@@ -2,7 +2,7 @@
 
     python -m flipsolver2d_gb300.build
 
-Compiles the four translation units in parallel with nvcc for sm_103a only
+Compiles the translation units in parallel with nvcc for sm_103a only
 and links them into flipsolver2d_gb300/_build/libfsgpu.so (in-tree, git
 ignored).  The particle and grid kernels and the host driver are built with
 -fmad=false (and the host compiler with -ffp-contract=off) so that every float
@@ -29,6 +29,7 @@ UNITS = {
     "fs_api.cu": ["-fmad=false"],
     "fs_pcg.cu": ["-fmad=true"],
     "fs_pcg_tma.cu": ["-fmad=true"],
+    "fs_spec.cu": ["-fmad=true"],
 }
 
 

@@ -29,6 +29,7 @@
 #include "../../include/fs_gpu.h"
 #include "fs_pcg.h"
 #include "fs_pcg_tma.h"
+#include "fs_spec.h"
 #include "fs_state.h"
 
 using namespace fsg;
@@ -1441,6 +1442,133 @@ extern "C" fs_status fs_pcg_solve_device(int ni, int nj, const int8_t *material_
     TRY(pcg_cache_get(dev, N, esz, std::min<long long>(T, (long long)N), &c));
     return pcg_solve_common(ni, nj, material_device, dt, density, dx, rhs_device, result_device,
                             iter_limit, tol, exec, iterations, c, prec);
+}
+
+// ---------------------------------------------------------------------------
+// fs_pcg_solve_spec: the pressure solve to a true relative residual with FP32
+// inner PCG iterations (textbook incomplete-Poisson preconditioner) and FP64
+// outer refinement (fs_spec.cu).
+// ---------------------------------------------------------------------------
+extern "C" fs_status fs_pcg_solve_spec(int ni, int nj, const int8_t *material, float dt, double density,
+                                       double dx, const double *rhs, double *result, double rel_tol,
+                                       int max_iter, const fs_exec_params *exec, int *iterations,
+                                       double *rel_residual)
+{
+    if (ni < 1 || nj < 1 || !material || !rhs || !result || max_iter < 0 || !(rel_tol > 0.0))
+        return fail(FS_ERR_BAD_ARG, "fs_pcg_solve_spec: invalid argument");
+    if (!valid_material(material, (size_t)ni * nj))
+        return fail(FS_ERR_BAD_ARG, "fs_pcg_solve_spec: unknown material code");
+    const long long N = (long long)ni * nj;
+    const int dev = exec ? exec->device : 0;
+    CK(cudaSetDevice(dev));
+    const double scale = (double)dt / (density * dx * dx);
+    cudaStream_t st = 0;
+    // device buffers for this call
+    std::vector<void *> bufs;
+    auto dalloc_tmp = [&](void **p, size_t bytes) -> fs_status {
+        cudaError_t e = cudaMalloc(p, bytes);
+        if (e != cudaSuccess) {
+            for (void *q : bufs) cudaFree(q);
+            return fail(e == cudaErrorMemoryAllocation ? FS_ERR_OOM : FS_ERR_CUDA,
+                        "fs_pcg_solve_spec: cudaMalloc: %s", cudaGetErrorString(e));
+        }
+        bufs.push_back(*p);
+        return FS_OK;
+    };
+    int8_t *mat = nullptr;
+    uint8_t *info = nullptr;
+    double *b = nullptr, *x = nullptr, *part = nullptr;
+    float *r = nullptr, *d = nullptr, *s = nullptr, *q = nullptr, *y = nullptr, *z = nullptr;
+    float2 *partials = nullptr;
+    int *chunk_last = nullptr;
+    Scalars *sc = nullptr;
+    unsigned *count = nullptr;
+    int *iters_dev = nullptr;
+    const int rblocks = 1024;
+    TRY(dalloc_tmp((void **)&mat, N));
+    TRY(dalloc_tmp((void **)&info, N));
+    TRY(dalloc_tmp((void **)&b, N * 8));
+    TRY(dalloc_tmp((void **)&x, N * 8));
+    TRY(dalloc_tmp((void **)&part, rblocks * 8));
+    float **fv[] = {&r, &d, &s, &q, &y, &z};
+    for (float **v : fv) TRY(dalloc_tmp((void **)v, N * 4));
+    TRY(dalloc_tmp((void **)&partials, (size_t)spec_partials_needed() * sizeof(float2)));
+    TRY(dalloc_tmp((void **)&chunk_last, 2 * sizeof(int)));
+    TRY(dalloc_tmp((void **)&sc, sizeof(Scalars)));
+    TRY(dalloc_tmp((void **)&count, sizeof(unsigned)));
+    TRY(dalloc_tmp((void **)&iters_dev, sizeof(int)));
+    auto release = [&]() {
+        for (void *p : bufs) cudaFree(p);
+        bufs.clear();
+    };
+    auto check = [&](cudaError_t e, const char *what) -> fs_status {
+        if (e == cudaSuccess) return FS_OK;
+        release();
+        return fail(FS_ERR_CUDA, "fs_pcg_solve_spec: %s: %s", what, cudaGetErrorString(e));
+    };
+    TRY(check(cudaMemcpyAsync(mat, material, N, cudaMemcpyHostToDevice, st), "upload"));
+    TRY(check(cudaMemcpyAsync(b, rhs, N * 8, cudaMemcpyHostToDevice, st), "upload"));
+    TRY(check(cudaMemsetAsync(x, 0, N * 8, st), "memset"));
+    TRY(check(cudaMemsetAsync(sc, 0, sizeof(Scalars), st), "memset"));
+    GridDims gd{ni, nj, ni / 3 + (ni % 3 != 0), nj / 3 + (nj % 3 != 0)};
+    Grids G;
+    G.material = mat;
+    G.cell_info = info;
+    launch_decomposition(gd, G, chunk_last, 1, N, 0, sc, st);
+    g_kernel_launches += 1;
+
+    std::vector<double> hp(rblocks);
+    double bnorm = 0.0, rnorm = 0.0;
+    int total_inner = 0;
+    int h_status = 0;
+    for (int outer = 0;; outer++) {
+        TRY(check(launch_spec_residual(info, b, x, r, N, nj, scale, part, rblocks, st), "residual"));
+        g_kernel_launches += 1;
+        TRY(check(cudaMemcpyAsync(hp.data(), part, rblocks * 8, cudaMemcpyDeviceToHost, st), "readback"));
+        TRY(check(cudaStreamSynchronize(st), "sync"));
+        double ss = 0.0;
+        for (double v : hp) ss += v;
+        rnorm = std::sqrt(ss);
+        if (outer == 0) bnorm = rnorm;
+        if (bnorm == 0.0 || rnorm <= rel_tol * bnorm || total_inner >= max_iter || outer >= 32) break;
+        SpecArgs a{};
+        a.ni = ni;
+        a.nj = nj;
+        a.N = N;
+        a.info = info;
+        a.scale = scale;
+        a.r = r;
+        a.d = d;
+        a.s = s;
+        a.q = q;
+        a.y = y;
+        a.z = z;
+        a.partials = partials;
+        a.count = count;
+        a.status = &sc->pcg_status;
+        a.iters = iters_dev;
+        a.eps_in = 1e-4f;
+        a.max_iter = max_iter - total_inner;
+        TRY(check(launch_spec_pcg(a, st), "inner PCG"));
+        TRY(check(launch_spec_update(x, d, N, st), "update"));
+        g_kernel_launches += 2;
+        int it = 0;
+        TRY(check(cudaMemcpyAsync(&it, iters_dev, sizeof(int), cudaMemcpyDeviceToHost, st), "readback"));
+        TRY(check(cudaMemcpyAsync(&h_status, &sc->pcg_status, sizeof(int), cudaMemcpyDeviceToHost, st),
+                  "readback"));
+        TRY(check(cudaStreamSynchronize(st), "sync"));
+        if (h_status != 0) {
+            release();
+            return fail(FS_ERR_TIMEOUT, "fs_pcg_solve_spec: a grid barrier wait timed out");
+        }
+        total_inner += it;
+        if (it == 0) break; // no progress possible
+    }
+    TRY(check(cudaMemcpy(result, x, N * 8, cudaMemcpyDeviceToHost), "download"));
+    release();
+    if (iterations) *iterations = total_inner;
+    if (rel_residual) *rel_residual = bnorm > 0.0 ? rnorm / bnorm : 0.0;
+    return FS_OK;
 }
 
 // ---------------------------------------------------------------------------

@@ -1,0 +1,363 @@
+// fs_spec.cu -- the spec-mode pressure solve: mixed precision to a true
+// relative residual.
+//
+// The reference's hot-path PCG (linearsolver.cpp:25-73 with the asymmetric
+// IPP of getIPPCoefficients) cannot reach a 1e-6 relative residual: its
+// preconditioner is not symmetric and the iteration stalls.  The reference
+// also ships a textbook incomplete-Poisson preconditioner it never uses on
+// the hot path (inversepoissonpreconditioner.h:45-79): M = K K^T with
+// K = I - L D^-1, L the strictly lower part of the pressure matrix A (linear
+// index order) and D its diagonal.  This file solves A x = b with it:
+//
+//   outer (FP64):  r = b - A x;  stop when ||r|| <= tol ||b||
+//   inner (FP32):  PCG on A d = r with M, to a relative reduction eps_in
+//   outer (FP64):  x += d
+//
+// A is the operator of getPressureProjectionMatrix exactly as the reference
+// builds it (unit rows with their fluid-neighbour mask and non-solid count,
+// linear-index neighbours, identity rows elsewhere), read from the packed
+// operator byte of k_decomposition.  K(c, n) for a lower neighbour n of unit
+// row c is scale / A(n, n) (Eigen's zero-diagonal rule: 1), i.e. 1 / count(n)
+// for a unit n.
+//
+// The inner PCG is one cooperative kernel over the linear index with FP32
+// vectors and float-pair reductions.  It forms q = A s as A z + beta q (the
+// same vector, one fewer grid barrier), so an iteration takes four barriers.
+#include <cfloat>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "fs_pcg.h"
+#include "fs_spec.h"
+
+namespace fsg {
+
+constexpr int kSpecThreads = 512;
+constexpr long long kSpecSpin = 1LL << 25;
+
+// ---------------------------------------------------------------------------
+// the operator and the preconditioner, from the packed operator byte
+// (bit 7 unit row, bits 4-6 non-solid count, bits 0-3 fluid-neighbour mask)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float spec_k(uint8_t info_n, float scale)
+{
+    const int cnt = (info_n >> 4) & 7;
+    return ((info_n & 0x80) && cnt > 0) ? 1.f / (float)cnt : scale;
+}
+
+template <typename T>
+__device__ __forceinline__ T spec_a(const uint8_t *__restrict__ info, const T *__restrict__ v, long long c,
+                                    long long N, int NJ, T scale)
+{
+    const uint8_t p = info[c];
+    const T vc = v[c];
+    if (!(p & 0x80)) return vc;
+    T nb = 0;
+    if ((p & 1) && c - NJ >= 0) nb += v[c - NJ];
+    if ((p & 2) && c + NJ < N) nb += v[c + NJ];
+    if ((p & 4) && c - 1 >= 0) nb += v[c - 1];
+    if ((p & 8) && c + 1 < N) nb += v[c + 1];
+    return scale * ((T)((p >> 4) & 7) * vc - nb);
+}
+
+// ---------------------------------------------------------------------------
+// FP64 outer residual r = b - A x, its FP32 copy and the block sums of r.r
+// ---------------------------------------------------------------------------
+__global__ void k_spec_residual(const uint8_t *__restrict__ info, const double *__restrict__ b,
+                                const double *__restrict__ x, float *__restrict__ r32, long long N,
+                                int NJ, double scale, double *__restrict__ partial)
+{
+    __shared__ double sm[32];
+    double acc = 0.0;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < N;
+         c += (long long)gridDim.x * blockDim.x) {
+        const double r = b[c] - spec_a<double>(info, x, c, N, NJ, scale);
+        r32[c] = (float)r;
+        acc += r * r;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < (blockDim.x >> 5) ? sm[threadIdx.x] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) partial[blockIdx.x] = v;
+    }
+}
+
+__global__ void k_spec_update(double *__restrict__ x, const float *__restrict__ d, long long N)
+{
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < N;
+         c += (long long)gridDim.x * blockDim.x)
+        x[c] += (double)d[c];
+}
+
+// ---------------------------------------------------------------------------
+// inner FP32 PCG
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void spec_two_sum(float a, float b, float &s, float &e)
+{
+    s = a + b;
+    const float bv = s - a;
+    e = (a - (s - bv)) + (b - bv);
+}
+__device__ __forceinline__ float2 spec_ff_add(float2 a, float2 b)
+{
+    float s, e;
+    spec_two_sum(a.x, b.x, s, e);
+    e += a.y + b.y;
+    const float h = s + e;
+    return make_float2(h, e - (h - s));
+}
+__device__ __forceinline__ float2 spec_shfl(float2 v, int o)
+{
+    return make_float2(__shfl_down_sync(0xffffffffu, v.x, o), __shfl_down_sync(0xffffffffu, v.y, o));
+}
+__device__ __forceinline__ float spec_ff_div(float2 a, float2 b)
+{
+    const float q = __fdiv_rn(a.x, b.x);
+    const float r = (fmaf(-q, b.x, a.x) + a.y) - q * b.y;
+    return q + __fdiv_rn(r, b.x);
+}
+
+// block sums of two per-thread values as float pairs; results in thread 0
+__device__ __forceinline__ void spec_bsum2(float v0, float v1, float2 *sm, float2 &o0, float2 &o1)
+{
+    float2 a = make_float2(v0, 0.f), b = make_float2(v1, 0.f);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a = spec_ff_add(a, spec_shfl(a, o));
+        b = spec_ff_add(b, spec_shfl(b, o));
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) {
+        sm[w] = a;
+        sm[32 + w] = b;
+    }
+    __syncthreads();
+    if (w == 0) {
+        const bool in = lane < (int)(blockDim.x >> 5);
+        a = in ? sm[lane] : make_float2(0.f, 0.f);
+        b = in ? sm[32 + lane] : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a = spec_ff_add(a, spec_shfl(a, o));
+            b = spec_ff_add(b, spec_shfl(b, o));
+        }
+    }
+    o0 = a;
+    o1 = b;
+    __syncthreads();
+}
+
+__device__ __forceinline__ unsigned spec_ld_acquire(const unsigned *p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+struct SpecGrid {
+    unsigned *count; // monotonic arrival counter (zeroed at launch)
+    int *status;
+    unsigned n;      // barriers passed
+};
+
+// grid barrier: fence + relaxed add, then one thread polls the counter
+__device__ __forceinline__ bool spec_sync(SpecGrid &g)
+{
+    __syncthreads();
+    g.n++;
+    if (threadIdx.x == 0) {
+        asm volatile("fence.acq_rel.gpu;" ::: "memory");
+        asm volatile("red.relaxed.gpu.global.add.u32 [%0], 1;" ::"l"(g.count) : "memory");
+        const unsigned target = g.n * gridDim.x;
+        long long spins = 0;
+        while ((int)(spec_ld_acquire(g.count) - target) < 0) {
+            if (++spins > kSpecSpin || ((spins & 1023) == 0 && *((volatile int *)g.status) != 0)) {
+                atomicExch(g.status, 1);
+                break;
+            }
+        }
+    }
+    __syncthreads();
+    return *((volatile int *)g.status) == 0;
+}
+
+// every block sums the per-block float pairs in the same order
+__device__ __forceinline__ float2 spec_psum(const float2 *p, int G, float2 *bc, int which)
+{
+    if (threadIdx.x < 32) {
+        float2 a = make_float2(0.f, 0.f);
+        for (int k = threadIdx.x; k < G; k += 32) a = spec_ff_add(a, __ldcg(p + k));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a = spec_ff_add(a, spec_shfl(a, o));
+        if (threadIdx.x == 0) bc[which] = a;
+    }
+    __syncthreads();
+    return bc[which];
+}
+
+__global__ void __launch_bounds__(kSpecThreads) k_pcg_spec(SpecArgs a)
+{
+    __shared__ float2 sm[64];
+    __shared__ float2 bc[4];
+    const long long N = a.N;
+    const int NJ = a.nj;
+    const int G = gridDim.x;
+    const long long stride = (long long)G * blockDim.x;
+    const long long c0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const float scale = (float)a.scale;
+    const uint8_t *__restrict__ info = a.info;
+    float *__restrict__ r = a.r, *__restrict__ s = a.s, *__restrict__ q = a.q;
+    float *__restrict__ y = a.y, *__restrict__ z = a.z, *__restrict__ d = a.d;
+    float2 *pA = a.partials, *pB = a.partials + G, *pC = a.partials + 2 * G;
+    SpecGrid g{a.count, a.status, 0u};
+
+    // y = K^T r
+    auto kt = [&](long long n) {
+        float v = r[n];
+        const float k = spec_k(info[n], scale);
+        if (n + NJ < N && (info[n + NJ] & 0x81) == 0x81) v = fmaf(k, r[n + NJ], v);
+        if (n + 1 < N && (info[n + 1] & 0x84) == 0x84) v = fmaf(k, r[n + 1], v);
+        return v;
+    };
+    // z = K y
+    auto kk = [&](long long c) {
+        const uint8_t p = info[c];
+        float v = y[c];
+        if (p & 0x80) {
+            if ((p & 1) && c - NJ >= 0) v = fmaf(spec_k(info[c - NJ], scale), y[c - NJ], v);
+            if ((p & 4) && c - 1 >= 0) v = fmaf(spec_k(info[c - 1], scale), y[c - 1], v);
+        }
+        return v;
+    };
+
+    // r_0 = the outer residual (already in r), d = 0, z = M r, s = z
+    for (long long c = c0; c < N; c += stride) {
+        d[c] = 0.f;
+        y[c] = kt(c);
+    }
+    if (!spec_sync(g)) return;
+    float rz = 0.f, rr = 0.f;
+    for (long long c = c0; c < N; c += stride) {
+        const float zc = kk(c);
+        z[c] = zc;
+        s[c] = zc;
+        rz = fmaf(r[c], zc, rz);
+        rr = fmaf(r[c], r[c], rr);
+    }
+    {
+        float2 b0, b1;
+        spec_bsum2(rz, rr, sm, b0, b1);
+        if (threadIdx.x == 0) {
+            pA[blockIdx.x] = b0;
+            pB[blockIdx.x] = b1;
+        }
+    }
+    if (!spec_sync(g)) return;
+    float2 sigma = spec_psum(pA, G, bc, 0);
+    const float2 rr0 = spec_psum(pB, G, bc, 1);
+    const float stop = a.eps_in * a.eps_in * rr0.x;
+    int it = 0;
+    bool first = true;
+    float fb = 0.f;
+    while (rr0.x > 0.f && it < a.max_iter) {
+        // s = z + beta s, q = A s = A z + beta q, and s.q
+        float sq = 0.f;
+        for (long long c = c0; c < N; c += stride) {
+            const float az = spec_a<float>(info, z, c, N, NJ, scale);
+            const float sc = first ? z[c] : fmaf(fb, s[c], z[c]);
+            const float qc = first ? az : fmaf(fb, q[c], az);
+            s[c] = sc;
+            q[c] = qc;
+            sq = fmaf(sc, qc, sq);
+        }
+        {
+            float2 b0, b1;
+            spec_bsum2(sq, 0.f, sm, b0, b1);
+            if (threadIdx.x == 0) pC[blockIdx.x] = b0;
+        }
+        if (!spec_sync(g)) return;
+        const float fa = spec_ff_div(sigma, spec_psum(pC, G, bc, 2));
+        for (long long c = c0; c < N; c += stride) {
+            d[c] = fmaf(fa, s[c], d[c]);
+            r[c] = fmaf(-fa, q[c], r[c]);
+        }
+        if (!spec_sync(g)) return;
+        for (long long c = c0; c < N; c += stride) y[c] = kt(c);
+        if (!spec_sync(g)) return;
+        rz = 0.f;
+        rr = 0.f;
+        for (long long c = c0; c < N; c += stride) {
+            const float zc = kk(c);
+            z[c] = zc;
+            rz = fmaf(r[c], zc, rz);
+            rr = fmaf(r[c], r[c], rr);
+        }
+        {
+            float2 b0, b1;
+            spec_bsum2(rz, rr, sm, b0, b1);
+            if (threadIdx.x == 0) {
+                pA[blockIdx.x] = b0;
+                pB[blockIdx.x] = b1;
+            }
+        }
+        if (!spec_sync(g)) return;
+        it++;
+        const float2 nsig = spec_psum(pA, G, bc, 0);
+        const float2 nrr = spec_psum(pB, G, bc, 1);
+        if (nrr.x <= stop) break;
+        fb = spec_ff_div(nsig, sigma);
+        sigma = nsig;
+        first = false;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.iters = it;
+}
+
+static int spec_grid()
+{
+    static int grid = 0;
+    if (!grid) {
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void *)k_pcg_spec, kSpecThreads, 0);
+        grid = sms * (per > 0 ? per : 1);
+    }
+    return grid;
+}
+
+int spec_partials_needed() { return 3 * spec_grid() + 8; }
+
+cudaError_t launch_spec_residual(const uint8_t *info, const double *b, const double *x, float *r32,
+                                 long long N, int NJ, double scale, double *partial, int nblocks,
+                                 cudaStream_t st)
+{
+    k_spec_residual<<<nblocks, 256, 0, st>>>(info, b, x, r32, N, NJ, scale, partial);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spec_update(double *x, const float *d, long long N, cudaStream_t st)
+{
+    const int blocks = (int)((N + 255) / 256 < 4096 ? (N + 255) / 256 : 4096);
+    k_spec_update<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(x, d, N);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spec_pcg(const SpecArgs &args, cudaStream_t st)
+{
+    SpecArgs a = args;
+    const long long want = (a.N + kSpecThreads - 1) / kSpecThreads;
+    int grid = spec_grid();
+    if (want < grid) grid = (int)(want < 1 ? 1 : want);
+    cudaError_t e = cudaMemsetAsync(a.count, 0, sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    void *kargs[] = {&a};
+    return cudaLaunchCooperativeKernel((const void *)k_pcg_spec, dim3(grid), dim3(kSpecThreads), kargs,
+                                       0, st);
+}
+
+} // namespace fsg

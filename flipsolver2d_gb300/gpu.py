@@ -94,6 +94,10 @@ _SIGS = {
                                            ctypes.c_float, ctypes.c_double, ctypes.c_double,
                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                            ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_pcg_solve_spec": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_float,
+                                         ctypes.c_double, ctypes.c_double, ctypes.c_void_p,
+                                         ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
+                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "fs_pcg_solve_device_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                                    ctypes.c_float, ctypes.c_double, ctypes.c_double,
                                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
@@ -317,3 +321,23 @@ def pcg_solve(material: np.ndarray, rhs: np.ndarray, dt: float, density: float, 
     it = GpuLinearSolver(precision, pool_threads).solve(material, dt, density, dx, x, rhs,
                                                         iter_limit, tol)
     return it, x
+
+
+def pcg_solve_spec(material: np.ndarray, rhs: np.ndarray, dt: float, density: float, dx: float,
+                   rel_tol: float = 1e-6, max_iter: int = 100000, device: int = 0):
+    """Spec-mode solve to a true relative residual (FP32 inner PCG with the
+    textbook IPP, FP64 refinement).  Returns (inner iterations, solution,
+    final relative residual)."""
+    lib = load()
+    ni, nj = material.shape
+    m = np.ascontiguousarray(material, np.int8)
+    b = np.ascontiguousarray(rhs, np.float64).reshape(ni, nj)
+    x = np.zeros((ni, nj), np.float64)
+    ex = ExecParams(FS_PCG_FP32, 0, device)
+    it = ctypes.c_int(0)
+    rr = ctypes.c_double(0.0)
+    st = lib.fs_pcg_solve_spec(ni, nj, m.ctypes.data, float(dt), float(density), float(dx),
+                               b.ctypes.data, x.ctypes.data, float(rel_tol), int(max_iter),
+                               ctypes.byref(ex), ctypes.byref(it), ctypes.byref(rr))
+    _check(st, "fs_pcg_solve_spec")
+    return int(it.value), x, float(rr.value)

@@ -238,3 +238,62 @@ def random_scene(side: int, seed: int, ppc: int = 4, **overrides) -> Scene:
         objs.append(SceneObject("solid", verts.astype(np.float32),
                                 friction=float(rng.uniform(0.0, 0.3))))
     return Scene(f"random_{side}_{seed}", p, objs)
+
+
+def poisson_case(n: int, seed: int = 0, target: float = 0.55, dt: float = 1.0 / 30,
+                 density: float = 1000.0):
+    """A standalone pressure problem of the mixed-precision configuration:
+    an n x n grid with a 1-cell SOLID border, a seeded star-shaped polygon of
+    16 vertices (angles sorted, radii scaled until 55 % +- 1 % of the cells
+    are FLUID by the cell-centre inside test) and EMPTY elsewhere (Dirichlet
+    0); the right-hand side is the reference's calcPressureRhs
+    (flipsolver2d.cpp:962-991) applied to a face-velocity field with i.i.d.
+    N(0, 1) FP32 values.  Returns (material int8 [n, n], rhs float64 [n, n],
+    dx)."""
+    rng = np.random.default_rng(seed)
+    dx = 1.0 / n
+    ang = np.sort(rng.uniform(0.0, 2.0 * np.pi, 16))
+    rad = rng.uniform(0.5, 1.0, 16)
+    yy, xx = np.mgrid[0:n, 0:n]
+    cy, cx = (yy + 0.5) / n - 0.5, (xx + 0.5) / n - 0.5
+    theta = np.mod(np.arctan2(cy, cx), 2.0 * np.pi)
+    rr = np.hypot(cy, cx)
+    # polygon radius along each cell's direction (linear between vertices)
+    a_ext = np.concatenate([ang, ang[:1] + 2.0 * np.pi])
+    r_ext = np.concatenate([rad, rad[:1]])
+    t = np.where(theta < ang[0], theta + 2.0 * np.pi, theta)
+    k = np.clip(np.searchsorted(a_ext, t) - 1, 0, 15)
+    w = (t - a_ext[k]) / (a_ext[k + 1] - a_ext[k])
+    prad = r_ext[k] * (1.0 - w) + r_ext[k + 1] * w
+    lo, hi = 0.0, 1.0
+    m = None
+    for _ in range(60):
+        s = 0.5 * (lo + hi)
+        inside = rr < s * prad
+        frac = inside[1:-1, 1:-1].mean() * (n - 2) ** 2 / n ** 2
+        if abs(frac - target) <= 0.01:
+            m = inside
+            break
+        if frac < target:
+            lo = s
+        else:
+            hi = s
+    if m is None:
+        m = rr < 0.5 * (lo + hi) * prad
+    mat = np.full((n, n), 0x10, np.int8)
+    mat[m] = 0x40
+    mat[0, :] = mat[-1, :] = mat[:, 0] = mat[:, -1] = 0x20
+    u = rng.standard_normal((n + 1, n)).astype(np.float32)
+    v = rng.standard_normal((n, n + 1)).astype(np.float32)
+    fluid = (mat & 0x40) != 0
+    solid = (mat & 0x20) != 0
+    pad = np.pad(solid, 1, mode="edge")
+    scale = 1.0 / dx
+    div = (u[1:, :] - u[:-1, :] + v[:, 1:] - v[:, :-1]).astype(np.float64)
+    rhs = -scale * div
+    rhs -= pad[0:n, 1:n + 1] * scale * u[:-1, :].astype(np.float64)      # solid at i-1
+    rhs += pad[2:n + 2, 1:n + 1] * scale * u[1:, :].astype(np.float64)   # solid at i+1
+    rhs -= pad[1:n + 1, 0:n] * scale * v[:, :-1].astype(np.float64)      # solid at j-1
+    rhs += pad[1:n + 1, 2:n + 2] * scale * v[:, 1:].astype(np.float64)   # solid at j+1
+    rhs[~fluid] = 0.0
+    return mat, rhs, dx

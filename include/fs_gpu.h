@@ -207,6 +207,21 @@ fs_status fs_pcg_solve_device(int ni, int nj, const int8_t *material_device, flo
                               void *result_device, int iter_limit, double tol,
                               const fs_exec_params *exec, int *iterations);
 
+/* Spec mode: solve the same pressure system to a true relative residual,
+ * ||rhs - A result|| <= rel_tol ||rhs|| (2-norms).  The reference's hot-path
+ * PCG cannot do this (its IPP is not symmetric and the iteration stalls);
+ * this uses the textbook incomplete-Poisson preconditioner the reference
+ * ships but does not use (inversepoissonpreconditioner.h:45-79),
+ * M = (I - L D^-1)(I - L D^-1)^T, in FP32 inner PCG iterations, with the
+ * residual recomputed and the solution accumulated in FP64 between them
+ * (iterative refinement).  max_iter caps the inner iterations in total;
+ * *iterations receives their count and *rel_residual the final FP64
+ * relative residual.  Host arrays as fs_pcg_solve; exec may be NULL. */
+fs_status fs_pcg_solve_spec(int ni, int nj, const int8_t *material, float dt, double density,
+                            double dx, const double *rhs, double *result, double rel_tol,
+                            int max_iter, const fs_exec_params *exec, int *iterations,
+                            double *rel_residual);
+
 /* fs_pcg_solve_device without any device allocation.  This entry point has
  * no counterpart in the reference.  It is for callers that cannot allocate
  * device memory while they run: a loop that reserved its whole device budget

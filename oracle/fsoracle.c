@@ -1785,3 +1785,122 @@ int fso_pcg_solve(int ni, int nj, const int8_t *material, float dt, double densi
     fso_destroy(s);
     return it;
 }
+
+
+/* ---- spec mode: full-FP64 PCG with the textbook IPP ---------------------- *
+ * The reference ships a second incomplete-Poisson preconditioner that it
+ * never uses on the hot path (inversepoissonpreconditioner.h:45-79):
+ * M = K K^T with K = I - L D^-1, L the strictly lower part of the pressure
+ * matrix A (linear index order) and D its diagonal.  With A built as in
+ * getPressureProjectionMatrix (unit rows only), K has 1 / count(n) at
+ * (c, n) for the lower fluid neighbours n = c - NJ (mask bit 1) and
+ * n = c - 1 (mask bit 4) of a unit row c.  This plain double-precision PCG
+ * with M and a true relative-residual stopping test is the FP64 oracle of
+ * the GPU's mixed-precision spec solve.  Serial and deterministic. */
+/* K(c, n) for a strictly lower neighbour n of unit row c:
+ * -A(c, n) / A(n, n) = scale / A(n, n), with Eigen's rule that a zero
+ * diagonal counts as 1; a non-unit row of A is an identity row. */
+static double spec_k(const fso_solver *s, long n)
+{
+    if (s->unit[n] && s->ucount[n] > 0) return 1.0 / s->ucount[n];
+    return s->mscale;
+}
+
+static void spec_apply_m(const fso_solver *s, const double *r, double *y, double *z)
+{
+    const long N = (long)s->ncell, NJ = s->nj;
+    /* y = K^T r: row n of K^T collects K(c, n) over the unit rows c whose
+     * lower neighbour is n */
+    for (long n = 0; n < N; n++) {
+        double v = r[n];
+        const double k = spec_k(s, n);
+        if (n + NJ < N && s->unit[n + NJ] && (s->mask[n + NJ] & 1)) v += k * r[n + NJ];
+        if (n + 1 < N && s->unit[n + 1] && (s->mask[n + 1] & 4)) v += k * r[n + 1];
+        y[n] = v;
+    }
+    /* z = K y */
+    for (long c = 0; c < N; c++) {
+        double v = y[c];
+        if (s->unit[c]) {
+            if ((s->mask[c] & 1) && c - NJ >= 0) v += spec_k(s, c - NJ) * y[c - NJ];
+            if ((s->mask[c] & 4) && c - 1 >= 0) v += spec_k(s, c - 1) * y[c - 1];
+        }
+        z[c] = v;
+    }
+}
+
+static void spec_apply_a(const fso_solver *s, const double *in, double *out)
+{
+    mv_ctx c = {(fso_solver *)s, in, out};
+    amul_range(&c, 0, s->ncell);
+}
+
+static double spec_dot(const double *a, const double *b, long n)
+{
+    double acc = 0.0;
+    for (long k = 0; k < n; k++) acc += a[k] * b[k];
+    return acc;
+}
+
+int fso_spec_solve(int ni, int nj, const int8_t *material, float dt, double density, double dx,
+                   const double *rhs, double *result, double rel_tol, int max_iter,
+                   double *rel_residual)
+{
+    fso_params p;
+    memset(&p, 0, sizeof(p));
+    p.fluidDensity = density;
+    p.dx = dx;
+    p.particlesPerCell = 4;
+    p.fps = 30;
+    p.maxSubsteps = 1;
+    p.pcgIterLimit = max_iter;
+    p.gridSizeI = ni;
+    p.gridSizeJ = nj;
+    fso_solver *s = fso_create(&p);
+    memcpy(s->material, material, s->ncell);
+    s->step_dt = dt;
+    build_matrix(s);
+    const long N = (long)s->ncell;
+    double *r = (double *)calloc(N, sizeof(double)), *z = (double *)calloc(N, sizeof(double));
+    double *y = (double *)calloc(N, sizeof(double)), *d = (double *)calloc(N, sizeof(double));
+    double *q = (double *)calloc(N, sizeof(double));
+    for (long k = 0; k < N; k++) {
+        result[k] = 0.0;
+        r[k] = rhs[k];
+    }
+    const double bnorm = sqrt(spec_dot(rhs, rhs, N));
+    int it = 0;
+    double rnorm = bnorm;
+    if (bnorm > 0.0) {
+        spec_apply_m(s, r, y, z);
+        memcpy(d, z, N * sizeof(double));
+        double rz = spec_dot(r, z, N);
+        for (it = 0; it < max_iter; it++) {
+            rnorm = sqrt(spec_dot(r, r, N));
+            if (rnorm <= rel_tol * bnorm) break;
+            spec_apply_a(s, d, q);
+            const double alpha = rz / spec_dot(d, q, N);
+            for (long k = 0; k < N; k++) {
+                result[k] += alpha * d[k];
+                r[k] -= alpha * q[k];
+            }
+            spec_apply_m(s, r, y, z);
+            const double rz2 = spec_dot(r, z, N);
+            const double beta = rz2 / rz;
+            rz = rz2;
+            for (long k = 0; k < N; k++) d[k] = z[k] + beta * d[k];
+        }
+        /* true residual of the returned solution */
+        spec_apply_a(s, result, q);
+        for (long k = 0; k < N; k++) q[k] = rhs[k] - q[k];
+        rnorm = sqrt(spec_dot(q, q, N));
+    }
+    if (rel_residual) *rel_residual = bnorm > 0.0 ? rnorm / bnorm : 0.0;
+    free(r);
+    free(z);
+    free(y);
+    free(d);
+    free(q);
+    fso_destroy(s);
+    return it;
+}

@@ -153,6 +153,14 @@ int fso_pcg_solve(int ni, int nj, const int8_t *material, float dt,
                   double density, double dx, const double *rhs, double *result,
                   int iter_limit, double tol);
 
+/* Spec-mode oracle: full-FP64 PCG with the reference's textbook incomplete-
+ * Poisson preconditioner (inversepoissonpreconditioner.h:45-79) on the same
+ * operator, stopped at ||b - A x|| <= rel_tol ||b||.  Returns the iteration
+ * count; *rel_residual receives the final true relative residual. */
+int fso_spec_solve(int ni, int nj, const int8_t *material, float dt, double density, double dx,
+                   const double *rhs, double *result, double rel_tol, int max_iter,
+                   double *rel_residual);
+
 #ifdef __cplusplus
 }
 #endif

@@ -77,6 +77,12 @@ def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
         f = getattr(lib, name)
         f.restype = res
         f.argtypes = args
+    # the spec-mode FP64 oracle exists in the C restatement only (the
+    # reference has no such solve on its hot path)
+    if hasattr(lib, "fso_spec_solve"):
+        lib.fso_spec_solve.restype = c_int
+        lib.fso_spec_solve.argtypes = [c_int, c_int, vp, c_float, c_double, c_double, vp, vp,
+                                       c_double, c_int, vp]
     return lib
 
 
@@ -230,3 +236,18 @@ def pcg_solve(material: np.ndarray, rhs: np.ndarray, dt: float, density: float, 
     it = lib.fso_pcg_solve(ni, nj, _ptr(m), float(dt), float(density), float(dx), _ptr(b),
                            _ptr(x), int(iter_limit), float(tol))
     return int(it), x
+
+
+def spec_solve(material: np.ndarray, rhs: np.ndarray, dt: float, density: float, dx: float,
+               rel_tol: float = 1e-6, max_iter: int = 100000):
+    """Full-FP64 PCG with the textbook IPP to a true relative residual.
+    Returns (iterations, solution, final relative residual)."""
+    lib = load("port")
+    ni, nj = material.shape
+    m = np.ascontiguousarray(material, np.int8)
+    b = np.ascontiguousarray(rhs, np.float64).reshape(ni, nj)
+    x = np.zeros((ni, nj), np.float64)
+    rr = ctypes.c_double(0.0)
+    it = lib.fso_spec_solve(ni, nj, _ptr(m), float(dt), float(density), float(dx), _ptr(b), _ptr(x),
+                            float(rel_tol), int(max_iter), ctypes.byref(rr))
+    return int(it), x, float(rr.value)

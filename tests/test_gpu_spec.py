@@ -1,0 +1,59 @@
+"""Spec-mode solve: FP32 inner PCG with the textbook incomplete-Poisson
+preconditioner and FP64 refinement, to a true relative residual of 1e-6,
+checked against the full-FP64 PCG oracle (oracle/fsoracle.c fso_spec_solve)
+on the same operator."""
+import numpy as np
+import pytest
+
+from flipsolver2d_gb300 import gpu, scenes
+import fsoracle as fo
+from test_gpu_pcg import apply_a, random_mask, rhs_for
+
+DT, DENSITY = 1.0 / 30, 1000.0
+REL_TOL = 1e-6
+# the solution's error against the FP64 oracle's (solved to 1e-10) is
+# bounded by the condition number times the residual; measured well below
+SOL_TOL = 1e-3
+
+
+def _true_rel_residual(m, b, x, dx):
+    return np.linalg.norm(b - apply_a(m, x, DT, DENSITY, dx)) / np.linalg.norm(b)
+
+
+def test_spec_oracle_converges(port_lib):
+    m = random_mask(48, 2)
+    b = rhs_for(m, 2)
+    it, x, rr = fo.spec_solve(m, b, DT, DENSITY, 1.0 / 48, 1e-10)
+    assert rr <= 1e-10
+    assert _true_rel_residual(m, b, x, 1.0 / 48) <= 1.01e-10
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,seed", [(64, 5), (128, 6), (256, 7)])
+def test_spec_reaches_relative_residual(port_lib, gpu_lib, n, seed):
+    m = random_mask(n, seed)
+    b = rhs_for(m, seed)
+    it, x, rr = gpu.pcg_solve_spec(m, b, DT, DENSITY, 1.0 / n, REL_TOL)
+    true_rr = _true_rel_residual(m, b, x, 1.0 / n)
+    assert rr <= REL_TOL and true_rr <= 1.01 * REL_TOL, (rr, true_rr)
+    _, x64, _ = fo.spec_solve(m, b, DT, DENSITY, 1.0 / n, 1e-10)
+    err = np.linalg.norm(x - x64) / np.linalg.norm(x64)
+    assert err <= SOL_TOL, f"error against the FP64 oracle {err}"
+
+
+@pytest.mark.gpu
+def test_spec_poisson_case(port_lib, gpu_lib):
+    m, b, dx = scenes.poisson_case(256, seed=3)
+    frac = ((m & 0x40) != 0).mean()
+    assert 0.53 <= frac <= 0.57
+    it, x, rr = gpu.pcg_solve_spec(m, b, DT, DENSITY, dx, REL_TOL)
+    assert rr <= REL_TOL and _true_rel_residual(m, b, x, dx) <= 1.01 * REL_TOL
+    _, x64, _ = fo.spec_solve(m, b, DT, DENSITY, dx, 1e-10)
+    assert np.linalg.norm(x - x64) / np.linalg.norm(x64) <= SOL_TOL
+
+
+@pytest.mark.gpu
+def test_spec_zero_rhs(gpu_lib):
+    m = random_mask(32, 1)
+    it, x, rr = gpu.pcg_solve_spec(m, np.zeros(m.shape), DT, DENSITY, 1.0 / 32, REL_TOL)
+    assert it == 0 and rr == 0.0 and not np.any(x)
