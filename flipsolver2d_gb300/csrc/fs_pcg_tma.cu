@@ -1117,11 +1117,15 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
                 __syncthreads();
                 if constexpr (RPS > 0) {
                     refresh_ring_row(Rr, Rb);
+                    // z on the tile rows came with the last sweep's z.r (step F);
+                    // only the 1-halo rows need the ring
 #pragma unroll
                     for (int rr = 0; rr < kR; rr++) {
-                        const int c = cbase + rr * w2;
-                        Sr[rr] = ipp_apply(Ost[rr * w1], inv, Rr[rr], up_of(Rr, Rb, rr, c),
-                                           dn_of(Rr, Rb, rr, c), Rb[c - 1], Rb[c + 1]);
+                        if (!on_tile(rr)) {
+                            const int c = cbase + rr * w2;
+                            Sr[rr] = ipp_apply(Ost[rr * w1], inv, Rr[rr], up_of(Rr, Rb, rr, c),
+                                               dn_of(Rr, Rb, rr, c), Rb[c - 1], Rb[c + 1]);
+                        }
                     }
                     for (int ed = edge0; ed < 2 * h1; ed += edge_step)
                         Ze[ed] = precond(edge_op(ed), Rb, edge_cell(ed), w2);
@@ -1182,13 +1186,20 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
         float qs = 0.f;
         if constexpr (RPS > 0) {
             const int gj = tj0 + qb - 1;
+            float prev = 0.f; // s of the row above, before it was overwritten
 #pragma unroll
             for (int rr = 0; rr < kR; rr++) {
                 const int c = cbase + rr * w2;
-                const float q = op_apply(Ost[rr * w1], scale, Sr[rr], up_of(Sr, Sb, rr, c),
-                                         dn_of(Sr, Sb, rr, c), Sb[c - 1], Sb[c + 1]);
+                const float cur = Sr[rr];
+                const float up = rr > 0 ? prev : Sb[c - w2];
+                const float q = op_apply(Ost[rr * w1], scale, cur, up, dn_of(Sr, Sb, rr, c),
+                                         Sb[c - 1], Sb[c + 1]);
                 // padding rows may hold anything, even inf: select, do not scale
-                qs = on_tile(rr) ? fmaf(q, Sr[rr], qs) : qs;
+                qs = on_tile(rr) ? fmaf(q, cur, qs) : qs;
+                // A s on the tile rows is the next sweep's A s there too; s
+                // itself stays in Sb
+                Sr[rr] = on_tile(rr) ? q : cur;
+                prev = cur;
             }
             // only the 2-cell band along the tile's border is published: it
             // is all that neighbours' rings read
@@ -1196,7 +1207,8 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
 #pragma unroll
                 for (int rr = 0; rr < kR; rr++) {
                     const int gi = ti0 + row0 + rr - 1;
-                    if (on_tile(rr) && in_band(rr) && gi < NI) s_pub[(size_t)gi * NJ + gj] = Sr[rr];
+                    if (on_tile(rr) && in_band(rr) && gi < NI)
+                        s_pub[(size_t)gi * NJ + gj] = Sb[cbase + rr * w2];
                 }
             }
         } else {
@@ -1233,16 +1245,11 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
         }
         // A s_it on the tile and its 1-halo while the grid barrier completes
         if constexpr (RPS > 0) {
-            if (!first) refresh_ring_row(Sr, Sb);
-            float prev = 0.f; // s of the row above, before it was overwritten
+            // the tile rows' A s came with s.As (step C); the 1-halo rows read
+            // the ring, all from Sb (s_it itself stays there)
 #pragma unroll
-            for (int rr = 0; rr < kR; rr++) {
-                const int c = cbase + rr * w2;
-                const float cur = Sr[rr];
-                const float up = rr > 0 ? prev : Sb[c - w2];
-                Sr[rr] = op_apply(Ost[rr * w1], scale, cur, up, dn_of(Sr, Sb, rr, c), Sb[c - 1], Sb[c + 1]);
-                prev = cur; // s_it itself stays in Sb
-            }
+            for (int rr = 0; rr < kR; rr++)
+                if (!on_tile(rr)) Sr[rr] = apply_a(Ost[rr * w1], Sb, cbase + rr * w2, w2);
             for (int ed = edge0; ed < 2 * h1; ed += edge_step) Ze[ed] = apply_a(edge_op(ed), Sb, edge_cell(ed), w2);
         } else {
             for_halo1(h1, w1, [&](int r, int q) {
@@ -1284,6 +1291,8 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
                 const float z = ipp_apply(Ost[rr * w1], inv, Rr[rr], up_of(Rr, Rb, rr, c), dn_of(Rr, Rb, rr, c),
                                           Rb[c - 1], Rb[c + 1]);
                 zr = on_tile(rr) ? fmaf(z, Rr[rr], zr) : zr;
+                // z on the tile rows is the next sweep's z there too
+                Sr[rr] = on_tile(rr) ? z : Sr[rr];
             }
             // the band only, as for s; the rare backward max-abs scan gets the
             // whole tile published on demand (publish_tile_r)
