@@ -447,35 +447,34 @@ __device__ __forceinline__ void ls_two_sum(float a, float b, float &s, float &e)
 // strictly inside one float's rounding interval, the cell is recomputed in
 // double exactly like the reference.  Either way the result is the
 // reference's float.
-// Running float-pair sum of a cell's smaller-marker neighbours, in the
-// reference's neighbour order (see bfs_value_finish).
-struct BfsSum {
+template <int W>
+__device__ __forceinline__ float bfs_layer_value(const int *mark, const float *val, int r, int q, int k,
+                                                 bool minus_one)
+{
     float s = 0.f, eh = 0.f, el = 0.f, m = 0.f;
     int count = 0, mine = INT_MAX;
     bool el_exact = true;
-    __device__ __forceinline__ void add(float x)
-    {
-        float t2, er, t3, er2;
-        ls_two_sum(s, x, t2, er);
-        s = t2;
-        ls_two_sum(eh, er, t3, er2);
-        eh = t3;
-        el_exact &= er2 == 0.f;
-        el += er2;
-        m += fabsf(x);
-        if (x != 0.f) mine = min(mine, ilogbf(x));
-        count++;
-    }
-};
-
-template <int W>
-__device__ __forceinline__ float bfs_value_finish(const BfsSum &acc, const int *mark, const float *val, int r,
-                                                  int q, int k, bool minus_one)
-{
-    const float s = acc.s, eh = acc.eh, el = acc.el, m = acc.m;
-    int count = acc.count;
-    const int mine = acc.mine;
-    const bool el_exact = acc.el_exact;
+#pragma unroll
+    for (int io = -1; io <= 1; io++)
+#pragma unroll
+        for (int jo = -1; jo <= 1; jo++) {
+            if (io == 0 && jo == 0) continue;
+            const int rr = r + io, qq = q + jo;
+            if (rr < 0 || rr >= W || qq < 0 || qq >= W) continue;
+            const int mk = mark[rr * W + qq];
+            if (mk == kMarkOut || mk >= k) continue;
+            const float x = val[rr * W + qq];
+            float t2, er, t3, er2;
+            ls_two_sum(s, x, t2, er);
+            s = t2;
+            ls_two_sum(eh, er, t3, er2);
+            eh = t3;
+            el_exact &= er2 == 0.f;
+            el += er2;
+            m += fabsf(x);
+            if (x != 0.f) mine = min(mine, ilogbf(x));
+            count++;
+        }
     const float cf = (float)count;
     const float qh = __fdiv_rn(s, cf);
     const float rem = fmaf(-qh, cf, s); // exact
@@ -531,23 +530,6 @@ __device__ __forceinline__ float bfs_value_finish(const BfsSum &acc, const int *
     return minus_one ? (float)(a - 1.f) : (float)a;
 }
 
-// A BFS cell handled by a group of 8 lanes, lane j holding neighbour j in the
-// reference's order (x and whether it counts); every lane of the group
-// returns the cell's value.
-template <int W>
-__device__ __forceinline__ float bfs_value_group(float x, bool use, const int *mark, const float *val, int r,
-                                                 int q, int k, bool minus_one)
-{
-    BfsSum acc;
-#pragma unroll
-    for (int j = 0; j < 8; j++) {
-        const float xj = __shfl_sync(0xffffffffu, x, j, 8);
-        const int uj = __shfl_sync(0xffffffffu, use ? 1 : 0, j, 8);
-        if (uj) acc.add(xj);
-    }
-    return bfs_value_finish<W>(acc, mark, val, r, q, k, minus_one);
-}
-
 template <int W>
 __device__ __forceinline__ bool bfs_touches(const int *mark, int r, int q, int k)
 {
@@ -595,59 +577,57 @@ __device__ __forceinline__ void bfs_layers(int *mark, float *val, short *fa, sho
     // cnt[k % 3]; cnt[(k + 2) % 3] is free while layer k is processed)
     if (threadIdx.x < 3) cnt[threadIdx.x] = 0;
     __syncthreads();
-    // the cells of layer k0 (final from earlier passes) next to an unmarked
-    // cell: the only ones that can discover layer k0 + 1
-    for (int e0 = 0; e0 < W * W; e0 += blockDim.x) {
-        const int e = e0 + (int)threadIdx.x;
-        bool mine = false;
-        if (e < W * W && mark[e] == k0) {
-            const int r = e / W, q = e - r * W;
+    // claims the unmarked neighbours of cell e for layer k + 1 and lists them
+    // (all threads of a warp call it; `live` says whether e is a real cell)
+    auto expand = [&](bool live, int e, int k, short *out, int *counter) {
+        int r = 0, q = 0;
+        unsigned got = 0; // bit (io+1)*3+(jo+1) for each neighbour claimed
+        if (live) {
+            r = e / W;
+            q = e - r * W;
 #pragma unroll
             for (int io = -1; io <= 1; io++)
 #pragma unroll
                 for (int jo = -1; jo <= 1; jo++) {
+                    if (io == 0 && jo == 0) continue;
                     const int rr = r + io, qq = q + jo;
-                    if ((io | jo) != 0 && rr >= 0 && rr < W && qq >= 0 && qq < W)
-                        mine |= mark[rr * W + qq] == kMarkInf;
+                    if (rr < 0 || rr >= W || qq < 0 || qq >= W) continue;
+                    const int n = rr * W + qq;
+                    if (mark[n] == kMarkInf && atomicCAS(&mark[n], kMarkInf, k + 1) == kMarkInf)
+                        got |= 1u << ((io + 1) * 3 + (jo + 1));
                 }
         }
-        const int slot = warp_append(&cnt[k0 % 3], mine ? 1 : 0);
-        if (mine) fa[slot] = (short)e;
+        int slot = warp_append(counter, __popc(got));
+#pragma unroll
+        for (int b = 0; b < 9; b++)
+            if (got & (1u << b)) out[slot++] = (short)((r + b / 3 - 1) * W + (q + b % 3 - 1));
+    };
+    // layer k0 (final from earlier passes) discovers layer k0 + 1
+    for (int e0 = 0; e0 < W * W; e0 += blockDim.x) {
+        const int e = e0 + (int)threadIdx.x;
+        expand(e < W * W && mark[e] == k0, e, k0, fa, &cnt[(k0 + 1) % 3]);
     }
     __syncthreads();
-    // 8 lanes per listed cell, lane j on neighbour j in the reference's
-    // order (-1,-1) (-1,0) (-1,1) (0,-1) (0,1) (1,-1) (1,0) (1,1)
-    const int gl = threadIdx.x & 7, grp = threadIdx.x >> 3, ngrp = blockDim.x >> 3;
-    const int dio = gl < 3 ? -1 : (gl < 5 ? 0 : 1);
-    const int djo = gl < 3 ? gl - 1 : (gl == 3 ? -1 : (gl == 4 ? 1 : gl - 6));
     short *cur = fa, *nxt = fb;
     // One phase per layer k: the values of layer-k cells (they read only
     // layers < k, all final) and the discovery of layer k + 1 from them
-    // (claiming unmarked cells; a value never counts a neighbour of layer k
-    // or above, so the two do not interfere).  Layer k0 only discovers.
-    for (int k = k0; k <= k0 + H; k++) {
+    // (claiming cells that are unmarked; a value never counts a neighbour of
+    // layer k or above, so the two do not interfere).
+    for (int k = k0 + 1; k <= k0 + H; k++) {
         const int ncur = cnt[k % 3];
         if (ncur == 0) break;
         if (threadIdx.x == 0) cnt[(k + 2) % 3] = 0;
-        const bool value = k > k0, more = k < k0 + H;
-        for (int f0 = 0; f0 < ncur; f0 += ngrp) {
-            const int f = f0 + grp;
+        const bool more = k < k0 + H;
+        for (int f0 = 0; f0 < ncur; f0 += blockDim.x) {
+            const int f = f0 + (int)threadIdx.x;
             const bool live = f < ncur;
-            const int e = live ? cur[f] : 0;
-            const int r = e / W, q = e - r * W;
-            const int rr = r + dio, qq = q + djo;
-            const bool inb = live && rr >= 0 && rr < W && qq >= 0 && qq < W;
-            const int n = inb ? rr * W + qq : 0;
-            const int mk = inb ? mark[n] : kMarkOut;
-            if (value) {
-                const float x = inb ? val[n] : 0.f;
-                const float v = bfs_value_group<W>(x, inb && mk != kMarkOut && mk < k, mark, val, r, q, k,
-                                                   minus_one);
-                if (live && gl == 0) val[e] = v;
+            int e = 0;
+            if (live) {
+                e = cur[f];
+                const int r = e / W, q = e - r * W;
+                val[e] = bfs_layer_value<W>(mark, val, r, q, k, minus_one);
             }
-            const bool got = more && mk == kMarkInf && atomicCAS(&mark[n], kMarkInf, k + 1) == kMarkInf;
-            const int slot = warp_append(&cnt[(k + 1) % 3], got ? 1 : 0);
-            if (got) nxt[slot] = (short)n;
+            if (more) expand(live, e, k, nxt, &cnt[(k + 1) % 3]);
         }
         __syncthreads();
         short *tmp = cur;

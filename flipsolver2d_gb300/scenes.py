@@ -297,3 +297,81 @@ def poisson_case(n: int, seed: int = 0, target: float = 0.55, dt: float = 1.0 / 
     rhs += pad[1:n + 1, 2:n + 2] * scale * v[:, 1:].astype(np.float64)   # solid at j+1
     rhs[~fluid] = 0.0
     return mat, rhs, dx
+
+
+class UnsupportedScene(ValueError):
+    """A scene file that needs a solver or object this GPU path does not have
+    (NB-FLIP, smoke, fire, or emitting sources)."""
+
+
+def scene_from_json(source, name: str = "json") -> Scene:
+    """JsonSceneReader::loadJson (Utils/jsonscenereader.cpp:8-77) for the
+    plain liquid solver: `source` is a path, a JSON text or an already parsed
+    dict in the reference's scene format ({"settings": {...}, "solver":
+    {"objects": [...]}}).  Settings take the reference's defaults
+    (populateFlipSolverParamsFromJson, :79-136); objects are added in file
+    order as addObjectFromJson does (:255-287): "solid" -> addGeometry with
+    its friction, "fluid" -> addInitialFluid with its viscosity, "sink" ->
+    addSink with its divergence; disabled objects are skipped and vertices
+    are multiplied by the scene scale.  Solver types other than "flip" /
+    "fluid" and "source" objects raise UnsupportedScene."""
+    import json
+    import os
+
+    if isinstance(source, dict):
+        doc = source
+    elif isinstance(source, str) and source.lstrip().startswith("{"):
+        doc = json.loads(source)
+    else:
+        with open(source) as f:
+            doc = json.load(f)
+        name = os.path.splitext(os.path.basename(str(source)))[0]
+    st = doc["settings"]
+    sim = st["simType"]
+    if sim not in ("flip", "fluid"):
+        raise UnsupportedScene(f"simType {sim!r}: only the plain FLIP liquid solver is on this path")
+
+    def get(key, default):
+        return st[key] if key in st else default
+
+    s = float(get("scale", 1.0))
+    handling = {"particle": PARAM_PARTICLE, "hybrid": PARAM_HYBRID, "grid": PARAM_GRID}
+    g = get("globalAcceleration", (9.8, 0.0))
+    p = FlipSolverParameters(
+        resolution=int(st["resolution"]),
+        domainSizeI=float(st["domainSizeI"]),
+        domainSizeJ=float(st["domainSizeJ"]),
+        fluidDensity=float(get("density", 1.0)),
+        seed=int(get("seed", 0)),
+        particlesPerCell=int(st["particlesPerCell"]),
+        globalAcceleration=(float(g[0]), float(g[1])),
+        fps=int(st["fps"]),
+        maxSubsteps=int(get("maxSubsteps", 30)),
+        picRatio=float(get("picRatio", 0.03)),
+        cflNumber=float(get("cflNumber", 10.0)),
+        particleScale=float(get("particleScale", 0.8)),
+        pcgIterLimit=int(get("pcgIterLimit", 200)),
+        sceneScale=s,
+        viscosityEnabled=bool(get("viscosityEnabled", False)),
+        useHeavyViscosity=bool(get("heavyViscosity", False)),
+        parameterHandlingMethod=handling.get(get("parameterHandlingMethod", "particle"), PARAM_PARTICLE),
+    )
+    if p.viscosityEnabled:
+        raise UnsupportedScene("viscosityEnabled: viscosity is not on this path")
+    objs: List[SceneObject] = []
+    for o in doc["solver"]["objects"]:
+        if not o.get("enabled", True):
+            continue
+        verts = (np.float32(s) * np.asarray(o["verts"], dtype=np.float32)).astype(np.float32)
+        kind = o["type"]
+        if kind == "solid":
+            objs.append(SceneObject("solid", verts, friction=float(o.get("friction", 0.0))))
+        elif kind == "fluid":
+            objs.append(SceneObject("fluid", verts, viscosity=float(o.get("viscosity", 0.0))))
+        elif kind == "sink":
+            objs.append(SceneObject("sink", verts, divergence=float(o.get("divergence", 0.0))))
+        elif kind == "source":
+            raise UnsupportedScene("source objects (emitters reseeding every substep) are not on this path")
+        else:
+            raise UnsupportedScene(f"object type {kind!r}")
+    return Scene(name, p, objs)

@@ -23,11 +23,15 @@ from conftest import POOL_THREADS
 
 pytestmark = pytest.mark.gpu
 
+from test_scenes_json import DAM_JSON  # noqa: E402
+
 SCENES = {
     "dam32": lambda: scenes.dam_break(32, seed=42),
     "dam48_obstacle": lambda: scenes.dam_break(48, seed=7, obstacle=True),
     "random40": lambda: scenes.random_scene(40, 1001),
     "random57": lambda: scenes.random_scene(57, 1003),
+    # the reference's scene-file format (friction obstacle, a disabled object)
+    "json_dam36": lambda: scenes.scene_from_json(DAM_JSON, "json_dam36"),
 }
 
 PARTICLE_KEYS = ["bin_counts", "pos", "vel", "visc", "dead"]

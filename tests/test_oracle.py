@@ -18,11 +18,14 @@ from conftest import POOL_THREADS
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 
+from test_scenes_json import DAM_JSON  # noqa: E402
+
 PIN_SCENES = {
     "dam32": lambda: scenes.dam_break(32, seed=42),
     "dam48_obstacle": lambda: scenes.dam_break(48, seed=7, obstacle=True),
     "random40": lambda: scenes.random_scene(40, 1001),
     "random33_literal_overlap": lambda: scenes.dam_break(33, seed=3, fluid_box=(0.0, 1.0, 0.0, 0.5)),
+    "json_dam36": lambda: scenes.scene_from_json(DAM_JSON, "json_dam36"),
 }
 
 

@@ -1,0 +1,98 @@
+"""Scene files in the reference's JSON format (Utils/jsonscenereader.cpp):
+settings with the reference's defaults, objects in file order, the scene
+scale applied to vertices, unsupported solver and object types refused."""
+import os
+
+import numpy as np
+import pytest
+
+from flipsolver2d_gb300 import scenes
+
+# a small dam break written in the reference's scene format (units of the
+# scene scale; the disabled object must be skipped)
+DAM_JSON = """
+{
+  "settings": {
+    "simType": "flip", "domainSizeI": 10, "domainSizeJ": 10, "resolution": 36,
+    "fps": 30, "density": 1000, "maxSubsteps": 10, "pcgIterLimit": 200, "seed": 3,
+    "particlesPerCell": 4, "picRatio": 0.03, "cflNumber": 5, "scale": 0.1,
+    "globalAcceleration": [9.81, 0]
+  },
+  "solver": {
+    "objects": [
+      {"type": "solid", "verts": [[0, 0], [0, 10], [0.3, 10], [0.3, 0]]},
+      {"type": "solid", "verts": [[9.7, 0], [9.7, 10], [10, 10], [10, 0]]},
+      {"type": "solid", "verts": [[0, 0], [0, 0.3], [10, 0.3], [10, 0]]},
+      {"type": "solid", "verts": [[0, 9.7], [0, 10], [10, 10], [10, 9.7]]},
+      {"type": "solid", "friction": 0.1, "verts": [[4, 4], [4, 6], [6, 6], [6, 4]]},
+      {"type": "solid", "enabled": false, "verts": [[1, 1], [1, 2], [2, 2], [2, 1]]},
+      {"type": "fluid", "verts": [[4.5, 0.3], [4.5, 3.8], [9.7, 3.8], [9.7, 0.3]]}
+    ]
+  }
+}
+"""
+
+
+def test_settings_and_objects():
+    sc = scenes.scene_from_json(DAM_JSON, "dam36")
+    p = sc.params
+    assert (p.resolution, p.fps, p.seed, p.particlesPerCell) == (36, 30, 3, 4)
+    assert p.fluidDensity == 1000 and p.cflNumber == 5 and p.maxSubsteps == 10
+    assert p.sceneScale == pytest.approx(0.1)
+    dx, gi, gj = p.grid()
+    assert (gi, gj) == (36, 36) and dx == pytest.approx(np.float32(1.0) / np.float32(36))
+    kinds = [o.kind for o in sc.objects]
+    assert kinds == ["solid"] * 5 + ["fluid"]  # the disabled solid is gone
+    assert sc.objects[4].friction == pytest.approx(0.1)
+    np.testing.assert_allclose(sc.objects[5].verts[0], [0.45, 0.03], rtol=1e-6)
+
+
+def test_defaults_follow_the_reference():
+    doc = {"settings": {"simType": "fluid", "domainSizeI": 1, "domainSizeJ": 2, "resolution": 64,
+                        "fps": 24, "particlesPerCell": 8},
+           "solver": {"objects": []}}
+    p = scenes.scene_from_json(doc).params
+    assert p.fluidDensity == 1.0 and p.seed == 0 and p.maxSubsteps == 30
+    assert p.cflNumber == 10.0 and p.pcgIterLimit == 200 and p.picRatio == pytest.approx(0.03)
+    assert p.globalAcceleration == (9.8, 0.0)
+    dx, gi, gj = p.grid()
+    assert (gi, gj) == (32, 64)  # the longer side gets the resolution
+
+
+@pytest.mark.parametrize("doc,what", [
+    ({"settings": {"simType": "nbflip"}, "solver": {"objects": []}}, "simType"),
+    ({"settings": {"simType": "smoke"}, "solver": {"objects": []}}, "simType"),
+])
+def test_unsupported_solvers(doc, what):
+    with pytest.raises(scenes.UnsupportedScene, match=what):
+        scenes.scene_from_json(doc)
+
+
+def test_sources_are_refused():
+    doc = {"settings": {"simType": "flip", "domainSizeI": 1, "domainSizeJ": 1, "resolution": 16,
+                        "fps": 30, "particlesPerCell": 4},
+           "solver": {"objects": [{"type": "source", "verts": [[0, 0], [0, 1], [1, 1]]}]}}
+    with pytest.raises(scenes.UnsupportedScene, match="source"):
+        scenes.scene_from_json(doc)
+
+
+import build as oracle_build  # noqa: E402  (oracle/ is on sys.path via conftest)
+
+REF_SCENES = os.path.join(oracle_build.reference_dir(), "Liquid2dRender", "scenes")
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_SCENES), reason="reference scene files not present")
+def test_reference_scene_files_parse_or_are_refused():
+    loaded, refused = 0, 0
+    for fn in sorted(os.listdir(REF_SCENES)):
+        if not fn.endswith(".json"):
+            continue
+        try:
+            sc = scenes.scene_from_json(os.path.join(REF_SCENES, fn))
+        except scenes.UnsupportedScene:
+            refused += 1
+            continue
+        dx, gi, gj = sc.params.grid()
+        assert gi > 0 and gj > 0 and dx > 0 and sc.objects
+        loaded += 1
+    assert loaded >= 1 and loaded + refused >= 10
