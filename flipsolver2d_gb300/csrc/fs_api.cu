@@ -988,6 +988,9 @@ extern "C" fs_status fs_run_stage(fs_solver *s, int which)
     if (!s) return fail(FS_ERR_BAD_ARG, "null handle");
     TRY(set_device(s));
     TRY(ensure_friction(s));
+    // a frame's last level set may still run on the side stream: a stage on
+    // its own comes after it (two level sets on one set of buffers race)
+    TRY(wait_side(s));
     k_set_dt<<<1, 1, 0, s->st>>>(s->sc, s->step_dt);
     if (which == FS_STAGE_DENSITY) CK(cudaMemsetAsync(&s->sc->density_iters, 0, sizeof(int), s->st));
     if (which == FS_STAGE_PROJECT) CK(cudaMemsetAsync(&s->sc->pressure_iters, 0, sizeof(int), s->st));

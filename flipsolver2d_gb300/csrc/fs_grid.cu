@@ -767,7 +767,6 @@ __global__ void __launch_bounds__(1024, 1) k_levelset_pass(GridDims d, float *__
     short *fa = reinterpret_cast<short *>(ls_smem + 2 * W * W);
     short *fb = fa + W * W;
     int *cnt = reinterpret_cast<int *>(fb + W * W);
-    if (pass > 0 && ((volatile int *)active)[pass - 1] == 0) return;
     const int si = d.ni, sj = d.nj;
     const int tiles_i = gridDim.y, tiles_j = gridDim.x;
     const int ntiles = tiles_i * tiles_j;
@@ -775,17 +774,28 @@ __global__ void __launch_bounds__(1024, 1) k_levelset_pass(GridDims d, float *__
     uint8_t *act_prev = act + (size_t)((pass + 2) % 3) * ntiles;
     uint8_t *act_cur = act + (size_t)(pass % 3) * ntiles;
     uint8_t *act_next = act + (size_t)((pass + 1) % 3) * ntiles;
-    if (threadIdx.x == 0) act_next[tile] = 0;
-    if (pass > 0) {
-        bool near = false;
-        for (int a = -1; a <= 1; a++)
-            for (int b = -1; b <= 1; b++) {
-                const int ti = (int)blockIdx.y + a, tj = (int)blockIdx.x + b;
-                if (ti >= 0 && ti < tiles_i && tj >= 0 && tj < tiles_j)
-                    near |= ((volatile uint8_t *)act_prev)[ti * tiles_j + tj] != 0;
+    // whether this tile works in this pass is decided once, by thread 0, and
+    // shared through the barrier: every thread of the block takes the same
+    // exit, so the warp-wide shuffles of the BFS always see full warps
+    bool work = true;
+    if (threadIdx.x == 0) {
+        if (pass > 0 && ((volatile int *)active)[pass - 1] == 0) {
+            work = false;
+        } else {
+            act_next[tile] = 0;
+            if (pass > 0) {
+                bool near = false;
+                for (int a = -1; a <= 1; a++)
+                    for (int b = -1; b <= 1; b++) {
+                        const int ti = (int)blockIdx.y + a, tj = (int)blockIdx.x + b;
+                        if (ti >= 0 && ti < tiles_i && tj >= 0 && tj < tiles_j)
+                            near |= ((volatile uint8_t *)act_prev)[ti * tiles_j + tj] != 0;
+                    }
+                work = near;
             }
-        if (!near) return;
+        }
     }
+    if (!__syncthreads_or(threadIdx.x == 0 && work)) return;
     const int ti0 = blockIdx.y * kLsTile, tj0 = blockIdx.x * kLsTile;
     const int k0 = pass * kLsH;
     int open = 0;

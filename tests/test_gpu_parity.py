@@ -235,3 +235,19 @@ def test_full_frames_fp32(scene):
         assert rel_l2(b["vel"], a["vel"]) <= 5e-2
     m = np.mean(o.get_grid("material") == g.get_grid("material"))
     assert m >= 0.98
+
+
+def test_stage_right_after_frame():
+    """A frame's last level set runs on a side stream and may still be in
+    flight when stepFrame returns; a level-set stage called at once must
+    order after it and give what it gives after an explicit synchronize."""
+    sc = scenes.dam_break(512, seed=7, obstacle=True)
+    out = []
+    for sync in (False, True):
+        g = gpu.GpuFlipSolver(sc, precision=gpu.FS_PCG_FP32, pool_threads=POOL_THREADS)
+        g.step_frame()
+        if sync:
+            g.synchronize()
+        g.stage(gpu.LEVELSET)
+        out.append(g.get_grid("fluid_sdf"))
+    assert np.array_equal(out[0].view(np.uint32), out[1].view(np.uint32))
