@@ -30,6 +30,7 @@ UNITS = {
     "fs_pcg.cu": ["-fmad=true"],
     "fs_pcg_tma.cu": ["-fmad=true"],
     "fs_spec.cu": ["-fmad=true"],
+    "fs_cluster.cu": ["-fmad=true"],
 }
 
 

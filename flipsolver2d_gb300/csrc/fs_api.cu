@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "../../include/fs_gpu.h"
+#include "fs_cluster.h"
 #include "fs_pcg.h"
 #include "fs_pcg_tma.h"
 #include "fs_spec.h"
@@ -140,6 +141,8 @@ struct Poly {
 };
 
 __global__ void k_set_dt(Scalars *sc, float dt) { sc->dt = dt; }
+// a batch round: the scene's dt from the batch's table
+__global__ void k_set_dt_from(Scalars *sc, const float *dt) { sc->dt = *dt; }
 __global__ void k_fill_i32(int *p, int v, size_t n)
 {
     size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -170,6 +173,9 @@ struct fs_solver {
     bool tma = false;          // TMA-staged FP32 PCG available for this grid
     int tma_ti = 0, tma_tj = 0;
     bool resident = false;     // FP32 PCG with every tile resident in shared memory
+    ClusterPlan spec_plan{};   // FS_PCG_SPEC: how the cluster solve runs this grid
+    ClusterSystem *spec_sys = nullptr; // FS_PCG_SPEC: the density and pressure systems
+    double *spec_rel = nullptr;        // their final relative residuals
     int res_ti = 0, res_tj = 0;
     TmaMaps maps_dens{}, maps_pres{};
     void *rebin_scratch = nullptr;
@@ -337,8 +343,10 @@ extern "C" fs_status fs_create(const fs_params *p, const fs_exec_params *exec, f
         delete s;
         return fail(FS_ERR_BAD_ARG, "fs_create: bad device ordinal");
     }
-    s->prec = s->ex.pcg_precision == FS_PCG_FP64 ? FS_PCG_FP64 : FS_PCG_FP32;
-    s->esz = s->prec == FS_PCG_FP64 ? 8 : 4;
+    s->prec = s->ex.pcg_precision == FS_PCG_FP64 ? FS_PCG_FP64
+            : s->ex.pcg_precision == FS_PCG_SPEC ? FS_PCG_SPEC
+                                                 : FS_PCG_FP32;
+    s->esz = s->prec == FS_PCG_FP32 ? 4 : 8;
     auto cleanup = [&](fs_status st) {
         fs_destroy(s);
         return st;
@@ -433,8 +441,8 @@ extern "C" fs_status fs_create(const fs_params *p, const fs_exec_params *exec, f
         A(dalloc(s, &q, vb));
         *v = q;
     }
-    s->pcg_grid = s->prec == FS_PCG_FP64 ? pcg_grid_size<double>((long long)n)
-                                         : pcg_grid_size<float>((long long)n);
+    s->pcg_grid = s->prec == FS_PCG_FP32 ? pcg_grid_size<float>((long long)n)
+                                         : pcg_grid_size<double>((long long)n);
     A(dalloc(s, &s->partials, (size_t)8 * s->pcg_grid + 16));
     A(dalloc(s, &s->bar, 1));
     if (s->prec == FS_PCG_FP32)
@@ -454,6 +462,28 @@ extern "C" fs_status fs_create(const fs_params *p, const fs_exec_params *exec, f
                  tma_store_maps(&s->maps_pres, d.ni, d.nj, s->tma_ti, s->tma_tj,
                                 (const float *)s->r0, (const float *)s->r1, (const float *)s->s0,
                                 (const float *)s->s1);
+    }
+    if (s->prec == FS_PCG_SPEC) {
+        if (!cluster_plan(d.ni, d.nj, &s->spec_plan))
+            return cleanup(fail(FS_ERR_UNSUPPORTED,
+                                "fs_create: FS_PCG_SPEC needs a grid of at most %lld cells", cluster_max_cells()));
+        A(dalloc(s, &s->spec_sys, 2));
+        A(dalloc(s, &s->spec_rel, 2));
+        ClusterSystem hs[2];
+        for (int k = 0; k < 2; k++) {
+            hs[k].ni = d.ni;
+            hs[k].nj = d.nj;
+            hs[k].info = G.cell_info;
+            hs[k].b = (const double *)(k == 0 ? s->dens_rhs : s->pres_rhs);
+            hs[k].x = (double *)(k == 0 ? s->dens_x : s->pres_x);
+            hs[k].dt = &s->sc->dt;
+            hs[k].density = p->fluidDensity;
+            hs[k].dx = p->dx;
+            hs[k].iters = k == 0 ? &s->sc->density_iters : &s->sc->pressure_iters;
+            hs[k].rel_res = s->spec_rel + k;
+        }
+        if (cudaMemcpy(s->spec_sys, hs, sizeof(hs), cudaMemcpyHostToDevice) != cudaSuccess)
+            return cleanup(fail(FS_ERR_CUDA, "fs_create: upload failed"));
     }
     std::vector<int> ends = split_range_ends((long long)n, s->ex.pool_threads);
     s->nchunks = (int)ends.size();
@@ -715,6 +745,21 @@ template <typename T> static PcgArgs<T> pcg_args(fs_solver *s, const void *b, vo
     return a;
 }
 
+// FS_PCG_SPEC: the relative residual every pressure and density solve
+// reaches, and its inner-iteration cap (a solve that hits it counts as
+// failed, like the reference's iteration limit)
+constexpr double kSpecRelTol = 1e-6;
+constexpr int kSpecMaxIter = 20000;
+static ClusterParams spec_params()
+{
+    ClusterParams cp;
+    cp.tol = kSpecRelTol;
+    cp.eps_in = 1e-4f;
+    cp.max_iter = kSpecMaxIter;
+    cp.max_outer = 32;
+    return cp;
+}
+
 static fs_status run_pcg(fs_solver *s, const void *b, void *x, int *iters)
 {
     const int slot = b == s->dens_rhs ? 0 : 1;
@@ -723,6 +768,9 @@ static fs_status run_pcg(fs_solver *s, const void *b, void *x, int *iters)
     int launched = 0;
     if (s->prec == FS_PCG_FP64) {
         e = launch_pcg<double>(pcg_args<double>(s, b, x, iters), s->st, &launched);
+    } else if (s->prec == FS_PCG_SPEC) {
+        e = launch_pcg_cluster(s->spec_sys + slot, 1, s->spec_plan, spec_params(), s->st);
+        launched = 1;
     } else if (s->resident) {
         PcgArgs<float> pa = pcg_args<float>(s, b, x, iters);
         pa.mode = 2; // unless a unit row sits on a j edge
@@ -765,7 +813,7 @@ static fs_status collect_pcg_timers(fs_solver *s)
 static fs_status stage(fs_solver *s, int which, bool in_step)
 {
     const GridDims &d = s->d;
-    const int dbl = s->prec == FS_PCG_FP64;
+    const int dbl = s->prec != FS_PCG_FP32;
     cudaStream_t q = s->st;
     switch (which) {
     case FS_STAGE_ADVECT:
@@ -791,7 +839,14 @@ static fs_status stage(fs_solver *s, int which, bool in_step)
         launch_density_grid(d, s->sp, s->P, s->G, s->dens_rhs, dbl, s->sc, q);
         g_kernel_launches += 1;
         TRY(run_pcg(s, s->dens_rhs, s->dens_x, &s->sc->density_iters));
-        launch_adjust(d, s->sp, s->P, s->G, s->dens_x, dbl, s->sc, q);
+        if (s->prec == FS_PCG_SPEC) {
+            // the push is skipped only when the solve ran out of iterations
+            SceneParams sp = s->sp;
+            sp.pcgIterLimit = kSpecMaxIter;
+            launch_adjust(d, sp, s->P, s->G, s->dens_x, dbl, s->sc, q);
+        } else {
+            launch_adjust(d, s->sp, s->P, s->G, s->dens_x, dbl, s->sc, q);
+        }
         g_kernel_launches += 1;
         break;
     case FS_STAGE_DENSITY_GRID:
@@ -1246,6 +1301,345 @@ extern "C" fs_status fs_synchronize(fs_solver *s)
 }
 
 // ---------------------------------------------------------------------------
+// fs_batch: solver handles stepped together (no reference counterpart)
+//
+// Every handle advances by whole frames with the CFL loop of fs_step_frame
+// (FlipSolver::stepFrame, flipsolver2d.cpp:464-500), substep by substep.  The
+// handles' substeps run in rounds: in a round every handle still inside its
+// frame runs one substep.  A substep is three captured CUDA graphs per handle
+// (everything before the density solve; between the solves; after the
+// pressure solve, ending with the max-velocity reduction the next round's dt
+// needs), and the density and pressure solves of all those handles are one
+// cluster launch per plan (fs_cluster.cu) in between.  The host waits once
+// per round, for the max velocities.
+//
+// A substep swaps the particle buffers once (the rebin) and the velocity
+// grids twice, so the device pointers a substep uses repeat with period two:
+// two versions of each graph are captured, for even and odd substeps, and
+// the handle's host-side pointer state follows the parity.
+// ---------------------------------------------------------------------------
+struct BatchScene {
+    fs_solver *s = nullptr;
+    cudaGraphExec_t g[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
+    long long launches[3] = {0, 0, 0};
+    Particles P[2];
+    Grids G[2];
+    int parity = 0;
+    cudaEvent_t ev = nullptr;
+    // the frame in progress (fs_step_frame's locals)
+    float substep_time = 0.f;
+    int substep_count = 0;
+    bool finished = true;
+};
+
+struct fs_batch {
+    std::vector<BatchScene> sc;
+    int device = 0;
+    cudaStream_t bst = nullptr; // merged solves
+    cudaEvent_t ev_solve = nullptr;
+    float *d_dt = nullptr, *h_dt = nullptr;                // per scene
+    ClusterSystem *d_list = nullptr, *h_list = nullptr;   // 2 n: the round's systems
+};
+
+static fs_status batch_capture(fs_batch *b, BatchScene &bs, int idx, int parity)
+{
+    fs_solver *s = bs.s;
+    const GridDims &d = s->d;
+    const int dbl = 1;
+    cudaStream_t q = s->st;
+    for (int seg = 0; seg < 3; seg++) {
+        const long long before = g_kernel_launches;
+        CK(cudaStreamBeginCapture(q, cudaStreamCaptureModeRelaxed));
+        fs_status st = FS_OK;
+        if (seg == 0) {
+            k_set_dt_from<<<1, 1, 0, q>>>(s->sc, b->d_dt + idx);
+            g_kernel_launches += 1;
+            cudaMemsetAsync(&s->sc->density_iters, 0, 2 * sizeof(int), q);
+            st = stage(s, FS_STAGE_ADVECT, true);
+            if (st == FS_OK) st = stage(s, FS_STAGE_DECOMPOSITION, true);
+            if (st == FS_OK) st = stage(s, FS_STAGE_REBIN, true);
+            if (st == FS_OK) {
+                launch_density_grid(d, s->sp, s->P, s->G, s->dens_rhs, dbl, s->sc, q);
+                g_kernel_launches += 1;
+            }
+        } else if (seg == 1) {
+            SceneParams sp = s->sp;
+            sp.pcgIterLimit = kSpecMaxIter;
+            launch_adjust(d, sp, s->P, s->G, s->dens_x, dbl, s->sc, q);
+            g_kernel_launches += 1;
+            st = stage(s, FS_STAGE_P2G, true);
+            if (st == FS_OK) st = stage(s, FS_STAGE_LEVELSET, true);
+            if (st == FS_OK) {
+                launch_vel_extrapolate(d, s->G, s->sp, s->sc, true, q);
+                launch_pressure_rhs(d, s->G, s->pres_rhs, dbl, s->sp, q);
+                g_kernel_launches += 2;
+                st = wait_side(s); // the level set joins before the graph ends
+            }
+        } else {
+            launch_apply_pressure(d, s->sp, s->G, s->pres_x, dbl, s->sc, true, q);
+            g_kernel_launches += 1;
+            st = stage(s, FS_STAGE_VEL_EXTRAP, true);
+            if (st == FS_OK) st = stage(s, FS_STAGE_G2P, true);
+            if (st == FS_OK) st = stage(s, FS_STAGE_COUNT, true);
+            if (st == FS_OK) {
+                launch_max_velocity(s->P, s->sc, q);
+                g_kernel_launches += 2;
+                cudaMemcpyAsync(s->sc_host, s->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, q);
+            }
+        }
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(q, &graph);
+        if (st != FS_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return st;
+        }
+        if (ec != cudaSuccess) return fail(FS_ERR_CUDA, "fs_batch_create: capture: %s", cudaGetErrorString(ec));
+        const cudaError_t ei = cudaGraphInstantiate(&bs.g[parity][seg], graph, 0);
+        cudaGraphDestroy(graph);
+        if (ei != cudaSuccess)
+            return fail(FS_ERR_CUDA, "fs_batch_create: instantiate: %s", cudaGetErrorString(ei));
+        bs.launches[seg] = g_kernel_launches - before;
+    }
+    return FS_OK;
+}
+
+static void batch_release_graphs(BatchScene &bs)
+{
+    for (auto &row : bs.g)
+        for (cudaGraphExec_t &e : row) {
+            if (e) cudaGraphExecDestroy(e);
+            e = nullptr;
+        }
+}
+
+// captures both substep parities from the handle's current buffers; the
+// handle's host-side pointer state is left as it was
+static fs_status batch_prepare(fs_batch *b, BatchScene &bs, int idx)
+{
+    fs_solver *s = bs.s;
+    batch_release_graphs(bs);
+    TRY(ensure_friction(s));
+    TRY(sync_all(s));
+    bs.P[0] = s->P;
+    bs.G[0] = s->G;
+    fs_status st = batch_capture(b, bs, idx, 0);
+    if (st == FS_OK) {
+        bs.P[1] = s->P;
+        bs.G[1] = s->G;
+        st = batch_capture(b, bs, idx, 1);
+    }
+    const bool back = memcmp(&s->P, &bs.P[0], sizeof(Particles)) == 0 &&
+                      memcmp(&s->G, &bs.G[0], sizeof(Grids)) == 0;
+    s->P = bs.P[0];
+    s->G = bs.G[0];
+    bs.parity = 0;
+    if (st == FS_OK && !back) st = fail(FS_ERR_CUDA, "fs_batch: substep buffers do not repeat");
+    if (st != FS_OK) batch_release_graphs(bs);
+    return st;
+}
+
+extern "C" fs_status fs_batch_destroy(fs_batch *b)
+{
+    if (!b) return FS_OK;
+    cudaSetDevice(b->device);
+    cudaDeviceSynchronize();
+    for (BatchScene &bs : b->sc) {
+        batch_release_graphs(bs);
+        if (bs.ev) cudaEventDestroy(bs.ev);
+    }
+    if (b->ev_solve) cudaEventDestroy(b->ev_solve);
+    if (b->bst) cudaStreamDestroy(b->bst);
+    if (b->d_dt) cudaFree(b->d_dt);
+    if (b->d_list) cudaFree(b->d_list);
+    if (b->h_dt) cudaFreeHost(b->h_dt);
+    if (b->h_list) cudaFreeHost(b->h_list);
+    delete b;
+    return FS_OK;
+}
+
+extern "C" fs_status fs_batch_create(fs_solver *const *solvers, int n, fs_batch **out)
+{
+    if (!out || n < 1 || !solvers) return fail(FS_ERR_BAD_ARG, "fs_batch_create: invalid argument");
+    *out = nullptr;
+    for (int k = 0; k < n; k++) {
+        if (!solvers[k]) return fail(FS_ERR_BAD_ARG, "fs_batch_create: null handle %d", k);
+        if (solvers[k]->prec != FS_PCG_SPEC)
+            return fail(FS_ERR_UNSUPPORTED, "fs_batch_create: handle %d is not in FS_PCG_SPEC mode", k);
+        if (solvers[k]->ex.device != solvers[0]->ex.device)
+            return fail(FS_ERR_BAD_ARG, "fs_batch_create: handles on different devices");
+        if (solvers[k]->timers) return fail(FS_ERR_UNSUPPORTED, "fs_batch_create: handle %d has timers on", k);
+        for (int j = 0; j < k; j++)
+            if (solvers[j] == solvers[k]) return fail(FS_ERR_BAD_ARG, "fs_batch_create: handle %d twice", k);
+    }
+    fs_batch *b = new fs_batch();
+    b->device = solvers[0]->ex.device;
+    auto cleanup = [&](fs_status st) {
+        fs_batch_destroy(b);
+        return st;
+    };
+    if (cudaSetDevice(b->device) != cudaSuccess) return cleanup(fail(FS_ERR_CUDA, "fs_batch_create: device"));
+    if (cudaStreamCreateWithFlags(&b->bst, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_solve, cudaEventDisableTiming) != cudaSuccess ||
+        cudaMalloc(&b->d_dt, (size_t)n * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&b->d_list, (size_t)2 * n * sizeof(ClusterSystem)) != cudaSuccess ||
+        cudaMallocHost(&b->h_dt, (size_t)n * sizeof(float)) != cudaSuccess ||
+        cudaMallocHost(&b->h_list, (size_t)2 * n * sizeof(ClusterSystem)) != cudaSuccess)
+        return cleanup(fail(FS_ERR_OOM, "fs_batch_create: allocation failed"));
+    b->sc.resize(n);
+    for (int k = 0; k < n; k++) {
+        BatchScene &bs = b->sc[k];
+        bs.s = solvers[k];
+        if (cudaEventCreateWithFlags(&bs.ev, cudaEventDisableTiming) != cudaSuccess)
+            return cleanup(fail(FS_ERR_CUDA, "fs_batch_create: event"));
+        // a handle that has not stepped yet is captured at its first frame,
+        // once its particles exist
+        if (bs.s->frame > 0) {
+            const fs_status st = batch_prepare(b, bs, k);
+            if (st != FS_OK) return cleanup(st);
+        }
+    }
+    *out = b;
+    return FS_OK;
+}
+
+// one merged solve (0 density, 1 pressure) over the scenes of `act`
+static fs_status batch_solve(fs_batch *b, const std::vector<int> &act, int which)
+{
+    const int n = (int)b->sc.size();
+    ClusterSystem *hl = b->h_list + (size_t)which * n;
+    ClusterSystem *dl = b->d_list + (size_t)which * n;
+    std::vector<int> order(act);
+    auto key = [&](int k) { return b->sc[k].s->spec_plan.C * 64 + b->sc[k].s->spec_plan.K; };
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return key(x) < key(y); });
+    for (int k : act) CK(cudaStreamWaitEvent(b->bst, b->sc[k].ev, 0));
+    for (size_t t = 0; t < order.size(); t++) {
+        fs_solver *s = b->sc[order[t]].s;
+        ClusterSystem &c = hl[t];
+        c.ni = s->d.ni;
+        c.nj = s->d.nj;
+        c.info = s->G.cell_info;
+        c.b = (const double *)(which == 0 ? s->dens_rhs : s->pres_rhs);
+        c.x = (double *)(which == 0 ? s->dens_x : s->pres_x);
+        c.dt = &s->sc->dt;
+        c.density = s->sp.fluidDensity;
+        c.dx = s->sp.dx;
+        c.iters = which == 0 ? &s->sc->density_iters : &s->sc->pressure_iters;
+        c.rel_res = s->spec_rel + which;
+    }
+    CK(cudaMemcpyAsync(dl, hl, order.size() * sizeof(ClusterSystem), cudaMemcpyHostToDevice, b->bst));
+    const ClusterParams cp = spec_params();
+    for (size_t t0 = 0; t0 < order.size();) {
+        size_t t1 = t0;
+        ClusterPlan g = b->sc[order[t0]].s->spec_plan;
+        while (t1 < order.size() && key(order[t1]) == key(order[t0]))
+            g.smem = std::max(g.smem, b->sc[order[t1++]].s->spec_plan.smem);
+        CK(launch_pcg_cluster(dl + t0, (int)(t1 - t0), g, cp, b->bst));
+        g_kernel_launches += 1;
+        t0 = t1;
+    }
+    CK(cudaEventRecord(b->ev_solve, b->bst));
+    return FS_OK;
+}
+
+extern "C" fs_status fs_batch_step_frame(fs_batch *b)
+{
+    if (!b) return fail(FS_ERR_BAD_ARG, "null batch");
+    CK(cudaSetDevice(b->device));
+    const int n = (int)b->sc.size();
+    // frame start: first-frame set-up and the max velocity of every handle
+    for (int k = 0; k < n; k++) {
+        BatchScene &bs = b->sc[k];
+        fs_solver *s = bs.s;
+        if (s->frame == 0) TRY(fs_first_frame_init(s));
+        TRY(sync_all(s));
+        // the graphs hold device pointers: capture again if the handle's
+        // buffers moved since (first-frame seeding, fs_set_particles, ...)
+        if (!bs.g[0][0] || memcmp(&s->P, &bs.P[bs.parity], sizeof(Particles)) != 0 ||
+            memcmp(&s->G, &bs.G[bs.parity], sizeof(Grids)) != 0) {
+            TRY(batch_prepare(b, bs, k));
+        }
+        launch_max_velocity(s->P, s->sc, s->st);
+        g_kernel_launches += 2;
+        CK(cudaMemcpyAsync(s->sc_host, s->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s->st));
+        bs.substep_time = 0.f;
+        bs.substep_count = 0;
+        bs.finished = false;
+        s->density_iters_max = s->pressure_iters_max = s->substeps = 0;
+    }
+    CK(cudaDeviceSynchronize());
+    std::vector<int> act;
+    for (;;) {
+        // the CFL step of every handle still in its frame (fs_step_frame)
+        act.clear();
+        for (int k = 0; k < n; k++) {
+            BatchScene &bs = b->sc[k];
+            fs_solver *s = bs.s;
+            if (bs.finished) continue;
+            if (s->sc_host->pcg_status != 0) return fail(FS_ERR_TIMEOUT, "batch handle %d: solver status", k);
+            if (bs.substep_count > 0) {
+                s->density_iters_max = std::max(s->density_iters_max, s->sc_host->density_iters);
+                s->pressure_iters_max = std::max(s->pressure_iters_max, s->sc_host->pressure_iters);
+            }
+            unsigned bits = s->sc_host->maxv2;
+            float v2;
+            memcpy(&v2, &bits, 4);
+            const float vel = std::sqrt(v2);
+            float maxSubstepSize = s->p.cflNumber / (vel + 1e-15f);
+            bool last = false;
+            if (bs.substep_time + maxSubstepSize >= s->frame_dt || bs.substep_count == (s->p.maxSubsteps - 1)) {
+                maxSubstepSize = s->frame_dt - bs.substep_time;
+                last = true;
+            } else if (bs.substep_time + 2.f * maxSubstepSize >= s->frame_dt) {
+                maxSubstepSize = 0.5f * (s->frame_dt - bs.substep_time);
+            }
+            s->step_dt = maxSubstepSize;
+            b->h_dt[k] = maxSubstepSize;
+            bs.substep_time += maxSubstepSize;
+            bs.substep_count++;
+            if (last || bs.substep_count > 50) bs.finished = true;
+            act.push_back(k);
+        }
+        if (act.empty()) break;
+        CK(cudaMemcpyAsync(b->d_dt, b->h_dt, (size_t)n * sizeof(float), cudaMemcpyHostToDevice, b->bst));
+        CK(cudaEventRecord(b->ev_solve, b->bst));
+        for (int k : act) {
+            BatchScene &bs = b->sc[k];
+            CK(cudaStreamWaitEvent(bs.s->st, b->ev_solve, 0));
+            CK(cudaGraphLaunch(bs.g[bs.parity][0], bs.s->st));
+            CK(cudaEventRecord(bs.ev, bs.s->st));
+            g_kernel_launches += bs.launches[0];
+        }
+        TRY(batch_solve(b, act, 0));
+        for (int k : act) {
+            BatchScene &bs = b->sc[k];
+            CK(cudaStreamWaitEvent(bs.s->st, b->ev_solve, 0));
+            CK(cudaGraphLaunch(bs.g[bs.parity][1], bs.s->st));
+            CK(cudaEventRecord(bs.ev, bs.s->st));
+            g_kernel_launches += bs.launches[1];
+        }
+        TRY(batch_solve(b, act, 1));
+        for (int k : act) {
+            BatchScene &bs = b->sc[k];
+            CK(cudaStreamWaitEvent(bs.s->st, b->ev_solve, 0));
+            CK(cudaGraphLaunch(bs.g[bs.parity][2], bs.s->st));
+            g_kernel_launches += bs.launches[2];
+            bs.parity ^= 1;
+            bs.s->substeps++;
+        }
+        CK(cudaDeviceSynchronize());
+    }
+    for (BatchScene &bs : b->sc) {
+        fs_solver *s = bs.s;
+        s->density_iters_max = std::max(s->density_iters_max, s->sc_host->density_iters);
+        s->pressure_iters_max = std::max(s->pressure_iters_max, s->sc_host->pressure_iters);
+        s->P = bs.P[bs.parity];
+        s->G = bs.G[bs.parity];
+        s->frame++;
+    }
+    return FS_OK;
+}
+
+// ---------------------------------------------------------------------------
 // standalone LinearSolver::solve drop-in
 // ---------------------------------------------------------------------------
 namespace {
@@ -1571,6 +1965,138 @@ extern "C" fs_status fs_pcg_solve_spec(int ni, int nj, const int8_t *material, f
     release();
     if (iterations) *iterations = total_inner;
     if (rel_residual) *rel_residual = bnorm > 0.0 ? rnorm / bnorm : 0.0;
+    return FS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// fs_pcg_solve_batch: many spec-mode solves in one launch per cluster size,
+// one thread-block cluster per system (fs_cluster.cu).
+// ---------------------------------------------------------------------------
+extern "C" fs_status fs_pcg_solve_batch(fs_poisson_system *systems, int n, double rel_tol,
+                                        int max_iter, const fs_exec_params *exec)
+{
+    if (n < 0 || (n > 0 && !systems) || max_iter < 0 || !(rel_tol > 0.0))
+        return fail(FS_ERR_BAD_ARG, "fs_pcg_solve_batch: invalid argument");
+    if (n == 0) return FS_OK;
+    const int dev = exec ? exec->device : 0;
+    CK(cudaSetDevice(dev));
+    std::vector<ClusterPlan> plan(n);
+    std::vector<size_t> off(n + 1, 0);
+    for (int k = 0; k < n; k++) {
+        const fs_poisson_system &q = systems[k];
+        if (q.ni < 1 || q.nj < 1 || !q.material || !q.rhs || !q.result)
+            return fail(FS_ERR_BAD_ARG, "fs_pcg_solve_batch: system %d: invalid argument", k);
+        if (!valid_material(q.material, (size_t)q.ni * q.nj))
+            return fail(FS_ERR_BAD_ARG, "fs_pcg_solve_batch: system %d: unknown material code", k);
+        if (!cluster_plan(q.ni, q.nj, &plan[k]))
+            return fail(FS_ERR_BAD_ARG,
+                        "fs_pcg_solve_batch: system %d (%d x %d) exceeds the on-chip limit of %lld cells",
+                        k, q.ni, q.nj, cluster_max_cells());
+        off[k + 1] = off[k] + (size_t)q.ni * q.nj;
+    }
+    const size_t N = off[n];
+    std::vector<void *> bufs;
+    auto release = [&]() {
+        for (void *p : bufs) cudaFree(p);
+        bufs.clear();
+    };
+    auto dalloc_tmp = [&](void **p, size_t bytes) -> fs_status {
+        cudaError_t e = cudaMalloc(p, bytes);
+        if (e != cudaSuccess) {
+            release();
+            return fail(e == cudaErrorMemoryAllocation ? FS_ERR_OOM : FS_ERR_CUDA,
+                        "fs_pcg_solve_batch: cudaMalloc: %s", cudaGetErrorString(e));
+        }
+        bufs.push_back(*p);
+        return FS_OK;
+    };
+    auto check = [&](cudaError_t e, const char *what) -> fs_status {
+        if (e == cudaSuccess) return FS_OK;
+        release();
+        return fail(FS_ERR_CUDA, "fs_pcg_solve_batch: %s: %s", what, cudaGetErrorString(e));
+    };
+    int8_t *mat = nullptr;
+    uint8_t *info = nullptr;
+    double *b = nullptr, *x = nullptr, *rel = nullptr;
+    float *dts = nullptr;
+    int *iters = nullptr, *chunk_last = nullptr;
+    Scalars *sc = nullptr;
+    ClusterSystem *sys = nullptr;
+    TRY(dalloc_tmp((void **)&mat, N));
+    TRY(dalloc_tmp((void **)&info, N));
+    TRY(dalloc_tmp((void **)&b, N * 8));
+    TRY(dalloc_tmp((void **)&x, N * 8));
+    TRY(dalloc_tmp((void **)&rel, (size_t)n * 8));
+    TRY(dalloc_tmp((void **)&dts, (size_t)n * 4));
+    TRY(dalloc_tmp((void **)&iters, (size_t)n * 4));
+    TRY(dalloc_tmp((void **)&chunk_last, 2 * sizeof(int)));
+    TRY(dalloc_tmp((void **)&sc, sizeof(Scalars)));
+    TRY(dalloc_tmp((void **)&sys, (size_t)n * sizeof(ClusterSystem)));
+    cudaStream_t st = 0;
+    std::vector<float> hdt(n);
+    for (int k = 0; k < n; k++) hdt[k] = systems[k].dt;
+    TRY(check(cudaMemcpyAsync(dts, hdt.data(), (size_t)n * 4, cudaMemcpyHostToDevice, st), "upload"));
+    TRY(check(cudaMemsetAsync(sc, 0, sizeof(Scalars), st), "memset"));
+    // the systems ordered by cluster size: one launch per size
+    std::vector<int> order(n);
+    for (int k = 0; k < n; k++) order[k] = k;
+    auto key = [&](int k) { return plan[k].C * 64 + plan[k].K; };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return key(a) < key(c); });
+    std::vector<ClusterSystem> hsys(n);
+    for (int t = 0; t < n; t++) {
+        const int k = order[t];
+        const fs_poisson_system &q = systems[k];
+        const size_t nk = (size_t)q.ni * q.nj;
+        TRY(check(cudaMemcpyAsync(mat + off[k], q.material, nk, cudaMemcpyHostToDevice, st), "upload"));
+        TRY(check(cudaMemcpyAsync(b + off[k], q.rhs, nk * 8, cudaMemcpyHostToDevice, st), "upload"));
+        GridDims gd{q.ni, q.nj, q.ni / 3 + (q.ni % 3 != 0), q.nj / 3 + (q.nj % 3 != 0)};
+        Grids G;
+        G.material = mat + off[k];
+        G.cell_info = info + off[k];
+        launch_decomposition(gd, G, chunk_last, 1, (long long)nk, 0, sc, st);
+        g_kernel_launches += 1;
+        ClusterSystem &c = hsys[t];
+        c.ni = q.ni;
+        c.nj = q.nj;
+        c.info = info + off[k];
+        c.b = b + off[k];
+        c.x = x + off[k];
+        c.dt = dts + k;
+        c.density = q.density;
+        c.dx = q.dx;
+        c.iters = iters + k;
+        c.rel_res = rel + k;
+    }
+    TRY(check(cudaMemcpyAsync(sys, hsys.data(), (size_t)n * sizeof(ClusterSystem), cudaMemcpyHostToDevice, st),
+              "upload"));
+    ClusterParams cp;
+    cp.tol = rel_tol;
+    cp.eps_in = 1e-4f;
+    cp.max_iter = max_iter;
+    cp.max_outer = 32;
+    for (int t0 = 0; t0 < n;) {
+        int t1 = t0;
+        ClusterPlan g = plan[order[t0]];
+        while (t1 < n && key(order[t1]) == key(order[t0])) g.smem = std::max(g.smem, plan[order[t1++]].smem);
+        TRY(check(launch_pcg_cluster(sys + t0, t1 - t0, g, cp, st), "cluster PCG"));
+        g_kernel_launches += 1;
+        t0 = t1;
+    }
+    std::vector<int> hit(n);
+    std::vector<double> hrel(n);
+    TRY(check(cudaMemcpyAsync(hit.data(), iters, (size_t)n * 4, cudaMemcpyDeviceToHost, st), "readback"));
+    TRY(check(cudaMemcpyAsync(hrel.data(), rel, (size_t)n * 8, cudaMemcpyDeviceToHost, st), "readback"));
+    for (int k = 0; k < n; k++) {
+        const size_t nk = (size_t)systems[k].ni * systems[k].nj;
+        TRY(check(cudaMemcpyAsync(systems[k].result, x + off[k], nk * 8, cudaMemcpyDeviceToHost, st),
+                  "download"));
+    }
+    TRY(check(cudaStreamSynchronize(st), "sync"));
+    release();
+    for (int k = 0; k < n; k++) {
+        systems[k].iterations = hit[k];
+        systems[k].rel_residual = hrel[k];
+    }
     return FS_OK;
 }
 

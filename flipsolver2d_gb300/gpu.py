@@ -24,7 +24,7 @@ FS_OK = 0
 # fs_status codes (include/fs_gpu.h)
 FS_ERR_BAD_ARG, FS_ERR_CUDA, FS_ERR_OOM, FS_ERR_TIMEOUT, FS_ERR_UNSUPPORTED, FS_ERR_STATE = \
     range(1, 7)
-FS_PCG_FP32, FS_PCG_FP64 = 0, 1
+FS_PCG_FP32, FS_PCG_FP64, FS_PCG_SPEC = 0, 1, 2
 
 # stage ids (FS_STAGE_*), identical to the oracle's
 ADVECT, DECOMPOSITION, REBIN, DENSITY, P2G, SDF, MATERIALS, AFTER_TRANSFER, LEVELSET, \
@@ -98,6 +98,11 @@ _SIGS = {
                                          ctypes.c_double, ctypes.c_double, ctypes.c_void_p,
                                          ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_batch_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "fs_batch_step_frame": (ctypes.c_int, [ctypes.c_void_p]),
+    "fs_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "fs_pcg_solve_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                          ctypes.c_void_p]),
     "fs_pcg_solve_device_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                                    ctypes.c_float, ctypes.c_double, ctypes.c_double,
                                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
@@ -321,6 +326,64 @@ def pcg_solve(material: np.ndarray, rhs: np.ndarray, dt: float, density: float, 
     it = GpuLinearSolver(precision, pool_threads).solve(material, dt, density, dx, x, rhs,
                                                         iter_limit, tol)
     return it, x
+
+
+class Batch:
+    """fs_batch: GpuFlipSolver handles (FS_PCG_SPEC) stepped frame by frame
+    together; each handle's results equal those of stepping it alone."""
+
+    def __init__(self, solvers):
+        self.lib = load()
+        self.solvers = list(solvers)
+        arr = (ctypes.c_void_p * len(self.solvers))(*[g.h.value for g in self.solvers])
+        h = ctypes.c_void_p()
+        _check(self.lib.fs_batch_create(arr, len(self.solvers), ctypes.byref(h)), "fs_batch_create")
+        self.h = h
+
+    def step_frame(self):
+        _check(self.lib.fs_batch_step_frame(self.h), "fs_batch_step_frame")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fs_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PoissonSystem(ctypes.Structure):
+    """fs_poisson_system (include/fs_gpu.h)."""
+    _fields_ = [("ni", ctypes.c_int), ("nj", ctypes.c_int), ("material", ctypes.c_void_p),
+                ("dt", ctypes.c_float), ("density", ctypes.c_double), ("dx", ctypes.c_double),
+                ("rhs", ctypes.c_void_p), ("result", ctypes.c_void_p),
+                ("iterations", ctypes.c_int), ("rel_residual", ctypes.c_double)]
+
+
+def pcg_solve_batch(problems, rel_tol: float = 1e-6, max_iter: int = 100000, device: int = 0):
+    """Batched spec-mode solve (fs_pcg_solve_batch): `problems` is a list of
+    (material int8 [ni, nj], rhs float64 [ni, nj], dt, density, dx).  Returns a
+    list of (inner iterations, solution float64 [ni, nj], relative residual)."""
+    lib = load()
+    n = len(problems)
+    arr = (PoissonSystem * max(n, 1))()
+    keep = []
+    for k, (mat, rhs, dt, density, dx) in enumerate(problems):
+        ni, nj = mat.shape
+        m = np.ascontiguousarray(mat, np.int8)
+        b = np.ascontiguousarray(rhs, np.float64).reshape(ni, nj)
+        x = np.zeros((ni, nj), np.float64)
+        keep.append((m, b, x))
+        arr[k] = PoissonSystem(ni, nj, m.ctypes.data, float(dt), float(density), float(dx),
+                               b.ctypes.data, x.ctypes.data, 0, 0.0)
+    ex = ExecParams(FS_PCG_FP32, 0, device)
+    st = lib.fs_pcg_solve_batch(ctypes.addressof(arr), n, float(rel_tol), int(max_iter),
+                                ctypes.byref(ex))
+    _check(st, "fs_pcg_solve_batch")
+    return [(int(arr[k].iterations), keep[k][2], float(arr[k].rel_residual)) for k in range(n)]
 
 
 def pcg_solve_spec(material: np.ndarray, rhs: np.ndarray, dt: float, density: float, dx: float,

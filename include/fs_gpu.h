@@ -61,11 +61,22 @@ typedef struct fs_params {
     int parameterHandlingMethod; /* 0 PARTICLE, 1 HYBRID, 2 GRID */
 } fs_params;
 
-enum { FS_PCG_FP32 = 0, FS_PCG_FP64 = 1 };
+/* Pressure and density solves of a solver handle:
+ *   FS_PCG_FP32  the reference's PCG and stopping rule with FP32 vectors
+ *   FS_PCG_FP64  the same in FP64, bit for bit the reference's
+ *   FS_PCG_SPEC  every solve to a true relative residual of 1e-6: FP32 inner
+ *                PCG with the textbook incomplete-Poisson preconditioner and
+ *                FP64 refinement (fs_pcg_solve_spec's method), on one
+ *                thread-block cluster; FP64 right-hand sides and pressures.
+ *                For grids up to the on-chip limit of fs_pcg_solve_batch
+ *                (fs_create fails with FS_ERR_UNSUPPORTED above it).  The
+ *                density push is skipped when its solve hits 20000 inner
+ *                iterations, the counterpart of the reference's limit test. */
+enum { FS_PCG_FP32 = 0, FS_PCG_FP64 = 1, FS_PCG_SPEC = 2 };
 
 /* Execution knobs with no counterpart in FlipSolverParameters. */
 typedef struct fs_exec_params {
-    int pcg_precision; /* FS_PCG_FP32 (default) or FS_PCG_FP64 vectors */
+    int pcg_precision; /* FS_PCG_FP32 (default), FS_PCG_FP64 or FS_PCG_SPEC */
     int pool_threads;  /* chunk count of the reference's max-abs residual test
                           (ThreadPool size, threadpool.cpp:12); 0 = this host's
                           std::thread::hardware_concurrency() like the reference */
@@ -221,6 +232,50 @@ fs_status fs_pcg_solve_spec(int ni, int nj, const int8_t *material, float dt, do
                             double dx, const double *rhs, double *result, double rel_tol,
                             int max_iter, const fs_exec_params *exec, int *iterations,
                             double *rel_residual);
+
+/* A batch of solver handles stepped together; no reference counterpart as a
+ * batch (each handle is a FlipSolver, flipsolver2d.h:183-432).
+ * fs_batch_step_frame advances every handle by one frame exactly as
+ * fs_step_frame would (FlipSolver::stepFrame's CFL loop,
+ * flipsolver2d.cpp:464-500) and gives the same results bit for bit; the
+ * handles' substeps are interleaved round by round, each substep runs as
+ * captured CUDA graphs, and the density and pressure solves of all handles
+ * in a round share one cluster launch per plan.  Every handle must use
+ * FS_PCG_SPEC, sit on one device, have timers off and appear once.  The
+ * graphs hold each handle's device buffers: between batch calls a handle
+ * may be read (fs_get_*) or stepped on its own, but fs_set_particles /
+ * fs_set_grid need a new batch.  After an error the handles' state is
+ * undefined.  fs_batch_destroy leaves the handles alive. */
+typedef struct fs_batch fs_batch;
+fs_status fs_batch_create(fs_solver *const *solvers, int n, fs_batch **out);
+fs_status fs_batch_step_frame(fs_batch *batch);
+fs_status fs_batch_destroy(fs_batch *batch);
+
+/* One system of fs_pcg_solve_batch: the problem of fs_pcg_solve_spec
+ * (host arrays; result and the two outputs are written). */
+typedef struct fs_poisson_system {
+    int ni, nj;
+    const int8_t *material; /* ni * nj material codes */
+    float dt;
+    double density, dx;
+    const double *rhs;      /* ni * nj */
+    double *result;         /* ni * nj, written */
+    int iterations;         /* out: inner PCG iterations */
+    double rel_residual;    /* out: ||rhs - A result|| / ||rhs|| (FP64) */
+} fs_poisson_system;
+
+/* Batched spec-mode solve, with no reference counterpart as a batch: every
+ * system is the solve of fs_pcg_solve_spec (the reference's pressure
+ * operator, LinearSolver::solve's problem, linearsolver.h:15-20, to a true
+ * relative residual), and all of them run at once -- one thread-block cluster
+ * per system, systems of one cluster size in one launch, every vector of the
+ * iteration held on chip.  A system's result does not depend on the other
+ * systems of the call.  A system larger than the on-chip limit (512 x 512
+ * cells on GB300) is rejected with FS_ERR_BAD_ARG before any device work; a
+ * system that does not reach rel_tol within max_iter inner iterations
+ * returns its best result with its residual.  exec may be NULL. */
+fs_status fs_pcg_solve_batch(fs_poisson_system *systems, int n, double rel_tol, int max_iter,
+                             const fs_exec_params *exec);
 
 /* fs_pcg_solve_device without any device allocation.  This entry point has
  * no counterpart in the reference.  It is for callers that cannot allocate
