@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cfloat>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -201,6 +202,8 @@ struct fs_solver {
     cudaEvent_t p0[2] = {nullptr, nullptr}, p1[2] = {nullptr, nullptr};
     bool pcg_timed[2] = {false, false};
     std::vector<void *> allocs;
+    std::vector<size_t> alloc_bytes; // beside allocs
+    size_t device_bytes = 0;
 };
 
 template <typename T> static fs_status dalloc(fs_solver *s, T **p, size_t count)
@@ -210,6 +213,8 @@ template <typename T> static fs_status dalloc(fs_solver *s, T **p, size_t count)
     if (bytes == 0) bytes = 16;
     CK(cudaMalloc(&q, bytes));
     s->allocs.push_back(q);
+    s->alloc_bytes.push_back(bytes);
+    s->device_bytes += bytes;
     *p = (T *)q;
     return FS_OK;
 }
@@ -218,7 +223,12 @@ static void dfree(fs_solver *s, void *p)
 {
     if (!p) return;
     auto it = std::find(s->allocs.begin(), s->allocs.end(), p);
-    if (it != s->allocs.end()) s->allocs.erase(it);
+    if (it != s->allocs.end()) {
+        const size_t k = (size_t)(it - s->allocs.begin());
+        s->device_bytes -= s->alloc_bytes[k];
+        s->alloc_bytes.erase(s->alloc_bytes.begin() + (long)k);
+        s->allocs.erase(it);
+    }
     cudaFree(p);
 }
 
@@ -256,6 +266,8 @@ static fs_status alloc_particles(fs_solver *s, int cap)
     void *q = nullptr;
     CK(cudaMalloc(&q, s->rebin_scratch_size));
     s->allocs.push_back(q);
+    s->alloc_bytes.push_back(s->rebin_scratch_size);
+    s->device_bytes += s->rebin_scratch_size;
     s->rebin_scratch = q;
     return FS_OK;
 }
@@ -1293,6 +1305,13 @@ extern "C" fs_status fs_get_stream(fs_solver *s, void **stream)
     return FS_OK;
 }
 
+extern "C" fs_status fs_device_bytes(fs_solver *s, size_t *bytes)
+{
+    if (!s || !bytes) return fail(FS_ERR_BAD_ARG, "null argument");
+    *bytes = s->device_bytes;
+    return FS_OK;
+}
+
 extern "C" fs_status fs_synchronize(fs_solver *s)
 {
     if (!s) return fail(FS_ERR_BAD_ARG, "null handle");
@@ -1318,8 +1337,11 @@ extern "C" fs_status fs_synchronize(fs_solver *s)
 // two versions of each graph are captured, for even and odd substeps, and
 // the handle's host-side pointer state follows the parity.
 // ---------------------------------------------------------------------------
+static bool valid_material(const int8_t *m, size_t n);
+
 struct BatchScene {
     fs_solver *s = nullptr;
+    int slot = 0; // its entry in the batch's dt table (fixed while it is a member)
     cudaGraphExec_t g[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
     long long launches[3] = {0, 0, 0};
     Particles P[2];
@@ -1327,21 +1349,48 @@ struct BatchScene {
     int parity = 0;
     cudaEvent_t ev = nullptr;
     // the frame in progress (fs_step_frame's locals)
+    bool in_frame = false;
+    bool last = false; // the substep of this round ends the frame
     float substep_time = 0.f;
     int substep_count = 0;
-    bool finished = true;
+};
+
+// a standalone system submitted to the batch: device copies of its arrays
+struct BatchSolve {
+    unsigned long long ticket = 0;
+    int ni = 0, nj = 0;
+    void *mem = nullptr; // one allocation: material, info, b, x, dt, iters, rel
+    ClusterSystem sys{};
+    ClusterPlan plan{};
+    bool done = false;
 };
 
 struct fs_batch {
     std::vector<BatchScene> sc;
+    std::vector<BatchSolve> solves;
+    unsigned long long next_ticket = 1;
     int device = 0;
+    static constexpr int kSlots = 4096;
+    std::vector<int> free_slots;
     cudaStream_t bst = nullptr; // merged solves
     cudaEvent_t ev_solve = nullptr;
-    float *d_dt = nullptr, *h_dt = nullptr;                // per scene
-    ClusterSystem *d_list = nullptr, *h_list = nullptr;   // 2 n: the round's systems
+    float *d_dt = nullptr, *h_dt = nullptr;              // kSlots
+    ClusterSystem *d_list = nullptr, *h_list = nullptr; // two lists of list_cap
+    size_t list_cap = 0;
+    int *chunk_last = nullptr; // decomposition scratch of submitted systems
+    Scalars *dsc = nullptr;
+    cudaEvent_t ev_t[4] = {nullptr, nullptr, nullptr, nullptr}; // merged solves, timed
+    // one stream per plan group, so that clusters of different sizes share
+    // the SMs (a GPC left over by 16-CTA clusters takes smaller ones)
+    static constexpr int kGroups = 6;
+    cudaStream_t gst[kGroups] = {};
+    cudaEvent_t gev[kGroups] = {};
+    cudaEvent_t ev_fork = nullptr;
+    double solve_ms = 0.0, frame_ms = 0.0;
+    long long rounds = 0;
 };
 
-static fs_status batch_capture(fs_batch *b, BatchScene &bs, int idx, int parity)
+static fs_status batch_capture(fs_batch *b, BatchScene &bs, int parity)
 {
     fs_solver *s = bs.s;
     const GridDims &d = s->d;
@@ -1352,7 +1401,7 @@ static fs_status batch_capture(fs_batch *b, BatchScene &bs, int idx, int parity)
         CK(cudaStreamBeginCapture(q, cudaStreamCaptureModeRelaxed));
         fs_status st = FS_OK;
         if (seg == 0) {
-            k_set_dt_from<<<1, 1, 0, q>>>(s->sc, b->d_dt + idx);
+            k_set_dt_from<<<1, 1, 0, q>>>(s->sc, b->d_dt + bs.slot);
             g_kernel_launches += 1;
             cudaMemsetAsync(&s->sc->density_iters, 0, 2 * sizeof(int), q);
             st = stage(s, FS_STAGE_ADVECT, true);
@@ -1393,11 +1442,10 @@ static fs_status batch_capture(fs_batch *b, BatchScene &bs, int idx, int parity)
             if (graph) cudaGraphDestroy(graph);
             return st;
         }
-        if (ec != cudaSuccess) return fail(FS_ERR_CUDA, "fs_batch_create: capture: %s", cudaGetErrorString(ec));
+        if (ec != cudaSuccess) return fail(FS_ERR_CUDA, "fs_batch: capture: %s", cudaGetErrorString(ec));
         const cudaError_t ei = cudaGraphInstantiate(&bs.g[parity][seg], graph, 0);
         cudaGraphDestroy(graph);
-        if (ei != cudaSuccess)
-            return fail(FS_ERR_CUDA, "fs_batch_create: instantiate: %s", cudaGetErrorString(ei));
+        if (ei != cudaSuccess) return fail(FS_ERR_CUDA, "fs_batch: instantiate: %s", cudaGetErrorString(ei));
         bs.launches[seg] = g_kernel_launches - before;
     }
     return FS_OK;
@@ -1414,7 +1462,7 @@ static void batch_release_graphs(BatchScene &bs)
 
 // captures both substep parities from the handle's current buffers; the
 // handle's host-side pointer state is left as it was
-static fs_status batch_prepare(fs_batch *b, BatchScene &bs, int idx)
+static fs_status batch_prepare(fs_batch *b, BatchScene &bs)
 {
     fs_solver *s = bs.s;
     batch_release_graphs(bs);
@@ -1422,11 +1470,11 @@ static fs_status batch_prepare(fs_batch *b, BatchScene &bs, int idx)
     TRY(sync_all(s));
     bs.P[0] = s->P;
     bs.G[0] = s->G;
-    fs_status st = batch_capture(b, bs, idx, 0);
+    fs_status st = batch_capture(b, bs, 0);
     if (st == FS_OK) {
         bs.P[1] = s->P;
         bs.G[1] = s->G;
-        st = batch_capture(b, bs, idx, 1);
+        st = batch_capture(b, bs, 1);
     }
     const bool back = memcmp(&s->P, &bs.P[0], sizeof(Particles)) == 0 &&
                       memcmp(&s->G, &bs.G[0], sizeof(Grids)) == 0;
@@ -1438,6 +1486,22 @@ static fs_status batch_prepare(fs_batch *b, BatchScene &bs, int idx)
     return st;
 }
 
+static BatchScene *batch_find(fs_batch *b, fs_solver *s)
+{
+    for (BatchScene &bs : b->sc)
+        if (bs.s == s) return &bs;
+    return nullptr;
+}
+
+static fs_status batch_check_handle(fs_batch *b, fs_solver *s, const char *where)
+{
+    if (!s) return fail(FS_ERR_BAD_ARG, "%s: null handle", where);
+    if (s->prec != FS_PCG_SPEC) return fail(FS_ERR_UNSUPPORTED, "%s: the handle is not in FS_PCG_SPEC mode", where);
+    if (s->ex.device != b->device) return fail(FS_ERR_BAD_ARG, "%s: the handle is on another device", where);
+    if (s->timers) return fail(FS_ERR_UNSUPPORTED, "%s: the handle has timers on", where);
+    return FS_OK;
+}
+
 extern "C" fs_status fs_batch_destroy(fs_batch *b)
 {
     if (!b) return FS_OK;
@@ -1447,32 +1511,84 @@ extern "C" fs_status fs_batch_destroy(fs_batch *b)
         batch_release_graphs(bs);
         if (bs.ev) cudaEventDestroy(bs.ev);
     }
+    for (BatchSolve &q : b->solves)
+        if (q.mem) cudaFree(q.mem);
     if (b->ev_solve) cudaEventDestroy(b->ev_solve);
+    for (cudaEvent_t e : b->ev_t)
+        if (e) cudaEventDestroy(e);
+    for (int g = 0; g < fs_batch::kGroups; g++) {
+        if (b->gst[g]) cudaStreamDestroy(b->gst[g]);
+        if (b->gev[g]) cudaEventDestroy(b->gev[g]);
+    }
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
     if (b->bst) cudaStreamDestroy(b->bst);
     if (b->d_dt) cudaFree(b->d_dt);
     if (b->d_list) cudaFree(b->d_list);
+    if (b->chunk_last) cudaFree(b->chunk_last);
+    if (b->dsc) cudaFree(b->dsc);
     if (b->h_dt) cudaFreeHost(b->h_dt);
     if (b->h_list) cudaFreeHost(b->h_list);
     delete b;
     return FS_OK;
 }
 
+extern "C" fs_status fs_batch_add(fs_batch *b, fs_solver *s)
+{
+    if (!b) return fail(FS_ERR_BAD_ARG, "null batch");
+    TRY(batch_check_handle(b, s, "fs_batch_add"));
+    if (batch_find(b, s)) return fail(FS_ERR_BAD_ARG, "fs_batch_add: the handle is already a member");
+    if (b->free_slots.empty()) return fail(FS_ERR_BAD_ARG, "fs_batch_add: the batch is full (%d)", fs_batch::kSlots);
+    CK(cudaSetDevice(b->device));
+    BatchScene bs;
+    bs.s = s;
+    if (cudaEventCreateWithFlags(&bs.ev, cudaEventDisableTiming) != cudaSuccess)
+        return fail(FS_ERR_CUDA, "fs_batch_add: event");
+    bs.slot = b->free_slots.back();
+    // a handle that has not stepped yet is captured at its first frame,
+    // once its particles exist
+    if (s->frame > 0) {
+        const fs_status st = batch_prepare(b, bs);
+        if (st != FS_OK) {
+            cudaEventDestroy(bs.ev);
+            return st;
+        }
+    }
+    b->free_slots.pop_back();
+    b->sc.push_back(bs);
+    return FS_OK;
+}
+
+extern "C" fs_status fs_batch_remove(fs_batch *b, fs_solver *s)
+{
+    if (!b || !s) return fail(FS_ERR_BAD_ARG, "null argument");
+    for (size_t k = 0; k < b->sc.size(); k++) {
+        BatchScene &bs = b->sc[k];
+        if (bs.s != s) continue;
+        if (bs.in_frame) return fail(FS_ERR_BAD_ARG, "fs_batch_remove: the handle is inside a frame");
+        CK(cudaSetDevice(b->device));
+        TRY(sync_all(s));
+        batch_release_graphs(bs);
+        if (bs.ev) cudaEventDestroy(bs.ev);
+        b->free_slots.push_back(bs.slot);
+        b->sc.erase(b->sc.begin() + (long)k);
+        return FS_OK;
+    }
+    return fail(FS_ERR_BAD_ARG, "fs_batch_remove: not a member");
+}
+
 extern "C" fs_status fs_batch_create(fs_solver *const *solvers, int n, fs_batch **out)
 {
-    if (!out || n < 1 || !solvers) return fail(FS_ERR_BAD_ARG, "fs_batch_create: invalid argument");
+    if (!out || n < 0 || (n > 0 && !solvers)) return fail(FS_ERR_BAD_ARG, "fs_batch_create: invalid argument");
     *out = nullptr;
-    for (int k = 0; k < n; k++) {
-        if (!solvers[k]) return fail(FS_ERR_BAD_ARG, "fs_batch_create: null handle %d", k);
-        if (solvers[k]->prec != FS_PCG_SPEC)
-            return fail(FS_ERR_UNSUPPORTED, "fs_batch_create: handle %d is not in FS_PCG_SPEC mode", k);
-        if (solvers[k]->ex.device != solvers[0]->ex.device)
-            return fail(FS_ERR_BAD_ARG, "fs_batch_create: handles on different devices");
-        if (solvers[k]->timers) return fail(FS_ERR_UNSUPPORTED, "fs_batch_create: handle %d has timers on", k);
-        for (int j = 0; j < k; j++)
-            if (solvers[j] == solvers[k]) return fail(FS_ERR_BAD_ARG, "fs_batch_create: handle %d twice", k);
+    int dev = 0;
+    if (n > 0) {
+        if (!solvers[0]) return fail(FS_ERR_BAD_ARG, "fs_batch_create: null handle 0");
+        dev = solvers[0]->ex.device;
+    } else {
+        CK(cudaGetDevice(&dev));
     }
     fs_batch *b = new fs_batch();
-    b->device = solvers[0]->ex.device;
+    b->device = dev;
     auto cleanup = [&](fs_status st) {
         fs_batch_destroy(b);
         return st;
@@ -1480,41 +1596,214 @@ extern "C" fs_status fs_batch_create(fs_solver *const *solvers, int n, fs_batch 
     if (cudaSetDevice(b->device) != cudaSuccess) return cleanup(fail(FS_ERR_CUDA, "fs_batch_create: device"));
     if (cudaStreamCreateWithFlags(&b->bst, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->ev_solve, cudaEventDisableTiming) != cudaSuccess ||
-        cudaMalloc(&b->d_dt, (size_t)n * sizeof(float)) != cudaSuccess ||
-        cudaMalloc(&b->d_list, (size_t)2 * n * sizeof(ClusterSystem)) != cudaSuccess ||
-        cudaMallocHost(&b->h_dt, (size_t)n * sizeof(float)) != cudaSuccess ||
-        cudaMallocHost(&b->h_list, (size_t)2 * n * sizeof(ClusterSystem)) != cudaSuccess)
+        cudaEventCreate(&b->ev_t[0]) != cudaSuccess || cudaEventCreate(&b->ev_t[1]) != cudaSuccess ||
+        cudaEventCreate(&b->ev_t[2]) != cudaSuccess || cudaEventCreate(&b->ev_t[3]) != cudaSuccess ||
+        cudaMalloc(&b->d_dt, (size_t)fs_batch::kSlots * sizeof(float)) != cudaSuccess ||
+        cudaMallocHost(&b->h_dt, (size_t)fs_batch::kSlots * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&b->chunk_last, 2 * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&b->dsc, sizeof(Scalars)) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess)
         return cleanup(fail(FS_ERR_OOM, "fs_batch_create: allocation failed"));
-    b->sc.resize(n);
+    for (int g = 0; g < fs_batch::kGroups; g++)
+        if (cudaStreamCreateWithFlags(&b->gst[g], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b->gev[g], cudaEventDisableTiming) != cudaSuccess)
+            return cleanup(fail(FS_ERR_CUDA, "fs_batch_create: stream"));
+    if (cudaMemset(b->dsc, 0, sizeof(Scalars)) != cudaSuccess)
+        return cleanup(fail(FS_ERR_CUDA, "fs_batch_create: memset"));
+    for (int k = fs_batch::kSlots - 1; k >= 0; k--) b->free_slots.push_back(k);
     for (int k = 0; k < n; k++) {
-        BatchScene &bs = b->sc[k];
-        bs.s = solvers[k];
-        if (cudaEventCreateWithFlags(&bs.ev, cudaEventDisableTiming) != cudaSuccess)
-            return cleanup(fail(FS_ERR_CUDA, "fs_batch_create: event"));
-        // a handle that has not stepped yet is captured at its first frame,
-        // once its particles exist
-        if (bs.s->frame > 0) {
-            const fs_status st = batch_prepare(b, bs, k);
-            if (st != FS_OK) return cleanup(st);
-        }
+        const fs_status st = fs_batch_add(b, solvers[k]);
+        if (st != FS_OK) return cleanup(st);
     }
     *out = b;
     return FS_OK;
 }
 
-// one merged solve (0 density, 1 pressure) over the scenes of `act`
-static fs_status batch_solve(fs_batch *b, const std::vector<int> &act, int which)
+// starts a frame of a member (fs_step_frame's set-up): first-frame seeding at
+// frame 0, a new capture if the handle's buffers moved since the last one
+// (seeding, fs_set_particles, ...), and the max velocity the first substep's
+// dt needs (into the pinned scalars; waited for before the round reads it)
+static fs_status batch_begin(fs_batch *b, BatchScene &bs)
 {
-    const int n = (int)b->sc.size();
-    ClusterSystem *hl = b->h_list + (size_t)which * n;
-    ClusterSystem *dl = b->d_list + (size_t)which * n;
-    std::vector<int> order(act);
-    auto key = [&](int k) { return b->sc[k].s->spec_plan.C * 64 + b->sc[k].s->spec_plan.K; };
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return key(x) < key(y); });
-    for (int k : act) CK(cudaStreamWaitEvent(b->bst, b->sc[k].ev, 0));
-    for (size_t t = 0; t < order.size(); t++) {
-        fs_solver *s = b->sc[order[t]].s;
-        ClusterSystem &c = hl[t];
+    fs_solver *s = bs.s;
+    if (s->frame == 0) TRY(fs_first_frame_init(s));
+    TRY(sync_all(s));
+    if (!bs.g[0][0] || memcmp(&s->P, &bs.P[bs.parity], sizeof(Particles)) != 0 ||
+        memcmp(&s->G, &bs.G[bs.parity], sizeof(Grids)) != 0)
+        TRY(batch_prepare(b, bs));
+    launch_max_velocity(s->P, s->sc, s->st);
+    g_kernel_launches += 2;
+    CK(cudaMemcpyAsync(s->sc_host, s->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s->st));
+    bs.substep_time = 0.f;
+    bs.substep_count = 0;
+    bs.in_frame = true;
+    s->density_iters_max = s->pressure_iters_max = s->substeps = 0;
+    return FS_OK;
+}
+
+extern "C" fs_status fs_batch_begin_frame(fs_batch *b, fs_solver *s)
+{
+    if (!b) return fail(FS_ERR_BAD_ARG, "null batch");
+    BatchScene *bs = batch_find(b, s);
+    if (!bs) return fail(FS_ERR_BAD_ARG, "fs_batch_begin_frame: not a member");
+    if (bs->in_frame) return fail(FS_ERR_BAD_ARG, "fs_batch_begin_frame: the handle is inside a frame");
+    CK(cudaSetDevice(b->device));
+    TRY(batch_begin(b, *bs));
+    CK(cudaStreamSynchronize(s->st));
+    return FS_OK;
+}
+
+extern "C" fs_status fs_batch_in_frame(fs_batch *b, fs_solver *s, int *in_frame)
+{
+    if (!b || !in_frame) return fail(FS_ERR_BAD_ARG, "null argument");
+    BatchScene *bs = batch_find(b, s);
+    if (!bs) return fail(FS_ERR_BAD_ARG, "fs_batch_in_frame: not a member");
+    *in_frame = bs->in_frame ? 1 : 0;
+    return FS_OK;
+}
+
+extern "C" fs_status fs_batch_submit_solve(fs_batch *b, const fs_poisson_system *q, unsigned long long *ticket)
+{
+    if (!b || !q || !ticket || q->ni < 1 || q->nj < 1 || !q->material || !q->rhs)
+        return fail(FS_ERR_BAD_ARG, "fs_batch_submit_solve: invalid argument");
+    const size_t N = (size_t)q->ni * q->nj;
+    if (!valid_material(q->material, N)) return fail(FS_ERR_BAD_ARG, "fs_batch_submit_solve: unknown material code");
+    BatchSolve v;
+    if (!cluster_plan(q->ni, q->nj, &v.plan))
+        return fail(FS_ERR_BAD_ARG, "fs_batch_submit_solve: %d x %d exceeds the on-chip limit of %lld cells",
+                    q->ni, q->nj, cluster_max_cells());
+    CK(cudaSetDevice(b->device));
+    const size_t a = (N + 255) & ~(size_t)255;
+    const size_t bytes = 2 * a + 16 * N + 256;
+    cudaError_t e = cudaMalloc(&v.mem, bytes);
+    if (e != cudaSuccess)
+        return fail(e == cudaErrorMemoryAllocation ? FS_ERR_OOM : FS_ERR_CUDA, "fs_batch_submit_solve: cudaMalloc: %s",
+                    cudaGetErrorString(e));
+    char *p = static_cast<char *>(v.mem);
+    int8_t *mat = reinterpret_cast<int8_t *>(p);
+    uint8_t *info = reinterpret_cast<uint8_t *>(p + a);
+    double *bv = reinterpret_cast<double *>(p + 2 * a);
+    double *xv = bv + N;
+    char *tail = reinterpret_cast<char *>(xv + N);
+    float *dt = reinterpret_cast<float *>(tail);
+    int *iters = reinterpret_cast<int *>(tail + 16);
+    double *rel = reinterpret_cast<double *>(tail + 32);
+    cudaStream_t st = b->bst;
+    auto bail = [&](cudaError_t err) {
+        cudaFree(v.mem);
+        return fail(FS_ERR_CUDA, "fs_batch_submit_solve: %s", cudaGetErrorString(err));
+    };
+    if ((e = cudaMemcpyAsync(mat, q->material, N, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(bv, q->rhs, N * 8, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(dt, &q->dt, sizeof(float), cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return bail(e);
+    GridDims gd{q->ni, q->nj, q->ni / 3 + (q->ni % 3 != 0), q->nj / 3 + (q->nj % 3 != 0)};
+    Grids G;
+    G.material = mat;
+    G.cell_info = info;
+    launch_decomposition(gd, G, b->chunk_last, 1, (long long)N, 0, b->dsc, st);
+    g_kernel_launches += 1;
+    if ((e = cudaGetLastError()) != cudaSuccess) return bail(e);
+    // the host arrays may be reused once this returns
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return bail(e);
+    v.ticket = b->next_ticket++;
+    v.ni = q->ni;
+    v.nj = q->nj;
+    ClusterSystem &c = v.sys;
+    c.ni = q->ni;
+    c.nj = q->nj;
+    c.info = info;
+    c.b = bv;
+    c.x = xv;
+    c.dt = dt;
+    c.density = q->density;
+    c.dx = q->dx;
+    c.iters = iters;
+    c.rel_res = rel;
+    b->solves.push_back(v);
+    *ticket = v.ticket;
+    return FS_OK;
+}
+
+static BatchSolve *batch_find_solve(fs_batch *b, unsigned long long ticket, size_t *index)
+{
+    for (size_t k = 0; k < b->solves.size(); k++)
+        if (b->solves[k].ticket == ticket) {
+            if (index) *index = k;
+            return &b->solves[k];
+        }
+    return nullptr;
+}
+
+extern "C" fs_status fs_batch_solve_done(fs_batch *b, unsigned long long ticket, int *done)
+{
+    if (!b || !done) return fail(FS_ERR_BAD_ARG, "null argument");
+    BatchSolve *v = batch_find_solve(b, ticket, nullptr);
+    if (!v) return fail(FS_ERR_BAD_ARG, "fs_batch_solve_done: unknown ticket");
+    *done = v->done ? 1 : 0;
+    return FS_OK;
+}
+
+extern "C" fs_status fs_batch_take_solve(fs_batch *b, unsigned long long ticket, fs_poisson_system *q)
+{
+    if (!b || !q || !q->result) return fail(FS_ERR_BAD_ARG, "null argument");
+    size_t k = 0;
+    BatchSolve *v = batch_find_solve(b, ticket, &k);
+    if (!v) return fail(FS_ERR_BAD_ARG, "fs_batch_take_solve: unknown ticket");
+    if (!v->done) return fail(FS_ERR_BAD_ARG, "fs_batch_take_solve: not solved yet");
+    if (q->ni != v->ni || q->nj != v->nj) return fail(FS_ERR_BAD_ARG, "fs_batch_take_solve: shape mismatch");
+    CK(cudaSetDevice(b->device));
+    const size_t N = (size_t)v->ni * v->nj;
+    int it = 0;
+    double rel = 0.0;
+    CK(cudaMemcpy(q->result, v->sys.x, N * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&it, v->sys.iters, sizeof(int), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&rel, v->sys.rel_res, sizeof(double), cudaMemcpyDeviceToHost));
+    q->iterations = it;
+    q->rel_residual = rel;
+    cudaFree(v->mem);
+    b->solves.erase(b->solves.begin() + (long)k);
+    return FS_OK;
+}
+
+extern "C" fs_status fs_batch_timer(fs_batch *b, int which, double *value)
+{
+    if (!b || !value) return fail(FS_ERR_BAD_ARG, "null argument");
+    switch (which) {
+    case 0: *value = b->solve_ms; return FS_OK;
+    case 1: *value = b->frame_ms; return FS_OK;
+    case 2: *value = (double)b->rounds; return FS_OK;
+    case 3: b->solve_ms = b->frame_ms = 0.0; b->rounds = 0; *value = 0.0; return FS_OK;
+    default: return fail(FS_ERR_BAD_ARG, "bad timer id");
+    }
+}
+
+// one merged solve (0 density, 1 pressure) over the scenes of `act` plus,
+// for the pressure solve, the submitted standalone systems `extra`
+static fs_status batch_solve(fs_batch *b, const std::vector<int> &act, const std::vector<int> &extra,
+                             int which)
+{
+    const size_t total = act.size() + (which == 1 ? extra.size() : 0);
+    if (total > b->list_cap) {
+        CK(cudaDeviceSynchronize());
+        if (b->d_list) cudaFree(b->d_list);
+        if (b->h_list) cudaFreeHost(b->h_list);
+        b->d_list = nullptr;
+        b->h_list = nullptr;
+        b->list_cap = 0;
+        const size_t cap = std::max<size_t>(2 * total, 64);
+        CK(cudaMalloc(&b->d_list, 2 * cap * sizeof(ClusterSystem)));
+        CK(cudaMallocHost(&b->h_list, 2 * cap * sizeof(ClusterSystem)));
+        b->list_cap = cap;
+    }
+    ClusterSystem *hl = b->h_list + (size_t)which * b->list_cap;
+    ClusterSystem *dl = b->d_list + (size_t)which * b->list_cap;
+    // entries: scenes then standalone systems, each with its plan
+    std::vector<std::pair<ClusterPlan, ClusterSystem>> ent;
+    ent.reserve(total);
+    for (int k : act) {
+        fs_solver *s = b->sc[k].s;
+        ClusterSystem c;
         c.ni = s->d.ni;
         c.nj = s->d.nj;
         c.info = s->G.cell_info;
@@ -1525,117 +1814,152 @@ static fs_status batch_solve(fs_batch *b, const std::vector<int> &act, int which
         c.dx = s->sp.dx;
         c.iters = which == 0 ? &s->sc->density_iters : &s->sc->pressure_iters;
         c.rel_res = s->spec_rel + which;
+        ent.push_back({s->spec_plan, c});
     }
-    CK(cudaMemcpyAsync(dl, hl, order.size() * sizeof(ClusterSystem), cudaMemcpyHostToDevice, b->bst));
+    if (which == 1)
+        for (int k : extra) ent.push_back({b->solves[k].plan, b->solves[k].sys});
+    if (ent.empty()) return FS_OK;
+    auto key = [](const ClusterPlan &q) { return q.C * 64 + q.K; };
+    // the largest clusters first: they wait longest for whole GPCs
+    std::stable_sort(ent.begin(), ent.end(), [&](const auto &x, const auto &y) { return key(x.first) > key(y.first); });
+    for (size_t t = 0; t < ent.size(); t++) hl[t] = ent[t].second;
+    for (int k : act) CK(cudaStreamWaitEvent(b->bst, b->sc[k].ev, 0));
+    CK(cudaMemcpyAsync(dl, hl, ent.size() * sizeof(ClusterSystem), cudaMemcpyHostToDevice, b->bst));
+    CK(cudaEventRecord(b->ev_t[2 * which], b->bst));
+    CK(cudaEventRecord(b->ev_fork, b->bst));
     const ClusterParams cp = spec_params();
-    for (size_t t0 = 0; t0 < order.size();) {
+    int ng = 0;
+    for (size_t t0 = 0; t0 < ent.size();) {
         size_t t1 = t0;
-        ClusterPlan g = b->sc[order[t0]].s->spec_plan;
-        while (t1 < order.size() && key(order[t1]) == key(order[t0]))
-            g.smem = std::max(g.smem, b->sc[order[t1++]].s->spec_plan.smem);
-        CK(launch_pcg_cluster(dl + t0, (int)(t1 - t0), g, cp, b->bst));
+        ClusterPlan g = ent[t0].first;
+        while (t1 < ent.size() && key(ent[t1].first) == key(ent[t0].first)) g.smem = std::max(g.smem, ent[t1++].first.smem);
+        const int gi = ng % fs_batch::kGroups;
+        cudaStream_t gs = b->gst[gi];
+        CK(cudaStreamWaitEvent(gs, b->ev_fork, 0));
+        CK(launch_pcg_cluster(dl + t0, (int)(t1 - t0), g, cp, gs));
+        CK(cudaEventRecord(b->gev[gi], gs));
+        ng++;
         g_kernel_launches += 1;
         t0 = t1;
     }
+    for (int gi = 0; gi < std::min(ng, (int)fs_batch::kGroups); gi++) CK(cudaStreamWaitEvent(b->bst, b->gev[gi], 0));
+    CK(cudaEventRecord(b->ev_t[2 * which + 1], b->bst));
     CK(cudaEventRecord(b->ev_solve, b->bst));
     return FS_OK;
 }
 
-extern "C" fs_status fs_batch_step_frame(fs_batch *b)
+// one round: a substep of every member inside a frame, the standalone
+// systems submitted so far solved with the round's pressure solves
+static fs_status batch_round(fs_batch *b, int *busy)
 {
-    if (!b) return fail(FS_ERR_BAD_ARG, "null batch");
-    CK(cudaSetDevice(b->device));
-    const int n = (int)b->sc.size();
-    // frame start: first-frame set-up and the max velocity of every handle
-    for (int k = 0; k < n; k++) {
+    const auto t0 = std::chrono::steady_clock::now();
+    std::vector<int> act, extra;
+    // the CFL step of every member inside its frame (fs_step_frame's loop)
+    for (int k = 0; k < (int)b->sc.size(); k++) {
         BatchScene &bs = b->sc[k];
         fs_solver *s = bs.s;
-        if (s->frame == 0) TRY(fs_first_frame_init(s));
-        TRY(sync_all(s));
-        // the graphs hold device pointers: capture again if the handle's
-        // buffers moved since (first-frame seeding, fs_set_particles, ...)
-        if (!bs.g[0][0] || memcmp(&s->P, &bs.P[bs.parity], sizeof(Particles)) != 0 ||
-            memcmp(&s->G, &bs.G[bs.parity], sizeof(Grids)) != 0) {
-            TRY(batch_prepare(b, bs, k));
+        if (!bs.in_frame) continue;
+        if (s->sc_host->pcg_status != 0) return fail(FS_ERR_TIMEOUT, "batch member %d: solver status", k);
+        if (bs.substep_count > 0) {
+            s->density_iters_max = std::max(s->density_iters_max, s->sc_host->density_iters);
+            s->pressure_iters_max = std::max(s->pressure_iters_max, s->sc_host->pressure_iters);
         }
-        launch_max_velocity(s->P, s->sc, s->st);
-        g_kernel_launches += 2;
-        CK(cudaMemcpyAsync(s->sc_host, s->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s->st));
-        bs.substep_time = 0.f;
-        bs.substep_count = 0;
-        bs.finished = false;
-        s->density_iters_max = s->pressure_iters_max = s->substeps = 0;
+        unsigned bits = s->sc_host->maxv2;
+        float v2;
+        memcpy(&v2, &bits, 4);
+        const float vel = std::sqrt(v2);
+        float maxSubstepSize = s->p.cflNumber / (vel + 1e-15f);
+        bool last = false;
+        if (bs.substep_time + maxSubstepSize >= s->frame_dt || bs.substep_count == (s->p.maxSubsteps - 1)) {
+            maxSubstepSize = s->frame_dt - bs.substep_time;
+            last = true;
+        } else if (bs.substep_time + 2.f * maxSubstepSize >= s->frame_dt) {
+            maxSubstepSize = 0.5f * (s->frame_dt - bs.substep_time);
+        }
+        s->step_dt = maxSubstepSize;
+        b->h_dt[bs.slot] = maxSubstepSize;
+        bs.substep_time += maxSubstepSize;
+        bs.substep_count++;
+        bs.last = last || bs.substep_count > 50;
+        act.push_back(k);
+    }
+    for (int k = 0; k < (int)b->solves.size(); k++)
+        if (!b->solves[k].done) extra.push_back(k);
+    if (act.empty() && extra.empty()) {
+        *busy = 0;
+        return FS_OK;
+    }
+    CK(cudaMemcpyAsync(b->d_dt, b->h_dt, (size_t)fs_batch::kSlots * sizeof(float), cudaMemcpyHostToDevice, b->bst));
+    CK(cudaEventRecord(b->ev_solve, b->bst));
+    for (int k : act) {
+        BatchScene &bs = b->sc[k];
+        CK(cudaStreamWaitEvent(bs.s->st, b->ev_solve, 0));
+        CK(cudaGraphLaunch(bs.g[bs.parity][0], bs.s->st));
+        CK(cudaEventRecord(bs.ev, bs.s->st));
+        g_kernel_launches += bs.launches[0];
+    }
+    if (!act.empty()) TRY(batch_solve(b, act, extra, 0));
+    for (int k : act) {
+        BatchScene &bs = b->sc[k];
+        CK(cudaStreamWaitEvent(bs.s->st, b->ev_solve, 0));
+        CK(cudaGraphLaunch(bs.g[bs.parity][1], bs.s->st));
+        CK(cudaEventRecord(bs.ev, bs.s->st));
+        g_kernel_launches += bs.launches[1];
+    }
+    TRY(batch_solve(b, act, extra, 1));
+    for (int k : act) {
+        BatchScene &bs = b->sc[k];
+        CK(cudaStreamWaitEvent(bs.s->st, b->ev_solve, 0));
+        CK(cudaGraphLaunch(bs.g[bs.parity][2], bs.s->st));
+        g_kernel_launches += bs.launches[2];
+        bs.parity ^= 1;
+        bs.s->substeps++;
     }
     CK(cudaDeviceSynchronize());
-    std::vector<int> act;
-    for (;;) {
-        // the CFL step of every handle still in its frame (fs_step_frame)
-        act.clear();
-        for (int k = 0; k < n; k++) {
-            BatchScene &bs = b->sc[k];
-            fs_solver *s = bs.s;
-            if (bs.finished) continue;
-            if (s->sc_host->pcg_status != 0) return fail(FS_ERR_TIMEOUT, "batch handle %d: solver status", k);
-            if (bs.substep_count > 0) {
-                s->density_iters_max = std::max(s->density_iters_max, s->sc_host->density_iters);
-                s->pressure_iters_max = std::max(s->pressure_iters_max, s->sc_host->pressure_iters);
-            }
-            unsigned bits = s->sc_host->maxv2;
-            float v2;
-            memcpy(&v2, &bits, 4);
-            const float vel = std::sqrt(v2);
-            float maxSubstepSize = s->p.cflNumber / (vel + 1e-15f);
-            bool last = false;
-            if (bs.substep_time + maxSubstepSize >= s->frame_dt || bs.substep_count == (s->p.maxSubsteps - 1)) {
-                maxSubstepSize = s->frame_dt - bs.substep_time;
-                last = true;
-            } else if (bs.substep_time + 2.f * maxSubstepSize >= s->frame_dt) {
-                maxSubstepSize = 0.5f * (s->frame_dt - bs.substep_time);
-            }
-            s->step_dt = maxSubstepSize;
-            b->h_dt[k] = maxSubstepSize;
-            bs.substep_time += maxSubstepSize;
-            bs.substep_count++;
-            if (last || bs.substep_count > 50) bs.finished = true;
-            act.push_back(k);
-        }
-        if (act.empty()) break;
-        CK(cudaMemcpyAsync(b->d_dt, b->h_dt, (size_t)n * sizeof(float), cudaMemcpyHostToDevice, b->bst));
-        CK(cudaEventRecord(b->ev_solve, b->bst));
-        for (int k : act) {
-            BatchScene &bs = b->sc[k];
-            CK(cudaStreamWaitEvent(bs.s->st, b->ev_solve, 0));
-            CK(cudaGraphLaunch(bs.g[bs.parity][0], bs.s->st));
-            CK(cudaEventRecord(bs.ev, bs.s->st));
-            g_kernel_launches += bs.launches[0];
-        }
-        TRY(batch_solve(b, act, 0));
-        for (int k : act) {
-            BatchScene &bs = b->sc[k];
-            CK(cudaStreamWaitEvent(bs.s->st, b->ev_solve, 0));
-            CK(cudaGraphLaunch(bs.g[bs.parity][1], bs.s->st));
-            CK(cudaEventRecord(bs.ev, bs.s->st));
-            g_kernel_launches += bs.launches[1];
-        }
-        TRY(batch_solve(b, act, 1));
-        for (int k : act) {
-            BatchScene &bs = b->sc[k];
-            CK(cudaStreamWaitEvent(bs.s->st, b->ev_solve, 0));
-            CK(cudaGraphLaunch(bs.g[bs.parity][2], bs.s->st));
-            g_kernel_launches += bs.launches[2];
-            bs.parity ^= 1;
-            bs.s->substeps++;
-        }
-        CK(cudaDeviceSynchronize());
+    for (int w = act.empty() ? 1 : 0; w < 2; w++) {
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, b->ev_t[2 * w], b->ev_t[2 * w + 1]));
+        b->solve_ms += ms;
     }
-    for (BatchScene &bs : b->sc) {
+    b->rounds++;
+    for (int k : extra) b->solves[k].done = true;
+    int still = 0;
+    for (int k : act) {
+        BatchScene &bs = b->sc[k];
+        if (!bs.last) {
+            still++;
+            continue;
+        }
+        // the frame ends (fs_step_frame after its loop)
         fs_solver *s = bs.s;
         s->density_iters_max = std::max(s->density_iters_max, s->sc_host->density_iters);
         s->pressure_iters_max = std::max(s->pressure_iters_max, s->sc_host->pressure_iters);
         s->P = bs.P[bs.parity];
         s->G = bs.G[bs.parity];
         s->frame++;
+        bs.in_frame = false;
     }
+    b->frame_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    *busy = still;
+    return FS_OK;
+}
+
+extern "C" fs_status fs_batch_round(fs_batch *b, int *busy)
+{
+    if (!b || !busy) return fail(FS_ERR_BAD_ARG, "null argument");
+    CK(cudaSetDevice(b->device));
+    return batch_round(b, busy);
+}
+
+extern "C" fs_status fs_batch_step_frame(fs_batch *b)
+{
+    if (!b) return fail(FS_ERR_BAD_ARG, "null batch");
+    CK(cudaSetDevice(b->device));
+    for (BatchScene &bs : b->sc)
+        if (bs.in_frame) return fail(FS_ERR_BAD_ARG, "fs_batch_step_frame: a member is inside a frame");
+    for (BatchScene &bs : b->sc) TRY(batch_begin(b, bs));
+    CK(cudaDeviceSynchronize());
+    for (int busy = 1; busy;) TRY(batch_round(b, &busy));
     return FS_OK;
 }
 

@@ -98,9 +98,19 @@ _SIGS = {
                                          ctypes.c_double, ctypes.c_double, ctypes.c_void_p,
                                          ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_device_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "fs_batch_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "fs_batch_add": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_batch_remove": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_batch_begin_frame": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_batch_round": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_batch_in_frame": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_batch_submit_solve": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_batch_solve_done": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_ulonglong, ctypes.c_void_p]),
+    "fs_batch_take_solve": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_ulonglong, ctypes.c_void_p]),
     "fs_batch_step_frame": (ctypes.c_int, [ctypes.c_void_p]),
     "fs_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "fs_batch_timer": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "fs_pcg_solve_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                           ctypes.c_void_p]),
     "fs_pcg_solve_device_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
@@ -217,6 +227,11 @@ class GpuFlipSolver:
         _check(self.lib.fs_max_particle_velocity(self.h, ctypes.byref(x)), "fs_max_particle_velocity")
         return float(x.value)
 
+    def device_bytes(self) -> int:
+        x = ctypes.c_size_t()
+        _check(self.lib.fs_device_bytes(self.h, ctypes.byref(x)), "fs_device_bytes")
+        return int(x.value)
+
     def stat(self, which: int) -> int:
         x = ctypes.c_int()
         _check(self.lib.fs_get_stat(self.h, which, ctypes.byref(x)), "fs_get_stat")
@@ -329,19 +344,76 @@ def pcg_solve(material: np.ndarray, rhs: np.ndarray, dt: float, density: float, 
 
 
 class Batch:
-    """fs_batch: GpuFlipSolver handles (FS_PCG_SPEC) stepped frame by frame
-    together; each handle's results equal those of stepping it alone."""
+    """fs_batch: GpuFlipSolver handles (FS_PCG_SPEC) stepped together; each
+    handle's results equal those of stepping it alone.  Members join and
+    leave between their frames; standalone systems can ride along."""
 
-    def __init__(self, solvers):
+    def __init__(self, solvers=()):
         self.lib = load()
         self.solvers = list(solvers)
-        arr = (ctypes.c_void_p * len(self.solvers))(*[g.h.value for g in self.solvers])
+        arr = (ctypes.c_void_p * max(len(self.solvers), 1))(*[g.h.value for g in self.solvers])
         h = ctypes.c_void_p()
         _check(self.lib.fs_batch_create(arr, len(self.solvers), ctypes.byref(h)), "fs_batch_create")
         self.h = h
+        self._solves = {}
 
     def step_frame(self):
         _check(self.lib.fs_batch_step_frame(self.h), "fs_batch_step_frame")
+
+    def add(self, g):
+        _check(self.lib.fs_batch_add(self.h, g.h), "fs_batch_add")
+        self.solvers.append(g)
+
+    def remove(self, g):
+        _check(self.lib.fs_batch_remove(self.h, g.h), "fs_batch_remove")
+        self.solvers.remove(g)
+
+    def begin_frame(self, g):
+        _check(self.lib.fs_batch_begin_frame(self.h, g.h), "fs_batch_begin_frame")
+
+    def in_frame(self, g) -> bool:
+        x = ctypes.c_int()
+        _check(self.lib.fs_batch_in_frame(self.h, g.h, ctypes.byref(x)), "fs_batch_in_frame")
+        return bool(x.value)
+
+    def round(self) -> int:
+        """One round; returns the members still inside a frame."""
+        x = ctypes.c_int()
+        _check(self.lib.fs_batch_round(self.h, ctypes.byref(x)), "fs_batch_round")
+        return int(x.value)
+
+    def submit_solve(self, material, rhs, dt, density, dx) -> int:
+        ni, nj = material.shape
+        m = np.ascontiguousarray(material, np.int8)
+        b = np.ascontiguousarray(rhs, np.float64).reshape(ni, nj)
+        sysd = PoissonSystem(ni, nj, m.ctypes.data, float(dt), float(density), float(dx),
+                             b.ctypes.data, None, 0, 0.0)
+        t = ctypes.c_ulonglong()
+        _check(self.lib.fs_batch_submit_solve(self.h, ctypes.byref(sysd), ctypes.byref(t)),
+               "fs_batch_submit_solve")
+        self._solves[int(t.value)] = (ni, nj)
+        return int(t.value)
+
+    def solve_done(self, ticket: int) -> bool:
+        x = ctypes.c_int()
+        _check(self.lib.fs_batch_solve_done(self.h, ctypes.c_ulonglong(ticket), ctypes.byref(x)),
+               "fs_batch_solve_done")
+        return bool(x.value)
+
+    def take_solve(self, ticket: int):
+        """(inner iterations, solution float64 [ni, nj], relative residual)."""
+        ni, nj = self._solves.pop(ticket)
+        x = np.zeros((ni, nj), np.float64)
+        sysd = PoissonSystem(ni, nj, None, 0.0, 0.0, 0.0, None, x.ctypes.data, 0, 0.0)
+        _check(self.lib.fs_batch_take_solve(self.h, ctypes.c_ulonglong(ticket), ctypes.byref(sysd)),
+               "fs_batch_take_solve")
+        return int(sysd.iterations), x, float(sysd.rel_residual)
+
+    def timer(self, which: int) -> float:
+        """0 merged-solve device ms, 1 round wall ms, 2 rounds; 3 resets."""
+        x = ctypes.c_double()
+        _check(self.lib.fs_batch_timer(self.h, int(which), ctypes.byref(x)), "fs_batch_timer")
+        return float(x.value)
 
     def close(self):
         if getattr(self, "h", None):

@@ -186,6 +186,9 @@ fs_status fs_grid_bytes(fs_solver *s, int which, size_t *bytes);
 fs_status fs_get_grid(fs_solver *s, int which, void *out, size_t bytes);
 fs_status fs_set_grid(fs_solver *s, int which, const void *in, size_t bytes);
 fs_status fs_get_stat(fs_solver *s, int which, int *out);
+/* Device memory the handle holds now, in bytes (no reference counterpart;
+ * for admission by footprint). */
+fs_status fs_device_bytes(fs_solver *s, size_t *bytes);
 
 /* Device timing of the last fs_step / fs_step_frame calls, accumulated since
  * fs_reset_timers: which = 0 whole substeps, 1 PCG kernels, 2 launches
@@ -233,24 +236,6 @@ fs_status fs_pcg_solve_spec(int ni, int nj, const int8_t *material, float dt, do
                             int max_iter, const fs_exec_params *exec, int *iterations,
                             double *rel_residual);
 
-/* A batch of solver handles stepped together; no reference counterpart as a
- * batch (each handle is a FlipSolver, flipsolver2d.h:183-432).
- * fs_batch_step_frame advances every handle by one frame exactly as
- * fs_step_frame would (FlipSolver::stepFrame's CFL loop,
- * flipsolver2d.cpp:464-500) and gives the same results bit for bit; the
- * handles' substeps are interleaved round by round, each substep runs as
- * captured CUDA graphs, and the density and pressure solves of all handles
- * in a round share one cluster launch per plan.  Every handle must use
- * FS_PCG_SPEC, sit on one device, have timers off and appear once.  The
- * graphs hold each handle's device buffers: between batch calls a handle
- * may be read (fs_get_*) or stepped on its own, but fs_set_particles /
- * fs_set_grid need a new batch.  After an error the handles' state is
- * undefined.  fs_batch_destroy leaves the handles alive. */
-typedef struct fs_batch fs_batch;
-fs_status fs_batch_create(fs_solver *const *solvers, int n, fs_batch **out);
-fs_status fs_batch_step_frame(fs_batch *batch);
-fs_status fs_batch_destroy(fs_batch *batch);
-
 /* One system of fs_pcg_solve_batch: the problem of fs_pcg_solve_spec
  * (host arrays; result and the two outputs are written). */
 typedef struct fs_poisson_system {
@@ -276,6 +261,51 @@ typedef struct fs_poisson_system {
  * returns its best result with its residual.  exec may be NULL. */
 fs_status fs_pcg_solve_batch(fs_poisson_system *systems, int n, double rel_tol, int max_iter,
                              const fs_exec_params *exec);
+
+/* A batch of solver handles stepped together; no reference counterpart as a
+ * batch (each handle is a FlipSolver, flipsolver2d.h:183-432).  Members
+ * advance by whole frames exactly as fs_step_frame would (FlipSolver::
+ * stepFrame's CFL loop, flipsolver2d.cpp:464-500) and give the same results
+ * bit for bit.  The members' substeps run in rounds: a round advances every
+ * member that is inside a frame by one substep, each substep as captured
+ * CUDA graphs, and the density and pressure solves of all of them -- plus
+ * any standalone systems submitted -- share one cluster launch per plan.
+ * Members must use FS_PCG_SPEC, sit on the batch's device and have timers
+ * off.  The graphs hold each member's device buffers; they are captured
+ * again when a frame starts on buffers that moved (first-frame seeding,
+ * fs_set_particles).  Between frames a member may be read or stepped on its
+ * own.  After an error the members' state is undefined.
+ *
+ * fs_batch_create   a batch of n members (n may be 0: the current device)
+ * fs_batch_add / fs_batch_remove   membership (not while inside a frame)
+ * fs_batch_begin_frame   start a frame of one member
+ * fs_batch_round    one round; *busy = members still inside a frame
+ * fs_batch_in_frame whether a member's frame is still running
+ * fs_batch_step_frame   one whole frame of every member
+ * fs_batch_submit_solve   copy a standalone system (fs_pcg_solve_spec's
+ *                   problem, host arrays; on-chip size limit as
+ *                   fs_pcg_solve_batch) to the device; the next round solves it
+ * fs_batch_solve_done / fs_batch_take_solve   its completion; take copies
+ *                   result, iterations and rel_residual out and frees it
+ * fs_batch_destroy  frees the batch; the members stay alive */
+typedef struct fs_batch fs_batch;
+fs_status fs_batch_create(fs_solver *const *solvers, int n, fs_batch **out);
+fs_status fs_batch_add(fs_batch *batch, fs_solver *solver);
+fs_status fs_batch_remove(fs_batch *batch, fs_solver *solver);
+fs_status fs_batch_begin_frame(fs_batch *batch, fs_solver *solver);
+fs_status fs_batch_round(fs_batch *batch, int *busy);
+fs_status fs_batch_in_frame(fs_batch *batch, fs_solver *solver, int *in_frame);
+fs_status fs_batch_step_frame(fs_batch *batch);
+fs_status fs_batch_submit_solve(fs_batch *batch, const fs_poisson_system *system,
+                                unsigned long long *ticket);
+fs_status fs_batch_solve_done(fs_batch *batch, unsigned long long ticket, int *done);
+fs_status fs_batch_take_solve(fs_batch *batch, unsigned long long ticket, fs_poisson_system *system);
+fs_status fs_batch_destroy(fs_batch *batch);
+/* Batch timing since creation or the last reset: which = 0 device time of
+ * the merged solves (ms, CUDA events on the batch's solve stream), 1 host
+ * wall time of the rounds (ms), 2 rounds run; 3 resets all three (and
+ * writes 0). */
+fs_status fs_batch_timer(fs_batch *batch, int which, double *value);
 
 /* fs_pcg_solve_device without any device allocation.  This entry point has
  * no counterpart in the reference.  It is for callers that cannot allocate
