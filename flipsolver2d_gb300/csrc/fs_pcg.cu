@@ -379,22 +379,26 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgArgs<T> a)
         if (threadIdx.x == 0) pB[blockIdx.x] = part;
         if (!grid_barrier(a.bar, G, a.status)) return;
 
-        // VOps::maxAbs with the reference's chunking (vmath.cpp:100-136)
-        if (threadIdx.x < 32) {
+        // VOps::maxAbs with the reference's chunking (vmath.cpp:100-136):
+        // one warp per chunk, the max over warps (order-independent)
+        {
+            const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
             double m = 0.0;
-            for (int k = threadIdx.x; k < a.nchunks; k += 32) {
+            for (int k = warp; k < a.nchunks; k += nw) {
                 const long long start = k == 0 ? 0 : a.chunk_end[k - 1];
-                long long idx = a.chunk_last_unit[k];
-                while (idx >= start && rn[idx] == (T)0) idx--;
+                const long long last = a.chunk_last_unit[k];
+                const long long idx =
+                    last < 0 ? -1 : warp_last_nonzero(start, last, [&](long long e) { return rn[e]; });
                 const double v = idx >= start ? fabs((double)rn[idx]) : DBL_MIN;
                 if (v > m) m = v;
             }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const double t = __shfl_down_sync(0xffffffffu, m, o);
-                if (t > m) m = t;
+            if (lane == 0) sm[warp] = m;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                for (int w = 1; w < nw; w++)
+                    if (sm[w] > m) m = sm[w];
+                bcast[0] = m;
             }
-            if (threadIdx.x == 0) bcast[0] = m;
         }
         __syncthreads();
         const double err = bcast[0];
@@ -746,9 +750,11 @@ __global__ void __launch_bounds__(kTiledThreads) k_pcg_tiled(PcgArgs<float> a, T
             if (threadIdx.x == 0) pB[blockIdx.x] = part;
         }
         if (!grid_sync_fast(a.bar, G, a.status)) return;
-        if (threadIdx.x < 32) {
+        {
+            // one warp per chunk, the max over warps (order-independent)
+            const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
             double m = 0.0;
-            for (int k = threadIdx.x; k < a.nchunks; k += 32) {
+            for (int k = warp; k < a.nchunks; k += nw) {
                 const long long start = k == 0 ? 0 : a.chunk_end[k - 1];
                 const int last = a.chunk_last_unit[k];
                 double v;
@@ -757,19 +763,20 @@ __global__ void __launch_bounds__(kTiledThreads) k_pcg_tiled(PcgArgs<float> a, T
                 } else {
                     v = ((volatile double *)chunk_val)[k];
                     if (v < 0.0) {
-                        long long idx = last - 1;
-                        while (idx >= start && ((volatile float *)rn)[idx] == 0.f) idx--;
+                        const long long idx = warp_last_nonzero(
+                            start, (long long)last - 1, [&](long long e) { return ((volatile float *)rn)[e]; });
                         v = idx >= start ? fabs((double)((volatile float *)rn)[idx]) : DBL_MIN;
                     }
                 }
                 if (v > m) m = v;
             }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const double t = __shfl_down_sync(0xffffffffu, m, o);
-                if (t > m) m = t;
+            if (lane == 0) sm[warp] = m;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                for (int w = 1; w < nw; w++)
+                    if (sm[w] > m) m = sm[w];
+                s_err = m;
             }
-            if (threadIdx.x == 0) s_err = m;
         }
         __syncthreads();
         const double err = s_err;

@@ -45,4 +45,32 @@ template <typename T> int pcg_grid_size(long long N);
 template <typename T> cudaError_t launch_pcg(const PcgArgs<T> &a, cudaStream_t st, int *launched);
 cudaError_t launch_pcg_linear_if_wrap(const PcgArgs<float> &a, cudaStream_t st);
 
+
+// The index of the last nonzero entry in [lo, hi], or lo - 1 if there is
+// none: the backward search of VOps::maxAbs (vmath.cpp:100-136) for a chunk
+// whose last unit row holds a zero.  Warp-cooperative: all 32 lanes of a
+// warp call it with the same arguments and get the same result; each step
+// reads 256 entries with eight loads in flight per lane.  (A residual that
+// is still zero over most of the grid -- a scene at rest -- otherwise means
+// a serial walk over tens of thousands of entries per chunk per iteration.)
+template <typename Load>
+__device__ __forceinline__ long long warp_last_nonzero(long long lo, long long hi, Load load)
+{
+    const int lane = threadIdx.x & 31;
+    for (; hi >= lo; hi -= 256) {
+        bool nz[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const long long e = hi - (j * 32 + lane);
+            nz[j] = e >= lo && load(e) != 0;
+        }
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const unsigned b = __ballot_sync(0xffffffffu, nz[j]);
+            if (b) return hi - (j * 32 + (__ffs((int)b) - 1));
+        }
+    }
+    return lo - 1;
+}
+
 } // namespace fsg

@@ -252,34 +252,44 @@ __device__ __forceinline__ bool gsync(GridBarrier *gb, unsigned nblocks, int *st
 __device__ __forceinline__ bool chunk_converged(const PcgArgs<float> &a, const float *rn,
                                                 const TolTest &tt, int *s_flag)
 {
-    if (threadIdx.x < 32) {
-        const float *cv = reinterpret_cast<const float *>(a.chunk_val);
-        float mx = 0.f;
-        int has_min = 0;
-        for (int k = threadIdx.x; k < a.nchunks; k += 32) {
-            const long long start = k == 0 ? 0 : a.chunk_end[k - 1];
-            const int last = a.chunk_last_unit[k];
-            if (last < 0) {
-                has_min = 1;
-                continue;
-            }
-            float v = __ldcg(cv + k);
-            if (v < 0.f) {
-                long long idx = last - 1;
-                while (idx >= start && __ldcg(rn + idx) == 0.f) idx--;
-                if (idx >= start) {
-                    v = fabsf(__ldcg(rn + idx));
-                } else {
-                    has_min = 1;
-                    v = 0.f;
-                }
-            }
-            mx = fmaxf(mx, v);
+    __shared__ float s_mx[32];
+    __shared__ int s_min[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const float *cv = reinterpret_cast<const float *>(a.chunk_val);
+    // one warp per chunk; the max is order-independent
+    float mx = 0.f;
+    int has_min = 0;
+    for (int k = warp; k < a.nchunks; k += nw) {
+        const long long start = k == 0 ? 0 : a.chunk_end[k - 1];
+        const int last = a.chunk_last_unit[k];
+        if (last < 0) {
+            has_min = 1;
+            continue;
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
-        has_min = __any_sync(0xffffffffu, has_min);
-        if (threadIdx.x == 0) *s_flag = tol_met(tt, mx, has_min) ? 1 : 0;
+        float v = __ldcg(cv + k);
+        if (v < 0.f) {
+            const long long idx = warp_last_nonzero(start, (long long)last - 1,
+                                                    [&](long long e) { return __ldcg(rn + e); });
+            if (idx >= start) {
+                v = fabsf(__ldcg(rn + idx));
+            } else {
+                has_min = 1;
+                v = 0.f;
+            }
+        }
+        mx = fmaxf(mx, v);
+    }
+    if (lane == 0) {
+        s_mx[warp] = mx;
+        s_min[warp] = has_min;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < nw; w++) {
+            mx = fmaxf(mx, s_mx[w]);
+            has_min |= s_min[w];
+        }
+        *s_flag = tol_met(tt, mx, has_min) ? 1 : 0;
     }
     __syncthreads();
     const int f = *s_flag;
