@@ -2211,7 +2211,7 @@ extern "C" fs_status fs_pcg_solve_spec(int ni, int nj, const int8_t *material, f
     TRY(dalloc_tmp((void **)&b, N * 8));
     TRY(dalloc_tmp((void **)&x, N * 8));
     TRY(dalloc_tmp((void **)&part, rblocks * 8));
-    float **fv[] = {&r, &d, &s, &q, &y, &z};
+    float **fv[] = {&r, &d, &s, &q, &z};
     for (float **v : fv) TRY(dalloc_tmp((void **)v, N * 4));
     TRY(dalloc_tmp((void **)&partials, (size_t)spec_partials_needed() * sizeof(float2)));
     TRY(dalloc_tmp((void **)&chunk_last, 2 * sizeof(int)));
@@ -2262,13 +2262,15 @@ extern "C" fs_status fs_pcg_solve_spec(int ni, int nj, const int8_t *material, f
         a.d = d;
         a.s = s;
         a.q = q;
-        a.y = y;
+        a.y = nullptr; // z = K K^T r is formed in one pass
         a.z = z;
         a.partials = partials;
         a.count = count;
         a.status = &sc->pcg_status;
         a.iters = iters_dev;
-        a.eps_in = 1e-4f;
+        // the inner solve only needs to bring the residual just below the
+        // target (never below what FP32 iterations reach)
+        a.eps_in = (float)std::min(std::max(0.3 * rel_tol * bnorm / rnorm, 1e-4), 0.5);
         a.max_iter = max_iter - total_inner;
         TRY(check(launch_spec_pcg(a, st), "inner PCG"));
         TRY(check(launch_spec_update(x, d, N, st), "update"));

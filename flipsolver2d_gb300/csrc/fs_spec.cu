@@ -21,8 +21,9 @@
 // for a unit n.
 //
 // The inner PCG is one cooperative kernel over the linear index with FP32
-// vectors and float-pair reductions.  It forms q = A s as A z + beta q (the
-// same vector, one fewer grid barrier), so an iteration takes four barriers.
+// vectors and float-pair reductions.  It forms q = A s as A z + beta q and
+// z = K K^T r in one pass (each saves a grid barrier), so an iteration takes
+// three barriers.
 #include <cfloat>
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -200,7 +201,10 @@ __device__ __forceinline__ float2 spec_psum(const float2 *p, int G, float2 *bc, 
     return bc[which];
 }
 
-__global__ void __launch_bounds__(kSpecThreads) k_pcg_spec(SpecArgs a)
+// two blocks per SM (64 registers a thread) and four cells in flight per
+// thread in every sweep: the sweeps stream vectors through L2 and HBM and are
+// bound by how many loads are outstanding
+__global__ void __launch_bounds__(kSpecThreads, 2) k_pcg_spec(SpecArgs a)
 {
     __shared__ float2 sm[64];
     __shared__ float2 bc[4];
@@ -212,7 +216,7 @@ __global__ void __launch_bounds__(kSpecThreads) k_pcg_spec(SpecArgs a)
     const float scale = (float)a.scale;
     const uint8_t *__restrict__ info = a.info;
     float *__restrict__ r = a.r, *__restrict__ s = a.s, *__restrict__ q = a.q;
-    float *__restrict__ y = a.y, *__restrict__ z = a.z, *__restrict__ d = a.d;
+    float *__restrict__ z = a.z, *__restrict__ d = a.d;
     float2 *pA = a.partials, *pB = a.partials + G, *pC = a.partials + 2 * G;
     SpecGrid g{a.count, a.status, 0u};
 
@@ -224,31 +228,41 @@ __global__ void __launch_bounds__(kSpecThreads) k_pcg_spec(SpecArgs a)
         if (n + 1 < N && (info[n + 1] & 0x84) == 0x84) v = fmaf(k, r[n + 1], v);
         return v;
     };
-    // z = K y
-    auto kk = [&](long long c) {
+    // z = K K^T r in one pass: K^T r at c and at its upper and left
+    // neighbours, combined in the order of z = K y (y = K^T r is not stored,
+    // which saves a sweep and a grid barrier per iteration)
+    auto kkt = [&](long long c) {
         const uint8_t p = info[c];
-        float v = y[c];
+        float v = kt(c);
         if (p & 0x80) {
-            if ((p & 1) && c - NJ >= 0) v = fmaf(spec_k(info[c - NJ], scale), y[c - NJ], v);
-            if ((p & 4) && c - 1 >= 0) v = fmaf(spec_k(info[c - 1], scale), y[c - 1], v);
+            if ((p & 1) && c - NJ >= 0) v = fmaf(spec_k(info[c - NJ], scale), kt(c - NJ), v);
+            if ((p & 4) && c - 1 >= 0) v = fmaf(spec_k(info[c - 1], scale), kt(c - 1), v);
         }
         return v;
     };
 
+    // f(c) for this thread's cells, four at a time (independent iterations
+    // the compiler interleaves)
+    auto sweep = [&](auto &&f) {
+        for (long long cb = c0; cb < N; cb += 4 * stride) {
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const long long c = cb + u * stride;
+                if (c < N) f(c);
+            }
+        }
+    };
+
     // r_0 = the outer residual (already in r), d = 0, z = M r, s = z
-    for (long long c = c0; c < N; c += stride) {
-        d[c] = 0.f;
-        y[c] = kt(c);
-    }
-    if (!spec_sync(g)) return;
     float rz = 0.f, rr = 0.f;
-    for (long long c = c0; c < N; c += stride) {
-        const float zc = kk(c);
+    sweep([&](long long c) {
+        const float zc = kkt(c);
+        d[c] = 0.f;
         z[c] = zc;
         s[c] = zc;
         rz = fmaf(r[c], zc, rz);
         rr = fmaf(r[c], r[c], rr);
-    }
+    });
     {
         float2 b0, b1;
         spec_bsum2(rz, rr, sm, b0, b1);
@@ -267,14 +281,14 @@ __global__ void __launch_bounds__(kSpecThreads) k_pcg_spec(SpecArgs a)
     while (rr0.x > 0.f && it < a.max_iter) {
         // s = z + beta s, q = A s = A z + beta q, and s.q
         float sq = 0.f;
-        for (long long c = c0; c < N; c += stride) {
+        sweep([&](long long c) {
             const float az = spec_a<float>(info, z, c, N, NJ, scale);
             const float sc = first ? z[c] : fmaf(fb, s[c], z[c]);
             const float qc = first ? az : fmaf(fb, q[c], az);
             s[c] = sc;
             q[c] = qc;
             sq = fmaf(sc, qc, sq);
-        }
+        });
         {
             float2 b0, b1;
             spec_bsum2(sq, 0.f, sm, b0, b1);
@@ -282,21 +296,19 @@ __global__ void __launch_bounds__(kSpecThreads) k_pcg_spec(SpecArgs a)
         }
         if (!spec_sync(g)) return;
         const float fa = spec_ff_div(sigma, spec_psum(pC, G, bc, 2));
-        for (long long c = c0; c < N; c += stride) {
+        sweep([&](long long c) {
             d[c] = fmaf(fa, s[c], d[c]);
             r[c] = fmaf(-fa, q[c], r[c]);
-        }
-        if (!spec_sync(g)) return;
-        for (long long c = c0; c < N; c += stride) y[c] = kt(c);
+        });
         if (!spec_sync(g)) return;
         rz = 0.f;
         rr = 0.f;
-        for (long long c = c0; c < N; c += stride) {
-            const float zc = kk(c);
+        sweep([&](long long c) {
+            const float zc = kkt(c);
             z[c] = zc;
             rz = fmaf(r[c], zc, rz);
             rr = fmaf(r[c], r[c], rr);
-        }
+        });
         {
             float2 b0, b1;
             spec_bsum2(rz, rr, sm, b0, b1);

@@ -13,7 +13,7 @@ struct SpecArgs {
     double scale;        // dt / (density dx^2)
     float *r;            // in: outer residual (FP32); out: inner residual
     float *d;            // out: correction
-    float *s, *q, *y, *z;
+    float *s, *q, *y, *z; // y unused: the kernel forms K K^T r in one pass
     float2 *partials;    // 3 * grid + 8
     unsigned *count;     // grid barrier counter
     int *status;         // 1 when a barrier wait gave up
