@@ -18,7 +18,10 @@ solver's stream, L2 flushed by a 256 MiB write between steps, outside the
 events); `e2e` goes through the C ABI with host-resident state uploaded and
 downloaded every step; `roofline` is for the PCG kernel, which dominates the
 substep; `cpu_baseline` is the CPU oracle on this host's cores on a bounded
-sample of the same workload.  With --impl reference only the CPU
+sample of the same workload.  `batch` (unless --no-batch) is the batched form
+of the path beside it: 64 scenes of the batched-scenes workload stepped
+together at a 1e-6 pressure residual, and the same scenes one at a time.
+With --impl reference only the CPU
 implementation is timed (the reference's sources are not present on GPU
 hosts, so its plain-C restatement, pinned bit for bit to it, stands in).
 """
@@ -340,9 +343,24 @@ def gpu_arm(args):
         "cpu_baseline": cpu,
         "clocks": clocks,
     }
+    s.close()
+    if rank == 0 and world == 1 and not args.no_batch:
+        # the batched form of the same path beside the single-scene line: 64
+        # scenes of the batched-scenes workload stepped together, and 16 of
+        # them one at a time, both at a 1e-6 pressure residual
+        try:
+            r = batch_measure(64, 2, 3, 16)
+            bv = r["work"] / (r["total_ms"] / 1e3)
+            line["batch"] = {"workload": "batch_64_scenes (sides 64-512, seeds 1000..1063)",
+                             "value": bv, "unit": METRIC, "frames": 3,
+                             "ms_per_frame": r["total_ms"] / 3,
+                             "single_scene": r["single"], "vs_single_scene": bv / r["single"],
+                             "merged_solve_share": r["solve_ms"] / max(r["rounds_ms"], 1e-9),
+                             "pcg": "FS_PCG_SPEC, 1e-6 true relative residual"}
+        except Exception as e:  # reported, never fatal for the main line
+            line["batch"] = {"error": str(e)}
     if rank == 0:
         print(json.dumps(line))
-    s.close()
     if dist:
         dist.destroy_process_group()
     return 0
@@ -400,6 +418,56 @@ def batch_scenes(n: int):
     return out
 
 
+def batch_measure(n: int, warm: int, frames: int, single_sample: int):
+    """Steps `n` scenes of the batched workload together: `warm` untimed
+    frames, then `frames` timed ones run pipelined (fs_batch_run_frames: a
+    scene whose frame ends starts its next one in the next round; host wall
+    clock around the blocking call), then `single_sample` of the same scenes
+    one at a time through fs_step_frame.  The work is the particles each
+    scene holds when the timed frames start times the substeps it runs.
+    Returns a dict of the figures."""
+    import torch
+    from flipsolver2d_gb300 import gpu
+
+    scs = batch_scenes(n)
+    hs = [gpu.GpuFlipSolver(sc, precision=gpu.FS_PCG_SPEC) for sc in scs]
+    b = gpu.Batch(hs)
+    b.run_frames(warm)
+    hs[0].reset_timers()
+    b.timer(3)
+    counts = [g.particle_count() for g in hs]
+    sub0 = [g.stat(5) for g in hs]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.run_frames(frames)  # returns after the device finished
+    total_ms = 1e3 * (time.perf_counter() - t0)
+    subs = [g.stat(5) - a for g, a in zip(hs, sub0)]
+    rounds = b.timer(2)
+    out = {"work": sum(c * k for c, k in zip(counts, subs)), "total_ms": total_ms,
+           "cells": sum(g.ni * g.nj * k for g, k in zip(hs, subs)),
+           # per round the dt table (4 B per scene) and the systems of the two
+           # merged solves (72 B each) go up, the scalars (32 B each) come down
+           "h2d": 4 * len(hs) * rounds + 2 * 72 * sum(subs), "d2h": 32 * sum(subs),
+           "launches": hs[0].timer(2), "solve_ms": b.timer(0), "rounds_ms": b.timer(1),
+           "rounds": rounds, "total_cells": int(sum(g.ni * g.nj for g in hs)),
+           "particles": int(sum(counts))}
+    b.close()
+    m = min(len(hs), single_sample)
+    single_work, single_s = 0, 0.0
+    for g in hs[:m]:
+        k = g.particle_count()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g.step_frame()
+        single_s += time.perf_counter() - t0
+        single_work += k * g.stat(2)
+    out["single"] = single_work / single_s if single_s > 0 else None
+    out["single_scenes"] = m
+    for g in hs:
+        g.close()
+    return out
+
+
 def batch_arm(args):
     """Batched scenes (--batch N): N independent scenes in FS_PCG_SPEC mode
     (every density and pressure solve to a 1e-6 true relative residual)
@@ -408,83 +476,46 @@ def batch_arm(args):
     The same scenes stepped one at a time through fs_step_frame (same mode,
     same residual) give the single-scene figure beside it."""
     import torch
-    from flipsolver2d_gb300 import build, gpu
+    from flipsolver2d_gb300 import build
 
     build.build()
     torch.cuda.set_device(0)
-    scs = batch_scenes(args.batch)
-    hs = [gpu.GpuFlipSolver(sc, precision=gpu.FS_PCG_SPEC) for sc in scs]
-    b = gpu.Batch(hs)
-    for _ in range(args.warmup):
-        b.step_frame()
-    hs[0].reset_timers()
-    b.timer(3)
     sampler = ClockSampler(0)
     sampler.start()
-    torch.cuda.synchronize()
-    work, frame_ms, cells, h2d, d2h = 0, [], 0, 0, 0
-    for _ in range(args.steps):
-        counts = [g.particle_count() for g in hs]
-        t0 = time.perf_counter()
-        b.step_frame()  # returns after the device finished the frame
-        frame_ms.append(1e3 * (time.perf_counter() - t0))
-        subs = [g.stat(2) for g in hs]
-        work += sum(c * n for c, n in zip(counts, subs))
-        cells += sum(g.ni * g.nj * n for g, n in zip(hs, subs))
-        # per round: the dt table and the systems of the two merged solves
-        # up (4 B per scene, 72 B per system), the scalars down (32 B each)
-        h2d += 4 * len(hs) * max(subs) + 2 * 72 * sum(subs)
-        d2h += 32 * sum(subs)
+    r = batch_measure(args.batch, args.warmup, args.steps, args.single_sample)
     clocks = sampler.stop()
-    launches = hs[0].timer(2)
-    solve_ms, rounds_ms, rounds = b.timer(0), b.timer(1), b.timer(2)
-    total_s = sum(frame_ms) / 1e3
-    value = work / total_s
-    b.close()
-    # the same scenes one at a time (a bounded sample of them)
-    m = min(len(hs), args.single_sample)
-    single_work, single_s = 0, 0.0
-    for g in hs[:m]:
-        n = g.particle_count()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        g.step_frame()
-        single_s += time.perf_counter() - t0
-        single_work += n * g.stat(2)
-    single = single_work / single_s if single_s > 0 else None
+    total_s = r["total_ms"] / 1e3
+    value = r["work"] / total_s
+    single = r["single"]
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": sum(frame_ms) / args.steps, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": r["total_ms"] / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded random scenes)",
         "config": {"workload": f"batch_{args.batch}_scenes", "sides": list(BATCH_SIDES),
-                   "scene_seeds": f"1000..{1000 + args.batch - 1}",
-                   "cells": int(sum(g.ni * g.nj for g in hs)),
-                   "particles": int(sum(g.particle_count() for g in hs)),
+                   "scene_seeds": f"1000..{1000 + args.batch - 1}", "cells": r["total_cells"],
+                   "particles": r["particles"],
                    "pcg": "FS_PCG_SPEC: FP32 PCG, textbook IPP, FP64 refinement to 1e-6, "
                           "one thread-block cluster per system",
-                   "l2": "working set of all scenes far above L2", "step": "one frame of every scene",
+                   "l2": "working set of all scenes far above L2",
+                   "step": "one frame of every scene, the frames run pipelined (fs_batch_run_frames)",
                    "parallelism": "single GPU"},
-        "step_latency_ms": {"p50": float(np.percentile(frame_ms, 50)),
-                            "p99": float(np.percentile(frame_ms, 99))},
-        "cell_substeps_per_s": cells / total_s,
-        "merged_solves": {"device_ms_per_step": solve_ms / args.steps,
-                          "rounds_ms_per_step": rounds_ms / args.steps,
-                          "rounds_per_step": rounds / args.steps},
-        "single_scene": {"value": single, "unit": METRIC, "scenes": m,
+        "cell_substeps_per_s": r["cells"] / total_s,
+        "merged_solves": {"device_ms_per_step": r["solve_ms"] / args.steps,
+                          "rounds_ms_per_step": r["rounds_ms"] / args.steps,
+                          "rounds_per_step": r["rounds"] / args.steps},
+        "single_scene": {"value": single, "unit": METRIC, "scenes": r["single_scenes"],
                          "path": "fs_step_frame per scene, FS_PCG_SPEC, one scene at a time"},
         "vs_single_scene": (value / single) if single else None,
-        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": int(h2d / args.steps),
-                "d2h_bytes_per_step": int(d2h / args.steps),
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": int(r["h2d"] / args.steps),
+                "d2h_bytes_per_step": int(r["d2h"] / args.steps),
                 "path": "value itself is host-timed around the public call fs_batch_step_frame on "
                         "resident scenes; per round the dt table and solve lists go up and the "
                         "scalars come down"},
-        "gpu_launches": int(launches),
+        "gpu_launches": int(r["launches"]),
         "clocks": clocks,
     }
     print(json.dumps(line))
-    for g in hs:
-        g.close()
     return 0
 
 
@@ -626,6 +657,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="skip the batched-scenes figure of the default line")
     ap.add_argument("--res", type=int, default=RES, help="grid side of the dam break (default 1024)")
     ap.add_argument("--poisson", type=int, default=0,
                     help="time standalone spec-mode pressure solves on an N x N grid instead")

@@ -194,6 +194,7 @@ struct fs_solver {
     bool initialized = false;
     bool after_advect = false;
     int density_iters_max = 0, pressure_iters_max = 0, substeps = 0;
+    long long substeps_total = 0; // every substep since creation
     bool timers = false;
     double t_step_ms = 0.0, t_pcg_ms = 0.0, launches = 0.0;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -989,6 +990,7 @@ extern "C" fs_status fs_step(fs_solver *s)
     CK(cudaMemsetAsync(&s->sc->density_iters, 0, 2 * sizeof(int), s->st));
     s->substeps = 0;
     TRY(step_impl(s));
+    s->substeps_total++;
     TRY(read_scalars(s));
     s->density_iters_max = s->sc_host->density_iters;
     s->pressure_iters_max = s->sc_host->pressure_iters;
@@ -1022,6 +1024,7 @@ extern "C" fs_status fs_step_frame(fs_solver *s)
         CK(cudaMemsetAsync(&s->sc->density_iters, 0, 2 * sizeof(int), s->st));
         TRY(step_impl(s));
         s->substeps++;
+        s->substeps_total++;
         substepTime += maxSubstepSize;
         substepCount++;
         if (substepCount > 50) break;
@@ -1268,6 +1271,7 @@ extern "C" fs_status fs_get_stat(fs_solver *s, int which, int *out)
     case FS_STAT_SUBSTEPS: *out = s->substeps; return FS_OK;
     case FS_STAT_FRAME: *out = s->frame; return FS_OK;
     case FS_STAT_POOL_THREADS: *out = s->ex.pool_threads; return FS_OK;
+    case FS_STAT_SUBSTEPS_TOTAL: *out = (int)s->substeps_total; return FS_OK;
     default: return fail(FS_ERR_BAD_ARG, "bad stat id");
     }
 }
@@ -1914,6 +1918,7 @@ static fs_status batch_round(fs_batch *b, int *busy)
         g_kernel_launches += bs.launches[2];
         bs.parity ^= 1;
         bs.s->substeps++;
+        bs.s->substeps_total++;
     }
     CK(cudaDeviceSynchronize());
     for (int w = act.empty() ? 1 : 0; w < 2; w++) {
@@ -1949,6 +1954,36 @@ extern "C" fs_status fs_batch_round(fs_batch *b, int *busy)
     if (!b || !busy) return fail(FS_ERR_BAD_ARG, "null argument");
     CK(cudaSetDevice(b->device));
     return batch_round(b, busy);
+}
+
+extern "C" fs_status fs_batch_run_frames(fs_batch *b, int frames)
+{
+    if (!b || frames < 0) return fail(FS_ERR_BAD_ARG, "fs_batch_run_frames: invalid argument");
+    CK(cudaSetDevice(b->device));
+    for (BatchScene &bs : b->sc)
+        if (bs.in_frame) return fail(FS_ERR_BAD_ARG, "fs_batch_run_frames: a member is inside a frame");
+    if (frames == 0) return FS_OK;
+    std::vector<int> left(b->sc.size(), frames);
+    for (size_t k = 0; k < b->sc.size(); k++) {
+        TRY(batch_begin(b, b->sc[k]));
+        left[k]--;
+    }
+    CK(cudaDeviceSynchronize());
+    for (;;) {
+        int busy = 0;
+        TRY(batch_round(b, &busy));
+        // a member whose frame ended starts its next one in the next round
+        bool began = false;
+        for (size_t k = 0; k < b->sc.size(); k++)
+            if (!b->sc[k].in_frame && left[k] > 0) {
+                TRY(batch_begin(b, b->sc[k]));
+                left[k]--;
+                began = true;
+            }
+        if (began) CK(cudaDeviceSynchronize());
+        if (!began && busy == 0) break;
+    }
+    return FS_OK;
 }
 
 extern "C" fs_status fs_batch_step_frame(fs_batch *b)

@@ -104,6 +104,7 @@ _SIGS = {
     "fs_batch_remove": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "fs_batch_begin_frame": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "fs_batch_round": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_batch_run_frames": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "fs_batch_in_frame": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "fs_batch_submit_solve": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "fs_batch_solve_done": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_ulonglong, ctypes.c_void_p]),
@@ -359,6 +360,10 @@ class Batch:
 
     def step_frame(self):
         _check(self.lib.fs_batch_step_frame(self.h), "fs_batch_step_frame")
+
+    def run_frames(self, frames: int):
+        """`frames` frames of every member, pipelined across members."""
+        _check(self.lib.fs_batch_run_frames(self.h, int(frames)), "fs_batch_run_frames")
 
     def add(self, g):
         _check(self.lib.fs_batch_add(self.h, g.h), "fs_batch_add")

@@ -138,7 +138,8 @@ enum {
     FS_STAT_PRESSURE_ITERS = 1, /* SolverStats::pressureIterations() */
     FS_STAT_SUBSTEPS = 2,       /* SolverStats::substepCount()       */
     FS_STAT_FRAME = 3,          /* FlipSolver::frameNumber()         */
-    FS_STAT_POOL_THREADS = 4    /* chunk count of the residual test  */
+    FS_STAT_POOL_THREADS = 4,   /* chunk count of the residual test  */
+    FS_STAT_SUBSTEPS_TOTAL = 5  /* substeps since fs_create (no reference counterpart) */
 };
 
 typedef struct fs_solver fs_solver;
@@ -282,6 +283,7 @@ fs_status fs_pcg_solve_batch(fs_poisson_system *systems, int n, double rel_tol, 
  * fs_batch_round    one round; *busy = members still inside a frame
  * fs_batch_in_frame whether a member's frame is still running
  * fs_batch_step_frame   one whole frame of every member
+ * fs_batch_run_frames   several frames of every member, pipelined
  * fs_batch_submit_solve   copy a standalone system (fs_pcg_solve_spec's
  *                   problem, host arrays; on-chip size limit as
  *                   fs_pcg_solve_batch) to the device; the next round solves it
@@ -296,6 +298,10 @@ fs_status fs_batch_begin_frame(fs_batch *batch, fs_solver *solver);
 fs_status fs_batch_round(fs_batch *batch, int *busy);
 fs_status fs_batch_in_frame(fs_batch *batch, fs_solver *solver, int *in_frame);
 fs_status fs_batch_step_frame(fs_batch *batch);
+/* `frames` whole frames of every member, pipelined: a member whose frame ends
+ * starts its next one in the next round instead of waiting for the others
+ * (each member's results are those of `frames` calls of fs_step_frame). */
+fs_status fs_batch_run_frames(fs_batch *batch, int frames);
 fs_status fs_batch_submit_solve(fs_batch *batch, const fs_poisson_system *system,
                                 unsigned long long *ticket);
 fs_status fs_batch_solve_done(fs_batch *batch, unsigned long long ticket, int *done);

@@ -49,6 +49,27 @@ def test_batch_equals_alone(gpu_lib):
     b.close()
 
 
+def test_batch_run_frames_pipelined_equals_alone(gpu_lib):
+    """Pipelined frames (a member starts its next frame while others are
+    still in theirs) change nothing for any member."""
+    alone = []
+    for sc in _scenes()[:3]:
+        g = gpu.GpuFlipSolver(sc, precision=gpu.FS_PCG_SPEC)
+        for _ in range(3):
+            g.step_frame()
+        alone.append((_state(g), g.stat(5)))
+        g.close()
+    hs = [gpu.GpuFlipSolver(sc, precision=gpu.FS_PCG_SPEC) for sc in _scenes()[:3]]
+    b = gpu.Batch(hs)
+    b.run_frames(3)
+    for k, g in enumerate(hs):
+        got = _state(g)
+        for a, c in zip(alone[k][0][:5], got[:5]):
+            assert a.shape == c.shape and np.array_equal(a.view(np.uint8), c.view(np.uint8)), k
+        assert g.stat(3) == 3 and g.stat(5) == alone[k][1]
+    b.close()
+
+
 def test_spec_solves_in_step(gpu_lib):
     """Run one substep stage by stage and check both solves against the
     operator assembled at its start (DECOMPOSITION precedes P2G)."""
