@@ -430,6 +430,13 @@ def batch_measure(n: int, warm: int, frames: int, single_sample: int):
     from flipsolver2d_gb300 import gpu
 
     scs = batch_scenes(n)
+    # the autotuner picks each grid shape's cluster size for throughput
+    # before any handle exists, so every handle of a shape shares the plan
+    plans = {}
+    for sc in scs:
+        _, ni, nj = sc.params.grid()
+        if (ni, nj) not in plans:
+            plans[(ni, nj)] = gpu.cluster_autotune(ni, nj, 0)
     hs = [gpu.GpuFlipSolver(sc, precision=gpu.FS_PCG_SPEC) for sc in scs]
     b = gpu.Batch(hs)
     b.run_frames(warm)
@@ -450,7 +457,9 @@ def batch_measure(n: int, warm: int, frames: int, single_sample: int):
            "h2d": 4 * len(hs) * rounds + 2 * 72 * sum(subs), "d2h": 32 * sum(subs),
            "launches": hs[0].timer(2), "solve_ms": b.timer(0), "rounds_ms": b.timer(1),
            "rounds": rounds, "total_cells": int(sum(g.ni * g.nj for g in hs)),
-           "particles": int(sum(counts))}
+           "particles": int(sum(counts)),
+           "plans": {f"{k[0]}x{k[1]}": {"ctas_per_cluster": v[0], "us_per_iteration": round(v[1], 2)}
+                     for k, v in sorted(plans.items())}}
     b.close()
     m = min(len(hs), single_sample)
     single_work, single_s = 0, 0.0
@@ -499,6 +508,7 @@ def batch_arm(args):
                           "one thread-block cluster per system",
                    "l2": "working set of all scenes far above L2",
                    "step": "one frame of every scene, the frames run pipelined (fs_batch_run_frames)",
+                   "autotuned_plans": r["plans"],
                    "parallelism": "single GPU"},
         "cell_substeps_per_s": r["cells"] / total_s,
         "merged_solves": {"device_ms_per_step": r["solve_ms"] / args.steps,

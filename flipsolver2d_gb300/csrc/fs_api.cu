@@ -2462,6 +2462,129 @@ extern "C" fs_status fs_pcg_solve_batch(fs_poisson_system *systems, int n, doubl
 }
 
 // ---------------------------------------------------------------------------
+// fs_cluster_autotune: picks the cluster size of the cluster solve for one
+// grid shape by timing every size that fits (no reference counterpart)
+// ---------------------------------------------------------------------------
+extern "C" fs_status fs_cluster_autotune(int ni, int nj, int objective, int device, int *clusters,
+                                         float *us_per_iteration)
+{
+    if (ni < 1 || nj < 1 || (objective != 0 && objective != 1))
+        return fail(FS_ERR_BAD_ARG, "fs_cluster_autotune: invalid argument");
+    CK(cudaSetDevice(device));
+    std::vector<ClusterPlan> cand;
+    cluster_candidates(ni, nj, &cand);
+    if (cand.empty())
+        return fail(FS_ERR_BAD_ARG, "fs_cluster_autotune: %d x %d exceeds the on-chip limit of %lld cells", ni,
+                    nj, cluster_max_cells());
+    // a synthetic system of this shape: fluid inside a one-cell solid wall,
+    // a seeded right-hand side on the fluid cells
+    const size_t N = (size_t)ni * nj;
+    std::vector<int8_t> mat(N, (int8_t)M_FLUID);
+    std::vector<double> rhs(N, 0.0);
+    unsigned long long rng = 0x9E3779B97F4A7C15ull;
+    for (int i = 0; i < ni; i++)
+        for (int j = 0; j < nj; j++) {
+            const size_t c = (size_t)i * nj + j;
+            if (i == 0 || j == 0 || i == ni - 1 || j == nj - 1) {
+                mat[c] = (int8_t)M_SOLID;
+            } else {
+                rng = rng * 6364136223846793005ull + 1442695040888963407ull;
+                rhs[c] = (double)((rng >> 11) * (1.0 / 9007199254740992.0)) - 0.5;
+            }
+        }
+    std::vector<void *> bufs;
+    auto release = [&]() {
+        for (void *p : bufs) cudaFree(p);
+        bufs.clear();
+    };
+    auto dev = [&](size_t bytes) -> void * {
+        void *p = nullptr;
+        if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+        bufs.push_back(p);
+        return p;
+    };
+    int8_t *dmat = (int8_t *)dev(N);
+    uint8_t *info = (uint8_t *)dev(N);
+    double *b = (double *)dev(N * 8), *x = (double *)dev(N * 8), *rel = (double *)dev(8);
+    float *dt = (float *)dev(4);
+    int *iters = (int *)dev(4), *chunk_last = (int *)dev(8);
+    Scalars *sc = (Scalars *)dev(sizeof(Scalars));
+    ClusterSystem *sys = (ClusterSystem *)dev(sizeof(ClusterSystem));
+    if (!dmat || !info || !b || !x || !rel || !dt || !iters || !chunk_last || !sc || !sys) {
+        release();
+        return fail(FS_ERR_OOM, "fs_cluster_autotune: cudaMalloc failed");
+    }
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto check = [&](cudaError_t e, const char *what) -> fs_status {
+        if (e == cudaSuccess) return FS_OK;
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        release();
+        return fail(FS_ERR_CUDA, "fs_cluster_autotune: %s: %s", what, cudaGetErrorString(e));
+    };
+    const float hdt = 1.f / 30.f;
+    TRY(check(cudaMemcpy(dmat, mat.data(), N, cudaMemcpyHostToDevice), "upload"));
+    TRY(check(cudaMemcpy(b, rhs.data(), N * 8, cudaMemcpyHostToDevice), "upload"));
+    TRY(check(cudaMemcpy(dt, &hdt, 4, cudaMemcpyHostToDevice), "upload"));
+    TRY(check(cudaMemset(sc, 0, sizeof(Scalars)), "memset"));
+    GridDims gd{ni, nj, ni / 3 + (ni % 3 != 0), nj / 3 + (nj % 3 != 0)};
+    Grids G;
+    G.material = dmat;
+    G.cell_info = info;
+    launch_decomposition(gd, G, chunk_last, 1, (long long)N, 0, sc, 0);
+    ClusterSystem hs;
+    hs.ni = ni;
+    hs.nj = nj;
+    hs.info = info;
+    hs.b = b;
+    hs.x = x;
+    hs.dt = dt;
+    hs.density = 1000.0;
+    hs.dx = 1.0 / std::max(ni, nj);
+    hs.iters = iters;
+    hs.rel_res = rel;
+    TRY(check(cudaMemcpy(sys, &hs, sizeof(hs), cudaMemcpyHostToDevice), "upload"));
+    TRY(check(cudaEventCreate(&e0), "event"));
+    TRY(check(cudaEventCreate(&e1), "event"));
+    // a fixed number of inner iterations (no stopping on the residual)
+    const int kIters = 64;
+    ClusterParams cp;
+    cp.tol = 1e-300;
+    cp.eps_in = 0.f;
+    cp.max_iter = kIters;
+    cp.max_outer = 1;
+    int best = -1;
+    float best_cost = 0.f, best_us = 0.f;
+    for (size_t k = 0; k < cand.size(); k++) {
+        float ms = 0.f;
+        for (int rep = 0; rep < 2; rep++) { // the first run warms up
+            TRY(check(cudaEventRecord(e0, 0), "event"));
+            TRY(check(launch_pcg_cluster(sys, 1, cand[k], cp, 0), "launch"));
+            TRY(check(cudaEventRecord(e1, 0), "event"));
+            TRY(check(cudaEventSynchronize(e1), "sync"));
+            TRY(check(cudaEventElapsedTime(&ms, e0, e1), "event"));
+        }
+        int it = 0;
+        TRY(check(cudaMemcpy(&it, iters, 4, cudaMemcpyDeviceToHost), "readback"));
+        const float us = 1e3f * ms / (float)std::max(it, 1);
+        // throughput: SM time per iteration; latency: time per iteration
+        const float cost = objective == 0 ? us * (float)cand[k].C : us;
+        if (best < 0 || cost < best_cost) {
+            best = (int)k;
+            best_cost = cost;
+            best_us = us;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    release();
+    cluster_set_tuned(ni, nj, cand[best]);
+    if (clusters) *clusters = cand[best].C;
+    if (us_per_iteration) *us_per_iteration = best_us;
+    return FS_OK;
+}
+
+// ---------------------------------------------------------------------------
 // fs_pcg_solve_device_noalloc: the FP32 device-pointer solve with all of its
 // scratch in one fixed device array (no counterpart in the reference).
 //

@@ -36,6 +36,10 @@
 #include <cstdint>
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
+#include <map>
+#include <mutex>
+#include <utility>
+#include <vector>
 
 #include "fs_cluster.h"
 
@@ -467,29 +471,63 @@ static void cl_init()
 }
 
 // Rows split over C CTAs at floor(k ni / C), so every CTA has at most
-// ceil(ni / C) rows and, for C <= ni, at least one.  The smallest C whose
-// CTAs fit (fewest CTAs for the work), then the fewest cells per thread.
+// ceil(ni / C) rows and, for C <= ni, at least one.  The plan for one C, if
+// its CTAs fit: the fewest cells per thread that hold the rows.
+static bool cl_plan_c(int ni, int nj, int C, size_t smem_limit, ClusterPlan *out)
+{
+    if (C > ni) return false;
+    const long long rows = (ni + C - 1) / C;
+    const long long cells = rows * nj;
+    if (cells > kClMaxOwn) return false;
+    const size_t need = cl_vec_bytes((int)rows, nj) + kClTail;
+    if (need > smem_limit) return false;
+    out->C = C;
+    out->K = cells <= 8 * kClThreads ? 8 : (cells <= 16 * kClThreads ? 16 : 32);
+    out->smem = need;
+    return true;
+}
+
+// the default: the smallest C whose CTAs fit (fewest CTAs for the work)
 static bool cl_plan(int ni, int nj, int max_c, size_t smem_limit, ClusterPlan *out)
 {
-    for (int C = 1; C <= max_c && C <= ni; C *= 2) {
-        const long long rows = (ni + C - 1) / C;
-        const long long cells = rows * nj;
-        if (cells > kClMaxOwn) continue;
-        const size_t need = cl_vec_bytes((int)rows, nj) + kClTail;
-        if (need > smem_limit) continue;
-        out->C = C;
-        out->K = cells <= 8 * kClThreads ? 8 : (cells <= 16 * kClThreads ? 16 : 32);
-        out->smem = need;
-        return true;
-    }
+    for (int C = 1; C <= max_c; C *= 2)
+        if (cl_plan_c(ni, nj, C, smem_limit, out)) return true;
     return false;
 }
+
+// plans chosen by the autotuner, by grid shape (this process)
+static std::mutex g_tuned_mu;
+static std::map<std::pair<int, int>, ClusterPlan> g_tuned;
 
 bool cluster_plan(int ni, int nj, ClusterPlan *plan)
 {
     cl_init();
     if (g_cl_max_cluster <= 0 || ni < 1 || nj < 1) return false;
+    {
+        std::lock_guard<std::mutex> lock(g_tuned_mu);
+        auto it = g_tuned.find({ni, nj});
+        if (it != g_tuned.end()) {
+            *plan = it->second;
+            return true;
+        }
+    }
     return cl_plan(ni, nj, g_cl_max_cluster, g_cl_smem_limit, plan);
+}
+
+void cluster_candidates(int ni, int nj, std::vector<ClusterPlan> *out)
+{
+    cl_init();
+    out->clear();
+    for (int C = 1; C <= g_cl_max_cluster; C *= 2) {
+        ClusterPlan p;
+        if (cl_plan_c(ni, nj, C, g_cl_smem_limit, &p)) out->push_back(p);
+    }
+}
+
+void cluster_set_tuned(int ni, int nj, const ClusterPlan &plan)
+{
+    std::lock_guard<std::mutex> lock(g_tuned_mu);
+    g_tuned[{ni, nj}] = plan;
 }
 
 long long cluster_max_cells()

@@ -5,6 +5,7 @@
 
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <vector>
 
 namespace fsg {
 
@@ -34,8 +35,14 @@ struct ClusterPlan {
     int C, K;
     size_t smem;
 };
-// false: the system does not fit on chip (or there is no device)
+// false: the system does not fit on chip (or there is no device).  The plan
+// the autotuner chose for this shape if there is one, else the smallest C
+// whose CTAs fit.
 bool cluster_plan(int ni, int nj, ClusterPlan *plan);
+// every C that fits, with its plan (the autotuner's candidates)
+void cluster_candidates(int ni, int nj, std::vector<ClusterPlan> *out);
+// records the autotuner's choice for a shape (later cluster_plan calls use it)
+void cluster_set_tuned(int ni, int nj, const ClusterPlan &plan);
 // the most cells a system may have
 long long cluster_max_cells();
 

@@ -99,6 +99,8 @@ _SIGS = {
                                          ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "fs_device_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_cluster_autotune": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_void_p, ctypes.c_void_p]),
     "fs_batch_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "fs_batch_add": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "fs_batch_remove": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
@@ -430,6 +432,17 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def cluster_autotune(ni: int, nj: int, objective: int = 0, device: int = 0):
+    """fs_cluster_autotune: (chosen CTAs per cluster, microseconds per inner
+    iteration).  objective 0 = throughput (batches), 1 = latency."""
+    lib = load()
+    c = ctypes.c_int()
+    us = ctypes.c_float()
+    _check(lib.fs_cluster_autotune(int(ni), int(nj), int(objective), int(device), ctypes.byref(c),
+                                   ctypes.byref(us)), "fs_cluster_autotune")
+    return int(c.value), float(us.value)
 
 
 class PoissonSystem(ctypes.Structure):

@@ -313,6 +313,19 @@ fs_status fs_batch_destroy(fs_batch *batch);
  * writes 0). */
 fs_status fs_batch_timer(fs_batch *batch, int which, double *value);
 
+/* Autotuner of the cluster solve (no reference counterpart): times every
+ * cluster size that fits an ni x nj system (64 inner iterations on a
+ * synthetic fluid-in-a-box system, CUDA events) and records the best for
+ * this shape in the process.  objective 0 minimises SM time per iteration
+ * (throughput: batches), 1 the time per iteration (latency: one system
+ * alone).  Every later plan of that shape uses the choice: FS_PCG_SPEC
+ * handles created afterwards, fs_pcg_solve_batch and batch solves -- so tune
+ * before creating the handles that should share a plan.  *clusters receives
+ * the chosen CTAs per cluster, *us_per_iteration its time per iteration
+ * (either may be NULL). */
+fs_status fs_cluster_autotune(int ni, int nj, int objective, int device, int *clusters,
+                              float *us_per_iteration);
+
 /* fs_pcg_solve_device without any device allocation.  This entry point has
  * no counterpart in the reference.  It is for callers that cannot allocate
  * device memory while they run: a loop that reserved its whole device budget

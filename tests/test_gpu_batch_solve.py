@@ -72,3 +72,16 @@ def test_batch_zero_rhs_and_limits(gpu_lib):
     big = np.full((600, 600), 0x20, np.int8)
     with pytest.raises(gpu.FsError):
         gpu.pcg_solve_batch([(big, np.zeros(big.shape), DT, DENSITY, 1.0 / 600)], REL_TOL)
+
+
+def test_autotuned_plan_is_used(port_lib, gpu_lib):
+    """The autotuner picks a cluster size that fits and later solves of that
+    shape run with it and still meet the residual."""
+    m, b, dx = scenes.poisson_case(192, seed=31)
+    for objective in (1, 0):
+        c, us = gpu.cluster_autotune(192, 192, objective)
+        assert c in (4, 8, 16) and us > 0.0  # 192 rows of 192 need at least 4 CTAs
+        it, x, rr = gpu.pcg_solve_batch([(m, b, DT, DENSITY, dx)], REL_TOL)[0]
+        assert rr <= REL_TOL and _true_rel(m, b, x, dx) <= 1.01 * REL_TOL
+    with pytest.raises(gpu.FsError):
+        gpu.cluster_autotune(700, 700)
