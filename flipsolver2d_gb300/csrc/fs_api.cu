@@ -198,6 +198,10 @@ struct fs_solver {
     bool timers = false;
     double t_step_ms = 0.0, t_pcg_ms = 0.0, launches = 0.0;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
+    // per-stage timing (timers on): events after each group of stages, and
+    // the accumulated milliseconds per SolverStage (flipsolver2d.h:58-72)
+    cudaEvent_t stage_ev[8] = {};
+    double t_stage_ms[12] = {};
     // PCG timing events per solve of a substep (0 density, 1 pressure); read
     // after the substep so that timing adds no host wait inside it
     cudaEvent_t p0[2] = {nullptr, nullptr}, p1[2] = {nullptr, nullptr};
@@ -552,6 +556,8 @@ extern "C" fs_status fs_destroy(fs_solver *s)
     if (s->sc_host) cudaFreeHost(s->sc_host);
     cudaEvent_t evs[] = {s->ev_p2g, s->ev_levelset, s->e0, s->e1, s->p0[0], s->p1[0], s->p0[1], s->p1[1]};
     for (cudaEvent_t e : evs)
+        if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : s->stage_ev)
         if (e) cudaEventDestroy(e);
     if (s->st) cudaStreamDestroy(s->st);
     if (s->side) cudaStreamDestroy(s->side);
@@ -928,24 +934,47 @@ static fs_status stage(fs_solver *s, int which, bool in_step)
     return FS_OK;
 }
 
+// SolverStage indices (flipsolver2d.h:58-72) of the timed stage groups, in
+// the order step() ends them (flipsolver2d.cpp:412-462): advect;
+// decomposition; prune + rebin; density correction; grid update (P2G, SDF
+// and materials, fused here); after transfer (level set, extrapolation,
+// saved grid, body forces); pressure; particle update (friction is in the
+// pressure apply here, then extrapolation and G2P); count and reseed
+static const int kStageOfGroup[9] = {0, 1, 3, 2, 5, 6, 7, 10, 11};
+
 static fs_status step_impl(fs_solver *s)
 {
     TRY(ensure_friction(s));
+    const bool timed = s->timers && s->stage_ev[0];
+    int group = 0;
+    auto mark = [&]() -> fs_status {
+        if (timed) CK(cudaEventRecord(s->stage_ev[group++], s->st));
+        return FS_OK;
+    };
     if (s->timers) CK(cudaEventRecord(s->e0, s->st));
     k_set_dt<<<1, 1, 0, s->st>>>(s->sc, s->step_dt);
     g_kernel_launches += 1;
     TRY(stage(s, FS_STAGE_ADVECT, true));
+    TRY(mark());
     TRY(stage(s, FS_STAGE_DECOMPOSITION, true));
+    TRY(mark());
     TRY(stage(s, FS_STAGE_REBIN, true));
+    TRY(mark());
     TRY(stage(s, FS_STAGE_DENSITY, true));
+    TRY(mark());
     TRY(stage(s, FS_STAGE_P2G, true)); // + updateSdf + updateMaterials
+    TRY(mark());
     TRY(stage(s, FS_STAGE_LEVELSET, true));
     // extrapolate(10), saved copy and body forces in one pass (:437-440)
     launch_vel_extrapolate(s->d, s->G, s->sp, s->sc, true, s->st);
     g_kernel_launches += 1;
+    if (timed) TRY(wait_side(s)); // the level set counts in its own stage
+    TRY(mark());
     TRY(stage(s, FS_STAGE_PROJECT, true)); // + updateVelocityFromSolids
+    TRY(mark());
     TRY(stage(s, FS_STAGE_VEL_EXTRAP, true));
     TRY(stage(s, FS_STAGE_G2P, true));
+    TRY(mark());
     TRY(stage(s, FS_STAGE_COUNT, true));
     if (s->timers) {
         TRY(wait_side(s));
@@ -954,6 +983,15 @@ static fs_status step_impl(fs_solver *s)
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, s->e0, s->e1));
         s->t_step_ms += ms;
+        if (timed) {
+            cudaEvent_t prev = s->e0;
+            for (int g = 0; g < 9; g++) {
+                cudaEvent_t cur = g < 8 ? s->stage_ev[g] : s->e1;
+                CK(cudaEventElapsedTime(&ms, prev, cur));
+                s->t_stage_ms[kStageOfGroup[g]] += ms;
+                prev = cur;
+            }
+        }
         TRY(collect_pcg_timers(s));
     }
     return FS_OK;
@@ -1279,6 +1317,10 @@ extern "C" fs_status fs_get_stat(fs_solver *s, int which, int *out)
 extern "C" fs_status fs_enable_timers(fs_solver *s, int enable)
 {
     if (!s) return fail(FS_ERR_BAD_ARG, "null handle");
+    if (enable && !s->stage_ev[0]) {
+        TRY(set_device(s));
+        for (cudaEvent_t &e : s->stage_ev) CK(cudaEventCreate(&e));
+    }
     s->timers = enable != 0;
     return FS_OK;
 }
@@ -1287,6 +1329,7 @@ extern "C" fs_status fs_reset_timers(fs_solver *s)
 {
     if (!s) return fail(FS_ERR_BAD_ARG, "null handle");
     s->t_step_ms = s->t_pcg_ms = 0.0;
+    for (double &t : s->t_stage_ms) t = 0.0;
     g_kernel_launches = 0;
     return FS_OK;
 }
@@ -1300,6 +1343,13 @@ extern "C" fs_status fs_get_timer(fs_solver *s, int which, double *value)
     case 2: *value = (double)g_kernel_launches.load(); return FS_OK;
     default: return fail(FS_ERR_BAD_ARG, "bad timer id");
     }
+}
+
+extern "C" fs_status fs_get_stage_time(fs_solver *s, int stage, double *ms)
+{
+    if (!s || !ms || stage < 0 || stage >= 12) return fail(FS_ERR_BAD_ARG, "fs_get_stage_time: invalid argument");
+    *ms = s->t_stage_ms[stage];
+    return FS_OK;
 }
 
 extern "C" fs_status fs_get_stream(fs_solver *s, void **stream)

@@ -99,6 +99,7 @@ _SIGS = {
                                          ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "fs_device_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_get_stage_time": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "fs_cluster_autotune": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                            ctypes.c_void_p, ctypes.c_void_p]),
     "fs_batch_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
@@ -229,6 +230,15 @@ class GpuFlipSolver:
         x = ctypes.c_float()
         _check(self.lib.fs_max_particle_velocity(self.h, ctypes.byref(x)), "fs_max_particle_velocity")
         return float(x.value)
+
+    def stage_times(self):
+        """Milliseconds per SolverStage (12 entries) since reset_timers."""
+        out = []
+        for k in range(12):
+            x = ctypes.c_double()
+            _check(self.lib.fs_get_stage_time(self.h, k, ctypes.byref(x)), "fs_get_stage_time")
+            out.append(float(x.value))
+        return out
 
     def device_bytes(self) -> int:
         x = ctypes.c_size_t()

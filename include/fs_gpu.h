@@ -196,6 +196,15 @@ fs_status fs_device_bytes(fs_solver *s, size_t *bytes);
  * counted (as a float).  Times in milliseconds from CUDA events recorded on
  * the handle's stream. */
 fs_status fs_enable_timers(fs_solver *s, int enable);
+/* With timers on, fs_step / fs_step_frame also time the stage groups that
+ * FlipSolver::step ends (flipsolver2d.cpp:412-462) with CUDA events; this
+ * returns the accumulated milliseconds of one SolverStage
+ * (flipsolver2d.h:58-72: 0 advection, 1 decomposition, 2 density,
+ * 3 particle rebin, 4 particle to grid (fused into 5 here), 5 grid update,
+ * 6 after transfer, 7 pressure, 8 viscosity and 9 repressure (always 0),
+ * 10 particle update, 11 particle reseed).  The level set joins the main
+ * stream while timed, so it counts in after transfer. */
+fs_status fs_get_stage_time(fs_solver *s, int stage, double *ms);
 fs_status fs_reset_timers(fs_solver *s);
 fs_status fs_get_timer(fs_solver *s, int which, double *value);
 /* the handle's cudaStream_t, as an opaque pointer */
