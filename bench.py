@@ -280,9 +280,20 @@ def gpu_arm(args):
     # end to end through the C ABI with host-resident state: upload particles
     # and the carried grids, one substep, download them again
     e2e_steps = max(1, min(args.steps, 5))
-    snap_p = s.get_particles()
+    # host state in pinned memory, room for twice the particles
+    cap = 2 * s.particle_count() + 1024
+
+    def pinned(shape, dtype):
+        return torch.empty(shape, dtype=dtype, pin_memory=True).numpy()
+
+    hp = {"bin_counts": pinned((s.bin_count(),), torch.int32), "pos": pinned((cap, 2), torch.float32),
+          "vel": pinned((cap, 2), torch.float32), "visc": pinned((cap,), torch.float32),
+          "dead": pinned((cap,), torch.uint8)}
     carried = ["u", "v", "material"]
-    snap_g = {g: s.get_grid(g) for g in carried}
+    tdt = {"u": torch.float32, "v": torch.float32, "material": torch.int8}
+    hg = {g: pinned(s.grid_shape(g), tdt[g]) for g in carried}
+    snap_p = s.get_particles(out=hp)
+    snap_g = {g: s.get_grid(g, out=hg[g]) for g in carried}
     h2d = sum(v.nbytes for k, v in snap_p.items() if k != "dead") + snap_p["dead"].nbytes
     h2d += sum(a.nbytes for a in snap_g.values())
     d2h = h2d
@@ -296,8 +307,8 @@ def gpu_arm(args):
         e2e_work += len(snap_p["pos"])
         s.set_dt(cfl_dt(s.max_particle_velocity(), p))
         s.step()
-        snap_p = s.get_particles()
-        snap_g = {g: s.get_grid(g) for g in carried}
+        snap_p = s.get_particles(out=hp)
+        snap_g = {g: s.get_grid(g, out=hg[g]) for g in carried}
     e2e_s = time.perf_counter() - t0
     e2e_ms, e2e_work = combine_replicas(1e3 * e2e_s, e2e_work, dist, f"cuda:{local}")
     e2e_value = e2e_work / (e2e_ms / 1e3)
@@ -331,7 +342,7 @@ def gpu_arm(args):
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
                 "path": "fs_set_particles + fs_set_grid(u, v, material) + fs_step + "
-                        "fs_get_particles + fs_get_grid, host buffers"},
+                        "fs_get_particles + fs_get_grid, pinned host buffers"},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": "k_pcg_resident",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -1157,6 +1157,29 @@ extern "C" fs_status fs_get_particles(fs_solver *s, int32_t *bin_counts, float *
     if (!s) return fail(FS_ERR_BAD_ARG, "null handle");
     TRY(set_device(s));
     TRY(sync_all(s));
+    if (!s->after_advect && s->P.cap > 0) {
+        // outside a substep no particle is marked: pack the bins on the
+        // device and copy each array straight into the caller's memory
+        // (pinned caller memory makes these full-bandwidth copies)
+        const Particles &P = s->P;
+        launch_gather_bins(P, s->rebin_scratch, s->st);
+        g_kernel_launches += 4;
+        int total = 0;
+        CK(cudaMemcpyAsync(&total, P.bin_start2 + P.nbins, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+        CK(cudaStreamSynchronize(s->st));
+        if (bin_counts)
+            CK(cudaMemcpyAsync(bin_counts, P.bin_count, (size_t)P.nbins * 4, cudaMemcpyDeviceToHost, s->st));
+        if (total > 0) {
+            if (pos_xy)
+                CK(cudaMemcpyAsync(pos_xy, P.pos2, (size_t)total * sizeof(float2), cudaMemcpyDeviceToHost, s->st));
+            if (vel_xy)
+                CK(cudaMemcpyAsync(vel_xy, P.vel2, (size_t)total * sizeof(float2), cudaMemcpyDeviceToHost, s->st));
+            if (visc) CK(cudaMemcpyAsync(visc, P.visc2, (size_t)total * sizeof(float), cudaMemcpyDeviceToHost, s->st));
+        }
+        CK(cudaStreamSynchronize(s->st));
+        if (dead) memset(dead, 0, (size_t)total);
+        return FS_OK;
+    }
     std::vector<int> st, ct;
     TRY(download_bins(s, st, ct));
     const int nslots = st[s->P.nbins];
@@ -1207,13 +1230,26 @@ extern "C" fs_status fs_set_particles(fs_solver *s, const int32_t *bin_counts, c
             if (dead[k])
                 return fail(FS_ERR_UNSUPPORTED,
                             "particles marked for death can only exist inside a substep");
-    std::vector<float2> p(total), v(total);
-    for (size_t k = 0; k < total; k++) {
-        p[k] = make_float2(pos_xy[2 * k], pos_xy[2 * k + 1]);
-        v[k] = make_float2(vel_xy[2 * k], vel_xy[2 * k + 1]);
+    // the positions and velocities are float pairs already: copy them
+    // straight from the caller's memory; the slot-to-bin map is built on the
+    // device
+    const int nb = s->P.nbins;
+    if ((int)total > s->P.cap || s->P.pos == nullptr) TRY(alloc_particles(s, (int)total));
+    std::vector<int> start(nb + 1, 0);
+    for (int b = 0; b < nb; b++) start[b + 1] = start[b] + counts[b];
+    Particles &P = s->P;
+    CK(cudaMemcpyAsync(P.bin_start, start.data(), (nb + 1) * sizeof(int), cudaMemcpyHostToDevice, s->st));
+    CK(cudaMemcpyAsync(P.bin_count, counts.data(), nb * sizeof(int), cudaMemcpyHostToDevice, s->st));
+    if (total) {
+        CK(cudaMemcpyAsync(P.pos, pos_xy, total * sizeof(float2), cudaMemcpyHostToDevice, s->st));
+        CK(cudaMemcpyAsync(P.vel, vel_xy, total * sizeof(float2), cudaMemcpyHostToDevice, s->st));
+        CK(cudaMemcpyAsync(P.visc, visc, total * sizeof(float), cudaMemcpyHostToDevice, s->st));
+        launch_slot_bin(P, s->st);
+        g_kernel_launches += 1;
     }
-    std::vector<float> vi(visc, visc + total);
-    TRY(upload_particles(s, counts, p, v, vi));
+    CK(cudaStreamSynchronize(s->st));
+    CK(cudaGetLastError());
+    s->after_advect = false;
     s->initialized = true;
     return FS_OK;
 }

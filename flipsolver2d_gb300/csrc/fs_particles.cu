@@ -467,6 +467,50 @@ void launch_rebin(const GridDims &d, Particles &P, void *scratch, size_t, cudaSt
 }
 
 // ---------------------------------------------------------------------------
+// particle state to and from the host in bin order (fs_get/set_particles)
+// ---------------------------------------------------------------------------
+// the live particles of every bin, packed in bin order at off[b]
+__global__ void k_gather_bins(Particles P, const int *__restrict__ off, float2 *__restrict__ pos_out,
+                              float2 *__restrict__ vel_out, float *__restrict__ visc_out)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= P.nbins) return;
+    const int s0 = P.bin_start[b], n = P.bin_count[b], o = off[b];
+    for (int k = 0; k < n; k++) {
+        pos_out[o + k] = P.pos[s0 + k];
+        vel_out[o + k] = P.vel[s0 + k];
+        visc_out[o + k] = P.visc[s0 + k];
+    }
+}
+
+// the bin of every occupied slot
+__global__ void k_slot_bin(Particles P)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= P.nbins) return;
+    const int s0 = P.bin_start[b], n = P.bin_count[b];
+    for (int k = 0; k < n; k++) P.slot_bin[s0 + k] = b;
+}
+
+// packs the particles into pos2 / vel2 / visc2 (free outside a substep) with
+// the bin offsets in bin_start2; off[nbins] is the total
+void launch_gather_bins(const Particles &P, void *scratch, cudaStream_t st)
+{
+    const int ntiles = nblk(P.cap > 0 ? P.cap : 1, kScanTile);
+    const int rtiles = nblk(P.cap > 0 ? P.cap : 1, kRadixTile);
+    char *p = (char *)scratch;
+    p += align256((size_t)(ntiles + 1) * sizeof(int));
+    p += align256((size_t)(256 * rtiles + 1) * sizeof(int));
+    scan_exclusive(P.bin_count, P.bin_start2, P.nbins, p, st);
+    k_gather_bins<<<nblk(P.nbins, kThreads), kThreads, 0, st>>>(P, P.bin_start2, P.pos2, P.vel2, P.visc2);
+}
+
+void launch_slot_bin(const Particles &P, cudaStream_t st)
+{
+    k_slot_bin<<<nblk(P.nbins, kThreads), kThreads, 0, st>>>(P);
+}
+
+// ---------------------------------------------------------------------------
 // density push: FlipSolver::adjustParticlesByDensityThread (:261-303)
 // ---------------------------------------------------------------------------
 template <typename T>

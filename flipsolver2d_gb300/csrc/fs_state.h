@@ -97,6 +97,11 @@ void launch_advect(const GridDims &d, const Particles &P, const Grids &G, const 
 void launch_rebin(const GridDims &d, Particles &P, void *scratch, size_t scratch_bytes,
                   cudaStream_t st);
 size_t rebin_scratch_bytes(const Particles &P);
+// fs_get_particles: pack the particles in bin order into pos2 / vel2 / visc2,
+// offsets in bin_start2 (scratch: the rebin scratch); fs_set_particles: the
+// bin of every occupied slot from bin_start / bin_count
+void launch_gather_bins(const Particles &P, void *scratch, cudaStream_t st);
+void launch_slot_bin(const Particles &P, cudaStream_t st);
 void launch_adjust(const GridDims &d, const SceneParams &sp, const Particles &P, const Grids &G,
                    const void *pressure, int pressure_is_double, const Scalars *sc,
                    cudaStream_t st);

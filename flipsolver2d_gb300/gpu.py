@@ -260,13 +260,21 @@ class GpuFlipSolver:
         _check(self.lib.fs_bin_count(self.h, ctypes.byref(x)), "fs_bin_count")
         return int(x.value)
 
-    def get_particles(self) -> dict:
+    def get_particles(self, out: Optional[dict] = None) -> dict:
+        """The particles in bin order.  `out` may hold preallocated arrays
+        (e.g. in pinned memory) with room for at least particle_count()
+        particles: bin_counts [nbins], pos [cap, 2], vel [cap, 2], visc [cap],
+        dead [cap]; the result then views them."""
         n = self.particle_count()
-        counts = np.zeros(self.bin_count(), np.int32)
-        pos = np.zeros((n, 2), np.float32)
-        vel = np.zeros((n, 2), np.float32)
-        visc = np.zeros(n, np.float32)
-        dead = np.zeros(n, np.uint8)
+        if out is None:
+            counts = np.zeros(self.bin_count(), np.int32)
+            pos = np.zeros((n, 2), np.float32)
+            vel = np.zeros((n, 2), np.float32)
+            visc = np.zeros(n, np.float32)
+            dead = np.zeros(n, np.uint8)
+        else:
+            counts, pos, vel = out["bin_counts"], out["pos"][:n], out["vel"][:n]
+            visc, dead = out["visc"][:n], out["dead"][:n]
         _check(self.lib.fs_get_particles(self.h, _ptr(counts), _ptr(pos), _ptr(vel), _ptr(visc),
                                          _ptr(dead)), "fs_get_particles")
         return {"bin_counts": counts, "pos": pos, "vel": vel, "visc": visc, "dead": dead}
@@ -285,9 +293,10 @@ class GpuFlipSolver:
         return {"c": (self.ni, self.nj), "u": (self.ni + 1, self.nj),
                 "v": (self.ni, self.nj + 1)}[kind]
 
-    def get_grid(self, name: str) -> np.ndarray:
+    def get_grid(self, name: str, out: Optional[np.ndarray] = None) -> np.ndarray:
         gid, dt, _ = GRIDS[name]
-        out = np.zeros(self.grid_shape(name), dt)
+        if out is None:
+            out = np.zeros(self.grid_shape(name), dt)
         _check(self.lib.fs_get_grid(self.h, gid, _ptr(out), out.nbytes), f"fs_get_grid({name})")
         return out
 
