@@ -18,7 +18,9 @@ solver's stream, L2 flushed by a 256 MiB write between steps, outside the
 events); `e2e` goes through the C ABI with host-resident state uploaded and
 downloaded every step; `roofline` is for the PCG kernel, which dominates the
 substep; `cpu_baseline` is the CPU oracle on this host's cores on a bounded
-sample of the same workload.  `batch` (unless --no-batch) is the batched form
+sample of the same workload.  `fp64_check` steps the final state once more
+in FP32 and in the FP64 parity mode from identical inputs and reports the
+FP32 error.  `batch` (unless --no-batch) is the batched form
 of the path beside it: 64 scenes of the batched-scenes workload stepped
 together at a 1e-6 pressure residual, and the same scenes one at a time.
 With --impl reference only the CPU
@@ -211,6 +213,43 @@ def reference_arm(args):
     return 0
 
 
+def fp64_check(s, sc, p):
+    """One substep from identical state in the measured FP32 mode and in the
+    FP64 parity mode (the reference's own arithmetic, bit for bit): the
+    error of the FP32 results against the FP64 ones.  Outside any timed
+    region."""
+    from flipsolver2d_gb300 import gpu
+
+    snap = s.get_particles()
+    grids = {g: s.get_grid(g) for g in ("u", "v", "material")}
+    dt = cfl_dt(s.max_particle_velocity(), p)
+    d = gpu.GpuFlipSolver(sc, precision=gpu.FS_PCG_FP64)
+    d.first_frame_init()  # the solid data; the fluid state is replaced below
+    out = []
+    for g in (s, d):
+        g.set_particles(snap)
+        for k, a in grids.items():
+            g.set_grid(k, a)
+        g.set_dt(dt)
+        g.step()
+        out.append((g.get_particles(), g.get_grid("pressure"), g.get_grid("u")))
+    d.close()
+    (a, pa, ua), (b, pb, ub) = out
+
+    def rel(x, y):
+        n = float(np.linalg.norm(y))
+        return float(np.linalg.norm(np.asarray(x, np.float64) - np.asarray(y, np.float64)) / n) if n else 0.0
+
+    res = {"dt": dt, "particles": int(len(b["pos"])), "pressure_rel_l2": rel(pa, pb),
+           "grid_u_rel_l2": rel(ua, ub)}
+    if a["pos"].shape == b["pos"].shape:
+        res["particle_vel_rel_l2"] = rel(a["vel"], b["vel"])
+        res["particle_pos_max_abs_cells"] = float(np.max(np.abs(a["pos"] - b["pos"])))
+    else:
+        res["particle_count_difference"] = int(len(a["pos"]) - len(b["pos"]))
+    return res
+
+
 def gpu_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -354,6 +393,11 @@ def gpu_arm(args):
         "cpu_baseline": cpu,
         "clocks": clocks,
     }
+    if rank == 0:
+        try:
+            line["fp64_check"] = fp64_check(s, sc, p)
+        except Exception as e:  # reported, never fatal for the main line
+            line["fp64_check"] = {"error": str(e)}
     s.close()
     if rank == 0 and world == 1 and not args.no_batch:
         # the batched form of the same path beside the single-scene line: 64
