@@ -43,6 +43,13 @@ std::atomic<long long> g_kernel_launches{0};
 // ---------------------------------------------------------------------------
 // errors
 // ---------------------------------------------------------------------------
+// FS_PCG_SPEC: the relative residual every pressure and density solve
+// reaches, and its inner-iteration cap (a solve that hits it counts as
+// failed, like the reference's iteration limit)
+constexpr double kSpecRelTol = 1e-6;
+constexpr int kSpecMaxIter = 20000;
+constexpr int kSpecMaxOuter = 12; // refinements of a chained solve (2 or 3 are typical)
+
 static thread_local std::string t_last_error;
 
 static fs_status fail(fs_status st, const char *fmt, ...)
@@ -177,6 +184,8 @@ struct fs_solver {
     ClusterPlan spec_plan{};   // FS_PCG_SPEC: how the cluster solve runs this grid
     ClusterSystem *spec_sys = nullptr; // FS_PCG_SPEC: the density and pressure systems
     double *spec_rel = nullptr;        // their final relative residuals
+    bool spec_large = false;           // FS_PCG_SPEC above the on-chip limit: chained
+    SpecSolve spec_chain[2] = {};      // cooperative solves (density, pressure)
     int res_ti = 0, res_tj = 0;
     TmaMaps maps_dens{}, maps_pres{};
     void *rebin_scratch = nullptr;
@@ -480,10 +489,52 @@ extern "C" fs_status fs_create(const fs_params *p, const fs_exec_params *exec, f
                                 (const float *)s->r0, (const float *)s->r1, (const float *)s->s0,
                                 (const float *)s->s1);
     }
-    if (s->prec == FS_PCG_SPEC) {
-        if (!cluster_plan(d.ni, d.nj, &s->spec_plan))
-            return cleanup(fail(FS_ERR_UNSUPPORTED,
-                                "fs_create: FS_PCG_SPEC needs a grid of at most %lld cells", cluster_max_cells()));
+    if (s->prec == FS_PCG_SPEC && !cluster_plan(d.ni, d.nj, &s->spec_plan)) {
+        // above the on-chip limit: the cooperative solve, chained on the
+        // device (launch_spec_chain)
+        s->spec_large = true;
+        A(dalloc(s, &s->spec_rel, 2));
+        float *r = nullptr, *dd = nullptr, *sv = nullptr, *q = nullptr, *z = nullptr;
+        float2 *parts = nullptr;
+        double *rpart = nullptr;
+        unsigned *count = nullptr;
+        SpecCtl *ctl = nullptr;
+        A(dalloc(s, &r, n));
+        A(dalloc(s, &dd, n));
+        A(dalloc(s, &sv, n));
+        A(dalloc(s, &q, n));
+        A(dalloc(s, &z, n));
+        A(dalloc(s, &parts, (size_t)spec_partials_needed()));
+        A(dalloc(s, &rpart, (size_t)kSpecResBlocks));
+        A(dalloc(s, &count, 1));
+        A(dalloc(s, &ctl, 1));
+        for (int k = 0; k < 2; k++) {
+            SpecSolve &c = s->spec_chain[k];
+            c.ni = d.ni;
+            c.nj = d.nj;
+            c.info = G.cell_info;
+            c.b = (const double *)(k == 0 ? s->dens_rhs : s->pres_rhs);
+            c.x = (double *)(k == 0 ? s->dens_x : s->pres_x);
+            c.dt = &s->sc->dt;
+            c.density = p->fluidDensity;
+            c.dx = p->dx;
+            c.r = r;
+            c.d = dd;
+            c.s = sv;
+            c.q = q;
+            c.z = z;
+            c.partials = parts;
+            c.rpart = rpart;
+            c.count = count;
+            c.status = &s->sc->pcg_status;
+            c.ctl = ctl;
+            c.iters_out = k == 0 ? &s->sc->density_iters : &s->sc->pressure_iters;
+            c.rel_out = s->spec_rel + k;
+            c.tol = kSpecRelTol;
+            c.max_iter = kSpecMaxIter;
+            c.max_outer = kSpecMaxOuter;
+        }
+    } else if (s->prec == FS_PCG_SPEC) {
         A(dalloc(s, &s->spec_sys, 2));
         A(dalloc(s, &s->spec_rel, 2));
         ClusterSystem hs[2];
@@ -764,11 +815,6 @@ template <typename T> static PcgArgs<T> pcg_args(fs_solver *s, const void *b, vo
     return a;
 }
 
-// FS_PCG_SPEC: the relative residual every pressure and density solve
-// reaches, and its inner-iteration cap (a solve that hits it counts as
-// failed, like the reference's iteration limit)
-constexpr double kSpecRelTol = 1e-6;
-constexpr int kSpecMaxIter = 20000;
 static ClusterParams spec_params()
 {
     ClusterParams cp;
@@ -787,6 +833,9 @@ static fs_status run_pcg(fs_solver *s, const void *b, void *x, int *iters)
     int launched = 0;
     if (s->prec == FS_PCG_FP64) {
         e = launch_pcg<double>(pcg_args<double>(s, b, x, iters), s->st, &launched);
+    } else if (s->prec == FS_PCG_SPEC && s->spec_large) {
+        e = launch_spec_chain(s->spec_chain[slot], s->st);
+        launched = 4 * kSpecMaxOuter + 2;
     } else if (s->prec == FS_PCG_SPEC) {
         e = launch_pcg_cluster(s->spec_sys + slot, 1, s->spec_plan, spec_params(), s->st);
         launched = 1;
@@ -1453,6 +1502,9 @@ struct BatchSolve {
     ClusterSystem sys{};
     ClusterPlan plan{};
     bool done = false;
+    bool large = false; // above the on-chip limit: a chained solve
+    SpecSolve chain{};
+    void *chain_mem = nullptr;
 };
 
 struct fs_batch {
@@ -1500,6 +1552,11 @@ static fs_status batch_capture(fs_batch *b, BatchScene &bs, int parity)
             if (st == FS_OK) {
                 launch_density_grid(d, s->sp, s->P, s->G, s->dens_rhs, dbl, s->sc, q);
                 g_kernel_launches += 1;
+                if (s->spec_large) { // its own chained solve, not a merged one
+                    if (launch_spec_chain(s->spec_chain[0], q) != cudaSuccess)
+                        st = fail(FS_ERR_CUDA, "fs_batch: capture of a chained solve");
+                    g_kernel_launches += 4 * kSpecMaxOuter + 2;
+                }
             }
         } else if (seg == 1) {
             SceneParams sp = s->sp;
@@ -1513,6 +1570,11 @@ static fs_status batch_capture(fs_batch *b, BatchScene &bs, int parity)
                 launch_pressure_rhs(d, s->G, s->pres_rhs, dbl, s->sp, q);
                 g_kernel_launches += 2;
                 st = wait_side(s); // the level set joins before the graph ends
+                if (st == FS_OK && s->spec_large) {
+                    if (launch_spec_chain(s->spec_chain[1], q) != cudaSuccess)
+                        st = fail(FS_ERR_CUDA, "fs_batch: capture of a chained solve");
+                    g_kernel_launches += 4 * kSpecMaxOuter + 2;
+                }
             }
         } else {
             launch_apply_pressure(d, s->sp, s->G, s->pres_x, dbl, s->sc, true, q);
@@ -1601,8 +1663,10 @@ extern "C" fs_status fs_batch_destroy(fs_batch *b)
         batch_release_graphs(bs);
         if (bs.ev) cudaEventDestroy(bs.ev);
     }
-    for (BatchSolve &q : b->solves)
+    for (BatchSolve &q : b->solves) {
         if (q.mem) cudaFree(q.mem);
+        if (q.chain_mem) cudaFree(q.chain_mem);
+    }
     if (b->ev_solve) cudaEventDestroy(b->ev_solve);
     for (cudaEvent_t e : b->ev_t)
         if (e) cudaEventDestroy(e);
@@ -1759,10 +1823,34 @@ extern "C" fs_status fs_batch_submit_solve(fs_batch *b, const fs_poisson_system 
     const size_t N = (size_t)q->ni * q->nj;
     if (!valid_material(q->material, N)) return fail(FS_ERR_BAD_ARG, "fs_batch_submit_solve: unknown material code");
     BatchSolve v;
-    if (!cluster_plan(q->ni, q->nj, &v.plan))
-        return fail(FS_ERR_BAD_ARG, "fs_batch_submit_solve: %d x %d exceeds the on-chip limit of %lld cells",
-                    q->ni, q->nj, cluster_max_cells());
+    v.large = !cluster_plan(q->ni, q->nj, &v.plan);
     CK(cudaSetDevice(b->device));
+    if (v.large) {
+        // the chained cooperative solve's vectors and control block
+        const size_t fb = ((N * 4 + 255) & ~(size_t)255);
+        const size_t pb = (((size_t)spec_partials_needed() * sizeof(float2) + 255) & ~(size_t)255);
+        const size_t cbytes = 5 * fb + pb + (size_t)kSpecResBlocks * 8 + 256;
+        cudaError_t ec = cudaMalloc(&v.chain_mem, cbytes);
+        if (ec != cudaSuccess)
+            return fail(ec == cudaErrorMemoryAllocation ? FS_ERR_OOM : FS_ERR_CUDA,
+                        "fs_batch_submit_solve: cudaMalloc: %s", cudaGetErrorString(ec));
+        char *c = static_cast<char *>(v.chain_mem);
+        v.chain.r = reinterpret_cast<float *>(c);
+        v.chain.d = reinterpret_cast<float *>(c + fb);
+        v.chain.s = reinterpret_cast<float *>(c + 2 * fb);
+        v.chain.q = reinterpret_cast<float *>(c + 3 * fb);
+        v.chain.z = reinterpret_cast<float *>(c + 4 * fb);
+        v.chain.partials = reinterpret_cast<float2 *>(c + 5 * fb);
+        v.chain.rpart = reinterpret_cast<double *>(c + 5 * fb + pb);
+        char *t = c + 5 * fb + pb + (size_t)kSpecResBlocks * 8;
+        v.chain.ctl = reinterpret_cast<SpecCtl *>(t);
+        v.chain.count = reinterpret_cast<unsigned *>(t + 64);
+        v.chain.status = reinterpret_cast<int *>(t + 128);
+        if ((ec = cudaMemset(t + 128, 0, sizeof(int))) != cudaSuccess) {
+            cudaFree(v.chain_mem);
+            return fail(FS_ERR_CUDA, "fs_batch_submit_solve: %s", cudaGetErrorString(ec));
+        }
+    }
     const size_t a = (N + 255) & ~(size_t)255;
     const size_t bytes = 2 * a + 16 * N + 256;
     cudaError_t e = cudaMalloc(&v.mem, bytes);
@@ -1810,6 +1898,22 @@ extern "C" fs_status fs_batch_submit_solve(fs_batch *b, const fs_poisson_system 
     c.dx = q->dx;
     c.iters = iters;
     c.rel_res = rel;
+    if (v.large) {
+        SpecSolve &ch = v.chain;
+        ch.ni = q->ni;
+        ch.nj = q->nj;
+        ch.info = info;
+        ch.b = bv;
+        ch.x = xv;
+        ch.dt = dt;
+        ch.density = q->density;
+        ch.dx = q->dx;
+        ch.iters_out = iters;
+        ch.rel_out = rel;
+        ch.tol = kSpecRelTol;
+        ch.max_iter = kSpecMaxIter;
+        ch.max_outer = kSpecMaxOuter;
+    }
     b->solves.push_back(v);
     *ticket = v.ticket;
     return FS_OK;
@@ -1849,10 +1953,14 @@ extern "C" fs_status fs_batch_take_solve(fs_batch *b, unsigned long long ticket,
     CK(cudaMemcpy(q->result, v->sys.x, N * 8, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(&it, v->sys.iters, sizeof(int), cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(&rel, v->sys.rel_res, sizeof(double), cudaMemcpyDeviceToHost));
+    int chain_status = 0;
+    if (v->large) CK(cudaMemcpy(&chain_status, v->chain.status, sizeof(int), cudaMemcpyDeviceToHost));
     q->iterations = it;
     q->rel_residual = rel;
     cudaFree(v->mem);
+    if (v->chain_mem) cudaFree(v->chain_mem);
     b->solves.erase(b->solves.begin() + (long)k);
+    if (chain_status != 0) return fail(FS_ERR_TIMEOUT, "fs_batch_take_solve: a grid barrier wait timed out");
     return FS_OK;
 }
 
@@ -1893,6 +2001,7 @@ static fs_status batch_solve(fs_batch *b, const std::vector<int> &act, const std
     ent.reserve(total);
     for (int k : act) {
         fs_solver *s = b->sc[k].s;
+        if (s->spec_large) continue; // solved inside its own graphs
         ClusterSystem c;
         c.ni = s->d.ni;
         c.nj = s->d.nj;
@@ -1907,8 +2016,23 @@ static fs_status batch_solve(fs_batch *b, const std::vector<int> &act, const std
         ent.push_back({s->spec_plan, c});
     }
     if (which == 1)
-        for (int k : extra) ent.push_back({b->solves[k].plan, b->solves[k].sys});
-    if (ent.empty()) return FS_OK;
+        for (int k : extra)
+            if (!b->solves[k].large) ent.push_back({b->solves[k].plan, b->solves[k].sys});
+    if (which == 1) {
+        // standalone systems above the on-chip limit: their chained solves
+        for (int k : act) CK(cudaStreamWaitEvent(b->bst, b->sc[k].ev, 0));
+        for (int k : extra)
+            if (b->solves[k].large) {
+                CK(launch_spec_chain(b->solves[k].chain, b->bst));
+                g_kernel_launches += 4 * kSpecMaxOuter + 2;
+            }
+    }
+    if (ent.empty()) {
+        CK(cudaEventRecord(b->ev_t[2 * which], b->bst));
+        CK(cudaEventRecord(b->ev_t[2 * which + 1], b->bst));
+        CK(cudaEventRecord(b->ev_solve, b->bst));
+        return FS_OK;
+    }
     auto key = [](const ClusterPlan &q) { return q.C * 64 + q.K; };
     // the largest clusters first: they wait longest for whole GPCs
     std::stable_sort(ent.begin(), ent.end(), [&](const auto &x, const auto &y) { return key(x.first) > key(y.first); });
@@ -2303,54 +2427,55 @@ extern "C" fs_status fs_pcg_solve_spec(int ni, int nj, const int8_t *material, f
     const long long N = (long long)ni * nj;
     const int dev = exec ? exec->device : 0;
     CK(cudaSetDevice(dev));
-    const double scale = (double)dt / (density * dx * dx);
     cudaStream_t st = 0;
     // device buffers for this call
     std::vector<void *> bufs;
+    auto release = [&]() {
+        for (void *q : bufs) cudaFree(q);
+        bufs.clear();
+    };
     auto dalloc_tmp = [&](void **p, size_t bytes) -> fs_status {
         cudaError_t e = cudaMalloc(p, bytes);
         if (e != cudaSuccess) {
-            for (void *q : bufs) cudaFree(q);
+            release();
             return fail(e == cudaErrorMemoryAllocation ? FS_ERR_OOM : FS_ERR_CUDA,
                         "fs_pcg_solve_spec: cudaMalloc: %s", cudaGetErrorString(e));
         }
         bufs.push_back(*p);
         return FS_OK;
     };
-    int8_t *mat = nullptr;
-    uint8_t *info = nullptr;
-    double *b = nullptr, *x = nullptr, *part = nullptr;
-    float *r = nullptr, *d = nullptr, *s = nullptr, *q = nullptr, *y = nullptr, *z = nullptr;
-    float2 *partials = nullptr;
-    int *chunk_last = nullptr;
-    Scalars *sc = nullptr;
-    unsigned *count = nullptr;
-    int *iters_dev = nullptr;
-    const int rblocks = 1024;
-    TRY(dalloc_tmp((void **)&mat, N));
-    TRY(dalloc_tmp((void **)&info, N));
-    TRY(dalloc_tmp((void **)&b, N * 8));
-    TRY(dalloc_tmp((void **)&x, N * 8));
-    TRY(dalloc_tmp((void **)&part, rblocks * 8));
-    float **fv[] = {&r, &d, &s, &q, &z};
-    for (float **v : fv) TRY(dalloc_tmp((void **)v, N * 4));
-    TRY(dalloc_tmp((void **)&partials, (size_t)spec_partials_needed() * sizeof(float2)));
-    TRY(dalloc_tmp((void **)&chunk_last, 2 * sizeof(int)));
-    TRY(dalloc_tmp((void **)&sc, sizeof(Scalars)));
-    TRY(dalloc_tmp((void **)&count, sizeof(unsigned)));
-    TRY(dalloc_tmp((void **)&iters_dev, sizeof(int)));
-    auto release = [&]() {
-        for (void *p : bufs) cudaFree(p);
-        bufs.clear();
-    };
     auto check = [&](cudaError_t e, const char *what) -> fs_status {
         if (e == cudaSuccess) return FS_OK;
         release();
         return fail(FS_ERR_CUDA, "fs_pcg_solve_spec: %s: %s", what, cudaGetErrorString(e));
     };
+    int8_t *mat = nullptr;
+    uint8_t *info = nullptr;
+    double *b = nullptr, *x = nullptr, *rpart = nullptr, *rel_dev = nullptr;
+    float *r = nullptr, *d = nullptr, *s = nullptr, *q = nullptr, *z = nullptr, *dt_dev = nullptr;
+    float2 *partials = nullptr;
+    int *chunk_last = nullptr, *iters_dev = nullptr;
+    Scalars *sc = nullptr;
+    unsigned *count = nullptr;
+    SpecCtl *ctl = nullptr;
+    TRY(dalloc_tmp((void **)&mat, N));
+    TRY(dalloc_tmp((void **)&info, N));
+    TRY(dalloc_tmp((void **)&b, N * 8));
+    TRY(dalloc_tmp((void **)&x, N * 8));
+    float **fv[] = {&r, &d, &s, &q, &z};
+    for (float **v : fv) TRY(dalloc_tmp((void **)v, N * 4));
+    TRY(dalloc_tmp((void **)&partials, (size_t)spec_partials_needed() * sizeof(float2)));
+    TRY(dalloc_tmp((void **)&rpart, (size_t)kSpecResBlocks * 8));
+    TRY(dalloc_tmp((void **)&chunk_last, 2 * sizeof(int)));
+    TRY(dalloc_tmp((void **)&sc, sizeof(Scalars)));
+    TRY(dalloc_tmp((void **)&count, sizeof(unsigned)));
+    TRY(dalloc_tmp((void **)&ctl, sizeof(SpecCtl)));
+    TRY(dalloc_tmp((void **)&dt_dev, sizeof(float)));
+    TRY(dalloc_tmp((void **)&iters_dev, sizeof(int)));
+    TRY(dalloc_tmp((void **)&rel_dev, sizeof(double)));
     TRY(check(cudaMemcpyAsync(mat, material, N, cudaMemcpyHostToDevice, st), "upload"));
     TRY(check(cudaMemcpyAsync(b, rhs, N * 8, cudaMemcpyHostToDevice, st), "upload"));
-    TRY(check(cudaMemsetAsync(x, 0, N * 8, st), "memset"));
+    TRY(check(cudaMemcpyAsync(dt_dev, &dt, sizeof(float), cudaMemcpyHostToDevice, st), "upload"));
     TRY(check(cudaMemsetAsync(sc, 0, sizeof(Scalars), st), "memset"));
     GridDims gd{ni, nj, ni / 3 + (ni % 3 != 0), nj / 3 + (nj % 3 != 0)};
     Grids G;
@@ -2358,60 +2483,47 @@ extern "C" fs_status fs_pcg_solve_spec(int ni, int nj, const int8_t *material, f
     G.cell_info = info;
     launch_decomposition(gd, G, chunk_last, 1, N, 0, sc, st);
     g_kernel_launches += 1;
-
-    std::vector<double> hp(rblocks);
-    double bnorm = 0.0, rnorm = 0.0;
-    int total_inner = 0;
-    int h_status = 0;
-    for (int outer = 0;; outer++) {
-        TRY(check(launch_spec_residual(info, b, x, r, N, nj, scale, part, rblocks, st), "residual"));
-        g_kernel_launches += 1;
-        TRY(check(cudaMemcpyAsync(hp.data(), part, rblocks * 8, cudaMemcpyDeviceToHost, st), "readback"));
-        TRY(check(cudaStreamSynchronize(st), "sync"));
-        double ss = 0.0;
-        for (double v : hp) ss += v;
-        rnorm = std::sqrt(ss);
-        if (outer == 0) bnorm = rnorm;
-        if (bnorm == 0.0 || rnorm <= rel_tol * bnorm || total_inner >= max_iter || outer >= 32) break;
-        SpecArgs a{};
-        a.ni = ni;
-        a.nj = nj;
-        a.N = N;
-        a.info = info;
-        a.scale = scale;
-        a.r = r;
-        a.d = d;
-        a.s = s;
-        a.q = q;
-        a.y = nullptr; // z = K K^T r is formed in one pass
-        a.z = z;
-        a.partials = partials;
-        a.count = count;
-        a.status = &sc->pcg_status;
-        a.iters = iters_dev;
-        // the inner solve only needs to bring the residual just below the
-        // target (never below what FP32 iterations reach)
-        a.eps_in = (float)std::min(std::max(0.3 * rel_tol * bnorm / rnorm, 1e-4), 0.5);
-        a.max_iter = max_iter - total_inner;
-        TRY(check(launch_spec_pcg(a, st), "inner PCG"));
-        TRY(check(launch_spec_update(x, d, N, st), "update"));
-        g_kernel_launches += 2;
-        int it = 0;
-        TRY(check(cudaMemcpyAsync(&it, iters_dev, sizeof(int), cudaMemcpyDeviceToHost, st), "readback"));
-        TRY(check(cudaMemcpyAsync(&h_status, &sc->pcg_status, sizeof(int), cudaMemcpyDeviceToHost, st),
-                  "readback"));
-        TRY(check(cudaStreamSynchronize(st), "sync"));
-        if (h_status != 0) {
-            release();
-            return fail(FS_ERR_TIMEOUT, "fs_pcg_solve_spec: a grid barrier wait timed out");
-        }
-        total_inner += it;
-        if (it == 0) break; // no progress possible
+    // the whole solve -- outer loop included -- enqueued at once
+    SpecSolve p{};
+    p.ni = ni;
+    p.nj = nj;
+    p.info = info;
+    p.b = b;
+    p.x = x;
+    p.dt = dt_dev;
+    p.density = density;
+    p.dx = dx;
+    p.r = r;
+    p.d = d;
+    p.s = s;
+    p.q = q;
+    p.z = z;
+    p.partials = partials;
+    p.rpart = rpart;
+    p.count = count;
+    p.status = &sc->pcg_status;
+    p.ctl = ctl;
+    p.iters_out = iters_dev;
+    p.rel_out = rel_dev;
+    p.tol = rel_tol;
+    p.max_iter = max_iter;
+    p.max_outer = kSpecMaxOuter;
+    TRY(check(launch_spec_chain(p, st), "solve"));
+    g_kernel_launches += 4 * kSpecMaxOuter + 2;
+    int h_status = 0, it = 0;
+    double rel = 0.0;
+    TRY(check(cudaMemcpyAsync(&h_status, &sc->pcg_status, sizeof(int), cudaMemcpyDeviceToHost, st), "readback"));
+    TRY(check(cudaMemcpyAsync(&it, iters_dev, sizeof(int), cudaMemcpyDeviceToHost, st), "readback"));
+    TRY(check(cudaMemcpyAsync(&rel, rel_dev, sizeof(double), cudaMemcpyDeviceToHost, st), "readback"));
+    TRY(check(cudaStreamSynchronize(st), "sync"));
+    if (h_status != 0) {
+        release();
+        return fail(FS_ERR_TIMEOUT, "fs_pcg_solve_spec: a grid barrier wait timed out");
     }
     TRY(check(cudaMemcpy(result, x, N * 8, cudaMemcpyDeviceToHost), "download"));
     release();
-    if (iterations) *iterations = total_inner;
-    if (rel_residual) *rel_residual = bnorm > 0.0 ? rnorm / bnorm : 0.0;
+    if (iterations) *iterations = it;
+    if (rel_residual) *rel_residual = rel;
     return FS_OK;
 }
 

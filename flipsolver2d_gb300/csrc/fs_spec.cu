@@ -66,9 +66,14 @@ __device__ __forceinline__ T spec_a(const uint8_t *__restrict__ info, const T *_
 // ---------------------------------------------------------------------------
 __global__ void k_spec_residual(const uint8_t *__restrict__ info, const double *__restrict__ b,
                                 const double *__restrict__ x, float *__restrict__ r32, long long N,
-                                int NJ, double scale, double *__restrict__ partial)
+                                int NJ, double scale, double *__restrict__ partial,
+                                const SpecCtl *ctl, const float *dt, double density, double dx)
 {
     __shared__ double sm[32];
+    if (ctl) {
+        if (*((volatile const int *)&ctl->done)) return;
+        scale = (double)*dt / (density * dx * dx);
+    }
     double acc = 0.0;
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < N;
          c += (long long)gridDim.x * blockDim.x) {
@@ -88,11 +93,45 @@ __global__ void k_spec_residual(const uint8_t *__restrict__ info, const double *
     }
 }
 
-__global__ void k_spec_update(double *__restrict__ x, const float *__restrict__ d, long long N)
+__global__ void k_spec_update(double *__restrict__ x, const float *__restrict__ d, long long N,
+                              const SpecCtl *ctl)
 {
+    if (ctl && *((volatile const int *)&ctl->done)) return;
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < N;
          c += (long long)gridDim.x * blockDim.x)
         x[c] += (double)d[c];
+}
+
+// the outer loop's decision: ||r||^2 from the residual partials (summed in a
+// fixed order), ||b||^2 the first time, stop or the next inner tolerance
+__global__ void k_spec_check(const double *__restrict__ partial, int nparts, SpecCtl *ctl, double tol,
+                             int max_iter, int max_outer, int *iters_out, double *rel_out)
+{
+    __shared__ double sm[32];
+    if (*((volatile const int *)&ctl->done)) return;
+    double v = 0.0;
+    for (int k = threadIdx.x; k < nparts; k += blockDim.x) v += partial[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double rr = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) rr += sm[w];
+        if (ctl->outer == 0) ctl->bb = rr;
+        const double bb = ctl->bb;
+        ctl->rr = rr;
+        const bool stop = bb == 0.0 || rr <= tol * tol * bb || ctl->total >= max_iter ||
+                          ctl->outer >= max_outer || (ctl->outer > 0 && ctl->last_it == 0);
+        // the inner solve needs to bring the residual just below the target
+        // (never below what FP32 iterations reach)
+        const double want = rr > 0.0 ? 0.3 * tol * sqrt(bb / rr) : 0.5;
+        ctl->eps_in = (float)fmin(fmax(want, 1e-4), 0.5);
+        ctl->outer++;
+        if (stop) ctl->done = 1;
+        if (iters_out) *iters_out = ctl->total;
+        if (rel_out) *rel_out = bb > 0.0 ? sqrt(rr / bb) : 0.0;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -213,12 +252,21 @@ __global__ void __launch_bounds__(kSpecThreads, 2) k_pcg_spec(SpecArgs a)
     const int G = gridDim.x;
     const long long stride = (long long)G * blockDim.x;
     const long long c0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    const float scale = (float)a.scale;
+    const float scale = a.dt ? (float)((double)*a.dt / (a.density * a.dx * a.dx)) : (float)a.scale;
     const uint8_t *__restrict__ info = a.info;
     float *__restrict__ r = a.r, *__restrict__ s = a.s, *__restrict__ q = a.q;
     float *__restrict__ z = a.z, *__restrict__ d = a.d;
     float2 *pA = a.partials, *pB = a.partials + G, *pC = a.partials + 2 * G;
     SpecGrid g{a.count, a.status, 0u};
+    float eps_in = a.eps_in;
+    int max_iter = a.max_iter;
+    if (a.ctl) {
+        // every block reads the same values before the first grid barrier;
+        // block 0 writes the totals back only after the last one
+        if (*((volatile const int *)&a.ctl->done)) return;
+        eps_in = *((volatile const float *)&a.ctl->eps_in);
+        max_iter = a.max_iter - *((volatile const int *)&a.ctl->total);
+    }
 
     // y = K^T r
     auto kt = [&](long long n) {
@@ -274,11 +322,11 @@ __global__ void __launch_bounds__(kSpecThreads, 2) k_pcg_spec(SpecArgs a)
     if (!spec_sync(g)) return;
     float2 sigma = spec_psum(pA, G, bc, 0);
     const float2 rr0 = spec_psum(pB, G, bc, 1);
-    const float stop = a.eps_in * a.eps_in * rr0.x;
+    const float stop = eps_in * eps_in * rr0.x;
     int it = 0;
     bool first = true;
     float fb = 0.f;
-    while (rr0.x > 0.f && it < a.max_iter) {
+    while (rr0.x > 0.f && it < max_iter) {
         // s = z + beta s, q = A s = A z + beta q, and s.q
         float sq = 0.f;
         sweep([&](long long c) {
@@ -326,7 +374,13 @@ __global__ void __launch_bounds__(kSpecThreads, 2) k_pcg_spec(SpecArgs a)
         sigma = nsig;
         first = false;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) *a.iters = it;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (a.iters) *a.iters = it;
+        if (a.ctl) {
+            a.ctl->total += it;
+            a.ctl->last_it = it;
+        }
+    }
 }
 
 static int spec_grid()
@@ -348,14 +402,15 @@ cudaError_t launch_spec_residual(const uint8_t *info, const double *b, const dou
                                  long long N, int NJ, double scale, double *partial, int nblocks,
                                  cudaStream_t st)
 {
-    k_spec_residual<<<nblocks, 256, 0, st>>>(info, b, x, r32, N, NJ, scale, partial);
+    k_spec_residual<<<nblocks, 256, 0, st>>>(info, b, x, r32, N, NJ, scale, partial, nullptr, nullptr, 0.0,
+                                             0.0);
     return cudaGetLastError();
 }
 
 cudaError_t launch_spec_update(double *x, const float *d, long long N, cudaStream_t st)
 {
     const int blocks = (int)((N + 255) / 256 < 4096 ? (N + 255) / 256 : 4096);
-    k_spec_update<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(x, d, N);
+    k_spec_update<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(x, d, N, nullptr);
     return cudaGetLastError();
 }
 
@@ -370,6 +425,49 @@ cudaError_t launch_spec_pcg(const SpecArgs &args, cudaStream_t st)
     void *kargs[] = {&a};
     return cudaLaunchCooperativeKernel((const void *)k_pcg_spec, dim3(grid), dim3(kSpecThreads), kargs,
                                        0, st);
+}
+
+cudaError_t launch_spec_chain(const SpecSolve &p, cudaStream_t st)
+{
+    const long long N = (long long)p.ni * p.nj;
+    cudaError_t e = cudaMemsetAsync(p.ctl, 0, sizeof(SpecCtl), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(p.x, 0, (size_t)N * 8, st);
+    if (e != cudaSuccess) return e;
+    const int ublocks = (int)((N + 255) / 256 < 4096 ? (N + 255) / 256 : 4096);
+    SpecArgs a{};
+    a.ni = p.ni;
+    a.nj = p.nj;
+    a.N = N;
+    a.info = p.info;
+    a.r = p.r;
+    a.d = p.d;
+    a.s = p.s;
+    a.q = p.q;
+    a.y = nullptr;
+    a.z = p.z;
+    a.partials = p.partials;
+    a.count = p.count;
+    a.status = p.status;
+    a.iters = nullptr;
+    a.eps_in = 1e-4f;
+    a.max_iter = p.max_iter;
+    a.ctl = p.ctl;
+    for (int round = 0;; round++) {
+        k_spec_residual<<<kSpecResBlocks, 256, 0, st>>>(p.info, p.b, p.x, p.r, N, p.nj, 0.0, p.rpart, p.ctl,
+                                                        p.dt, p.density, p.dx);
+        k_spec_check<<<1, 1024, 0, st>>>(p.rpart, kSpecResBlocks, p.ctl, p.tol, p.max_iter, p.max_outer,
+                                         p.iters_out, p.rel_out);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if (round == p.max_outer) break;
+        a.dt = p.dt; // the scale from the device dt, like the residual
+        a.density = p.density;
+        a.dx = p.dx;
+        e = launch_spec_pcg(a, st);
+        if (e != cudaSuccess) return e;
+        k_spec_update<<<ublocks > 0 ? ublocks : 1, 256, 0, st>>>(p.x, p.d, N, p.ctl);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 } // namespace fsg

@@ -6,6 +6,19 @@
 
 namespace fsg {
 
+// the state of one chained solve on the device (launch_spec_chain): the
+// outer loop's decisions live here, so the whole solve is enqueued at once
+struct SpecCtl {
+    double bb;    // ||b||^2 (the first check)
+    double rr;    // ||b - A x||^2 of the last check
+    float eps_in; // relative reduction asked of the next inner solve
+    int done;     // 1: stop (converged, out of iterations, or no progress)
+    int outer;    // checks run
+    int total;    // inner iterations so far
+    int last_it;  // inner iterations of the last inner solve
+    int pad;
+};
+
 struct SpecArgs {
     int ni, nj;
     long long N;
@@ -20,7 +33,36 @@ struct SpecArgs {
     int *iters;          // out: inner iterations
     float eps_in;        // relative reduction of the inner residual norm
     int max_iter;
+    SpecCtl *ctl;        // chained solves: skip when done, eps_in and the
+                         // remaining iterations from here, totals back here
+    const float *dt;     // when set: scale = *dt / (density dx^2) on the device
+    double density, dx;
 };
+
+// one whole spec-mode solve of A x = b enqueued on a stream with no host
+// synchronisation: x = 0, then max_outer rounds of FP64 residual, check,
+// inner FP32 PCG and FP64 update, then a last residual and check.  Each
+// kernel reads the control block and does nothing once the solve is done.
+constexpr int kSpecResBlocks = 1024;
+struct SpecSolve {
+    int ni, nj;
+    const uint8_t *info;
+    const double *b;
+    double *x;
+    const float *dt; // device: scale = dt / (density dx^2)
+    double density, dx;
+    float *r, *d, *s, *q, *z;  // N floats each
+    float2 *partials;          // spec_partials_needed()
+    double *rpart;             // kSpecResBlocks
+    unsigned *count;
+    int *status;
+    SpecCtl *ctl;
+    int *iters_out;   // optional: total inner iterations
+    double *rel_out;  // optional: final relative residual
+    double tol;
+    int max_iter, max_outer;
+};
+cudaError_t launch_spec_chain(const SpecSolve &p, cudaStream_t st);
 
 int spec_partials_needed();
 cudaError_t launch_spec_residual(const uint8_t *info, const double *b, const double *x, float *r32,

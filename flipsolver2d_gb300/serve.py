@@ -189,7 +189,7 @@ class Server:
 
 # ----------------------------------------------------------------- workload
 def serving_workload(n_requests: int, rate: float = 2000.0, seed: int = 9, pool: int = 32,
-                     frame_sides=(64, 512), solve_sides=(256, 512), solve_fraction: float = 0.2):
+                     frame_sides=(64, 1024), solve_sides=(256, 2048), solve_fraction: float = 0.2):
     """The serving workload: Poisson arrivals at `rate` per second from
     default_rng(seed); a fraction `solve_fraction` are standalone solves with
     a side log-uniform in `solve_sides` and the masks of scenes.poisson_case,

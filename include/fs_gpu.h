@@ -66,12 +66,13 @@ typedef struct fs_params {
  *   FS_PCG_FP64  the same in FP64, bit for bit the reference's
  *   FS_PCG_SPEC  every solve to a true relative residual of 1e-6: FP32 inner
  *                PCG with the textbook incomplete-Poisson preconditioner and
- *                FP64 refinement (fs_pcg_solve_spec's method), on one
- *                thread-block cluster; FP64 right-hand sides and pressures.
- *                For grids up to the on-chip limit of fs_pcg_solve_batch
- *                (fs_create fails with FS_ERR_UNSUPPORTED above it).  The
- *                density push is skipped when its solve hits 20000 inner
- *                iterations, the counterpart of the reference's limit test. */
+ *                FP64 refinement (fs_pcg_solve_spec's method); FP64
+ *                right-hand sides and pressures.  Up to the on-chip limit
+ *                of fs_pcg_solve_batch a solve runs on one thread-block
+ *                cluster, above it as the whole-GPU cooperative solve with
+ *                its outer loop on the device.  The density push is skipped
+ *                when its solve hits 20000 inner iterations, the counterpart
+ *                of the reference's limit test. */
 enum { FS_PCG_FP32 = 0, FS_PCG_FP64 = 1, FS_PCG_SPEC = 2 };
 
 /* Execution knobs with no counterpart in FlipSolverParameters. */
@@ -294,8 +295,10 @@ fs_status fs_pcg_solve_batch(fs_poisson_system *systems, int n, double rel_tol, 
  * fs_batch_step_frame   one whole frame of every member
  * fs_batch_run_frames   several frames of every member, pipelined
  * fs_batch_submit_solve   copy a standalone system (fs_pcg_solve_spec's
- *                   problem, host arrays; on-chip size limit as
- *                   fs_pcg_solve_batch) to the device; the next round solves it
+ *                   problem, host arrays, any size) to the device; the next
+ *                   round solves it (in the merged launch up to the on-chip
+ *                   limit of fs_pcg_solve_batch, as a chained cooperative
+ *                   solve above it)
  * fs_batch_solve_done / fs_batch_take_solve   its completion; take copies
  *                   result, iterations and rel_residual out and frees it
  * fs_batch_destroy  frees the batch; the members stay alive */

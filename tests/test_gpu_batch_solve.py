@@ -85,3 +85,18 @@ def test_autotuned_plan_is_used(port_lib, gpu_lib):
         assert rr <= REL_TOL and _true_rel(m, b, x, dx) <= 1.01 * REL_TOL
     with pytest.raises(gpu.FsError):
         gpu.cluster_autotune(700, 700)
+
+
+def test_batch_round_takes_a_large_system(port_lib, gpu_lib):
+    """A standalone system above the on-chip limit rides in a batch round as
+    a chained cooperative solve and equals the standalone spec solve."""
+    m, b, dx = scenes.poisson_case(600, seed=41)
+    it0, x0, rr0 = gpu.pcg_solve_spec(m, b, DT, DENSITY, dx, REL_TOL)
+    bt = gpu.Batch()
+    t = bt.submit_solve(m, b, DT, DENSITY, dx)
+    bt.round()
+    assert bt.solve_done(t)
+    it, x, rr = bt.take_solve(t)
+    assert rr <= REL_TOL and _true_rel(m, b, x, dx) <= 1.01 * REL_TOL
+    assert it == it0 and np.array_equal(x.view(np.uint64), x0.view(np.uint64))
+    bt.close()
