@@ -655,8 +655,8 @@ def solve_batch_arm(args):
 def serve_arm(args):
     """Serving loop (--serve R): R requests from a seeded Poisson stream at
     2000 per second (default_rng(9)), 80 % frame requests to 32 resident
-    scenes with sides log-uniform in [64, 512] and 20 % standalone solves of
-    sides log-uniform in [256, 512], served by continuous batching under a
+    scenes with sides log-uniform in [64, 1024] and 20 % standalone solves of
+    sides log-uniform in [256, 2048], served by continuous batching under a
     150 GB device-memory budget (flipsolver2d_gb300/serve.py).  Every scene
     first gets one warm-up frame so its creation, seeding and graph capture
     are outside the measurement.  `value` is frame work served per second of
@@ -667,7 +667,7 @@ def serve_arm(args):
     build.build()
     torch.cuda.set_device(0)
     specs, reqs = serve.serving_workload(args.serve, rate=2000.0, seed=9, pool=32,
-                                         frame_sides=(64, 512), solve_sides=(256, 512))
+                                         frame_sides=(64, 1024), solve_sides=(256, 2048))
     srv = serve.Server(budget_bytes=150e9)
     for k, sc in specs.items():
         srv.register_scene(k, sc)
@@ -693,7 +693,7 @@ def serve_arm(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded request stream, random scenes and star masks)",
         "config": {"workload": f"serve_{len(reqs)}_requests", "rate_per_s": 2000.0, "seed": 9,
-                   "scenes": len(specs), "frame_sides": [64, 512], "solve_sides": [256, 512],
+                   "scenes": len(specs), "frame_sides": [64, 1024], "solve_sides": [256, 2048],
                    "solve_fraction": 0.2, "budget_bytes": 150e9,
                    "pcg": "FS_PCG_SPEC, 1e-6 true relative residual",
                    "step": "one request", "parallelism": "single GPU"},
