@@ -134,11 +134,17 @@ class SceneObject:
     divergence: float = 0.0
 
 
+SIM_FLIP, SIM_NBFLIP = "flip", "nbflip"
+
+
 @dataclass
 class Scene:
     name: str
     params: FlipSolverParameters
     objects: List[SceneObject] = field(default_factory=list)
+    # the solver class the reference's scene reader picks from "simType":
+    # FlipSolver ("flip" / "fluid") or NBFlipSolver ("nbflip")
+    sim_type: str = SIM_FLIP
 
 
 def rect(i0: float, j0: float, i1: float, j1: float) -> np.ndarray:
@@ -209,6 +215,23 @@ def dam_break(resolution: int = 128, seed: int = 42, obstacle: bool = False,
         objs.append(SceneObject("solid", convex_polygon(rng, 6, 0.35, 0.65), friction=0.1))
     name = f"dam_break_{resolution}" + ("_obstacle" if obstacle else "")
     return Scene(name, p, objs)
+
+
+def nb_dam_break(resolution: int = 128, seed: int = 0, obstacle: bool = False,
+                 viscosity: float = 10.0, **overrides) -> Scene:
+    """NB-FLIP dam break (NBFlipSolver): the dam_break layout with 8
+    particles per cell, particle viscosity `viscosity` and an iteration limit
+    of 1000, stepped by the narrow-band solver.  NB-FLIP seeds no particles
+    at start; its first substep fills the band below the fluid surface."""
+    kw = dict(particlesPerCell=8, pcgIterLimit=1000)
+    kw.update(overrides)
+    sc = dam_break(resolution, seed=seed, obstacle=obstacle, **kw)
+    for o in sc.objects:
+        if o.kind == "fluid":
+            o.viscosity = float(viscosity)
+    sc.name = "nb_" + sc.name
+    sc.sim_type = SIM_NBFLIP
+    return sc
 
 
 def random_scene(side: int, seed: int, ppc: int = 4, **overrides) -> Scene:
@@ -313,8 +336,10 @@ def scene_from_json(source, name: str = "json") -> Scene:
     order as addObjectFromJson does (:255-287): "solid" -> addGeometry with
     its friction, "fluid" -> addInitialFluid with its viscosity, "sink" ->
     addSink with its divergence; disabled objects are skipped and vertices
-    are multiplied by the scene scale.  Solver types other than "flip" /
-    "fluid" and "source" objects raise UnsupportedScene."""
+    are multiplied by the scene scale.  "nbflip" selects NBFlipSolver
+    (jsonscenereader.cpp creates it for that simType).  Solver types other
+    than "flip" / "fluid" / "nbflip" and "source" objects raise
+    UnsupportedScene."""
     import json
     import os
 
@@ -328,8 +353,8 @@ def scene_from_json(source, name: str = "json") -> Scene:
         name = os.path.splitext(os.path.basename(str(source)))[0]
     st = doc["settings"]
     sim = st["simType"]
-    if sim not in ("flip", "fluid"):
-        raise UnsupportedScene(f"simType {sim!r}: only the plain FLIP liquid solver is on this path")
+    if sim not in ("flip", "fluid", "nbflip"):
+        raise UnsupportedScene(f"simType {sim!r}: only the FLIP and NB-FLIP liquid solvers are on this path")
 
     def get(key, default):
         return st[key] if key in st else default
@@ -374,4 +399,4 @@ def scene_from_json(source, name: str = "json") -> Scene:
             raise UnsupportedScene("source objects (emitters reseeding every substep) are not on this path")
         else:
             raise UnsupportedScene(f"object type {kind!r}")
-    return Scene(name, p, objs)
+    return Scene(name, p, objs, sim_type=SIM_NBFLIP if sim == "nbflip" else SIM_FLIP)

@@ -348,6 +348,9 @@ struct fso_solver {
     int nsinks;
 
     mt19937 rng;
+    /* NB-FLIP (nbflipsolver.h:63-75): the advected grids */
+    int nb;
+    float *adv_u, *adv_v, *adv_sdf, *adv_visc;
     int density_iters, pressure_iters, substeps;
     int ref_threads, host_threads;
     pool *pool;
@@ -632,6 +635,32 @@ fso_solver *fso_create(const fso_params *p)
     return s;
 }
 
+fso_solver *fso_create_nbflip(const fso_params *p) /* nbflipsolver.cpp:9-23 */
+{
+    fso_solver *s = fso_create(p);
+    s->nb = 1;
+    s->adv_u = (float *)calloc(s->nu, sizeof(float));
+    s->adv_v = (float *)calloc(s->nv, sizeof(float));
+    s->adv_sdf = (float *)calloc(s->ncell, sizeof(float));
+    s->adv_visc = (float *)calloc(s->ncell, sizeof(float));
+    return s;
+}
+
+int fso_get_rng(fso_solver *s, uint32_t state[625])
+{
+    memcpy(state, s->rng.mt, sizeof(s->rng.mt));
+    state[624] = (uint32_t)s->rng.idx;
+    return 0;
+}
+
+int fso_set_rng(fso_solver *s, const uint32_t state[625])
+{
+    if (state[624] > 624) return -1;
+    memcpy(s->rng.mt, state, sizeof(s->rng.mt));
+    s->rng.idx = (int)state[624];
+    return 0;
+}
+
 static void free_polys(poly *p, int n)
 {
     for (int i = 0; i < n; i++) free(p[i].xy);
@@ -654,7 +683,7 @@ void fso_destroy(fso_solver *s)
                     s->counts, s->u, s->v, s->su, s->sv, s->uvalid, s->vvalid, s->suvalid,
                     s->svvalid, s->visc_grid, s->known, s->divc, s->dens, s->dens_rhs, s->dens_p,
                     s->pres, s->pres_rhs, s->unit, s->mask, s->ucount, s->ipp, s->w_r,
-                    s->w_aux, s->w_s};
+                    s->w_aux, s->w_s, s->adv_u, s->adv_v, s->adv_sdf, s->adv_visc};
     for (size_t k = 0; k < sizeof(ptrs) / sizeof(ptrs[0]); k++) free(ptrs[k]);
     free_polys(s->obst, s->nobst);
     free_polys(s->fluids, s->nfluids);
@@ -765,8 +794,14 @@ static void seed_initial_fluid(fso_solver *s) /* :682-707 */
         }
 }
 
+static void nb_first_frame_init(fso_solver *s);
+
 void fso_first_frame_init(fso_solver *s)
 {
+    if (s->nb) {
+        nb_first_frame_init(s);
+        return;
+    }
     update_sinks(s);
     update_solids(s);
     update_initial_fluid(s);
@@ -1107,8 +1142,9 @@ static int linear_solve(fso_solver *s, double *result, const double *vec, int it
     return iterLimit;
 }
 
-static double project_tolerance(const fso_solver *s) /* flipsolver2d.cpp:73 */
+static double project_tolerance(const fso_solver *s) /* flipsolver2d.cpp:73; nbflipsolver.cpp:22 */
 {
+    if (s->nb) return 1e-6;
     return s->p.viscosityEnabled ? 1e-6 : 1e-2;
 }
 
@@ -1234,10 +1270,15 @@ static void p2g_range(void *ctx, size_t a, size_t b) /* :1329-1377 */
     }
 }
 
-static void centered_range(void *ctx, size_t a, size_t b) /* :1394-1431 */
+/* FlipSolver::centeredParamsToGridThread (:1394-1431); NB-FLIP's override
+ * (nbflipsolver.cpp:463-504) accumulates the same sums in the same order
+ * into the cleared grid and a weight grid starting at 1e-10, keeps weights
+ * with |w| > 1e-6 and divides only where a weight was kept, which is 0 / w
+ * otherwise: the result differs only in the threshold. */
+static void centered_range(void *ctx, size_t a, size_t b)
 {
     fso_solver *s = (fso_solver *)ctx;
-    const float threshold = 1e-9f;
+    const float threshold = s->nb ? 1e-6f : 1e-9f;
     for (size_t idx = a; idx < b; idx++) {
         long ci = (long)idx / s->nj, cj = (long)idx - ci * s->nj;
         long bl[9];
@@ -1249,7 +1290,7 @@ static void centered_range(void *ctx, size_t a, size_t b) /* :1394-1431 */
             const pbin *bin = &s->bins[bl[q]];
             for (size_t k = 0; k < bin->n; k++) {
                 float w = sm_qbspline(bin->pos[2 * k] - (float)ci, bin->pos[2 * k + 1] - (float)cj);
-                if (w > threshold) {
+                if ((s->nb ? fabsf(w) : w) > threshold) {
                     wT += w;
                     val += w * bin->visc[k];
                     valid = 1;
@@ -1332,18 +1373,21 @@ static void neighborhood(long si, long sj, long i, long j, long out[8])
         }
 }
 
-/* shared FIFO BFS of extrapolateLevelsetInside (flipsolver2d.cpp:1433-1494)
- * and simmath::breadthFirstExtrapolate (mathfuncs.cpp:152-215).
+/* shared FIFO BFS of extrapolateLevelsetInside (flipsolver2d.cpp:1433-1494),
+ * extrapolateLevelsetOutside (:1496-1558) and simmath::breadthFirstExtrapolate
+ * (mathfuncs.cpp:152-215).
  * mode 0: level set inside (seed: value > 0, no depth limit, value - 1);
- * mode 1: velocity (seed: flag set, depth limit `radius`, sets flags). */
+ * mode 1: velocity (seed: flag set, depth limit `radius`, sets flags);
+ * mode 2: level set outside (seed: value < si * sj, no depth limit, value + 1). */
 static void bfs_extrapolate(float *grid, uint8_t *flag, long si, long sj, int mode, int radius)
 {
     size_t n = (size_t)si * sj;
     int *markers = (int *)malloc(n * sizeof(int));
     size_t *queue = (size_t *)malloc(n * sizeof(size_t));
     size_t head = 0, tail = 0;
+    const float maxSdf = (float)n; /* :1500 */
     for (size_t k = 0; k < n; k++) {
-        int seed = mode == 0 ? (grid[k] > 0.f) : (flag[k] != 0);
+        int seed = mode == 0 ? (grid[k] > 0.f) : mode == 2 ? (grid[k] < maxSdf) : (flag[k] != 0);
         markers[k] = seed ? 0 : INT_MAX;
     }
     long nb[8];
@@ -1372,7 +1416,7 @@ static void bfs_extrapolate(float *grid, uint8_t *flag, long si, long sj, int mo
                 avg += grid[nb[q]];
                 count++;
             }
-            int lim_ok = mode == 0 ? (markers[index] <= 1e6) : (markers[index] <= radius);
+            int lim_ok = mode != 1 ? (markers[index] <= 1e6) : (markers[index] <= radius);
             if (markers[nb[q]] == INT_MAX && lim_ok) {
                 markers[nb[q]] = markers[index] + 1;
                 queue[tail++] = (size_t)nb[q];
@@ -1380,6 +1424,8 @@ static void bfs_extrapolate(float *grid, uint8_t *flag, long si, long sj, int mo
         }
         if (mode == 0) {
             grid[index] = (float)(avg / count - 1.f);
+        } else if (mode == 2) {
+            grid[index] = (float)(avg / count + 1.f);
         } else {
             grid[index] = (float)(avg / count);
             flag[index] = 1;
@@ -1545,6 +1591,172 @@ static void count_particles(fso_solver *s)
 }
 
 /* ------------------------------------------------------------------------ */
+/* NB-FLIP (nbflipsolver.cpp), without sources: no cell is a source and     */
+/* every emitter id is -1                                                   */
+/* ------------------------------------------------------------------------ */
+#define NB_NARROW_BAND (-3.f)      /* m_narrowBand,      nbflipsolver.cpp:20 */
+#define NB_COMBINATION_BAND (-2.f) /* m_combinationBand, :21 */
+#define NB_RESAMPLING_BAND (-1.f)  /* m_resamplingBand,  :22 */
+
+/* NBFlipSolver::pruneNarrowBand (:227-253).  Particles already marked (killed
+ * in advect, or moved: scheduleRebin marked the original and the copy in the
+ * rebin set keeps its unmarked flag) are skipped: marking them again changes
+ * nothing. */
+static void nb_prune_band(fso_solver *s)
+{
+    const int cap = 2 * s->p.particlesPerCell;
+    for (size_t b = 0; b < s->nbins; b++) {
+        pbin *bin = &s->bins[b];
+        for (size_t k = 0; k < bin->n; k++) {
+            if (bin->dead[k]) continue;
+            float x = bin->pos[2 * k], y = bin->pos[2 * k + 1];
+            long i = (long)x, j = (long)y; /* ssize_t i = position.x() */
+            float sdf = grid_lerp(s->fluid_sdf, s->ni, s->nj, 0.f, 0.f, x, y);
+            if (sdf < NB_NARROW_BAND) {
+                bin->dead[k] = 1;
+                continue;
+            }
+            if (sdf < NB_RESAMPLING_BAND && s->counts[i * s->nj + j] > cap) bin->dead[k] = 1;
+        }
+    }
+}
+
+/* FlipSolver::eulerAdvectionThread (flipsolver2d.cpp:340-351): every sample
+ * (i, j) of the output grid traced back with rk4Integrate(-dt) through the
+ * velocity grid, then the input grid (offset ox, oy) sampled there. */
+static void nb_euler(fso_solver *s, const float *in, int si, int sj, float ox, float oy, float *out)
+{
+    for (long i = 0; i < si; i++)
+        for (long j = 0; j < sj; j++) {
+            float x = (float)i, y = (float)j;
+            rk4(s, &x, &y, -s->step_dt);
+            out[i * sj + j] = grid_lerp(in, si, sj, ox, oy, x, y);
+        }
+}
+
+/* NBFlipSolver::advect (:66-109) */
+static void nb_advect(fso_solver *s)
+{
+    advect(s);
+    nb_prune_band(s);
+    nb_euler(s, s->u, s->ni + 1, s->nj, 0.5f, 0.f, s->adv_u);
+    nb_euler(s, s->v, s->ni, s->nj + 1, 0.f, 0.5f, s->adv_v);
+    nb_euler(s, s->fluid_sdf, s->ni, s->nj, 0.f, 0.f, s->adv_sdf);
+    nb_euler(s, s->visc_grid, s->ni, s->nj, 0.5f, 0.5f, s->adv_visc);
+}
+
+/* NBFlipSolver::afterTransfer (:111-116): FlipSolver::afterTransfer (sources
+ * only), updateGridFromSources (:332-364: with no source the distance stays
+ * FLT_MAX and the SDF becomes std::min(FLT_MAX, sdf)), combineAdvectedGrids
+ * (:366-427). */
+static void nb_after_transfer(fso_solver *s)
+{
+    const long ni = s->ni, nj = s->nj;
+    for (size_t k = 0; k < s->ncell; k++) {
+        float sdf = s->fluid_sdf[k];
+        s->fluid_sdf[k] = sdf < FLT_MAX ? sdf : FLT_MAX;
+    }
+    /* combineLevelset: std::min(advected + h, sdf), h = 1 */
+    for (size_t k = 0; k < s->ncell; k++) {
+        float a = s->adv_sdf[k] + 1.f, b = s->fluid_sdf[k];
+        s->fluid_sdf[k] = b < a ? b : a;
+    }
+    /* combineVelocityGrid: nbCombine(advected, particle, sdf) keeps the
+     * particle (transferred) value where sdf > m_combinationBand */
+    for (long i = 0; i < ni + 1; i++)
+        for (long j = 0; j < nj; j++) {
+            float sdf = grid_lerp(s->fluid_sdf, (int)ni, (int)nj, 0.f, 0.f, (float)i, 0.5f + (float)j);
+            long l = i * nj + j;
+            s->u[l] = sdf > NB_COMBINATION_BAND ? s->u[l] : s->adv_u[l];
+        }
+    for (long i = 0; i < ni; i++)
+        for (long j = 0; j < nj + 1; j++) {
+            float sdf = grid_lerp(s->fluid_sdf, (int)ni, (int)nj, 0.f, 0.f, 0.5f + (float)i, (float)j);
+            long l = i * (nj + 1) + j;
+            s->v[l] = sdf > NB_COMBINATION_BAND ? s->v[l] : s->adv_v[l];
+        }
+    /* combineCenteredGrids */
+    for (long i = 0; i < ni; i++)
+        for (long j = 0; j < nj; j++) {
+            float sdf = grid_lerp(s->fluid_sdf, (int)ni, (int)nj, 0.f, 0.f, 0.5f + (float)i,
+                                  (float)((double)j + 0.5));
+            long l = i * nj + j;
+            s->visc_grid[l] = sdf > NB_COMBINATION_BAND ? s->visc_grid[l] : s->adv_visc[l];
+        }
+}
+
+/* NBFlipSolver::reseedParticles (:118-201): cells inside the resampling band
+ * with fewer than particlesPerCell particles get jittered candidates; each
+ * candidate draws two numbers, and is kept unless its interpolated SDF is
+ * below the narrow band.  Kept particles are appended to the bin of their
+ * position with zero velocity; the viscosity is stored through the cell's
+ * bin at the index the position's bin returned (both are the same bin unless
+ * i + U(0,1) rounded up into the next bin).  A candidate whose position
+ * rounded out of the grid has no bin (the reference indexes past its bin
+ * array there) and is dropped. */
+static void nb_reseed(fso_solver *s)
+{
+    const int ppc = s->p.particlesPerCell;
+    for (long i = 0; i < s->ni; i++)
+        for (long j = 0; j < s->nj; j++) {
+            long l = i * s->nj + j;
+            float sc = s->fluid_sdf[l];
+            if (!(sc < NB_RESAMPLING_BAND && sc > NB_NARROW_BAND)) continue;
+            int additional = ppc - s->counts[l];
+            if (additional <= 0) continue;
+            pbin *cellbin = &s->bins[bin_of_cell(s, i, j)];
+            for (int q = 0; q < additional; q++) {
+                float x = (float)i + mt_uniform01f(&s->rng);
+                float y = (float)j + mt_uniform01f(&s->rng);
+                float nsdf = grid_lerp(s->fluid_sdf, s->ni, s->nj, 0.f, 0.f, x, y);
+                if (nsdf < NB_NARROW_BAND) continue;
+                float visc = grid_lerp(s->visc_grid, s->ni, s->nj, 0.5f, 0.5f, x, y);
+                long pb = bin_of_pos(s, x, y);
+                if (pb < 0) continue;
+                size_t idx = bin_push(&s->bins[pb], x, y, 0.f, 0.f, 0.f, 0);
+                if (idx < cellbin->n) cellbin->visc[idx] = visc;
+            }
+        }
+}
+
+/* NBFlipSolver::firstFrameInit (:203-211): updateSinks, updateSources (no
+ * sources), updateSolids, fluidSdfFromInitialFluid (:299-330), counts = 0,
+ * initialFluidSeed (:255-297), which adds no particle (its add is commented
+ * out in the reference) but draws two numbers per candidate: particlesPerCell
+ * candidates in every cell with a negative SDF. */
+static void nb_first_frame_init(fso_solver *s)
+{
+    update_sinks(s);
+    update_solids(s);
+    float dx = (float)s->dx;
+    for (long i = 0; i < s->ni; i++)
+        for (long j = 0; j < s->nj; j++) {
+            float dist = FLT_MAX;
+            int fluidId = -1;
+            for (int k = 0; k < s->nfluids; k++) {
+                /* (static_cast<float>(i)+0.5)*dx is evaluated in double */
+                float x = (float)(((double)(float)i + 0.5) * (double)dx);
+                float y = (float)(((double)(float)j + 0.5) * (double)dx);
+                float sdf = polygon_sdf(&s->fluids[k], x, y) / dx;
+                if (sdf < dist) {
+                    dist = sdf;
+                    fluidId = k;
+                }
+            }
+            long l = i * s->nj + j;
+            s->fluid_sdf[l] = dist;
+            if (dist < 0) {
+                s->material[l] = M_FLUID;
+                if (fluidId != -1) s->visc_grid[l] = s->fluids[fluidId].a;
+            }
+        }
+    memset(s->counts, 0, s->ncell * sizeof(int32_t));
+    for (size_t l = 0; l < s->ncell; l++)
+        if (s->fluid_sdf[l] < 0.f)
+            for (int q = 0; q < 2 * s->p.particlesPerCell; q++) (void)mt_next(&s->rng);
+}
+
+/* ------------------------------------------------------------------------ */
 /* driver                                                                   */
 /* ------------------------------------------------------------------------ */
 static int run_stage(fso_solver *s, int stage);
@@ -1561,7 +1773,10 @@ int fso_run_stage(fso_solver *s, int stage)
 static int run_stage(fso_solver *s, int stage)
 {
     switch (stage) {
-    case FSO_ADVECT: advect(s); break;
+    case FSO_ADVECT:
+        if (s->nb) nb_advect(s);
+        else advect(s);
+        break;
     case FSO_DECOMPOSITION: build_matrix(s); break;
     case FSO_REBIN: prune(s); rebin(s); break;
     case FSO_DENSITY:
@@ -1570,7 +1785,9 @@ static int run_stage(fso_solver *s, int stage)
     case FSO_P2G: particle_to_grid(s); break;
     case FSO_SDF: update_sdf(s); break;
     case FSO_MATERIALS: update_materials(s); break;
-    case FSO_AFTER_TRANSFER: break; /* sources only */
+    case FSO_AFTER_TRANSFER: /* sources only, plus NB-FLIP's grid combination */
+        if (s->nb) nb_after_transfer(s);
+        break;
     case FSO_LEVELSET: bfs_extrapolate(s->fluid_sdf, NULL, s->ni, s->nj, 0, 0); break;
     case FSO_VEL_EXTRAP: extrapolate_velocity(s); break;
     case FSO_SAVE_GRID:
@@ -1584,8 +1801,11 @@ static int run_stage(fso_solver *s, int stage)
     case FSO_FRICTION: friction(s); break;
     case FSO_G2P: g2p(s); break;
     case FSO_COUNT: count_particles(s); break;
-    case FSO_RESEED: break; /* sources only */
+    case FSO_RESEED: /* sources only, or NB-FLIP's band reseeding */
+        if (s->nb) nb_reseed(s);
+        break;
     case FSO_DENSITY_GRID: update_density_grid(s); break;
+    case FSO_LEVELSET_OUTSIDE: bfs_extrapolate(s->fluid_sdf, NULL, s->ni, s->nj, 2, 0); break;
     default: return -1;
     }
     return 0;
@@ -1597,6 +1817,15 @@ static void step(fso_solver *s) /* FlipSolver::step, flipsolver2d.cpp:412-462 */
                                 FSO_SDF, FSO_MATERIALS, FSO_AFTER_TRANSFER, FSO_LEVELSET,
                                 FSO_VEL_EXTRAP, FSO_SAVE_GRID, FSO_BODY_FORCES, FSO_PROJECT,
                                 FSO_FRICTION, FSO_VEL_EXTRAP, FSO_G2P, FSO_COUNT, FSO_RESEED};
+    /* NBFlipSolver::step (nbflipsolver.cpp:26-64), gridUpdate (:213-225) */
+    static const int nb_order[] = {FSO_ADVECT, FSO_REBIN, FSO_P2G, FSO_VEL_EXTRAP, FSO_SAVE_GRID,
+                                   FSO_SDF, FSO_LEVELSET_OUTSIDE, FSO_AFTER_TRANSFER, FSO_LEVELSET,
+                                   FSO_MATERIALS, FSO_BODY_FORCES, FSO_DECOMPOSITION, FSO_PROJECT,
+                                   FSO_FRICTION, FSO_VEL_EXTRAP, FSO_G2P, FSO_COUNT, FSO_RESEED};
+    if (s->nb) {
+        for (size_t k = 0; k < sizeof(nb_order) / sizeof(nb_order[0]); k++) run_stage(s, nb_order[k]);
+        return;
+    }
     for (size_t k = 0; k < sizeof(order) / sizeof(order[0]); k++) run_stage(s, order[k]);
 }
 
@@ -1705,6 +1934,9 @@ size_t fso_grid_bytes(fso_solver *s, int which)
     case FSO_G_V_VALID: return s->nv;
     case FSO_G_DENSITY_RHS: case FSO_G_DENSITY_PRESSURE: case FSO_G_PRESSURE:
     case FSO_G_PRESSURE_RHS: return n * 8;
+    case FSO_G_ADVECTED_U: return s->nb ? s->nu * 4 : 0;
+    case FSO_G_ADVECTED_V: return s->nb ? s->nv * 4 : 0;
+    case FSO_G_ADVECTED_SDF: case FSO_G_ADVECTED_VISCOSITY: return s->nb ? n * 4 : 0;
     default: return 0;
     }
 }
@@ -1732,6 +1964,10 @@ static void *grid_ptr(fso_solver *s, int which)
     case FSO_G_PRESSURE: return s->pres;
     case FSO_G_PRESSURE_RHS: return s->pres_rhs;
     case FSO_G_EMITTER_ID: return s->emitter_id;
+    case FSO_G_ADVECTED_U: return s->adv_u;
+    case FSO_G_ADVECTED_V: return s->adv_v;
+    case FSO_G_ADVECTED_SDF: return s->adv_sdf;
+    case FSO_G_ADVECTED_VISCOSITY: return s->adv_visc;
     default: return NULL;
     }
 }

@@ -77,8 +77,24 @@ enum fso_stage {
     FSO_COUNT = 15,        /* countParticles()                           :459 */
     FSO_RESEED = 16,       /* reseedParticles()                          :460 */
     FSO_DENSITY_GRID = 17, /* updateDensityGrid() alone                  :166 */
-    FSO_STAGE_COUNT = 18
+    FSO_LEVELSET_OUTSIDE = 18, /* extrapolateLevelsetOutside(m_fluidSdf)  :1496-1558 */
+    FSO_STAGE_COUNT = 19
 };
+
+/* NB-FLIP (NBFlipSolver, nbflipsolver.cpp) runs the same stage ids; four of
+ * them are its overrides:
+ *   FSO_ADVECT          NBFlipSolver::advect: FlipSolver::advect, then
+ *                       pruneNarrowBand and the semi-Lagrangian advection of
+ *                       u, v, the fluid SDF and the viscosity     :66-109, 227-253
+ *   FSO_P2G             particleToGrid with NBFlipSolver::centeredParamsToGrid
+ *                                                                  :445-504
+ *   FSO_AFTER_TRANSFER  FlipSolver::afterTransfer, updateGridFromSources,
+ *                       combineAdvectedGrids                       :111-116, 332-427
+ *   FSO_RESEED          NBFlipSolver::reseedParticles              :118-201
+ * and its step (:26-64) is advect, rebin, P2G, extrapolation, saved grid,
+ * SDF, outside level set, after transfer, inside level set, materials, body
+ * forces, decomposition, projection, friction, extrapolation, G2P, count,
+ * reseed. */
 
 /* Grids that can be read and written. */
 enum fso_grid {
@@ -102,7 +118,11 @@ enum fso_grid {
     FSO_G_PRESSURE = 17,       /* double NI*NJ     projection pressure   */
     FSO_G_PRESSURE_RHS = 18,   /* double NI*NJ     projection RHS        */
     FSO_G_EMITTER_ID = 19,     /* int32  NI*NJ     m_emitterId           */
-    FSO_G_COUNT = 20
+    FSO_G_ADVECTED_U = 20,     /* float  (NI+1)*NJ NB-FLIP m_advectedVelocity U */
+    FSO_G_ADVECTED_V = 21,     /* float  NI*(NJ+1) NB-FLIP m_advectedVelocity V */
+    FSO_G_ADVECTED_SDF = 22,   /* float  NI*NJ     NB-FLIP m_advectedSdf       */
+    FSO_G_ADVECTED_VISCOSITY = 23, /* float NI*NJ  NB-FLIP m_advectedViscosity */
+    FSO_G_COUNT = 24
 };
 
 enum fso_stat {
@@ -116,7 +136,15 @@ enum fso_stat {
 typedef struct fso_solver fso_solver;
 
 fso_solver *fso_create(const fso_params *p);
+/* NBFlipSolver(const NBFlipParameters *) (nbflipsolver.cpp:9-23);
+ * NBFlipParameters adds nothing to FlipSolverParameters. */
+fso_solver *fso_create_nbflip(const fso_params *p);
 void fso_destroy(fso_solver *s);
+
+/* The solver's std::mt19937 (m_randEngine, flipsolver2d.h:371): the 624
+ * state words and the position of the next word, in this order. */
+int fso_get_rng(fso_solver *s, uint32_t state[625]);
+int fso_set_rng(fso_solver *s, const uint32_t state[625]);
 
 /* Scene objects; vertices are (x, y) pairs in scene units (metres). */
 int fso_add_geometry(fso_solver *s, float friction, const float *xy, int n);

@@ -25,12 +25,17 @@ PORT_LIB = os.path.join(HERE, "_build", "libfsoracle.so")
 # stage ids (fsoracle.h enum fso_stage)
 ADVECT, DECOMPOSITION, REBIN, DENSITY, P2G, SDF, MATERIALS, AFTER_TRANSFER, LEVELSET, \
     VEL_EXTRAP, SAVE_GRID, BODY_FORCES, PROJECT, FRICTION, G2P, COUNT, RESEED, \
-    DENSITY_GRID = range(18)
+    DENSITY_GRID, LEVELSET_OUTSIDE = range(19)
 
 # the order in which FlipSolver::step() (flipsolver2d.cpp:412-462) runs them
 STEP_STAGES = [ADVECT, DECOMPOSITION, REBIN, DENSITY, P2G, SDF, MATERIALS, AFTER_TRANSFER,
                LEVELSET, VEL_EXTRAP, SAVE_GRID, BODY_FORCES, PROJECT, FRICTION, VEL_EXTRAP,
                G2P, COUNT, RESEED]
+
+# NBFlipSolver::step (nbflipsolver.cpp:26-64) with gridUpdate (:213-225)
+NB_STEP_STAGES = [ADVECT, REBIN, P2G, VEL_EXTRAP, SAVE_GRID, SDF, LEVELSET_OUTSIDE,
+                  AFTER_TRANSFER, LEVELSET, MATERIALS, BODY_FORCES, DECOMPOSITION, PROJECT,
+                  FRICTION, VEL_EXTRAP, G2P, COUNT, RESEED]
 
 # grid ids and numpy dtypes (fsoracle.h enum fso_grid)
 GRIDS: Dict[str, tuple] = {
@@ -44,11 +49,14 @@ GRIDS: Dict[str, tuple] = {
     "density_rhs": (15, np.float64, "c"), "density_pressure": (16, np.float64, "c"),
     "pressure": (17, np.float64, "c"), "pressure_rhs": (18, np.float64, "c"),
     "emitter_id": (19, np.int32, "c"),
+    "advected_u": (20, np.float32, "u"), "advected_v": (21, np.float32, "v"),
+    "advected_sdf": (22, np.float32, "c"), "advected_viscosity": (23, np.float32, "c"),
 }
 STATE_GRIDS = ["material", "solid_sdf", "fluid_sdf", "u", "v", "u_valid", "v_valid",
                "saved_u", "saved_v", "viscosity", "known_centered", "density",
                "particle_counts", "solid_id", "div_control", "density_rhs",
                "density_pressure", "emitter_id"]
+NB_GRIDS = ["advected_u", "advected_v", "advected_sdf", "advected_viscosity"]
 
 _libs: Dict[str, ctypes.CDLL] = {}
 
@@ -57,7 +65,8 @@ def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
     vp, c_int, c_float, c_double = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_double
     sz = ctypes.c_size_t
     sig = {
-        "fso_create": (vp, [vp]), "fso_destroy": (None, [vp]),
+        "fso_create": (vp, [vp]), "fso_create_nbflip": (vp, [vp]), "fso_destroy": (None, [vp]),
+        "fso_get_rng": (c_int, [vp, vp]), "fso_set_rng": (c_int, [vp, vp]),
         "fso_add_geometry": (c_int, [vp, c_float, vp, c_int]),
         "fso_add_initial_fluid": (c_int, [vp, c_float, vp, c_int]),
         "fso_add_sink": (c_int, [vp, c_float, vp, c_int]),
@@ -115,7 +124,9 @@ class OracleSolver:
         self.scene = scene
         self._cp = scene.params.to_c()
         self.ni, self.nj = self._cp.gridSizeI, self._cp.gridSizeJ
-        self.h = self.lib.fso_create(ctypes.byref(self._cp))
+        self.nb = getattr(scene, "sim_type", "flip") == "nbflip"
+        create = self.lib.fso_create_nbflip if self.nb else self.lib.fso_create
+        self.h = create(ctypes.byref(self._cp))
         for o in scene.objects:
             v = np.ascontiguousarray(o.verts, dtype=np.float32)
             if o.kind == "solid":
@@ -210,17 +221,32 @@ class OracleSolver:
         a = np.ascontiguousarray(a, dtype=dt).reshape(self.grid_shape(name))
         assert self.lib.fso_set_grid(self.h, gid, _ptr(a)) == 0
 
+    def get_rng(self) -> np.ndarray:
+        """The std::mt19937 state: 624 words and the index of the next one."""
+        st = np.zeros(625, np.uint32)
+        assert self.lib.fso_get_rng(self.h, _ptr(st)) == 0
+        return st
+
+    def set_rng(self, st: np.ndarray):
+        st = np.ascontiguousarray(st, np.uint32)
+        assert st.shape == (625,) and self.lib.fso_set_rng(self.h, _ptr(st)) == 0
+
+    def state_grids(self):
+        return STATE_GRIDS + (NB_GRIDS if self.nb else [])
+
     def snapshot(self) -> dict:
-        s = {"particles": self.get_particles(), "dt": self.dt}
-        for g in STATE_GRIDS:
+        s = {"particles": self.get_particles(), "dt": self.dt, "rng": self.get_rng()}
+        for g in self.state_grids():
             s[g] = self.get_grid(g)
         return s
 
     def restore(self, snap: dict):
         self.set_particles(snap["particles"])
-        for g in STATE_GRIDS:
+        for g in self.state_grids():
             if g in snap:
                 self.set_grid(g, snap[g])
+        if "rng" in snap:
+            self.set_rng(snap["rng"])
         self.set_dt(snap["dt"])
 
 

@@ -12,15 +12,60 @@
 #include "fsoracle.h"
 
 #include <cstring>
+#include <sstream>
+#include <type_traits>
 #include <vector>
 
 #include "flipsolver2d.h"
+#include "nbflipsolver.h"
 
 namespace {
 
-class RefSolver : public FlipSolver {
+// what the C interface calls, for either solver class
+struct RefApi {
+    virtual ~RefApi() = default;
+    virtual void runStage(int stage) = 0;
+    virtual void stepOnce() = 0;
+    virtual void frame() = 0;
+    virtual void setStepDt(float dt) = 0;
+    virtual float getStepDt() = 0;
+    virtual void firstInit() = 0;
+    virtual float maxVel() = 0;
+    virtual size_t gridBytes(int which) = 0;
+    virtual int getGrid(int which, void *out) = 0;
+    virtual int setGrid(int which, const void *in) = 0;
+    virtual size_t binCount() = 0;
+    virtual size_t nParticles() = 0;
+    virtual void getParticles(int32_t *counts, float *pos, float *vel, float *visc, uint8_t *dead) = 0;
+    virtual void setParticles(const int32_t *counts, const float *pos, const float *vel,
+                              const float *visc, const uint8_t *dead) = 0;
+    virtual int stat(int which) = 0;
+    virtual int getRng(uint32_t *state) = 0;
+    virtual int setRng(const uint32_t *state) = 0;
+    virtual void addGeom(Obstacle &o) = 0;
+    virtual void addFluid(Emitter &e) = 0;
+    virtual void addSinkObj(Sink &k) = 0;
+};
+
+// Base: FlipSolver or NBFlipSolver.  The stages reach the protected methods
+// step() calls; virtual dispatch selects NB-FLIP's overrides of advect,
+// afterTransfer, centeredParamsToGrid, reseedParticles, firstFrameInit and
+// step.
+template <class Base> class RefSolverT : public Base, public RefApi {
 public:
-    explicit RefSolver(const FlipSolverParameters *p) : FlipSolver(p) {}
+    using Base::m_stats; using Base::m_stepDt; using Base::m_viscosityPropertyIndex;
+    using Base::m_sizeI; using Base::m_sizeJ; using Base::m_materialGrid; using Base::m_solidSdf;
+    using Base::m_fluidSdf; using Base::m_fluidVelocityGrid; using Base::m_savedFluidVelocityGrid;
+    using Base::m_viscosityGrid; using Base::m_knownCenteredParams; using Base::m_densityGrid;
+    using Base::m_fluidParticleCounts; using Base::m_solidId; using Base::m_divergenceControl;
+    using Base::m_pressureRhs; using Base::m_pressureSolverResult; using Base::m_emitterId;
+    using Base::m_markerParticles; using Base::m_pressureMatrix; using Base::m_pressurePrecond;
+    using Base::m_pressureSolver; using Base::m_pcgIterLimit; using Base::m_projectTolerance;
+    using Base::m_viscosityEnabled; using Base::m_randEngine;
+    using Base::getPressureProjectionMatrix; using Base::getIPPCoefficients; using Base::cellCount;
+    using Base::calcPressureRhs;
+
+    template <class P> explicit RefSolverT(const P *p) : Base(p) {}
 
     bool capturePressure = true;
     std::vector<double> capRhs;
@@ -43,57 +88,98 @@ public:
         FlipSolver::project();
     }
 
-    void runStage(int stage)
+    void runStage(int stage) override
     {
         switch (stage) {
-        case FSO_ADVECT: advect(); break;
+        case FSO_ADVECT: this->advect(); break;
         case FSO_DECOMPOSITION:
             m_pressureMatrix = getPressureProjectionMatrix();
             m_pressurePrecond = getIPPCoefficients(m_pressureMatrix);
             break;
         case FSO_REBIN:
-            pruneParticles();
+            this->pruneParticles();
             m_markerParticles.rebinParticles();
             break;
         case FSO_DENSITY:
             m_stats.reset(); // report this stage's solve
-            if (!m_viscosityEnabled) densityCorrection();
+            if (!m_viscosityEnabled) this->densityCorrection();
             break;
-        case FSO_P2G: particleToGrid(); break;
-        case FSO_SDF: updateSdf(); break;
-        case FSO_MATERIALS: updateMaterials(); break;
-        case FSO_AFTER_TRANSFER: afterTransfer(); break;
-        case FSO_LEVELSET: extrapolateLevelsetInside(m_fluidSdf); break;
+        case FSO_P2G: this->particleToGrid(); break;
+        case FSO_SDF: this->updateSdf(); break;
+        case FSO_MATERIALS: this->updateMaterials(); break;
+        case FSO_AFTER_TRANSFER: this->afterTransfer(); break;
+        case FSO_LEVELSET: this->extrapolateLevelsetInside(m_fluidSdf); break;
+        case FSO_LEVELSET_OUTSIDE: this->extrapolateLevelsetOutside(m_fluidSdf); break;
         case FSO_VEL_EXTRAP: m_fluidVelocityGrid.extrapolate(10); break;
         case FSO_SAVE_GRID: m_savedFluidVelocityGrid = m_fluidVelocityGrid; break;
-        case FSO_BODY_FORCES: applyBodyForces(); break;
+        case FSO_BODY_FORCES: this->applyBodyForces(); break;
         case FSO_PROJECT:
             m_stats.reset();
             project();
             break;
-        case FSO_FRICTION: updateVelocityFromSolids(); break;
-        case FSO_G2P: particleUpdate(); break;
-        case FSO_COUNT: countParticles(); break;
-        case FSO_RESEED: reseedParticles(); break;
-        case FSO_DENSITY_GRID: updateDensityGrid(); break;
+        case FSO_FRICTION: this->updateVelocityFromSolids(); break;
+        case FSO_G2P: this->particleUpdate(); break;
+        case FSO_COUNT: this->countParticles(); break;
+        case FSO_RESEED: this->reseedParticles(); break;
+        case FSO_DENSITY_GRID: this->updateDensityGrid(); break;
         default: break;
         }
     }
 
-    void stepOnce()
+    void stepOnce() override
     {
         m_stats.reset();
-        step();
+        this->step();
     }
+    void frame() override { this->stepFrame(); }
 
-    void setStepDt(float dt) { m_stepDt = dt; }
-    void firstInit() { firstFrameInit(); }
-    float maxVel() { return maxParticleVelocity(); }
+    void setStepDt(float dt) override { m_stepDt = dt; }
+    float getStepDt() override { return this->stepDt(); }
+    void firstInit() override { this->firstFrameInit(); }
+    float maxVel() override { return this->maxParticleVelocity(); }
+    size_t nParticles() override { return this->particleCount(); }
+    void addGeom(Obstacle &o) override { this->addGeometry(o); }
+    void addFluid(Emitter &e) override { this->addInitialFluid(e); }
+    void addSinkObj(Sink &k) override { this->addSink(k); }
+
+    // libstdc++ writes the 624 state words, then the position of the next one
+    int getRng(uint32_t *state) override
+    {
+        std::ostringstream os;
+        os << m_randEngine;
+        std::istringstream is(os.str());
+        for (int k = 0; k < 625; k++) {
+            unsigned long v = 0;
+            if (!(is >> v)) return -1;
+            state[k] = static_cast<uint32_t>(v);
+        }
+        return 0;
+    }
+    int setRng(const uint32_t *state) override
+    {
+        std::ostringstream os;
+        for (int k = 0; k < 625; k++) os << state[k] << (k < 624 ? " " : "");
+        std::istringstream is(os.str());
+        is >> m_randEngine;
+        return is.fail() ? -1 : 0;
+    }
+    int stat(int which) override
+    {
+        switch (which) {
+        case FSO_S_DENSITY_ITERS: return m_stats.densityIterations();
+        case FSO_S_PRESSURE_ITERS: return m_stats.pressureIterations();
+        case FSO_S_SUBSTEPS: return m_stats.substepCount();
+        case FSO_S_FRAME: return this->frameNumber();
+        case FSO_S_POOL_THREADS: return static_cast<int>(ThreadPool::i()->threadCount());
+        default: return -1;
+        }
+    }
+    static constexpr bool kNb = std::is_same_v<Base, NBFlipSolver>;
 
     size_t viscIndex() const { return m_viscosityPropertyIndex; }
     const SolverStats &stats() const { return m_stats; }
 
-    size_t gridBytes(int which)
+    size_t gridBytes(int which) override
     {
         const size_t n = static_cast<size_t>(m_sizeI) * m_sizeJ;
         const size_t nu = static_cast<size_t>(m_sizeI + 1) * m_sizeJ;
@@ -110,6 +196,9 @@ public:
         case FSO_G_PARTICLE_COUNTS: case FSO_G_SOLID_ID: case FSO_G_EMITTER_ID: return n * 4;
         case FSO_G_DENSITY_RHS: case FSO_G_DENSITY_PRESSURE: case FSO_G_PRESSURE:
         case FSO_G_PRESSURE_RHS: return n * 8;
+        case FSO_G_ADVECTED_U: return kNb ? nu * 4 : 0;
+        case FSO_G_ADVECTED_V: return kNb ? nv * 4 : 0;
+        case FSO_G_ADVECTED_SDF: case FSO_G_ADVECTED_VISCOSITY: return kNb ? n * 4 : 0;
         default: return 0;
         }
     }
@@ -135,7 +224,7 @@ public:
         for (size_t i = 0; i < v.size(); i++) v[i] = p[i] != 0;
     }
 
-    int getGrid(int which, void *out)
+    int getGrid(int which, void *out) override
     {
         const size_t bytes = gridBytes(which);
         switch (which) {
@@ -159,12 +248,19 @@ public:
         case FSO_G_PRESSURE: getVec(capPressure, out, bytes); break;
         case FSO_G_PRESSURE_RHS: getVec(capRhs, out, bytes); break;
         case FSO_G_EMITTER_ID: getVec(m_emitterId.data(), out, bytes); break;
+        case FSO_G_ADVECTED_U: case FSO_G_ADVECTED_V: case FSO_G_ADVECTED_SDF:
+        case FSO_G_ADVECTED_VISCOSITY:
+            if constexpr (kNb) {
+                getVec(nbGrid(which), out, bytes);
+                break;
+            }
+            return -1;
         default: return -1;
         }
         return 0;
     }
 
-    int setGrid(int which, const void *in)
+    int setGrid(int which, const void *in) override
     {
         const size_t bytes = gridBytes(which);
         switch (which) {
@@ -188,14 +284,21 @@ public:
         case FSO_G_PRESSURE: setVec(capPressure, in, bytes); break;
         case FSO_G_PRESSURE_RHS: setVec(capRhs, in, bytes); break;
         case FSO_G_EMITTER_ID: std::memcpy(m_emitterId.data().data(), in, bytes); break;
+        case FSO_G_ADVECTED_U: case FSO_G_ADVECTED_V: case FSO_G_ADVECTED_SDF:
+        case FSO_G_ADVECTED_VISCOSITY:
+            if constexpr (kNb) {
+                std::memcpy(nbGrid(which).data(), in, bytes);
+                break;
+            }
+            return -1;
         default: return -1;
         }
         return 0;
     }
 
-    size_t binCount() { return m_markerParticles.bins().linearSize(); }
+    size_t binCount() override { return m_markerParticles.bins().linearSize(); }
 
-    void getParticles(int32_t *counts, float *pos, float *vel, float *visc, uint8_t *dead)
+    void getParticles(int32_t *counts, float *pos, float *vel, float *visc, uint8_t *dead) override
     {
         auto &bins = m_markerParticles.bins().data();
         size_t k = 0;
@@ -215,7 +318,7 @@ public:
     }
 
     void setParticles(const int32_t *counts, const float *pos, const float *vel,
-                      const float *visc, const uint8_t *dead)
+                      const float *visc, const uint8_t *dead) override
     {
         auto &bins = m_markerParticles.bins().data();
         size_t k = 0;
@@ -229,6 +332,21 @@ public:
                 if (dead[k]) bin.markForDeath(idx);
             }
         }
+    }
+
+    // the advected grids of NB-FLIP (nbflipsolver.h:63-66)
+    std::vector<float> &nbGrid(int which)
+    {
+        if constexpr (kNb) {
+            switch (which) {
+            case FSO_G_ADVECTED_U: return this->m_advectedVelocity.velocityGridU().data();
+            case FSO_G_ADVECTED_V: return this->m_advectedVelocity.velocityGridV().data();
+            case FSO_G_ADVECTED_SDF: return this->m_advectedSdf.data();
+            default: return this->m_advectedViscosity.data();
+            }
+        }
+        static std::vector<float> none;
+        return none;
     }
 
     // LinearSolver::solve on the system built from the current material grid.
@@ -279,7 +397,10 @@ Geometry2d polygon(const float *xy, int n)
     return g;
 }
 
-RefSolver *S(fso_solver *s) { return reinterpret_cast<RefSolver *>(s); }
+using RefSolver = RefSolverT<FlipSolver>;
+using RefNBSolver = RefSolverT<NBFlipSolver>;
+
+RefApi *S(fso_solver *s) { return reinterpret_cast<RefApi *>(s); }
 
 } // namespace
 
@@ -292,16 +413,29 @@ fso_solver *fso_create(const fso_params *p)
     // JsonSceneReader::loadJson calls this right after construction
     // (jsonscenereader.cpp:64); it registers the viscosity particle property.
     s->initAdditionalParameters();
-    return reinterpret_cast<fso_solver *>(s);
+    return reinterpret_cast<fso_solver *>(static_cast<RefApi *>(s));
+}
+
+fso_solver *fso_create_nbflip(const fso_params *p)
+{
+    FlipSolverParameters r = toRef(p);
+    NBFlipParameters nr;
+    static_cast<FlipSolverParameters &>(nr) = r;
+    RefNBSolver *s = new RefNBSolver(&nr);
+    s->initAdditionalParameters();
+    return reinterpret_cast<fso_solver *>(static_cast<RefApi *>(s));
 }
 
 void fso_destroy(fso_solver *s) { delete S(s); }
+
+int fso_get_rng(fso_solver *s, uint32_t state[625]) { return S(s)->getRng(state); }
+int fso_set_rng(fso_solver *s, const uint32_t state[625]) { return S(s)->setRng(state); }
 
 int fso_add_geometry(fso_solver *s, float friction, const float *xy, int n)
 {
     Geometry2d g = polygon(xy, n);
     Obstacle o(friction, g);
-    S(s)->addGeometry(o);
+    S(s)->addGeom(o);
     return 0;
 }
 
@@ -316,7 +450,7 @@ int fso_add_initial_fluid(fso_solver *s, float viscosity, const float *xy, int n
     e.setDivergence(0.f);
     e.setVelocity(Vec3());
     e.setVelocityTransfer(false);
-    S(s)->addInitialFluid(e);
+    S(s)->addFluid(e);
     return 0;
 }
 
@@ -324,14 +458,14 @@ int fso_add_sink(fso_solver *s, float divergence, const float *xy, int n)
 {
     Geometry2d g = polygon(xy, n);
     Sink k(divergence, g);
-    S(s)->addSink(k);
+    S(s)->addSinkObj(k);
     return 0;
 }
 
 void fso_first_frame_init(fso_solver *s) { S(s)->firstInit(); }
-void fso_step_frame(fso_solver *s) { S(s)->stepFrame(); }
+void fso_step_frame(fso_solver *s) { S(s)->frame(); }
 void fso_set_step_dt(fso_solver *s, float dt) { S(s)->setStepDt(dt); }
-float fso_step_dt(fso_solver *s) { return S(s)->stepDt(); }
+float fso_step_dt(fso_solver *s) { return S(s)->getStepDt(); }
 void fso_step(fso_solver *s) { S(s)->stepOnce(); }
 float fso_max_particle_velocity(fso_solver *s) { return S(s)->maxVel(); }
 
@@ -343,7 +477,7 @@ int fso_run_stage(fso_solver *s, int stage)
 }
 
 size_t fso_bin_count(fso_solver *s) { return S(s)->binCount(); }
-size_t fso_particle_count(fso_solver *s) { return S(s)->particleCount(); }
+size_t fso_particle_count(fso_solver *s) { return S(s)->nParticles(); }
 
 void fso_get_particles(fso_solver *s, int32_t *counts, float *pos, float *vel, float *visc,
                        uint8_t *dead)
@@ -361,18 +495,7 @@ size_t fso_grid_bytes(fso_solver *s, int which) { return S(s)->gridBytes(which);
 int fso_get_grid(fso_solver *s, int which, void *out) { return S(s)->getGrid(which, out); }
 int fso_set_grid(fso_solver *s, int which, const void *in) { return S(s)->setGrid(which, in); }
 
-int fso_stat(fso_solver *s, int which)
-{
-    RefSolver *r = S(s);
-    switch (which) {
-    case FSO_S_DENSITY_ITERS: return r->stats().densityIterations();
-    case FSO_S_PRESSURE_ITERS: return r->stats().pressureIterations();
-    case FSO_S_SUBSTEPS: return r->stats().substepCount();
-    case FSO_S_FRAME: return r->frameNumber();
-    case FSO_S_POOL_THREADS: return static_cast<int>(ThreadPool::i()->threadCount());
-    default: return -1;
-    }
-}
+int fso_stat(fso_solver *s, int which) { return S(s)->stat(which); }
 
 int fso_pcg_solve(int ni, int nj, const int8_t *material, float dt, double density,
                   double dx, const double *rhs, double *result, int iter_limit, double tol)

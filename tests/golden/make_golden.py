@@ -29,7 +29,8 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-FRAME_SCENES = ["dam32", "random40"]
+FRAME_SCENES = ["dam32", "random40", "nbdam40"]
+NB_FRAMES = 5  # NB-FLIP seeds its first particles at the end of frame 1
 FLUID, SOLID, EMPTY = 0x40, 0x20, 0x10
 
 
@@ -37,7 +38,8 @@ def scene_by_name(name):
     from flipsolver2d_gb300 import scenes
 
     return {"dam32": lambda: scenes.dam_break(32, seed=42),
-            "random40": lambda: scenes.random_scene(40, 1001)}[name]()
+            "random40": lambda: scenes.random_scene(40, 1001),
+            "nbdam40": lambda: scenes.nb_dam_break(40, seed=3, obstacle=True)}[name]()
 
 
 def parse_matviz(ref: str):
@@ -113,20 +115,23 @@ def make_matviz(ref: str):
     return len(units)
 
 
-def make_frames(frames: int = 3):
+def make_frames(frames: int = 3, names=FRAME_SCENES):
+    """NB-FLIP scenes also record the advected grids and the engine state."""
     import fsoracle as fo
 
-    for name in FRAME_SCENES:
+    for name in names:
         s = fo.OracleSolver(scene_by_name(name), "ref")
         out = {"pool_threads": np.int32(s.stat(4))}
-        for f in range(1, frames + 1):
+        for f in range(1, (NB_FRAMES if s.nb else frames) + 1):
             s.step_frame()
             p = s.get_particles()
             for k, v in p.items():
                 out[f"f{f}_{k}"] = v
             for g in ["material", "fluid_sdf", "u", "v", "u_valid", "v_valid", "density",
-                      "particle_counts", "pressure"]:
+                      "particle_counts", "pressure"] + (fo.NB_GRIDS + ["viscosity"] if s.nb else []):
                 out[f"f{f}_{g}"] = s.get_grid(g)
+            if s.nb:
+                out[f"f{f}_rng"] = s.get_rng()
             out[f"f{f}_stats"] = np.array([s.stat(0), s.stat(1), s.stat(2)], np.int32)
             out[f"f{f}_dt"] = np.float32(s.dt)
         np.savez_compressed(os.path.join(HERE, f"frames_{name}.npz"), **out)
@@ -136,13 +141,15 @@ def make_frames(frames: int = 3):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("FS_REFERENCE_DIR", "/root/reference"))
+    ap.add_argument("--only", nargs="*", default=None, help="frame scenes to regenerate")
     a = ap.parse_args()
     os.environ["FS_REFERENCE_DIR"] = a.reference
     import build as oracle_build
 
     oracle_build.build_ref()
-    print("matviz units:", make_matviz(a.reference))
-    make_frames()
+    if a.only is None:
+        print("matviz units:", make_matviz(a.reference))
+    make_frames(names=a.only if a.only is not None else FRAME_SCENES)
     print("frames written")
 
 

@@ -60,12 +60,22 @@ def test_defaults_follow_the_reference():
 
 
 @pytest.mark.parametrize("doc,what", [
-    ({"settings": {"simType": "nbflip"}, "solver": {"objects": []}}, "simType"),
     ({"settings": {"simType": "smoke"}, "solver": {"objects": []}}, "simType"),
+    ({"settings": {"simType": "fire"}, "solver": {"objects": []}}, "simType"),
 ])
 def test_unsupported_solvers(doc, what):
     with pytest.raises(scenes.UnsupportedScene, match=what):
         scenes.scene_from_json(doc)
+
+
+def test_nbflip_selects_the_narrow_band_solver():
+    doc = {"settings": {"simType": "nbflip", "domainSizeI": 5, "domainSizeJ": 5, "resolution": 32,
+                        "fps": 30, "particlesPerCell": 8},
+           "solver": {"objects": [{"type": "fluid", "viscosity": 10,
+                                   "verts": [[2, 0.3], [2, 1.3], [4.7, 1.3], [4.7, 0.3]]}]}}
+    sc = scenes.scene_from_json(doc)
+    assert sc.sim_type == scenes.SIM_NBFLIP and sc.objects[0].viscosity == 10
+    assert scenes.scene_from_json(DAM_JSON).sim_type == scenes.SIM_FLIP
 
 
 def test_sources_are_refused():
@@ -83,7 +93,7 @@ REF_SCENES = os.path.join(oracle_build.reference_dir(), "Liquid2dRender", "scene
 
 @pytest.mark.skipif(not os.path.isdir(REF_SCENES), reason="reference scene files not present")
 def test_reference_scene_files_parse_or_are_refused():
-    loaded, refused = 0, 0
+    loaded, refused, nb = 0, 0, 0
     for fn in sorted(os.listdir(REF_SCENES)):
         if not fn.endswith(".json"):
             continue
@@ -95,4 +105,29 @@ def test_reference_scene_files_parse_or_are_refused():
         dx, gi, gj = sc.params.grid()
         assert gi > 0 and gj > 0 and dx > 0 and sc.objects
         loaded += 1
+        nb += sc.sim_type == scenes.SIM_NBFLIP
     assert loaded >= 1 and loaded + refused >= 10
+    assert nb >= 2  # dam_break.json and level_eq.json: NB-FLIP without sources
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_SCENES), reason="reference scene files not present")
+def test_reference_nbflip_scene_runs_the_same_on_both_oracles(port_lib, ref_lib):
+    """The reference's NB-FLIP dam break file, at a reduced resolution, on the
+    reference build and on the C restatement: identical particles, grids and
+    engine state frame by frame."""
+    import fsoracle as fo
+
+    sc = scenes.scene_from_json(os.path.join(REF_SCENES, "dam_break.json"))
+    assert sc.sim_type == scenes.SIM_NBFLIP
+    sc.params.resolution = 64
+    r, p = fo.OracleSolver(sc, "ref"), fo.OracleSolver(sc, "port")
+    for _ in range(6):
+        r.step_frame()
+        p.step_frame()
+        pr, pp = r.get_particles(), p.get_particles()
+        for k in pr:
+            assert np.array_equal(pr[k], pp[k]), k
+        for g in r.state_grids():
+            assert np.array_equal(r.get_grid(g), p.get_grid(g), equal_nan=True), g
+        assert np.array_equal(r.get_rng(), p.get_rng())
+    assert r.particle_count() > 0
