@@ -26,6 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 UNITS = {
     "fs_particles.cu": ["-fmad=false"],
     "fs_grid.cu": ["-fmad=false"],
+    "fs_nbflip.cu": ["-fmad=false"],
     "fs_api.cu": ["-fmad=false"],
     "fs_pcg.cu": ["-fmad=true"],
     "fs_pcg_tma.cu": ["-fmad=true"],

@@ -17,12 +17,14 @@
 #include <atomic>
 #include <cfloat>
 #include <chrono>
+#include <climits>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <random>
+#include <sstream>
 #include <string>
 #include <thread>
 #include <vector>
@@ -198,6 +200,11 @@ struct fs_solver {
     float *d_obst_friction = nullptr;
     bool friction_dirty = true;
     std::mt19937 rng; // m_randEngine (flipsolver2d.cpp:71), persists across calls
+    bool nb = false;  // NBFlipSolver (nbflipsolver.cpp); its engine state lives in R.rng
+    NbGrids N;
+    NbReseed R;
+    int nb_max_cand = 0;     // particlesPerCell candidates per cell at most
+    void *nb_scan = nullptr; // scan scratch for the candidate counts
     int frame = 0;
     float step_dt = 0.f, frame_dt = 0.f;
     bool initialized = false;
@@ -292,7 +299,11 @@ static fs_status upload_particles(fs_solver *s, const std::vector<int> &counts,
 {
     const int nb = s->P.nbins;
     const int total = (int)pos.size();
-    if (total > s->P.cap || s->P.pos == nullptr) TRY(alloc_particles(s, total));
+    if (total > s->P.cap || s->P.pos == nullptr) {
+        // NB-FLIP keeps room for 2 particlesPerCell per cell (reseeding)
+        const long long keep = s->nb ? 2LL * s->p.particlesPerCell * (long long)s->ncell : 0;
+        TRY(alloc_particles(s, (int)std::max<long long>(total, keep)));
+    }
     std::vector<int> start(nb + 1, 0), slot_bin(total);
     for (int b = 0; b < nb; b++) start[b + 1] = start[b] + counts[b];
     for (int b = 0; b < nb; b++)
@@ -344,7 +355,7 @@ static fs_status sync_all(fs_solver *s)
     return FS_OK;
 }
 
-extern "C" fs_status fs_create(const fs_params *p, const fs_exec_params *exec, fs_solver **out)
+static fs_status create_impl(const fs_params *p, const fs_exec_params *exec, bool nb, fs_solver **out)
 {
     if (!p || !out) return fail(FS_ERR_BAD_ARG, "fs_create: null argument");
     *out = nullptr;
@@ -355,8 +366,11 @@ extern "C" fs_status fs_create(const fs_params *p, const fs_exec_params *exec, f
         return fail(FS_ERR_BAD_ARG, "fs_create: grid too large");
     if (p->viscosityEnabled)
         return fail(FS_ERR_UNSUPPORTED, "fs_create: viscosity is not part of this path");
-    if (p->simulationMethod != 0)
-        return fail(FS_ERR_UNSUPPORTED, "fs_create: only SIMULATION_LIQUID is supported");
+    // SIMULATION_LIQUID, or SIMULATION_NBFLIP for the narrow-band solver
+    if (p->simulationMethod != 0 && !(nb && p->simulationMethod == 3))
+        return fail(FS_ERR_UNSUPPORTED, "fs_create: only the liquid solvers are supported");
+    if (nb && (long long)p->gridSizeI * p->gridSizeJ * p->particlesPerCell * 2 > INT_MAX)
+        return fail(FS_ERR_BAD_ARG, "fs_create_nbflip: particle capacity above 2^31");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
         return fail(FS_ERR_CUDA, "fs_create: no CUDA device");
@@ -398,6 +412,7 @@ extern "C" fs_status fs_create(const fs_params *p, const fs_exec_params *exec, f
     sp.parameterHandlingMethod = p->parameterHandlingMethod;
     sp.viscosityEnabled = p->viscosityEnabled;
     sp.projectTolerance = p->viscosityEnabled ? 1e-6 : 1e-2; // flipsolver2d.cpp:73
+    if (nb) sp.projectTolerance = 1e-6;                       // nbflipsolver.cpp:22
     s->step_dt = 1.f / p->fps; // flipsolver2d.cpp:46-47
     s->frame_dt = 1.f / p->fps;
     s->rng = std::mt19937(p->seed);
@@ -591,10 +606,100 @@ extern "C" fs_status fs_create(const fs_params *p, const fs_exec_params *exec, f
     ok = ok && cudaMemsetAsync(s->sc, 0, sizeof(Scalars), q) == cudaSuccess;
     ok = ok && cudaStreamSynchronize(q) == cudaSuccess;
     if (!ok) return cleanup(fail(FS_ERR_CUDA, "fs_create: initialisation failed"));
-    A(alloc_particles(s, 0));
+    if (nb) {
+        // NB-FLIP: after countParticles every cell holds at most
+        // 2 particlesPerCell, and reseeding tops band cells up to
+        // particlesPerCell, so 2 particlesPerCell per cell bounds the count
+        s->nb = true;
+        const int ppc = p->particlesPerCell;
+        A(alloc_particles(s, (int)(2LL * ppc * (long long)n)));
+        NbGrids &N = s->N;
+        A(dalloc(s, &N.adv_u, s->nu));
+        A(dalloc(s, &N.adv_v, s->nv));
+        A(dalloc(s, &N.adv_sdf, n));
+        A(dalloc(s, &N.adv_visc, n));
+        s->nb_max_cand = (int)((long long)ppc * (long long)n);
+        const size_t mc = (size_t)s->nb_max_cand;
+        NbReseed &R = s->R;
+        R.ncell = (int)n;
+        A(dalloc(s, &R.rng, 625));
+        A(dalloc(s, &R.cand_n, n));
+        A(dalloc(s, &R.cand_off, n + 1));
+        A(dalloc(s, &R.draws, 2 * mc));
+        A(dalloc(s, &R.cand_pos, mc));
+        A(dalloc(s, &R.cand_visc, mc));
+        A(dalloc(s, &R.cand_bin, mc));
+        A(dalloc(s, &R.cand_cb, mc));
+        A(dalloc(s, &R.pos_of, mc));
+        A(dalloc(s, &R.cross, (size_t)kNbCrossMax));
+        A(dalloc(s, &R.cross_n, 1));
+        R.status = &s->sc->nb_overflow;
+        char *scan = nullptr;
+        A(dalloc(s, &scan, scan_scratch_bytes((int)n)));
+        s->nb_scan = scan;
+        ok = true;
+        for (float *g : {N.adv_u, N.adv_v}) ok = ok && cudaMemsetAsync(g, 0, (g == N.adv_u ? s->nu : s->nv) * 4, q) == cudaSuccess;
+        for (float *g : {N.adv_sdf, N.adv_visc}) ok = ok && cudaMemsetAsync(g, 0, n * 4, q) == cudaSuccess;
+        uint32_t st0[625];
+        mt_seed_host(st0, p->seed); // m_randEngine = std::mt19937(p->seed), flipsolver2d.cpp:71
+        ok = ok && cudaMemcpyAsync(R.rng, st0, sizeof(st0), cudaMemcpyHostToDevice, q) == cudaSuccess;
+        ok = ok && cudaStreamSynchronize(q) == cudaSuccess;
+        if (!ok) return cleanup(fail(FS_ERR_CUDA, "fs_create_nbflip: initialisation failed"));
+    } else {
+        A(alloc_particles(s, 0));
+    }
     *out = s;
     return FS_OK;
 #undef A
+}
+
+extern "C" fs_status fs_create(const fs_params *p, const fs_exec_params *exec, fs_solver **out)
+{
+    return create_impl(p, exec, false, out);
+}
+
+extern "C" fs_status fs_create_nbflip(const fs_params *p, const fs_exec_params *exec, fs_solver **out)
+{
+    return create_impl(p, exec, true, out);
+}
+
+extern "C" fs_status fs_get_rng_state(fs_solver *s, uint32_t *state)
+{
+    if (!s || !state) return fail(FS_ERR_BAD_ARG, "null argument");
+    TRY(set_device(s));
+    if (s->nb) {
+        TRY(sync_all(s));
+        CK(cudaMemcpy(state, s->R.rng, 625 * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        return FS_OK;
+    }
+    // libstdc++ writes the 624 state words, then the index of the next one
+    std::ostringstream os;
+    os << s->rng;
+    std::istringstream is(os.str());
+    for (int k = 0; k < 625; k++) {
+        unsigned long v = 0;
+        if (!(is >> v)) return fail(FS_ERR_CUDA, "fs_get_rng_state: unexpected engine format");
+        state[k] = (uint32_t)v;
+    }
+    return FS_OK;
+}
+
+extern "C" fs_status fs_set_rng_state(fs_solver *s, const uint32_t *state)
+{
+    if (!s || !state) return fail(FS_ERR_BAD_ARG, "null argument");
+    if (state[624] > 624) return fail(FS_ERR_BAD_ARG, "fs_set_rng_state: index above 624");
+    TRY(set_device(s));
+    if (s->nb) {
+        TRY(sync_all(s));
+        CK(cudaMemcpy(s->R.rng, state, 625 * sizeof(uint32_t), cudaMemcpyHostToDevice));
+        return FS_OK;
+    }
+    std::ostringstream os;
+    for (int k = 0; k < 625; k++) os << state[k] << (k < 624 ? " " : "");
+    std::istringstream is(os.str());
+    is >> s->rng;
+    if (is.fail()) return fail(FS_ERR_BAD_ARG, "fs_set_rng_state: rejected state");
+    return FS_OK;
 }
 
 extern "C" fs_status fs_destroy(fs_solver *s)
@@ -699,11 +804,33 @@ extern "C" fs_status fs_first_frame_init(fs_solver *s)
         CK(cudaMemcpy(dval, val.data(), val.size() * 4, cudaMemcpyHostToDevice));
     }
     // updateSinks, updateSources (none), updateSolids, updateInitialFluid
-    launch_scene_classify(d, s->G, (float)s->p.dx, dxy, doff, dkind, dval, (int)s->polys.size(), s->st);
+    launch_scene_classify(d, s->G, (float)s->p.dx, dxy, doff, dkind, dval, (int)s->polys.size(),
+                          s->nb, s->st);
     g_kernel_launches += 1;
     CK(cudaGetLastError());
     s->friction_dirty = true;
     TRY(ensure_friction(s));
+    if (s->nb) {
+        // NBFlipSolver::initialFluidSeed (nbflipsolver.cpp:255-297) adds no
+        // particle but draws two numbers for each of particlesPerCell
+        // candidates in every cell with a negative SDF
+        std::vector<float> sdf(s->ncell);
+        CK(cudaMemcpyAsync(sdf.data(), s->G.fluid_sdf, s->ncell * 4, cudaMemcpyDeviceToHost, s->st));
+        std::vector<uint32_t> rs(625);
+        CK(cudaMemcpyAsync(rs.data(), s->R.rng, 625 * 4, cudaMemcpyDeviceToHost, s->st));
+        CK(cudaStreamSynchronize(s->st));
+        unsigned long long neg = 0;
+        for (float v : sdf) neg += v < 0.f;
+        mt_discard_host(rs.data(), neg * 2ULL * (unsigned long long)s->p.particlesPerCell);
+        CK(cudaMemcpyAsync(s->R.rng, rs.data(), 625 * 4, cudaMemcpyHostToDevice, s->st));
+        CK(cudaStreamSynchronize(s->st));
+        dfree(s, dxy);
+        dfree(s, doff);
+        dfree(s, dkind);
+        dfree(s, dval);
+        s->initialized = true;
+        return FS_OK;
+    }
     // seedInitialFluid (flipsolver2d.cpp:682-707) on the host
     std::vector<int8_t> mat(s->ncell);
     std::vector<float> visc(s->ncell), u(s->nu), v(s->nv);
@@ -887,6 +1014,10 @@ static fs_status stage(fs_solver *s, int which, bool in_step)
     case FS_STAGE_ADVECT:
         launch_advect(d, s->P, s->G, s->sc, q);
         g_kernel_launches += 1;
+        if (s->nb) { // NBFlipSolver::advect: narrow band, then the grids (:66-109)
+            launch_nb_advect_extra(d, s->sp, s->P, s->G, s->N, s->sc, q);
+            g_kernel_launches += 2;
+        }
         s->after_advect = true;
         break;
     case FS_STAGE_DECOMPOSITION:
@@ -923,23 +1054,45 @@ static fs_status stage(fs_solver *s, int which, bool in_step)
         break;
     case FS_STAGE_P2G:
         TRY(wait_side(s)); // the previous level-set pass writes the fluid SDF
-        launch_p2g_sdf_materials(d, s->sp, s->P, s->G, q);
+        launch_p2g_sdf_materials(d, s->sp, s->P, s->G, s->nb, q);
         g_kernel_launches += 1;
         break;
-    case FS_STAGE_SDF:
-    case FS_STAGE_MATERIALS:
-    case FS_STAGE_AFTER_TRANSFER:
-    case FS_STAGE_RESEED:
+    case FS_STAGE_SDF: // fused into FS_STAGE_P2G
+        break;
+    case FS_STAGE_MATERIALS: // fused into FS_STAGE_P2G, except for NB-FLIP
+        if (s->nb) {
+            launch_nb_materials(d, s->G, q);
+            g_kernel_launches += 1;
+        }
+        break;
+    case FS_STAGE_AFTER_TRANSFER: // sources only, plus NB-FLIP's combination
+        if (s->nb) {
+            launch_nb_combine(d, s->G, s->N, q);
+            g_kernel_launches += 2;
+        }
+        break;
+    case FS_STAGE_RESEED: // sources only, or NB-FLIP's band reseeding
+        if (s->nb) {
+            launch_nb_candidates(d, s->sp, s->G, s->R, s->nb_scan, q);
+            launch_nb_append(s->P, s->R, s->nb_max_cand, s->rebin_scratch, q);
+            int bits = 0;
+            while ((1 << bits) < s->P.nbins) bits++;
+            g_kernel_launches += 6 + 16 + 5 * ((bits + 7) / 8);
+        }
+        break;
+    case FS_STAGE_LEVELSET_OUTSIDE:
+        launch_levelset(d, s->G, true, q);
+        g_kernel_launches += 1 + levelset_max_passes(d);
         break;
     case FS_STAGE_LEVELSET:
-        if (in_step) {
+        if (in_step && !s->nb) {
             CK(cudaEventRecord(s->ev_p2g, q));
             CK(cudaStreamWaitEvent(s->side, s->ev_p2g, 0));
-            launch_levelset(d, s->G, s->side);
+            launch_levelset(d, s->G, false, s->side);
             CK(cudaEventRecord(s->ev_levelset, s->side));
             s->levelset_pending = true;
         } else {
-            launch_levelset(d, s->G, q);
+            launch_levelset(d, s->G, false, q);
         }
         g_kernel_launches += 1 + levelset_max_passes(d);
         break;
@@ -991,18 +1144,9 @@ static fs_status stage(fs_solver *s, int which, bool in_step)
 // pressure apply here, then extrapolation and G2P); count and reseed
 static const int kStageOfGroup[9] = {0, 1, 3, 2, 5, 6, 7, 10, 11};
 
-static fs_status step_impl(fs_solver *s)
+// FlipSolver::step (flipsolver2d.cpp:412-462)
+template <class Mark> static fs_status step_flip(fs_solver *s, bool timed, Mark &mark)
 {
-    TRY(ensure_friction(s));
-    const bool timed = s->timers && s->stage_ev[0];
-    int group = 0;
-    auto mark = [&]() -> fs_status {
-        if (timed) CK(cudaEventRecord(s->stage_ev[group++], s->st));
-        return FS_OK;
-    };
-    if (s->timers) CK(cudaEventRecord(s->e0, s->st));
-    k_set_dt<<<1, 1, 0, s->st>>>(s->sc, s->step_dt);
-    g_kernel_launches += 1;
     TRY(stage(s, FS_STAGE_ADVECT, true));
     TRY(mark());
     TRY(stage(s, FS_STAGE_DECOMPOSITION, true));
@@ -1025,6 +1169,46 @@ static fs_status step_impl(fs_solver *s)
     TRY(stage(s, FS_STAGE_G2P, true));
     TRY(mark());
     TRY(stage(s, FS_STAGE_COUNT, true));
+    return FS_OK;
+}
+
+// NBFlipSolver::step (nbflipsolver.cpp:26-64) ends its stages as: advection;
+// rebin; particle to grid (P2G, extrapolation, saved grid); after transfer
+// (inside gridUpdate, :213-225: SDF, outside level set, combination, inside
+// level set); grid update (materials, body forces); decomposition; pressure;
+// particle update; reseed
+static const int kNbStageOfGroup[9] = {0, 3, 4, 6, 5, 1, 7, 10, 11};
+
+static fs_status step_impl(fs_solver *s)
+{
+    TRY(ensure_friction(s));
+    const bool timed = s->timers && s->stage_ev[0];
+    int group = 0;
+    auto mark = [&]() -> fs_status {
+        if (timed) CK(cudaEventRecord(s->stage_ev[group++], s->st));
+        return FS_OK;
+    };
+    if (s->timers) CK(cudaEventRecord(s->e0, s->st));
+    k_set_dt<<<1, 1, 0, s->st>>>(s->sc, s->step_dt);
+    g_kernel_launches += 1;
+    if (s->nb) {
+        static const int groups[9][4] = {
+            {FS_STAGE_ADVECT, -1},
+            {FS_STAGE_REBIN, -1},
+            {FS_STAGE_P2G, FS_STAGE_VEL_EXTRAP, FS_STAGE_SAVE_GRID, -1},
+            {FS_STAGE_LEVELSET_OUTSIDE, FS_STAGE_AFTER_TRANSFER, FS_STAGE_LEVELSET, -1},
+            {FS_STAGE_MATERIALS, FS_STAGE_BODY_FORCES, -1},
+            {FS_STAGE_DECOMPOSITION, -1},
+            {FS_STAGE_PROJECT, -1}, // + updateVelocityFromSolids
+            {FS_STAGE_VEL_EXTRAP, FS_STAGE_G2P, -1},
+            {FS_STAGE_COUNT, FS_STAGE_RESEED, -1}};
+        for (int g = 0; g < 9; g++) {
+            for (int k = 0; k < 4 && groups[g][k] >= 0; k++) TRY(stage(s, groups[g][k], true));
+            if (g < 8) TRY(mark());
+        }
+    } else {
+        TRY(step_flip(s, timed, mark));
+    }
     if (s->timers) {
         TRY(wait_side(s));
         CK(cudaEventRecord(s->e1, s->st));
@@ -1033,11 +1217,12 @@ static fs_status step_impl(fs_solver *s)
         CK(cudaEventElapsedTime(&ms, s->e0, s->e1));
         s->t_step_ms += ms;
         if (timed) {
+            const int *of = s->nb ? kNbStageOfGroup : kStageOfGroup;
             cudaEvent_t prev = s->e0;
             for (int g = 0; g < 9; g++) {
                 cudaEvent_t cur = g < 8 ? s->stage_ev[g] : s->e1;
                 CK(cudaEventElapsedTime(&ms, prev, cur));
-                s->t_stage_ms[kStageOfGroup[g]] += ms;
+                s->t_stage_ms[of[g]] += ms;
                 prev = cur;
             }
         }
@@ -1054,6 +1239,11 @@ static fs_status read_scalars(fs_solver *s)
     CK(cudaStreamSynchronize(s->st));
     if (s->sc_host->pcg_status != 0)
         return fail(FS_ERR_TIMEOUT, "a PCG grid barrier wait timed out");
+    if (s->sc_host->nb_overflow != 0)
+        return fail(FS_ERR_UNSUPPORTED,
+                    "NB-FLIP reseeding: more than %d candidates left their cell's bin, or the "
+                    "particles exceeded the capacity (more than 2 particlesPerCell in a cell)",
+                    kNbCrossMax);
     return FS_OK;
 }
 
@@ -1283,7 +1473,11 @@ extern "C" fs_status fs_set_particles(fs_solver *s, const int32_t *bin_counts, c
     // straight from the caller's memory; the slot-to-bin map is built on the
     // device
     const int nb = s->P.nbins;
-    if ((int)total > s->P.cap || s->P.pos == nullptr) TRY(alloc_particles(s, (int)total));
+    if ((int)total > s->P.cap || s->P.pos == nullptr) {
+        // NB-FLIP keeps room for 2 particlesPerCell per cell (reseeding)
+        const long long keep = s->nb ? 2LL * s->p.particlesPerCell * (long long)s->ncell : 0;
+        TRY(alloc_particles(s, (int)std::max<long long>((long long)total, keep)));
+    }
     std::vector<int> start(nb + 1, 0);
     for (int b = 0; b < nb; b++) start[b + 1] = start[b] + counts[b];
     Particles &P = s->P;
@@ -1336,6 +1530,10 @@ static bool grid_ref(fs_solver *s, int which, GridRef &g)
     case FS_GRID_PRESSURE: g = {s->pres_x, n, e, 8, true}; return true;
     case FS_GRID_PRESSURE_RHS: g = {s->pres_rhs, n, e, 8, true}; return true;
     case FS_GRID_EMITTER_ID: g = {s->G.emitter_id, n, 4, 4, false}; return true;
+    case FS_GRID_ADVECTED_U: g = {s->N.adv_u, s->nu, 4, 4, false}; return s->nb;
+    case FS_GRID_ADVECTED_V: g = {s->N.adv_v, s->nv, 4, 4, false}; return s->nb;
+    case FS_GRID_ADVECTED_SDF: g = {s->N.adv_sdf, n, 4, 4, false}; return s->nb;
+    case FS_GRID_ADVECTED_VISCOSITY: g = {s->N.adv_visc, n, 4, 4, false}; return s->nb;
     default: return false;
     }
 }
@@ -1692,6 +1890,7 @@ extern "C" fs_status fs_batch_add(fs_batch *b, fs_solver *s)
     TRY(batch_check_handle(b, s, "fs_batch_add"));
     if (batch_find(b, s)) return fail(FS_ERR_BAD_ARG, "fs_batch_add: the handle is already a member");
     if (b->free_slots.empty()) return fail(FS_ERR_BAD_ARG, "fs_batch_add: the batch is full (%d)", fs_batch::kSlots);
+    if (s->nb) return fail(FS_ERR_UNSUPPORTED, "fs_batch_add: NB-FLIP scenes step on their own");
     CK(cudaSetDevice(b->device));
     BatchScene bs;
     bs.s = s;

@@ -54,7 +54,7 @@ __device__ float polygon_sdf(const float *__restrict__ xy, int n, float px, floa
 // 2 sink (value = divergence)
 __global__ void k_scene_classify(GridDims d, Grids G, float dx, const float *__restrict__ xy,
                                  const int *__restrict__ off, const int *__restrict__ kind,
-                                 const float *__restrict__ val, int npoly)
+                                 const float *__restrict__ val, int npoly, int nb)
 {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= d.ni * d.nj) return;
@@ -88,13 +88,34 @@ __global__ void k_scene_classify(GridDims d, Grids G, float dx, const float *__r
         m = M_SOLID;
         G.solid_id[c] = minIdx;
     }
-    // updateInitialFluid (:573-590)
-    for (int k = 0; k < npoly; k++) {
-        if (kind[k] != 1) continue;
-        if (polygon_sdf(xy + 2 * off[k], off[k + 1] - off[k], ((float)i + 0.5f) * dx,
-                        ((float)j + 0.5f) * dx) <= 0.f) {
+    if (nb) {
+        // NBFlipSolver::fluidSdfFromInitialFluid (nbflipsolver.cpp:299-330):
+        // the nearest initial fluid's signed distance at the cell centre
+        float fd = FLT_MAX;
+        int fid = -1;
+        for (int k = 0; k < npoly; k++) {
+            if (kind[k] != 1) continue;
+            const float sdf = polygon_sdf(xy + 2 * off[k], off[k + 1] - off[k], x, y) / dx;
+            if (sdf < fd) {
+                fd = sdf;
+                fid = k;
+            }
+        }
+        G.fluid_sdf[c] = fd;
+        if (fd < 0) {
             m = M_FLUID;
-            G.visc[c] = val[k];
+            if (fid != -1) G.visc[c] = val[fid];
+        }
+        G.counts[c] = 0;
+    } else {
+        // updateInitialFluid (:573-590)
+        for (int k = 0; k < npoly; k++) {
+            if (kind[k] != 1) continue;
+            if (polygon_sdf(xy + 2 * off[k], off[k + 1] - off[k], ((float)i + 0.5f) * dx,
+                            ((float)j + 0.5f) * dx) <= 0.f) {
+                m = M_FLUID;
+                G.visc[c] = val[k];
+            }
         }
     }
     G.material[c] = m;
@@ -102,10 +123,10 @@ __global__ void k_scene_classify(GridDims d, Grids G, float dx, const float *__r
 
 void launch_scene_classify(const GridDims &d, const Grids &G, float dx, const float *poly_xy,
                            const int *poly_off, const int *poly_kind, const float *poly_val,
-                           int npoly, cudaStream_t st)
+                           int npoly, bool nb, cudaStream_t st)
 {
     k_scene_classify<<<nblk((long long)d.ni * d.nj, kThreads), kThreads, 0, st>>>(
-        d, G, dx, poly_xy, poly_off, poly_kind, poly_val, npoly);
+        d, G, dx, poly_xy, poly_off, poly_kind, poly_val, npoly, nb ? 1 : 0);
 }
 
 // updateVelocityFromSolids (flipsolver2d.cpp:1077-1104) depends only on solid
@@ -292,6 +313,11 @@ void launch_density_grid(const GridDims &d, const SceneParams &sp, const Particl
 // The U row i = NI and the V column j = NJ are never written by the
 // reference's loop over NI*NJ cells and stay at their fill values 0 / false.
 // ---------------------------------------------------------------------------
+// NB: NB-FLIP's centredParamsToGrid (nbflipsolver.cpp:463-504) keeps
+// centred weights with |w| > 1e-6 (the same sums otherwise, and 0 where none
+// is kept, which 0 / 1e-10 also gives), and its materials are classified
+// only after the grid combination (k_nb_materials)
+template <bool NB>
 __global__ void k_p2g_sdf_materials(GridDims d, Particles P, Grids G, float particleScale,
                                     int handling)
 {
@@ -300,6 +326,7 @@ __global__ void k_p2g_sdf_materials(GridDims d, Particles P, Grids G, float part
     const int ci = c / d.nj, cj = c - ci * d.nj;
     const int cbi = ci / 3, cbj = cj / 3;
     const float threshold = 1e-9f;
+    const float c_threshold = NB ? 1e-6f : threshold;
     float uW = 1e-10f, vW = 1e-10f, uVel = 0.0f, vVel = 0.0f;
     bool uValid = false, vValid = false;
     float wT = (float)1e-10, vis = 0.0f;
@@ -338,7 +365,7 @@ __global__ void k_p2g_sdf_materials(GridDims d, Particles P, Grids G, float part
                 }
                 if (handling != 2) {
                     const float wc = sm_qbspline(p.x - fi, p.y - fj);
-                    if (wc > threshold) {
+                    if ((NB ? fabsf(wc) : wc) > c_threshold) {
                         wT += wc;
                         vis += wc * P.visc[st + k];
                         visValid = true;
@@ -367,6 +394,7 @@ __global__ void k_p2g_sdf_materials(GridDims d, Particles P, Grids G, float part
     }
     const float sdf = sqrtf(d2) - particleScale;
     G.fluid_sdf[c] = sdf;
+    if (NB) return;
     const int8_t mc = G.material[c];
     if (sdf < 0.f) {
         if (t_empty(mc)) G.material[c] = M_FLUID;
@@ -376,10 +404,14 @@ __global__ void k_p2g_sdf_materials(GridDims d, Particles P, Grids G, float part
 }
 
 void launch_p2g_sdf_materials(const GridDims &d, const SceneParams &sp, const Particles &P,
-                              const Grids &G, cudaStream_t st)
+                              const Grids &G, bool nb, cudaStream_t st)
 {
-    k_p2g_sdf_materials<<<nblk((long long)d.ni * d.nj, kThreads), kThreads, 0, st>>>(
-        d, P, G, sp.particleScale, sp.parameterHandlingMethod);
+    if (nb)
+        k_p2g_sdf_materials<true><<<nblk((long long)d.ni * d.nj, kThreads), kThreads, 0, st>>>(
+            d, P, G, sp.particleScale, sp.parameterHandlingMethod);
+    else
+        k_p2g_sdf_materials<false><<<nblk((long long)d.ni * d.nj, kThreads), kThreads, 0, st>>>(
+            d, P, G, sp.particleScale, sp.parameterHandlingMethod);
 }
 
 // ---------------------------------------------------------------------------
@@ -449,7 +481,7 @@ __device__ __forceinline__ void ls_two_sum(float a, float b, float &s, float &e)
 // reference's float.
 template <int W>
 __device__ __forceinline__ float bfs_layer_value(const int *mark, const float *val, int r, int q, int k,
-                                                 bool minus_one)
+                                                 int add)
 {
     float s = 0.f, eh = 0.f, el = 0.f, m = 0.f;
     int count = 0, mine = INT_MAX;
@@ -487,8 +519,8 @@ __device__ __forceinline__ float bfs_layer_value(const int *mark, const float *v
     // and ql times the count gives them back
     const bool q_exact = ev == 0.f && eu == 0.f && fmaf(ql, cf, -u) == 0.f;
     float h, l, err3 = 0.f;
-    if (minus_one) {
-        ls_two_sum(qh, -1.f, h, l);
+    if (add != 0) {
+        ls_two_sum(qh, (float)add, h, l);
         float l2;
         ls_two_sum(l, ql, l2, err3);
         l = l2;
@@ -509,11 +541,11 @@ __device__ __forceinline__ float bfs_layer_value(const int *mark, const float *v
         const int ea = qh != 0.f ? ilogbf(qh) : -1000;
         const int lsb = min(qh != 0.f ? ilogbf(qh) - 23 : INT_MAX, ql != 0.f ? ilogbf(ql) - 23 : INT_MAX);
         // qh + ql (the quotient) must fit a double, and so must it minus one
-        const bool sub_exact = minus_one ? (max(ea, 0) + 1 - min(lsb, 0) <= 52) : (ea - lsb <= 51);
+        const bool sub_exact = add != 0 ? (max(ea, 0) + 1 - min(lsb, 0) <= 52) : (ea - lsb <= 51);
         if (sum_exact && sub_exact) {
             if (f != 0.f && isfinite(f)) return f;
             // an exact zero sum: the reference's double sum is +0 as well
-            if (!minus_one && s == 0.f && eh == 0.f && el == 0.f) return 0.f;
+            if (add == 0 && s == 0.f && eh == 0.f && el == 0.f) return 0.f;
         }
     }
     const float d = (h - f) + l;
@@ -527,7 +559,7 @@ __device__ __forceinline__ float bfs_layer_value(const int *mark, const float *v
     // by the reciprocal -- and a multiply has a fraction of the latency
     const double inv2 = count == 1 ? 1.0 : count == 2 ? 0.5 : count == 4 ? 0.25 : 0.125;
     const double a = (count & (count - 1)) == 0 ? avg * inv2 : avg / count;
-    return minus_one ? (float)(a - 1.f) : (float)a;
+    return add != 0 ? (float)(a + (double)add) : (float)a;
 }
 
 template <int W>
@@ -551,7 +583,8 @@ __device__ __forceinline__ bool bfs_touches(const int *mark, int r, int q, int k
 // with a compare-and-swap, so each is listed once); their values are then
 // computed from neighbours of smaller layers, in the reference's neighbour
 // order.  The set of cells per layer, hence every value, is deterministic.
-// `minus_one` selects the level-set form (average - 1).
+// `add` selects the form: 0 the velocity average, -1 the inside level set
+// (average - 1), +1 the outside level set (average + 1).
 // Appends `cnt_mine` entries per thread to a shared list with one atomic per
 // warp; returns this thread's first slot.  All threads of the warp call it.
 __device__ __forceinline__ int warp_append(int *counter, int cnt_mine)
@@ -571,7 +604,7 @@ __device__ __forceinline__ int warp_append(int *counter, int cnt_mine)
 
 template <int W, int H>
 __device__ __forceinline__ void bfs_layers(int *mark, float *val, short *fa, short *fb, int *cnt,
-                                           int k0, bool minus_one)
+                                           int k0, int add)
 {
     // cnt[0..2]: rotating list lengths (the list of layer k is counted in
     // cnt[k % 3]; cnt[(k + 2) % 3] is free while layer k is processed)
@@ -625,7 +658,7 @@ __device__ __forceinline__ void bfs_layers(int *mark, float *val, short *fa, sho
             if (live) {
                 e = cur[f];
                 const int r = e / W, q = e - r * W;
-                val[e] = bfs_layer_value<W>(mark, val, r, q, k, minus_one);
+                val[e] = bfs_layer_value<W>(mark, val, r, q, k, add);
             }
             if (more) expand(live, e, k, nxt, &cnt[(k + 1) % 3]);
         }
@@ -680,7 +713,7 @@ __global__ void __launch_bounds__(1024) k_vel_extrap(GridDims d, Grids G, float 
     // a tile whose loaded region lacks either seeds or unknown cells assigns
     // nothing and only copies its interior through
     const bool work = __syncthreads_or(has_seed) && __syncthreads_or(has_inf);
-    if (work) bfs_layers<W, kVelH>(t.mark, t.val, fa, fb, cnt, 0, false);
+    if (work) bfs_layers<W, kVelH>(t.mark, t.val, fa, fb, cnt, 0, 0);
     const float factor = (float)((double)sc->dt / dx);
     const float add = factor * (isV ? gJ : gI);
     for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
@@ -714,7 +747,9 @@ void launch_vel_extrapolate(const GridDims &d, Grids &G, const SceneParams &sp,
 }
 
 // Level set inside extrapolation (flipsolver2d.cpp:1433-1494): seeds are
-// cells with sdf > 0, depth unbounded, value = average - 1.  Pass p advances
+// cells with sdf > 0, depth unbounded, value = average - 1.  The outside
+// form (:1496-1558, NB-FLIP) seeds every cell below NI * NJ and assigns
+// average + 1; both run the same passes.  Pass p advances
 // layers p*H+1 .. (p+1)*H.  Each cell's (marker, value) pair lives in one
 // 64-bit word that is read and written whole.  A tile only trusts halo cells
 // of earlier passes (markers <= p*H, final since the previous launch); cells
@@ -739,15 +774,18 @@ __device__ __forceinline__ unsigned long long ls_pack(int mark, float v)
     return ((unsigned long long)(unsigned)mark << 32) | (unsigned long long)__float_as_uint(v);
 }
 
+// seeds: sdf > 0 inside; sdf < NI * NJ outside (extrapolateLevelsetOutside,
+// flipsolver2d.cpp:1496-1512: everything else is unknown)
 __global__ void k_levelset_init(GridDims d, const float *__restrict__ sdf,
                                 unsigned long long *__restrict__ cells, uint8_t *__restrict__ act,
-                                int ntiles, int *__restrict__ active, int passes)
+                                int ntiles, int *__restrict__ active, int passes, int outside)
 {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long N = (long long)d.ni * d.nj;
     if (c < N) {
         const float v = sdf[c];
-        cells[c] = ls_pack(v > 0.f ? 0 : kMarkInf, v);
+        const bool seed = outside ? v < (float)((size_t)d.ni * (size_t)d.nj) : v > 0.f;
+        cells[c] = ls_pack(seed ? 0 : kMarkInf, v);
     }
     if (c < 3LL * ntiles) act[c] = 0;
     if (c < passes) active[c] = 0;
@@ -756,7 +794,7 @@ __global__ void k_levelset_init(GridDims d, const float *__restrict__ sdf,
 __global__ void __launch_bounds__(1024, 1) k_levelset_pass(GridDims d, float *__restrict__ sdf,
                                                        unsigned long long *__restrict__ cells,
                                                        uint8_t *__restrict__ act,
-                                                       int *__restrict__ active, int pass)
+                                                       int *__restrict__ active, int pass, int add)
 {
     extern __shared__ int ls_smem[];
     constexpr int W = kLsW;
@@ -819,7 +857,7 @@ __global__ void __launch_bounds__(1024, 1) k_levelset_pass(GridDims d, float *__
     }
     // a tile whose cells are all assigned already has nothing to do
     if (!__syncthreads_or(open)) return;
-    bfs_layers<W, kLsH>(t.mark, t.val, fa, fb, cnt, k0, true);
+    bfs_layers<W, kLsH>(t.mark, t.val, fa, fb, cnt, k0, add);
     bool assigned = false;
     for (int e = threadIdx.x; e < kLsTile * kLsTile; e += blockDim.x) {
         const int r = e / kLsTile + kLsH, q = e % kLsTile + kLsH;
@@ -846,7 +884,7 @@ int levelset_max_passes(const GridDims &d)
     return m / kLsH + 2;
 }
 
-void launch_levelset(const GridDims &d, Grids &G, cudaStream_t st)
+void launch_levelset(const GridDims &d, Grids &G, bool outside, cudaStream_t st)
 {
     const int passes = levelset_max_passes(d);
     dim3 grid(nblk(d.nj, kLsTile), nblk(d.ni, kLsTile));
@@ -857,12 +895,13 @@ void launch_levelset(const GridDims &d, Grids &G, cudaStream_t st)
     unsigned long long *cells = reinterpret_cast<unsigned long long *>(G.levelset_cells);
     k_levelset_init<<<nblk(init_n, kThreads), kThreads, 0, st>>>(d, G.fluid_sdf, cells,
                                                                G.levelset_act, ntiles,
-                                                               G.levelset_active, passes);
+                                                               G.levelset_active, passes,
+                                                               outside ? 1 : 0);
     cudaFuncSetAttribute((const void *)k_levelset_pass, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)kLsSmem);
     for (int p = 0; p < passes; p++)
         k_levelset_pass<<<grid, 1024, kLsSmem, st>>>(d, G.fluid_sdf, cells, G.levelset_act,
-                                                      G.levelset_active, p);
+                                                      G.levelset_active, p, outside ? 1 : -1);
 }
 
 // ---------------------------------------------------------------------------

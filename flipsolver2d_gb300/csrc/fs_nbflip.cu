@@ -1,0 +1,341 @@
+// fs_nbflip.cu -- the kernels NB-FLIP (NBFlipSolver, nbflipsolver.cpp) adds to
+// the FLIP substep: narrow-band pruning, semi-Lagrangian advection of the
+// grids, the combination of advected and transferred grids, the material
+// update after it, band reseeding with the solver's std::mt19937 stream, and
+// the engine itself.
+//
+// Built with -fmad=false like the other FLIP kernels: every float expression
+// rounds as the reference's CPU build does.
+//
+// Scenes on this path have no sources: no cell is a source and every emitter
+// id is -1, which removes the source branches of pruneNarrowBand,
+// updateGridFromSources and reseedParticles.
+#include <cfloat>
+#include <cstdint>
+
+#include "fs_state.h"
+
+namespace fsg {
+
+namespace {
+constexpr int kThreads = 256;
+inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
+
+constexpr float kNarrowBand = -3.f;      // m_narrowBand,      nbflipsolver.cpp:20
+constexpr float kCombinationBand = -2.f; // m_combinationBand, :21
+constexpr float kResamplingBand = -1.f;  // m_resamplingBand,  :22
+} // namespace
+
+// ---------------------------------------------------------------------------
+// the Mersenne Twister MT19937 (Matsumoto and Nishimura 1998), the engine of
+// std::mt19937: 624 state words, regenerated 624 at a time, tempered on
+// output.  State layout: words 0..623, then the index of the next word.
+// ---------------------------------------------------------------------------
+constexpr int kMtN = 624, kMtM = 397;
+constexpr uint32_t kMtMatrix = 0x9908b0dfu, kMtUpper = 0x80000000u, kMtLower = 0x7fffffffu;
+
+__host__ __device__ inline uint32_t mt_temper(uint32_t y)
+{
+    y ^= y >> 11;
+    y ^= (y << 7) & 0x9d2c5680u;
+    y ^= (y << 15) & 0xefc60000u;
+    y ^= y >> 18;
+    return y;
+}
+
+__host__ __device__ inline uint32_t mt_mix(uint32_t a, uint32_t b, uint32_t c)
+{
+    const uint32_t y = (a & kMtUpper) | (b & kMtLower);
+    return c ^ (y >> 1) ^ ((y & 1u) ? kMtMatrix : 0u);
+}
+
+void mt_seed_host(uint32_t *st, uint32_t seed)
+{
+    st[0] = seed;
+    for (int i = 1; i < kMtN; i++) st[i] = 1812433253u * (st[i - 1] ^ (st[i - 1] >> 30)) + (uint32_t)i;
+    st[kMtN] = kMtN;
+}
+
+static void mt_twist_host(uint32_t *x)
+{
+    for (int k = 0; k < kMtN; k++) x[k] = mt_mix(x[k], x[(k + 1) % kMtN], x[(k + kMtM) % kMtN]);
+}
+
+void mt_discard_host(uint32_t *st, unsigned long long n)
+{
+    while (n > 0) {
+        if (st[kMtN] >= (uint32_t)kMtN) {
+            mt_twist_host(st);
+            st[kMtN] = 0;
+        }
+        const unsigned long long take = n < (unsigned long long)(kMtN - st[kMtN])
+                                            ? n
+                                            : (unsigned long long)(kMtN - st[kMtN]);
+        st[kMtN] += (uint32_t)take;
+        n -= take;
+    }
+}
+
+// std::uniform_real_distribution<float>(0, 1) over a 32-bit engine: one word,
+// converted to float (round to nearest), scaled by 2^-32 (exact), a result
+// that rounded up to 1 replaced by the largest float below 1, then
+// (b - a) * r + a = r
+__device__ __forceinline__ float mt_canonical(uint32_t w)
+{
+    float r = __uint2float_rn(w) * 0x1p-32f;
+    if (r >= 1.f) r = 0x1.fffffep-1f;
+    return r;
+}
+
+// The next per * count[0] draws of the engine, in order, as floats in [0, 1).
+// One block: a regeneration runs as four dependent phases (words 0..226 read
+// old words only; 227..453 read words 0..226; 454..622 read 227..395; 623
+// reads word 0 and 396), each read into registers before any is written.
+__global__ void __launch_bounds__(1024) k_mt_draws(uint32_t *__restrict__ st, float *__restrict__ out,
+                                                   const int *__restrict__ count, int per)
+{
+    __shared__ uint32_t x[kMtN];
+    const int t = threadIdx.x;
+    for (int i = t; i < kMtN; i += blockDim.x) x[i] = st[i];
+    int idx = (int)st[kMtN];
+    const long long n = (long long)count[0] * per;
+    __syncthreads();
+    long long done = 0;
+    auto phase = [&](int lo, int hi) {
+        uint32_t v = 0;
+        const int k = lo + t;
+        if (k < hi) v = mt_mix(x[k], x[(k + 1) % kMtN], x[(k + kMtM) % kMtN]);
+        __syncthreads();
+        if (k < hi) x[k] = v;
+        __syncthreads();
+    };
+    while (done < n) {
+        if (idx >= kMtN) {
+            phase(0, kMtN - kMtM);
+            phase(kMtN - kMtM, 2 * (kMtN - kMtM));
+            phase(2 * (kMtN - kMtM), kMtN - 1);
+            phase(kMtN - 1, kMtN);
+            idx = 0;
+        }
+        const long long left = n - done;
+        const int take = left < (long long)(kMtN - idx) ? (int)left : kMtN - idx;
+        for (int k = t; k < take; k += blockDim.x) out[done + k] = mt_canonical(mt_temper(x[idx + k]));
+        idx += take;
+        done += take;
+        __syncthreads(); // the next regeneration overwrites what was read
+    }
+    for (int i = t; i < kMtN; i += blockDim.x) st[i] = x[i];
+    if (t == 0) st[kMtN] = (uint32_t)idx;
+}
+
+void launch_mt_draws(uint32_t *state, float *out, const int *count, int per, cudaStream_t st)
+{
+    k_mt_draws<<<1, 1024, 0, st>>>(state, out, count, per);
+}
+
+// ---------------------------------------------------------------------------
+// NBFlipSolver::pruneNarrowBand (:227-253).  Killed particles and the
+// originals of moved ones are already marked (a moved particle's copy in the
+// rebin set keeps its unmarked flag); marking them again changes nothing, so
+// only particles that stay in their bin are tested.
+// ---------------------------------------------------------------------------
+__global__ void k_nb_prune_band(GridDims d, Particles P, const float *__restrict__ sdf,
+                                const int *__restrict__ counts, int cap2)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= P.bin_start[P.nbins] || P.flag[s] != P_STAY) return;
+    const float2 p = P.pos[s];
+    const long long i = (long long)p.x, j = (long long)p.y; // ssize_t i = position.x()
+    const float v = grid_lerp(sdf, d.ni, d.nj, 0.f, 0.f, p.x, p.y);
+    if (v < kNarrowBand || (v < kResamplingBand && counts[i * d.nj + j] > cap2)) P.flag[s] = P_KILL;
+}
+
+// FlipSolver::rk4Integrate (flipsolver2d.cpp:1195-1203) through the velocity grid
+__device__ __forceinline__ float2 rk4_integrate(const float *__restrict__ u, const float *__restrict__ v,
+                                                const GridDims &d, float2 p, float dt)
+{
+    float2 k = velocity_at(u, v, d, p.x, p.y);
+    const float k1x = k.x * dt, k1y = k.y * dt;
+    k = velocity_at(u, v, d, p.x + k1x * 0.5f, p.y + k1y * 0.5f);
+    const float k2x = k.x * dt, k2y = k.y * dt;
+    k = velocity_at(u, v, d, p.x + k2x * 0.5f, p.y + k2y * 0.5f);
+    const float k3x = k.x * dt, k3y = k.y * dt;
+    k = velocity_at(u, v, d, p.x + k3x, p.y + k3y);
+    const float k4x = k.x * dt, k4y = k.y * dt;
+    const float sx = ((k1x + k2x * 2.f) + k3x * 2.f) + k4x;
+    const float sy = ((k1y + k2y * 2.f) + k3y * 2.f) + k4y;
+    return make_float2(p.x + sx * (1.0f / 6.0f), p.y + sy * (1.0f / 6.0f));
+}
+
+// FlipSolver::eulerAdvectionThread (flipsolver2d.cpp:340-351) for the four
+// grids of NBFlipSolver::advect (:66-109) in one launch: every sample (i, j)
+// of U, V, the fluid SDF and the viscosity traced back by rk4Integrate(-dt)
+// and the input grid (with its offset) sampled there
+__global__ void k_nb_euler(GridDims d, const float *__restrict__ u, const float *__restrict__ v,
+                           const float *__restrict__ sdf, const float *__restrict__ visc,
+                           float *__restrict__ au, float *__restrict__ av, float *__restrict__ asdf,
+                           float *__restrict__ avisc, const Scalars *__restrict__ sc)
+{
+    const long long nu = (long long)(d.ni + 1) * d.nj, nv = (long long)d.ni * (d.nj + 1);
+    const long long nc = (long long)d.ni * d.nj;
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const float *in;
+    float *out;
+    int si, sj;
+    float ox, oy;
+    if (e < nu) {
+        in = u; out = au; si = d.ni + 1; sj = d.nj; ox = 0.5f; oy = 0.f;
+    } else if ((e -= nu) < nv) {
+        in = v; out = av; si = d.ni; sj = d.nj + 1; ox = 0.f; oy = 0.5f;
+    } else if ((e -= nv) < nc) {
+        in = sdf; out = asdf; si = d.ni; sj = d.nj; ox = 0.f; oy = 0.f;
+    } else if ((e -= nc) < nc) {
+        in = visc; out = avisc; si = d.ni; sj = d.nj; ox = 0.5f; oy = 0.5f;
+    } else {
+        return;
+    }
+    const long long i = e / sj, j = e - i * sj;
+    const float2 p = rk4_integrate(u, v, d, make_float2((float)i, (float)j), -sc->dt);
+    out[e] = grid_lerp(in, si, sj, ox, oy, p.x, p.y);
+}
+
+void launch_nb_advect_extra(const GridDims &d, const SceneParams &sp, const Particles &P,
+                            const Grids &G, const NbGrids &N, const Scalars *sc, cudaStream_t st)
+{
+    if (P.cap > 0)
+        k_nb_prune_band<<<nblk(P.cap, kThreads), kThreads, 0, st>>>(d, P, G.fluid_sdf, G.counts,
+                                                                    2 * sp.particlesPerCell);
+    const long long n = (long long)(d.ni + 1) * d.nj + (long long)d.ni * (d.nj + 1) +
+                        2LL * d.ni * d.nj;
+    k_nb_euler<<<nblk(n, kThreads), kThreads, 0, st>>>(d, G.u, G.v, G.fluid_sdf, G.visc, N.adv_u,
+                                                       N.adv_v, N.adv_sdf, N.adv_visc, sc);
+}
+
+// ---------------------------------------------------------------------------
+// NBFlipSolver::afterTransfer (:111-116) without sources: updateGridFromSources
+// (:332-364) leaves the SDF at std::min(FLT_MAX, sdf); combineLevelset
+// (:373-384) takes std::min(advected + 1, sdf); combineVelocityGrid and
+// combineCenteredGrids (:386-427) keep the transferred value where the SDF
+// sampled at the face or cell centre exceeds the combination band, else the
+// advected one.  std::min(a, b) is (b < a) ? b : a.
+// ---------------------------------------------------------------------------
+__global__ void k_nb_combine_sdf(long long n, float *__restrict__ sdf, const float *__restrict__ asdf)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    float b = sdf[c];
+    b = b < FLT_MAX ? b : FLT_MAX;
+    const float a = asdf[c] + 1.f;
+    sdf[c] = b < a ? b : a;
+}
+
+__global__ void k_nb_combine_grids(GridDims d, Grids G, NbGrids N)
+{
+    const long long nu = (long long)(d.ni + 1) * d.nj, nv = (long long)d.ni * (d.nj + 1);
+    const long long nc = (long long)d.ni * d.nj;
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < nu) {
+        const long long i = e / d.nj, j = e - i * d.nj;
+        const float s = grid_lerp(G.fluid_sdf, d.ni, d.nj, 0.f, 0.f, (float)i, 0.5f + (float)j);
+        if (!(s > kCombinationBand)) G.u[e] = N.adv_u[e];
+    } else if ((e -= nu) < nv) {
+        const long long i = e / (d.nj + 1), j = e - i * (d.nj + 1);
+        const float s = grid_lerp(G.fluid_sdf, d.ni, d.nj, 0.f, 0.f, 0.5f + (float)i, (float)j);
+        if (!(s > kCombinationBand)) G.v[e] = N.adv_v[e];
+    } else if ((e -= nv) < nc) {
+        const long long i = e / d.nj, j = e - i * d.nj;
+        // Vec3(0.5f + i, j + 0.5): the second coordinate is a double sum
+        const float s = grid_lerp(G.fluid_sdf, d.ni, d.nj, 0.f, 0.f, 0.5f + (float)i,
+                                  (float)((double)j + 0.5));
+        if (!(s > kCombinationBand)) G.visc[e] = N.adv_visc[e];
+    }
+}
+
+// FlipSolver::updateMaterials (flipsolver2d.cpp:1053-1075), which NB-FLIP
+// runs after the combination and the inside level set
+__global__ void k_nb_materials(long long n, const float *__restrict__ sdf, int8_t *__restrict__ mat)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const int8_t m = mat[c];
+    if (sdf[c] < 0.f) {
+        if (t_empty(m)) mat[c] = M_FLUID;
+    } else if (t_strict_fluid(m)) {
+        mat[c] = M_EMPTY;
+    }
+}
+
+void launch_nb_combine(const GridDims &d, const Grids &G, const NbGrids &N, cudaStream_t st)
+{
+    const long long nc = (long long)d.ni * d.nj;
+    k_nb_combine_sdf<<<nblk(nc, kThreads), kThreads, 0, st>>>(nc, G.fluid_sdf, N.adv_sdf);
+    const long long n = (long long)(d.ni + 1) * d.nj + (long long)d.ni * (d.nj + 1) + nc;
+    k_nb_combine_grids<<<nblk(n, kThreads), kThreads, 0, st>>>(d, G, N);
+}
+
+void launch_nb_materials(const GridDims &d, const Grids &G, cudaStream_t st)
+{
+    const long long nc = (long long)d.ni * d.nj;
+    k_nb_materials<<<nblk(nc, kThreads), kThreads, 0, st>>>(nc, G.fluid_sdf, G.material);
+}
+
+// ---------------------------------------------------------------------------
+// NBFlipSolver::reseedParticles (:118-201), candidate side.  Cells inside
+// the resampling band with fewer than particlesPerCell particles get
+// particlesPerCell - count candidates, in row-major cell order; each takes
+// two draws (jitteredPosInCell, flipsolver2d.cpp:1013-1019) and is kept
+// unless its interpolated SDF is below the narrow band.  A kept candidate
+// goes to the bin of its position with zero velocity and the viscosity
+// interpolated there.  A position rounded out of the grid has no bin (the
+// reference indexes past its bin array) and is dropped.
+// ---------------------------------------------------------------------------
+__global__ void k_nb_cand_count(long long n, const float *__restrict__ sdf,
+                                const int *__restrict__ counts, int ppc, int *__restrict__ cand_n)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const float s = sdf[c];
+    int add = 0;
+    if (s < kResamplingBand && s > kNarrowBand) add = ppc - counts[c];
+    cand_n[c] = add > 0 ? add : 0;
+}
+
+__global__ void k_nb_place(GridDims d, NbReseed R, const float *__restrict__ sdf,
+                           const float *__restrict__ visc)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= (long long)d.ni * d.nj) return;
+    const int k0 = R.cand_off[c], k1 = R.cand_off[c + 1];
+    if (k0 == k1) return;
+    const long long i = c / d.nj, j = c - i * d.nj;
+    const int cb = bin_of_cell(d, i, j);
+    for (int k = k0; k < k1; k++) {
+        const float x = (float)i + R.draws[2 * (size_t)k];
+        const float y = (float)j + R.draws[2 * (size_t)k + 1];
+        const float ns = grid_lerp(sdf, d.ni, d.nj, 0.f, 0.f, x, y);
+        const int pb = bin_of_pos(d, x, y);
+        const bool keep = !(ns < kNarrowBand) && pb >= 0;
+        R.cand_pos[k] = make_float2(x, y);
+        R.cand_visc[k] = grid_lerp(visc, d.ni, d.nj, 0.5f, 0.5f, x, y);
+        R.cand_bin[k] = keep ? pb : -1;
+        R.cand_cb[k] = cb;
+        if (keep && pb != cb) {
+            const int q = atomicAdd(R.cross_n, 1);
+            if (q < kNbCrossMax) R.cross[q] = k;
+        }
+    }
+}
+
+void launch_nb_candidates(const GridDims &d, const SceneParams &sp, const Grids &G,
+                          const NbReseed &R, void *scan_scratch, cudaStream_t st)
+{
+    const long long nc = (long long)d.ni * d.nj;
+    k_nb_cand_count<<<nblk(nc, kThreads), kThreads, 0, st>>>(nc, G.fluid_sdf, G.counts,
+                                                            sp.particlesPerCell, R.cand_n);
+    scan_exclusive(R.cand_n, R.cand_off, (int)nc, scan_scratch, st);
+    launch_mt_draws(R.rng, R.draws, R.cand_off + nc, 2, st);
+    cudaMemsetAsync(R.cross_n, 0, sizeof(int), st);
+    k_nb_place<<<nblk(nc, kThreads), kThreads, 0, st>>>(d, R, G.fluid_sdf, G.visc);
+}
+
+} // namespace fsg

@@ -467,6 +467,190 @@ void launch_rebin(const GridDims &d, Particles &P, void *scratch, size_t, cudaSt
 }
 
 // ---------------------------------------------------------------------------
+// NB-FLIP reseeding, append side (nbflipsolver.cpp:118-201): kept candidates
+// are appended to their bins in candidate (row-major cell, then draw) order,
+// as ParticleBin::addMarkerParticle pushes them back one by one.  Existing
+// particles keep their order; the layout is rebuilt without gaps.
+// ---------------------------------------------------------------------------
+__global__ void k_nb_bins_init(Particles P)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= P.nbins) return;
+    P.survivors[b] = P.bin_count[b];
+    P.incoming[b] = 0;
+}
+
+// stable compaction of kept candidates in candidate order: count per tile
+__global__ void k_nb_keep_tile_counts(const int *__restrict__ cand_bin, const int *__restrict__ nptr,
+                                      int *__restrict__ tile_counts)
+{
+    __shared__ int sw[33];
+    const int n = *nptr;
+    const int base = blockIdx.x * kScanTile;
+    int c = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        const int e = base + threadIdx.x * kScanItems + k;
+        if (e < n && cand_bin[e] >= 0) c++;
+    }
+    int total;
+    block_excl_scan<kScanBlock>(c, sw, total);
+    if (threadIdx.x == 0) tile_counts[blockIdx.x] = total;
+}
+
+__global__ void k_nb_keep_write(Particles P, const int *__restrict__ cand_bin,
+                                const int *__restrict__ nptr, const int *__restrict__ tile_off)
+{
+    __shared__ int sw[33];
+    const int n = *nptr;
+    const int base = blockIdx.x * kScanTile;
+    int c = 0;
+    int bk[kScanItems];
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        const int e = base + threadIdx.x * kScanItems + k;
+        bk[k] = e < n ? cand_bin[e] : -1;
+        c += bk[k] >= 0;
+    }
+    int total;
+    int off = block_excl_scan<kScanBlock>(c, sw, total) + tile_off[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        if (bk[k] >= 0) {
+            P.mkey[off] = bk[k];
+            P.mval[off] = base + threadIdx.x * kScanItems + k;
+            atomicAdd(&P.incoming[bk[k]], 1); // order-independent count
+            off++;
+        }
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *P.nmoved = tile_off[gridDim.x];
+}
+
+// every live particle to the same place in its bin of the new layout (a
+// layout beyond the capacity -- possible only for a state loaded with more
+// than 2 particlesPerCell in a cell and reseeded without counting -- is not
+// written and raises the status)
+__global__ void k_nb_scatter_live(Particles P, int *status)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= P.bin_start[P.nbins]) return;
+    if (P.bin_start2[P.nbins] > P.cap) {
+        if (s == 0) atomicExch(status, 1);
+        return;
+    }
+    const int b = P.slot_bin[s];
+    const int r = s - P.bin_start[b];
+    if (r >= P.bin_count[b]) return;
+    const int dst = P.bin_start2[b] + r;
+    P.pos2[dst] = P.pos[s];
+    P.vel2[dst] = P.vel[s];
+    P.visc2[dst] = P.visc[s];
+    P.slot_bin2[dst] = b;
+}
+
+// the kept candidates after them; the viscosity goes through the cell's bin,
+// so a particle whose position lies in another bin keeps 0 (the fix-up
+// below stores its viscosity where the reference does)
+__global__ void k_nb_scatter_new(Particles P, NbReseed R)
+{
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= *P.nmoved || P.bin_start2[P.nbins] > P.cap) return;
+    const int d = P.mkey[m], k = P.mval[m];
+    const int dst = P.bin_start2[d] + P.survivors[d] + (m - P.inc_off[d]);
+    P.pos2[dst] = R.cand_pos[k];
+    P.vel2[dst] = make_float2(0.f, 0.f);
+    P.visc2[dst] = R.cand_cb[k] == d ? R.cand_visc[k] : 0.f;
+    P.slot_bin2[dst] = d;
+    R.pos_of[k] = m;
+}
+
+// The reference stores a reseeded particle's viscosity in the property
+// vector of the cell's bin at the index the position's bin returned
+// (nbflipsolver.cpp:190-194); where the two bins differ (i + U(0,1) rounded
+// into the next bin) that overwrites an earlier particle of the cell's bin,
+// if the index exists there at that moment.  These cases are rare; one
+// thread replays them in candidate order.
+__global__ void k_nb_cross_fix(Particles P, NbReseed R)
+{
+    if (P.bin_start2[P.nbins] > P.cap) return;
+    const int n = min(*R.cross_n, kNbCrossMax);
+    if (*R.cross_n > kNbCrossMax) atomicExch(R.status, 1);
+    for (int a = 1; a < n; a++) { // insertion sort: the list is short
+        const int v = R.cross[a];
+        int b = a - 1;
+        while (b >= 0 && R.cross[b] > v) {
+            R.cross[b + 1] = R.cross[b];
+            b--;
+        }
+        R.cross[b + 1] = v;
+    }
+    for (int a = 0; a < n; a++) {
+        const int k = R.cross[a];
+        const int pb = R.cand_bin[k], cb = R.cand_cb[k];
+        const int pidx = P.survivors[pb] + (R.pos_of[k] - P.inc_off[pb]);
+        // the cell's bin at that moment: its old particles and its kept
+        // candidates that come before k (sorted by candidate index)
+        int lo = P.inc_off[cb], hi = P.inc_off[cb] + P.incoming[cb];
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (P.mval[mid] < k) lo = mid + 1;
+            else hi = mid;
+        }
+        const int size = P.survivors[cb] + (lo - P.inc_off[cb]);
+        if (pidx < size) P.visc2[P.bin_start2[cb] + pidx] = R.cand_visc[k];
+    }
+}
+
+void launch_nb_append(Particles &P, const NbReseed &R, int max_cand, void *scratch,
+                      cudaStream_t st)
+{
+    if (P.cap == 0) return;
+    const int ntiles = nblk(max_cand > 0 ? max_cand : 1, kScanTile);
+    const int ptiles = nblk(P.cap, kScanTile);
+    const int rtiles = nblk(P.cap, kRadixTile);
+    char *p = (char *)scratch;
+    int *tile_counts = (int *)p;
+    p += align256((size_t)(ptiles + 1) * sizeof(int));
+    int *hist = (int *)p;
+    p += align256((size_t)(256 * rtiles + 1) * sizeof(int));
+    void *scan_tmp = p;
+    const int *ncand = R.cand_off + R.ncell;
+
+    k_nb_bins_init<<<nblk(P.nbins, kThreads), kThreads, 0, st>>>(P);
+    k_nb_keep_tile_counts<<<ntiles, kScanBlock, 0, st>>>(R.cand_bin, ncand, tile_counts);
+    scan_exclusive(tile_counts, tile_counts, ntiles, scan_tmp, st);
+    k_nb_keep_write<<<ntiles, kScanBlock, 0, st>>>(P, R.cand_bin, ncand, tile_counts);
+    int bits = 0;
+    while ((1 << bits) < P.nbins) bits++;
+    int *kin = P.mkey, *vin = P.mval, *kout = P.mkey2, *vout = P.mval2;
+    for (int shift = 0; shift < bits; shift += 8) {
+        k_radix_hist<<<rtiles, kRadixBlock, 0, st>>>(kin, P.nmoved, shift, hist, rtiles);
+        scan_exclusive(hist, hist, 256 * rtiles, scan_tmp, st);
+        k_radix_scatter<<<rtiles, kRadixBlock, 0, st>>>(kin, vin, kout, vout, P.nmoved, shift,
+                                                        hist, rtiles);
+        int *t = kin; kin = kout; kout = t;
+        t = vin; vin = vout; vout = t;
+    }
+    if (kin != P.mkey) {
+        int *t = P.mkey; P.mkey = P.mkey2; P.mkey2 = t;
+        t = P.mval; P.mval = P.mval2; P.mval2 = t;
+    }
+    scan_exclusive(P.incoming, P.inc_off, P.nbins, scan_tmp, st);
+    k_new_counts<<<nblk(P.nbins, kThreads), kThreads, 0, st>>>(P);
+    scan_exclusive(P.bin_count2, P.bin_start2, P.nbins, scan_tmp, st);
+    k_nb_scatter_live<<<nblk(P.cap, kThreads), kThreads, 0, st>>>(P, R.status);
+    k_nb_scatter_new<<<nblk(max_cand > 0 ? max_cand : 1, kThreads), kThreads, 0, st>>>(P, R);
+    k_nb_cross_fix<<<1, 1, 0, st>>>(P, R);
+    float2 *tp;
+    tp = P.pos; P.pos = P.pos2; P.pos2 = tp;
+    tp = P.vel; P.vel = P.vel2; P.vel2 = tp;
+    float *tf = P.visc; P.visc = P.visc2; P.visc2 = tf;
+    int *ti = P.slot_bin; P.slot_bin = P.slot_bin2; P.slot_bin2 = ti;
+    ti = P.bin_start; P.bin_start = P.bin_start2; P.bin_start2 = ti;
+    ti = P.bin_count; P.bin_count = P.bin_count2; P.bin_count2 = ti;
+}
+
+// ---------------------------------------------------------------------------
 // particle state to and from the host in bin order (fs_get/set_particles)
 // ---------------------------------------------------------------------------
 // the live particles of every bin, packed in bin order at off[b]

@@ -88,7 +88,33 @@ struct Scalars {
     int pressure_iters;
     int pcg_status;        // 0 ok, 1 a grid-barrier wait timed out
     int wrap_units;        // a unit row lies on the j = 0 or j = NJ-1 edge
-    int pad[2];
+    int nb_overflow;       // NB-FLIP reseeding: more bin-crossing candidates than kept
+    int pad;
+};
+
+// NB-FLIP (nbflipsolver.h:63-66): the grids advected semi-Lagrangian each
+// substep, same shapes as U, V and the cell grids
+struct NbGrids {
+    float *adv_u = nullptr, *adv_v = nullptr, *adv_sdf = nullptr, *adv_visc = nullptr;
+};
+
+// NB-FLIP reseeding scratch; candidates are numbered in the reference's
+// order (row-major cell, then draw)
+constexpr int kNbCrossMax = 1 << 16; // candidates whose position left their cell's bin
+struct NbReseed {
+    uint32_t *rng = nullptr;   // std::mt19937 state: 624 words, next index
+    int *cand_n = nullptr;     // ncell: candidates per cell
+    int *cand_off = nullptr;   // ncell + 1: first candidate per cell, total at [ncell]
+    float *draws = nullptr;    // 2 per candidate
+    float2 *cand_pos = nullptr;
+    float *cand_visc = nullptr;
+    int *cand_bin = nullptr;   // bin of the position, -1 when not kept
+    int *cand_cb = nullptr;    // bin of the cell
+    int *pos_of = nullptr;     // rank in the sorted list of kept candidates
+    int *cross = nullptr;      // kNbCrossMax
+    int *cross_n = nullptr;
+    int *status = nullptr;     // 1 when more than kNbCrossMax crossed bins
+    int ncell = 0;
 };
 
 // launch helpers implemented in the kernel files
@@ -119,9 +145,12 @@ void launch_decomposition(const GridDims &d, const Grids &G, int *chunk_last, in
 void launch_density_grid(const GridDims &d, const SceneParams &sp, const Particles &P,
                          const Grids &G, void *rhs, int rhs_is_double, const Scalars *sc,
                          cudaStream_t st);
+// nb: NB-FLIP's centred weights, and no material update (it follows the
+// grid combination there)
 void launch_p2g_sdf_materials(const GridDims &d, const SceneParams &sp, const Particles &P,
-                              const Grids &G, cudaStream_t st);
-void launch_levelset(const GridDims &d, Grids &G, cudaStream_t st);
+                              const Grids &G, bool nb, cudaStream_t st);
+// extrapolateLevelsetInside, or with `outside` extrapolateLevelsetOutside
+void launch_levelset(const GridDims &d, Grids &G, bool outside, cudaStream_t st);
 void launch_vel_extrapolate(const GridDims &d, Grids &G, const SceneParams &sp,
                             const Scalars *sc, bool save_and_gravity, cudaStream_t st);
 void launch_pressure_rhs(const GridDims &d, const Grids &G, void *rhs, int rhs_is_double,
@@ -134,12 +163,28 @@ void launch_save_grid(const GridDims &d, const Grids &G, cudaStream_t st);
 void launch_body_forces(const GridDims &d, const SceneParams &sp, const Grids &G,
                         const Scalars *sc, cudaStream_t st);
 int levelset_max_passes(const GridDims &d);
+// sinks, solids and the initial fluid; with `nb` the initial fluid sets the
+// fluid SDF as NBFlipSolver::fluidSdfFromInitialFluid does and clears counts
 void launch_scene_classify(const GridDims &d, const Grids &G, float dx, const float *poly_xy,
                            const int *poly_off, const int *poly_kind, const float *poly_val,
-                           int npoly, cudaStream_t st);
+                           int npoly, bool nb, cudaStream_t st);
 void launch_friction_factors(const GridDims &d, const Grids &G, const float *obst_friction,
                              cudaStream_t st);
 void launch_fill_u8(uint8_t *p, uint8_t v, size_t n, cudaStream_t st);
+
+// NB-FLIP (fs_nbflip.cu, fs_particles.cu)
+void mt_seed_host(uint32_t *state, uint32_t seed);
+void mt_discard_host(uint32_t *state, unsigned long long n);
+void launch_mt_draws(uint32_t *state, float *out, const int *count, int per, cudaStream_t st);
+// narrow-band pruning after advection, then the four semi-Lagrangian grids
+void launch_nb_advect_extra(const GridDims &d, const SceneParams &sp, const Particles &P,
+                            const Grids &G, const NbGrids &N, const Scalars *sc, cudaStream_t st);
+void launch_nb_combine(const GridDims &d, const Grids &G, const NbGrids &N, cudaStream_t st);
+void launch_nb_materials(const GridDims &d, const Grids &G, cudaStream_t st);
+void launch_nb_candidates(const GridDims &d, const SceneParams &sp, const Grids &G,
+                          const NbReseed &R, void *scan_scratch, cudaStream_t st);
+void launch_nb_append(Particles &P, const NbReseed &R, int max_cand, void *scratch,
+                      cudaStream_t st);
 
 // exclusive scan of n ints (out may alias nothing); writes the total to out[n]
 size_t scan_scratch_bytes(int n);

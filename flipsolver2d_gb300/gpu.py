@@ -29,7 +29,7 @@ FS_PCG_FP32, FS_PCG_FP64, FS_PCG_SPEC = 0, 1, 2
 # stage ids (FS_STAGE_*), identical to the oracle's
 ADVECT, DECOMPOSITION, REBIN, DENSITY, P2G, SDF, MATERIALS, AFTER_TRANSFER, LEVELSET, \
     VEL_EXTRAP, SAVE_GRID, BODY_FORCES, PROJECT, FRICTION, G2P, COUNT, RESEED, \
-    DENSITY_GRID = range(18)
+    DENSITY_GRID, LEVELSET_OUTSIDE = range(19)
 
 GRIDS: Dict[str, tuple] = {
     "material": (0, np.int8, "c"), "solid_sdf": (1, np.float32, "c"),
@@ -42,7 +42,10 @@ GRIDS: Dict[str, tuple] = {
     "density_rhs": (15, np.float64, "c"), "density_pressure": (16, np.float64, "c"),
     "pressure": (17, np.float64, "c"), "pressure_rhs": (18, np.float64, "c"),
     "emitter_id": (19, np.int32, "c"),
+    "advected_u": (20, np.float32, "u"), "advected_v": (21, np.float32, "v"),
+    "advected_sdf": (22, np.float32, "c"), "advected_viscosity": (23, np.float32, "c"),
 }
+NB_GRIDS = ["advected_u", "advected_v", "advected_sdf", "advected_viscosity"]
 
 
 class FsError(RuntimeError):
@@ -62,6 +65,9 @@ _SIGS = {
     "fs_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "fs_last_error": (ctypes.c_char_p, []),
     "fs_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_create_nbflip": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_get_rng_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_set_rng_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "fs_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "fs_add_geometry": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p, ctypes.c_int]),
     "fs_add_initial_fluid": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p, ctypes.c_int]),
@@ -168,7 +174,8 @@ def exec_params(precision: int = FS_PCG_FP32, pool_threads: int = 0, device: int
 
 
 class GpuFlipSolver:
-    """FlipSolver (flipsolver2d.h:183-432) with its substep on the GPU."""
+    """FlipSolver (flipsolver2d.h:183-432) with its substep on the GPU, or
+    NBFlipSolver (nbflipsolver.h:12-78) for scenes of simType "nbflip"."""
 
     def __init__(self, scene, precision: int = FS_PCG_FP32, pool_threads: int = 0,
                  device: int = 0):
@@ -178,8 +185,10 @@ class GpuFlipSolver:
         self.ni, self.nj = self._cp.gridSizeI, self._cp.gridSizeJ
         self._ex = exec_params(precision, pool_threads, device)
         h = ctypes.c_void_p()
-        _check(self.lib.fs_create(ctypes.byref(self._cp), ctypes.byref(self._ex), ctypes.byref(h)),
-               "fs_create")
+        self.nb = getattr(scene, "sim_type", "flip") == "nbflip"
+        create = "fs_create_nbflip" if self.nb else "fs_create"
+        _check(getattr(self.lib, create)(ctypes.byref(self._cp), ctypes.byref(self._ex),
+                                         ctypes.byref(h)), create)
         self.h = h
         for o in scene.objects:
             v = np.ascontiguousarray(o.verts, dtype=np.float32)
@@ -305,11 +314,26 @@ class GpuFlipSolver:
         a = np.ascontiguousarray(a, dtype=dt).reshape(self.grid_shape(name))
         _check(self.lib.fs_set_grid(self.h, gid, _ptr(a), a.nbytes), f"fs_set_grid({name})")
 
+    def get_rng(self) -> np.ndarray:
+        """The std::mt19937 state: 624 words and the index of the next one."""
+        st = np.zeros(625, np.uint32)
+        _check(self.lib.fs_get_rng_state(self.h, _ptr(st)), "fs_get_rng_state")
+        return st
+
+    def set_rng(self, st: np.ndarray):
+        st = np.ascontiguousarray(st, np.uint32)
+        assert st.shape == (625,)
+        _check(self.lib.fs_set_rng_state(self.h, _ptr(st)), "fs_set_rng_state")
+
     def restore(self, snap: dict, grids=None):
-        """Load an oracle snapshot (particles + grids + dt)."""
+        """Load an oracle snapshot (particles + grids + dt, and the engine
+        state when the snapshot has one)."""
         self.set_particles(snap["particles"])
-        for g in (grids or [k for k in GRIDS if k in snap]):
+        names = grids or [k for k in GRIDS if k in snap and (self.nb or k not in NB_GRIDS)]
+        for g in names:
             self.set_grid(g, snap[g])
+        if "rng" in snap:
+            self.set_rng(snap["rng"])
         self.set_dt(snap["dt"])
 
     # timing

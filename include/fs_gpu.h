@@ -106,8 +106,24 @@ enum {
     FS_STAGE_G2P = 14,           /* particleUpdate()                  :456 */
     FS_STAGE_COUNT = 15,         /* countParticles()                  :459 */
     FS_STAGE_RESEED = 16,        /* reseedParticles(): sources only, no-op */
-    FS_STAGE_DENSITY_GRID = 17   /* updateDensityGrid() alone (plus its RHS) */
+    FS_STAGE_DENSITY_GRID = 17,  /* updateDensityGrid() alone (plus its RHS) */
+    FS_STAGE_LEVELSET_OUTSIDE = 18 /* extrapolateLevelsetOutside       :1496-1558 */
 };
+
+/* An NB-FLIP handle (fs_create_nbflip) runs the same stage ids, four of them
+ * as NBFlipSolver's overrides (nbflipsolver.cpp):
+ *   FS_STAGE_ADVECT          advect(): FlipSolver::advect, pruneNarrowBand, and
+ *                            the semi-Lagrangian u, v, SDF and viscosity :66-109
+ *   FS_STAGE_P2G             particleToGrid() with its centredParamsToGrid
+ *                            (:445-504), fused with updateSdf(); no materials
+ *   FS_STAGE_MATERIALS       updateMaterials(), which NB-FLIP runs after the
+ *                            combination
+ *   FS_STAGE_AFTER_TRANSFER  afterTransfer(): updateGridFromSources and
+ *                            combineAdvectedGrids                       :111-116
+ *   FS_STAGE_RESEED          reseedParticles(): band reseeding         :118-201
+ * Its step (:26-64) is ADVECT, REBIN, P2G, VEL_EXTRAP, SAVE_GRID,
+ * LEVELSET_OUTSIDE, AFTER_TRANSFER, LEVELSET, MATERIALS, BODY_FORCES,
+ * DECOMPOSITION, PROJECT (+ FRICTION), VEL_EXTRAP, G2P, COUNT, RESEED. */
 
 /* Grid ids for fs_get_grid / fs_set_grid.  c = NI*NJ, u = (NI+1)*NJ,
  * v = NI*(NJ+1) elements, row-major. */
@@ -131,7 +147,11 @@ enum {
     FS_GRID_DENSITY_PRESSURE = 16,/* double c  m_pressureSolverResult */
     FS_GRID_PRESSURE = 17,        /* double c  projection pressure */
     FS_GRID_PRESSURE_RHS = 18,    /* double c  projection right-hand side */
-    FS_GRID_EMITTER_ID = 19       /* int32  c  m_emitterId */
+    FS_GRID_EMITTER_ID = 19,      /* int32  c  m_emitterId */
+    FS_GRID_ADVECTED_U = 20,      /* float  u  NB-FLIP m_advectedVelocity (nbflipsolver.h:64) */
+    FS_GRID_ADVECTED_V = 21,      /* float  v  */
+    FS_GRID_ADVECTED_SDF = 22,    /* float  c  NB-FLIP m_advectedSdf (:65) */
+    FS_GRID_ADVECTED_VISCOSITY = 23 /* float c NB-FLIP m_advectedViscosity (:63) */
 };
 
 enum {
@@ -151,6 +171,15 @@ const char *fs_last_error(void);
 /* FlipSolver::FlipSolver(const FlipSolverParameters*) (flipsolver2d.cpp:27-86)
  * followed by initAdditionalParameters() (:1613-1616).  exec may be NULL. */
 fs_status fs_create(const fs_params *p, const fs_exec_params *exec, fs_solver **out);
+/* NBFlipSolver::NBFlipSolver(const NBFlipParameters*) (nbflipsolver.cpp:9-24)
+ * followed by initAdditionalParameters(); NBFlipParameters adds nothing to
+ * FlipSolverParameters.  The handle takes every other call below; its
+ * particle capacity is 2 particlesPerCell per cell.  fs_batch_add refuses it. */
+fs_status fs_create_nbflip(const fs_params *p, const fs_exec_params *exec, fs_solver **out);
+/* The solver's std::mt19937 (m_randEngine, flipsolver2d.h:371): 625 words,
+ * the 624 state words then the index of the next one (0..624). */
+fs_status fs_get_rng_state(fs_solver *s, uint32_t *state);
+fs_status fs_set_rng_state(fs_solver *s, const uint32_t *state);
 /* FlipSolver::~FlipSolver */
 fs_status fs_destroy(fs_solver *s);
 
