@@ -421,6 +421,197 @@ def gpu_arm(args):
     return 0
 
 
+NB_WARM_FRAMES = 4
+
+
+def nb_scene(res: int):
+    from flipsolver2d_gb300 import scenes
+
+    return scenes.nb_dam_break(res, seed=SEED, obstacle=True)
+
+
+def nb_measure(res: int, warmup: int, steps: int, local: int = 0, with_e2e: bool = True,
+               want_snapshot: bool = False):
+    """NB-FLIP substeps of the narrow-band dam break at res^2 (FP32 PCG),
+    device-timed like the FLIP line; e2e through the C ABI with the state a
+    substep carries (particles, u, v, material, fluid SDF, viscosity, counts,
+    engine state) uploaded and downloaded every step."""
+    import torch
+
+    from flipsolver2d_gb300 import gpu
+
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")
+    sc = nb_scene(res)
+    p = sc.params
+    s = gpu.GpuFlipSolver(sc, precision=gpu.FS_PCG_FP32, device=local)
+    for _ in range(NB_WARM_FRAMES):
+        s.step_frame()
+
+    def one_step():
+        n = s.particle_count()
+        s.set_dt(cfl_dt(s.max_particle_velocity(), p))
+        s.step()
+        return n
+
+    for _ in range(warmup):
+        one_step()
+    s.enable_timers(True)
+    torch.cuda.synchronize()
+    work, step_ms, pcg_ms, launches, iters = 0, [], 0.0, 0.0, []
+    stages = np.zeros(12)
+    for _ in range(steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        s.reset_timers()
+        work += one_step()
+        step_ms.append(s.timer(0))
+        pcg_ms += s.timer(1)
+        launches += s.timer(2)
+        stages += np.array(s.stage_times())
+        iters.append(executed_iters(s.stat(1), p.pcgIterLimit))
+    s.enable_timers(False)
+    out = {"work": work, "total_ms": float(sum(step_ms)), "pcg_ms": pcg_ms, "launches": launches,
+           "cells": s.ni * s.nj, "pressure_iters": iters, "step_ms": step_ms,
+           "stage_ms": (stages / steps).tolist()}
+    if with_e2e:
+        carried = ["u", "v", "material", "fluid_sdf", "viscosity", "particle_counts"]
+        e2e_steps = max(1, min(steps, 5))
+        cap = 2 * p.particlesPerCell * s.ni * s.nj
+
+        def pinned(shape, dtype):
+            return torch.empty(shape, dtype=dtype, pin_memory=True).numpy()
+
+        tdt = {np.float32: torch.float32, np.int8: torch.int8, np.int32: torch.int32}
+        hp = {"bin_counts": pinned((s.bin_count(),), torch.int32), "pos": pinned((cap, 2), torch.float32),
+              "vel": pinned((cap, 2), torch.float32), "visc": pinned((cap,), torch.float32),
+              "dead": pinned((cap,), torch.uint8)}
+        hg = {g: pinned(s.grid_shape(g), tdt[gpu.GRIDS[g][1]]) for g in carried}
+        snap_p = s.get_particles(out=hp)
+        snap_g = {g: s.get_grid(g, out=hg[g]) for g in carried}
+        rng = s.get_rng()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_work, h2d = 0, 0
+        for _ in range(e2e_steps):
+            s.set_particles(snap_p)
+            for g, a in snap_g.items():
+                s.set_grid(g, a)
+            s.set_rng(rng)
+            h2d = sum(v.nbytes for v in snap_p.values()) + sum(a.nbytes for a in snap_g.values())
+            e2e_work += len(snap_p["pos"])
+            s.set_dt(cfl_dt(s.max_particle_velocity(), p))
+            s.step()
+            snap_p = s.get_particles(out=hp)
+            snap_g = {g: s.get_grid(g, out=hg[g]) for g in carried}
+            rng = s.get_rng()
+        e2e_s = time.perf_counter() - t0
+        out["e2e"] = {"value": e2e_work / e2e_s, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
+                      "d2h_bytes_per_step": int(h2d), "steps": e2e_steps,
+                      "path": "fs_set_particles + fs_set_grid(u, v, material, fluid_sdf, "
+                              "viscosity, particle_counts) + fs_set_rng_state + fs_step + the "
+                              "matching gets, pinned host buffers"}
+    if want_snapshot:
+        # the state the CPU sample starts from (the oracle's snapshot layout)
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import fsoracle as fo
+
+        snap = {"particles": s.get_particles(), "dt": s.dt, "rng": s.get_rng()}
+        for g in fo.STATE_GRIDS + fo.NB_GRIDS:
+            snap[g] = s.get_grid(g)
+        out["snapshot"] = snap
+    s.close()
+    return out
+
+
+def nb_cpu_sample(res: int, threads: int, substeps: int = 1, snapshot=None):
+    """The CPU oracle on the NB-FLIP workload: `substeps` timed substeps
+    from `snapshot` (the GPU's state after the warm frames; stepping the warm
+    frames on the CPU would take minutes), else from the oracle's own warm
+    frames."""
+    os.environ["FSO_HOST_THREADS"] = str(threads)
+    os.environ.setdefault("FSO_REF_THREADS", str(threads))
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import build as oracle_build
+
+    oracle_build.build_port()
+    import fsoracle as fo
+
+    kind = "reference" if fo.available("ref") else "port"
+    sc = nb_scene(res)
+    o = fo.OracleSolver(sc, "ref" if kind == "reference" else "port")
+    o.first_frame_init()
+    if snapshot is not None:
+        o.restore(snapshot)
+    else:
+        for _ in range(NB_WARM_FRAMES):
+            o.step_frame()
+    work, t_total, times = 0, 0.0, []
+    for _ in range(substeps):
+        n = o.particle_count()
+        o.set_dt(cfl_dt(o.max_particle_velocity(), sc.params))
+        t0 = time.perf_counter()
+        o.step()
+        dt = time.perf_counter() - t0
+        times.append(dt)
+        t_total += dt
+        work += n
+    o.close()
+    return {"value": work / t_total, "unit": METRIC, "cores": threads, "kind": kind,
+            "sample": f"{substeps} substep(s) of nb_dam_break_{res}_obstacle from "
+                      f"{'the GPU state' if snapshot is not None else 'the oracle state'} after "
+                      f"{NB_WARM_FRAMES} frames ({work} particle-substeps, {t_total:.1f} s)",
+            "step_s": times}
+
+
+def nbflip_arm(args):
+    """NB-FLIP (NBFlipSolver) substeps of the narrow-band dam break."""
+    from flipsolver2d_gb300 import build
+
+    build.build()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    sampler = ClockSampler(local)
+    sampler.start()
+    r = nb_measure(args.res, args.warmup, args.steps, local, want_snapshot=not args.no_cpu)
+    clocks = sampler.stop()
+    value = r["work"] / (r["total_ms"] / 1e3)
+    cpu = None
+    if not args.no_cpu:
+        try:
+            cpu = nb_cpu_sample(args.res, os.cpu_count() or 1, 1, r.get("snapshot"))
+            cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        except Exception as e:  # reported, never fatal for the GPU line
+            cpu = {"value": None, "unit": METRIC, "cores": 0, "kind": "port", "sample": f"failed: {e}"}
+    peak, peak_kind = measured_peaks()
+    cell_iters = sum(r["cells"] * it for it in r["pressure_iters"])
+    bytes_pcg = sum(r["cells"] * (16 + 34 * it) for it in r["pressure_iters"])
+    achieved = bytes_pcg / (r["pcg_ms"] / 1e3) / 1e9 if r["pcg_ms"] > 0 else None
+    names = ["advection", "decomposition", "density", "rebin", "particle_to_grid", "grid_update",
+             "after_transfer", "pressure", "viscosity", "repressure", "particle_update", "reseed"]
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["total_ms"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded NB-FLIP dam-break scene)",
+        "config": {"workload": f"nb_dam_break_{args.res}_obstacle", "solver": "NBFlipSolver",
+                   "grid": args.res, "seed": SEED, "particles": int(r["work"] / args.steps),
+                   "pcg": "PCG+IPP FP32, reference stopping (limit 1000, abs tol 1e-6 max-abs)",
+                   "l2": "flushed between steps (256 MiB write)", "warm_frames": NB_WARM_FRAMES},
+        "cell_substeps_per_s": r["cells"] * args.steps / (r["total_ms"] / 1e3),
+        "pcg_cell_iter_per_s": cell_iters / (r["pcg_ms"] / 1e3) if r["pcg_ms"] > 0 else None,
+        "pressure_iterations_per_step": r["pressure_iters"],
+        "stage_ms_per_step": {n: round(v, 4) for n, v in zip(names, r["stage_ms"]) if v > 0},
+        "e2e": r["e2e"], "gpu_launches": int(r["launches"]),
+        "roofline": {"bound": "hbm", "kernel": "k_pcg_resident", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+                     "traffic": None, "peak_source": peak_kind,
+                     "bytes_model": "per solve 16 B/cell + 34 B/cell-iteration",
+                     "launches": args.steps, "avg_launch_ms": r["pcg_ms"] / args.steps},
+        "cpu_baseline": cpu, "clocks": clocks,
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def poisson_arm(args):
     """Standalone mixed-precision pressure solves (--poisson N): the spec-mode
     solve to a 1e-6 true relative residual on a seeded 55 %-fluid star mask
@@ -731,6 +922,8 @@ def main():
                     help="time N scenes stepped together (fs_batch) instead")
     ap.add_argument("--solve-batch", type=int, default=0,
                     help="time N standalone systems of side --res solved in one merged launch")
+    ap.add_argument("--nbflip", action="store_true",
+                    help="NB-FLIP (NBFlipSolver) substeps of the narrow-band dam break at --res")
     ap.add_argument("--serve", type=int, default=0,
                     help="serve R requests of the seeded request stream instead")
     ap.add_argument("--single-sample", type=int, default=32,
@@ -749,6 +942,8 @@ def main():
         return serve_arm(args)
     if args.solve_batch:
         return solve_batch_arm(args)
+    if args.nbflip:
+        return nbflip_arm(args)
     if args.impl == "reference":
         return reference_arm(args)
     return gpu_arm(args)
