@@ -267,6 +267,7 @@ static fs_status alloc_particles(fs_solver *s, int cap)
     for (void *q : old) dfree(s, q);
     dfree(s, s->rebin_scratch);
     P.cap = cap;
+    P.bound = cap;
     const size_t n = (size_t)std::max(cap, 1);
     TRY(dalloc(s, &P.pos, n));
     TRY(dalloc(s, &P.vel, n));
@@ -319,6 +320,7 @@ static fs_status upload_particles(fs_solver *s, const std::vector<int> &counts,
     }
     CK(cudaStreamSynchronize(s->st));
     s->after_advect = false;
+    if (s->nb) P.bound = std::max(total, 1);
     return FS_OK;
 }
 
@@ -1074,7 +1076,11 @@ static fs_status stage(fs_solver *s, int which, bool in_step)
     case FS_STAGE_RESEED: // sources only, or NB-FLIP's band reseeding
         if (s->nb) {
             launch_nb_candidates(d, s->sp, s->G, s->R, s->nb_scan, q);
-            launch_nb_append(s->P, s->R, s->nb_max_cand, s->rebin_scratch, q);
+            // the candidate total sizes the append's launches (one small read)
+            int ncand = 0;
+            CK(cudaMemcpyAsync(&ncand, s->R.cand_off + s->ncell, sizeof(int), cudaMemcpyDeviceToHost, q));
+            CK(cudaStreamSynchronize(q));
+            launch_nb_append(s->P, s->R, ncand, s->rebin_scratch, q);
             int bits = 0;
             while ((1 << bits) < s->P.nbins) bits++;
             g_kernel_launches += 6 + 16 + 5 * ((bits + 7) / 8);
@@ -1172,6 +1178,18 @@ template <class Mark> static fs_status step_flip(fs_solver *s, bool timed, Mark 
     return FS_OK;
 }
 
+// NB-FLIP's particle count changes every substep (reseeding): per-slot
+// launches are sized by the occupied slots, read here (the stream is idle at
+// a substep's start in the frame loop, so the read costs one round trip)
+static fs_status nb_refresh_bound(fs_solver *s)
+{
+    int n = 0;
+    CK(cudaMemcpyAsync(&n, s->P.bin_start + s->P.nbins, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    s->P.bound = std::max(1, std::min(n, s->P.cap));
+    return FS_OK;
+}
+
 // NBFlipSolver::step (nbflipsolver.cpp:26-64) ends its stages as: advection;
 // rebin; particle to grid (P2G, extrapolation, saved grid); after transfer
 // (inside gridUpdate, :213-225: SDF, outside level set, combination, inside
@@ -1192,6 +1210,7 @@ static fs_status step_impl(fs_solver *s)
     k_set_dt<<<1, 1, 0, s->st>>>(s->sc, s->step_dt);
     g_kernel_launches += 1;
     if (s->nb) {
+        TRY(nb_refresh_bound(s));
         static const int groups[9][4] = {
             {FS_STAGE_ADVECT, -1},
             {FS_STAGE_REBIN, -1},
@@ -1339,6 +1358,7 @@ extern "C" fs_status fs_run_stage(fs_solver *s, int which)
     // its own comes after it (two level sets on one set of buffers race)
     TRY(wait_side(s));
     k_set_dt<<<1, 1, 0, s->st>>>(s->sc, s->step_dt);
+    if (s->nb && !s->after_advect) TRY(nb_refresh_bound(s));
     if (which == FS_STAGE_DENSITY) CK(cudaMemsetAsync(&s->sc->density_iters, 0, sizeof(int), s->st));
     if (which == FS_STAGE_PROJECT) CK(cudaMemsetAsync(&s->sc->pressure_iters, 0, sizeof(int), s->st));
     TRY(stage(s, which, false));
@@ -1494,6 +1514,7 @@ extern "C" fs_status fs_set_particles(fs_solver *s, const int32_t *bin_counts, c
     CK(cudaGetLastError());
     s->after_advect = false;
     s->initialized = true;
+    if (s->nb) P.bound = std::max((int)total, 1);
     return FS_OK;
 }
 

@@ -203,7 +203,7 @@ void launch_nb_advect_extra(const GridDims &d, const SceneParams &sp, const Part
                             const Grids &G, const NbGrids &N, const Scalars *sc, cudaStream_t st)
 {
     if (P.cap > 0)
-        k_nb_prune_band<<<nblk(P.cap, kThreads), kThreads, 0, st>>>(d, P, G.fluid_sdf, G.counts,
+        k_nb_prune_band<<<nblk(P.bound, kThreads), kThreads, 0, st>>>(d, P, G.fluid_sdf, G.counts,
                                                                     2 * sp.particlesPerCell);
     const long long n = (long long)(d.ni + 1) * d.nj + (long long)d.ni * (d.nj + 1) +
                         2LL * d.ni * d.nj;

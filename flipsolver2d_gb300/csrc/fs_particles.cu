@@ -213,7 +213,7 @@ void launch_advect(const GridDims &d, const Particles &P, const Grids &G, const 
                    cudaStream_t st)
 {
     if (P.cap == 0) return;
-    k_advect<<<nblk(P.cap, kThreads), kThreads, 0, st>>>(d, P, G.u, G.v, G.solid_sdf,
+    k_advect<<<nblk(P.bound, kThreads), kThreads, 0, st>>>(d, P, G.u, G.v, G.solid_sdf,
                                                          G.material, sc);
 }
 
@@ -420,14 +420,15 @@ __global__ void k_scatter_incoming(Particles P)
 void launch_rebin(const GridDims &d, Particles &P, void *scratch, size_t, cudaStream_t st)
 {
     if (P.cap == 0) return;
-    const int ntiles = nblk(P.cap, kScanTile);
-    const int rtiles = nblk(P.cap, kRadixTile);
+    // scratch laid out for the capacity, launches sized for the bound
     char *p = (char *)scratch;
     int *tile_counts = (int *)p;
-    p += align256((size_t)(ntiles + 1) * sizeof(int));
+    p += align256((size_t)(nblk(P.cap, kScanTile) + 1) * sizeof(int));
     int *hist = (int *)p;
-    p += align256((size_t)(256 * rtiles + 1) * sizeof(int));
+    p += align256((size_t)(256 * nblk(P.cap, kRadixTile) + 1) * sizeof(int));
     void *scan_tmp = p;
+    const int ntiles = nblk(P.bound, kScanTile);
+    const int rtiles = nblk(P.bound, kRadixTile);
 
     k_prune<<<nblk(P.nbins, kThreads), kThreads, 0, st>>>(P);
     k_moved_tile_counts<<<ntiles, kScanBlock, 0, st>>>(P, tile_counts);
@@ -454,8 +455,8 @@ void launch_rebin(const GridDims &d, Particles &P, void *scratch, size_t, cudaSt
     scan_exclusive(P.incoming, P.inc_off, P.nbins, scan_tmp, st);
     k_new_counts<<<nblk(P.nbins, kThreads), kThreads, 0, st>>>(P);
     scan_exclusive(P.bin_count2, P.bin_start2, P.nbins, scan_tmp, st);
-    k_scatter_survivors<<<nblk(P.cap, kThreads), kThreads, 0, st>>>(P);
-    k_scatter_incoming<<<nblk(P.cap, kThreads), kThreads, 0, st>>>(P);
+    k_scatter_survivors<<<nblk(P.bound, kThreads), kThreads, 0, st>>>(P);
+    k_scatter_incoming<<<nblk(P.bound, kThreads), kThreads, 0, st>>>(P);
     // swap buffers
     float2 *tp;
     tp = P.pos; P.pos = P.pos2; P.pos2 = tp;
@@ -601,25 +602,25 @@ __global__ void k_nb_cross_fix(Particles P, NbReseed R)
     }
 }
 
-void launch_nb_append(Particles &P, const NbReseed &R, int max_cand, void *scratch,
+void launch_nb_append(Particles &P, const NbReseed &R, int ncand, void *scratch,
                       cudaStream_t st)
 {
-    if (P.cap == 0) return;
-    const int ntiles = nblk(max_cand > 0 ? max_cand : 1, kScanTile);
-    const int ptiles = nblk(P.cap, kScanTile);
-    const int rtiles = nblk(P.cap, kRadixTile);
+    if (P.cap == 0 || ncand <= 0) return;
     char *p = (char *)scratch;
     int *tile_counts = (int *)p;
-    p += align256((size_t)(ptiles + 1) * sizeof(int));
+    p += align256((size_t)(nblk(P.cap, kScanTile) + 1) * sizeof(int));
     int *hist = (int *)p;
-    p += align256((size_t)(256 * rtiles + 1) * sizeof(int));
+    p += align256((size_t)(256 * nblk(P.cap, kRadixTile) + 1) * sizeof(int));
     void *scan_tmp = p;
-    const int *ncand = R.cand_off + R.ncell;
+    // the candidates and the occupied slots are known bounds here
+    const int ntiles = nblk(ncand, kScanTile);
+    const int rtiles = nblk(ncand, kRadixTile);
+    const int *ncand_dev = R.cand_off + R.ncell;
 
     k_nb_bins_init<<<nblk(P.nbins, kThreads), kThreads, 0, st>>>(P);
-    k_nb_keep_tile_counts<<<ntiles, kScanBlock, 0, st>>>(R.cand_bin, ncand, tile_counts);
+    k_nb_keep_tile_counts<<<ntiles, kScanBlock, 0, st>>>(R.cand_bin, ncand_dev, tile_counts);
     scan_exclusive(tile_counts, tile_counts, ntiles, scan_tmp, st);
-    k_nb_keep_write<<<ntiles, kScanBlock, 0, st>>>(P, R.cand_bin, ncand, tile_counts);
+    k_nb_keep_write<<<ntiles, kScanBlock, 0, st>>>(P, R.cand_bin, ncand_dev, tile_counts);
     int bits = 0;
     while ((1 << bits) < P.nbins) bits++;
     int *kin = P.mkey, *vin = P.mval, *kout = P.mkey2, *vout = P.mval2;
@@ -638,8 +639,8 @@ void launch_nb_append(Particles &P, const NbReseed &R, int max_cand, void *scrat
     scan_exclusive(P.incoming, P.inc_off, P.nbins, scan_tmp, st);
     k_new_counts<<<nblk(P.nbins, kThreads), kThreads, 0, st>>>(P);
     scan_exclusive(P.bin_count2, P.bin_start2, P.nbins, scan_tmp, st);
-    k_nb_scatter_live<<<nblk(P.cap, kThreads), kThreads, 0, st>>>(P, R.status);
-    k_nb_scatter_new<<<nblk(max_cand > 0 ? max_cand : 1, kThreads), kThreads, 0, st>>>(P, R);
+    k_nb_scatter_live<<<nblk(P.bound, kThreads), kThreads, 0, st>>>(P, R.status);
+    k_nb_scatter_new<<<nblk(ncand, kThreads), kThreads, 0, st>>>(P, R);
     k_nb_cross_fix<<<1, 1, 0, st>>>(P, R);
     float2 *tp;
     tp = P.pos; P.pos = P.pos2; P.pos2 = tp;
@@ -648,6 +649,8 @@ void launch_nb_append(Particles &P, const NbReseed &R, int max_cand, void *scrat
     int *ti = P.slot_bin; P.slot_bin = P.slot_bin2; P.slot_bin2 = ti;
     ti = P.bin_start; P.bin_start = P.bin_start2; P.bin_start2 = ti;
     ti = P.bin_count; P.bin_count = P.bin_count2; P.bin_count2 = ti;
+    const long long nb = (long long)P.bound + ncand;
+    P.bound = nb < (long long)P.cap ? (int)nb : P.cap;
 }
 
 // ---------------------------------------------------------------------------
@@ -740,11 +743,11 @@ void launch_adjust(const GridDims &d, const SceneParams &sp, const Particles &P,
 {
     if (P.cap == 0) return;
     if (is_double)
-        k_adjust<double><<<nblk(P.cap, kThreads), kThreads, 0, st>>>(
+        k_adjust<double><<<nblk(P.bound, kThreads), kThreads, 0, st>>>(
             d, P, (const double *)pressure, G.material, sp.fluidDensity, sp.dx, sc,
             sp.pcgIterLimit);
     else
-        k_adjust<float><<<nblk(P.cap, kThreads), kThreads, 0, st>>>(
+        k_adjust<float><<<nblk(P.bound, kThreads), kThreads, 0, st>>>(
             d, P, (const float *)pressure, G.material, sp.fluidDensity, sp.dx, sc,
             sp.pcgIterLimit);
 }
@@ -778,7 +781,7 @@ void launch_g2p(const GridDims &d, const SceneParams &sp, const Particles &P, co
                 cudaStream_t st)
 {
     if (P.cap == 0) return;
-    k_g2p<<<nblk(P.cap, kThreads), kThreads, 0, st>>>(d, P, G.u, G.v, G.su, G.sv, sp.picRatio);
+    k_g2p<<<nblk(P.bound, kThreads), kThreads, 0, st>>>(d, P, G.u, G.v, G.su, G.sv, sp.picRatio);
 }
 
 // ---------------------------------------------------------------------------
@@ -876,7 +879,7 @@ void launch_max_velocity(const Particles &P, Scalars *sc, cudaStream_t st)
 {
     k_reset_maxv2<<<1, 1, 0, st>>>(sc);
     if (P.cap == 0) return;
-    k_max_v2<<<nblk(P.cap, kThreads), kThreads, 0, st>>>(P, sc);
+    k_max_v2<<<nblk(P.bound, kThreads), kThreads, 0, st>>>(P, sc);
 }
 
 } // namespace fsg

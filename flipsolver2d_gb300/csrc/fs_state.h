@@ -53,6 +53,8 @@ struct Particles {
     int *mkey = nullptr, *mval = nullptr, *mkey2 = nullptr, *mval2 = nullptr; // moved list
     int *nmoved = nullptr;     // device scalar
     int cap = 0;               // slot capacity
+    int bound = 0;             // launch bound for per-slot kernels: >= the occupied slots
+                               // (the capacity, or NB-FLIP's count read at each substep)
     int nbins = 0;
 };
 
@@ -183,7 +185,8 @@ void launch_nb_combine(const GridDims &d, const Grids &G, const NbGrids &N, cuda
 void launch_nb_materials(const GridDims &d, const Grids &G, cudaStream_t st);
 void launch_nb_candidates(const GridDims &d, const SceneParams &sp, const Grids &G,
                           const NbReseed &R, void *scan_scratch, cudaStream_t st);
-void launch_nb_append(Particles &P, const NbReseed &R, int max_cand, void *scratch,
+// ncand: the candidate total of launch_nb_candidates, read back by the host
+void launch_nb_append(Particles &P, const NbReseed &R, int ncand, void *scratch,
                       cudaStream_t st);
 
 // exclusive scan of n ints (out may alias nothing); writes the total to out[n]
