@@ -759,15 +759,21 @@ void launch_vel_extrapolate(const GridDims &d, Grids &G, const SceneParams &sp,
 // works in pass p only if a tile within one tile of it assigned cells in pass
 // p-1: the frontier of layer p*H is otherwise out of its reach.  Once a pass
 // assigns nothing, the remaining passes return immediately.
-// 64 x 64 tiles with a 32-cell halo: (64 + 64)^2 cells of (marker, value)
-// plus two frontier lists, 192 KiB of dynamic shared memory; 32 layers a
-// pass.  Larger tiles than the velocity extrapolation's cut the halo cells a
-// tile reloads per interior cell (4x against 14x for 32 x 32 with 15) and the
-// number of passes.
-constexpr int kLsTile = 64;
-constexpr int kLsH = 32;
-constexpr int kLsW = kLsTile + 2 * kLsH;
-constexpr size_t kLsSmem = (size_t)kLsW * kLsW * (4 + 4 + 2 + 2) + 16;
+// Two tile shapes (T x T tiles with an H-cell halo, 1024 threads a tile):
+// - 64 x 64 with H = 32: (64 + 64)^2 cells of (marker, value) plus two
+//   frontier lists, 192 KiB of dynamic shared memory, 32 layers a pass;
+// - 86 x 86 with H = 24: 210 KiB, 24 layers a pass.  At 1024^2 this is 144
+//   tiles, one wave on 152 SMs, where 64 x 64 tiles need two waves a pass.
+// launch_levelset picks the shape with the fewer waves per layer.  Larger
+// tiles than the velocity extrapolation's cut the halo cells a tile reloads
+// per interior cell and the number of passes.
+template <int T, int H> struct LsShape {
+    static constexpr int kTile = T, kHalo = H, kW = T + 2 * H;
+    static constexpr size_t kSmem = (size_t)kW * kW * (4 + 4 + 2 + 2) + 16;
+};
+using LsNarrow = LsShape<64, 32>;
+using LsWide = LsShape<86, 24>;
+static_assert(LsWide::kW * LsWide::kW < 32768, "frontier indices are shorts");
 
 __device__ __forceinline__ unsigned long long ls_pack(int mark, float v)
 {
@@ -791,13 +797,15 @@ __global__ void k_levelset_init(GridDims d, const float *__restrict__ sdf,
     if (c < passes) active[c] = 0;
 }
 
+template <class S>
 __global__ void __launch_bounds__(1024, 1) k_levelset_pass(GridDims d, float *__restrict__ sdf,
                                                        unsigned long long *__restrict__ cells,
                                                        uint8_t *__restrict__ act,
                                                        int *__restrict__ active, int pass, int add)
 {
     extern __shared__ int ls_smem[];
-    constexpr int W = kLsW;
+    constexpr int W = S::kW;
+    constexpr int kLsTile = S::kTile, kLsH = S::kHalo;
     struct {
         int *mark;
         float *val;
@@ -878,14 +886,33 @@ __global__ void __launch_bounds__(1024, 1) k_levelset_pass(GridDims d, float *__
     }
 }
 
+// waves per BFS layer: a pass of H layers plus the tile load (about five
+// layers' time) runs its tiles in ceil(tiles / SMs) waves
+static bool ls_wide(const GridDims &d)
+{
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
+            sms = 1;
+    }
+    auto cost = [&](int T, int H) {
+        const long long tiles = (long long)nblk(d.ni, T) * nblk(d.nj, T);
+        return (double)((tiles + sms - 1) / sms) * (H + 5) / H;
+    };
+    return cost(LsWide::kTile, LsWide::kHalo) < cost(LsNarrow::kTile, LsNarrow::kHalo);
+}
+
 int levelset_max_passes(const GridDims &d)
 {
     int m = d.ni > d.nj ? d.ni : d.nj;
-    return m / kLsH + 2;
+    return m / (ls_wide(d) ? LsWide::kHalo : LsNarrow::kHalo) + 2;
 }
 
-void launch_levelset(const GridDims &d, Grids &G, bool outside, cudaStream_t st)
+template <class S> static void launch_levelset_shape(const GridDims &d, Grids &G, bool outside, cudaStream_t st)
 {
+    constexpr int kLsTile = S::kTile;
     const int passes = levelset_max_passes(d);
     dim3 grid(nblk(d.nj, kLsTile), nblk(d.ni, kLsTile));
     const int ntiles = grid.x * grid.y;
@@ -897,11 +924,17 @@ void launch_levelset(const GridDims &d, Grids &G, bool outside, cudaStream_t st)
                                                                G.levelset_act, ntiles,
                                                                G.levelset_active, passes,
                                                                outside ? 1 : 0);
-    cudaFuncSetAttribute((const void *)k_levelset_pass, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)kLsSmem);
+    cudaFuncSetAttribute((const void *)k_levelset_pass<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)S::kSmem);
     for (int p = 0; p < passes; p++)
-        k_levelset_pass<<<grid, 1024, kLsSmem, st>>>(d, G.fluid_sdf, cells, G.levelset_act,
-                                                      G.levelset_active, p, outside ? 1 : -1);
+        k_levelset_pass<S><<<grid, 1024, S::kSmem, st>>>(d, G.fluid_sdf, cells, G.levelset_act,
+                                                          G.levelset_active, p, outside ? 1 : -1);
+}
+
+void launch_levelset(const GridDims &d, Grids &G, bool outside, cudaStream_t st)
+{
+    if (ls_wide(d)) launch_levelset_shape<LsWide>(d, G, outside, st);
+    else launch_levelset_shape<LsNarrow>(d, G, outside, st);
 }
 
 // ---------------------------------------------------------------------------

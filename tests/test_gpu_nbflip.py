@@ -217,3 +217,33 @@ def test_rng_state_roundtrip_and_batch_refusal(gpu_lib):
     f = gpu.GpuFlipSolver(scenes.dam_break(32, seed=1))
     fs = f.get_rng()
     assert fs[624] == 624 and fs[0] == 1  # std::mt19937(1) before any draw
+
+
+@pytest.mark.parametrize("shape", [(900, 1000), (1024, 1024)])
+def test_level_sets_on_large_grids(port_lib, gpu_lib, shape):
+    """The inside and outside level sets at sizes where the 86 x 86 tiles
+    (one wave a pass) are used: a synthetic field with a particle-SDF-like
+    band, deep unknown regions (values above NI * NJ) and fluid pockets,
+    bit-exact against the oracle's FIFO BFS."""
+    ni, nj = shape
+    sc = scenes.nb_dam_break(max(ni, nj), seed=4)
+    sc.params.domainSizeI, sc.params.domainSizeJ = ni / max(ni, nj), nj / max(ni, nj)
+    o = fo.OracleSolver(sc, "port")
+    g = gpu.GpuFlipSolver(sc, precision=gpu.FS_PCG_FP64, pool_threads=POOL_THREADS)
+    assert (o.ni, o.nj) == (g.ni, g.nj) == (ni, nj)
+    rng = np.random.default_rng(ni)
+    ii, jj = np.meshgrid(np.arange(ni), np.arange(nj), indexing="ij")
+    sdf = np.full((ni, nj), 1.8446743e19, np.float32)  # no particle nearby
+    for _ in range(6):  # rings of known values around random centres
+        ci, cj, r = rng.uniform(0, ni), rng.uniform(0, nj), rng.uniform(20, 200)
+        d = np.sqrt((ii - ci) ** 2 + (jj - cj) ** 2) - r
+        band = np.abs(d) < 2.5
+        sdf[band] = np.minimum(sdf[band], (d[band] * 0.7).astype(np.float32))
+    for stage, field in ((fo.LEVELSET_OUTSIDE, sdf),
+                         (fo.LEVELSET, np.where(sdf > 1e6, rng.uniform(-1, 1, sdf.shape), sdf))):
+        f = np.ascontiguousarray(field, np.float32)
+        o.set_grid("fluid_sdf", f)
+        g.set_grid("fluid_sdf", f)
+        o.stage(stage)
+        g.stage(stage)
+        assert_grid_equal(o, g, "fluid_sdf", f"level set stage {stage} at {shape}")
