@@ -22,7 +22,8 @@ sample of the same workload.  `fp64_check` steps the final state once more
 in FP32 and in the FP64 parity mode from identical inputs and reports the
 FP32 error.  `batch` (unless --no-batch) is the batched form
 of the path beside it: 64 scenes of the batched-scenes workload stepped
-together at a 1e-6 pressure residual, and the same scenes one at a time.
+together at a 1e-6 pressure residual, and the same scenes one at a time;
+`nbflip` is the same scene stepped by the narrow-band solver (NB-FLIP).
 With --impl reference only the CPU
 implementation is timed (the reference's sources are not present on GPU
 hosts, so its plain-C restatement, pinned bit for bit to it, stands in).
@@ -414,6 +415,18 @@ def gpu_arm(args):
                              "pcg": "FS_PCG_SPEC, 1e-6 true relative residual"}
         except Exception as e:  # reported, never fatal for the main line
             line["batch"] = {"error": str(e)}
+    if rank == 0 and world == 1 and not args.no_batch:
+        # the narrow-band variant of the same scene beside it (NBFlipSolver)
+        try:
+            r = nb_measure(RES, 3, 5, local, with_e2e=False)
+            line["nbflip"] = {"workload": f"nb_dam_break_{RES}_obstacle (NBFlipSolver, 8 per cell, "
+                                          "limit 1000, tolerance 1e-6)",
+                              "value": r["work"] / (r["total_ms"] / 1e3), "unit": METRIC,
+                              "ms_per_step": r["total_ms"] / 5, "steps": 5,
+                              "cell_substeps_per_s": r["cells"] * 5 / (r["total_ms"] / 1e3),
+                              "particles": int(r["work"] / 5)}
+        except Exception as e:  # reported, never fatal for the main line
+            line["nbflip"] = {"error": str(e)}
     if rank == 0:
         print(json.dumps(line))
     if dist:

@@ -168,35 +168,30 @@ __device__ __forceinline__ float2 rk4_integrate(const float *__restrict__ u, con
 }
 
 // FlipSolver::eulerAdvectionThread (flipsolver2d.cpp:340-351) for the four
-// grids of NBFlipSolver::advect (:66-109) in one launch: every sample (i, j)
-// of U, V, the fluid SDF and the viscosity traced back by rk4Integrate(-dt)
-// and the input grid (with its offset) sampled there
+// grids of NBFlipSolver::advect (:66-109) in one launch.  Every sample (i, j)
+// of U, V, the fluid SDF and the viscosity starts its rk4Integrate(-dt) trace
+// at Vec3(i, j) through the same velocity grid, so the trace is computed once
+// per lattice point (i, j), 0 <= i <= NI, 0 <= j <= NJ, and every grid that
+// has a sample (i, j) is sampled there (with its own offset).
 __global__ void k_nb_euler(GridDims d, const float *__restrict__ u, const float *__restrict__ v,
                            const float *__restrict__ sdf, const float *__restrict__ visc,
                            float *__restrict__ au, float *__restrict__ av, float *__restrict__ asdf,
                            float *__restrict__ avisc, const Scalars *__restrict__ sc)
 {
-    const long long nu = (long long)(d.ni + 1) * d.nj, nv = (long long)d.ni * (d.nj + 1);
-    const long long nc = (long long)d.ni * d.nj;
-    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const float *in;
-    float *out;
-    int si, sj;
-    float ox, oy;
-    if (e < nu) {
-        in = u; out = au; si = d.ni + 1; sj = d.nj; ox = 0.5f; oy = 0.f;
-    } else if ((e -= nu) < nv) {
-        in = v; out = av; si = d.ni; sj = d.nj + 1; ox = 0.f; oy = 0.5f;
-    } else if ((e -= nv) < nc) {
-        in = sdf; out = asdf; si = d.ni; sj = d.nj; ox = 0.f; oy = 0.f;
-    } else if ((e -= nc) < nc) {
-        in = visc; out = avisc; si = d.ni; sj = d.nj; ox = 0.5f; oy = 0.5f;
-    } else {
-        return;
-    }
-    const long long i = e / sj, j = e - i * sj;
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long cols = d.nj + 1;
+    if (e >= (long long)(d.ni + 1) * cols) return;
+    const int i = (int)(e / cols), j = (int)(e - (long long)i * cols);
     const float2 p = rk4_integrate(u, v, d, make_float2((float)i, (float)j), -sc->dt);
-    out[e] = grid_lerp(in, si, sj, ox, oy, p.x, p.y);
+    if (j < d.nj) au[(size_t)i * d.nj + j] = grid_lerp(u, d.ni + 1, d.nj, 0.5f, 0.f, p.x, p.y);
+    if (i < d.ni) {
+        av[(size_t)i * (d.nj + 1) + j] = grid_lerp(v, d.ni, d.nj + 1, 0.f, 0.5f, p.x, p.y);
+        if (j < d.nj) {
+            const size_t c = (size_t)i * d.nj + j;
+            asdf[c] = grid_lerp(sdf, d.ni, d.nj, 0.f, 0.f, p.x, p.y);
+            avisc[c] = grid_lerp(visc, d.ni, d.nj, 0.5f, 0.5f, p.x, p.y);
+        }
+    }
 }
 
 void launch_nb_advect_extra(const GridDims &d, const SceneParams &sp, const Particles &P,
@@ -205,8 +200,7 @@ void launch_nb_advect_extra(const GridDims &d, const SceneParams &sp, const Part
     if (P.cap > 0)
         k_nb_prune_band<<<nblk(P.bound, kThreads), kThreads, 0, st>>>(d, P, G.fluid_sdf, G.counts,
                                                                     2 * sp.particlesPerCell);
-    const long long n = (long long)(d.ni + 1) * d.nj + (long long)d.ni * (d.nj + 1) +
-                        2LL * d.ni * d.nj;
+    const long long n = (long long)(d.ni + 1) * (d.nj + 1);
     k_nb_euler<<<nblk(n, kThreads), kThreads, 0, st>>>(d, G.u, G.v, G.fluid_sdf, G.visc, N.adv_u,
                                                        N.adv_v, N.adv_sdf, N.adv_visc, sc);
 }
