@@ -9,9 +9,12 @@ same headers, as CSV (the reference writes XLSX through OpenXLSX, which is
 not part of this path).
 
 Stage times are device times from CUDA events (fs_get_stage_time); the
-frame time is the host wall time of fs_step_frame.  The reference's grid
-update includes particle-to-grid, which is fused into it here, so "Particle
-to grid" is 0; viscosity is not on this path, so its columns are 0.
+frame time is the host wall time of fs_step_frame.  For FLIP scenes the
+reference's grid update includes particle-to-grid, which is fused into it
+here, so "Particle to grid" is 0.  NB-FLIP scenes (simType "nbflip") end
+their stages as NBFlipSolver::step does (nbflipsolver.cpp:26-64): particle to
+grid on its own, no density correction, the level sets in after transfer.
+Viscosity is not on this path, so its columns are 0.
 
     python -m flipsolver2d_gb300.autobench scene.json [more.json] --frames 60 --out stats.csv
 """

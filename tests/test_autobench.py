@@ -44,3 +44,17 @@ def test_stage_times_add_up(gpu_lib):
         assert np.all(stages >= 0.0) and stages[1] > 0 and stages[7] > 0
         assert stages[4] == 0.0 and stages[8] == 0.0 and stages[9] == 0.0
         assert r[2] >= 0.9 * stages.sum()  # the wall time covers the device stages
+
+
+@pytest.mark.gpu
+def test_nbflip_stage_times(gpu_lib):
+    """NB-FLIP ends its stages differently (nbflipsolver.cpp:26-64): particle
+    to grid has its own time, there is no density correction, and the level
+    sets count in after transfer."""
+    rows = autobench.run_scene(scenes.nb_dam_break(96, seed=3), 3)
+    for r in rows[1:]:
+        stages = np.array(r[3:15])
+        assert np.all(stages >= 0.0)
+        assert stages[4] > 0 and stages[6] > 0 and stages[7] > 0 and stages[11] > 0
+        assert stages[2] == 0.0 and stages[8] == 0.0 and stages[9] == 0.0
+        assert r[2] >= 0.9 * stages.sum()
