@@ -43,6 +43,10 @@ from . import gpu, scenes
 # right-hand side and solution, plus the small per-system scalars
 SOLVE_BYTES_PER_CELL = 18
 SOLVE_BYTES_FIXED = 512
+# above the on-chip limit of the cluster solve (about 512^2 cells) a system
+# is solved by the chained cooperative kernel with five FP32 vectors
+SOLVE_CHAIN_CELLS = 512 * 512
+SOLVE_CHAIN_BYTES_PER_CELL = 20
 
 
 def scene_bytes_estimate(scene) -> int:
@@ -132,6 +136,8 @@ class Server:
             else:
                 mat = rq.problem[0]
                 need = SOLVE_BYTES_PER_CELL * mat.size + SOLVE_BYTES_FIXED
+                if mat.size > SOLVE_CHAIN_CELLS:
+                    need += SOLVE_CHAIN_BYTES_PER_CELL * mat.size
                 if self.used_bytes() + need > self.budget:
                     keep.append(rq)
                     continue
