@@ -437,20 +437,36 @@ struct BfsTile {
 
 // average over the 8-neighbourhood in the reference's order, neighbours with
 // a smaller marker only, summed in double
+// the markers of the eight neighbours of (r, q) in the reference's order,
+// kMarkOut outside the window
 template <int W>
-__device__ __forceinline__ double bfs_avg(const int *mark, const float *val, int r, int q, int k,
-                                          int &count)
+__device__ __forceinline__ void bfs_marks(const int *mark, int r, int q, int nm[8])
 {
-    double avg = 0;
-    count = 0;
+    int k = 0;
 #pragma unroll
     for (int io = -1; io <= 1; io++)
 #pragma unroll
         for (int jo = -1; jo <= 1; jo++) {
             if (io == 0 && jo == 0) continue;
             const int rr = r + io, qq = q + jo;
-            if (rr < 0 || rr >= W || qq < 0 || qq >= W) continue;
-            const int mk = mark[rr * W + qq];
+            nm[k++] = (rr < 0 || rr >= W || qq < 0 || qq >= W) ? kMarkOut : mark[rr * W + qq];
+        }
+}
+
+template <int W>
+__device__ __forceinline__ double bfs_avg(const int *nm, const float *val, int r, int q, int k,
+                                          int &count)
+{
+    double avg = 0;
+    count = 0;
+    int t = 0;
+#pragma unroll
+    for (int io = -1; io <= 1; io++)
+#pragma unroll
+        for (int jo = -1; jo <= 1; jo++) {
+            if (io == 0 && jo == 0) continue;
+            const int rr = r + io, qq = q + jo;
+            const int mk = nm[t++];
             if (mk == kMarkOut) continue;
             if (mk < k) {
                 avg += (double)val[rr * W + qq];
@@ -480,20 +496,20 @@ __device__ __forceinline__ void ls_two_sum(float a, float b, float &s, float &e)
 // double exactly like the reference.  Either way the result is the
 // reference's float.
 template <int W>
-__device__ __forceinline__ float bfs_layer_value(const int *mark, const float *val, int r, int q, int k,
+__device__ __forceinline__ float bfs_layer_value(const int *nm, const float *val, int r, int q, int k,
                                                  int add)
 {
     float s = 0.f, eh = 0.f, el = 0.f, m = 0.f;
     int count = 0, mine = INT_MAX;
     bool el_exact = true;
+    int t = 0;
 #pragma unroll
     for (int io = -1; io <= 1; io++)
 #pragma unroll
         for (int jo = -1; jo <= 1; jo++) {
             if (io == 0 && jo == 0) continue;
             const int rr = r + io, qq = q + jo;
-            if (rr < 0 || rr >= W || qq < 0 || qq >= W) continue;
-            const int mk = mark[rr * W + qq];
+            const int mk = nm[t++];
             if (mk == kMarkOut || mk >= k) continue;
             const float x = val[rr * W + qq];
             float t2, er, t3, er2;
@@ -504,7 +520,11 @@ __device__ __forceinline__ float bfs_layer_value(const int *mark, const float *v
             el_exact &= er2 == 0.f;
             el += er2;
             m += fabsf(x);
-            if (x != 0.f) mine = min(mine, ilogbf(x));
+            if (x != 0.f) {
+                // ilogbf from the exponent field for normal numbers
+                const int ex = (__float_as_int(x) >> 23) & 255;
+                mine = min(mine, (ex != 0 && ex != 255) ? ex - 127 : ilogbf(x));
+            }
             count++;
         }
     const float cf = (float)count;
@@ -554,27 +574,12 @@ __device__ __forceinline__ float bfs_layer_value(const int *mark, const float *v
     if (count > 0 && isfinite(f) && isfinite(m) && fabsf(f) >= 0x1p-100f &&
         fabsf(d) + bound < 0.99f * gap)
         return f;
-    const double avg = bfs_avg<W>(mark, val, r, q, k, count);
+    const double avg = bfs_avg<W>(nm, val, r, q, k, count);
     // dividing by 1, 2, 4 or 8 is an exact scaling, the same as multiplying
     // by the reciprocal -- and a multiply has a fraction of the latency
     const double inv2 = count == 1 ? 1.0 : count == 2 ? 0.5 : count == 4 ? 0.25 : 0.125;
     const double a = (count & (count - 1)) == 0 ? avg * inv2 : avg / count;
     return add != 0 ? (float)(a + (double)add) : (float)a;
-}
-
-template <int W>
-__device__ __forceinline__ bool bfs_touches(const int *mark, int r, int q, int k)
-{
-#pragma unroll
-    for (int io = -1; io <= 1; io++)
-#pragma unroll
-        for (int jo = -1; jo <= 1; jo++) {
-            if (io == 0 && jo == 0) continue;
-            const int rr = r + io, qq = q + jo;
-            if (rr < 0 || rr >= W || qq < 0 || qq >= W) continue;
-            if (mark[rr * W + qq] == k) return true;
-        }
-    return false;
 }
 
 // Advance layers k0+1 .. k0+H of the breadth-first extrapolation inside a
@@ -612,21 +617,24 @@ __device__ __forceinline__ void bfs_layers(int *mark, float *val, short *fa, sho
     __syncthreads();
     // claims the unmarked neighbours of cell e for layer k + 1 and lists them
     // (all threads of a warp call it; `live` says whether e is a real cell)
-    auto expand = [&](bool live, int e, int k, short *out, int *counter) {
+    // nm: the neighbours' markers read before (a claim by another thread
+    // since then only makes the compare-and-swap fail)
+    auto expand = [&](bool live, int e, const int *nm, int k, short *out, int *counter) {
         int r = 0, q = 0;
         unsigned got = 0; // bit (io+1)*3+(jo+1) for each neighbour claimed
         if (live) {
             r = e / W;
             q = e - r * W;
+            int t = 0;
 #pragma unroll
             for (int io = -1; io <= 1; io++)
 #pragma unroll
                 for (int jo = -1; jo <= 1; jo++) {
                     if (io == 0 && jo == 0) continue;
-                    const int rr = r + io, qq = q + jo;
-                    if (rr < 0 || rr >= W || qq < 0 || qq >= W) continue;
-                    const int n = rr * W + qq;
-                    if (mark[n] == kMarkInf && atomicCAS(&mark[n], kMarkInf, k + 1) == kMarkInf)
+                    const int mk = nm[t++];
+                    if (mk != kMarkInf) continue; // also outside the window (kMarkOut)
+                    const int n = (r + io) * W + (q + jo);
+                    if (atomicCAS(&mark[n], kMarkInf, k + 1) == kMarkInf)
                         got |= 1u << ((io + 1) * 3 + (jo + 1));
                 }
         }
@@ -638,7 +646,10 @@ __device__ __forceinline__ void bfs_layers(int *mark, float *val, short *fa, sho
     // layer k0 (final from earlier passes) discovers layer k0 + 1
     for (int e0 = 0; e0 < W * W; e0 += blockDim.x) {
         const int e = e0 + (int)threadIdx.x;
-        expand(e < W * W && mark[e] == k0, e, k0, fa, &cnt[(k0 + 1) % 3]);
+        const bool live = e < W * W && mark[e] == k0;
+        int nm[8];
+        if (live) bfs_marks<W>(mark, e / W, e - (e / W) * W, nm);
+        expand(live, e, nm, k0, fa, &cnt[(k0 + 1) % 3]);
     }
     __syncthreads();
     short *cur = fa, *nxt = fb;
@@ -655,12 +666,14 @@ __device__ __forceinline__ void bfs_layers(int *mark, float *val, short *fa, sho
             const int f = f0 + (int)threadIdx.x;
             const bool live = f < ncur;
             int e = 0;
+            int nm[8];
             if (live) {
                 e = cur[f];
                 const int r = e / W, q = e - r * W;
-                val[e] = bfs_layer_value<W>(mark, val, r, q, k, add);
+                bfs_marks<W>(mark, r, q, nm);
+                val[e] = bfs_layer_value<W>(nm, val, r, q, k, add);
             }
-            if (more) expand(live, e, k, nxt, &cnt[(k + 1) % 3]);
+            if (more) expand(live, e, nm, k, nxt, &cnt[(k + 1) % 3]);
         }
         __syncthreads();
         short *tmp = cur;
