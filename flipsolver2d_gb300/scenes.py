@@ -127,11 +127,15 @@ class FlipSolverParameters:
 
 @dataclass
 class SceneObject:
-    kind: str  # "solid" | "fluid" | "sink"
+    kind: str  # "solid" | "fluid" | "sink" | "source"
     verts: np.ndarray  # (n, 2) float32, metres
     friction: float = 0.0
     viscosity: float = 0.0
     divergence: float = 0.0
+    # sources (Emitter): velocity in scene units per second, applied to the
+    # grid and the new particles only when transfer_velocity is set
+    velocity: Tuple[float, float] = (0.0, 0.0)
+    transfer_velocity: bool = False
 
 
 SIM_FLIP, SIM_NBFLIP = "flip", "nbflip"
@@ -231,6 +235,19 @@ def nb_dam_break(resolution: int = 128, seed: int = 0, obstacle: bool = False,
             o.viscosity = float(viscosity)
     sc.name = "nb_" + sc.name
     sc.sim_type = SIM_NBFLIP
+    return sc
+
+
+def with_source(sc: Scene, box=(0.15, 0.3, 0.45, 0.6), velocity=(2.0, -1.0),
+                transfer: bool = True, viscosity: float = 0.0) -> Scene:
+    """The scene plus one rectangular source (FlipSolver::addSource) of the
+    given box (I0, I1, J0, J1 in metres), emitter velocity (metres per
+    second) and viscosity."""
+    i0, i1, j0, j1 = box
+    sc.objects.append(SceneObject("source", rect(i0, j0, i1, j1), viscosity=float(viscosity),
+                                  velocity=(float(velocity[0]), float(velocity[1])),
+                                  transfer_velocity=bool(transfer)))
+    sc.name += "_source"
     return sc
 
 
@@ -335,10 +352,11 @@ def scene_from_json(source, name: str = "json") -> Scene:
     (populateFlipSolverParamsFromJson, :79-136); objects are added in file
     order as addObjectFromJson does (:255-287): "solid" -> addGeometry with
     its friction, "fluid" -> addInitialFluid with its viscosity, "sink" ->
-    addSink with its divergence; disabled objects are skipped and vertices
-    are multiplied by the scene scale.  "nbflip" selects NBFlipSolver
-    (jsonscenereader.cpp creates it for that simType).  Solver types other
-    than "flip" / "fluid" / "nbflip" and "source" objects raise
+    addSink with its divergence, "source" -> addSource with its viscosity,
+    divergence, velocity and transferVelocity (emitterFromJson, :197-225);
+    disabled objects are skipped and vertices are multiplied by the scene
+    scale.  "nbflip" selects NBFlipSolver (jsonscenereader.cpp creates it for
+    that simType).  Solver types other than "flip" / "fluid" / "nbflip" raise
     UnsupportedScene."""
     import json
     import os
@@ -396,7 +414,11 @@ def scene_from_json(source, name: str = "json") -> Scene:
         elif kind == "sink":
             objs.append(SceneObject("sink", verts, divergence=float(o.get("divergence", 0.0))))
         elif kind == "source":
-            raise UnsupportedScene("source objects (emitters reseeding every substep) are not on this path")
+            vel = o.get("velocity", (0.0, 0.0))
+            objs.append(SceneObject("source", verts, viscosity=float(o.get("viscosity", 0.0)),
+                                    divergence=float(o.get("divergence", 0.0)),
+                                    velocity=(float(vel[0]), float(vel[1])),
+                                    transfer_velocity=bool(o.get("transferVelocity", False))))
         else:
             raise UnsupportedScene(f"object type {kind!r}")
     return Scene(name, p, objs, sim_type=SIM_NBFLIP if sim == "nbflip" else SIM_FLIP)

@@ -292,6 +292,13 @@ typedef struct poly {
     float a; /* friction / viscosity / divergence */
 } poly;
 
+/* Emitter (emitter.h): a polygon with the parameters the liquid solvers read */
+typedef struct source {
+    poly g;
+    float visc, div, vx, vy;
+    int transfer; /* velocityTransfer() */
+} source;
+
 typedef struct rebin_rec {
     size_t particle;
     size_t dest;
@@ -346,6 +353,8 @@ struct fso_solver {
     int nfluids;
     poly *sinks;
     int nsinks;
+    source *sources;
+    int nsources;
 
     mt19937 rng;
     /* NB-FLIP (nbflipsolver.h:63-75): the advected grids */
@@ -373,6 +382,7 @@ static inline int is_strict_fluid(const fso_solver *s, long i, long j) { return 
 static inline int is_empty(const fso_solver *s, long i, long j) { return (mat_at(s, i, j) & M_EMPTY) != 0; }
 static inline int is_solid(const fso_solver *s, long i, long j) { return (mat_at(s, i, j) & M_SOLID) != 0; }
 static inline int is_sink(const fso_solver *s, long i, long j) { return mat_at(s, i, j) == M_SINK; }
+static inline int is_source(const fso_solver *s, long i, long j) { return mat_at(s, i, j) == M_SOURCE; }
 
 /* LinearIndexable2d::linearIndex (linearindexable2d.h:30-37) */
 static inline long lin_index(const fso_solver *s, long i, long j)
@@ -688,6 +698,8 @@ void fso_destroy(fso_solver *s)
     free_polys(s->obst, s->nobst);
     free_polys(s->fluids, s->nfluids);
     free_polys(s->sinks, s->nsinks);
+    for (int k = 0; k < s->nsources; k++) free(s->sources[k].g.xy);
+    free(s->sources);
     free(s);
 }
 
@@ -700,6 +712,24 @@ static void add_poly(poly **arr, int *n, float a, const float *xy, int nv)
     g->xy = (float *)malloc((size_t)nv * 2 * sizeof(float));
     memcpy(g->xy, xy, (size_t)nv * 2 * sizeof(float));
     (*n)++;
+}
+
+int fso_add_source(fso_solver *s, const float *xy, int n, float viscosity, float divergence,
+                   float vx, float vy, int transfer) /* FlipSolver::addSource, :602-605 */
+{
+    s->sources = (source *)realloc(s->sources, (size_t)(s->nsources + 1) * sizeof(source));
+    source *e = &s->sources[s->nsources];
+    e->g.n = n;
+    e->g.a = 0.f;
+    e->g.xy = (float *)malloc((size_t)n * 2 * sizeof(float));
+    memcpy(e->g.xy, xy, (size_t)n * 2 * sizeof(float));
+    e->visc = viscosity;
+    e->div = divergence;
+    e->vx = vx;
+    e->vy = vy;
+    e->transfer = transfer != 0;
+    s->nsources++;
+    return 0;
 }
 
 int fso_add_geometry(fso_solver *s, float friction, const float *xy, int n)
@@ -730,6 +760,20 @@ static void update_sinks(fso_solver *s) /* :554-571 */
                 if (polygon_sdf(&s->sinks[k], ((float)i + 0.5f) * dx, ((float)j + 0.5f) * dx) <= 0.f) {
                     s->material[i * s->nj + j] = M_SINK;
                     s->divc[i * s->nj + j] = s->sinks[k].a;
+                }
+}
+
+static void update_sources(fso_solver *s) /* :532-552 */
+{
+    const float dx = (float)s->dx;
+    const float hdx = (float)(dx / 2.0);
+    for (long i = 0; i < s->ni; i++)
+        for (long j = 0; j < s->nj; j++)
+            for (int k = 0; k < s->nsources; k++)
+                if (polygon_sdf(&s->sources[k].g, (float)i * dx + hdx, (float)j * dx + hdx) <= 0.f) {
+                    s->material[i * s->nj + j] = M_SOURCE;
+                    s->emitter_id[i * s->nj + j] = k;
+                    s->divc[i * s->nj + j] = s->sources[k].div;
                 }
 }
 
@@ -803,6 +847,7 @@ void fso_first_frame_init(fso_solver *s)
         return;
     }
     update_sinks(s);
+    update_sources(s);
     update_solids(s);
     update_initial_fluid(s);
     seed_initial_fluid(s);
@@ -1591,8 +1636,56 @@ static void count_particles(fso_solver *s)
 }
 
 /* ------------------------------------------------------------------------ */
-/* NB-FLIP (nbflipsolver.cpp), without sources: no cell is a source and     */
-/* every emitter id is -1                                                   */
+/* sources (emitters)                                                       */
+/* ------------------------------------------------------------------------ */
+/* FlipSolver::afterTransfer (flipsolver2d.cpp:390-410): source cells take
+ * the emitter's viscosity and, when it transfers velocity, the faces (i, j)
+ * of U and V take its velocity / dx (float / double) and become valid. */
+static void sources_after_transfer(fso_solver *s)
+{
+    for (long i = 0; i < s->ni; i++)
+        for (long j = 0; j < s->nj; j++) {
+            if (!is_source(s, i, j)) continue;
+            const source *e = &s->sources[s->emitter_id[i * s->nj + j]];
+            s->visc_grid[i * s->nj + j] = e->visc;
+            if (e->transfer) {
+                s->u[i * s->nj + j] = (float)((double)e->vx / s->dx);
+                s->v[i * (s->nj + 1) + j] = (float)((double)e->vy / s->dx);
+                s->uvalid[i * s->nj + j] = 1;
+                s->vvalid[i * (s->nj + 1) + j] = 1;
+            }
+        }
+}
+
+/* FlipSolver::reseedParticles (flipsolver2d.cpp:627-680): source cells with
+ * fewer than particlesPerCell / 2 particles get the difference, jittered,
+ * with the grid velocity there when the emitter transfers velocity (else
+ * zero) and the emitter's viscosity, stored through the cell's bin as in
+ * seedInitialFluid. */
+static void flip_reseed(fso_solver *s)
+{
+    for (long i = 0; i < s->ni; i++)
+        for (long j = 0; j < s->nj; j++) {
+            const long l = i * s->nj + j;
+            const int additional = (s->p.particlesPerCell / 2) - s->counts[l];
+            if (additional <= 0 || !is_source(s, i, j)) continue;
+            const source *e = &s->sources[s->emitter_id[l]];
+            pbin *cellbin = &s->bins[bin_of_cell(s, i, j)];
+            for (int q = 0; q < additional; q++) {
+                float x = (float)i + mt_uniform01f(&s->rng);
+                float y = (float)j + mt_uniform01f(&s->rng);
+                float vx = 0.f, vy = 0.f;
+                if (e->transfer) velocity_at(s, s->u, s->v, x, y, &vx, &vy);
+                long pb = bin_of_pos(s, x, y);
+                if (pb < 0) continue;
+                size_t idx = bin_push(&s->bins[pb], x, y, vx, vy, 0.f, 0);
+                if (idx < cellbin->n) cellbin->visc[idx] = e->visc;
+            }
+        }
+}
+
+/* ------------------------------------------------------------------------ */
+/* NB-FLIP (nbflipsolver.cpp)                                               */
 /* ------------------------------------------------------------------------ */
 #define NB_NARROW_BAND (-3.f)      /* m_narrowBand,      nbflipsolver.cpp:20 */
 #define NB_COMBINATION_BAND (-2.f) /* m_combinationBand, :21 */
@@ -1612,11 +1705,12 @@ static void nb_prune_band(fso_solver *s)
             float x = bin->pos[2 * k], y = bin->pos[2 * k + 1];
             long i = (long)x, j = (long)y; /* ssize_t i = position.x() */
             float sdf = grid_lerp(s->fluid_sdf, s->ni, s->nj, 0.f, 0.f, x, y);
-            if (sdf < NB_NARROW_BAND) {
+            const int src = is_source(s, i, j);
+            if (!src && sdf < NB_NARROW_BAND) {
                 bin->dead[k] = 1;
                 continue;
             }
-            if (sdf < NB_RESAMPLING_BAND && s->counts[i * s->nj + j] > cap) bin->dead[k] = 1;
+            if ((src || sdf < NB_RESAMPLING_BAND) && s->counts[i * s->nj + j] > cap) bin->dead[k] = 1;
         }
     }
 }
@@ -1652,10 +1746,29 @@ static void nb_advect(fso_solver *s)
 static void nb_after_transfer(fso_solver *s)
 {
     const long ni = s->ni, nj = s->nj;
-    for (size_t k = 0; k < s->ncell; k++) {
-        float sdf = s->fluid_sdf[k];
-        s->fluid_sdf[k] = sdf < FLT_MAX ? sdf : FLT_MAX;
-    }
+    sources_after_transfer(s);
+    /* updateGridFromSources (:332-364): the nearest source's distance at the
+     * cell corner (i dx, j dx) */
+    const float dxf = (float)s->dx;
+    for (long i = 0; i < ni; i++)
+        for (long j = 0; j < nj; j++) {
+            float dist = FLT_MAX;
+            int id = -1;
+            for (int k = 0; k < s->nsources; k++) {
+                float sdf = polygon_sdf(&s->sources[k].g, (float)i * dxf, (float)j * dxf) / dxf;
+                if (sdf < dist) {
+                    dist = sdf;
+                    id = k;
+                }
+            }
+            const long l = i * nj + j;
+            const float f = s->fluid_sdf[l];
+            s->fluid_sdf[l] = f < dist ? f : dist; /* std::min(dist, sdf) */
+            if (dist < 0 && id != -1) {
+                s->visc_grid[l] = s->sources[id].visc;
+                s->adv_visc[l] = s->sources[id].visc;
+            }
+        }
     /* combineLevelset: std::min(advected + h, sdf), h = 1 */
     for (size_t k = 0; k < s->ncell; k++) {
         float a = s->adv_sdf[k] + 1.f, b = s->fluid_sdf[k];
@@ -1701,19 +1814,24 @@ static void nb_reseed(fso_solver *s)
         for (long j = 0; j < s->nj; j++) {
             long l = i * s->nj + j;
             float sc = s->fluid_sdf[l];
-            if (!(sc < NB_RESAMPLING_BAND && sc > NB_NARROW_BAND)) continue;
+            const int src = is_source(s, i, j);
+            if (!(src || (sc < NB_RESAMPLING_BAND && sc > NB_NARROW_BAND))) continue;
             int additional = ppc - s->counts[l];
             if (additional <= 0) continue;
+            const int eid = s->emitter_id[l];
             pbin *cellbin = &s->bins[bin_of_cell(s, i, j)];
             for (int q = 0; q < additional; q++) {
                 float x = (float)i + mt_uniform01f(&s->rng);
                 float y = (float)j + mt_uniform01f(&s->rng);
                 float nsdf = grid_lerp(s->fluid_sdf, s->ni, s->nj, 0.f, 0.f, x, y);
-                if (nsdf < NB_NARROW_BAND) continue;
-                float visc = grid_lerp(s->visc_grid, s->ni, s->nj, 0.5f, 0.5f, x, y);
+                if ((src && sc > NB_RESAMPLING_BAND) || nsdf < NB_NARROW_BAND) continue;
+                float vx = 0.f, vy = 0.f;
+                if (eid != -1 && s->sources[eid].transfer) velocity_at(s, s->u, s->v, x, y, &vx, &vy);
+                float visc = eid != -1 ? s->sources[eid].visc
+                                       : grid_lerp(s->visc_grid, s->ni, s->nj, 0.5f, 0.5f, x, y);
                 long pb = bin_of_pos(s, x, y);
                 if (pb < 0) continue;
-                size_t idx = bin_push(&s->bins[pb], x, y, 0.f, 0.f, 0.f, 0);
+                size_t idx = bin_push(&s->bins[pb], x, y, vx, vy, 0.f, 0);
                 if (idx < cellbin->n) cellbin->visc[idx] = visc;
             }
         }
@@ -1727,6 +1845,7 @@ static void nb_reseed(fso_solver *s)
 static void nb_first_frame_init(fso_solver *s)
 {
     update_sinks(s);
+    update_sources(s);
     update_solids(s);
     float dx = (float)s->dx;
     for (long i = 0; i < s->ni; i++)
@@ -1785,8 +1904,9 @@ static int run_stage(fso_solver *s, int stage)
     case FSO_P2G: particle_to_grid(s); break;
     case FSO_SDF: update_sdf(s); break;
     case FSO_MATERIALS: update_materials(s); break;
-    case FSO_AFTER_TRANSFER: /* sources only, plus NB-FLIP's grid combination */
+    case FSO_AFTER_TRANSFER: /* sources, plus NB-FLIP's grid combination */
         if (s->nb) nb_after_transfer(s);
+        else sources_after_transfer(s);
         break;
     case FSO_LEVELSET: bfs_extrapolate(s->fluid_sdf, NULL, s->ni, s->nj, 0, 0); break;
     case FSO_VEL_EXTRAP: extrapolate_velocity(s); break;
@@ -1801,8 +1921,9 @@ static int run_stage(fso_solver *s, int stage)
     case FSO_FRICTION: friction(s); break;
     case FSO_G2P: g2p(s); break;
     case FSO_COUNT: count_particles(s); break;
-    case FSO_RESEED: /* sources only, or NB-FLIP's band reseeding */
+    case FSO_RESEED: /* sources, or NB-FLIP's band reseeding */
         if (s->nb) nb_reseed(s);
+        else flip_reseed(s);
         break;
     case FSO_DENSITY_GRID: update_density_grid(s); break;
     case FSO_LEVELSET_OUTSIDE: bfs_extrapolate(s->fluid_sdf, NULL, s->ni, s->nj, 2, 0); break;

@@ -150,6 +150,10 @@ int fso_set_rng(fso_solver *s, const uint32_t state[625]);
 int fso_add_geometry(fso_solver *s, float friction, const float *xy, int n);
 int fso_add_initial_fluid(fso_solver *s, float viscosity, const float *xy, int n);
 int fso_add_sink(fso_solver *s, float divergence, const float *xy, int n);
+/* FlipSolver::addSource (flipsolver2d.cpp:607-610) with an Emitter
+ * (emitter.h) of these parameters; velocity in scene units per second. */
+int fso_add_source(fso_solver *s, const float *xy, int n, float viscosity, float divergence,
+                   float vx, float vy, int velocity_transfer);
 
 void fso_first_frame_init(fso_solver *s);
 void fso_step_frame(fso_solver *s);

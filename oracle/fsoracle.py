@@ -70,6 +70,7 @@ def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
         "fso_add_geometry": (c_int, [vp, c_float, vp, c_int]),
         "fso_add_initial_fluid": (c_int, [vp, c_float, vp, c_int]),
         "fso_add_sink": (c_int, [vp, c_float, vp, c_int]),
+        "fso_add_source": (c_int, [vp, vp, c_int, c_float, c_float, c_float, c_float, c_int]),
         "fso_first_frame_init": (None, [vp]), "fso_step_frame": (None, [vp]),
         "fso_set_step_dt": (None, [vp, c_float]), "fso_step_dt": (c_float, [vp]),
         "fso_step": (None, [vp]), "fso_run_stage": (c_int, [vp, c_int]),
@@ -135,6 +136,10 @@ class OracleSolver:
                 self.lib.fso_add_initial_fluid(self.h, o.viscosity, _ptr(v), len(v))
             elif o.kind == "sink":
                 self.lib.fso_add_sink(self.h, o.divergence, _ptr(v), len(v))
+            elif o.kind == "source":
+                self.lib.fso_add_source(self.h, _ptr(v), len(v), o.viscosity, o.divergence,
+                                        float(o.velocity[0]), float(o.velocity[1]),
+                                        int(o.transfer_velocity))
             else:
                 raise ValueError(o.kind)
 

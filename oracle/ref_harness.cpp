@@ -45,6 +45,7 @@ struct RefApi {
     virtual void addGeom(Obstacle &o) = 0;
     virtual void addFluid(Emitter &e) = 0;
     virtual void addSinkObj(Sink &k) = 0;
+    virtual void addSrc(Emitter &e) = 0;
 };
 
 // Base: FlipSolver or NBFlipSolver.  The stages reach the protected methods
@@ -141,6 +142,7 @@ public:
     void addGeom(Obstacle &o) override { this->addGeometry(o); }
     void addFluid(Emitter &e) override { this->addInitialFluid(e); }
     void addSinkObj(Sink &k) override { this->addSink(k); }
+    void addSrc(Emitter &e) override { this->addSource(e); }
 
     // libstdc++ writes the 624 state words, then the position of the next one
     int getRng(uint32_t *state) override
@@ -451,6 +453,24 @@ int fso_add_initial_fluid(fso_solver *s, float viscosity, const float *xy, int n
     e.setVelocity(Vec3());
     e.setVelocityTransfer(false);
     S(s)->addFluid(e);
+    return 0;
+}
+
+int fso_add_source(fso_solver *s, const float *xy, int n, float viscosity, float divergence,
+                   float vx, float vy, int velocity_transfer)
+{
+    // JsonSceneReader::emitterFromJson (jsonscenereader.cpp:200-225) with its
+    // defaults for the parameters the liquid solvers do not read
+    Geometry2d g = polygon(xy, n);
+    Emitter e(g);
+    e.setTemperature(273.f);
+    e.setConcentrartion(1.f);
+    e.setViscosity(viscosity);
+    e.setFuel(1.f);
+    e.setDivergence(divergence);
+    e.setVelocity(Vec3(vx, vy));
+    e.setVelocityTransfer(velocity_transfer != 0);
+    S(s)->addSrc(e);
     return 0;
 }
 

@@ -28,6 +28,11 @@ PIN_SCENES = {
     "json_dam36": lambda: scenes.scene_from_json(DAM_JSON, "json_dam36"),
     "nb_dam48_obstacle": lambda: scenes.nb_dam_break(48, seed=7, obstacle=True),
     "nb_dam37_inviscid": lambda: scenes.nb_dam_break(37, seed=5, viscosity=0.0),
+    # sources: FLIP reseeding and grid transfer, NB-FLIP's source branches
+    "dam40_source": lambda: scenes.with_source(scenes.dam_break(40, seed=9), viscosity=3.0),
+    "nb_dam44_source": lambda: scenes.with_source(scenes.nb_dam_break(44, seed=6), transfer=False,
+                                                  box=(0.2, 0.35, 0.5, 0.7), viscosity=2.0),
+    "nb_dam44_source_transfer": lambda: scenes.with_source(scenes.nb_dam_break(44, seed=6)),
 }
 
 

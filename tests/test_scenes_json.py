@@ -78,12 +78,16 @@ def test_nbflip_selects_the_narrow_band_solver():
     assert scenes.scene_from_json(DAM_JSON).sim_type == scenes.SIM_FLIP
 
 
-def test_sources_are_refused():
+def test_sources_follow_emitter_from_json():
     doc = {"settings": {"simType": "flip", "domainSizeI": 1, "domainSizeJ": 1, "resolution": 16,
                         "fps": 30, "particlesPerCell": 4},
-           "solver": {"objects": [{"type": "source", "verts": [[0, 0], [0, 1], [1, 1]]}]}}
-    with pytest.raises(scenes.UnsupportedScene, match="source"):
-        scenes.scene_from_json(doc)
+           "solver": {"objects": [{"type": "source", "verts": [[0, 0], [0, 1], [1, 1]],
+                                   "velocity": [-7, 2], "viscosity": 4, "transferVelocity": True},
+                                  {"type": "source", "verts": [[0, 0], [0, 1], [1, 1]]}]}}
+    a, b = scenes.scene_from_json(doc).objects
+    assert a.kind == b.kind == "source"
+    assert a.velocity == (-7.0, 2.0) and a.viscosity == 4.0 and a.transfer_velocity
+    assert b.velocity == (0.0, 0.0) and b.viscosity == 0.0 and not b.transfer_velocity
 
 
 import build as oracle_build  # noqa: E402  (oracle/ is on sys.path via conftest)
@@ -111,17 +115,22 @@ def test_reference_scene_files_parse_or_are_refused():
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_SCENES), reason="reference scene files not present")
-def test_reference_nbflip_scene_runs_the_same_on_both_oracles(port_lib, ref_lib):
-    """The reference's NB-FLIP dam break file, at a reduced resolution, on the
-    reference build and on the C restatement: identical particles, grids and
-    engine state frame by frame."""
+def test_reference_scene_files_run_the_same_on_both_oracles(port_lib, ref_lib):
+    """The reference's NB-FLIP dam break and its scenes with sources (NB-FLIP
+    glass pour and waterfall, the FLIP test scene), at a reduced resolution,
+    on the reference build and on the C restatement: identical particles,
+    grids and engine state frame by frame."""
     import fsoracle as fo
 
-    sc = scenes.scene_from_json(os.path.join(REF_SCENES, "dam_break.json"))
-    assert sc.sim_type == scenes.SIM_NBFLIP
-    sc.params.resolution = 64
+    for fn in ("dam_break.json", "glass_pour.json", "waterfall.json", "test_scene.json"):
+        sc = scenes.scene_from_json(os.path.join(REF_SCENES, fn))
+        sc.params.resolution = 64
+        _same_on_both(fo, sc)
+
+
+def _same_on_both(fo, sc, frames=6):
     r, p = fo.OracleSolver(sc, "ref"), fo.OracleSolver(sc, "port")
-    for _ in range(6):
+    for _ in range(frames):
         r.step_frame()
         p.step_frame()
         pr, pp = r.get_particles(), p.get_particles()
