@@ -201,6 +201,10 @@ struct fs_solver {
     bool friction_dirty = true;
     std::mt19937 rng; // m_randEngine (flipsolver2d.cpp:71), persists across calls
     bool nb = false;  // NBFlipSolver (nbflipsolver.cpp); its engine state lives in R.rng
+    std::vector<SourceParams> src_params; // addSource order
+    Sources S;               // device copy from first-frame init on
+    bool grows = false;      // particles are added every substep (NB-FLIP or sources)
+    bool rng_dev = false;    // the engine state is R.rng (else the host's rng)
     NbGrids N;
     NbReseed R;
     int nb_max_cand = 0;     // particlesPerCell candidates per cell at most
@@ -302,7 +306,7 @@ static fs_status upload_particles(fs_solver *s, const std::vector<int> &counts,
     const int total = (int)pos.size();
     if (total > s->P.cap || s->P.pos == nullptr) {
         // NB-FLIP keeps room for 2 particlesPerCell per cell (reseeding)
-        const long long keep = s->nb ? 2LL * s->p.particlesPerCell * (long long)s->ncell : 0;
+        const long long keep = s->grows ? 2LL * s->p.particlesPerCell * (long long)s->ncell : 0;
         TRY(alloc_particles(s, (int)std::max<long long>(total, keep)));
     }
     std::vector<int> start(nb + 1, 0), slot_bin(total);
@@ -320,7 +324,7 @@ static fs_status upload_particles(fs_solver *s, const std::vector<int> &counts,
     }
     CK(cudaStreamSynchronize(s->st));
     s->after_advect = false;
-    if (s->nb) P.bound = std::max(total, 1);
+    if (s->grows) P.bound = std::max(total, 1);
     return FS_OK;
 }
 
@@ -629,6 +633,7 @@ static fs_status create_impl(const fs_params *p, const fs_exec_params *exec, boo
         A(dalloc(s, &R.cand_off, n + 1));
         A(dalloc(s, &R.draws, 2 * mc));
         A(dalloc(s, &R.cand_pos, mc));
+        A(dalloc(s, &R.cand_vel, mc));
         A(dalloc(s, &R.cand_visc, mc));
         A(dalloc(s, &R.cand_bin, mc));
         A(dalloc(s, &R.cand_cb, mc));
@@ -647,6 +652,8 @@ static fs_status create_impl(const fs_params *p, const fs_exec_params *exec, boo
         ok = ok && cudaMemcpyAsync(R.rng, st0, sizeof(st0), cudaMemcpyHostToDevice, q) == cudaSuccess;
         ok = ok && cudaStreamSynchronize(q) == cudaSuccess;
         if (!ok) return cleanup(fail(FS_ERR_CUDA, "fs_create_nbflip: initialisation failed"));
+        s->grows = true;
+        s->rng_dev = true;
     } else {
         A(alloc_particles(s, 0));
     }
@@ -669,7 +676,7 @@ extern "C" fs_status fs_get_rng_state(fs_solver *s, uint32_t *state)
 {
     if (!s || !state) return fail(FS_ERR_BAD_ARG, "null argument");
     TRY(set_device(s));
-    if (s->nb) {
+    if (s->rng_dev) {
         TRY(sync_all(s));
         CK(cudaMemcpy(state, s->R.rng, 625 * sizeof(uint32_t), cudaMemcpyDeviceToHost));
         return FS_OK;
@@ -691,7 +698,7 @@ extern "C" fs_status fs_set_rng_state(fs_solver *s, const uint32_t *state)
     if (!s || !state) return fail(FS_ERR_BAD_ARG, "null argument");
     if (state[624] > 624) return fail(FS_ERR_BAD_ARG, "fs_set_rng_state: index above 624");
     TRY(set_device(s));
-    if (s->nb) {
+    if (s->rng_dev) {
         TRY(sync_all(s));
         CK(cudaMemcpy(s->R.rng, state, 625 * sizeof(uint32_t), cudaMemcpyHostToDevice));
         return FS_OK;
@@ -748,6 +755,21 @@ extern "C" fs_status fs_add_sink(fs_solver *s, float divergence, const float *xy
     return add_poly(s, 2, divergence, xy, n);
 }
 
+extern "C" fs_status fs_add_source(fs_solver *s, const float *xy, int n, float viscosity,
+                                   float divergence, float vx, float vy, int velocity_transfer)
+{
+    if (s && s->initialized) return fail(FS_ERR_STATE, "fs_add_source: the scene is initialised");
+    TRY(add_poly(s, 3, divergence, xy, n));
+    SourceParams e{};
+    e.visc = viscosity;
+    e.div = divergence;
+    e.vx = vx;
+    e.vy = vy;
+    e.transfer = velocity_transfer != 0;
+    s->src_params.push_back(e);
+    return FS_OK;
+}
+
 static fs_status download_bins(fs_solver *s, std::vector<int> &start, std::vector<int> &count);
 
 // ---- host restatement of the sampler used for seeding (grid2d.h:187-216) --
@@ -775,6 +797,83 @@ static float h_grid_lerp(const std::vector<float> &g, int si, int sj, float ox, 
     float v1 = h_lerp(h_get(g, si, sj, ci, cj), h_get(g, si, sj, c3i, cj), il);
     float v2 = h_lerp(h_get(g, si, sj, ci, c2j), h_get(g, si, sj, c3i, c2j), il);
     return h_lerp(v1, v2, jl);
+}
+
+// the source table and polygons on the device for the substeps (frame-0
+// setup copies every polygon only for the classification)
+static fs_status upload_sources(fs_solver *s)
+{
+    if (s->src_params.empty() || s->S.n) return FS_OK;
+    std::vector<float> xy;
+    std::vector<int> off(1, 0);
+    for (const Poly &g : s->polys)
+        if (g.kind == 3) {
+            xy.insert(xy.end(), g.xy.begin(), g.xy.end());
+            off.push_back(off.back() + (int)(g.xy.size() / 2));
+        }
+    SourceParams *p = nullptr;
+    float *dxy = nullptr;
+    int *doff = nullptr;
+    TRY(dalloc(s, &p, s->src_params.size()));
+    TRY(dalloc(s, &dxy, xy.size()));
+    TRY(dalloc(s, &doff, off.size()));
+    CK(cudaMemcpy(p, s->src_params.data(), s->src_params.size() * sizeof(SourceParams),
+                  cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dxy, xy.data(), xy.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(doff, off.data(), off.size() * 4, cudaMemcpyHostToDevice));
+    s->S.p = p;
+    s->S.xy = dxy;
+    s->S.off = doff;
+    s->S.n = (int)s->src_params.size();
+    return FS_OK;
+}
+
+// FLIP with sources reseeds every substep (reseedParticles): the same
+// candidate scratch as NB-FLIP, sized for particlesPerCell / 2 per cell
+static fs_status alloc_flip_reseed(fs_solver *s)
+{
+    if (s->R.rng) return FS_OK;
+    const size_t n = s->ncell;
+    const int per = std::max(1, s->p.particlesPerCell / 2);
+    s->nb_max_cand = (int)std::min<long long>((long long)per * (long long)n, INT_MAX / 2);
+    const size_t mc = (size_t)s->nb_max_cand;
+    NbReseed &R = s->R;
+    R.ncell = (int)n;
+    TRY(dalloc(s, &R.rng, 625));
+    TRY(dalloc(s, &R.cand_n, n));
+    TRY(dalloc(s, &R.cand_off, n + 1));
+    TRY(dalloc(s, &R.draws, 2 * mc));
+    TRY(dalloc(s, &R.cand_pos, mc));
+    TRY(dalloc(s, &R.cand_vel, mc));
+    TRY(dalloc(s, &R.cand_visc, mc));
+    TRY(dalloc(s, &R.cand_bin, mc));
+    TRY(dalloc(s, &R.cand_cb, mc));
+    TRY(dalloc(s, &R.pos_of, mc));
+    TRY(dalloc(s, &R.cross, (size_t)kNbCrossMax));
+    TRY(dalloc(s, &R.cross_n, 1));
+    R.status = &s->sc->nb_overflow;
+    char *scan = nullptr;
+    TRY(dalloc(s, &scan, scan_scratch_bytes((int)n)));
+    s->nb_scan = scan;
+    return FS_OK;
+}
+
+// the host engine state (std::mt19937, after the frame-0 seeding) to the
+// device, where the substeps' reseeding draws from it
+static fs_status rng_to_device(fs_solver *s)
+{
+    std::ostringstream os;
+    os << s->rng; // libstdc++: the 624 state words, then the index of the next
+    std::istringstream is(os.str());
+    uint32_t st[625];
+    for (int k = 0; k < 625; k++) {
+        unsigned long v = 0;
+        if (!(is >> v)) return fail(FS_ERR_CUDA, "unexpected engine format");
+        st[k] = (uint32_t)v;
+    }
+    CK(cudaMemcpy(s->R.rng, st, sizeof(st), cudaMemcpyHostToDevice));
+    s->rng_dev = true;
+    return FS_OK;
 }
 
 extern "C" fs_status fs_first_frame_init(fs_solver *s)
@@ -812,6 +911,11 @@ extern "C" fs_status fs_first_frame_init(fs_solver *s)
     CK(cudaGetLastError());
     s->friction_dirty = true;
     TRY(ensure_friction(s));
+    TRY(upload_sources(s));
+    if (s->S.n && !s->nb) {
+        s->grows = true; // the seeding upload below keeps room for the sources' particles
+        TRY(alloc_flip_reseed(s));
+    }
     if (s->nb) {
         // NBFlipSolver::initialFluidSeed (nbflipsolver.cpp:255-297) adds no
         // particle but draws two numbers for each of particlesPerCell
@@ -902,6 +1006,7 @@ extern "C" fs_status fs_first_frame_init(fs_solver *s)
         pv.insert(pv.end(), bvisc[b].begin(), bvisc[b].end());
     }
     TRY(upload_particles(s, counts, pos, vel, pv));
+    if (s->S.n) TRY(rng_to_device(s));
     dfree(s, dxy);
     dfree(s, doff);
     dfree(s, dkind);
@@ -1067,15 +1172,18 @@ static fs_status stage(fs_solver *s, int which, bool in_step)
             g_kernel_launches += 1;
         }
         break;
-    case FS_STAGE_AFTER_TRANSFER: // sources only, plus NB-FLIP's combination
+    case FS_STAGE_AFTER_TRANSFER: // sources, plus NB-FLIP's combination
         if (s->nb) {
-            launch_nb_combine(d, s->G, s->N, q);
-            g_kernel_launches += 2;
+            launch_nb_combine(d, s->G, s->N, s->S, s->p.dx, q);
+            g_kernel_launches += 3 + (s->S.n ? 1 : 0);
+        } else if (s->S.n) {
+            launch_sources_after_transfer(d, s->G, s->S, s->p.dx, q);
+            g_kernel_launches += 1;
         }
         break;
-    case FS_STAGE_RESEED: // sources only, or NB-FLIP's band reseeding
-        if (s->nb) {
-            launch_nb_candidates(d, s->sp, s->G, s->R, s->nb_scan, q);
+    case FS_STAGE_RESEED: // sources, or NB-FLIP's band reseeding
+        if (s->nb || (s->S.n && s->R.rng)) {
+            launch_nb_candidates(d, s->sp, s->G, s->R, s->S, s->nb, s->nb_scan, q);
             // the candidate total sizes the append's launches (one small read)
             int ncand = 0;
             CK(cudaMemcpyAsync(&ncand, s->R.cand_off + s->ncell, sizeof(int), cudaMemcpyDeviceToHost, q));
@@ -1163,6 +1271,7 @@ template <class Mark> static fs_status step_flip(fs_solver *s, bool timed, Mark 
     TRY(mark());
     TRY(stage(s, FS_STAGE_P2G, true)); // + updateSdf + updateMaterials
     TRY(mark());
+    if (s->S.n) TRY(stage(s, FS_STAGE_AFTER_TRANSFER, true)); // sources (:435)
     TRY(stage(s, FS_STAGE_LEVELSET, true));
     // extrapolate(10), saved copy and body forces in one pass (:437-440)
     launch_vel_extrapolate(s->d, s->G, s->sp, s->sc, true, s->st);
@@ -1175,6 +1284,7 @@ template <class Mark> static fs_status step_flip(fs_solver *s, bool timed, Mark 
     TRY(stage(s, FS_STAGE_G2P, true));
     TRY(mark());
     TRY(stage(s, FS_STAGE_COUNT, true));
+    if (s->S.n) TRY(stage(s, FS_STAGE_RESEED, true)); // sources (:460)
     return FS_OK;
 }
 
@@ -1226,6 +1336,7 @@ static fs_status step_impl(fs_solver *s)
             if (g < 8) TRY(mark());
         }
     } else {
+        if (s->grows) TRY(nb_refresh_bound(s));
         TRY(step_flip(s, timed, mark));
     }
     if (s->timers) {
@@ -1358,7 +1469,7 @@ extern "C" fs_status fs_run_stage(fs_solver *s, int which)
     // its own comes after it (two level sets on one set of buffers race)
     TRY(wait_side(s));
     k_set_dt<<<1, 1, 0, s->st>>>(s->sc, s->step_dt);
-    if (s->nb && !s->after_advect) TRY(nb_refresh_bound(s));
+    if (s->grows && !s->after_advect) TRY(nb_refresh_bound(s));
     if (which == FS_STAGE_DENSITY) CK(cudaMemsetAsync(&s->sc->density_iters, 0, sizeof(int), s->st));
     if (which == FS_STAGE_PROJECT) CK(cudaMemsetAsync(&s->sc->pressure_iters, 0, sizeof(int), s->st));
     TRY(stage(s, which, false));
@@ -1495,7 +1606,7 @@ extern "C" fs_status fs_set_particles(fs_solver *s, const int32_t *bin_counts, c
     const int nb = s->P.nbins;
     if ((int)total > s->P.cap || s->P.pos == nullptr) {
         // NB-FLIP keeps room for 2 particlesPerCell per cell (reseeding)
-        const long long keep = s->nb ? 2LL * s->p.particlesPerCell * (long long)s->ncell : 0;
+        const long long keep = s->grows ? 2LL * s->p.particlesPerCell * (long long)s->ncell : 0;
         TRY(alloc_particles(s, (int)std::max<long long>((long long)total, keep)));
     }
     std::vector<int> start(nb + 1, 0);
@@ -1514,7 +1625,7 @@ extern "C" fs_status fs_set_particles(fs_solver *s, const int32_t *bin_counts, c
     CK(cudaGetLastError());
     s->after_advect = false;
     s->initialized = true;
-    if (s->nb) P.bound = std::max((int)total, 1);
+    if (s->grows) P.bound = std::max((int)total, 1);
     return FS_OK;
 }
 
@@ -1912,6 +2023,8 @@ extern "C" fs_status fs_batch_add(fs_batch *b, fs_solver *s)
     if (batch_find(b, s)) return fail(FS_ERR_BAD_ARG, "fs_batch_add: the handle is already a member");
     if (b->free_slots.empty()) return fail(FS_ERR_BAD_ARG, "fs_batch_add: the batch is full (%d)", fs_batch::kSlots);
     if (s->nb) return fail(FS_ERR_UNSUPPORTED, "fs_batch_add: NB-FLIP scenes step on their own");
+    if (!s->src_params.empty())
+        return fail(FS_ERR_UNSUPPORTED, "fs_batch_add: scenes with sources step on their own");
     CK(cudaSetDevice(b->device));
     BatchScene bs;
     bs.s = s;

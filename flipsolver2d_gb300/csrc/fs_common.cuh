@@ -118,6 +118,29 @@ __device__ __forceinline__ float2 velocity_at(const float *__restrict__ u, const
                        grid_lerp(v, d.ni, d.nj + 1, 0.f, 0.5f, x, y));
 }
 
+// Geometry2d::signedDistance (geometry2d.cpp:54-73)
+__device__ __forceinline__ float polygon_sdf(const float *__restrict__ xy, int n, float px, float py)
+{
+    float dx0 = px - xy[0], dy0 = py - xy[1];
+    float sq = dx0 * dx0 + dy0 * dy0 + 0.f * 0.f;
+    float sgn = 1.0f;
+    for (int i = 0, j = n - 1; i < n; j = i, i++) {
+        float ex = xy[2 * j] - xy[2 * i], ey = xy[2 * j + 1] - xy[2 * i + 1];
+        float wx = px - xy[2 * i], wy = py - xy[2 * i + 1];
+        float wde = wx * ex + wy * ey + 0.f * 0.f;
+        float ede = ex * ex + ey * ey + 0.f * 0.f;
+        float h = clampf(wde / ede, 0.0f, 1.0f);
+        float bx = wx - ex * h, by = wy - ey * h;
+        float bb = bx * bx + by * by + 0.f * 0.f;
+        sq = (bb < sq) ? bb : sq;
+        bool xf = py >= xy[2 * i + 1];
+        bool yf = py < xy[2 * j + 1];
+        bool zf = ex * wy > ey * wx;
+        if ((xf && yf && zf) || (!xf && !yf && !zf)) sgn = -sgn;
+    }
+    return (float)((double)sgn * sqrt((double)sq));
+}
+
 // MarkerParticleSystem::gridToBinIdx (markerparticlesystem.cpp:97-102, 156-159)
 __device__ __forceinline__ int bin_of_cell(const GridDims &d, long long i, long long j)
 {

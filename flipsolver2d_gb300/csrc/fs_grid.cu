@@ -27,31 +27,8 @@ static inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
 // ---------------------------------------------------------------------------
 // scene classification (flipsolver2d.cpp:502-590), frame 0 only
 // ---------------------------------------------------------------------------
-// Geometry2d::signedDistance (geometry2d.cpp:54-73)
-__device__ float polygon_sdf(const float *__restrict__ xy, int n, float px, float py)
-{
-    float dx0 = px - xy[0], dy0 = py - xy[1];
-    float sq = dx0 * dx0 + dy0 * dy0 + 0.f * 0.f;
-    float sgn = 1.0f;
-    for (int i = 0, j = n - 1; i < n; j = i, i++) {
-        float ex = xy[2 * j] - xy[2 * i], ey = xy[2 * j + 1] - xy[2 * i + 1];
-        float wx = px - xy[2 * i], wy = py - xy[2 * i + 1];
-        float wde = wx * ex + wy * ey + 0.f * 0.f;
-        float ede = ex * ex + ey * ey + 0.f * 0.f;
-        float h = clampf(wde / ede, 0.0f, 1.0f);
-        float bx = wx - ex * h, by = wy - ey * h;
-        float bb = bx * bx + by * by + 0.f * 0.f;
-        sq = (bb < sq) ? bb : sq;
-        bool xf = py >= xy[2 * i + 1];
-        bool yf = py < xy[2 * j + 1];
-        bool zf = ex * wy > ey * wx;
-        if ((xf && yf && zf) || (!xf && !yf && !zf)) sgn = -sgn;
-    }
-    return (float)((double)sgn * sqrt((double)sq));
-}
-
 // kind: 0 solid (value = friction), 1 initial fluid (value = viscosity),
-// 2 sink (value = divergence)
+// 2 sink (value = divergence), 3 source (value = divergence)
 __global__ void k_scene_classify(GridDims d, Grids G, float dx, const float *__restrict__ xy,
                                  const int *__restrict__ off, const int *__restrict__ kind,
                                  const float *__restrict__ val, int npoly, int nb)
@@ -67,6 +44,22 @@ __global__ void k_scene_classify(GridDims d, Grids G, float dx, const float *__r
                         ((float)j + 0.5f) * dx) <= 0.f) {
             m = M_SINK;
             G.divc[c] = val[k];
+        }
+    }
+    // updateSources (:532-552): the last source containing the cell centre
+    // (i dx + dx / 2, in float) makes it a source
+    {
+        const float hdx = (float)((double)dx / 2.0);
+        int src = 0;
+        for (int k = 0; k < npoly; k++) {
+            if (kind[k] != 3) continue;
+            if (polygon_sdf(xy + 2 * off[k], off[k + 1] - off[k], (float)i * dx + hdx,
+                            (float)j * dx + hdx) <= 0.f) {
+                m = M_SOURCE;
+                G.emitter_id[c] = src;
+                G.divc[c] = val[k];
+            }
+            src++;
         }
     }
     // updateSolids (:502-530); (float(i)+0.5)*dx is evaluated in double

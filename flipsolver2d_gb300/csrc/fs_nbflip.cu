@@ -7,9 +7,10 @@
 // Built with -fmad=false like the other FLIP kernels: every float expression
 // rounds as the reference's CPU build does.
 //
-// Scenes on this path have no sources: no cell is a source and every emitter
-// id is -1, which removes the source branches of pruneNarrowBand,
-// updateGridFromSources and reseedParticles.
+// Sources (emitters) enter through the material (SOURCE cells), the
+// emitter id grid and the source table: FlipSolver::afterTransfer, NB-FLIP's
+// pruneNarrowBand, updateGridFromSources and reseedParticles, and FLIP's
+// reseedParticles read them.
 #include <cfloat>
 #include <cstdint>
 
@@ -140,14 +141,17 @@ void launch_mt_draws(uint32_t *state, float *out, const int *count, int per, cud
 // only particles that stay in their bin are tested.
 // ---------------------------------------------------------------------------
 __global__ void k_nb_prune_band(GridDims d, Particles P, const float *__restrict__ sdf,
-                                const int *__restrict__ counts, int cap2)
+                                const int *__restrict__ counts, const int8_t *__restrict__ material,
+                                int cap2)
 {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= P.bin_start[P.nbins] || P.flag[s] != P_STAY) return;
     const float2 p = P.pos[s];
     const long long i = (long long)p.x, j = (long long)p.y; // ssize_t i = position.x()
     const float v = grid_lerp(sdf, d.ni, d.nj, 0.f, 0.f, p.x, p.y);
-    if (v < kNarrowBand || (v < kResamplingBand && counts[i * d.nj + j] > cap2)) P.flag[s] = P_KILL;
+    const bool src = material[i * d.nj + j] == M_SOURCE;
+    if ((!src && v < kNarrowBand) || ((src || v < kResamplingBand) && counts[i * d.nj + j] > cap2))
+        P.flag[s] = P_KILL;
 }
 
 // FlipSolver::rk4Integrate (flipsolver2d.cpp:1195-1203) through the velocity grid
@@ -199,7 +203,7 @@ void launch_nb_advect_extra(const GridDims &d, const SceneParams &sp, const Part
 {
     if (P.cap > 0)
         k_nb_prune_band<<<nblk(P.bound, kThreads), kThreads, 0, st>>>(d, P, G.fluid_sdf, G.counts,
-                                                                    2 * sp.particlesPerCell);
+                                                                    G.material, 2 * sp.particlesPerCell);
     const long long n = (long long)(d.ni + 1) * (d.nj + 1);
     k_nb_euler<<<nblk(n, kThreads), kThreads, 0, st>>>(d, G.u, G.v, G.fluid_sdf, G.visc, N.adv_u,
                                                        N.adv_v, N.adv_sdf, N.adv_visc, sc);
@@ -213,12 +217,55 @@ void launch_nb_advect_extra(const GridDims &d, const SceneParams &sp, const Part
 // sampled at the face or cell centre exceeds the combination band, else the
 // advected one.  std::min(a, b) is (b < a) ? b : a.
 // ---------------------------------------------------------------------------
+// FlipSolver::afterTransfer (flipsolver2d.cpp:390-410): source cells take the
+// emitter's viscosity and, when it transfers velocity, faces (i, j) of U and
+// V take its velocity / dx (float / double) and become valid
+__global__ void k_sources_after_transfer(GridDims d, Grids G, Sources S, double dx)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= (long long)d.ni * d.nj || G.material[c] != M_SOURCE) return;
+    const long long i = c / d.nj, j = c - i * d.nj;
+    const SourceParams e = S.p[G.emitter_id[c]];
+    G.visc[c] = e.visc;
+    if (e.transfer) {
+        G.u[i * d.nj + j] = (float)((double)e.vx / dx);
+        G.v[i * (d.nj + 1) + j] = (float)((double)e.vy / dx);
+        G.uvalid[i * d.nj + j] = 1;
+        G.vvalid[i * (d.nj + 1) + j] = 1;
+    }
+}
+
+// updateGridFromSources (:332-364): the nearest source's signed distance at
+// the cell corner (i dx, j dx) in cells; sdf = std::min(dist, sdf) (FLT_MAX
+// with no source); inside a source the viscosity grids take its viscosity
+__global__ void k_nb_sources_grid(GridDims d, Grids G, NbGrids N, Sources S, float dx)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= (long long)d.ni * d.nj) return;
+    const long long i = c / d.nj, j = c - i * d.nj;
+    float dist = FLT_MAX;
+    int id = -1;
+    for (int k = 0; k < S.n; k++) {
+        const float v = polygon_sdf(S.xy + 2 * S.off[k], S.off[k + 1] - S.off[k], (float)i * dx,
+                                    (float)j * dx) / dx;
+        if (v < dist) {
+            dist = v;
+            id = k;
+        }
+    }
+    const float f = G.fluid_sdf[c];
+    G.fluid_sdf[c] = f < dist ? f : dist;
+    if (dist < 0 && id != -1) {
+        G.visc[c] = S.p[id].visc;
+        N.adv_visc[c] = S.p[id].visc;
+    }
+}
+
 __global__ void k_nb_combine_sdf(long long n, float *__restrict__ sdf, const float *__restrict__ asdf)
 {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n) return;
-    float b = sdf[c];
-    b = b < FLT_MAX ? b : FLT_MAX;
+    const float b = sdf[c];
     const float a = asdf[c] + 1.f;
     sdf[c] = b < a ? b : a;
 }
@@ -259,9 +306,20 @@ __global__ void k_nb_materials(long long n, const float *__restrict__ sdf, int8_
     }
 }
 
-void launch_nb_combine(const GridDims &d, const Grids &G, const NbGrids &N, cudaStream_t st)
+void launch_sources_after_transfer(const GridDims &d, const Grids &G, const Sources &S, double dx,
+                                   cudaStream_t st)
+{
+    if (S.n == 0) return;
+    const long long nc = (long long)d.ni * d.nj;
+    k_sources_after_transfer<<<nblk(nc, kThreads), kThreads, 0, st>>>(d, G, S, dx);
+}
+
+void launch_nb_combine(const GridDims &d, const Grids &G, const NbGrids &N, const Sources &S,
+                       double dx, cudaStream_t st)
 {
     const long long nc = (long long)d.ni * d.nj;
+    launch_sources_after_transfer(d, G, S, dx, st);
+    k_nb_sources_grid<<<nblk(nc, kThreads), kThreads, 0, st>>>(d, G, N, S, (float)dx);
     k_nb_combine_sdf<<<nblk(nc, kThreads), kThreads, 0, st>>>(nc, G.fluid_sdf, N.adv_sdf);
     const long long n = (long long)(d.ni + 1) * d.nj + (long long)d.ni * (d.nj + 1) + nc;
     k_nb_combine_grids<<<nblk(n, kThreads), kThreads, 0, st>>>(d, G, N);
@@ -283,19 +341,37 @@ void launch_nb_materials(const GridDims &d, const Grids &G, cudaStream_t st)
 // interpolated there.  A position rounded out of the grid has no bin (the
 // reference indexes past its bin array) and is dropped.
 // ---------------------------------------------------------------------------
+// NB-FLIP: band and source cells top up to particlesPerCell; FLIP
+// (reseedParticles, flipsolver2d.cpp:627-680): source cells to
+// particlesPerCell / 2
 __global__ void k_nb_cand_count(long long n, const float *__restrict__ sdf,
-                                const int *__restrict__ counts, int ppc, int *__restrict__ cand_n)
+                                const int *__restrict__ counts, const int8_t *__restrict__ material,
+                                int ppc, int nb, int *__restrict__ cand_n)
 {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n) return;
-    const float s = sdf[c];
+    const bool src = material[c] == M_SOURCE;
     int add = 0;
-    if (s < kResamplingBand && s > kNarrowBand) add = ppc - counts[c];
+    if (nb) {
+        const float s = sdf[c];
+        if (src || (s < kResamplingBand && s > kNarrowBand)) add = ppc - counts[c];
+    } else if (src) {
+        add = ppc / 2 - counts[c];
+    }
     cand_n[c] = add > 0 ? add : 0;
 }
 
+// a candidate's position, test, velocity and viscosity:
+//  NB-FLIP  dropped when the cell is a source with sdf above the resampling
+//           band or the position's sdf is below the narrow band; velocity
+//           from the grid when the cell's emitter transfers velocity;
+//           the emitter's viscosity, else the grid's at the position
+//  FLIP     source cells only: always kept, velocity as above, the
+//           emitter's viscosity
 __global__ void k_nb_place(GridDims d, NbReseed R, const float *__restrict__ sdf,
-                           const float *__restrict__ visc)
+                           const float *__restrict__ visc, const int8_t *__restrict__ material,
+                           const int *__restrict__ emitter_id, const float *__restrict__ u,
+                           const float *__restrict__ v, Sources S, int nb)
 {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= (long long)d.ni * d.nj) return;
@@ -303,14 +379,23 @@ __global__ void k_nb_place(GridDims d, NbReseed R, const float *__restrict__ sdf
     if (k0 == k1) return;
     const long long i = c / d.nj, j = c - i * d.nj;
     const int cb = bin_of_cell(d, i, j);
+    const bool src = material[c] == M_SOURCE;
+    const float sc = sdf[c];
+    const int eid = emitter_id[c];
+    const bool has_e = eid != -1 && eid < S.n;
+    const bool transfer = has_e && S.p[eid].transfer;
     for (int k = k0; k < k1; k++) {
         const float x = (float)i + R.draws[2 * (size_t)k];
         const float y = (float)j + R.draws[2 * (size_t)k + 1];
-        const float ns = grid_lerp(sdf, d.ni, d.nj, 0.f, 0.f, x, y);
         const int pb = bin_of_pos(d, x, y);
-        const bool keep = !(ns < kNarrowBand) && pb >= 0;
+        bool keep = pb >= 0;
+        if (nb) {
+            const float ns = grid_lerp(sdf, d.ni, d.nj, 0.f, 0.f, x, y);
+            keep = keep && !((src && sc > kResamplingBand) || ns < kNarrowBand);
+        }
         R.cand_pos[k] = make_float2(x, y);
-        R.cand_visc[k] = grid_lerp(visc, d.ni, d.nj, 0.5f, 0.5f, x, y);
+        R.cand_vel[k] = transfer ? velocity_at(u, v, d, x, y) : make_float2(0.f, 0.f);
+        R.cand_visc[k] = has_e ? S.p[eid].visc : grid_lerp(visc, d.ni, d.nj, 0.5f, 0.5f, x, y);
         R.cand_bin[k] = keep ? pb : -1;
         R.cand_cb[k] = cb;
         if (keep && pb != cb) {
@@ -321,15 +406,17 @@ __global__ void k_nb_place(GridDims d, NbReseed R, const float *__restrict__ sdf
 }
 
 void launch_nb_candidates(const GridDims &d, const SceneParams &sp, const Grids &G,
-                          const NbReseed &R, void *scan_scratch, cudaStream_t st)
+                          const NbReseed &R, const Sources &S, bool nb, void *scan_scratch,
+                          cudaStream_t st)
 {
     const long long nc = (long long)d.ni * d.nj;
-    k_nb_cand_count<<<nblk(nc, kThreads), kThreads, 0, st>>>(nc, G.fluid_sdf, G.counts,
-                                                            sp.particlesPerCell, R.cand_n);
+    k_nb_cand_count<<<nblk(nc, kThreads), kThreads, 0, st>>>(nc, G.fluid_sdf, G.counts, G.material,
+                                                            sp.particlesPerCell, nb ? 1 : 0, R.cand_n);
     scan_exclusive(R.cand_n, R.cand_off, (int)nc, scan_scratch, st);
     launch_mt_draws(R.rng, R.draws, R.cand_off + nc, 2, st);
     cudaMemsetAsync(R.cross_n, 0, sizeof(int), st);
-    k_nb_place<<<nblk(nc, kThreads), kThreads, 0, st>>>(d, R, G.fluid_sdf, G.visc);
+    k_nb_place<<<nblk(nc, kThreads), kThreads, 0, st>>>(d, R, G.fluid_sdf, G.visc, G.material,
+                                                        G.emitter_id, G.u, G.v, S, nb ? 1 : 0);
 }
 
 } // namespace fsg

@@ -549,7 +549,8 @@ __global__ void k_nb_scatter_live(Particles P, int *status)
     P.slot_bin2[dst] = b;
 }
 
-// the kept candidates after them; the viscosity goes through the cell's bin,
+// the kept candidates after them (velocity and viscosity as placed); the
+// viscosity goes through the cell's bin,
 // so a particle whose position lies in another bin keeps 0 (the fix-up
 // below stores its viscosity where the reference does)
 __global__ void k_nb_scatter_new(Particles P, NbReseed R)
@@ -559,7 +560,7 @@ __global__ void k_nb_scatter_new(Particles P, NbReseed R)
     const int d = P.mkey[m], k = P.mval[m];
     const int dst = P.bin_start2[d] + P.survivors[d] + (m - P.inc_off[d]);
     P.pos2[dst] = R.cand_pos[k];
-    P.vel2[dst] = make_float2(0.f, 0.f);
+    P.vel2[dst] = R.cand_vel[k];
     P.visc2[dst] = R.cand_cb[k] == d ? R.cand_visc[k] : 0.f;
     P.slot_bin2[dst] = d;
     R.pos_of[k] = m;

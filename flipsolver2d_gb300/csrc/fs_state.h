@@ -100,8 +100,21 @@ struct NbGrids {
     float *adv_u = nullptr, *adv_v = nullptr, *adv_sdf = nullptr, *adv_visc = nullptr;
 };
 
-// NB-FLIP reseeding scratch; candidates are numbered in the reference's
-// order (row-major cell, then draw)
+// an Emitter's parameters (emitter.h) as the liquid solvers read them;
+// velocity in scene units per second
+struct SourceParams {
+    float visc, div, vx, vy;
+    int transfer, pad[3];
+};
+struct Sources {
+    const SourceParams *p = nullptr; // device, n entries
+    int n = 0;
+    const float *xy = nullptr;       // device polygon vertices (the scene's)
+    const int *off = nullptr;        // vertex offsets per source polygon (n + 1)
+};
+
+// reseeding scratch (NB-FLIP's band, or FLIP's source cells); candidates are
+// numbered in the reference's order (row-major cell, then draw)
 constexpr int kNbCrossMax = 1 << 16; // candidates whose position left their cell's bin
 struct NbReseed {
     uint32_t *rng = nullptr;   // std::mt19937 state: 624 words, next index
@@ -109,6 +122,7 @@ struct NbReseed {
     int *cand_off = nullptr;   // ncell + 1: first candidate per cell, total at [ncell]
     float *draws = nullptr;    // 2 per candidate
     float2 *cand_pos = nullptr;
+    float2 *cand_vel = nullptr;
     float *cand_visc = nullptr;
     int *cand_bin = nullptr;   // bin of the position, -1 when not kept
     int *cand_cb = nullptr;    // bin of the cell
@@ -167,6 +181,8 @@ void launch_body_forces(const GridDims &d, const SceneParams &sp, const Grids &G
 int levelset_max_passes(const GridDims &d);
 // sinks, solids and the initial fluid; with `nb` the initial fluid sets the
 // fluid SDF as NBFlipSolver::fluidSdfFromInitialFluid does and clears counts
+// (poly_kind 0 solid, 1 initial fluid, 2 sink, 3 source; poly_val the
+// friction, viscosity, divergence or divergence)
 void launch_scene_classify(const GridDims &d, const Grids &G, float dx, const float *poly_xy,
                            const int *poly_off, const int *poly_kind, const float *poly_val,
                            int npoly, bool nb, cudaStream_t st);
@@ -181,10 +197,18 @@ void launch_mt_draws(uint32_t *state, float *out, const int *count, int per, cud
 // narrow-band pruning after advection, then the four semi-Lagrangian grids
 void launch_nb_advect_extra(const GridDims &d, const SceneParams &sp, const Particles &P,
                             const Grids &G, const NbGrids &N, const Scalars *sc, cudaStream_t st);
-void launch_nb_combine(const GridDims &d, const Grids &G, const NbGrids &N, cudaStream_t st);
+// FlipSolver::afterTransfer's source cells; with NB-FLIP also
+// updateGridFromSources and combineAdvectedGrids
+void launch_sources_after_transfer(const GridDims &d, const Grids &G, const Sources &S, double dx,
+                                   cudaStream_t st);
+void launch_nb_combine(const GridDims &d, const Grids &G, const NbGrids &N, const Sources &S,
+                       double dx, cudaStream_t st);
 void launch_nb_materials(const GridDims &d, const Grids &G, cudaStream_t st);
+// nb: NB-FLIP's band and source cells, else FlipSolver::reseedParticles'
+// source cells
 void launch_nb_candidates(const GridDims &d, const SceneParams &sp, const Grids &G,
-                          const NbReseed &R, void *scan_scratch, cudaStream_t st);
+                          const NbReseed &R, const Sources &S, bool nb, void *scan_scratch,
+                          cudaStream_t st);
 // ncand: the candidate total of launch_nb_candidates, read back by the host
 void launch_nb_append(Particles &P, const NbReseed &R, int ncand, void *scratch,
                       cudaStream_t st);

@@ -72,6 +72,8 @@ _SIGS = {
     "fs_add_geometry": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p, ctypes.c_int]),
     "fs_add_initial_fluid": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p, ctypes.c_int]),
     "fs_add_sink": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p, ctypes.c_int]),
+    "fs_add_source": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_float,
+                                     ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_int]),
     "fs_first_frame_init": (ctypes.c_int, [ctypes.c_void_p]),
     "fs_step_frame": (ctypes.c_int, [ctypes.c_void_p]),
     "fs_step": (ctypes.c_int, [ctypes.c_void_p]),
@@ -199,6 +201,10 @@ class GpuFlipSolver:
                        "fs_add_initial_fluid")
             elif o.kind == "sink":
                 _check(self.lib.fs_add_sink(self.h, o.divergence, _ptr(v), len(v)), "fs_add_sink")
+            elif o.kind == "source":
+                _check(self.lib.fs_add_source(self.h, _ptr(v), len(v), o.viscosity, o.divergence,
+                                              float(o.velocity[0]), float(o.velocity[1]),
+                                              int(o.transfer_velocity)), "fs_add_source")
             else:
                 raise ValueError(o.kind)
 

@@ -188,6 +188,14 @@ fs_status fs_destroy(fs_solver *s);
 fs_status fs_add_geometry(fs_solver *s, float friction, const float *xy, int n);
 fs_status fs_add_initial_fluid(fs_solver *s, float viscosity, const float *xy, int n);
 fs_status fs_add_sink(fs_solver *s, float divergence, const float *xy, int n);
+/* FlipSolver::addSource (flipsolver2d.cpp:607-610) with an Emitter
+ * (emitter.h): polygon in scene units, viscosity, divergence, velocity
+ * (vx, vy) in scene units per second and whether it transfers velocity
+ * (velocityTransfer).  Source cells reseed every substep
+ * (reseedParticles, flipsolver2d.cpp:627-680; nbflipsolver.cpp:118-201).
+ * Before fs_first_frame_init only; fs_batch_add refuses such a handle. */
+fs_status fs_add_source(fs_solver *s, const float *xy, int n, float viscosity, float divergence,
+                        float vx, float vy, int velocity_transfer);
 
 /* FlipSolver::firstFrameInit (flipsolver2d.cpp:788-795) */
 fs_status fs_first_frame_init(fs_solver *s);
