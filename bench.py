@@ -233,16 +233,21 @@ def fp64_check(s, sc, p):
             g.set_grid(k, a)
         g.set_dt(dt)
         g.step()
-        out.append((g.get_particles(), g.get_grid("pressure"), g.get_grid("u")))
+        out.append((g.get_particles(), g.get_grid("pressure"), g.get_grid("u"),
+                    [g.stat(0), g.stat(1)]))
     d.close()
-    (a, pa, ua), (b, pb, ub) = out
+    (a, pa, ua, ia), (b, pb, ub, ib) = out
 
     def rel(x, y):
         n = float(np.linalg.norm(y))
         return float(np.linalg.norm(np.asarray(x, np.float64) - np.asarray(y, np.float64)) / n) if n else 0.0
 
     res = {"dt": dt, "particles": int(len(b["pos"])), "pressure_rel_l2": rel(pa, pb),
-           "grid_u_rel_l2": rel(ua, ub)}
+           "grid_u_rel_l2": rel(ua, ub),
+           # iterations of the density and pressure solves in each mode: a
+           # different stopping iteration under the absolute max-abs test
+           # tells a branch apart from rounding in the unconverged solve
+           "pcg_iters_fp32": ia, "pcg_iters_fp64": ib}
     if a["pos"].shape == b["pos"].shape:
         res["particle_vel_rel_l2"] = rel(a["vel"], b["vel"])
         res["particle_pos_max_abs_cells"] = float(np.max(np.abs(a["pos"] - b["pos"])))

@@ -21,6 +21,7 @@
 // (fence.proxy.async) before it arrives at the grid barrier; after the barrier
 // the loading thread fences again before issuing the next TMA loads.
 #include <cfloat>
+#include <initializer_list>
 #include <cstdio>
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -1468,11 +1469,10 @@ static int strip_rows(int ti, int tj)
     if (tj % 32 != 0 || tj / 32 > warps || warps % (tj / 32) != 0) return 0;
     const int nstrips = warps / (tj / 32);
     const int rps = (ti + 2 + nstrips - 1) / nstrips;
-    if (rps <= 1) return 1;
-    if (rps <= 2) return 2;
-    if (rps <= 4) return 4;
-    if (rps <= 8) return 8;
-    if (rps <= 16) return 16;
+    // the instantiated strip heights; the smallest that covers the rows, so
+    // that few padding rows are computed (56 rows in 4 strips: 14, not 16)
+    for (int h : {1, 2, 4, 8, 12, 14, 16})
+        if (rps <= h) return h;
     return 0;
 }
 
@@ -1540,6 +1540,8 @@ cudaError_t launch_pcg_resident(const PcgArgs<float> &a, int ti, int tj, cudaStr
     case 2: return launch_resident_rps<2>(a, ti, tj, grid, st);
     case 4: return launch_resident_rps<4>(a, ti, tj, grid, st);
     case 8: return launch_resident_rps<8>(a, ti, tj, grid, st);
+    case 12: return launch_resident_rps<12>(a, ti, tj, grid, st);
+    case 14: return launch_resident_rps<14>(a, ti, tj, grid, st);
     case 16: return launch_resident_rps<16>(a, ti, tj, grid, st);
     default: return launch_resident_rps<0>(a, ti, tj, grid, st);
     }
