@@ -1471,7 +1471,7 @@ static int strip_rows(int ti, int tj)
     const int rps = (ti + 2 + nstrips - 1) / nstrips;
     // the instantiated strip heights; the smallest that covers the rows, so
     // that few padding rows are computed (56 rows in 4 strips: 14, not 16)
-    for (int h : {1, 2, 4, 8, 12, 14, 16})
+    for (int h : {1, 2, 4, 6, 8, 10, 12, 14, 16})
         if (rps <= h) return h;
     return 0;
 }
@@ -1539,7 +1539,9 @@ cudaError_t launch_pcg_resident(const PcgArgs<float> &a, int ti, int tj, cudaStr
     case 1: return launch_resident_rps<1>(a, ti, tj, grid, st);
     case 2: return launch_resident_rps<2>(a, ti, tj, grid, st);
     case 4: return launch_resident_rps<4>(a, ti, tj, grid, st);
+    case 6: return launch_resident_rps<6>(a, ti, tj, grid, st);
     case 8: return launch_resident_rps<8>(a, ti, tj, grid, st);
+    case 10: return launch_resident_rps<10>(a, ti, tj, grid, st);
     case 12: return launch_resident_rps<12>(a, ti, tj, grid, st);
     case 14: return launch_resident_rps<14>(a, ti, tj, grid, st);
     case 16: return launch_resident_rps<16>(a, ti, tj, grid, st);

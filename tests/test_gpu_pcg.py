@@ -74,8 +74,10 @@ def test_fp64_matches_reference_loop(port_lib, gpu_lib, n, seed):
         assert err <= 1e-9, f"n={n} limit={limit}: {err}"
 
 
-# 768 and 1000 put the resident kernel's register strips at 12 and 14 rows
-@pytest.mark.parametrize("n,seed", [(64, 5), (128, 6), (256, 7), (768, 8), (1000, 9)])
+# 600, 768, 900 and 1000 put the resident kernel's register strips at 6, 10,
+# 12 and 14 rows
+@pytest.mark.parametrize("n,seed", [(64, 5), (128, 6), (256, 7), (600, 10), (768, 8), (900, 11),
+                                    (1000, 9)])
 def test_fp32_close_to_fp64(port_lib, gpu_lib, n, seed):
     m = random_mask(n, seed)
     b = rhs_for(m, seed)
