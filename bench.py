@@ -100,17 +100,25 @@ class ClockSampler:
         self.device = device
         self.proc = None
         self.lines = []
+        self.pre = []
 
     def start(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except Exception:
             self.proc = None
+            return
+        # nvidia-smi takes a moment to start: wait for its first sample, so
+        # that the samples kept are the ones taken inside the timed region
+        t0 = time.time()
+        while not self.lines and self.proc.poll() is None and time.time() - t0 < 5:
+            time.sleep(0.01)
+        self.pre, self.lines = self.lines, []
 
     def _read(self):
         for line in self.proc.stdout:
@@ -126,7 +134,9 @@ class ClockSampler:
             self.proc.kill()
         sms, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        # a region shorter than the sampling period: the sample just before it
+        in_region = len(self.lines)
+        for ln in self.lines if in_region else self.pre[-1:]:
             parts = [x.strip() for x in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -139,7 +149,7 @@ class ClockSampler:
                 if v.lower() == "active":
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sms) if sms else None, "sm_max_mhz": mx,
-                "reasons": sorted(reasons), "samples": len(sms)}
+                "reasons": sorted(reasons), "samples": len(sms), "samples_in_region": in_region}
 
 
 def combine_replicas(ms: float, work: float, dist=None, device: str = "cpu"):
