@@ -1581,6 +1581,21 @@ extern "C" fs_status fs_get_particles(fs_solver *s, int32_t *bin_counts, float *
     return FS_OK;
 }
 
+// whether any of n bytes is nonzero: an OR over 8-byte words, no early exit,
+// so the loop vectorises
+static bool any_nonzero(const uint8_t *p, size_t n)
+{
+    uint64_t acc = 0;
+    size_t k = 0;
+    for (; k + 8 <= n; k += 8) {
+        uint64_t w;
+        memcpy(&w, p + k, 8);
+        acc |= w;
+    }
+    for (; k < n; k++) acc |= p[k];
+    return acc != 0;
+}
+
 extern "C" fs_status fs_set_particles(fs_solver *s, const int32_t *bin_counts, const float *pos_xy,
                                       const float *vel_xy, const float *visc, const uint8_t *dead)
 {
@@ -1588,32 +1603,38 @@ extern "C" fs_status fs_set_particles(fs_solver *s, const int32_t *bin_counts, c
         return fail(FS_ERR_BAD_ARG, "null argument");
     TRY(set_device(s));
     TRY(sync_all(s));
-    std::vector<int> counts(bin_counts, bin_counts + s->P.nbins);
+    const int nb = s->P.nbins;
     size_t total = 0;
-    for (int c : counts) {
-        if (c < 0) return fail(FS_ERR_BAD_ARG, "negative bin count");
-        total += (size_t)c;
+    bool negative = false;
+    for (int b = 0; b < nb; b++) {
+        negative |= bin_counts[b] < 0;
+        total += (size_t)(unsigned)bin_counts[b];
     }
+    if (negative) return fail(FS_ERR_BAD_ARG, "negative bin count");
     if (total > (size_t)INT32_MAX / 2) return fail(FS_ERR_BAD_ARG, "too many particles");
-    if (dead)
-        for (size_t k = 0; k < total; k++)
-            if (dead[k])
-                return fail(FS_ERR_UNSUPPORTED,
-                            "particles marked for death can only exist inside a substep");
+    if (dead && any_nonzero(dead, total))
+        return fail(FS_ERR_UNSUPPORTED, "particles marked for death can only exist inside a substep");
     // the positions and velocities are float pairs already: copy them
     // straight from the caller's memory; the slot-to-bin map is built on the
     // device
-    const int nb = s->P.nbins;
     if ((int)total > s->P.cap || s->P.pos == nullptr) {
         // NB-FLIP keeps room for 2 particlesPerCell per cell (reseeding)
         const long long keep = s->grows ? 2LL * s->p.particlesPerCell * (long long)s->ncell : 0;
         TRY(alloc_particles(s, (int)std::max<long long>((long long)total, keep)));
     }
-    std::vector<int> start(nb + 1, 0);
-    for (int b = 0; b < nb; b++) start[b + 1] = start[b] + counts[b];
     Particles &P = s->P;
-    CK(cudaMemcpyAsync(P.bin_start, start.data(), (nb + 1) * sizeof(int), cudaMemcpyHostToDevice, s->st));
-    CK(cudaMemcpyAsync(P.bin_count, counts.data(), nb * sizeof(int), cudaMemcpyHostToDevice, s->st));
+    // the counts straight from the caller's memory; the bin starts by a device
+    // scan of them (pinned caller memory then needs no staging copy)
+    CK(cudaMemcpyAsync(P.bin_count, bin_counts, nb * sizeof(int), cudaMemcpyHostToDevice, s->st));
+    if (s->rebin_scratch && scan_scratch_bytes(nb) <= s->rebin_scratch_size) {
+        scan_exclusive(P.bin_count, P.bin_start, nb, s->rebin_scratch, s->st);
+        g_kernel_launches += 3;
+    } else {
+        std::vector<int> start(nb + 1, 0);
+        for (int b = 0; b < nb; b++) start[b + 1] = start[b] + bin_counts[b];
+        CK(cudaMemcpyAsync(P.bin_start, start.data(), (nb + 1) * sizeof(int), cudaMemcpyHostToDevice,
+                           s->st));
+    }
     if (total) {
         CK(cudaMemcpyAsync(P.pos, pos_xy, total * sizeof(float2), cudaMemcpyHostToDevice, s->st));
         CK(cudaMemcpyAsync(P.vel, vel_xy, total * sizeof(float2), cudaMemcpyHostToDevice, s->st));
