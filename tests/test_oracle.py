@@ -19,6 +19,7 @@ from conftest import POOL_THREADS
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 
 from test_scenes_json import DAM_JSON  # noqa: E402
+from edge_scenes import EDGE_SCENES  # noqa: E402
 
 PIN_SCENES = {
     "dam32": lambda: scenes.dam_break(32, seed=42),
@@ -33,6 +34,8 @@ PIN_SCENES = {
     "nb_dam44_source": lambda: scenes.with_source(scenes.nb_dam_break(44, seed=6), transfer=False,
                                                   box=(0.2, 0.35, 0.5, 0.7), viscosity=2.0),
     "nb_dam44_source_transfer": lambda: scenes.with_source(scenes.nb_dam_break(44, seed=6)),
+    # a ragged grid, a sink that kills particles, a scene without fluid
+    **EDGE_SCENES,
 }
 
 
