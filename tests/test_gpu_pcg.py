@@ -138,3 +138,34 @@ def test_matviz_known_answer(gpu_lib):
     fluid = (m & 0x40) != 0
     err = np.linalg.norm(x[fluid] - x_ref[fluid]) / np.linalg.norm(x_ref[fluid])
     assert err < 1e-4, f"relative-L2 vs the reference's vout: {err}"
+
+
+def ragged_mask(ni, nj, seed):
+    """random_mask cropped to ni x nj, with its 1-cell solid border redrawn."""
+    m = random_mask(max(ni, nj), seed)[:ni, :nj].copy()
+    m[0, :] = m[-1, :] = m[:, 0] = m[:, -1] = 0x20
+    return m
+
+
+@pytest.mark.parametrize("ni,nj,seed", [(37, 90, 21), (130, 47, 22), (700, 1024, 23)])
+def test_ragged_grids(port_lib, gpu_lib, ni, nj, seed):
+    """gridSizeI != gridSizeJ.  The reference recurrence is chaotic on the two
+    narrow systems: a 1e-15 relative change of b moves the oracle's own
+    200-iteration result by 2.5e-5 (37 x 90) and 2.3e-2 (130 x 47), against
+    7.6e-14 and 1.8e-10 after 37 iterations.  So the FP64 mode keeps the
+    oracle's iteration count at both limits and its pressure to 1e-8 after 37
+    iterations; the FP32 mode keeps the true residual after 37 iterations."""
+    m = ragged_mask(ni, nj, seed)
+    b = rhs_for(m, seed)
+    dx = 1.0 / max(ni, nj)
+    for limit in (200, 37):
+        it_o, x_o = fo.pcg_solve(m, b, 1.0 / 30, 1000.0, dx, limit, 1e-2)
+        it_g, x_g = gpu.pcg_solve(m, b, 1.0 / 30, 1000.0, dx, limit, 1e-2,
+                                  precision=gpu.FS_PCG_FP64, pool_threads=POOL_THREADS)
+        assert it_g == it_o, f"limit {limit}"
+    assert np.linalg.norm(x_g - x_o) / np.linalg.norm(x_o) <= 1e-8
+    _, x_f = gpu.pcg_solve(m, b, 1.0 / 30, 1000.0, dx, 37, 1e-2,
+                           precision=gpu.FS_PCG_FP32, pool_threads=POOL_THREADS)
+    res_o = np.linalg.norm(b - apply_a(m, x_o, 1.0 / 30, 1000.0, dx))
+    res_f = np.linalg.norm(b - apply_a(m, x_f, 1.0 / 30, 1000.0, dx))
+    assert res_f <= 1.05 * res_o + 1e-6 * np.linalg.norm(b), (res_f, res_o)
