@@ -8,7 +8,8 @@ GPU parity tests (test_gpu_edges.py):
                     (FlipSolver::addSink, sink.h): particles in SINK cells
                     are killed during advection (flipsolver2d.cpp:305-338);
   * empty_box    -- walls and an obstacle, no fluid: zero particles from the
-                    first frame on.
+                    first frame on;
+  * nb_ragged_dam -- the ragged dam stepped by NBFlipSolver.
 """
 from flipsolver2d_gb300 import scenes
 from flipsolver2d_gb300.scenes import FlipSolverParameters, Scene, SceneObject
@@ -47,4 +48,18 @@ def empty_box(res: int = 32, seed: int = 13) -> Scene:
     return Scene(f"empty_box_{res}", p, objs)
 
 
-EDGE_SCENES = {"ragged_dam40": ragged_dam, "sink_dam36": sink_dam, "empty_box32": empty_box}
+def nb_ragged_dam(res: int = 40, seed: int = 14) -> Scene:
+    """ragged_dam stepped by NBFlipSolver, with nb_dam_break's settings."""
+    sc = ragged_dam(res, seed)
+    sc.params.particlesPerCell = 8
+    sc.params.pcgIterLimit = 1000
+    for o in sc.objects:
+        if o.kind == "fluid":
+            o.viscosity = 10.0
+    sc.sim_type = scenes.SIM_NBFLIP
+    sc.name = f"nb_ragged_dam_{res}"
+    return sc
+
+
+EDGE_SCENES = {"ragged_dam40": ragged_dam, "sink_dam36": sink_dam, "empty_box32": empty_box,
+               "nb_ragged_dam40": nb_ragged_dam}
