@@ -29,17 +29,23 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-FRAME_SCENES = ["dam32", "random40", "nbdam40"]
+FRAME_SCENES = ["dam32", "random40", "nbdam40", "sink36", "ragged40"]
 NB_FRAMES = 5  # NB-FLIP seeds its first particles at the end of frame 1
+SCENE_FRAMES = {"sink36": 6}  # the front reaches the sink in frame 4
 FLUID, SOLID, EMPTY = 0x40, 0x20, 0x10
 
 
 def scene_by_name(name):
     from flipsolver2d_gb300 import scenes
 
+    sys.path.insert(0, os.path.dirname(HERE))
+    import edge_scenes
+
     return {"dam32": lambda: scenes.dam_break(32, seed=42),
             "random40": lambda: scenes.random_scene(40, 1001),
-            "nbdam40": lambda: scenes.nb_dam_break(40, seed=3, obstacle=True)}[name]()
+            "nbdam40": lambda: scenes.nb_dam_break(40, seed=3, obstacle=True),
+            "sink36": edge_scenes.sink_dam,
+            "ragged40": edge_scenes.ragged_dam}[name]()
 
 
 def parse_matviz(ref: str):
@@ -122,7 +128,7 @@ def make_frames(frames: int = 3, names=FRAME_SCENES):
     for name in names:
         s = fo.OracleSolver(scene_by_name(name), "ref")
         out = {"pool_threads": np.int32(s.stat(4))}
-        for f in range(1, (NB_FRAMES if s.nb else frames) + 1):
+        for f in range(1, (NB_FRAMES if s.nb else SCENE_FRAMES.get(name, frames)) + 1):
             s.step_frame()
             p = s.get_particles()
             for k, v in p.items():

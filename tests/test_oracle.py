@@ -105,7 +105,8 @@ def test_port_matches_reference_nbflip_stages(port_lib, ref_lib):
 
 
 GOLDEN_SCENES = {"dam32": PIN_SCENES["dam32"], "random40": PIN_SCENES["random40"],
-                 "nbdam40": lambda: scenes.nb_dam_break(40, seed=3, obstacle=True)}
+                 "nbdam40": lambda: scenes.nb_dam_break(40, seed=3, obstacle=True),
+                 "sink36": EDGE_SCENES["sink_dam36"], "ragged40": EDGE_SCENES["ragged_dam40"]}
 
 
 @pytest.mark.parametrize("name", sorted(GOLDEN_SCENES))
