@@ -49,10 +49,10 @@ SEED = 7
 WARM_FRAMES = 2
 METRIC = "particle-substeps/s"
 WORKLOAD = "dam_break_1024_obstacle"
-# DRAM bytes (read + write) of one k_pcg_resident launch at 1024^2, from the
-# ncu capture summarised in profiles/k_pcg_resident_dam_break.md; the solve
-# keeps its vectors on chip, so this is little more than b and the operator
-# in, x out
+# DRAM bytes (read + write) of one k_pcg_resident launch at 1024^2, measured
+# by ncu (dram__bytes_read.sum + dram__bytes_write.sum) on this workload; the
+# solve keeps its vectors on chip, so this is little more than b and the
+# operator in, x out
 PCG_TRAFFIC_BYTES = 13026560
 
 
@@ -172,11 +172,44 @@ def executed_iters(ret: int, limit: int) -> int:
     return limit if ret >= limit else ret + 1
 
 
-def run_cpu_sample(threads: int, substeps: int = 2):
-    """The CPU oracle on a bounded sample: frame-0 setup (untimed), then
-    `substeps` substeps of the same workload."""
+def cpu_info():
+    """What the CPU baseline ran on: the CPU model (lscpu), the processors
+    the OS reports and this process may use, and the count the reference's
+    thread pool would take (std::thread::hardware_concurrency())."""
+    import platform
+
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                model = ln.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    info = {"cpu_model": model, "machine": platform.machine(), "nproc": os.cpu_count(),
+            "affinity_cpus": len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else None}
+    try:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import fsoracle as fo
+
+        info["hardware_concurrency"] = int(fo.load("port").fso_hardware_concurrency())
+    except Exception:
+        info["hardware_concurrency"] = None
+    return info
+
+
+def run_cpu_sample(threads: int, substeps: int = 2, snapshot=None, warmup: int = 3):
+    """The CPU implementation on a bounded sample of the work the GPU arm
+    times: the workload after WARM_FRAMES frames and `warmup` CFL substeps,
+    then `substeps` timed substeps, each with the CFL dt of the frame loop.
+    The warm state is `snapshot` (the GPU's state at that point, in the
+    oracle's layout) when given, else the oracle steps it itself; either way
+    it is untimed.  The reference build runs where its sources are present,
+    else the pinned plain-C port, on `threads` host threads with the
+    reference's pool size for its chunked reductions."""
     os.environ["FSO_HOST_THREADS"] = str(threads)
-    os.environ.setdefault("FSO_REF_THREADS", str(threads))
+    os.environ["FSO_REF_THREADS"] = str(threads)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import build as oracle_build
 
@@ -187,7 +220,19 @@ def run_cpu_sample(threads: int, substeps: int = 2):
     sc = scene()
     o = fo.OracleSolver(sc, "ref" if kind == "reference" else "port")
     o.first_frame_init()
-    work, t_total, times = 0, 0.0, []
+    t_warm = time.perf_counter()
+    if snapshot is not None:
+        o.restore(snapshot)
+        start = "the GPU's state"
+    else:
+        for _ in range(WARM_FRAMES):
+            o.step_frame()
+        for _ in range(warmup):
+            o.set_dt(cfl_dt(o.max_particle_velocity(), sc.params))
+            o.step()
+        start = "its own state"
+    t_warm = time.perf_counter() - t_warm
+    work, t_total, times, iters = 0, 0.0, [], []
     for _ in range(substeps):
         n = o.particle_count()
         o.set_dt(cfl_dt(o.max_particle_velocity(), sc.params))
@@ -197,10 +242,26 @@ def run_cpu_sample(threads: int, substeps: int = 2):
         times.append(dt)
         t_total += dt
         work += n
+        iters.append([executed_iters(o.stat(0), sc.params.pcgIterLimit),
+                      executed_iters(o.stat(1), sc.params.pcgIterLimit)])
     o.close()
+    info = cpu_info()
     return {"value": work / t_total, "unit": METRIC, "cores": threads, "kind": kind,
-            "sample": f"{substeps} substeps of {WORKLOAD} from frame 0 ({work} particle-substeps, "
-                      f"{t_total:.1f} s)", "step_s": times}
+            "sample": f"{substeps} substeps of {WORKLOAD} from {start} after {WARM_FRAMES} frames "
+                      f"and {warmup} substeps ({work} particle-substeps, {t_total:.1f} s; "
+                      f"warm-up {t_warm:.1f} s untimed)",
+            "pcg_iterations_per_step": iters, "step_s": times, **info}
+
+
+def bench_config(warmup: int):
+    """`config` of both arms: the workload and the point it is timed at."""
+    return {"workload": WORKLOAD, "grid": RES, "seed": SEED, "warm_frames": WARM_FRAMES,
+            "warm_substeps": warmup, "pcg_iter_limit": 200,
+            "stopping": "reference absolute 1e-2 max-abs test"}
+
+
+CPU_KEYS = ("value", "unit", "cores", "kind", "sample", "cpu_model", "machine", "nproc",
+            "affinity_cpus", "hardware_concurrency", "pcg_iterations_per_step")
 
 
 def reference_arm(args):
@@ -209,26 +270,63 @@ def reference_arm(args):
         return 0
     threads = os.cpu_count() or 1
     steps = max(1, min(args.steps, 3))
-    cb = run_cpu_sample(threads, substeps=steps)
+    cb = run_cpu_sample(threads, substeps=steps, warmup=args.warmup)
     line = {"metric": METRIC, "value": cb["value"], "unit": METRIC, "n_gpus": args.gpus,
-            "steps": steps, "warmup": 0, "ms_per_step": 1e3 * float(np.mean(cb["step_s"])),
+            "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(cb["step_s"])),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded dam-break scene)",
-            "config": {"workload": WORKLOAD, "grid": RES, "seed": SEED,
-                       "pcg": "reference PCG+IPP, FP64, limit 200, abs tol 1e-2"},
+            "data": "synthetic (seeded dam-break scene)", "config": bench_config(args.warmup),
+            "pcg": "reference PCG+IPP, FP64, limit 200, abs tol 1e-2",
             "impl": "reference",
-            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "cpu_baseline": {k: cb[k] for k in CPU_KEYS if k in cb},
             "e2e": {"value": cb["value"], "unit": METRIC, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
 
 
+def apply_operator(mat, x, dt, density, dx):
+    """The reference's pressure operator (IndexedPressureParameterUnit::
+    multiply, pressuredata.h:132-146, rows as getPressureProjectionMatrix
+    builds them, flipsolver2d.cpp:797-887) applied in float64 on the host:
+    scale (count x_c - sum of fluid neighbours) on fluid rows, identity on the
+    others.  Used only to measure residuals outside any timed region."""
+    ni, nj = mat.shape
+    scale = np.float64(np.float32(dt)) / (density * dx * dx)
+    fl = (mat & 0x40) != 0
+    solid = (mat & 0x20) != 0
+    pad_s = np.pad(solid, 1, mode="edge")
+    pad_f = np.pad(fl, 1, mode="edge")
+    xp = np.pad(x, 1)
+    cnt = np.zeros_like(x)
+    acc = np.zeros_like(x)
+    for di, dj in ((-1, 0), (1, 0), (0, -1), (0, 1)):
+        cnt += ~pad_s[1 + di:ni + 1 + di, 1 + dj:nj + 1 + dj]
+        acc += pad_f[1 + di:ni + 1 + di, 1 + dj:nj + 1 + dj] * xp[1 + di:ni + 1 + di, 1 + dj:nj + 1 + dj]
+    out = x.copy()
+    out[fl] = (scale * (cnt * x - acc))[fl]
+    return out
+
+
+# the FP32 production mode's bar against the FP64 parity mode on one substep
+# from identical inputs (the 200-iteration solve does not converge, so the
+# bar is on residuals, velocities and the recurrence's own spread)
+FP64_CHECK_VEL_BAR = 1e-2
+FP64_CHECK_SPREAD_FACTOR = 10.0
+
+
 def fp64_check(s, sc, p):
     """One substep from identical state in the measured FP32 mode and in the
-    FP64 parity mode (the reference's own arithmetic, bit for bit): the
-    error of the FP32 results against the FP64 ones.  Outside any timed
-    region."""
+    FP64 parity mode (the reference's own arithmetic): the FP32 error and the
+    bar it is held to.  Outside any timed region.
+
+    * pressure_rel_l2: FP32 pressure against FP64;
+    * true_rel_residual_fp32 / _fp64: ||b - A p|| / ||b|| of each mode's
+      pressure on its own right-hand side, with the reference's operator;
+    * fp64_spread_rel_l2: how far the FP64 solve itself moves when b moves by
+      1e-7 relative (about one FP32 rounding): the recurrence's sensitivity;
+    * grid_velocity_rel_l2, particle_vel_rel_l2: the projected velocities.
+    The bar: FP32 residual <= 1.05 x FP64 residual + 1e-6, velocities within
+    1e-2, pressure within max(1e-2, 10 x spread)."""
     from flipsolver2d_gb300 import gpu
 
     snap = s.get_particles()
@@ -243,17 +341,33 @@ def fp64_check(s, sc, p):
             g.set_grid(k, a)
         g.set_dt(dt)
         g.step()
-        out.append((g.get_particles(), g.get_grid("pressure"), g.get_grid("u"),
-                    [g.stat(0), g.stat(1)]))
+        out.append((g.get_particles(), g.get_grid("pressure"), g.get_grid("pressure_rhs"),
+                    g.get_grid("u"), g.get_grid("v"), [g.stat(0), g.stat(1)]))
     d.close()
-    (a, pa, ua, ia), (b, pb, ub, ib) = out
+    (a, pa, ba, ua, va, ia), (b, pb, bb, ub, vb, ib) = out
 
     def rel(x, y):
         n = float(np.linalg.norm(y))
         return float(np.linalg.norm(np.asarray(x, np.float64) - np.asarray(y, np.float64)) / n) if n else 0.0
 
+    mat = grids["material"]  # the operator of this substep's solves
+    dx = 1.0 / RES
+
+    def rel_residual(x, rhs):
+        n = float(np.linalg.norm(rhs))
+        return float(np.linalg.norm(rhs - apply_operator(mat, x, dt, p.fluidDensity, dx)) / n) if n else 0.0
+
+    _, p0 = gpu.pcg_solve(mat, bb, dt, p.fluidDensity, dx, p.pcgIterLimit, 1e-2,
+                          precision=gpu.FS_PCG_FP64)
+    xi = np.random.default_rng(5).standard_normal(bb.shape)
+    _, p1 = gpu.pcg_solve(mat, bb * (1.0 + 1e-7 * xi), dt, p.fluidDensity, dx, p.pcgIterLimit, 1e-2,
+                          precision=gpu.FS_PCG_FP64)
+    spread = rel(p1, p0)
+    rr32, rr64 = rel_residual(pa, ba), rel_residual(pb, bb)
     res = {"dt": dt, "particles": int(len(b["pos"])), "pressure_rel_l2": rel(pa, pb),
-           "grid_u_rel_l2": rel(ua, ub),
+           "true_rel_residual_fp32": rr32, "true_rel_residual_fp64": rr64,
+           "fp64_spread_rel_l2": spread,
+           "grid_velocity_rel_l2": max(rel(ua, ub), rel(va, vb)),
            # iterations of the density and pressure solves in each mode: a
            # different stopping iteration under the absolute max-abs test
            # tells a branch apart from rounding in the unconverged solve
@@ -263,7 +377,90 @@ def fp64_check(s, sc, p):
         res["particle_pos_max_abs_cells"] = float(np.max(np.abs(a["pos"] - b["pos"])))
     else:
         res["particle_count_difference"] = int(len(a["pos"]) - len(b["pos"]))
+    res["bar"] = {"residual": rr32 <= 1.05 * rr64 + 1e-6,
+                  "velocity": res["grid_velocity_rel_l2"] <= FP64_CHECK_VEL_BAR
+                  and res.get("particle_vel_rel_l2", 1.0) <= FP64_CHECK_VEL_BAR,
+                  "pressure": res["pressure_rel_l2"] <= max(1e-2, FP64_CHECK_SPREAD_FACTOR * spread),
+                  "stated": "residual <= 1.05 x FP64 + 1e-6; velocities <= 1e-2 rel-L2; "
+                            "pressure <= max(1e-2, 10 x FP64 spread under a 1e-7 change of b)"}
+    res["bar"]["pass"] = res["bar"]["residual"] and res["bar"]["velocity"] and res["bar"]["pressure"]
     return res
+
+
+def gpu_snapshot(s):
+    """The handle's state in the oracle's snapshot layout (the CPU sample
+    starts from it)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import fsoracle as fo
+
+    snap = {"particles": s.get_particles(), "dt": s.dt, "rng": s.get_rng()}
+    for g in fo.STATE_GRIDS:
+        snap[g] = s.get_grid(g)
+    return snap
+
+
+def spec_single_measure(local: int, steps: int):
+    """The bench scene alone in FS_PCG_SPEC mode: every density and pressure
+    solve to a 1e-6 true relative residual (FP32 inner PCG, FP64 refinement);
+    after the same warm frames and 3 warm-up substeps, `steps` substeps
+    device-timed like the main line (L2 flushed between them)."""
+    import torch
+    from flipsolver2d_gb300 import gpu
+
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")
+    sc = scene()
+    p = sc.params
+    s = gpu.GpuFlipSolver(sc, precision=gpu.FS_PCG_SPEC, device=local)
+    for _ in range(WARM_FRAMES):
+        s.step_frame()
+
+    def one_step():
+        n = s.particle_count()
+        s.set_dt(cfl_dt(s.max_particle_velocity(), p))
+        s.step()
+        return n
+
+    for _ in range(3):
+        one_step()
+    s.enable_timers(True)
+    work, step_ms = 0, []
+    for _ in range(steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        s.reset_timers()
+        work += one_step()
+        step_ms.append(s.timer(0))
+    s.enable_timers(False)
+    s.close()
+    total = float(sum(step_ms))
+    return {"workload": f"{WORKLOAD}, FS_PCG_SPEC", "value": work / (total / 1e3), "unit": METRIC,
+            "ms_per_step": total / steps, "steps": steps,
+            "step_latency_ms": {"p50": float(np.percentile(step_ms, 50)),
+                                "p99": float(np.percentile(step_ms, 99))},
+            "pcg": "every solve to a 1e-6 true relative residual: FP32 inner PCG, textbook IPP, "
+                   "FP64 refinement"}
+
+
+def poisson_measure(n: int, warmup: int, steps: int):
+    """The mixed-precision configuration: fs_pcg_solve_spec on the seeded
+    n x n star mask (55 % fluid) with the divergence of N(0, 1) faces, to a
+    1e-6 true relative residual; host arrays, so the time includes the
+    uploads and the download."""
+    from flipsolver2d_gb300 import gpu, scenes
+
+    m, b, dx = scenes.poisson_case(n, seed=0)
+    for _ in range(warmup):
+        gpu.pcg_solve_spec(m, b, 1.0 / 30, 1000.0, dx, 1e-6)
+    times, iters, rr = [], [], 0.0
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        it, x, rr = gpu.pcg_solve_spec(m, b, 1.0 / 30, 1000.0, dx, 1e-6)
+        times.append(time.perf_counter() - t0)
+        iters.append(it)
+    total = sum(times)
+    return {"workload": f"poisson_{n}_spec", "value": n * n * sum(iters) / total,
+            "unit": "cell-iter/s", "ms_per_solve": 1e3 * total / steps, "inner_iterations": iters,
+            "rel_residual": rr, "path": "fs_pcg_solve_spec with host arrays (uploads included)"}
 
 
 def gpu_arm(args):
@@ -304,6 +501,8 @@ def gpu_arm(args):
 
     for _ in range(args.warmup):
         one_step()
+    # the state the timed substeps start from, for the CPU sample
+    cpu_start = gpu_snapshot(s) if (rank == 0 and not args.no_cpu) else None
     s.enable_timers(True)
     sampler = ClockSampler(local)
     sampler.start()
@@ -375,8 +574,9 @@ def gpu_arm(args):
     cpu = None
     if rank == 0 and not args.no_cpu:
         try:
-            cpu = run_cpu_sample(os.cpu_count() or 1, substeps=2)
-            cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+            cpu = run_cpu_sample(os.cpu_count() or 1, substeps=2, snapshot=cpu_start,
+                                 warmup=args.warmup)
+            cpu = {k: cpu[k] for k in CPU_KEYS if k in cpu}
         except Exception as e:  # reported, never fatal for the GPU line
             cpu = {"value": None, "unit": METRIC, "cores": 0, "kind": "port",
                    "sample": f"failed: {e}"}
@@ -385,11 +585,12 @@ def gpu_arm(args):
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded dam-break scene)",
-        "config": {"workload": WORKLOAD, "grid": RES, "seed": SEED, "particles": int(work / args.steps),
-                   "pcg": "PCG+IPP FP32 vectors, float-pair reductions and scalars, reference "
-                          "stopping (limit 200, abs tol 1e-2 max-abs)",
-                   "l2": "flushed between steps (256 MiB write)", "warm_frames": WARM_FRAMES,
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": bench_config(args.warmup),
+        "particles": int(work / args.steps),
+        "pcg": "PCG+IPP FP32 vectors, float-pair reductions and scalars, reference stopping "
+               "(limit 200, abs tol 1e-2 max-abs)",
+        "l2": "flushed between steps (256 MiB write)",
+        "parallelism": "replicas" if world > 1 else "single GPU",
         "pcg_cell_iter_per_s": cell_iters / (pcg_ms / 1e3) if pcg_ms > 0 else None,
         "pcg_iterations_per_step": [list(x) for x in iters],
         "step_latency_ms": {"p50": float(np.percentile(step_ms, 50)),
@@ -416,14 +617,28 @@ def gpu_arm(args):
             line["fp64_check"] = {"error": str(e)}
     s.close()
     if rank == 0 and world == 1 and not args.no_batch:
+        # the plain single-scene path at a 1e-6 pressure residual: the same
+        # scene in FS_PCG_SPEC mode (the figure the batched form divides by)
+        try:
+            line["spec_single"] = spec_single_measure(local, 5)
+        except Exception as e:  # reported, never fatal for the main line
+            line["spec_single"] = {"error": str(e)}
+        # the mixed-precision configuration: one 2048^2 standalone solve
+        try:
+            line["poisson_2048"] = poisson_measure(2048, 1, 3)
+        except Exception as e:  # reported, never fatal for the main line
+            line["poisson_2048"] = {"error": str(e)}
+    if rank == 0 and world == 1 and not args.no_batch:
         # the batched form of the same path beside the single-scene line: 64
         # scenes of the batched-scenes workload stepped together, and 16 of
         # them one at a time, both at a 1e-6 pressure residual
         try:
             r = batch_measure(64, 2, 3, 16)
             bv = r["work"] / (r["total_ms"] / 1e3)
+            ss = line.get("spec_single", {}).get("value")
             line["batch"] = {"workload": "batch_64_scenes (sides 64-512, seeds 1000..1063)",
                              "value": bv, "unit": METRIC, "frames": 3,
+                             "vs_spec_single_1024": bv / ss if ss else None,
                              "ms_per_frame": r["total_ms"] / 3,
                              "single_scene": r["single"], "vs_single_scene": bv / r["single"],
                              "merged_solve_share": r["solve_ms"] / max(r["rounds_ms"], 1e-9),

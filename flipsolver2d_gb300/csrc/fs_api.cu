@@ -183,6 +183,7 @@ struct fs_solver {
     bool tma = false;          // TMA-staged FP32 PCG available for this grid
     int tma_ti = 0, tma_tj = 0;
     bool resident = false;     // FP32 PCG with every tile resident in shared memory
+    LlBuffers ll;              // the resident PCG's exchange words
     ClusterPlan spec_plan{};   // FS_PCG_SPEC: how the cluster solve runs this grid
     ClusterSystem *spec_sys = nullptr; // FS_PCG_SPEC: the density and pressure systems
     double *spec_rel = nullptr;        // their final relative residuals
@@ -494,6 +495,12 @@ static fs_status create_impl(const fs_params *p, const fs_exec_params *exec, boo
     A(dalloc(s, &s->bar, 1));
     if (s->prec == FS_PCG_FP32)
         s->resident = resident_tile_shape(d.ni, d.nj, &s->res_ti, &s->res_tj);
+    if (s->resident) {
+        s->ll.words = n;
+        A(dalloc(s, &s->ll.r, n));
+        A(dalloc(s, &s->ll.s, n));
+        A(dalloc(s, &s->ll.rec, kLlRecWords));
+    }
     if (s->prec == FS_PCG_FP32 && tma_tile_shape(d.ni, d.nj, &s->tma_ti, &s->tma_tj)) {
         s->tma = tma_maps(&s->maps_dens, d.ni, d.nj, s->tma_ti, s->tma_tj, G.cell_info,
                           (const float *)s->dens_rhs, (const float *)s->dens_x,
@@ -1031,6 +1038,8 @@ template <typename T> static PcgArgs<T> pcg_args(fs_solver *s, const void *b, vo
     a.r1 = (T *)s->r1;
     a.s0 = (T *)s->s0;
     a.s1 = (T *)s->s1;
+    a.ll_r = s->ll.r;
+    a.ll_s = s->ll.s;
     a.partials = s->partials;
     a.chunk_end = s->chunk_end;
     a.chunk_last_unit = s->chunk_last;
@@ -1076,7 +1085,7 @@ static fs_status run_pcg(fs_solver *s, const void *b, void *x, int *iters)
     } else if (s->resident) {
         PcgArgs<float> pa = pcg_args<float>(s, b, x, iters);
         pa.mode = 2; // unless a unit row sits on a j edge
-        e = launch_pcg_resident(pa, s->res_ti, s->res_tj, s->st);
+        e = launch_pcg_resident(pa, s->res_ti, s->res_tj, s->st, &s->ll);
         if (e == cudaSuccess) e = launch_pcg_linear_if_wrap(pa, s->st);
         launched = 2;
     } else if (s->tma) {
@@ -2581,9 +2590,11 @@ struct PcgCache {
     GridBarrier *bar = nullptr;
     Scalars *sc = nullptr;
     Scalars *sc_host = nullptr;
+    LlBuffers ll; // the resident FP32 kernel's exchange words
     void release()
     {
-        void *ps[] = {material, info, b, x, r0, r1, s0, s1, partials, chunk_end, chunk_last, chunk_val, bar, sc};
+        void *ps[] = {material, info, b, x, r0, r1, s0, s1, partials, chunk_end, chunk_last, chunk_val, bar, sc,
+                      ll.r, ll.s, ll.rec};
         for (void *p : ps)
             if (p) cudaFree(p);
         if (sc_host) cudaFreeHost(sc_host);
@@ -2612,6 +2623,12 @@ static fs_status pcg_cache_get(int dev, size_t cells, size_t esz, int nchunks, P
     CK(cudaMalloc(&c.info, cells));
     void **vs[] = {&c.b, &c.x, &c.r0, &c.r1, &c.s0, &c.s1};
     for (void **v : vs) CK(cudaMalloc(v, cells * esz));
+    if (esz == 4) {
+        c.ll.words = cells;
+        CK(cudaMalloc(&c.ll.r, cells * sizeof(unsigned long long)));
+        CK(cudaMalloc(&c.ll.s, cells * sizeof(unsigned long long)));
+        CK(cudaMalloc(&c.ll.rec, kLlRecWords * sizeof(unsigned long long)));
+    }
     int maxgrid = std::max(pcg_grid_size<double>(1LL << 40), pcg_grid_size<float>(1LL << 40));
     CK(cudaMalloc(&c.partials, (size_t)(8 * maxgrid + 16) * sizeof(double)));
     CK(cudaMalloc(&c.chunk_end, (size_t)c.chunk_cap * sizeof(int)));
@@ -2672,6 +2689,7 @@ static fs_status pcg_solve_common(int ni, int nj, const int8_t *mat_dev, float d
         a.ni = ni; a.nj = nj; a.N = (long long)N; a.info = c->info;
         a.b = (const float *)rhs_dev; a.x = (float *)res_dev;
         a.r0 = (float *)c->r0; a.r1 = (float *)c->r1; a.s0 = (float *)c->s0; a.s1 = (float *)c->s1;
+        a.ll_r = c->ll.r; a.ll_s = c->ll.s;
         a.partials = c->partials; a.chunk_end = c->chunk_end; a.chunk_last_unit = c->chunk_last;
         a.chunk_val = c->chunk_val;
         a.nchunks = (int)ends.size(); a.sc = c->sc; a.density = density; a.dx = dx;
@@ -2682,7 +2700,7 @@ static fs_status pcg_solve_common(int ni, int nj, const int8_t *mat_dev, float d
         TmaMaps maps;
         if (resident_tile_shape(ni, nj, &ti, &tj)) {
             a.mode = 2;
-            e = launch_pcg_resident(a, ti, tj, st);
+            e = launch_pcg_resident(a, ti, tj, st, &c->ll);
             if (e == cudaSuccess) e = launch_pcg_linear_if_wrap(a, st);
             launched = 2;
         } else if (tma_tile_shape(ni, nj, &ti, &tj) &&
@@ -3155,7 +3173,9 @@ extern "C" fs_status fs_cluster_autotune(int ni, int nj, int objective, int devi
 //
 // The first call on a device looks up the array's address there
 // (cudaGetSymbolAddress, with that device current); make that first call
-// before any stream capture begins.  All calls use the same array and it keeps
+// before any stream capture begins.  The address is kept for the life of the
+// process, so calls after a reset of that device (cudaDeviceReset) are not
+// supported.  All calls use the same array and it keeps
 // whatever the last call left in it, so each call clears the words that must
 // start at zero (scalars, barrier counter, epoch flags) itself.  Two calls that
 // overlapped on the GPU would race on the array; this function holds a
@@ -3176,7 +3196,10 @@ constexpr size_t kNaPartials = na_up(kNaS1 + 4 * kNoAllocMaxCells);
 constexpr size_t kNaChunkEnd = na_up(kNaPartials + 8 * (8 * (size_t)kNoAllocMaxGrid + 16));
 constexpr size_t kNaChunkLast = na_up(kNaChunkEnd + 4 * ((size_t)kNoAllocMaxParts + 1));
 constexpr size_t kNaChunkVal = na_up(kNaChunkLast + 4 * ((size_t)kNoAllocMaxParts + 1));
-constexpr size_t kNaBar = na_up(kNaChunkVal + 8 * ((size_t)kNoAllocMaxParts + 1));
+constexpr size_t kNaLlR = na_up(kNaChunkVal + 8 * ((size_t)kNoAllocMaxParts + 1));
+constexpr size_t kNaLlS = na_up(kNaLlR + 8 * kNoAllocMaxCells);
+constexpr size_t kNaLlRec = na_up(kNaLlS + 8 * kNoAllocMaxCells);
+constexpr size_t kNaBar = na_up(kNaLlRec + 8 * kLlRecWords);
 constexpr size_t kNaScalars = na_up(kNaBar + sizeof(GridBarrier));
 constexpr size_t kNaBytes = na_up(kNaScalars + sizeof(Scalars));
 } // namespace
@@ -3185,6 +3208,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
 
 static std::mutex g_noalloc_mu;
 static unsigned char *g_noalloc_base[64]; // the array's address per device
+static LlBuffers g_noalloc_ll[64];        // its exchange-word regions per device
 
 // splitRange chunk ends (the reference's partition of [0, N) into parts)
 __global__ void k_na_chunk_ends(int *ends, int parts, long long ps, long long rem)
@@ -3262,6 +3286,13 @@ extern "C" fs_status fs_pcg_solve_device_noalloc(int ni, int nj, const int8_t *m
     a.r1 = reinterpret_cast<float *>(base + kNaR1);
     a.s0 = reinterpret_cast<float *>(base + kNaS0);
     a.s1 = reinterpret_cast<float *>(base + kNaS1);
+    LlBuffers &ll = g_noalloc_ll[dev];
+    ll.r = reinterpret_cast<unsigned long long *>(base + kNaLlR);
+    ll.s = reinterpret_cast<unsigned long long *>(base + kNaLlS);
+    ll.rec = reinterpret_cast<unsigned long long *>(base + kNaLlRec);
+    ll.words = kNoAllocMaxCells;
+    a.ll_r = ll.r;
+    a.ll_s = ll.s;
     a.partials = reinterpret_cast<double *>(base + kNaPartials);
     a.chunk_end = chunk_end;
     a.chunk_last_unit = chunk_last;
@@ -3279,9 +3310,21 @@ extern "C" fs_status fs_pcg_solve_device_noalloc(int ni, int nj, const int8_t *m
     a.mode = 0;
     cudaError_t e;
     int launched = 0, ti = 0, tj = 0;
+    // the kernel choice of fs_pcg_solve_device: resident tiles, else TMA
+    // tiles (their tensor maps are host structures that point into the fixed
+    // array and the caller's buffers), else the tiled / linear-index pair
+    TmaMaps maps;
     if (resident_tile_shape(ni, nj, &ti, &tj)) {
         a.mode = 2; // the linear-index kernel takes over when a unit row wraps
-        e = launch_pcg_resident(a, ti, tj, st);
+        e = launch_pcg_resident(a, ti, tj, st, &ll);
+        if (e == cudaSuccess) e = launch_pcg_linear_if_wrap(a, st);
+        launched = 2;
+    } else if (tma_tile_shape(ni, nj, &ti, &tj) &&
+               tma_maps(&maps, ni, nj, ti, tj, info, rhs_device, result_device, a.r0, a.r1, a.s0,
+                        a.s1) &&
+               tma_store_maps(&maps, ni, nj, ti, tj, a.r0, a.r1, a.s0, a.s1)) {
+        a.mode = 2;
+        e = launch_pcg_tma(a, maps, ti, tj, st);
         if (e == cudaSuccess) e = launch_pcg_linear_if_wrap(a, st);
         launched = 2;
     } else {

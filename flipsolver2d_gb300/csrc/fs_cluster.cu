@@ -42,6 +42,7 @@
 #include <vector>
 
 #include "fs_cluster.h"
+#include "fs_device.h"
 
 namespace cg = cooperative_groups;
 
@@ -422,8 +423,15 @@ k_pcg_cluster(const ClusterSystem *__restrict__ systems, ClusterParams P)
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-static int g_cl_max_cluster = -1;
-static size_t g_cl_smem_limit = 0;
+// per device: the largest cluster it co-schedules with full-size CTAs and
+// the opt-in shared memory per CTA (-1: not yet probed).  Function
+// attributes belong to a device's context, so they are set once per device.
+struct ClDevice {
+    int max_cluster = -1;
+    size_t smem_limit = 0;
+};
+static std::mutex g_cl_mu;
+static ClDevice g_cl[kMaxDevices];
 
 template <int K> static void cl_set_attributes(int optin)
 {
@@ -432,22 +440,20 @@ template <int K> static void cl_set_attributes(int optin)
     cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
 }
 
-// the largest cluster the device co-schedules with full-size CTAs
-static void cl_init()
+static ClDevice cl_probe(int dev)
 {
-    if (g_cl_max_cluster >= 0) return;
-    int dev = 0, optin = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+    ClDevice d;
+    int optin = 0;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
         cudaGetLastError();
-        g_cl_max_cluster = 0;
-        return;
+        d.max_cluster = 0;
+        return d;
     }
-    g_cl_smem_limit = (size_t)optin;
+    d.smem_limit = (size_t)optin;
     cl_set_attributes<8>(optin);
     cl_set_attributes<16>(optin);
     cl_set_attributes<32>(optin);
-    g_cl_max_cluster = 1;
+    d.max_cluster = 1;
     for (int C = 16; C >= 2; C /= 2) {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(C);
@@ -463,11 +469,26 @@ static void cl_init()
         int nc = 0;
         if (cudaOccupancyMaxActiveClusters(&nc, (const void *)k_pcg_cluster<32>, &cfg) == cudaSuccess &&
             nc > 0) {
-            g_cl_max_cluster = C;
+            d.max_cluster = C;
             break;
         }
         cudaGetLastError();
     }
+    return d;
+}
+
+// the current device's cluster facts, probed on first use there
+static ClDevice cl_init()
+{
+    const int dev = current_device();
+    if (dev < 0) {
+        cudaGetLastError();
+        return ClDevice{0, 0};
+    }
+    if (dev >= kMaxDevices) return cl_probe(dev);
+    std::lock_guard<std::mutex> lock(g_cl_mu);
+    if (g_cl[dev].max_cluster < 0) g_cl[dev] = cl_probe(dev);
+    return g_cl[dev];
 }
 
 // Rows split over C CTAs at floor(k ni / C), so every CTA has at most
@@ -501,8 +522,8 @@ static std::map<std::pair<int, int>, ClusterPlan> g_tuned;
 
 bool cluster_plan(int ni, int nj, ClusterPlan *plan)
 {
-    cl_init();
-    if (g_cl_max_cluster <= 0 || ni < 1 || nj < 1) return false;
+    const ClDevice D = cl_init();
+    if (D.max_cluster <= 0 || ni < 1 || nj < 1) return false;
     {
         std::lock_guard<std::mutex> lock(g_tuned_mu);
         auto it = g_tuned.find({ni, nj});
@@ -511,16 +532,16 @@ bool cluster_plan(int ni, int nj, ClusterPlan *plan)
             return true;
         }
     }
-    return cl_plan(ni, nj, g_cl_max_cluster, g_cl_smem_limit, plan);
+    return cl_plan(ni, nj, D.max_cluster, D.smem_limit, plan);
 }
 
 void cluster_candidates(int ni, int nj, std::vector<ClusterPlan> *out)
 {
-    cl_init();
+    const ClDevice D = cl_init();
     out->clear();
-    for (int C = 1; C <= g_cl_max_cluster; C *= 2) {
+    for (int C = 1; C <= D.max_cluster; C *= 2) {
         ClusterPlan p;
-        if (cl_plan_c(ni, nj, C, g_cl_smem_limit, &p)) out->push_back(p);
+        if (cl_plan_c(ni, nj, C, D.smem_limit, &p)) out->push_back(p);
     }
 }
 
@@ -532,8 +553,8 @@ void cluster_set_tuned(int ni, int nj, const ClusterPlan &plan)
 
 long long cluster_max_cells()
 {
-    cl_init();
-    return g_cl_max_cluster > 0 ? (long long)g_cl_max_cluster * kClMaxOwn : 0;
+    const ClDevice D = cl_init();
+    return D.max_cluster > 0 ? (long long)D.max_cluster * kClMaxOwn : 0;
 }
 
 template <int K>
@@ -559,9 +580,9 @@ static cudaError_t launch_k(const ClusterSystem *systems_dev, int n, int C, size
 cudaError_t launch_pcg_cluster(const ClusterSystem *systems_dev, int n, const ClusterPlan &plan,
                                const ClusterParams &p, cudaStream_t st)
 {
-    cl_init();
+    const ClDevice D = cl_init();
     if (n <= 0) return cudaSuccess;
-    if (plan.C < 1 || plan.C > g_cl_max_cluster || plan.smem > g_cl_smem_limit) return cudaErrorInvalidValue;
+    if (plan.C < 1 || plan.C > D.max_cluster || plan.smem > D.smem_limit) return cudaErrorInvalidValue;
     switch (plan.K) {
     case 8: return launch_k<8>(systems_dev, n, plan.C, plan.smem, p, st);
     case 16: return launch_k<16>(systems_dev, n, plan.C, plan.smem, p, st);

@@ -17,6 +17,7 @@
 #include <cfloat>
 #include <climits>
 
+#include "fs_device.h"
 #include "fs_state.h"
 
 namespace fsg {
@@ -896,13 +897,7 @@ __global__ void __launch_bounds__(1024, 1) k_levelset_pass(GridDims d, float *__
 // layers' time) runs its tiles in ceil(tiles / SMs) waves
 static bool ls_wide(const GridDims &d)
 {
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
-            sms = 1;
-    }
+    const int sms = device_sm_count();
     auto cost = [&](int T, int H) {
         const long long tiles = (long long)nblk(d.ni, T) * nblk(d.nj, T);
         return (double)((tiles + sms - 1) / sms) * (H + 5) / H;

@@ -30,6 +30,7 @@
 #include <cstdio>
 #include <cuda/atomic>
 
+#include "fs_device.h"
 #include "fs_pcg.h"
 
 namespace fsg {
@@ -819,28 +820,18 @@ static TileShape tile_shape(int ni, int nj, int blocks)
     }
 }
 
-static int occupancy_grid(const void *fn, int threads, int max_per_sm)
+// resident blocks of the linear-index kernel on the current device
+template <typename T> static int linear_grid()
 {
-    int dev = 0, sms = 0, per = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, threads, 0);
-    if (per < 1) per = 1;
-    if (per > max_per_sm) per = max_per_sm;
-    return sms * per;
+    static std::atomic<int> slots[kMaxDevices];
+    return device_cached(slots, [] { return occupancy_grid((const void *)k_pcg<T>, kPcgThreads, 64); });
 }
 
 // largest grid any PCG launch may use (sizes the partial-sum buffer)
 template <typename T> int pcg_grid_size(long long N)
 {
-    static int lin = 0, sms = 0;
-    if (!lin) lin = occupancy_grid((const void *)k_pcg<T>, kPcgThreads, 64);
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    }
     (void)N;
+    const int lin = linear_grid<T>(), sms = device_sm_count();
     return lin > sms ? lin : sms;
 }
 
@@ -855,8 +846,7 @@ static cudaError_t coop(const void *fn, PcgArgs<T> args, int grid, int threads, 
 
 template <typename T> cudaError_t launch_pcg(const PcgArgs<T> &a, cudaStream_t st, int *launched)
 {
-    static int lin = 0;
-    if (!lin) lin = occupancy_grid((const void *)k_pcg<T>, kPcgThreads, 64);
+    const int lin = linear_grid<T>();
     long long want = (a.N + kPcgThreads * 4 - 1) / (kPcgThreads * 4);
     int glin = (int)(want < 1 ? 1 : (want < lin ? want : lin));
     if (sizeof(T) == 8) {
@@ -865,14 +855,14 @@ template <typename T> cudaError_t launch_pcg(const PcgArgs<T> &a, cudaStream_t s
         *launched = 1;
         return coop((const void *)k_pcg<T>, b, glin, kPcgThreads, st);
     }
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int sms = device_sm_count();
+    {
+        // a function attribute belongs to the current device's context
         const TileShape big{kMaxTileCells / 128, 128};
-        cudaFuncSetAttribute((const void *)k_pcg_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)tiled_smem(big));
+        cudaError_t e = cudaFuncSetAttribute((const void *)k_pcg_tiled,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)tiled_smem(big));
+        if (e != cudaSuccess) return e;
     }
     const TileShape ts = tile_shape(a.ni, a.nj, sms);
     const long long ntiles = (long long)((a.ni + ts.ti - 1) / ts.ti) * ((a.nj + ts.tj - 1) / ts.tj);
@@ -900,8 +890,7 @@ template <typename T> cudaError_t launch_pcg(const PcgArgs<T> &a, cudaStream_t s
 // rows on the j edges (the TMA kernel runs otherwise)
 cudaError_t launch_pcg_linear_if_wrap(const PcgArgs<float> &a, cudaStream_t st)
 {
-    static int lin = 0;
-    if (!lin) lin = occupancy_grid((const void *)k_pcg<float>, kPcgThreads, 64);
+    const int lin = linear_grid<float>();
     long long want = (a.N + kPcgThreads * 4 - 1) / (kPcgThreads * 4);
     int glin = (int)(want < 1 ? 1 : (want < lin ? want : lin));
     PcgArgs<float> b = a;

@@ -21,7 +21,13 @@ template <typename T> struct PcgArgs {
     const T *b;                // right-hand side
     T *x;                      // solution
     T *r0, *r1, *s0, *s1;      // ping-pong work vectors
-    double *partials;          // 8 * grid + 16 doubles (per-block partials, epoch flags)
+    // The resident kernel's exchange words (fs_pcg_tma.cu): N 8-byte words
+    // each for r and s, a float and the epoch that published it, and the
+    // first epoch of this launch (set by launch_pcg_resident)
+    unsigned long long *ll_r, *ll_s;
+    unsigned long long *ll_rec; // per-block partial records of its reductions
+    unsigned ll_base;
+    double *partials;          // 8 * grid + 16 doubles (per-block partial records)
     const int *chunk_end;      // splitRange chunk ends (exclusive)
     const int *chunk_last_unit;// last unit row per chunk or -1
     double *chunk_val;         // per chunk |r| at its last unit row (scratch)
@@ -37,6 +43,21 @@ template <typename T> struct PcgArgs {
                                // the j = 0 or j = NJ-1 edge (linear-index wrap)
     int mode;                  // 0 run, 1 run only if *wrap_flag, 2 only if !*wrap_flag
 };
+
+// Owner of a set of exchange-word buffers (a solver handle, the per-device
+// cache of the standalone solves, the fixed scratch of the no-allocation
+// solve).  Epochs grow across the launches that share the buffers, so words
+// left by an earlier launch never match; the buffers are cleared on first use
+// and when the epochs would wrap.
+struct LlBuffers {
+    unsigned long long *r = nullptr, *s = nullptr; // `words` words each
+    unsigned long long *rec = nullptr;             // kLlRecWords words
+    size_t words = 0;
+    unsigned next = 0; // first epoch of the next launch; 0: clear first
+};
+// the partial records: two sets of at most 256 blocks (the resident kernel's
+// tile limit) of four words
+constexpr size_t kLlRecWords = 2 * 256 * 4;
 
 template <typename T> int pcg_grid_size(long long N);
 // Runs the solve: FP32 uses the shared-memory tiled kernel, falling back to

@@ -26,6 +26,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include "fs_device.h"
 #include "fs_pcg.h"
 #include "fs_pcg_tma.h"
 
@@ -250,7 +251,8 @@ __device__ __forceinline__ bool gsync(GridBarrier *gb, unsigned nblocks, int *st
 // stopping test: the value of a chunk is |r| at its last nonzero entry.  The
 // owner tile of each chunk's last unit row stored |r| there in chunk_val (or
 // -1 when it is zero, then the chunk is scanned backwards here).
-__device__ __forceinline__ bool chunk_converged(const PcgArgs<float> &a, const float *rn,
+template <typename Load>
+__device__ __forceinline__ bool chunk_converged(const PcgArgs<float> &a, Load rn,
                                                 const TolTest &tt, int *s_flag)
 {
     __shared__ float s_mx[32];
@@ -269,10 +271,9 @@ __device__ __forceinline__ bool chunk_converged(const PcgArgs<float> &a, const f
         }
         float v = __ldcg(cv + k);
         if (v < 0.f) {
-            const long long idx = warp_last_nonzero(start, (long long)last - 1,
-                                                    [&](long long e) { return __ldcg(rn + e); });
+            const long long idx = warp_last_nonzero(start, (long long)last - 1, rn);
             if (idx >= start) {
-                v = fabsf(__ldcg(rn + idx));
+                v = fabsf(rn(idx));
             } else {
                 has_min = 1;
                 v = 0.f;
@@ -605,7 +606,7 @@ k_pcg_tma(PcgArgs<float> a, const __grid_constant__ TmaMaps m, int ti, int tj)
         if (!gsync(a.bar, G, a.status)) return;
         const float *rn = (it & 1) ? a.r0 : a.r1;
         const float2 newSigma = psum(pB, G, sm);
-        if (chunk_converged(a, rn, tt, &s_flag)) {
+        if (chunk_converged(a, [&](long long e) { return __ldcg(rn + e); }, tt, &s_flag)) {
             result = it;
             break;
         }
@@ -697,12 +698,48 @@ __device__ __forceinline__ void load_ring(float *dst, const float *__restrict__ 
     }
 }
 
-// byte offset of the per-block epoch flags inside the partials buffer of the
-// resident kernel: after G float4 records and G float2 pairs, 32-byte aligned
-__host__ __device__ inline size_t res_flags_offset(int G)
+// ---------------------------------------------------------------------------
+// Exchange words.  The resident kernel moves everything another block reads
+// -- the per-block partials of the two grid reductions and the 2-cell bands
+// along tile borders -- as 8-byte words that hold a 32-bit payload and the
+// epoch that published it.  An aligned 8-byte access is single-copy atomic,
+// so a reader that sees the epoch it expects also sees that epoch's payload:
+// no fence, no separate flag and no counter round trip is needed.  Epochs
+// only grow across the launches that share a buffer (the host hands each
+// launch a fresh range), so a word left by an earlier launch never matches.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long ll_pack(unsigned payload, unsigned epoch)
 {
-    return ((size_t)G * 24 + 31) & ~(size_t)31;
+    return ((unsigned long long)epoch << 32) | payload;
 }
+__device__ __forceinline__ unsigned ll_epoch(unsigned long long w) { return (unsigned)(w >> 32); }
+__device__ __forceinline__ void st_ll(unsigned long long *p, unsigned long long w)
+{
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(w) : "memory");
+}
+__device__ __forceinline__ void st_ll2(unsigned long long *p, unsigned long long a, unsigned long long b)
+{
+    asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p), "l"(a), "l"(b) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_ll(const unsigned long long *p)
+{
+    unsigned long long w;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(w) : "l"(p) : "memory");
+    return w;
+}
+__device__ __forceinline__ void ld_ll2(const unsigned long long *p, unsigned long long &a,
+                                       unsigned long long &b)
+{
+    asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(a), "=l"(b) : "l"(p) : "memory");
+}
+
+// words of one block's partial record: hi, lo of a float-pair sum, then a
+// word whose low 31 bits are a non-negative float (a max) and whose top bit
+// is a flag (an OR), then one unused word -- 32 bytes, one sector
+constexpr int kRecWords = 4;
+
+// reduction k of a launch uses set k & 1 of two sets of G records
+static_assert(kRecWords * 2 * 256 == kLlRecWords, "record buffer");
 
 // float-pair accumulation without renormalising: hi carries the running
 // sum, lo the rounding errors of the additions and the low parts
@@ -848,7 +885,7 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     extern __shared__ unsigned char smem_dyn[];
     __shared__ float smf[64];
     __shared__ float4 s_bcast;
-    __shared__ int s_flag;
+    __shared__ int s_flag, s_fail;
     __shared__ float inv[8];
     __shared__ int s_cmax, s_cscan;
     __shared__ int s_nown;           // chunks whose last unit row is in this tile
@@ -872,19 +909,17 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     unsigned *Op = reinterpret_cast<unsigned *>(base + L.off_op);
     const int NI = a.ni, NJ = a.nj;
     const int G = gridDim.x;
-    const int tiles_j = (NJ + tj - 1) / tj, tiles_i = (NI + ti - 1) / ti;
+    const int tiles_j = (NJ + tj - 1) / tj;
     const int ti0 = ((int)blockIdx.x / tiles_j) * ti, tj0 = ((int)blockIdx.x % tiles_j) * tj;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int w2 = L.w2, w1 = L.w1, h1 = L.h1;
-    // partials: z.r records (float4), then the s.As pairs (float2); the
-    // zero test of b uses the record area before the first iteration; then
-    // the epoch flags, one 32-byte sector per block (zeroed at launch)
-    float4 *pB = reinterpret_cast<float4 *>(a.partials);
-    float2 *pA = reinterpret_cast<float2 *>(pB + G), *pC = reinterpret_cast<float2 *>(pB);
-    unsigned *flags =
-        reinterpret_cast<unsigned *>(reinterpret_cast<unsigned char *>(a.partials) + res_flags_offset(G));
-    unsigned *count = &a.bar->count;
-    unsigned barriers = 0; // grid barriers arrived at so far
+    // partial records of the grid reductions (exchange words, two sets of G
+    // records); reduction k of this launch has epoch ep0 + 1 + k
+    unsigned long long *recs = a.ll_rec;
+    const unsigned ep0 = a.ll_base;
+    unsigned nred = 0;                // reductions published so far
+    unsigned *count = &a.bar->count;  // arrivals at the rare fenced barrier
+    unsigned nfenced = 0;
     // chunks without a unit row report DBL_MIN (VOps::maxAbs) on every iteration
     int has_min_static = 0;
     for (int k = 0; k < a.nchunks; k++) has_min_static |= a.chunk_last_unit[k] < 0;
@@ -896,70 +931,102 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     if (threadIdx.x < 8)
         inv[threadIdx.x] = (threadIdx.x >= 1 && threadIdx.x <= 4) ? (float)(1.0 / (threadIdx.x * scale_d)) : 0.f;
 
-    // thread 0, after the block barrier: publish an epoch (0: none) and
-    // arrive at the next grid barrier
-    auto arrive = [&](unsigned epoch) {
-        barriers++;
+    // thread 0, holding the block's partial (hi, lo) and the extra word:
+    // publish them as this block's record of the next reduction.  Every
+    // thread counts the reduction.
+    auto publish = [&](float2 part, unsigned extra) {
         if (threadIdx.x == 0) {
-            fence_acq_rel_gpu();
-            if (epoch) st_relaxed_u32(flags + 8 * blockIdx.x, epoch);
-            red_relaxed_add(count, 1u);
+            const unsigned ep = ep0 + 1 + nred;
+            unsigned long long *r = recs + ((size_t)(nred & 1) * G + blockIdx.x) * kRecWords;
+            st_ll2(r, ll_pack(__float_as_uint(part.x), ep), ll_pack(__float_as_uint(part.y), ep));
+            st_ll(r + 2, ll_pack(extra, ep));
         }
+        nred++;
     };
-    // completes the last grid barrier and sums the blocks' float2 partials
-    // (or float4 records: pair sum, max, max) in a fixed order, so every
-    // block obtains the same scalars; the result is in every thread
-    auto wait_sum = [&](const void *parts, bool rec4) -> float4 {
+    // completes the last reduction published: warp 0 gathers the G records
+    // (each lane's loads all in flight at once, then only the records not yet
+    // published are polled again) and sums them in a fixed order, so every
+    // block obtains the same scalars: (pair hi, lo, max, flag) in every
+    // thread.  s_fail, read after it, is block-uniform: 1 after a timeout.
+    auto wait_sum = [&]() -> float4 {
         if (warp == 0) {
-            bool ok = true;
-            if (lane == 0) ok = spin_until(count, barriers * (unsigned)G, a.status);
-            ok = __shfl_sync(0xffffffffu, ok, 0);
-            float2 acc = make_float2(0.f, 0.f);
-            float mx = 0.f, sc = 0.f;
-            if (ok) {
-                // all of a lane's loads are issued before any is consumed:
-                // one L2 round trip instead of one per partial (G <= 32 kPartRounds)
-                if (rec4) {
-                    float4 v[kPartRounds];
+            const unsigned k = nred - 1, ep = ep0 + nred;
+            const unsigned long long *base = recs + (size_t)(k & 1) * G * kRecWords;
+            unsigned long long w0[kPartRounds], w1[kPartRounds], w2[kPartRounds];
+            unsigned pending = 0;
 #pragma unroll
-                    for (int i = 0; i < kPartRounds; i++) {
-                        const int k = lane + 32 * i;
-                        v[i] = k < G ? __ldcg(reinterpret_cast<const float4 *>(parts) + k)
-                                     : make_float4(0.f, 0.f, 0.f, 0.f);
-                    }
-#pragma unroll
-                    for (int i = 0; i < kPartRounds; i++) {
-                        acc = ff_acc(acc, make_float2(v[i].x, v[i].y));
-                        mx = fmaxf(mx, v[i].z);
-                        sc = fmaxf(sc, v[i].w);
-                    }
+            for (int i = 0; i < kPartRounds; i++) {
+                const int b = lane + 32 * i;
+                if (b < G) {
+                    ld_ll2(base + (size_t)b * kRecWords, w0[i], w1[i]);
+                    w2[i] = ld_ll(base + (size_t)b * kRecWords + 2);
+                    if (ll_epoch(w0[i]) != ep || ll_epoch(w1[i]) != ep || ll_epoch(w2[i]) != ep)
+                        pending |= 1u << i;
                 } else {
-                    float2 v[kPartRounds];
-#pragma unroll
-                    for (int i = 0; i < kPartRounds; i++) {
-                        const int k = lane + 32 * i;
-                        v[i] = k < G ? __ldcg(reinterpret_cast<const float2 *>(parts) + k)
-                                     : make_float2(0.f, 0.f);
-                    }
-#pragma unroll
-                    for (int i = 0; i < kPartRounds; i++) acc = ff_acc(acc, v[i]);
+                    w0[i] = w1[i] = w2[i] = 0ull;
                 }
+            }
+            long long spins = 0;
+            bool failed = false;
+            while (pending) {
+                if (++spins > kSpinLimit || ((spins & 255) == 0 && *((volatile int *)a.status) != 0)) {
+                    atomicExch(a.status, 1);
+                    failed = true;
+                    break;
+                }
+#pragma unroll
+                for (int i = 0; i < kPartRounds; i++) {
+                    if (pending & (1u << i)) {
+                        const int b = lane + 32 * i;
+                        ld_ll2(base + (size_t)b * kRecWords, w0[i], w1[i]);
+                        w2[i] = ld_ll(base + (size_t)b * kRecWords + 2);
+                        if (ll_epoch(w0[i]) == ep && ll_epoch(w1[i]) == ep && ll_epoch(w2[i]) == ep)
+                            pending &= ~(1u << i);
+                    }
+                }
+            }
+            unsigned p0[kPartRounds], p1[kPartRounds], p2[kPartRounds];
+#pragma unroll
+            for (int i = 0; i < kPartRounds; i++) { p0[i] = (unsigned)w0[i]; p1[i] = (unsigned)w1[i]; p2[i] = (unsigned)w2[i]; }
+            float2 acc = make_float2(0.f, 0.f);
+            float mx = 0.f;
+            unsigned flag = 0;
+#pragma unroll
+            for (int i = 0; i < kPartRounds; i++) {
+                acc = ff_acc(acc, make_float2(__uint_as_float(p0[i]), __uint_as_float(p1[i])));
+                mx = fmaxf(mx, __uint_as_float(p2[i] & 0x7fffffffu));
+                flag |= p2[i] >> 31;
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 acc = ff_acc(acc, ff_shfl_down(acc, o));
                 mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
-                sc = fmaxf(sc, __shfl_down_sync(0xffffffffu, sc, o));
+                flag |= __shfl_down_sync(0xffffffffu, flag, o);
             }
+            failed = __any_sync(0xffffffffu, failed);
             if (lane == 0) {
                 acc = ff_norm(acc);
-                s_bcast = make_float4(acc.x, acc.y, mx, sc);
+                s_bcast = make_float4(acc.x, acc.y, mx, flag ? 1.f : 0.f);
+                s_fail = (failed || *((volatile int *)a.status) != 0) ? 1 : 0;
             }
         }
         __syncthreads();
         return s_bcast;
     };
-    auto ok = [&]() { return *((volatile int *)a.status) == 0; };
+    // block-uniform: no wait of this launch has timed out (a block barrier)
+    auto ok = [&]() { return __syncthreads_or(*((volatile int *)a.status) != 0) == 0; };
+    // the rare full barrier with release / acquire semantics (the backward
+    // max-abs scan reads r anywhere and the chunk-end values of all tiles)
+    auto fenced_barrier = [&]() -> bool {
+        __syncthreads();
+        nfenced++;
+        if (threadIdx.x == 0) {
+            fence_acq_rel_gpu();
+            red_relaxed_add(count, 1u);
+            spin_until(count, nfenced * (unsigned)G, a.status);
+        }
+        return ok();
+    };
 
     // load the operator rows (bytes, into B1 for now) and r_0 = s_0 = b with
     // their halo; x = 0
@@ -1006,40 +1073,43 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
                 ((unsigned)((Ib[c2 + w2] >> 4) & 7) << 11) |
                 ((unsigned)((Ib[c2 - 1] >> 4) & 7) << 14) | ((unsigned)((Ib[c2 + 1] >> 4) & 7) << 17);
     }
-    float sigma_hi, sigma_lo;
+    float2 sigma;
     bool zero;
     {
         const float2 part = bsum0(bb, smf); // its block barrier also retires Ib
         const int anynz = __syncthreads_or(nz);
-        if (threadIdx.x == 0) {
-            pA[blockIdx.x] = part;
-            pC[blockIdx.x] = make_float2(anynz ? 1.f : 0.f, 0.f);
-        }
-        __syncthreads();
-        arrive(0u);
-        const float4 s0 = wait_sum(pA, false);
-        if (!ok()) return;
-        sigma_hi = s0.x;
-        sigma_lo = s0.y;
-        __syncthreads(); // everyone has read the broadcast slot
-        zero = wait_sum(pC, false).x == 0.f; // same barrier, already complete
+        publish(part, anynz ? 0x80000000u : 0u); // the flag: b has a nonzero
+        const float4 s0 = wait_sum();
+        if (s_fail) return;
+        sigma = make_float2(s0.x, s0.y);
+        zero = s0.w == 0.f;
     }
-    float2 sigma = make_float2(sigma_hi, sigma_lo);
 
-    // neighbour tiles whose cells the 2-deep ring reads: threads 0..nn-1
-    // each watch one of them (at most 5 rows x 3 columns of tiles)
-    const int bi_lo = ti0 - 2 < 0 ? 0 : (ti0 - 2) / ti;
-    const int bi_hi = min(tiles_i - 1, (ti0 + ti + 1) / ti);
-    const int bj_lo = tj0 - 2 < 0 ? 0 : (tj0 - 2) / tj;
-    const int bj_hi = min(tiles_j - 1, (tj0 + tj + 1) / tj);
-    const int ncols = bj_hi - bj_lo + 1;
-    const int nn = (bi_hi - bi_lo + 1) * ncols;
-    const unsigned *watch = nullptr;
-    if ((int)threadIdx.x < nn)
-        watch = flags + 8 * ((bi_lo + (int)threadIdx.x / ncols) * tiles_j + bj_lo + (int)threadIdx.x % ncols);
-    auto wait_neighbours = [&](unsigned epoch) -> bool {
-        if (watch) spin_until(watch, epoch, a.status);
-        __syncthreads();
+    // the neighbours' values on the 2-deep ring around the tile, from their
+    // exchange words of epoch ep (bounded polls); a block barrier, then a
+    // block-uniform false on timeout
+    auto load_ring_ll = [&](float *dst, const unsigned long long *src, unsigned ep) -> bool {
+        const int n = 4 * w2 + 4 * ti;
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
+            int r, q;
+            ring_cell(k, ti, tj, r, q);
+            const int gi = ti0 + r, gj = tj0 + q;
+            float v = 0.f;
+            if (gi >= 0 && gi < NI && gj >= 0 && gj < NJ) {
+                const unsigned long long *p = src + (size_t)gi * NJ + gj;
+                unsigned long long w = ld_ll(p);
+                long long spins = 0;
+                while (ll_epoch(w) != ep) {
+                    if (++spins > kSpinLimit || ((spins & 255) == 0 && *((volatile int *)a.status) != 0)) {
+                        atomicExch(a.status, 1);
+                        break;
+                    }
+                    w = ld_ll(p);
+                }
+                v = __uint_as_float((unsigned)w);
+            }
+            dst[(r + 2) * w2 + (q + 2)] = v;
+        }
         return ok();
     };
 
@@ -1087,13 +1157,16 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
         const int tr = row0 + rr - 1;
         return col_band || tr < 2 || tr >= ti - 2;
     };
-    auto publish_tile_r = [&](float *dst) {
+    // all of the tile's r (in Rb) as exchange words of epoch ep
+    auto publish_tile_r = [&](unsigned ep) {
         for (int r = warp; r < ti; r += nw) {
             const int gi = ti0 + r;
             if (gi >= NI) break;
             for (int q = lane; q < tj; q += 32) {
                 const int gj = tj0 + q;
-                if (gj < NJ) dst[(size_t)gi * NJ + gj] = Rb[(r + 2) * w2 + (q + 2)];
+                if (gj < NJ)
+                    st_ll(a.ll_r + (size_t)gi * NJ + gj,
+                          ll_pack(__float_as_uint(Rb[(r + 2) * w2 + (q + 2)]), ep));
             }
         }
     };
@@ -1114,8 +1187,8 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     int result = zero ? 0 : a.iter_limit;
     for (int it = 0; !zero && a.iter_limit > 0; it++) {
         const bool first = it == 0;
-        float *s_pub = (it & 1) ? a.s1 : a.s0; // s_it published here
-        float *r_pub = (it & 1) ? a.r0 : a.r1; // r_{it+1} published here
+        const unsigned ep_s = ep0 + 2u * it + 1u; // epoch of s_it's exchange words
+        const unsigned ep_r = ep0 + 2u * it + 2u; // epoch of r_{it+1}'s
 
         // ---- sweep 1 -------------------------------------------------------
         if (!first) {
@@ -1123,9 +1196,7 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
             if (more) {
                 // z_it = M r_it on the tile and its 1-halo while the grid
                 // barrier of the last sweep completes
-                if (!wait_neighbours(2u * it)) return;
-                load_ring(Rb, (it & 1) ? a.r1 : a.r0, ti0, tj0, ti, tj, NI, NJ);
-                __syncthreads();
+                if (!load_ring_ll(Rb, a.ll_r, ep0 + 2u * it)) return;
                 if constexpr (RPS > 0) {
                     refresh_ring_row(Rr, Rb);
                     // z on the tile rows came with the last sweep's z.r (step F);
@@ -1147,23 +1218,24 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
                 }
             }
             // end of iteration it - 1: beta and the stopping test
-            const float4 rec = wait_sum(pB, true);
-            if (!ok()) return;
+            const float4 rec = wait_sum();
+            if (s_fail) return;
             const float2 newSigma = make_float2(rec.x, rec.y);
             // a zero at a chunk-end unit row needs the backward scan; otherwise
             // the largest |r| over the blocks decides
-            if (RPS > 0 && rec.w != 0.f) {
+            if (rec.w != 0.f) {
                 // the scan reads r anywhere in a chunk: every tile publishes
-                // all of r_it (still intact in Rb) and the grid waits for it
-                publish_tile_r((it & 1) ? a.r1 : a.r0);
-                __syncthreads();
-                arrive(0u);
-                wait_sum(pA, false); // completes the barrier (the sum is unused)
-                if (!ok()) return;
+                // all of r_it (still intact in Rb) and the grid meets at a
+                // fenced barrier
+                publish_tile_r(ep0 + 2u * it);
+                if (!fenced_barrier()) return;
             }
-            const bool done = rec.w != 0.f
-                                  ? chunk_converged(a, (it & 1) ? a.r1 : a.r0, tt, &s_flag)
-                                  : tol_met(tt, rec.z, has_min_static);
+            const bool done =
+                rec.w != 0.f
+                    ? chunk_converged(
+                          a, [&](long long e) { return __uint_as_float((unsigned)__ldcg(a.ll_r + e)); },
+                          tt, &s_flag)
+                    : tol_met(tt, rec.z, has_min_static);
             if (done) {
                 result = it - 1;
                 break;
@@ -1219,7 +1291,7 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
                 for (int rr = 0; rr < kR; rr++) {
                     const int gi = ti0 + row0 + rr - 1;
                     if (on_tile(rr) && in_band(rr) && gi < NI)
-                        s_pub[(size_t)gi * NJ + gj] = Sb[cbase + rr * w2];
+                        st_ll(a.ll_s + (size_t)gi * NJ + gj, ll_pack(__float_as_uint(Sb[cbase + rr * w2]), ep_s));
                 }
             }
         } else {
@@ -1232,7 +1304,8 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
                     qs = fmaf(apply_a(Op[c1], B1, c1, w1), s_c, qs);
                     if (!first) {
                         Sb[(r + 2) * w2 + (q + 2)] = s_c;
-                        if (gi < NI && gj < NJ) s_pub[(size_t)gi * NJ + gj] = s_c;
+                        if (gi < NI && gj < NJ)
+                            st_ll(a.ll_s + (size_t)gi * NJ + gj, ll_pack(__float_as_uint(s_c), ep_s));
                     }
                 }
             }
@@ -1240,20 +1313,14 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
         {
             const float2 part = bsum0(qs, smf);
             if (threadIdx.x == 0) {
-                pA[blockIdx.x] = part;
                 s_cmax = 0;
                 s_cscan = 0;
             }
+            publish(part, 0u);
         }
-        __syncthreads();
-        arrive(first ? 0u : 2u * it + 1u);
 
         // ---- sweep 2 -------------------------------------------------------
-        if (!first) {
-            if (!wait_neighbours(2u * it + 1u)) return;
-            load_ring(Sb, s_pub, ti0, tj0, ti, tj, NI, NJ); // neighbours' s_it
-            __syncthreads();
-        }
+        if (!first && !load_ring_ll(Sb, a.ll_s, ep_s)) return; // neighbours' s_it
         // A s_it on the tile and its 1-halo while the grid barrier completes
         if constexpr (RPS > 0) {
             // the tile rows' A s came with s.As (step C); the 1-halo rows read
@@ -1267,8 +1334,8 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
                 B1[r * w1 + q] = apply_a(Op[r * w1 + q], Sb, (r + 1) * w2 + (q + 1), w2);
             });
         }
-        const float4 qsum = wait_sum(pA, false);
-        if (!ok()) return;
+        const float4 qsum = wait_sum();
+        if (s_fail) return;
         const float fa = ff_div(sigma, ff_add(make_float2(qsum.x, qsum.y), eps8));
         // r_{it+1} = r_it - alpha A s_it (and x += alpha s_it on the tile)
         if constexpr (RPS > 0) {
@@ -1311,7 +1378,8 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
 #pragma unroll
                 for (int rr = 0; rr < kR; rr++) {
                     const int gi = ti0 + row0 + rr - 1;
-                    if (on_tile(rr) && in_band(rr) && gi < NI) r_pub[(size_t)gi * NJ + gj] = Rr[rr];
+                    if (on_tile(rr) && in_band(rr) && gi < NI)
+                        st_ll(a.ll_r + (size_t)gi * NJ + gj, ll_pack(__float_as_uint(Rr[rr]), ep_r));
                 }
             }
         } else {
@@ -1325,7 +1393,8 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
                     zr = fmaf(precond(Op[c1], B1, c1, w1), r_c, zr);
                     Xt[r * tj + q] = fmaf(Sb[c2], fa, Xt[r * tj + q]);
                     Rb[c2] = r_c;
-                    if (gi < NI && gj < NJ) r_pub[(size_t)gi * NJ + gj] = r_c;
+                    if (gi < NI && gj < NJ)
+                        st_ll(a.ll_r + (size_t)gi * NJ + gj, ll_pack(__float_as_uint(r_c), ep_r));
                 }
             }
         }
@@ -1350,11 +1419,8 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
         }
         {
             const float2 part = bsum0(zr, smf); // its barrier also orders s_cmax / s_cscan
-            if (threadIdx.x == 0)
-                pB[blockIdx.x] = make_float4(part.x, part.y, __int_as_float(s_cmax), s_cscan ? 1.f : 0.f);
+            publish(part, (unsigned)s_cmax | (s_cscan ? 0x80000000u : 0u));
         }
-        __syncthreads();
-        arrive(2u * it + 2u);
     }
     // the solution leaves shared memory once
     for (int r = warp; r < ti; r += nw) {
@@ -1371,19 +1437,20 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
+// the driver's tensor-map encoder (one process-wide entry point; the
+// initialisation of a function-local static is thread-safe)
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
 {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    static bool tried = false;
-    if (!tried) {
-        tried = true;
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
         void *p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
                                              &q) == cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    }
+            return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        cudaGetLastError();
+        return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+    }();
     return fn;
 }
 
@@ -1402,13 +1469,7 @@ static bool encode(CUtensorMap *map, const void *ptr, CUtensorMapDataType dt, in
            CUDA_SUCCESS;
 }
 
-static int sm_count()
-{
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    return sms > 0 ? sms : 1;
-}
+static int sm_count() { return device_sm_count(); }
 
 constexpr int kMaxTmaCells = 54 * 128;
 
@@ -1527,13 +1588,37 @@ static cudaError_t launch_resident_rps(const PcgArgs<float> &a, int ti, int tj, 
                                        dim3(RPS > 0 ? kStripThreads : kThreads), kargs, smem, st);
 }
 
-cudaError_t launch_pcg_resident(const PcgArgs<float> &a, int ti, int tj, cudaStream_t st)
+cudaError_t launch_pcg_resident(const PcgArgs<float> &a0, int ti, int tj, cudaStream_t st,
+                                LlBuffers *ll)
 {
-    const int grid = ((a.ni + ti - 1) / ti) * ((a.nj + tj - 1) / tj);
-    cudaError_t e = cudaMemsetAsync(a.bar, 0, sizeof(GridBarrier), st);
+    const int grid = ((a0.ni + ti - 1) / ti) * ((a0.nj + tj - 1) / tj);
+    if (!ll || !ll->r || !ll->s || !ll->rec || ll->words < (size_t)a0.N || grid > 256)
+        return cudaErrorInvalidValue;
+    // epochs one launch may use: 1 + 2 per iteration for the reductions and
+    // 2 per iteration for the ring words, with slack
+    const unsigned long long span = 2ull * (unsigned long long)(a0.iter_limit > 0 ? a0.iter_limit : 0) + 8ull;
+    if (span > (1ull << 30)) return cudaErrorInvalidValue;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(st, &cs);
     if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(reinterpret_cast<unsigned char *>(a.partials) + res_flags_offset(grid), 0,
-                        (size_t)grid * 32, st);
+    // a captured launch replays with the same epochs, so it clears the
+    // buffers inside the capture every time and leaves them to be cleared
+    // again before the next launch outside it
+    const bool capturing = cs != cudaStreamCaptureStatusNone;
+    if (capturing || ll->next == 0 || (unsigned long long)ll->next + span > 0xfffffff0ull) {
+        e = cudaMemsetAsync(ll->r, 0, ll->words * sizeof(unsigned long long), st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(ll->s, 0, ll->words * sizeof(unsigned long long), st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(ll->rec, 0, kLlRecWords * sizeof(unsigned long long), st);
+        if (e != cudaSuccess) return e;
+        ll->next = 1;
+    }
+    PcgArgs<float> a = a0;
+    a.ll_r = ll->r;
+    a.ll_s = ll->s;
+    a.ll_rec = ll->rec;
+    a.ll_base = ll->next;
+    ll->next = capturing ? 0u : (unsigned)(ll->next + span);
+    e = cudaMemsetAsync(a.bar, 0, sizeof(GridBarrier), st);
     if (e != cudaSuccess) return e;
     switch (strip_rows(ti, tj)) {
     case 1: return launch_resident_rps<1>(a, ti, tj, grid, st);

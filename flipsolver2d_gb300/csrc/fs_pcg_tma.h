@@ -27,6 +27,9 @@ cudaError_t launch_pcg_tma(const PcgArgs<float> &a, const TmaMaps &maps, int ti,
 // one tile per block resident in shared memory for the whole solve; false
 // when the grid needs more tiles than there are SMs
 bool resident_tile_shape(int ni, int nj, int *ti, int *tj);
-cudaError_t launch_pcg_resident(const PcgArgs<float> &a, int ti, int tj, cudaStream_t st);
+// The shared-memory-resident FP32 solve; `ll` owns the exchange-word buffers
+// (a.ll_r / a.ll_s are taken from it) and their epoch counter.
+cudaError_t launch_pcg_resident(const PcgArgs<float> &a, int ti, int tj, cudaStream_t st,
+                                LlBuffers *ll);
 
 } // namespace fsg

@@ -28,6 +28,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "fs_device.h"
 #include "fs_pcg.h"
 #include "fs_spec.h"
 
@@ -385,15 +386,8 @@ __global__ void __launch_bounds__(kSpecThreads, 2) k_pcg_spec(SpecArgs a)
 
 static int spec_grid()
 {
-    static int grid = 0;
-    if (!grid) {
-        int dev = 0, sms = 0, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void *)k_pcg_spec, kSpecThreads, 0);
-        grid = sms * (per > 0 ? per : 1);
-    }
-    return grid;
+    static std::atomic<int> slots[kMaxDevices];
+    return device_cached(slots, [] { return occupancy_grid((const void *)k_pcg_spec, kSpecThreads, 1 << 30); });
 }
 
 int spec_partials_needed() { return 3 * spec_grid() + 8; }

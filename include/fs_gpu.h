@@ -386,7 +386,9 @@ fs_status fs_cluster_autotune(int ni, int nj, int objective, int device, int *cl
  * larger requests fail with FS_ERR_BAD_ARG before any device work, and
  * pcg_precision FS_PCG_FP64 fails with FS_ERR_UNSUPPORTED.
  * The first call on a device looks up the scratch array's address on that
- * device; make that first call before any stream capture begins.  All calls
+ * device; make that first call before any stream capture begins.  The address
+ * is kept for the life of the process: calls after a reset of that device
+ * (cudaDeviceReset) are not supported.  All calls
  * share the array and it keeps what the last call left in it (each call
  * clears what must start at zero).  Calls that overlapped on the GPU would
  * race on it: the function holds a process-wide lock, runs on the legacy

@@ -16,9 +16,14 @@
  * `ref_threads` chunks exactly as ThreadPool::splitRange does
  * (threadpool.cpp:41-76), independent of the host thread count.
  *
- * Not restated: sources/emitters (reseeding with the RNG after frame 0),
- * viscosity, and the smoke/fire/NB-FLIP solvers -- the scenes this oracle runs
- * have none of them.
+ * Restated: the FLIP step (FlipSolver, flipsolver2d.cpp) and the narrow-band
+ * step (NBFlipSolver, nbflipsolver.cpp) with its std::mt19937 draws, the
+ * sources/emitters of both (addSource, updateSources, reseedParticles,
+ * updateGridFromSources), and the FP64 spec-mode solve fso_spec_solve (a plain
+ * double-precision PCG with the textbook incomplete-Poisson preconditioner,
+ * inversepoissonpreconditioner.h:45-79).
+ * Not restated: viscosity (viscositymodel.cpp, whose solves are Eigen's
+ * conjugate gradient) and the smoke and fire solvers.
  */
 #define _GNU_SOURCE
 #include "fsoracle.h"
@@ -29,6 +34,7 @@
 #include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
+#include <sys/sysinfo.h>
 
 /* material codes, materialgrid.h:6-13 */
 enum { M_FLUID = 0x40, M_SOURCE = 0x41, M_SOLID = 0x20, M_SINK = 0x12, M_EMPTY = 0x10 };
@@ -2153,7 +2159,7 @@ int fso_pcg_solve(int ni, int nj, const int8_t *material, float dt, double densi
  * (c, n) for the lower fluid neighbours n = c - NJ (mask bit 1) and
  * n = c - 1 (mask bit 4) of a unit row c.  This plain double-precision PCG
  * with M and a true relative-residual stopping test is the FP64 oracle of
- * the GPU's mixed-precision spec solve.  Serial and deterministic. */
+ * the GPU's mixed-precision spec solve.  Deterministic for any thread count. */
 /* K(c, n) for a strictly lower neighbour n of unit row c:
  * -A(c, n) / A(n, n) = scale / A(n, n), with Eigen's rule that a zero
  * diagonal counts as 1; a non-unit row of A is an identity row. */
@@ -2163,40 +2169,111 @@ static double spec_k(const fso_solver *s, long n)
     return s->mscale;
 }
 
-static void spec_apply_m(const fso_solver *s, const double *r, double *y, double *z)
+/* The loops below run on the solver's pool (FSO_HOST_THREADS threads).  Every
+ * cell is written by one thread, and the dot products sum SPEC_CHUNKS fixed
+ * chunks in chunk order, so the results do not depend on the thread count. */
+#define SPEC_CHUNKS 64
+
+typedef struct spec_ctx {
+    const fso_solver *s;
+    const double *in, *in2;
+    double *out, *out2;
+    double alpha;
+    long n;
+    double part[SPEC_CHUNKS];
+} spec_ctx;
+
+/* y = K^T r: row n of K^T collects K(c, n) over the unit rows c whose lower
+ * neighbour is n */
+static void spec_kt_range(void *ctx, size_t a, size_t b)
 {
+    spec_ctx *c = (spec_ctx *)ctx;
+    const fso_solver *s = c->s;
     const long N = (long)s->ncell, NJ = s->nj;
-    /* y = K^T r: row n of K^T collects K(c, n) over the unit rows c whose
-     * lower neighbour is n */
-    for (long n = 0; n < N; n++) {
+    const double *r = c->in;
+    for (long n = (long)a; n < (long)b; n++) {
         double v = r[n];
         const double k = spec_k(s, n);
         if (n + NJ < N && s->unit[n + NJ] && (s->mask[n + NJ] & 1)) v += k * r[n + NJ];
         if (n + 1 < N && s->unit[n + 1] && (s->mask[n + 1] & 4)) v += k * r[n + 1];
-        y[n] = v;
+        c->out[n] = v;
     }
-    /* z = K y */
-    for (long c = 0; c < N; c++) {
-        double v = y[c];
-        if (s->unit[c]) {
-            if ((s->mask[c] & 1) && c - NJ >= 0) v += spec_k(s, c - NJ) * y[c - NJ];
-            if ((s->mask[c] & 4) && c - 1 >= 0) v += spec_k(s, c - 1) * y[c - 1];
+}
+
+/* z = K y */
+static void spec_k_range(void *ctx, size_t a, size_t b)
+{
+    spec_ctx *c = (spec_ctx *)ctx;
+    const fso_solver *s = c->s;
+    const long NJ = s->nj;
+    const double *y = c->in;
+    for (long k = (long)a; k < (long)b; k++) {
+        double v = y[k];
+        if (s->unit[k]) {
+            if ((s->mask[k] & 1) && k - NJ >= 0) v += spec_k(s, k - NJ) * y[k - NJ];
+            if ((s->mask[k] & 4) && k - 1 >= 0) v += spec_k(s, k - 1) * y[k - 1];
         }
-        z[c] = v;
+        c->out[k] = v;
     }
+}
+
+static void spec_apply_m(const fso_solver *s, const double *r, double *y, double *z)
+{
+    spec_ctx c;
+    c.s = s;
+    c.in = r;
+    c.out = y;
+    par_for(s->pool, s->ncell, spec_kt_range, &c);
+    c.in = y;
+    c.out = z;
+    par_for(s->pool, s->ncell, spec_k_range, &c);
 }
 
 static void spec_apply_a(const fso_solver *s, const double *in, double *out)
 {
     mv_ctx c = {(fso_solver *)s, in, out};
-    amul_range(&c, 0, s->ncell);
+    par_for(s->pool, s->ncell, amul_range, &c);
 }
 
-static double spec_dot(const double *a, const double *b, long n)
+static void spec_dot_range(void *ctx, size_t a, size_t b)
 {
+    spec_ctx *c = (spec_ctx *)ctx;
+    for (size_t k = a; k < b; k++) {
+        size_t lo, hi;
+        pool_chunk((size_t)c->n, SPEC_CHUNKS, (int)k, &lo, &hi);
+        double acc = 0.0;
+        for (size_t e = lo; e < hi; e++) acc += c->in[e] * c->in2[e];
+        c->part[k] = acc;
+    }
+}
+
+static double spec_dot(const fso_solver *s, const double *a, const double *b, long n)
+{
+    spec_ctx c;
+    c.in = a;
+    c.in2 = b;
+    c.n = n;
+    par_for(s->pool, SPEC_CHUNKS, spec_dot_range, &c);
     double acc = 0.0;
-    for (long k = 0; k < n; k++) acc += a[k] * b[k];
+    for (int k = 0; k < SPEC_CHUNKS; k++) acc += c.part[k];
     return acc;
+}
+
+/* x += alpha d and r -= alpha q */
+static void spec_update_range(void *ctx, size_t a, size_t b)
+{
+    spec_ctx *c = (spec_ctx *)ctx;
+    for (size_t k = a; k < b; k++) {
+        c->out[k] += c->alpha * c->in[k];
+        c->out2[k] -= c->alpha * c->in2[k];
+    }
+}
+
+/* d = z + beta d */
+static void spec_dir_range(void *ctx, size_t a, size_t b)
+{
+    spec_ctx *c = (spec_ctx *)ctx;
+    for (size_t k = a; k < b; k++) c->out[k] = c->in[k] + c->alpha * c->out[k];
 }
 
 int fso_spec_solve(int ni, int nj, const int8_t *material, float dt, double density, double dx,
@@ -2225,32 +2302,36 @@ int fso_spec_solve(int ni, int nj, const int8_t *material, float dt, double dens
         result[k] = 0.0;
         r[k] = rhs[k];
     }
-    const double bnorm = sqrt(spec_dot(rhs, rhs, N));
+    const double bnorm = sqrt(spec_dot(s, rhs, rhs, N));
     int it = 0;
     double rnorm = bnorm;
+    spec_ctx c;
     if (bnorm > 0.0) {
         spec_apply_m(s, r, y, z);
         memcpy(d, z, N * sizeof(double));
-        double rz = spec_dot(r, z, N);
+        double rz = spec_dot(s, r, z, N);
         for (it = 0; it < max_iter; it++) {
-            rnorm = sqrt(spec_dot(r, r, N));
+            rnorm = sqrt(spec_dot(s, r, r, N));
             if (rnorm <= rel_tol * bnorm) break;
             spec_apply_a(s, d, q);
-            const double alpha = rz / spec_dot(d, q, N);
-            for (long k = 0; k < N; k++) {
-                result[k] += alpha * d[k];
-                r[k] -= alpha * q[k];
-            }
+            c.alpha = rz / spec_dot(s, d, q, N);
+            c.in = d;
+            c.in2 = q;
+            c.out = result;
+            c.out2 = r;
+            par_for(s->pool, (size_t)N, spec_update_range, &c);
             spec_apply_m(s, r, y, z);
-            const double rz2 = spec_dot(r, z, N);
-            const double beta = rz2 / rz;
+            const double rz2 = spec_dot(s, r, z, N);
+            c.alpha = rz2 / rz; /* beta */
             rz = rz2;
-            for (long k = 0; k < N; k++) d[k] = z[k] + beta * d[k];
+            c.in = z;
+            c.out = d;
+            par_for(s->pool, (size_t)N, spec_dir_range, &c);
         }
         /* true residual of the returned solution */
         spec_apply_a(s, result, q);
         for (long k = 0; k < N; k++) q[k] = rhs[k] - q[k];
-        rnorm = sqrt(spec_dot(q, q, N));
+        rnorm = sqrt(spec_dot(s, q, q, N));
     }
     if (rel_residual) *rel_residual = bnorm > 0.0 ? rnorm / bnorm : 0.0;
     free(r);
@@ -2260,4 +2341,12 @@ int fso_spec_solve(int ni, int nj, const int8_t *material, float dt, double dens
     free(q);
     fso_destroy(s);
     return it;
+}
+
+/* The processor count std::thread::hardware_concurrency() reports on this
+ * host (libstdc++ asks glibc's get_nprocs), which sizes the reference's
+ * thread pool (threadpool.cpp:12); recorded beside the CPU baseline. */
+int fso_hardware_concurrency(void)
+{
+    return get_nprocs();
 }

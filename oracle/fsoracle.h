@@ -193,6 +193,9 @@ int fso_spec_solve(int ni, int nj, const int8_t *material, float dt, double dens
                    const double *rhs, double *result, double rel_tol, int max_iter,
                    double *rel_residual);
 
+/* std::thread::hardware_concurrency() of this host (glibc get_nprocs) */
+int fso_hardware_concurrency(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -87,6 +87,9 @@ def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
         f = getattr(lib, name)
         f.restype = res
         f.argtypes = args
+    if hasattr(lib, "fso_hardware_concurrency"):
+        lib.fso_hardware_concurrency.restype = c_int
+        lib.fso_hardware_concurrency.argtypes = []
     # the spec-mode FP64 oracle exists in the C restatement only (the
     # reference has no such solve on its hot path)
     if hasattr(lib, "fso_spec_solve"):

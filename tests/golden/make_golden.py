@@ -1,6 +1,6 @@
 """Regenerate the golden fixtures in tests/golden/ from the reference itself.
 
-    python tests/golden/make_golden.py [--reference /root/reference]
+    python tests/golden/make_golden.py [--reference <checkout of the reference project>]
 
 Writes:
   * matviz.npz -- the reference's own known-answer system
@@ -145,12 +145,13 @@ def make_frames(frames: int = 3, names=FRAME_SCENES):
 
 
 def main():
+    import build as oracle_build
+
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default=os.environ.get("FS_REFERENCE_DIR", "/root/reference"))
+    ap.add_argument("--reference", default=oracle_build.reference_dir())
     ap.add_argument("--only", nargs="*", default=None, help="frame scenes to regenerate")
     a = ap.parse_args()
     os.environ["FS_REFERENCE_DIR"] = a.reference
-    import build as oracle_build
 
     oracle_build.build_ref()
     if a.only is None:

@@ -1,0 +1,154 @@
+"""The dam-break configurations at their own sizes.
+
+* C1: the plain dam break at 128^2 (4 particles per cell, seed 42).
+* C2: the large dam break at 1024^2 with its 6-vertex obstacle (seed 7).
+
+Each is stepped on the GPU in the FP64 parity mode through two frames and a
+few substeps, so that the fluid moves and both solves run to their
+200-iteration limit.  From that shared warm state:
+
+1. Every stage of one substep runs on the GPU and on the oracle port
+   (oracle/fsoracle.c, pinned bit for bit to the reference build), each
+   stage from the oracle's state, with the bars of test_gpu_parity.py.
+2. At 1024^2, one whole substep runs in the FP32 production mode and in the
+   FP64 parity mode from identical inputs.  The 200-iteration solve does not
+   converge (the reference's IPP is not symmetric), and its recurrence
+   amplifies rounding.  So a pressure bar of a fixed relative-L2 would
+   measure the recurrence, not the arithmetic.  The bar is instead:
+   - the FP32 pressure's true relative residual ||b - A p|| / ||b|| is no
+     worse than 1.05 times the FP64 one (+1e-6), each on its own right-hand
+     side and with the reference's operator;
+   - the projected grid velocities and the particle velocities are within
+     VEL_BAR relative-L2 of the FP64 mode's;
+   - the FP32 pressure is within PRESSURE_SPREAD_FACTOR times the FP64
+     recurrence's own spread: the relative-L2 change of the FP64 solve when
+     b changes by 1e-7 relative (about one FP32 rounding), with a floor of
+     1e-2.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import fsoracle as fo
+from flipsolver2d_gb300 import gpu, scenes
+
+from conftest import POOL_THREADS
+from test_gpu_parity import check_stages
+from test_gpu_pcg import apply_a
+
+pytestmark = pytest.mark.gpu
+
+VEL_BAR = 1e-2
+PRESSURE_SPREAD_FACTOR = 10.0
+DENSITY = 1000.0
+
+CONFIGS = {
+    "c1_dam_128": dict(res=128, seed=42, obstacle=False),
+    "c2_dam_1024": dict(res=1024, seed=7, obstacle=True),
+}
+
+
+def cfl_dt(vel, p):
+    """First substep size of FlipSolver::stepFrame (flipsolver2d.cpp:478-489)."""
+    f32 = np.float32
+    frame_dt = f32(1.0) / f32(p.fps)
+    m = f32(p.cflNumber) / (f32(vel) + f32(1e-15))
+    if m >= frame_dt or p.maxSubsteps == 1:
+        return float(frame_dt)
+    if f32(2.0) * m >= frame_dt:
+        return float(f32(0.5) * frame_dt)
+    return float(m)
+
+
+def gpu_snapshot(g):
+    """The handle's state in the oracle's snapshot layout."""
+    snap = {"particles": g.get_particles(), "dt": g.dt, "rng": g.get_rng()}
+    for name in fo.STATE_GRIDS:
+        snap[name] = g.get_grid(name)
+    return snap
+
+
+def warm_state(name, substeps):
+    """The configuration after two frames and `substeps` CFL substeps in the
+    FP64 parity mode, and the dt of the next substep."""
+    cfg = CONFIGS[name]
+    sc = scenes.dam_break(cfg["res"], seed=cfg["seed"], obstacle=cfg["obstacle"])
+    g = gpu.GpuFlipSolver(sc, precision=gpu.FS_PCG_FP64, pool_threads=POOL_THREADS)
+    for _ in range(2):
+        g.step_frame()
+    for _ in range(substeps):
+        g.set_dt(cfl_dt(g.max_particle_velocity(), sc.params))
+        g.step()
+    g.set_dt(cfl_dt(g.max_particle_velocity(), sc.params))
+    snap = gpu_snapshot(g)
+    g.close()
+    return sc, snap
+
+
+def rel(a, b):
+    n = float(np.linalg.norm(b))
+    return float(np.linalg.norm(np.asarray(a, np.float64) - np.asarray(b, np.float64)) / n) if n else 0.0
+
+
+@pytest.mark.parametrize("name", sorted(CONFIGS))
+def test_substep_stages_at_configured_size(port_lib, gpu_lib, name, monkeypatch):
+    monkeypatch.setenv("FSO_HOST_THREADS", str(os.cpu_count() or 1))
+    sc, snap = warm_state(name, 3)
+    o = fo.OracleSolver(sc, "port")
+    o.first_frame_init()
+    o.restore(snap)
+    g = gpu.GpuFlipSolver(sc, precision=gpu.FS_PCG_FP64, pool_threads=POOL_THREADS)
+    g.first_frame_init()
+    # the FP64 pressures: the reference recurrence with the dot products
+    # summed in another order, over 200 unconverged iterations at these sizes
+    check_stages(o, g, gpu.FS_PCG_FP64, pcg_bar=1e-6)
+    g.close()
+    o.close()
+
+
+def substep(sc, snap, precision):
+    g = gpu.GpuFlipSolver(sc, precision=precision, pool_threads=POOL_THREADS)
+    g.first_frame_init()
+    g.restore(snap)
+    g.step()
+    out = {"pressure": g.get_grid("pressure"), "rhs": g.get_grid("pressure_rhs"),
+           "u": g.get_grid("u"), "v": g.get_grid("v"), "particles": g.get_particles(),
+           "iters": (g.stat(0), g.stat(1))}
+    g.close()
+    return out
+
+
+@pytest.mark.parametrize("warm_substeps", [3, 5])
+def test_fp32_substep_against_fp64_at_c2(gpu_lib, warm_substeps):
+    sc, snap = warm_state("c2_dam_1024", warm_substeps)
+    n = sc.params.gridSizeI
+    dx, dt = 1.0 / n, snap["dt"]
+    mat = snap["material"]  # the operator of this substep's solves
+    d = substep(sc, snap, gpu.FS_PCG_FP64)
+    f = substep(sc, snap, gpu.FS_PCG_FP32)
+
+    def rel_residual(p, b):
+        return float(np.linalg.norm(b - apply_a(mat, p, dt, DENSITY, dx)) / np.linalg.norm(b))
+
+    rr64, rr32 = rel_residual(d["pressure"], d["rhs"]), rel_residual(f["pressure"], f["rhs"])
+    # the FP64 recurrence's own spread: the same system, b moved by 1e-7
+    it_a, p_a = gpu.pcg_solve(mat, d["rhs"], dt, DENSITY, dx, 200, 1e-2,
+                              precision=gpu.FS_PCG_FP64, pool_threads=POOL_THREADS)
+    xi = np.random.default_rng(5).standard_normal(d["rhs"].shape)
+    it_b, p_b = gpu.pcg_solve(mat, d["rhs"] * (1.0 + 1e-7 * xi), dt, DENSITY, dx, 200, 1e-2,
+                              precision=gpu.FS_PCG_FP64, pool_threads=POOL_THREADS)
+    spread = rel(p_b, p_a)
+    p_err = rel(f["pressure"], d["pressure"])
+    u_err = max(rel(f["u"], d["u"]), rel(f["v"], d["v"]))
+    a, b = f["particles"], d["particles"]
+    print(f"\nC2 FP32 vs FP64 after {warm_substeps} warm substeps: iterations {f['iters']} / "
+          f"{d['iters']}, true residual {rr32:.4e} / {rr64:.4e}, pressure {p_err:.3e}, "
+          f"FP64 spread {spread:.3e}, grid velocity {u_err:.3e}")
+    # the standalone solve of the captured system is the in-step solve
+    assert rel(p_a, d["pressure"]) <= 1e-9
+    assert rr32 <= 1.05 * rr64 + 1e-6, (rr32, rr64)
+    assert u_err <= VEL_BAR, u_err
+    assert a["pos"].shape == b["pos"].shape
+    assert rel(a["vel"], b["vel"]) <= VEL_BAR
+    assert p_err <= max(1e-2, PRESSURE_SPREAD_FACTOR * spread), (p_err, spread)

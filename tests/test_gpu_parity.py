@@ -85,8 +85,16 @@ def test_stages_from_identical_snapshots(scene, precision):
     o = warm_oracle(scene, 3)
     o.set_dt(o.dt * 0.9)  # any substep size; both sides use the same
     g = gpu.GpuFlipSolver(scene, precision=precision, pool_threads=POOL_THREADS)
-    snap = o.snapshot()
-    g.restore(snap)
+    check_stages(o, g, precision)
+
+
+def check_stages(o, g, precision, pcg_bar=1e-9):
+    """Runs every stage of FlipSolver::step on the oracle `o` and the GPU
+    handle `g`, each stage started from the oracle's current state, and
+    checks the bars of the module docstring.  pcg_bar is the relative-L2 bar
+    of the FP64-mode pressures (the reference recurrence with the dot
+    products summed in another order)."""
+    g.restore(o.snapshot())
 
     def resync():
         g.restore(o.snapshot())
@@ -116,7 +124,7 @@ def test_stages_from_identical_snapshots(scene, precision):
     po, pg = o.get_grid("density_pressure"), g.get_grid("density_pressure")
     if precision == gpu.FS_PCG_FP64:
         assert it_o == it_g
-        assert rel_l2(pg, po) <= 1e-9
+        assert rel_l2(pg, po) <= pcg_bar
         a, b = o.get_particles(), g.get_particles()
         assert np.mean(a["pos"] == b["pos"]) > 0.999
         assert np.max(np.abs(a["pos"] - b["pos"])) < 1e-4
@@ -157,9 +165,9 @@ def test_stages_from_identical_snapshots(scene, precision):
     if precision == gpu.FS_PCG_FP64:
         assert_grid_equal(o, g, "pressure_rhs", "pressure rhs")
         assert o.stat(1) == g.stat(1)
-        assert rel_l2(pg, po) <= 1e-9
+        assert rel_l2(pg, po) <= pcg_bar
         for name in ["u", "v"]:
-            assert rel_l2(g.get_grid(name), o.get_grid(name)) <= 1e-6
+            assert rel_l2(g.get_grid(name), o.get_grid(name)) <= max(1e-6, pcg_bar)
         for name in ["u_valid", "v_valid"]:
             assert_grid_equal(o, g, name, "projection validity")
     else:

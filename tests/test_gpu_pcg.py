@@ -152,20 +152,60 @@ def test_ragged_grids(port_lib, gpu_lib, ni, nj, seed):
     """gridSizeI != gridSizeJ.  The reference recurrence is chaotic on the two
     narrow systems: a 1e-15 relative change of b moves the oracle's own
     200-iteration result by 2.5e-5 (37 x 90) and 2.3e-2 (130 x 47), against
-    7.6e-14 and 1.8e-10 after 37 iterations.  So the FP64 mode keeps the
-    oracle's iteration count at both limits and its pressure to 1e-8 after 37
-    iterations; the FP32 mode keeps the true residual after 37 iterations."""
+    7.6e-14 and 1.8e-10 after 37 iterations.  So on those two the FP64 mode
+    keeps the oracle's iteration count at both limits and its pressure to
+    1e-8 after 37 iterations, and the FP32 mode keeps the true residual after
+    37 iterations.  The 700 x 1024 system is not chaotic (its spread stays
+    below 1e-10): there both limits keep the FP64 pressure to 1e-8, and the
+    FP32 pressure stays within 1e-2 relative-L2 of the oracle's (the bar of
+    the square systems) with a true residual no worse than 1.05x."""
     m = ragged_mask(ni, nj, seed)
     b = rhs_for(m, seed)
     dx = 1.0 / max(ni, nj)
+    chaotic = (ni, nj) != (700, 1024)
+    x_o = {}
     for limit in (200, 37):
-        it_o, x_o = fo.pcg_solve(m, b, 1.0 / 30, 1000.0, dx, limit, 1e-2)
+        it_o, x_o[limit] = fo.pcg_solve(m, b, 1.0 / 30, 1000.0, dx, limit, 1e-2)
         it_g, x_g = gpu.pcg_solve(m, b, 1.0 / 30, 1000.0, dx, limit, 1e-2,
                                   precision=gpu.FS_PCG_FP64, pool_threads=POOL_THREADS)
         assert it_g == it_o, f"limit {limit}"
-    assert np.linalg.norm(x_g - x_o) / np.linalg.norm(x_o) <= 1e-8
-    _, x_f = gpu.pcg_solve(m, b, 1.0 / 30, 1000.0, dx, 37, 1e-2,
-                           precision=gpu.FS_PCG_FP32, pool_threads=POOL_THREADS)
+        if limit == 37 or not chaotic:
+            err = np.linalg.norm(x_g - x_o[limit]) / np.linalg.norm(x_o[limit])
+            assert err <= 1e-8, f"FP64 limit {limit}: relative-L2 {err}"
+    for limit in ((37,) if chaotic else (37, 200)):
+        _, x_f = gpu.pcg_solve(m, b, 1.0 / 30, 1000.0, dx, limit, 1e-2,
+                               precision=gpu.FS_PCG_FP32, pool_threads=POOL_THREADS)
+        res_o = np.linalg.norm(b - apply_a(m, x_o[limit], 1.0 / 30, 1000.0, dx))
+        res_f = np.linalg.norm(b - apply_a(m, x_f, 1.0 / 30, 1000.0, dx))
+        assert res_f <= 1.05 * res_o + 1e-6 * np.linalg.norm(b), (limit, res_f, res_o)
+        if not chaotic:
+            err = np.linalg.norm(x_f - x_o[limit]) / np.linalg.norm(x_o[limit])
+            assert err <= 1e-2, f"FP32 limit {limit}: relative-L2 {err}"
+
+
+# Grids too large for one resident tile per SM run the streaming kernels:
+# 1536^2 and 2048^2 (row pitch a multiple of 16 bytes) the TMA-tile kernel
+# k_pcg_tma, 1500^2 the tiled kernel k_pcg_tiled; FP64 runs the linear-index
+# kernel.  Reference stopping (limit 200, absolute 1e-2).  FP64 keeps the
+# oracle's iteration count and its pressure to 1e-8 (the square systems are
+# not chaotic: their spread under a 1e-15 change of b stays below 1e-10);
+# FP32 keeps the bar of the smaller square systems.
+@pytest.mark.parametrize("n,seed", [(1500, 41), (1536, 42), (2048, 43)])
+def test_streaming_kernels_at_size(port_lib, gpu_lib, n, seed, monkeypatch):
+    monkeypatch.setenv("FSO_HOST_THREADS", str(os.cpu_count() or 1))
+    m = random_mask(n, seed)
+    b = rhs_for(m, seed)
+    dx = 1.0 / n
+    it_o, x_o = fo.pcg_solve(m, b, 1.0 / 30, 1000.0, dx, 200, 1e-2)
+    it_d, x_d = gpu.pcg_solve(m, b, 1.0 / 30, 1000.0, dx, 200, 1e-2, precision=gpu.FS_PCG_FP64,
+                              pool_threads=POOL_THREADS)
+    assert it_d == it_o
+    err = np.linalg.norm(x_d - x_o) / np.linalg.norm(x_o)
+    assert err <= 1e-8, f"FP64 relative-L2 {err}"
+    it_f, x_f = gpu.pcg_solve(m, b, 1.0 / 30, 1000.0, dx, 200, 1e-2, precision=gpu.FS_PCG_FP32,
+                              pool_threads=POOL_THREADS)
+    err = np.linalg.norm(x_f - x_o) / np.linalg.norm(x_o)
+    assert err <= 1e-2, f"FP32 relative-L2 {err} (iterations {it_f} vs {it_o})"
     res_o = np.linalg.norm(b - apply_a(m, x_o, 1.0 / 30, 1000.0, dx))
     res_f = np.linalg.norm(b - apply_a(m, x_f, 1.0 / 30, 1000.0, dx))
     assert res_f <= 1.05 * res_o + 1e-6 * np.linalg.norm(b), (res_f, res_o)

@@ -2,6 +2,8 @@
 preconditioner and FP64 refinement, to a true relative residual of 1e-6,
 checked against the full-FP64 PCG oracle (oracle/fsoracle.c fso_spec_solve)
 on the same operator."""
+import os
+
 import numpy as np
 import pytest
 
@@ -14,6 +16,7 @@ REL_TOL = 1e-6
 # the solution's error against the FP64 oracle's (solved to 1e-10) is
 # bounded by the condition number times the residual; measured well below
 SOL_TOL = 1e-3
+SOL_TOL_2048 = 2e-2
 
 
 def _true_rel_residual(m, b, x, dx):
@@ -57,3 +60,36 @@ def test_spec_zero_rhs(gpu_lib):
     m = random_mask(32, 1)
     it, x, rr = gpu.pcg_solve_spec(m, np.zeros(m.shape), DT, DENSITY, 1.0 / 32, REL_TOL)
     assert it == 0 and rr == 0.0 and not np.any(x)
+
+
+@pytest.mark.gpu
+def test_spec_mixed_precision_configuration(port_lib, gpu_lib, monkeypatch):
+    """The mixed-precision configuration itself: 2048^2 cells, a 55 % star
+    mask, the divergence of N(0, 1) face velocities.  Both GPU forms of the
+    solve -- fs_pcg_solve_spec (the cooperative solve, outer loop on the
+    host) and a batch-submitted system (the chained cooperative solve, outer
+    loop on the device) -- reach the 1e-6 true residual (recomputed here in
+    FP64) and agree with the FP64 oracle solved to 1e-8.  At this size a
+    residual of 1e-6 leaves a larger error than on the small grids: the FP64
+    oracle itself, stopped at 1e-6, is 7.4e-3 relative-L2 from its 1e-8
+    solution.  So the bar here is 2e-2, under three times that."""
+    monkeypatch.setenv("FSO_HOST_THREADS", str(os.cpu_count() or 1))
+    m, b, dx = scenes.poisson_case(2048, seed=0)
+    _, x64, rr64 = fo.spec_solve(m, b, DT, DENSITY, dx, 1e-8)
+    assert rr64 <= 1e-8
+    it, x, rr = gpu.pcg_solve_spec(m, b, DT, DENSITY, dx, REL_TOL)
+    true_rr = _true_rel_residual(m, b, x, dx)
+    assert rr <= REL_TOL and true_rr <= 1.01 * REL_TOL, (rr, true_rr)
+    assert np.linalg.norm(x - x64) / np.linalg.norm(x64) <= SOL_TOL_2048
+    bt = gpu.Batch()
+    t = bt.submit_solve(m, b, DT, DENSITY, dx)
+    for _ in range(8):  # the chained solve completes within its round
+        bt.round()
+        if bt.solve_done(t):
+            break
+    assert bt.solve_done(t)
+    it_c, x_c, rr_c = bt.take_solve(t)
+    bt.close()
+    true_rr = _true_rel_residual(m, b, x_c, dx)
+    assert rr_c <= REL_TOL and true_rr <= 1.01 * REL_TOL, (rr_c, true_rr)
+    assert np.linalg.norm(x_c - x64) / np.linalg.norm(x64) <= SOL_TOL_2048
