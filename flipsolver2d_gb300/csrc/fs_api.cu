@@ -2653,23 +2653,46 @@ static bool valid_material(const int8_t *m, size_t n)
 static fs_status pcg_solve_common(int ni, int nj, const int8_t *mat_dev, float dt, double density,
                                   double dx, const void *rhs_dev, void *res_dev, int iter_limit,
                                   double tol, const fs_exec_params *exec, int *iterations,
-                                  PcgCache *c, int prec)
+                                  PcgCache *c, int prec, const uint8_t *info_host = nullptr,
+                                  double scale = 0.0)
 {
     const size_t N = (size_t)ni * nj;
     const int T = (exec && exec->pool_threads > 0) ? exec->pool_threads : default_pool_threads();
     std::vector<int> ends = split_range_ends((long long)N, T);
     cudaStream_t st = 0;
     CK(cudaMemcpyAsync(c->chunk_end, ends.data(), ends.size() * sizeof(int), cudaMemcpyHostToDevice, st));
-    GridDims d{ni, nj, ni / 3 + (ni % 3 != 0), nj / 3 + (nj % 3 != 0)};
-    Grids G;
-    G.material = const_cast<int8_t *>(mat_dev);
-    G.cell_info = c->info;
-    long long ps = 1, rem = 0;
-    split_range_params((long long)N, T, &ps, &rem);
-    launch_decomposition(d, G, c->chunk_last, (int)ends.size(), ps, rem, c->sc, st);
+    if (info_host) {
+        // the operator comes packed from the caller: what the decomposition
+        // derives from it -- the last unit row of each chunk and whether a
+        // unit row sits on a j edge -- is found here
+        std::vector<int> last(ends.size(), -1);
+        int wrap = 0;
+        size_t k = 0;
+        for (size_t cidx = 0; cidx < N; cidx++) {
+            while (k + 1 < ends.size() && (long long)cidx >= ends[k]) k++;
+            if (info_host[cidx] & 0x80) {
+                last[k] = (int)cidx;
+                const size_t j = cidx % (size_t)nj;
+                if (j == 0 || j == (size_t)nj - 1) wrap = 1;
+            }
+        }
+        CK(cudaMemcpyAsync(c->info, info_host, N, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(c->chunk_last, last.data(), last.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(&c->sc->wrap_units, &wrap, sizeof(int), cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st)); // the host vectors above go out of scope
+    } else {
+        GridDims d{ni, nj, ni / 3 + (ni % 3 != 0), nj / 3 + (nj % 3 != 0)};
+        Grids G;
+        G.material = const_cast<int8_t *>(mat_dev);
+        G.cell_info = c->info;
+        long long ps = 1, rem = 0;
+        split_range_params((long long)N, T, &ps, &rem);
+        launch_decomposition(d, G, c->chunk_last, (int)ends.size(), ps, rem, c->sc, st);
+        g_kernel_launches += 1;
+    }
     k_set_dt<<<1, 1, 0, st>>>(c->sc, dt);
     CK(cudaMemsetAsync(&c->sc->pcg_status, 0, sizeof(int), st));
-    g_kernel_launches += 2;
+    g_kernel_launches += 1;
     cudaError_t e;
     int launched = 0;
     if (prec == FS_PCG_FP64) {
@@ -2679,7 +2702,7 @@ static fs_status pcg_solve_common(int ni, int nj, const int8_t *mat_dev, float d
         a.r0 = (double *)c->r0; a.r1 = (double *)c->r1; a.s0 = (double *)c->s0; a.s1 = (double *)c->s1;
         a.partials = c->partials; a.chunk_end = c->chunk_end; a.chunk_last_unit = c->chunk_last;
         a.chunk_val = c->chunk_val;
-        a.nchunks = (int)ends.size(); a.sc = c->sc; a.density = density; a.dx = dx;
+        a.nchunks = (int)ends.size(); a.sc = c->sc; a.density = density; a.dx = dx; a.scale = scale;
         a.iter_limit = iter_limit; a.tol = tol; a.iters_out = &c->sc->density_iters;
         a.status = &c->sc->pcg_status; a.bar = c->bar;
         a.wrap_flag = &c->sc->wrap_units; a.mode = 0;
@@ -2692,7 +2715,7 @@ static fs_status pcg_solve_common(int ni, int nj, const int8_t *mat_dev, float d
         a.ll_r = c->ll.r; a.ll_s = c->ll.s;
         a.partials = c->partials; a.chunk_end = c->chunk_end; a.chunk_last_unit = c->chunk_last;
         a.chunk_val = c->chunk_val;
-        a.nchunks = (int)ends.size(); a.sc = c->sc; a.density = density; a.dx = dx;
+        a.nchunks = (int)ends.size(); a.sc = c->sc; a.density = density; a.dx = dx; a.scale = scale;
         a.iter_limit = iter_limit; a.tol = tol; a.iters_out = &c->sc->density_iters;
         a.status = &c->sc->pcg_status; a.bar = c->bar;
         a.wrap_flag = &c->sc->wrap_units; a.mode = 0;
@@ -2780,6 +2803,53 @@ extern "C" fs_status fs_pcg_solve_device(int ni, int nj, const int8_t *material_
     TRY(pcg_cache_get(dev, N, esz, std::min<long long>(T, (long long)N), &c));
     return pcg_solve_common(ni, nj, material_device, dt, density, dx, rhs_device, result_device,
                             iter_limit, tol, exec, iterations, c, prec);
+}
+
+extern "C" fs_status fs_pcg_solve_operator(int ni, int nj, const uint8_t *cell_info, double scale,
+                                           const double *rhs, double *result, int iter_limit,
+                                           double tol, const fs_exec_params *exec, int *iterations)
+{
+    if (ni < 1 || nj < 1 || !cell_info || !rhs || !result || iter_limit < 0 || !(scale > 0.0))
+        return fail(FS_ERR_BAD_ARG, "fs_pcg_solve_operator: invalid argument");
+    const size_t N = (size_t)ni * nj;
+    // a neighbour whose linear index falls outside [0, N) reads as 0 in the
+    // reference's multiply (pressuredata.h:132-146): its mask bit is dropped
+    std::vector<uint8_t> info(cell_info, cell_info + N);
+    for (size_t k = 0; k < N; k++) {
+        uint8_t b = info[k];
+        if (((b >> 4) & 7) > 4 || (!(b & 0x80) && (b & 0x0f)))
+            return fail(FS_ERR_BAD_ARG, "fs_pcg_solve_operator: cell %zu: bad operator byte 0x%02x", k, b);
+        if (k < (size_t)nj) b &= (uint8_t)~1u;
+        if (k + (size_t)nj >= N) b &= (uint8_t)~2u;
+        if (k == 0) b &= (uint8_t)~4u;
+        if (k + 1 >= N) b &= (uint8_t)~8u;
+        info[k] = b;
+    }
+    const int dev = exec ? exec->device : 0;
+    const int prec = (exec && exec->pcg_precision == FS_PCG_FP64) ? FS_PCG_FP64 : FS_PCG_FP32;
+    const size_t esz = prec == FS_PCG_FP64 ? 8 : 4;
+    std::lock_guard<std::mutex> lk(g_pcg_mu);
+    CK(cudaSetDevice(dev));
+    const int T = (exec && exec->pool_threads > 0) ? exec->pool_threads : default_pool_threads();
+    PcgCache *c = nullptr;
+    TRY(pcg_cache_get(dev, N, esz, std::min<long long>(T, (long long)N), &c));
+    if (prec == FS_PCG_FP64) {
+        CK(cudaMemcpy(c->b, rhs, N * 8, cudaMemcpyHostToDevice));
+    } else {
+        std::vector<float> tmp(N);
+        for (size_t k = 0; k < N; k++) tmp[k] = (float)rhs[k];
+        CK(cudaMemcpy(c->b, tmp.data(), N * 4, cudaMemcpyHostToDevice));
+    }
+    TRY(pcg_solve_common(ni, nj, nullptr, 0.f, 1.0, 1.0, c->b, c->x, iter_limit, tol, exec, iterations,
+                         c, prec, info.data(), scale));
+    if (prec == FS_PCG_FP64) {
+        CK(cudaMemcpy(result, c->x, N * 8, cudaMemcpyDeviceToHost));
+    } else {
+        std::vector<float> tmp(N);
+        CK(cudaMemcpy(tmp.data(), c->x, N * 4, cudaMemcpyDeviceToHost));
+        for (size_t k = 0; k < N; k++) result[k] = tmp[k];
+    }
+    return FS_OK;
 }
 
 // ---------------------------------------------------------------------------

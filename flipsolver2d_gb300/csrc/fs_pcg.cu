@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgArgs<T> a)
     double *pA = a.partials, *pB = a.partials + 2 * G;
 
     // operator coefficients (flipsolver2d.cpp:799, 891, 924-927)
-    const double scale_d = (double)a.sc->dt / (a.density * a.dx * a.dx);
+    const double scale_d = pcg_scale(a);
     Coef<T> cf;
     cf.ascale = (T)scale_d;
 #pragma unroll
@@ -609,7 +609,7 @@ __global__ void __launch_bounds__(kTiledThreads) k_pcg_tiled(PcgArgs<float> a, T
     double *pA = a.partials, *pB = a.partials + G, *pC = a.partials + 2 * G;
     double *chunk_val = a.chunk_val;
 
-    const double scale_d = (double)a.sc->dt / (a.density * a.dx * a.dx);
+    const double scale_d = pcg_scale(a);
     const float scale = (float)scale_d;
     float inv[5];
     inv[0] = 0.f; // only outside the grid

@@ -34,6 +34,8 @@ template <typename T> struct PcgArgs {
     int nchunks;
     const Scalars *sc;         // dt of the substep
     double density, dx;
+    double scale;              // > 0: the operator's scale dt / (density dx^2) as
+                               // given (fs_pcg_solve_operator); else from dt
     int iter_limit;
     double tol;
     int *iters_out;
@@ -58,6 +60,12 @@ struct LlBuffers {
 // the partial records: two sets of at most 256 blocks (the resident kernel's
 // tile limit) of four words
 constexpr size_t kLlRecWords = 2 * 256 * 4;
+
+// scale = dt / (density dx^2) of the pressure operator (flipsolver2d.cpp:797-887)
+template <typename T> __device__ __forceinline__ double pcg_scale(const PcgArgs<T> &a)
+{
+    return a.scale > 0.0 ? a.scale : (double)a.sc->dt / (a.density * a.dx * a.dx);
+}
 
 template <typename T> int pcg_grid_size(long long N);
 // Runs the solve: FP32 uses the shared-memory tiled kernel, falling back to

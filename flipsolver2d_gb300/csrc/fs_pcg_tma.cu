@@ -392,7 +392,7 @@ k_pcg_tma(PcgArgs<float> a, const __grid_constant__ TmaMaps m, int ti, int tj)
     __syncthreads();
     unsigned phase = 0;
 
-    const double scale_d = (double)a.sc->dt / (a.density * a.dx * a.dx);
+    const double scale_d = pcg_scale(a);
     const float scale = (float)scale_d;
     __shared__ float inv[8];
     if (threadIdx.x < 8) inv[threadIdx.x] = (threadIdx.x >= 1 && threadIdx.x <= 4)
@@ -926,7 +926,7 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     const TolTest tt = tol_test(a.tol);
     const float2 eps8 = make_float2((float)1e-8, (float)(1e-8 - (double)(float)1e-8));
 
-    const double scale_d = (double)a.sc->dt / (a.density * a.dx * a.dx);
+    const double scale_d = pcg_scale(a);
     const float scale = (float)scale_d;
     if (threadIdx.x < 8)
         inv[threadIdx.x] = (threadIdx.x >= 1 && threadIdx.x <= 4) ? (float)(1.0 / (threadIdx.x * scale_d)) : 0.f;

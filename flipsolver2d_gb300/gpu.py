@@ -102,6 +102,9 @@ _SIGS = {
                                            ctypes.c_float, ctypes.c_double, ctypes.c_double,
                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                            ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_pcg_solve_operator": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_double,
+                                             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                             ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]),
     "fs_pcg_solve_spec": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_float,
                                          ctypes.c_double, ctypes.c_double, ctypes.c_void_p,
                                          ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
@@ -393,6 +396,23 @@ def pcg_solve(material: np.ndarray, rhs: np.ndarray, dt: float, density: float, 
     it = GpuLinearSolver(precision, pool_threads).solve(material, dt, density, dx, x, rhs,
                                                         iter_limit, tol)
     return it, x
+
+
+def pcg_solve_operator(cell_info: np.ndarray, rhs: np.ndarray, scale: float, iter_limit: int,
+                       tol: float, precision: int = FS_PCG_FP32, pool_threads: int = 8, device: int = 0):
+    """fs_pcg_solve_operator: LinearSolver::solve on an operator given as one
+    byte per cell (unit bit 7, non-solid count bits 4-6, fluid-neighbour mask
+    bits 0-3) and its scale.  Returns (iterations, solution float64)."""
+    lib = load()
+    ni, nj = cell_info.shape
+    info = np.ascontiguousarray(cell_info, np.uint8)
+    b = np.ascontiguousarray(rhs, np.float64).reshape(ni, nj)
+    x = np.zeros((ni, nj), np.float64)
+    it = ctypes.c_int()
+    ex = exec_params(precision, pool_threads, device)
+    _check(lib.fs_pcg_solve_operator(ni, nj, _ptr(info), scale, _ptr(b), _ptr(x), iter_limit, tol,
+                                     ctypes.byref(ex), ctypes.byref(it)), "fs_pcg_solve_operator")
+    return int(it.value), x
 
 
 class Batch:

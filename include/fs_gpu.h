@@ -269,6 +269,21 @@ fs_status fs_pcg_solve_device(int ni, int nj, const int8_t *material_device, flo
                               void *result_device, int iter_limit, double tol,
                               const fs_exec_params *exec, int *iterations);
 
+/* LinearSolver::solve (linearsolver.cpp:25-73) on an operator given as its
+ * rows rather than as a material grid: what IndexedPressureParameters and
+ * IndexedIPPCoefficients hold (pressuredata.h:97-151,
+ * PressureIPPCoeficients.h:11-47), one byte per cell:
+ *   bit 7     the cell is a unit row (IndexedPressureParameterUnit)
+ *   bits 4-6  its nonsolidNeighborCount (0..4); needed for every cell that
+ *             neighbours a unit row, because the IPP coefficients are
+ *             1 / (count(neighbour) * scale) (flipsolver2d.cpp:924-927)
+ *   bits 0-3  fluidNeighborMask (NeighborMask: i-1, i+1, j-1, j+1); unit rows only
+ * scale is IndexedPressureParameters' m_scale, dt / (density dx^2).  Host
+ * arrays; precision, iterations and return convention as fs_pcg_solve. */
+fs_status fs_pcg_solve_operator(int ni, int nj, const uint8_t *cell_info, double scale,
+                                const double *rhs, double *result, int iter_limit, double tol,
+                                const fs_exec_params *exec, int *iterations);
+
 /* Spec mode: solve the same pressure system to a true relative residual,
  * ||rhs - A result|| <= rel_tol ||rhs|| (2-norms).  The reference's hot-path
  * PCG cannot do this (its IPP is not symmetric and the iteration stalls);

@@ -209,3 +209,24 @@ def test_streaming_kernels_at_size(port_lib, gpu_lib, n, seed, monkeypatch):
     res_o = np.linalg.norm(b - apply_a(m, x_o, 1.0 / 30, 1000.0, dx))
     res_f = np.linalg.norm(b - apply_a(m, x_f, 1.0 / 30, 1000.0, dx))
     assert res_f <= 1.05 * res_o + 1e-6 * np.linalg.norm(b), (res_f, res_o)
+
+
+@pytest.mark.parametrize("precision", [gpu.FS_PCG_FP64, gpu.FS_PCG_FP32])
+def test_operator_entry_point_matches_material_solve(gpu_lib, precision):
+    """fs_pcg_solve_operator (the operator as its rows, what the C++
+    LinearSolver drop-in passes) and fs_pcg_solve (the operator built from the
+    material grid) run the same solve: the same iteration count and the same
+    bits, in both precisions."""
+    from operator_bytes import decomposition_bytes
+
+    n = 96
+    m = random_mask(n, 13)
+    b = rhs_for(m, 13)
+    dt, density, dx = 1.0 / 30, 1000.0, 1.0 / n
+    scale = float(np.float32(dt)) / (density * dx * dx)
+    it_m, x_m = gpu.pcg_solve(m, b, dt, density, dx, 200, 1e-2, precision=precision,
+                              pool_threads=POOL_THREADS)
+    it_o, x_o = gpu.pcg_solve_operator(decomposition_bytes(m), b, scale, 200, 1e-2,
+                                       precision=precision, pool_threads=POOL_THREADS)
+    assert it_o == it_m
+    assert np.array_equal(x_o, x_m)
