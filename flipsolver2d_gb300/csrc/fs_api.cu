@@ -93,6 +93,7 @@ extern "C" const char *fs_status_string(fs_status s)
     case FS_ERR_TIMEOUT: return "device wait timed out";
     case FS_ERR_UNSUPPORTED: return "unsupported";
     case FS_ERR_STATE: return "invalid state";
+    case FS_ERR_NONFINITE: return "non-finite value";
     }
     return "unknown";
 }
@@ -1052,6 +1053,7 @@ template <typename T> static PcgArgs<T> pcg_args(fs_solver *s, const void *b, vo
     a.tol = s->sp.projectTolerance;
     a.iters_out = iters;
     a.status = &s->sc->pcg_status;
+    a.spin_limit = s->ex.wait_polls;
     a.bar = s->bar;
     a.wrap_flag = &s->sc->wrap_units;
     a.mode = 0;
@@ -1245,7 +1247,7 @@ static fs_status stage(fs_solver *s, int which, bool in_step)
         }
         break;
     case FS_STAGE_G2P:
-        launch_g2p(d, s->sp, s->P, s->G, q);
+        launch_g2p(d, s->sp, s->P, s->G, s->sc, q);
         g_kernel_launches += 1;
         break;
     case FS_STAGE_COUNT:
@@ -1378,6 +1380,11 @@ static fs_status read_scalars(fs_solver *s)
     CK(cudaStreamSynchronize(s->st));
     if (s->sc_host->pcg_status != 0)
         return fail(FS_ERR_TIMEOUT, "a PCG grid barrier wait timed out");
+    if (s->sc_host->nonfinite != 0) {
+        // reported once; the state that produced it stays as it is
+        CK(cudaMemsetAsync(&s->sc->nonfinite, 0, sizeof(int), s->st));
+        return fail(FS_ERR_NONFINITE, "a substep left a NaN or infinite particle velocity");
+    }
     if (s->sc_host->nb_overflow != 0)
         return fail(FS_ERR_UNSUPPORTED,
                     "NB-FLIP reseeding: more than %d candidates left their cell's bin, or the "
@@ -2437,6 +2444,8 @@ static fs_status batch_round(fs_batch *b, int *busy)
         fs_solver *s = bs.s;
         if (!bs.in_frame) continue;
         if (s->sc_host->pcg_status != 0) return fail(FS_ERR_TIMEOUT, "batch member %d: solver status", k);
+        if (s->sc_host->nonfinite != 0)
+            return fail(FS_ERR_NONFINITE, "batch member %d: a substep left a NaN or infinite particle velocity", k);
         if (bs.substep_count > 0) {
             s->density_iters_max = std::max(s->density_iters_max, s->sc_host->density_iters);
             s->pressure_iters_max = std::max(s->pressure_iters_max, s->sc_host->pressure_iters);
@@ -2705,6 +2714,7 @@ static fs_status pcg_solve_common(int ni, int nj, const int8_t *mat_dev, float d
         a.nchunks = (int)ends.size(); a.sc = c->sc; a.density = density; a.dx = dx; a.scale = scale;
         a.iter_limit = iter_limit; a.tol = tol; a.iters_out = &c->sc->density_iters;
         a.status = &c->sc->pcg_status; a.bar = c->bar;
+        a.spin_limit = exec ? exec->wait_polls : 0;
         a.wrap_flag = &c->sc->wrap_units; a.mode = 0;
         e = launch_pcg<double>(a, st, &launched);
     } else {
@@ -2718,6 +2728,7 @@ static fs_status pcg_solve_common(int ni, int nj, const int8_t *mat_dev, float d
         a.nchunks = (int)ends.size(); a.sc = c->sc; a.density = density; a.dx = dx; a.scale = scale;
         a.iter_limit = iter_limit; a.tol = tol; a.iters_out = &c->sc->density_iters;
         a.status = &c->sc->pcg_status; a.bar = c->bar;
+        a.spin_limit = exec ? exec->wait_polls : 0;
         a.wrap_flag = &c->sc->wrap_units; a.mode = 0;
         int ti = 0, tj = 0;
         TmaMaps maps;
@@ -3375,6 +3386,7 @@ extern "C" fs_status fs_pcg_solve_device_noalloc(int ni, int nj, const int8_t *m
     a.tol = tol;
     a.iters_out = &sc->density_iters;
     a.status = &sc->pcg_status;
+    a.spin_limit = exec ? exec->wait_polls : 0;
     a.bar = reinterpret_cast<GridBarrier *>(base + kNaBar);
     a.wrap_flag = &sc->wrap_units;
     a.mode = 0;

@@ -758,7 +758,7 @@ void launch_adjust(const GridDims &d, const SceneParams &sp, const Particles &P,
 // ---------------------------------------------------------------------------
 __global__ void k_g2p(GridDims d, Particles P, const float *__restrict__ u,
                       const float *__restrict__ v, const float *__restrict__ su,
-                      const float *__restrict__ sv, float pic)
+                      const float *__restrict__ sv, float pic, Scalars *__restrict__ sc)
 {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     const int nslots = P.bin_start[P.nbins];
@@ -776,13 +776,16 @@ __global__ void k_g2p(GridDims d, Particles P, const float *__restrict__ u,
     vel.x = ax + tx * flip;
     vel.y = ay + ty * flip;
     P.vel[s] = vel;
+    // the substep's sentinel: every particle velocity it leaves is finite
+    // (isfinite of NaN and of +-inf is false); one flag word, set rarely
+    if (!(isfinite(vel.x) && isfinite(vel.y))) atomicOr(&sc->nonfinite, 1);
 }
 
 void launch_g2p(const GridDims &d, const SceneParams &sp, const Particles &P, const Grids &G,
-                cudaStream_t st)
+                Scalars *sc, cudaStream_t st)
 {
     if (P.cap == 0) return;
-    k_g2p<<<nblk(P.bound, kThreads), kThreads, 0, st>>>(d, P, G.u, G.v, G.su, G.sv, sp.picRatio);
+    k_g2p<<<nblk(P.bound, kThreads), kThreads, 0, st>>>(d, P, G.u, G.v, G.su, G.sv, sp.picRatio, sc);
 }
 
 // ---------------------------------------------------------------------------

@@ -41,7 +41,8 @@ constexpr long long kBarrierSpinLimit = 1LL << 24; // ~2 s with 64 ns sleeps
 // Bounded-spin grid barrier.  Co-residency is guaranteed by the cooperative
 // launch; if a wait still exceeds the limit the kernel records status 1 and
 // every block returns, leaving the context usable.
-__device__ __forceinline__ bool grid_barrier(GridBarrier *gb, unsigned nblocks, int *status)
+__device__ __forceinline__ bool grid_barrier(GridBarrier *gb, unsigned nblocks, int *status,
+                                             long long lim)
 {
     __shared__ int ok;
     __syncthreads();
@@ -58,7 +59,7 @@ __device__ __forceinline__ bool grid_barrier(GridBarrier *gb, unsigned nblocks, 
         } else {
             long long spins = 0;
             while (gen.load(cuda::memory_order_acquire) == g) {
-                if (++spins > kBarrierSpinLimit) {
+                if (++spins > lim) {
                     atomicExch(status, 1);
                     ok = 0;
                     break;
@@ -67,9 +68,11 @@ __device__ __forceinline__ bool grid_barrier(GridBarrier *gb, unsigned nblocks, 
             }
         }
         __threadfence();
+        // one verdict for the whole block (status can change between reads)
+        if (*((volatile int *)status) != 0) ok = 0;
     }
     __syncthreads();
-    return ok != 0 && *((volatile int *)status) == 0;
+    return ok != 0;
 }
 
 // block-wide FP64 sum; result valid in every thread
@@ -265,6 +268,7 @@ __device__ __forceinline__ T q_at(const uint8_t *__restrict__ info, const T *__r
 template <typename T>
 __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgArgs<T> a)
 {
+    const long long lim = a.spin_limit > 0 ? a.spin_limit : kBarrierSpinLimit;
     __shared__ double sm[40];
     __shared__ double bcast[4];
     if (a.mode == 1 && *a.wrap_flag == 0) return;
@@ -303,7 +307,7 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgArgs<T> a)
         pA[blockIdx.x] = part;
         pA[G + blockIdx.x] = anynz ? 1.0 : 0.0;
     }
-    if (!grid_barrier(a.bar, G, a.status)) return;
+    if (!grid_barrier(a.bar, G, a.status, lim)) return;
     double sigma = grid_sum(pA, G, sm);
     const double nzsum = grid_sum(pA + G, G, sm);
     if (nzsum == 0.0) {
@@ -337,7 +341,7 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgArgs<T> a)
         }
         part = block_sum(sizeof(T) == 4 ? (double)qs_f : qs_d, sm);
         if (threadIdx.x == 0) pA[blockIdx.x] = part;
-        if (!grid_barrier(a.bar, G, a.status)) return;
+        if (!grid_barrier(a.bar, G, a.status, lim)) return;
         const double qs = grid_sum(pA, G, sm);
         const double alpha = sigma / (qs + 1e-8);
         const T ta = (T)alpha;
@@ -378,7 +382,7 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgArgs<T> a)
         }
         part = block_sum(sizeof(T) == 4 ? (double)zr_f : zr_d, sm);
         if (threadIdx.x == 0) pB[blockIdx.x] = part;
-        if (!grid_barrier(a.bar, G, a.status)) return;
+        if (!grid_barrier(a.bar, G, a.status, lim)) return;
 
         // VOps::maxAbs with the reference's chunking (vmath.cpp:100-136):
         // one warp per chunk, the max over warps (order-independent)
@@ -524,8 +528,10 @@ __device__ __forceinline__ double sum_partials_w(const double *partials, int nbl
 
 // Tight-spin grid barrier (bounded like grid_barrier; spins without sleeping
 // first, since a barrier here normally completes within microseconds).
-__device__ __forceinline__ bool grid_sync_fast(GridBarrier *gb, unsigned nblocks, int *status)
+__device__ __forceinline__ bool grid_sync_fast(GridBarrier *gb, unsigned nblocks, int *status,
+                                               long long lim)
 {
+    __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         volatile unsigned *vgen = &gb->gen;
@@ -539,7 +545,7 @@ __device__ __forceinline__ bool grid_sync_fast(GridBarrier *gb, unsigned nblocks
         } else {
             long long spins = 0;
             while (*vgen == g) {
-                if (++spins > (kBarrierSpinLimit << 4)) {
+                if (++spins > lim) {
                     atomicExch(status, 1);
                     break;
                 }
@@ -547,9 +553,11 @@ __device__ __forceinline__ bool grid_sync_fast(GridBarrier *gb, unsigned nblocks
             }
         }
         __threadfence();
+        // one verdict for the whole block (status can change between reads)
+        s_ok = *((volatile int *)status) == 0;
     }
     __syncthreads();
-    return *((volatile int *)status) == 0;
+    return s_ok != 0;
 }
 
 // sum of the per-block partials after a barrier: one load per thread, then a
@@ -591,6 +599,8 @@ __device__ __forceinline__ void load_region(V *__restrict__ dst, const V *__rest
 
 __global__ void __launch_bounds__(kTiledThreads) k_pcg_tiled(PcgArgs<float> a, TileShape ts)
 {
+    // tight spins first, so the default allows more polls than grid_barrier's
+    const long long lim_fast = a.spin_limit > 0 ? a.spin_limit : (kBarrierSpinLimit << 4);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ double sm[40];
     __shared__ double s_err;
@@ -638,7 +648,7 @@ __global__ void __launch_bounds__(kTiledThreads) k_pcg_tiled(PcgArgs<float> a, T
             pC[blockIdx.x] = anynz ? 1.0 : 0.0;
         }
     }
-    if (!grid_sync_fast(a.bar, G, a.status)) return;
+    if (!grid_sync_fast(a.bar, G, a.status, lim_fast)) return;
     double sigma = sum_partials_w(pA, G, sm);
     if (sum_partials_w(pC, G, sm) == 0.0) {
         if (blockIdx.x == 0 && threadIdx.x == 0) *a.iters_out = 0;
@@ -688,7 +698,7 @@ __global__ void __launch_bounds__(kTiledThreads) k_pcg_tiled(PcgArgs<float> a, T
             const double part = block_sum_ff(qs, sm);
             if (threadIdx.x == 0) pA[blockIdx.x] = part;
         }
-        if (!grid_sync_fast(a.bar, G, a.status)) return;
+        if (!grid_sync_fast(a.bar, G, a.status, lim_fast)) return;
         const double alpha = sigma / (sum_partials_w(pA, G, sm) + 1e-8);
         const float fa = (float)alpha;
 
@@ -750,7 +760,7 @@ __global__ void __launch_bounds__(kTiledThreads) k_pcg_tiled(PcgArgs<float> a, T
             const double part = block_sum_ff(zr, sm);
             if (threadIdx.x == 0) pB[blockIdx.x] = part;
         }
-        if (!grid_sync_fast(a.bar, G, a.status)) return;
+        if (!grid_sync_fast(a.bar, G, a.status, lim_fast)) return;
         {
             // one warp per chunk, the max over warps (order-independent)
             const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;

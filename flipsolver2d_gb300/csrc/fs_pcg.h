@@ -40,6 +40,8 @@ template <typename T> struct PcgArgs {
     double tol;
     int *iters_out;
     int *status;               // set to 1 when a barrier wait times out
+    long long spin_limit;      // polls after which a device wait gives up (0: the
+                               // kernel's default, seconds)
     GridBarrier *bar;
     const int *wrap_flag;      // set by the decomposition when a unit row sits on
                                // the j = 0 or j = NJ-1 edge (linear-index wrap)

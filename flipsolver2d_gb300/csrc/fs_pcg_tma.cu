@@ -36,7 +36,7 @@ constexpr int kThreads = 1024;
 constexpr int kStripThreads = 512;
 constexpr int kMaxOwnedChunks = 64; // chunk ends a resident tile lists in shared memory
 constexpr int kPartRounds = 8;      // per-lane partial loads: up to 256 resident blocks // resident kernel with register strips: 128 registers a thread
-constexpr long long kSpinLimit = 1LL << 25; // a few seconds with the sleeps
+constexpr long long kSpinLimit = 1LL << 25; // default polls of a device wait: seconds
 
 __device__ __forceinline__ unsigned smem_u32(const void *p)
 {
@@ -216,9 +216,10 @@ __device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v)
 // barrier); the last block resets the counter and releases the next
 // generation, which the others acquire.  With async_proxy the block's TMA
 // stores are complete and fenced for the generic proxy before it arrives.
-__device__ __forceinline__ bool gsync(GridBarrier *gb, unsigned nblocks, int *status,
+__device__ __forceinline__ bool gsync(GridBarrier *gb, unsigned nblocks, int *status, long long lim,
                                       bool async_proxy = true)
 {
+    __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         if (async_proxy) {
@@ -234,7 +235,7 @@ __device__ __forceinline__ bool gsync(GridBarrier *gb, unsigned nblocks, int *st
             long long spins = 0;
             while (ld_acquire_u32(&gb->gen) == g) {
                 ++spins;
-                if (spins > kSpinLimit ||
+                if (spins > lim ||
                     ((spins & 1023) == 0 && *((volatile int *)status) != 0)) {
                     atomicExch(status, 1);
                     break;
@@ -242,9 +243,11 @@ __device__ __forceinline__ bool gsync(GridBarrier *gb, unsigned nblocks, int *st
             }
         }
         if (async_proxy) fence_async_all();
+        // one verdict for the whole block (status can change between reads)
+        s_ok = *((volatile int *)status) == 0;
     }
     __syncthreads();
-    return *((volatile int *)status) == 0;
+    return s_ok != 0;
 }
 
 // VOps::maxAbs (vmath.cpp:100-136) with the reference's chunking, then the
@@ -299,18 +302,26 @@ __device__ __forceinline__ bool chunk_converged(const PcgArgs<float> &a, Load rn
     return f != 0;
 }
 
-// wait for the current TMA load batch (bounded)
-__device__ __forceinline__ bool load_wait(unsigned long long *bar, unsigned &phase, int *status)
+// wait for the current TMA load batch.  After `lim` polls (or once another
+// block reported a timeout) the solve is given up, but the block still waits
+// -- bounded again -- for its own copies to land in its shared memory before
+// it may leave.  Block-uniform result (a block barrier).
+__device__ __forceinline__ bool load_wait(unsigned long long *bar, unsigned &phase, int *status,
+                                          long long lim)
 {
     long long spins = 0;
+    bool failed = false;
     while (!mbar_try_wait(bar, phase & 1)) {
-        if (++spins > kSpinLimit || *((volatile int *)status) != 0) {
+        ++spins;
+        if (!failed && (spins > lim || *((volatile int *)status) != 0)) {
             atomicExch(status, 1);
-            return false;
+            failed = true;
+            spins = 0;
         }
+        if (failed && spins > kSpinLimit) break; // a copy that never lands
     }
     phase++;
-    return true;
+    return __syncthreads_or(failed) == 0;
 }
 
 struct SmemLayout {
@@ -358,6 +369,7 @@ __host__ __device__ inline SmemLayout smem_layout(int ti, int tj)
 __global__ void __launch_bounds__(kThreads, 1)
 k_pcg_tma(PcgArgs<float> a, const __grid_constant__ TmaMaps m, int ti, int tj)
 {
+    const long long lim = a.spin_limit > 0 ? a.spin_limit : kSpinLimit;
     extern __shared__ unsigned char smem_dyn[];
     __shared__ float2 sm[40];
     __shared__ int s_flag;
@@ -418,7 +430,7 @@ k_pcg_tma(PcgArgs<float> a, const __grid_constant__ TmaMaps m, int ti, int tj)
             pC[blockIdx.x] = make_float2(anynz ? 1.f : 0.f, 0.f);
         }
     }
-    if (!gsync(a.bar, G, a.status)) return;
+    if (!gsync(a.bar, G, a.status, lim)) return;
     float2 sigma = psum(pA, G, sm);
     if (psum(pC, G, sm).x == 0.f) {
         // the reference leaves result at zero
@@ -452,7 +464,7 @@ k_pcg_tma(PcgArgs<float> a, const __grid_constant__ TmaMaps m, int ti, int tj)
                 if (!first) tma_load_2d(RB, mr_cur, tj0 - 4, ti0 - 2, &bar);
                 tma_load_2d(SB, first ? ms_cur : ms_prev, tj0 - 4, ti0 - 2, &bar);
             }
-            if (!load_wait(&bar, phase, a.status)) return;
+            if (!load_wait(&bar, phase, a.status, lim)) return;
             // s on the tile and its 1-halo
             for (int r = warp; r < L.h1; r += nw) {
                 const int rr = r - 1;
@@ -516,7 +528,7 @@ k_pcg_tma(PcgArgs<float> a, const __grid_constant__ TmaMaps m, int ti, int tj)
             const float2 part = bsum(qs, sm);
             if (threadIdx.x == 0) pA[blockIdx.x] = part;
         }
-        if (!gsync(a.bar, G, a.status)) return;
+        if (!gsync(a.bar, G, a.status, lim)) return;
         const float fa = ff_div(sigma, ff_add(psum(pA, G, sm), eps8));
 
         // ---- sweep 2: r' = r - alpha A s on the halo, z = M r', x += alpha s
@@ -531,7 +543,7 @@ k_pcg_tma(PcgArgs<float> a, const __grid_constant__ TmaMaps m, int ti, int tj)
                 tma_load_2d(RB, mr_cur, tj0 - 4, ti0 - 2, &bar);
                 if (!first) tma_load_2d(XB, &m.x, tj0, ti0, &bar);
             }
-            if (!load_wait(&bar, phase, a.status)) return;
+            if (!load_wait(&bar, phase, a.status, lim)) return;
             // r' on the tile and its 1-halo
             for (int r = warp; r < L.h1; r += nw) {
                 const int rr = r - 1;
@@ -603,7 +615,7 @@ k_pcg_tma(PcgArgs<float> a, const __grid_constant__ TmaMaps m, int ti, int tj)
             const float2 part = bsum(zr, sm);
             if (threadIdx.x == 0) pB[blockIdx.x] = part;
         }
-        if (!gsync(a.bar, G, a.status)) return;
+        if (!gsync(a.bar, G, a.status, lim)) return;
         const float *rn = (it & 1) ? a.r0 : a.r1;
         const float2 newSigma = psum(pB, G, sm);
         if (chunk_converged(a, [&](long long e) { return __ldcg(rn + e); }, tt, &s_flag)) {
@@ -800,12 +812,13 @@ __device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_re
 
 // Bounded spin of one thread until *p >= target (acquire); false on timeout
 // or when another block reported one.
-__device__ __forceinline__ bool spin_until(const unsigned *p, unsigned target, int *status)
+__device__ __forceinline__ bool spin_until(const unsigned *p, unsigned target, int *status,
+                                           long long lim)
 {
     long long spins = 0;
     while ((int)(ld_acquire_u32(p) - target) < 0) {
         ++spins;
-        if (spins > kSpinLimit || ((spins & 1023) == 0 && *((volatile int *)status) != 0)) {
+        if (spins > lim || ((spins & 1023) == 0 && *((volatile int *)status) != 0)) {
             atomicExch(status, 1);
             return false;
         }
@@ -882,6 +895,7 @@ template <int RPS>
 __global__ void __launch_bounds__(RPS > 0 ? kStripThreads : kThreads, 1)
 k_pcg_resident(PcgArgs<float> a, int ti, int tj)
 {
+    const long long lim = a.spin_limit > 0 ? a.spin_limit : kSpinLimit;
     extern __shared__ unsigned char smem_dyn[];
     __shared__ float smf[64];
     __shared__ float4 s_bcast;
@@ -969,7 +983,7 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
             long long spins = 0;
             bool failed = false;
             while (pending) {
-                if (++spins > kSpinLimit || ((spins & 255) == 0 && *((volatile int *)a.status) != 0)) {
+                if (++spins > lim || ((spins & 255) == 0 && *((volatile int *)a.status) != 0)) {
                     atomicExch(a.status, 1);
                     failed = true;
                     break;
@@ -1023,7 +1037,7 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
         if (threadIdx.x == 0) {
             fence_acq_rel_gpu();
             red_relaxed_add(count, 1u);
-            spin_until(count, nfenced * (unsigned)G, a.status);
+            spin_until(count, nfenced * (unsigned)G, a.status, lim);
         }
         return ok();
     };
@@ -1100,7 +1114,7 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
                 unsigned long long w = ld_ll(p);
                 long long spins = 0;
                 while (ll_epoch(w) != ep) {
-                    if (++spins > kSpinLimit || ((spins & 255) == 0 && *((volatile int *)a.status) != 0)) {
+                    if (++spins > lim || ((spins & 255) == 0 && *((volatile int *)a.status) != 0)) {
                         atomicExch(a.status, 1);
                         break;
                     }

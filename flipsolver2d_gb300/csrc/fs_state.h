@@ -91,7 +91,7 @@ struct Scalars {
     int pcg_status;        // 0 ok, 1 a grid-barrier wait timed out
     int wrap_units;        // a unit row lies on the j = 0 or j = NJ-1 edge
     int nb_overflow;       // NB-FLIP reseeding: more bin-crossing candidates than kept
-    int pad;
+    int nonfinite;         // a particle velocity of a substep was NaN or infinite
 };
 
 // NB-FLIP (nbflipsolver.h:63-66): the grids advected semi-Lagrangian each
@@ -148,6 +148,7 @@ void launch_adjust(const GridDims &d, const SceneParams &sp, const Particles &P,
                    const void *pressure, int pressure_is_double, const Scalars *sc,
                    cudaStream_t st);
 void launch_g2p(const GridDims &d, const SceneParams &sp, const Particles &P, const Grids &G,
+                Scalars *sc,
                 cudaStream_t st);
 void launch_count_erase(const GridDims &d, const SceneParams &sp, Particles &P, const Grids &G,
                         cudaStream_t st);

@@ -22,8 +22,8 @@ HEADER = os.path.join(os.path.dirname(HERE), "include", "fs_gpu.h")
 
 FS_OK = 0
 # fs_status codes (include/fs_gpu.h)
-FS_ERR_BAD_ARG, FS_ERR_CUDA, FS_ERR_OOM, FS_ERR_TIMEOUT, FS_ERR_UNSUPPORTED, FS_ERR_STATE = \
-    range(1, 7)
+FS_ERR_BAD_ARG, FS_ERR_CUDA, FS_ERR_OOM, FS_ERR_TIMEOUT, FS_ERR_UNSUPPORTED, FS_ERR_STATE, \
+    FS_ERR_NONFINITE = range(1, 8)
 FS_PCG_FP32, FS_PCG_FP64, FS_PCG_SPEC = 0, 1, 2
 
 # stage ids (FS_STAGE_*), identical to the oracle's
@@ -56,7 +56,7 @@ class FsError(RuntimeError):
 
 class ExecParams(ctypes.Structure):
     _fields_ = [("pcg_precision", ctypes.c_int), ("pool_threads", ctypes.c_int),
-                ("device", ctypes.c_int), ("reserved", ctypes.c_int * 5)]
+                ("device", ctypes.c_int), ("wait_polls", ctypes.c_int), ("reserved", ctypes.c_int * 4)]
 
 
 _lib: Optional[ctypes.CDLL] = None
@@ -170,11 +170,13 @@ def _ptr(a: np.ndarray):
     return a.ctypes.data_as(ctypes.c_void_p)
 
 
-def exec_params(precision: int = FS_PCG_FP32, pool_threads: int = 0, device: int = 0) -> ExecParams:
+def exec_params(precision: int = FS_PCG_FP32, pool_threads: int = 0, device: int = 0,
+                wait_polls: int = 0) -> ExecParams:
     e = ExecParams()
     e.pcg_precision = precision
     e.pool_threads = pool_threads
     e.device = device
+    e.wait_polls = wait_polls
     return e
 
 
@@ -183,12 +185,12 @@ class GpuFlipSolver:
     NBFlipSolver (nbflipsolver.h:12-78) for scenes of simType "nbflip"."""
 
     def __init__(self, scene, precision: int = FS_PCG_FP32, pool_threads: int = 0,
-                 device: int = 0):
+                 device: int = 0, wait_polls: int = 0):
         self.lib = load()
         self.scene = scene
         self._cp = scene.params.to_c()
         self.ni, self.nj = self._cp.gridSizeI, self._cp.gridSizeJ
-        self._ex = exec_params(precision, pool_threads, device)
+        self._ex = exec_params(precision, pool_threads, device, wait_polls)
         h = ctypes.c_void_p()
         self.nb = getattr(scene, "sim_type", "flip") == "nbflip"
         create = "fs_create_nbflip" if self.nb else "fs_create"
@@ -371,9 +373,10 @@ class GpuLinearSolver:
     arguments and return convention (iteration count; == iterLimit means the
     solve failed)."""
 
-    def __init__(self, precision: int = FS_PCG_FP32, pool_threads: int = 0, device: int = 0):
+    def __init__(self, precision: int = FS_PCG_FP32, pool_threads: int = 0, device: int = 0,
+                 wait_polls: int = 0):
         self.lib = load()
-        self._ex = exec_params(precision, pool_threads, device)
+        self._ex = exec_params(precision, pool_threads, device, wait_polls)
 
     def solve(self, material: np.ndarray, dt: float, density: float, dx: float,
               result: np.ndarray, vec: np.ndarray, iter_limit: int = 20, tol: float = 1e-6) -> int:
@@ -390,11 +393,12 @@ class GpuLinearSolver:
 
 
 def pcg_solve(material: np.ndarray, rhs: np.ndarray, dt: float, density: float, dx: float,
-              iter_limit: int, tol: float, precision: int = FS_PCG_FP32, pool_threads: int = 8):
+              iter_limit: int, tol: float, precision: int = FS_PCG_FP32, pool_threads: int = 8,
+              wait_polls: int = 0):
     """Functional form returning (iterations, solution)."""
     x = np.zeros(material.shape, np.float64)
-    it = GpuLinearSolver(precision, pool_threads).solve(material, dt, density, dx, x, rhs,
-                                                        iter_limit, tol)
+    it = GpuLinearSolver(precision, pool_threads, wait_polls=wait_polls).solve(
+        material, dt, density, dx, x, rhs, iter_limit, tol)
     return it, x
 
 

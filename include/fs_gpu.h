@@ -31,7 +31,10 @@ typedef enum fs_status {
     FS_ERR_OOM = 3,         /* device allocation failed */
     FS_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up */
     FS_ERR_UNSUPPORTED = 5, /* feature outside the supported path */
-    FS_ERR_STATE = 6        /* call not valid in the handle's current state */
+    FS_ERR_STATE = 6,       /* call not valid in the handle's current state */
+    FS_ERR_NONFINITE = 7    /* a substep produced a NaN or infinite particle velocity
+                               (checked on every particle in G2P); the handle's
+                               state is left as the substep made it */
 } fs_status;
 
 /* Field-for-field FlipSolverParameters (flipsolver2d.h:33-56); units and
@@ -82,7 +85,11 @@ typedef struct fs_exec_params {
                           (ThreadPool size, threadpool.cpp:12); 0 = this host's
                           std::thread::hardware_concurrency() like the reference */
     int device;        /* CUDA device ordinal */
-    int reserved[5];
+    int wait_polls;    /* every bounded device-side wait of the PCG kernels (grid
+                          barriers, neighbour hand-offs, TMA completions) gives
+                          up after this many polls and the call returns
+                          FS_ERR_TIMEOUT; 0 = the default, seconds of polling */
+    int reserved[4];
 } fs_exec_params;
 
 /* Stage ids: the calls FlipSolver::step() makes, in order
