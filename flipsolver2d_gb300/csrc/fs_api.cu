@@ -3246,7 +3246,7 @@ extern "C" fs_status fs_cluster_autotune(int ni, int nj, int objective, int devi
 // are busy.  This path calls neither, nor any other allocating routine; it
 // uses only the array below, which is part of the library's device image and
 // so exists, on every device the library is loaded on, before the first call.
-// Its cost for everyone is kNaBytes (about 4.7 MB) of device memory.
+// Its cost for everyone is kNaBytes (about 9 MB) of device memory.
 //
 // Limit: ni * nj <= kNoAllocMaxCells (512 x 512 = 262144 cells), FP32 only,
 // at most kNoAllocMaxParts pool threads.  Larger requests are rejected before
