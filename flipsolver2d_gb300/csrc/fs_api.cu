@@ -2497,12 +2497,17 @@ static fs_status batch_round(fs_batch *b, int *busy)
         BatchScene &bs = b->sc[k];
         CK(cudaStreamWaitEvent(bs.s->st, b->ev_solve, 0));
         CK(cudaGraphLaunch(bs.g[bs.parity][2], bs.s->st));
+        CK(cudaEventRecord(bs.ev, bs.s->st));
         g_kernel_launches += bs.launches[2];
         bs.parity ^= 1;
         bs.s->substeps++;
         bs.s->substeps_total++;
     }
-    CK(cudaDeviceSynchronize());
+    // the round's own work only: each member's last graph (it ends with the
+    // scalars the next CFL step reads) and the merged solves; unrelated work
+    // on the device does not hold the round
+    for (int k : act) CK(cudaEventSynchronize(b->sc[k].ev));
+    CK(cudaEventSynchronize(b->ev_solve));
     for (int w = act.empty() ? 1 : 0; w < 2; w++) {
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, b->ev_t[2 * w], b->ev_t[2 * w + 1]));

@@ -251,6 +251,21 @@ def with_source(sc: Scene, box=(0.15, 0.3, 0.45, 0.6), velocity=(2.0, -1.0),
     return sc
 
 
+def with_viscosity(sc: Scene, viscosity: float = 5.0, heavy: bool = False) -> Scene:
+    """The scene with viscosity on (FlipSolverParameters::viscosityEnabled and
+    useHeavyViscosity, flipsolver2d.h:51-52): its initial fluid carries the
+    particle viscosity `viscosity`, and each substep applies the light or the
+    heavy model (viscositymodel.cpp) after the pressure projection and
+    projects again."""
+    sc.params.viscosityEnabled = True
+    sc.params.useHeavyViscosity = bool(heavy)
+    for o in sc.objects:
+        if o.kind == "fluid":
+            o.viscosity = float(viscosity)
+    sc.name += "_viscous_heavy" if heavy else "_viscous"
+    return sc
+
+
 def random_scene(side: int, seed: int, ppc: int = 4, **overrides) -> Scene:
     """Randomised scene used by the parity tests and the batched workload:
     fluid box corners uniform in [0.1, 0.9] m, 1-3 convex solids of 4-8

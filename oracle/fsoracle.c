@@ -367,6 +367,7 @@ struct fso_solver {
     int nb;
     float *adv_u, *adv_v, *adv_sdf, *adv_visc;
     int density_iters, pressure_iters, substeps;
+    int viscosity_iters; /* SolverStats::viscosityIterations */
     int ref_threads, host_threads;
     pool *pool;
 };
@@ -1568,6 +1569,331 @@ static void project(fso_solver *s) /* :93-126 */
     apply_pressure(s, s->pres);
 }
 
+/* ---- viscosity (viscositymodel.cpp) ---------------------------------- */
+/* The reference assembles its viscosity systems with Eigen::SparseMatrix::
+ * coeffRef and solves them with Eigen::ConjugateGradient<..., Eigen::Upper>
+ * and Eigen's default diagonal preconditioner (viscositymodel.h:21).  Eigen
+ * (3.4.0, a pinned dependency) is absent here: the reference build compiles
+ * against oracle/refshim/Eigen, whose matrix stores entries per row in column
+ * order and whose conjugate gradient restates Eigen's published algorithm.
+ * This is the same assembly and the same solver, operation for operation. */
+typedef struct vrow {
+    long *col;
+    double *val;
+    int n, cap;
+} vrow;
+
+/* coeffRef(r, c): the entry, created as 0 in column order when absent */
+static double *vrow_ref(vrow *row, long c)
+{
+    int k = 0;
+    while (k < row->n && row->col[k] < c) k++;
+    if (k < row->n && row->col[k] == c) return &row->val[k];
+    if (row->n == row->cap) {
+        row->cap = row->cap ? 2 * row->cap : 8;
+        row->col = (long *)realloc(row->col, (size_t)row->cap * sizeof(long));
+        row->val = (double *)realloc(row->val, (size_t)row->cap * sizeof(double));
+    }
+    memmove(row->col + k + 1, row->col + k, (size_t)(row->n - k) * sizeof(long));
+    memmove(row->val + k + 1, row->val + k, (size_t)(row->n - k) * sizeof(double));
+    row->col[k] = c;
+    row->val[k] = 0.0;
+    row->n++;
+    return &row->val[k];
+}
+
+static void vrows_free(vrow *rows, long n)
+{
+    for (long r = 0; r < n; r++) {
+        free(rows[r].col);
+        free(rows[r].val);
+    }
+    free(rows);
+}
+
+/* ConjugateGradient<SparseMatrix<double>, Upper>::compute then solve: the
+ * matrix acts as the self-adjoint matrix of its upper triangle; Jacobi
+ * preconditioner (1 / diagonal, 1 where the diagonal is zero or absent);
+ * x0 = 0; stop when ||r||^2 < max(tol^2 ||b||^2, DBL_MIN) or after 2n
+ * iterations.  Returns the iteration count; *ok is Eigen's Success test
+ * sqrt(||r||^2 / ||b||^2) <= tol. */
+static double visc_dot(const double *a, const double *b, long n)
+{
+    double s = 0.0;
+    for (long k = 0; k < n; k++) s += a[k] * b[k];
+    return s;
+}
+
+static void vapply(const vrow *rows, long n, const double *x, double *y)
+{
+    for (long k = 0; k < n; k++) y[k] = 0.0;
+    for (long r = 0; r < n; r++) {
+        double acc = 0.0;
+        for (int e = 0; e < rows[r].n; e++) {
+            const long c = rows[r].col[e];
+            if (c < r) continue; /* the lower triangle is not read */
+            acc += rows[r].val[e] * x[c];
+            if (c != r) y[c] += rows[r].val[e] * x[r];
+        }
+        y[r] += acc;
+    }
+}
+
+static long vcg_solve(const vrow *rows, long n, double tol, const double *b, double *x, int *ok)
+{
+    double *invdiag = (double *)malloc((size_t)n * sizeof(double));
+    double *r = (double *)malloc((size_t)n * sizeof(double)), *p = (double *)malloc((size_t)n * sizeof(double));
+    double *z = (double *)malloc((size_t)n * sizeof(double)), *t = (double *)malloc((size_t)n * sizeof(double));
+    for (long k = 0; k < n; k++) {
+        invdiag[k] = 1.0;
+        for (int e = 0; e < rows[k].n; e++)
+            if (rows[k].col[e] == k && rows[k].val[e] != 0.0) invdiag[k] = 1.0 / rows[k].val[e];
+        x[k] = 0.0;
+        r[k] = b[k];
+    }
+    long iters = 0;
+    double err = 0.0;
+    const double rhsNorm2 = visc_dot(b, b, n);
+    if (rhsNorm2 == 0.0) {
+        *ok = 1;
+        goto done;
+    }
+    {
+        const double threshold = fmax(tol * tol * rhsNorm2, DBL_MIN);
+        double residualNorm2 = visc_dot(r, r, n);
+        if (residualNorm2 < threshold) {
+            err = sqrt(residualNorm2 / rhsNorm2);
+            *ok = err <= tol;
+            goto done;
+        }
+        for (long k = 0; k < n; k++) p[k] = invdiag[k] * r[k];
+        double absNew = visc_dot(r, p, n);
+        long i = 0;
+        while (i < 2 * n) {
+            vapply(rows, n, p, t);
+            const double alpha = absNew / visc_dot(p, t, n);
+            for (long k = 0; k < n; k++) x[k] += alpha * p[k];
+            for (long k = 0; k < n; k++) r[k] -= alpha * t[k];
+            residualNorm2 = visc_dot(r, r, n);
+            if (residualNorm2 < threshold) break;
+            for (long k = 0; k < n; k++) z[k] = invdiag[k] * r[k];
+            const double absOld = absNew;
+            absNew = visc_dot(r, z, n);
+            const double beta = absNew / absOld;
+            for (long k = 0; k < n; k++) p[k] = z[k] + beta * p[k];
+            i++;
+        }
+        err = sqrt(residualNorm2 / rhsNorm2);
+        iters = i;
+        *ok = err <= tol;
+    }
+done:
+    free(invdiag);
+    free(r);
+    free(p);
+    free(z);
+    free(t);
+    return iters;
+}
+
+/* Grid2d::at of the viscosity grid: an unchecked read in the reference; the
+ * out-of-grid reads it makes are never stored, so any value serves */
+static inline float visc_at(const fso_solver *s, long i, long j)
+{
+    i = i < 0 ? 0 : (i >= s->ni ? s->ni - 1 : i);
+    j = j < 0 ? 0 : (j >= s->nj ? s->nj - 1 : j);
+    return s->visc_grid[i * s->nj + j];
+}
+
+/* LightViscosityModel::apply (viscositymodel.cpp:4-63) with getMatrix
+ * (:65-135), fillRhs (:137-148) and applyResult (:150-161): one system on
+ * the NI x NJ cells, solved for U (rows 0..NI-1 of the U grid) and then for V
+ * (columns 0..NJ-1 of the V grid).  The tolerance is 1e-4.  Returns the V
+ * solve's iteration count, or -1 when a solve fails (the reference returns
+ * without applying that solve). */
+static int viscosity_light(fso_solver *s)
+{
+    const long NI = s->ni, NJ = s->nj, N = NI * NJ;
+    const float dt = s->step_dt;
+    const float density = (float)s->p.fluidDensity;
+    const double scale = dt;
+    vrow *rows = (vrow *)calloc((size_t)N, sizeof(vrow));
+    for (long i = 0; i < NI; i++) {
+        for (long j = 0; j < NJ; j++) {
+            const long idx = i * NJ + j;
+            double diag = 4.0, ip1 = 1.0, jp1 = 1.0, im1 = 1.0, jm1 = 1.0;
+            if (is_solid(s, i, j)) {
+                *vrow_ref(&rows[idx], idx) = 1.0;
+                continue;
+            }
+            ip1 *= (double)(is_solid(s, i + 1, j) ? visc_at(s, i, j) : visc_at(s, i + 1, j)) * scale;
+            jp1 *= (double)(is_solid(s, i, j + 1) ? visc_at(s, i, j) : visc_at(s, i, j + 1)) * scale;
+            im1 *= (double)(is_solid(s, i - 1, j) ? visc_at(s, i, j) : visc_at(s, i - 1, j)) * scale;
+            jm1 *= (double)(is_solid(s, i, j - 1) ? visc_at(s, i, j) : visc_at(s, i, j - 1)) * scale;
+            diag *= (double)visc_at(s, i, j) * scale;
+            diag += 1.;
+            *vrow_ref(&rows[idx], idx) = diag;
+            if (i + 1 < NI) {
+                *vrow_ref(&rows[idx], idx + NJ) = ip1;
+                *vrow_ref(&rows[idx + NJ], idx) = ip1;
+            }
+            if (j + 1 < NJ) {
+                *vrow_ref(&rows[idx], idx + 1) = jp1;
+                *vrow_ref(&rows[idx + 1], idx) = jp1;
+            }
+            if (i - 1 >= 0) {
+                *vrow_ref(&rows[idx], idx - NJ) = im1;
+                *vrow_ref(&rows[idx - NJ], idx) = im1;
+            }
+            if (j - 1 >= 0) {
+                *vrow_ref(&rows[idx], idx - 1) = jm1;
+                *vrow_ref(&rows[idx - 1], idx) = jm1;
+            }
+        }
+    }
+    double *b = (double *)calloc((size_t)N, sizeof(double)), *x = (double *)calloc((size_t)N, sizeof(double));
+    int ok = 0;
+    long iters = -1;
+    for (long k = 0; k < N; k++) b[k] = (double)(density * s->u[(k / NJ) * NJ + k % NJ]);
+    vcg_solve(rows, N, 1e-4, b, x, &ok);
+    if (ok) {
+        for (long k = 0; k < N; k++) s->u[(k / NJ) * NJ + k % NJ] = (float)(x[k] / (double)density);
+        for (long k = 0; k < N; k++) b[k] = (double)(density * s->v[(k / NJ) * (NJ + 1) + k % NJ]);
+        iters = vcg_solve(rows, N, 1e-4, b, x, &ok);
+        if (ok) {
+            for (long k = 0; k < N; k++) s->v[(k / NJ) * (NJ + 1) + k % NJ] = (float)(x[k] / (double)density);
+        } else {
+            iters = -1;
+        }
+    }
+    free(b);
+    free(x);
+    vrows_free(rows, N);
+    return (int)iters;
+}
+
+/* HeavyViscosityModel::apply (viscositymodel.cpp:164-200) with getMatrix
+ * (:202-402), getRhs (:404-434) and applyResult (:436-469): one coupled
+ * system over every U face then every V face.  Each entry accumulates
+ * (coeffRef +=) the terms of its own row in the reference's order; float
+ * products, double sums.  The viscosity at a face corner is
+ * Grid2d::interpolateAt with the grid's (0.5, 0.5) offset.  The column
+ * uIpOneJmOneLinearIdx is a V-grid linear index used in the U range, as in
+ * the reference (:383, :395).  Tolerance 1e-4; returns the iteration count or
+ * -1 when the solve fails (nothing applied). */
+static inline long u_index(const fso_solver *s, long i, long j) /* U: (NI+1) x NJ */
+{
+    return (i < 0 || i > s->ni || j < 0 || j >= s->nj) ? -1 : i * s->nj + j;
+}
+static inline long v_index(const fso_solver *s, long i, long j) /* V: NI x (NJ+1) */
+{
+    return (i < 0 || i >= s->ni || j < 0 || j > s->nj) ? -1 : i * (s->nj + 1) + j;
+}
+static inline float visc_get(const fso_solver *s, long i, long j) /* getAt, OOB_EXTEND */
+{
+    return visc_at(s, i, j);
+}
+static inline float visc_interp(const fso_solver *s, float i, float j)
+{
+    return grid_lerp(s->visc_grid, (int)s->ni, (int)s->nj, 0.5f, 0.5f, i, j);
+}
+
+static int viscosity_heavy(fso_solver *s)
+{
+    const long NI = s->ni, NJ = s->nj;
+    const long NU = (NI + 1) * NJ, NV = NI * (NJ + 1), N = NU + NV;
+    const float dt = s->step_dt, dx = (float)s->p.dx;
+    const float density = (float)s->p.fluidDensity;
+    const float scaleTwoDt = 2 * dt / (dx * dx);
+    const float scaleTwoDx = dt / (2 * dx * dx);
+    const long vb = NU;
+    vrow *rows = (vrow *)calloc((size_t)N, sizeof(vrow));
+#define A(r, c) (*vrow_ref(&rows[(r)], (c)))
+    for (long i = 0; i < NI + 1; i++) {
+        for (long j = 0; j < NJ + 1; j++) {
+            const long idxU = u_index(s, i, j), idxV = v_index(s, i, j);
+            const float fi = (float)i, fj = (float)j;
+            if (idxU != -1) {
+                A(idxU, idxU) += density;
+                const long uim1 = u_index(s, i - 1, j);
+                if (uim1 != -1) {
+                    A(idxU, uim1) += -scaleTwoDt * visc_get(s, i - 1, j);
+                    A(idxU, idxU) += scaleTwoDt * visc_get(s, i - 1, j);
+                }
+                const long uip1 = u_index(s, i + 1, j);
+                if (uip1 != -1) {
+                    A(idxU, uip1) += -scaleTwoDt * visc_get(s, i, j);
+                    A(idxU, idxU) += scaleTwoDt * visc_get(s, i, j);
+                }
+                const long ujm1 = u_index(s, i, j - 1), vim1 = v_index(s, i - 1, j);
+                if (ujm1 != -1 && idxV != -1 && vim1 != -1) {
+                    const float lv = visc_interp(s, fi - 0.5f, fj - 0.5f);
+                    A(idxU, ujm1) += -scaleTwoDx * lv;
+                    A(idxU, vb + idxV) += scaleTwoDx * lv;
+                    A(idxU, vb + vim1) += -scaleTwoDx * lv;
+                    A(idxU, idxU) += scaleTwoDx * lv;
+                }
+                const long ujp1 = u_index(s, i, j + 1), vjp1 = v_index(s, i, j + 1);
+                const long vim1jp1 = v_index(s, i - 1, j + 1);
+                if (ujp1 != -1 && vjp1 != -1 && vim1jp1 != -1) {
+                    const float lv = visc_interp(s, fi - 0.5f, fj + 0.5f);
+                    A(idxU, ujp1) += -scaleTwoDx * lv;
+                    A(idxU, vb + vjp1) += -scaleTwoDx * lv;
+                    A(idxU, vb + vim1jp1) += scaleTwoDx * lv;
+                    A(idxU, idxU) += scaleTwoDx * lv;
+                }
+            }
+            if (idxV != -1) {
+                const long r = vb + idxV;
+                A(r, r) += density;
+                const long vjm1 = v_index(s, i, j - 1);
+                if (vjm1 != -1) {
+                    A(r, vb + vjm1) += -scaleTwoDt * visc_get(s, i, j - 1);
+                    A(r, r) += scaleTwoDt * visc_get(s, i, j - 1);
+                }
+                const long vjp1 = v_index(s, i, j + 1);
+                if (vjp1 != -1) {
+                    A(r, vb + vjp1) += -scaleTwoDt * visc_get(s, i, j);
+                    A(r, r) += scaleTwoDt * visc_get(s, i, j);
+                }
+                const long ujm1 = u_index(s, i, j - 1), vim1 = v_index(s, i - 1, j);
+                if (idxU != -1 && ujm1 != -1 && vim1 != -1) {
+                    const float lv = visc_interp(s, fi - 0.5f, fj - 0.5f);
+                    A(r, idxU) += scaleTwoDx * lv;
+                    A(r, ujm1) += -scaleTwoDx * lv;
+                    A(r, vb + vim1) += -scaleTwoDx * lv;
+                    A(r, r) += scaleTwoDx * lv;
+                }
+                const long uip1 = u_index(s, i + 1, j), uip1jm1 = v_index(s, i + 1, j - 1);
+                const long vip1 = v_index(s, i + 1, j);
+                if (uip1 != -1 && uip1jm1 != -1 && vip1 != -1) {
+                    const float lv = visc_interp(s, fi + 0.5f, fj - 0.5f);
+                    A(r, uip1) += -scaleTwoDx * lv;
+                    A(r, uip1jm1) += scaleTwoDx * lv;
+                    A(r, vb + vip1) += -scaleTwoDx * lv;
+                    A(r, r) += scaleTwoDx * lv;
+                }
+            }
+        }
+    }
+#undef A
+    double *b = (double *)calloc((size_t)N, sizeof(double)), *x = (double *)calloc((size_t)N, sizeof(double));
+    for (long k = 0; k < NU; k++) b[k] = (double)(density * s->u[k]);
+    for (long k = 0; k < NV; k++) b[vb + k] = (double)(density * s->v[k]);
+    int ok = 0;
+    long iters = vcg_solve(rows, N, 1e-4, b, x, &ok);
+    if (ok) {
+        for (long k = 0; k < NU; k++) s->u[k] = (float)x[k];
+        for (long k = 0; k < NV; k++) s->v[k] = (float)x[vb + k];
+    } else {
+        iters = -1;
+    }
+    free(b);
+    free(x);
+    vrows_free(rows, N);
+    return (int)iters;
+}
+
 static void friction(fso_solver *s) /* :1077-1104, validSolidNeighborIds :766-786 */
 {
     const long NJ = s->nj, NV = s->nj + 1;
@@ -1933,6 +2259,9 @@ static int run_stage(fso_solver *s, int stage)
         break;
     case FSO_DENSITY_GRID: update_density_grid(s); break;
     case FSO_LEVELSET_OUTSIDE: bfs_extrapolate(s->fluid_sdf, NULL, s->ni, s->nj, 2, 0); break;
+    case FSO_VISCOSITY: /* FlipSolver::applyViscosity, flipsolver2d.cpp:128-136 */
+        s->viscosity_iters = s->p.useHeavyViscosity ? viscosity_heavy(s) : viscosity_light(s);
+        break;
     default: return -1;
     }
     return 0;
@@ -1949,11 +2278,17 @@ static void step(fso_solver *s) /* FlipSolver::step, flipsolver2d.cpp:412-462 */
                                    FSO_SDF, FSO_LEVELSET_OUTSIDE, FSO_AFTER_TRANSFER, FSO_LEVELSET,
                                    FSO_MATERIALS, FSO_BODY_FORCES, FSO_DECOMPOSITION, FSO_PROJECT,
                                    FSO_FRICTION, FSO_VEL_EXTRAP, FSO_G2P, FSO_COUNT, FSO_RESEED};
-    if (s->nb) {
-        for (size_t k = 0; k < sizeof(nb_order) / sizeof(nb_order[0]); k++) run_stage(s, nb_order[k]);
-        return;
+    const int *ord = s->nb ? nb_order : order;
+    const size_t n = s->nb ? sizeof(nb_order) / sizeof(nb_order[0]) : sizeof(order) / sizeof(order[0]);
+    for (size_t k = 0; k < n; k++) {
+        run_stage(s, ord[k]);
+        /* with viscosity on, both steps apply it after the friction update
+         * and project again (flipsolver2d.cpp:448-454, nbflipsolver.cpp:50-56) */
+        if (ord[k] == FSO_FRICTION && s->p.viscosityEnabled) {
+            run_stage(s, FSO_VISCOSITY);
+            run_stage(s, FSO_PROJECT);
+        }
     }
-    for (size_t k = 0; k < sizeof(order) / sizeof(order[0]); k++) run_stage(s, order[k]);
 }
 
 void fso_step(fso_solver *s)
@@ -2123,6 +2458,7 @@ int fso_stat(fso_solver *s, int which)
     case FSO_S_SUBSTEPS: return s->substeps;
     case FSO_S_FRAME: return s->frame;
     case FSO_S_POOL_THREADS: return s->ref_threads;
+    case FSO_S_VISCOSITY_ITERS: return s->viscosity_iters;
     default: return -1;
     }
 }

@@ -78,7 +78,8 @@ enum fso_stage {
     FSO_RESEED = 16,       /* reseedParticles()                          :460 */
     FSO_DENSITY_GRID = 17, /* updateDensityGrid() alone                  :166 */
     FSO_LEVELSET_OUTSIDE = 18, /* extrapolateLevelsetOutside(m_fluidSdf)  :1496-1558 */
-    FSO_STAGE_COUNT = 19
+    FSO_VISCOSITY = 19,    /* applyViscosity(): the light or heavy model :128-136 */
+    FSO_STAGE_COUNT = 20
 };
 
 /* NB-FLIP (NBFlipSolver, nbflipsolver.cpp) runs the same stage ids; four of
@@ -130,7 +131,8 @@ enum fso_stat {
     FSO_S_PRESSURE_ITERS = 1,  /* iterations of the last pressure solve   */
     FSO_S_SUBSTEPS = 2,        /* substeps of the last stepFrame          */
     FSO_S_FRAME = 3,           /* frame number                            */
-    FSO_S_POOL_THREADS = 4     /* chunk count used by the vector kernels  */
+    FSO_S_POOL_THREADS = 4,    /* chunk count used by the vector kernels  */
+    FSO_S_VISCOSITY_ITERS = 5  /* the viscosity model's return value      */
 };
 
 typedef struct fso_solver fso_solver;

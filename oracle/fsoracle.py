@@ -25,7 +25,7 @@ PORT_LIB = os.path.join(HERE, "_build", "libfsoracle.so")
 # stage ids (fsoracle.h enum fso_stage)
 ADVECT, DECOMPOSITION, REBIN, DENSITY, P2G, SDF, MATERIALS, AFTER_TRANSFER, LEVELSET, \
     VEL_EXTRAP, SAVE_GRID, BODY_FORCES, PROJECT, FRICTION, G2P, COUNT, RESEED, \
-    DENSITY_GRID, LEVELSET_OUTSIDE = range(19)
+    DENSITY_GRID, LEVELSET_OUTSIDE, VISCOSITY = range(20)
 
 # the order in which FlipSolver::step() (flipsolver2d.cpp:412-462) runs them
 STEP_STAGES = [ADVECT, DECOMPOSITION, REBIN, DENSITY, P2G, SDF, MATERIALS, AFTER_TRANSFER,

@@ -123,6 +123,7 @@ public:
         case FSO_COUNT: this->countParticles(); break;
         case FSO_RESEED: this->reseedParticles(); break;
         case FSO_DENSITY_GRID: this->updateDensityGrid(); break;
+        case FSO_VISCOSITY: this->applyViscosity(); break;
         default: break;
         }
     }
@@ -173,6 +174,7 @@ public:
         case FSO_S_SUBSTEPS: return m_stats.substepCount();
         case FSO_S_FRAME: return this->frameNumber();
         case FSO_S_POOL_THREADS: return static_cast<int>(ThreadPool::i()->threadCount());
+        case FSO_S_VISCOSITY_ITERS: return m_stats.viscosityIterations();
         default: return -1;
         }
     }

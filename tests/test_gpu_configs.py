@@ -101,8 +101,11 @@ def test_substep_stages_at_configured_size(port_lib, gpu_lib, name, monkeypatch)
     g = gpu.GpuFlipSolver(sc, precision=gpu.FS_PCG_FP64, pool_threads=POOL_THREADS)
     g.first_frame_init()
     # the FP64 pressures: the reference recurrence with the dot products
-    # summed in another order, over 200 unconverged iterations at these sizes
-    check_stages(o, g, gpu.FS_PCG_FP64, pcg_bar=1e-6)
+    # summed in another order, over 200 unconverged iterations -- chaotic at
+    # these sizes (at the 128^2 state a 1e-15 change of b moves the oracle's
+    # own density pressure by 1e-2, and its relative residual is 8.4)
+    dx = sc.params.grid()[0]
+    check_stages(o, g, gpu.FS_PCG_FP64, chaotic=(dx, sc.params.fluidDensity, sc.params.pcgIterLimit))
     g.close()
     o.close()
 
@@ -122,8 +125,7 @@ def substep(sc, snap, precision):
 @pytest.mark.parametrize("warm_substeps", [3, 5])
 def test_fp32_substep_against_fp64_at_c2(gpu_lib, warm_substeps):
     sc, snap = warm_state("c2_dam_1024", warm_substeps)
-    n = sc.params.gridSizeI
-    dx, dt = 1.0 / n, snap["dt"]
+    dx, dt = sc.params.grid()[0], snap["dt"]
     mat = snap["material"]  # the operator of this substep's solves
     d = substep(sc, snap, gpu.FS_PCG_FP64)
     f = substep(sc, snap, gpu.FS_PCG_FP32)

@@ -88,12 +88,20 @@ def test_stages_from_identical_snapshots(scene, precision):
     check_stages(o, g, precision)
 
 
-def check_stages(o, g, precision, pcg_bar=1e-9):
+def check_stages(o, g, precision, pcg_bar=1e-9, chaotic=None):
     """Runs every stage of FlipSolver::step on the oracle `o` and the GPU
     handle `g`, each stage started from the oracle's current state, and
     checks the bars of the module docstring.  pcg_bar is the relative-L2 bar
     of the FP64-mode pressures (the reference recurrence with the dot
-    products summed in another order)."""
+    products summed in another order).
+
+    chaotic = (dx, density, limit) switches the two solves' FP64 bars for
+    states where the reference's unconverged 200-iteration recurrence
+    amplifies rounding (the oracle's own result moves by 1e-2 under a 1e-15
+    change of b): the iteration count, the bit-exact right-hand side and the
+    validity grids stay, the pressure keeps a true relative residual within
+    1.05x of the oracle's, the density push (skipped at the iteration limit)
+    stays bit-exact, and the projected velocities stay within 5e-2."""
     g.restore(o.snapshot())
 
     def resync():
@@ -105,6 +113,7 @@ def check_stages(o, g, precision, pcg_bar=1e-9):
     assert_particles_equal(o.get_particles(), g.get_particles(), what="advect")
     o.stage(fo.DECOMPOSITION)
     g.stage(gpu.DECOMPOSITION)
+    mat_dec = o.get_grid("material")  # the operator of this substep's solves
     o.stage(fo.REBIN)
     g.stage(gpu.REBIN)
     assert_particles_equal(o.get_particles(), g.get_particles(), what="rebin")
@@ -122,7 +131,19 @@ def check_stages(o, g, precision, pcg_bar=1e-9):
     it_o = o.stat(0)
     it_g = g.stat(0)
     po, pg = o.get_grid("density_pressure"), g.get_grid("density_pressure")
-    if precision == gpu.FS_PCG_FP64:
+    def rel_residual(x, rhs):
+        from test_gpu_pcg import apply_a
+
+        dx, density, _ = chaotic
+        return np.linalg.norm(rhs - apply_a(mat_dec, x, o.dt, density, dx)) / max(np.linalg.norm(rhs), 1e-300)
+
+    if precision == gpu.FS_PCG_FP64 and chaotic:
+        assert it_o == it_g
+        rhs = o.get_grid("density_rhs")
+        assert rel_residual(pg, rhs) <= 1.05 * rel_residual(po, rhs) + 1e-6
+        if it_o >= chaotic[2]:  # densityCorrection skips the push (flipsolver2d.cpp:179-182)
+            assert_particles_equal(o.get_particles(), g.get_particles(), what="density push skipped")
+    elif precision == gpu.FS_PCG_FP64:
         assert it_o == it_g
         assert rel_l2(pg, po) <= pcg_bar
         a, b = o.get_particles(), g.get_particles()
@@ -162,7 +183,16 @@ def check_stages(o, g, precision, pcg_bar=1e-9):
     o.stage(fo.PROJECT)
     g.stage(gpu.PROJECT)
     po, pg = o.get_grid("pressure"), g.get_grid("pressure")
-    if precision == gpu.FS_PCG_FP64:
+    if precision == gpu.FS_PCG_FP64 and chaotic:
+        assert_grid_equal(o, g, "pressure_rhs", "pressure rhs")
+        assert o.stat(1) == g.stat(1)
+        rhs = o.get_grid("pressure_rhs")
+        assert rel_residual(pg, rhs) <= 1.05 * rel_residual(po, rhs) + 1e-6
+        for name in ["u", "v"]:
+            assert rel_l2(g.get_grid(name), o.get_grid(name)) <= 5e-2, name
+        for name in ["u_valid", "v_valid"]:
+            assert_grid_equal(o, g, name, "projection validity")
+    elif precision == gpu.FS_PCG_FP64:
         assert_grid_equal(o, g, "pressure_rhs", "pressure rhs")
         assert o.stat(1) == g.stat(1)
         assert rel_l2(pg, po) <= pcg_bar

@@ -34,6 +34,10 @@ PIN_SCENES = {
     "nb_dam44_source": lambda: scenes.with_source(scenes.nb_dam_break(44, seed=6), transfer=False,
                                                   box=(0.2, 0.35, 0.5, 0.7), viscosity=2.0),
     "nb_dam44_source_transfer": lambda: scenes.with_source(scenes.nb_dam_break(44, seed=6)),
+    # viscosity: the light and heavy models (viscositymodel.cpp), FLIP and NB-FLIP
+    "dam32_viscous": lambda: scenes.with_viscosity(scenes.dam_break(32, seed=42), 5.0),
+    "dam32_viscous_heavy": lambda: scenes.with_viscosity(scenes.dam_break(32, seed=42), 5.0, heavy=True),
+    "nb_dam40_viscous": lambda: scenes.with_viscosity(scenes.nb_dam_break(40, seed=7), 10.0),
     # a ragged grid, a sink that kills particles, a scene without fluid
     **EDGE_SCENES,
 }
