@@ -509,6 +509,8 @@ def gpu_arm(args):
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
+    if args.profile_timed:  # ncu --profile-from-start off sees the timed substeps only
+        torch.cuda.profiler.start()
     work, step_ms, pcg_ms, iters, bytes_pcg = 0, [], 0.0, [], 0.0
     launches = 0.0
     for _ in range(args.steps):
@@ -526,6 +528,8 @@ def gpu_arm(args):
         # + 34 B per cell-iteration (FP32 x, r, s and the u8 operator row)
         bytes_pcg += ncell * (2 * 16 + 34 * (itd + itp))
     torch.cuda.synchronize()
+    if args.profile_timed:
+        torch.cuda.profiler.stop()
     clocks = sampler.stop()
     s.enable_timers(False)
     total_ms, work = combine_replicas(float(sum(step_ms)), work, dist, f"cuda:{local}")
@@ -1169,6 +1173,9 @@ def main():
                     help="NB-FLIP (NBFlipSolver) substeps of the narrow-band dam break at --res")
     ap.add_argument("--serve", type=int, default=0,
                     help="serve R requests of the seeded request stream instead")
+    ap.add_argument("--profile-timed", action="store_true",
+                    help="bracket the timed substeps with cudaProfilerStart/Stop, for "
+                         "ncu --profile-from-start off")
     ap.add_argument("--single-sample", type=int, default=32,
                     help="scenes stepped one at a time for the single-scene figure of --batch")
     args = ap.parse_args()

@@ -32,6 +32,7 @@ UNITS = {
     "fs_pcg_tma.cu": ["-fmad=true"],
     "fs_spec.cu": ["-fmad=true"],
     "fs_cluster.cu": ["-fmad=true"],
+    "fs_viscosity.cu": ["-fmad=false"],
 }
 
 

@@ -35,6 +35,7 @@
 #include "fs_pcg_tma.h"
 #include "fs_spec.h"
 #include "fs_state.h"
+#include "fs_viscosity.h"
 
 using namespace fsg;
 
@@ -222,8 +223,13 @@ struct fs_solver {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     // per-stage timing (timers on): events after each group of stages, and
     // the accumulated milliseconds per SolverStage (flipsolver2d.h:58-72)
-    cudaEvent_t stage_ev[8] = {};
+    cudaEvent_t stage_ev[10] = {};
+    int stage_of[10] = {};   // the SolverStage each recorded event ends
     double t_stage_ms[12] = {};
+    // viscosity (FlipSolverParameters::viscosityEnabled): the model's system
+    // and solver buffers, and its return value of the last substep
+    ViscBuffers visc;
+    int visc_iters = 0;
     // PCG timing events per solve of a substep (0 density, 1 pressure); read
     // after the substep so that timing adds no host wait inside it
     cudaEvent_t p0[2] = {nullptr, nullptr}, p1[2] = {nullptr, nullptr};
@@ -372,8 +378,6 @@ static fs_status create_impl(const fs_params *p, const fs_exec_params *exec, boo
         return fail(FS_ERR_BAD_ARG, "fs_create: invalid parameters");
     if ((long long)p->gridSizeI * p->gridSizeJ > (1LL << 30))
         return fail(FS_ERR_BAD_ARG, "fs_create: grid too large");
-    if (p->viscosityEnabled)
-        return fail(FS_ERR_UNSUPPORTED, "fs_create: viscosity is not part of this path");
     // SIMULATION_LIQUID, or SIMULATION_NBFLIP for the narrow-band solver
     if (p->simulationMethod != 0 && !(nb && p->simulationMethod == 3))
         return fail(FS_ERR_UNSUPPORTED, "fs_create: only the liquid solvers are supported");
@@ -482,6 +486,19 @@ static fs_status create_impl(const fs_params *p, const fs_exec_params *exec, boo
     A(dalloc(s, &s->sc, 1));
     if (cudaMallocHost(&s->sc_host, sizeof(Scalars)) != cudaSuccess)
         return cleanup(fail(FS_ERR_OOM, "fs_create: pinned allocation failed"));
+    if (p->viscosityEnabled) { // the light or heavy model's system (viscositymodel.cpp)
+        ViscBuffers &V = s->visc;
+        const bool heavy = p->useHeavyViscosity != 0;
+        V.n = visc_unknowns(d, heavy);
+        V.ncoef = visc_coef_count(d, heavy);
+        double **vv[] = {&V.b, &V.x, &V.r, &V.p, &V.t, &V.invdiag};
+        for (double **q : vv) A(dalloc(s, q, (size_t)V.n));
+        A(dalloc(s, &V.coef, (size_t)V.ncoef));
+        A(dalloc(s, &V.part, (size_t)3 * kViscBlocksMax));
+        A(dalloc(s, &V.ctl, 1));
+        if (cudaMallocHost(&V.ctl_host, sizeof(ViscCtl)) != cudaSuccess)
+            return cleanup(fail(FS_ERR_OOM, "fs_create: pinned allocation failed"));
+    }
     // PCG vectors
     const size_t vb = n * s->esz;
     void **vecs[] = {&s->dens_rhs, &s->dens_x, &s->pres_rhs, &s->pres_x, &s->r0, &s->r1, &s->s0, &s->s1};
@@ -727,6 +744,7 @@ extern "C" fs_status fs_destroy(fs_solver *s)
     if (s->side) cudaStreamSynchronize(s->side);
     for (void *q : s->allocs) cudaFree(q);
     if (s->sc_host) cudaFreeHost(s->sc_host);
+    if (s->visc.ctl_host) cudaFreeHost(s->visc.ctl_host);
     cudaEvent_t evs[] = {s->ev_p2g, s->ev_levelset, s->e0, s->e1, s->p0[0], s->p1[0], s->p0[1], s->p1[1]};
     for (cudaEvent_t e : evs)
         if (e) cudaEventDestroy(e);
@@ -1254,6 +1272,20 @@ static fs_status stage(fs_solver *s, int which, bool in_step)
         launch_count_erase(d, s->sp, s->P, s->G, q);
         g_kernel_launches += 1;
         break;
+    case FS_STAGE_VISCOSITY: { // FlipSolver::applyViscosity (flipsolver2d.cpp:128-136)
+        if (!s->sp.viscosityEnabled)
+            return fail(FS_ERR_STATE, "FS_STAGE_VISCOSITY: the handle was created without viscosity");
+        long long launched = 0;
+        const cudaError_t e =
+            s->p.useHeavyViscosity
+                ? visc_heavy(d, s->G, s->step_dt, (float)s->p.dx, (float)s->sp.fluidDensity, s->visc, q,
+                             &s->visc_iters, &launched)
+                : visc_light(d, s->G, s->step_dt, (float)s->sp.fluidDensity, s->visc, q, &s->visc_iters,
+                             &launched);
+        g_kernel_launches += launched;
+        if (e != cudaSuccess) return fail(FS_ERR_CUDA, "viscosity: %s", cudaGetErrorString(e));
+        break;
+    }
     default:
         return fail(FS_ERR_BAD_ARG, "unknown stage %d", which);
     }
@@ -1261,39 +1293,46 @@ static fs_status stage(fs_solver *s, int which, bool in_step)
     return FS_OK;
 }
 
-// SolverStage indices (flipsolver2d.h:58-72) of the timed stage groups, in
-// the order step() ends them (flipsolver2d.cpp:412-462): advect;
+// Timed stage groups end with mark(SolverStage index, flipsolver2d.h:58-72)
+// in the order step() ends them (flipsolver2d.cpp:412-462): advect;
 // decomposition; prune + rebin; density correction; grid update (P2G, SDF
 // and materials, fused here); after transfer (level set, extrapolation,
-// saved grid, body forces); pressure; particle update (friction is in the
-// pressure apply here, then extrapolation and G2P); count and reseed
-static const int kStageOfGroup[9] = {0, 1, 3, 2, 5, 6, 7, 10, 11};
+// saved grid, body forces); pressure; with viscosity, the viscosity model and
+// the second projection; particle update (friction is in the pressure apply
+// here, then extrapolation and G2P); the last group, count and reseed, ends
+// the substep.
 
 // FlipSolver::step (flipsolver2d.cpp:412-462)
 template <class Mark> static fs_status step_flip(fs_solver *s, bool timed, Mark &mark)
 {
     TRY(stage(s, FS_STAGE_ADVECT, true));
-    TRY(mark());
+    TRY(mark(0));
     TRY(stage(s, FS_STAGE_DECOMPOSITION, true));
-    TRY(mark());
+    TRY(mark(1));
     TRY(stage(s, FS_STAGE_REBIN, true));
-    TRY(mark());
-    TRY(stage(s, FS_STAGE_DENSITY, true));
-    TRY(mark());
+    TRY(mark(3));
+    TRY(stage(s, FS_STAGE_DENSITY, true)); // skipped with viscosity on (:425-430)
+    TRY(mark(2));
     TRY(stage(s, FS_STAGE_P2G, true)); // + updateSdf + updateMaterials
-    TRY(mark());
+    TRY(mark(5));
     if (s->S.n) TRY(stage(s, FS_STAGE_AFTER_TRANSFER, true)); // sources (:435)
     TRY(stage(s, FS_STAGE_LEVELSET, true));
     // extrapolate(10), saved copy and body forces in one pass (:437-440)
     launch_vel_extrapolate(s->d, s->G, s->sp, s->sc, true, s->st);
     g_kernel_launches += 1;
     if (timed) TRY(wait_side(s)); // the level set counts in its own stage
-    TRY(mark());
+    TRY(mark(6));
     TRY(stage(s, FS_STAGE_PROJECT, true)); // + updateVelocityFromSolids
-    TRY(mark());
+    TRY(mark(7));
+    if (s->sp.viscosityEnabled) { // applyViscosity, then project() again (:448-454)
+        TRY(stage(s, FS_STAGE_VISCOSITY, true));
+        TRY(mark(8));
+        TRY(stage(s, FS_STAGE_PROJECT, false));
+        TRY(mark(9));
+    }
     TRY(stage(s, FS_STAGE_VEL_EXTRAP, true));
     TRY(stage(s, FS_STAGE_G2P, true));
-    TRY(mark());
+    TRY(mark(10));
     TRY(stage(s, FS_STAGE_COUNT, true));
     if (s->S.n) TRY(stage(s, FS_STAGE_RESEED, true)); // sources (:460)
     return FS_OK;
@@ -1315,6 +1354,7 @@ static fs_status nb_refresh_bound(fs_solver *s)
 // rebin; particle to grid (P2G, extrapolation, saved grid); after transfer
 // (inside gridUpdate, :213-225: SDF, outside level set, combination, inside
 // level set); grid update (materials, body forces); decomposition; pressure;
+// with viscosity, the viscosity model and the second projection (:49-56);
 // particle update; reseed
 static const int kNbStageOfGroup[9] = {0, 3, 4, 6, 5, 1, 7, 10, 11};
 
@@ -1323,8 +1363,11 @@ static fs_status step_impl(fs_solver *s)
     TRY(ensure_friction(s));
     const bool timed = s->timers && s->stage_ev[0];
     int group = 0;
-    auto mark = [&]() -> fs_status {
-        if (timed) CK(cudaEventRecord(s->stage_ev[group++], s->st));
+    auto mark = [&](int solver_stage) -> fs_status {
+        if (timed) {
+            s->stage_of[group] = solver_stage;
+            CK(cudaEventRecord(s->stage_ev[group++], s->st));
+        }
         return FS_OK;
     };
     if (s->timers) CK(cudaEventRecord(s->e0, s->st));
@@ -1344,7 +1387,13 @@ static fs_status step_impl(fs_solver *s)
             {FS_STAGE_COUNT, FS_STAGE_RESEED, -1}};
         for (int g = 0; g < 9; g++) {
             for (int k = 0; k < 4 && groups[g][k] >= 0; k++) TRY(stage(s, groups[g][k], true));
-            if (g < 8) TRY(mark());
+            if (g < 8) TRY(mark(kNbStageOfGroup[g]));
+            if (groups[g][0] == FS_STAGE_PROJECT && s->sp.viscosityEnabled) {
+                TRY(stage(s, FS_STAGE_VISCOSITY, true));
+                TRY(mark(8));
+                TRY(stage(s, FS_STAGE_PROJECT, false));
+                TRY(mark(9));
+            }
         }
     } else {
         if (s->grows) TRY(nb_refresh_bound(s));
@@ -1358,12 +1407,11 @@ static fs_status step_impl(fs_solver *s)
         CK(cudaEventElapsedTime(&ms, s->e0, s->e1));
         s->t_step_ms += ms;
         if (timed) {
-            const int *of = s->nb ? kNbStageOfGroup : kStageOfGroup;
             cudaEvent_t prev = s->e0;
-            for (int g = 0; g < 9; g++) {
-                cudaEvent_t cur = g < 8 ? s->stage_ev[g] : s->e1;
+            for (int g = 0; g <= group; g++) {
+                cudaEvent_t cur = g < group ? s->stage_ev[g] : s->e1;
                 CK(cudaEventElapsedTime(&ms, prev, cur));
-                s->t_stage_ms[of[g]] += ms;
+                s->t_stage_ms[g < group ? s->stage_of[g] : 11] += ms; // the last: PARTICLE_RESEED
                 prev = cur;
             }
         }
@@ -1762,6 +1810,7 @@ extern "C" fs_status fs_get_stat(fs_solver *s, int which, int *out)
     case FS_STAT_FRAME: *out = s->frame; return FS_OK;
     case FS_STAT_POOL_THREADS: *out = s->ex.pool_threads; return FS_OK;
     case FS_STAT_SUBSTEPS_TOTAL: *out = (int)s->substeps_total; return FS_OK;
+    case FS_STAT_VISCOSITY_ITERS: *out = s->visc_iters; return FS_OK;
     default: return fail(FS_ERR_BAD_ARG, "bad stat id");
     }
 }
@@ -2062,6 +2111,10 @@ extern "C" fs_status fs_batch_add(fs_batch *b, fs_solver *s)
     if (s->nb) return fail(FS_ERR_UNSUPPORTED, "fs_batch_add: NB-FLIP scenes step on their own");
     if (!s->src_params.empty())
         return fail(FS_ERR_UNSUPPORTED, "fs_batch_add: scenes with sources step on their own");
+    // the viscosity solve reads its stopping flag on the host between
+    // iteration batches, which a captured substep graph cannot
+    if (s->sp.viscosityEnabled)
+        return fail(FS_ERR_UNSUPPORTED, "fs_batch_add: scenes with viscosity step on their own");
     CK(cudaSetDevice(b->device));
     BatchScene bs;
     bs.s = s;

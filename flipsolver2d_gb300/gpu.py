@@ -25,11 +25,14 @@ FS_OK = 0
 FS_ERR_BAD_ARG, FS_ERR_CUDA, FS_ERR_OOM, FS_ERR_TIMEOUT, FS_ERR_UNSUPPORTED, FS_ERR_STATE, \
     FS_ERR_NONFINITE = range(1, 8)
 FS_PCG_FP32, FS_PCG_FP64, FS_PCG_SPEC = 0, 1, 2
+# fs_stat ids (FS_STAT_*)
+FS_STAT_DENSITY_ITERS, FS_STAT_PRESSURE_ITERS, FS_STAT_SUBSTEPS, FS_STAT_FRAME, \
+    FS_STAT_POOL_THREADS, FS_STAT_SUBSTEPS_TOTAL, FS_STAT_VISCOSITY_ITERS = range(7)
 
 # stage ids (FS_STAGE_*), identical to the oracle's
 ADVECT, DECOMPOSITION, REBIN, DENSITY, P2G, SDF, MATERIALS, AFTER_TRANSFER, LEVELSET, \
     VEL_EXTRAP, SAVE_GRID, BODY_FORCES, PROJECT, FRICTION, G2P, COUNT, RESEED, \
-    DENSITY_GRID, LEVELSET_OUTSIDE = range(19)
+    DENSITY_GRID, LEVELSET_OUTSIDE, VISCOSITY = range(20)
 
 GRIDS: Dict[str, tuple] = {
     "material": (0, np.int8, "c"), "solid_sdf": (1, np.float32, "c"),

@@ -414,8 +414,6 @@ def scene_from_json(source, name: str = "json") -> Scene:
         useHeavyViscosity=bool(get("heavyViscosity", False)),
         parameterHandlingMethod=handling.get(get("parameterHandlingMethod", "particle"), PARAM_PARTICLE),
     )
-    if p.viscosityEnabled:
-        raise UnsupportedScene("viscosityEnabled: viscosity is not on this path")
     objs: List[SceneObject] = []
     for o in doc["solver"]["objects"]:
         if not o.get("enabled", True):

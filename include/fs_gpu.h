@@ -58,8 +58,12 @@ typedef struct fs_params {
     int gridSizeI;
     int gridSizeJ;
     float sceneScale;
-    int viscosityEnabled;        /* must be 0 (viscosity is not on this path) */
-    int useHeavyViscosity;
+    int viscosityEnabled;        /* each substep applies the viscosity model after
+                                    the friction update and projects again, and
+                                    the density correction is skipped (:425-454);
+                                    the projection's tolerance becomes 1e-6 (:73) */
+    int useHeavyViscosity;       /* the heavy (coupled U+V) model instead of the
+                                    light one (:77-84, viscositymodel.cpp) */
     int simulationMethod;        /* must be 0 = SIMULATION_LIQUID */
     int parameterHandlingMethod; /* 0 PARTICLE, 1 HYBRID, 2 GRID */
 } fs_params;
@@ -114,7 +118,11 @@ enum {
     FS_STAGE_COUNT = 15,         /* countParticles()                  :459 */
     FS_STAGE_RESEED = 16,        /* reseedParticles(): sources only, no-op */
     FS_STAGE_DENSITY_GRID = 17,  /* updateDensityGrid() alone (plus its RHS) */
-    FS_STAGE_LEVELSET_OUTSIDE = 18 /* extrapolateLevelsetOutside       :1496-1558 */
+    FS_STAGE_LEVELSET_OUTSIDE = 18, /* extrapolateLevelsetOutside      :1496-1558 */
+    FS_STAGE_VISCOSITY = 19      /* applyViscosity(): the light or heavy model of
+                                    viscositymodel.cpp on U and V      :128-136;
+                                    fs_step runs it (then FS_STAGE_PROJECT again)
+                                    after the friction update when viscosity is on */
 };
 
 /* An NB-FLIP handle (fs_create_nbflip) runs the same stage ids, four of them
@@ -167,7 +175,9 @@ enum {
     FS_STAT_SUBSTEPS = 2,       /* SolverStats::substepCount()       */
     FS_STAT_FRAME = 3,          /* FlipSolver::frameNumber()         */
     FS_STAT_POOL_THREADS = 4,   /* chunk count of the residual test  */
-    FS_STAT_SUBSTEPS_TOTAL = 5  /* substeps since fs_create (no reference counterpart) */
+    FS_STAT_SUBSTEPS_TOTAL = 5, /* substeps since fs_create (no reference counterpart) */
+    FS_STAT_VISCOSITY_ITERS = 6 /* SolverStats::viscosityIterations(): the model's return
+                                   value of the last substep (-1: its solve failed) */
 };
 
 typedef struct fs_solver fs_solver;

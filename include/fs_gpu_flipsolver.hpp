@@ -160,12 +160,14 @@ private:
  * uploads the particles and the state grids, runs fs_step with m_stepDt and
  * writes the results back into the reference's members, so every accessor
  * (markerParticles(), materialGrid(), fluidVelocityGrid(), ...) reads the
- * GPU's results.  Viscosity must be off (fs_create refuses it). */
+ * GPU's results.  With viscosityEnabled the substep applies the light or
+ * heavy viscosity model on the GPU and projects again, like FlipSolver::step
+ * (flipsolver2d.cpp:448-454). */
 class GpuStepSolver : public FlipSolver {
 public:
     explicit GpuStepSolver(const FlipSolverParameters *p, int precision = FS_PCG_FP32,
                            int pool_threads = 0, int device = 0)
-        : FlipSolver(p)
+        : FlipSolver(p), m_heavyViscosity(p->useHeavyViscosity)
     {
         std::memset(&m_exec, 0, sizeof(m_exec));
         m_exec.pcg_precision = precision;
@@ -218,6 +220,8 @@ private:
         q.gridSizeJ = (int)m_sizeJ;
         q.sceneScale = m_sceneScale;
         q.viscosityEnabled = m_viscosityEnabled ? 1 : 0;
+        // FlipSolver keeps only the model it built from this flag (:77-84)
+        q.useHeavyViscosity = m_heavyViscosity ? 1 : 0;
         q.simulationMethod = (int)m_simulationMethod;
         q.parameterHandlingMethod = (int)m_parameterHandlingMethod;
         return q;
@@ -389,10 +393,15 @@ private:
         m_stats.setDensityIters(it);
         check(fs_get_stat(m_handle, FS_STAT_PRESSURE_ITERS, &it), "fs_get_stat");
         m_stats.setPressureIterations(it);
+        if (m_viscosityEnabled) {
+            check(fs_get_stat(m_handle, FS_STAT_VISCOSITY_ITERS, &it), "fs_get_stat");
+            m_stats.setViscosityIterations(it);
+        }
     }
 
     fs_exec_params m_exec;
     fs_solver *m_handle = nullptr;
+    bool m_heavyViscosity;
 };
 
 } // namespace fsgpu

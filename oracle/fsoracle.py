@@ -27,6 +27,9 @@ ADVECT, DECOMPOSITION, REBIN, DENSITY, P2G, SDF, MATERIALS, AFTER_TRANSFER, LEVE
     VEL_EXTRAP, SAVE_GRID, BODY_FORCES, PROJECT, FRICTION, G2P, COUNT, RESEED, \
     DENSITY_GRID, LEVELSET_OUTSIDE, VISCOSITY = range(20)
 
+# statistic ids (fsoracle.h enum fso_stat)
+S_DENSITY_ITERS, S_PRESSURE_ITERS, S_SUBSTEPS, S_FRAME, S_POOL_THREADS, S_VISCOSITY_ITERS = range(6)
+
 # the order in which FlipSolver::step() (flipsolver2d.cpp:412-462) runs them
 STEP_STAGES = [ADVECT, DECOMPOSITION, REBIN, DENSITY, P2G, SDF, MATERIALS, AFTER_TRANSFER,
                LEVELSET, VEL_EXTRAP, SAVE_GRID, BODY_FORCES, PROJECT, FRICTION, VEL_EXTRAP,

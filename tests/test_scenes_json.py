@@ -128,6 +128,32 @@ def test_reference_scene_files_run_the_same_on_both_oracles(port_lib, ref_lib):
         _same_on_both(fo, sc)
 
 
+@pytest.mark.skipif(not os.path.isdir(REF_SCENES), reason="reference scene files not present")
+def test_reference_viscosity_scenes_run_the_same_on_both_oracles(port_lib, ref_lib):
+    """The reference's scene files with viscosity on (the light model; FLIP
+    and NB-FLIP), at a reduced resolution, on the reference build (its own
+    viscositymodel.cpp) and on the C restatement: identical frame by frame."""
+    import fsoracle as fo
+
+    for fn in ("double_dam_break.json", "viscosity_bar.json", "viscosity_test.json", "bounds_check.json"):
+        sc = scenes.scene_from_json(os.path.join(REF_SCENES, fn))
+        assert sc.params.viscosityEnabled, fn
+        sc.params.resolution = 48
+        _same_on_both(fo, sc, frames=3)
+
+
+def test_viscosity_settings_from_json():
+    doc = {"settings": {"simType": "flip", "domainSizeI": 1, "domainSizeJ": 1, "resolution": 16,
+                        "fps": 30, "particlesPerCell": 4, "viscosityEnabled": True,
+                        "heavyViscosity": True},
+           "solver": {"objects": [{"type": "fluid", "viscosity": 25,
+                                   "verts": [[0.2, 0.2], [0.2, 0.6], [0.6, 0.6], [0.6, 0.2]]}]}}
+    sc = scenes.scene_from_json(doc)
+    assert sc.params.viscosityEnabled and sc.params.useHeavyViscosity
+    assert sc.objects[0].viscosity == 25.0
+    assert not scenes.scene_from_json(DAM_JSON).params.viscosityEnabled
+
+
 def _same_on_both(fo, sc, frames=6):
     r, p = fo.OracleSolver(sc, "ref"), fo.OracleSolver(sc, "port")
     for _ in range(frames):
