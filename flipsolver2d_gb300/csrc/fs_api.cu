@@ -614,6 +614,9 @@ static fs_status create_impl(const fs_params *p, const fs_exec_params *exec, boo
     bool ok = cudaMemsetAsync(G.material, 0x10, n, q) == cudaSuccess; // EMPTY
     k_fill_i32<<<(unsigned)((n + 255) / 256), 256, 0, q>>>(G.solid_id, -1, n);
     k_fill_i32<<<(unsigned)((n + 255) / 256), 256, 0, q>>>(G.emitter_id, -1, n);
+    // no unit row anywhere until the first decomposition: a solve run before
+    // it (fs_run_stage) sees an operator of identity rows
+    k_fill_i32<<<(unsigned)((ends.size() + 256) / 256), 256, 0, q>>>(s->chunk_last, -1, ends.size() + 1);
     void *zero[] = {G.solid_sdf, G.fluid_sdf, G.visc, G.known, G.divc, G.density, G.counts,
                     G.cell_info};
     size_t zsz[] = {n * 4, n * 4, n * 4, n, n * 4, n * 4, n * 4, n};
@@ -1311,8 +1314,10 @@ template <class Mark> static fs_status step_flip(fs_solver *s, bool timed, Mark 
     TRY(mark(1));
     TRY(stage(s, FS_STAGE_REBIN, true));
     TRY(mark(3));
-    TRY(stage(s, FS_STAGE_DENSITY, true)); // skipped with viscosity on (:425-430)
-    TRY(mark(2));
+    if (!s->sp.viscosityEnabled) { // densityCorrection and its endStage (:425-430)
+        TRY(stage(s, FS_STAGE_DENSITY, true));
+        TRY(mark(2));
+    }
     TRY(stage(s, FS_STAGE_P2G, true)); // + updateSdf + updateMaterials
     TRY(mark(5));
     if (s->S.n) TRY(stage(s, FS_STAGE_AFTER_TRANSFER, true)); // sources (:435)

@@ -106,13 +106,29 @@ def scene(request, port_lib, gpu_lib):
 
 def oracle_before_viscosity(sc, frames):
     """The oracle after `frames` frames and the stages of one more substep up
-    to the friction update: the state applyViscosity starts from."""
+    to the friction update (the state applyViscosity starts from), and its
+    snapshot just before that substep's decomposition (the state the
+    pressure operator is frozen from)."""
     o = fo.OracleSolver(sc, "port")
     for _ in range(frames):
         o.step_frame()
+    at_decomposition = None
     for s in (NB_ORDER if sc.sim_type == scenes.SIM_NBFLIP else FLIP_ORDER):
+        if s == fo.DECOMPOSITION:
+            at_decomposition = o.snapshot()
         o.stage(s)
-    return o
+    return o, at_decomposition
+
+
+def gpu_at(sc, o, at_decomposition):
+    """A GPU handle in the oracle's state, its pressure operator frozen from
+    the same material as the oracle's."""
+    g = gpu.GpuFlipSolver(sc, precision=gpu.FS_PCG_FP64, pool_threads=POOL_THREADS)
+    g.first_frame_init()
+    g.restore(at_decomposition)
+    g.stage(gpu.DECOMPOSITION)
+    g.restore(o.snapshot())
+    return g
 
 
 def velocity_bar(it_o, it_g):
@@ -120,10 +136,8 @@ def velocity_bar(it_o, it_g):
 
 
 def test_viscosity_stage_from_identical_state(scene):
-    o = oracle_before_viscosity(scene, 3)
-    g = gpu.GpuFlipSolver(scene, precision=gpu.FS_PCG_FP64, pool_threads=POOL_THREADS)
-    g.first_frame_init()
-    g.restore(o.snapshot())
+    o, at_dec = oracle_before_viscosity(scene, 3)
+    g = gpu_at(scene, o, at_dec)
     u0 = o.get_grid("u")
     o.stage(fo.VISCOSITY)
     g.stage(gpu.VISCOSITY)
@@ -139,13 +153,15 @@ def test_viscosity_stage_from_identical_state(scene):
     for name in ("u_valid", "v_valid", "material", "fluid_sdf", "viscosity", "saved_u", "saved_v"):
         assert_grid_equal(o, g, name, "viscosity stage")
 
-    # the projection that follows (FP64 parity mode)
+    # the projection that follows (FP64 parity mode; the FP64 velocity bar of
+    # test_gpu_parity.py, or ten times what the viscosity stage left)
     o.stage(fo.PROJECT)
     g.stage(gpu.PROJECT)
-    po, pg = o.stat(1), g.stat(1)
-    assert po == pg or min(po, pg) >= scene.params.pcgIterLimit
+    po, pg = o.stat(fo.S_PRESSURE_ITERS), g.stat(gpu.FS_STAT_PRESSURE_ITERS)
+    print(f"  second projection: iterations {pg} / oracle {po}")
+    assert po > 0 and (po == pg or min(po, pg) >= scene.params.pcgIterLimit)
     for name in ("u", "v"):
-        assert rel_l2(g.get_grid(name), o.get_grid(name)) <= max(10 * du, 1e-7), name
+        assert rel_l2(g.get_grid(name), o.get_grid(name)) <= max(10 * du, 1e-6), name
     g.close()
     o.close()
 
@@ -153,7 +169,7 @@ def test_viscosity_stage_from_identical_state(scene):
 def test_viscosity_stage_is_deterministic(scene):
     """Two runs of the stage from one state give the same bits: the fixed-order
     block sums make the GPU solve reproducible run to run."""
-    o = oracle_before_viscosity(scene, 2)
+    o, _ = oracle_before_viscosity(scene, 2)
     snap = o.snapshot()
     out = []
     for _ in range(2):
@@ -217,7 +233,9 @@ def test_stage_times_include_viscosity(gpu_lib):
     g.enable_timers(True)
     g.step_frame()
     t = g.stage_times()
-    assert t[8] > 0 and t[9] > 0 and t[2] == 0.0  # no density correction with viscosity
+    # with viscosity the density correction and its endStage(DENSITY) are
+    # skipped (flipsolver2d.cpp:425-430)
+    assert t[8] > 0 and t[9] > 0 and t[2] == 0.0
     g.close()
 
 
