@@ -79,3 +79,23 @@ def test_full_frames_fp64(scene):
         assert counts[-1] < counts[0], "the sink kills particles"
     if scene.name.startswith("empty"):
         assert counts == [0] * len(counts)
+
+
+@pytest.mark.parametrize("precision", [gpu.FS_PCG_FP64, gpu.FS_PCG_FP32])
+def test_solves_before_any_decomposition(port_lib, gpu_lib, precision):
+    """A density or pressure stage run on a fresh handle, before any
+    decomposition has frozen an operator: the solve sees identity rows and no
+    chunk with a unit row, and leaves the handle usable: the chunk ends start
+    as 'no unit row', never as uninitialised memory."""
+    from flipsolver2d_gb300 import scenes
+
+    sc = scenes.dam_break(40, seed=3)
+    g = gpu.GpuFlipSolver(sc, precision=precision, pool_threads=POOL_THREADS)
+    g.first_frame_init()
+    g.stage(gpu.DENSITY)
+    g.stage(gpu.PROJECT)
+    for which in (gpu.FS_STAT_DENSITY_ITERS, gpu.FS_STAT_PRESSURE_ITERS):
+        assert 0 <= g.stat(which) <= sc.params.pcgIterLimit
+    g.step_frame()  # and the handle steps normally afterwards
+    assert g.particle_count() > 0
+    g.close()

@@ -35,6 +35,7 @@ from test_gpu_parity import assert_grid_equal, rel_l2
 pytestmark = pytest.mark.gpu
 
 ITER_SLACK = 1
+PROJECT_STOP_BAR = 1e-4
 SAME_ITER_BAR = 1e-8
 ONE_ITER_BAR = 1e-3
 
@@ -112,9 +113,13 @@ def oracle_before_viscosity(sc, frames):
     o = fo.OracleSolver(sc, "port")
     for _ in range(frames):
         o.step_frame()
-    at_decomposition = None
-    for s in (NB_ORDER if sc.sim_type == scenes.SIM_NBFLIP else FLIP_ORDER):
-        if s == fo.DECOMPOSITION:
+    nb = sc.sim_type == scenes.SIM_NBFLIP
+    # FLIP decomposes right after advection, which moves particles only: the
+    # substep's starting state has the same material (and no particle
+    # marked for death, which only exists inside a substep)
+    at_decomposition = None if nb else o.snapshot()
+    for s in (NB_ORDER if nb else FLIP_ORDER):
+        if s == fo.DECOMPOSITION and nb:
             at_decomposition = o.snapshot()
         o.stage(s)
     return o, at_decomposition
@@ -153,15 +158,25 @@ def test_viscosity_stage_from_identical_state(scene):
     for name in ("u_valid", "v_valid", "material", "fluid_sdf", "viscosity", "saved_u", "saved_v"):
         assert_grid_equal(o, g, name, "viscosity stage")
 
-    # the projection that follows (FP64 parity mode; the FP64 velocity bar of
-    # test_gpu_parity.py, or ten times what the viscosity stage left)
+    # the projection that follows (FP64 parity mode, tolerance 1e-6 with
+    # viscosity on).  With identical inputs it keeps the oracle's iteration
+    # count and the FP64 velocity bar of test_gpu_parity.py.  Near the 1e-6
+    # absolute stop the chunked max-abs residual can hover at the tolerance
+    # for several iterations, so the dot products' other summation order may
+    # stop it elsewhere: then both solves must have met the tolerance and the
+    # velocities stay within PROJECT_STOP_BAR.
     o.stage(fo.PROJECT)
     g.stage(gpu.PROJECT)
     po, pg = o.stat(fo.S_PRESSURE_ITERS), g.stat(gpu.FS_STAT_PRESSURE_ITERS)
-    print(f"  second projection: iterations {pg} / oracle {po}")
-    assert po > 0 and (po == pg or min(po, pg) >= scene.params.pcgIterLimit)
-    for name in ("u", "v"):
-        assert rel_l2(g.get_grid(name), o.get_grid(name)) <= max(10 * du, 1e-6), name
+    dv = max(rel_l2(g.get_grid(n), o.get_grid(n)) for n in ("u", "v"))
+    print(f"  second projection: iterations {pg} / oracle {po}, u,v rel-L2 {dv:.3e}")
+    limit = scene.params.pcgIterLimit
+    assert po > 0
+    if po == pg:
+        assert dv <= max(10 * du, 1e-6)
+    else:
+        assert po < limit and pg < limit
+        assert dv <= PROJECT_STOP_BAR
     g.close()
     o.close()
 
