@@ -751,7 +751,7 @@ __device__ __forceinline__ void ld_ll2(const unsigned long long *p, unsigned lon
 constexpr int kRecWords = 4;
 
 // reduction k of a launch uses set k & 1 of two sets of G records
-static_assert(kRecWords * 2 * 256 == kLlRecWords, "record buffer");
+static_assert(kRecWords * 2 * 256 == (int)kLlRecWords, "record buffer");
 
 // float-pair accumulation without renormalising: hi carries the running
 // sum, lo the rounding errors of the additions and the low parts
@@ -899,6 +899,7 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     extern __shared__ unsigned char smem_dyn[];
     __shared__ float smf[64];
     __shared__ float4 s_bcast;
+    __shared__ float4 s_gw[8]; // per-warp sums of a reduction's records
     __shared__ int s_flag, s_fail;
     __shared__ float inv[8];
     __shared__ int s_cmax, s_cscan;
@@ -906,7 +907,10 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     __shared__ int2 s_own[kMaxOwnedChunks]; // (chunk, Rb index)
     if (a.mode == 1 && *a.wrap_flag == 0) return;
     if (a.mode == 2 && *a.wrap_flag != 0) return;
-    if (threadIdx.x == 0) s_nown = 0; // ordered before its use by the set-up barriers
+    if (threadIdx.x == 0) { // ordered before their use by the set-up barriers
+        s_nown = 0;
+        s_fail = 0;
+    }
     // no TMA here, so the 16-byte alignment of dynamic shared memory is
     // enough; indexing smem_dyn directly keeps the accesses in the shared
     // window (32-bit addresses, LDS/STS)
@@ -957,60 +961,42 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
         }
         nred++;
     };
-    // completes the last reduction published: warp 0 gathers the G records
-    // (each lane's loads all in flight at once, then only the records not yet
-    // published are polled again) and sums them in a fixed order, so every
+    // completes the last reduction published: warp w gathers records
+    // 32 w .. 32 w + 31 (one per lane; the G <= 256 records take at most 8
+    // warps, whose loads are all in flight at once), sums them in a fixed
+    // order (a shuffle tree per warp, then the warps in order), so every
     // block obtains the same scalars: (pair hi, lo, max, flag) in every
     // thread.  s_fail, read after it, is block-uniform: 1 after a timeout.
+    // (One warp polling all G records, several per lane, took 4-5 us from
+    // the last block's publish to completion at 1024^2; a lane per record
+    // and a warp per 32 records take under 1 us.)
     auto wait_sum = [&]() -> float4 {
-        if (warp == 0) {
-            const unsigned k = nred - 1, ep = ep0 + nred;
+        const unsigned k = nred - 1, ep = ep0 + nred;
+        const int ngw = (G + 31) >> 5;
+        if (warp < ngw) {
             const unsigned long long *base = recs + (size_t)(k & 1) * G * kRecWords;
-            unsigned long long w0[kPartRounds], w1[kPartRounds], w2[kPartRounds];
-            unsigned pending = 0;
-#pragma unroll
-            for (int i = 0; i < kPartRounds; i++) {
-                const int b = lane + 32 * i;
-                if (b < G) {
-                    ld_ll2(base + (size_t)b * kRecWords, w0[i], w1[i]);
-                    w2[i] = ld_ll(base + (size_t)b * kRecWords + 2);
-                    if (ll_epoch(w0[i]) != ep || ll_epoch(w1[i]) != ep || ll_epoch(w2[i]) != ep)
-                        pending |= 1u << i;
-                } else {
-                    w0[i] = w1[i] = w2[i] = 0ull;
-                }
-            }
-            long long spins = 0;
+            const int b = warp * 32 + lane;
+            unsigned long long w0 = 0ull, w1 = 0ull, w2 = 0ull;
             bool failed = false;
-            while (pending) {
-                if (++spins > lim || ((spins & 255) == 0 && *((volatile int *)a.status) != 0)) {
-                    atomicExch(a.status, 1);
-                    failed = true;
-                    break;
-                }
-#pragma unroll
-                for (int i = 0; i < kPartRounds; i++) {
-                    if (pending & (1u << i)) {
-                        const int b = lane + 32 * i;
-                        ld_ll2(base + (size_t)b * kRecWords, w0[i], w1[i]);
-                        w2[i] = ld_ll(base + (size_t)b * kRecWords + 2);
-                        if (ll_epoch(w0[i]) == ep && ll_epoch(w1[i]) == ep && ll_epoch(w2[i]) == ep)
-                            pending &= ~(1u << i);
+            if (b < G) {
+                const unsigned long long *rp = base + (size_t)b * kRecWords;
+                ld_ll2(rp, w0, w1);
+                w2 = ld_ll(rp + 2);
+                long long spins = 0;
+                while (ll_epoch(w0) != ep || ll_epoch(w1) != ep || ll_epoch(w2) != ep) {
+                    if (++spins > lim || ((spins & 255) == 0 && *((volatile int *)a.status) != 0)) {
+                        atomicExch(a.status, 1);
+                        failed = true;
+                        break;
                     }
+                    ld_ll2(rp, w0, w1);
+                    w2 = ld_ll(rp + 2);
                 }
             }
-            unsigned p0[kPartRounds], p1[kPartRounds], p2[kPartRounds];
-#pragma unroll
-            for (int i = 0; i < kPartRounds; i++) { p0[i] = (unsigned)w0[i]; p1[i] = (unsigned)w1[i]; p2[i] = (unsigned)w2[i]; }
-            float2 acc = make_float2(0.f, 0.f);
-            float mx = 0.f;
-            unsigned flag = 0;
-#pragma unroll
-            for (int i = 0; i < kPartRounds; i++) {
-                acc = ff_acc(acc, make_float2(__uint_as_float(p0[i]), __uint_as_float(p1[i])));
-                mx = fmaxf(mx, __uint_as_float(p2[i] & 0x7fffffffu));
-                flag |= p2[i] >> 31;
-            }
+            // records past G are zeros: adding them changes nothing
+            float2 acc = make_float2(__uint_as_float((unsigned)w0), __uint_as_float((unsigned)w1));
+            float mx = __uint_as_float((unsigned)w2 & 0x7fffffffu);
+            unsigned flag = (unsigned)w2 >> 31;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 acc = ff_acc(acc, ff_shfl_down(acc, o));
@@ -1019,10 +1005,23 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
             }
             failed = __any_sync(0xffffffffu, failed);
             if (lane == 0) {
-                acc = ff_norm(acc);
-                s_bcast = make_float4(acc.x, acc.y, mx, flag ? 1.f : 0.f);
-                s_fail = (failed || *((volatile int *)a.status) != 0) ? 1 : 0;
+                s_gw[warp] = make_float4(acc.x, acc.y, mx, flag ? 1.f : 0.f);
+                if (failed) s_fail = 1;
             }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float2 acc = make_float2(0.f, 0.f);
+            float mx = 0.f, flag = 0.f;
+            for (int w = 0; w < ngw; w++) {
+                const float4 g = s_gw[w];
+                acc = ff_acc(acc, make_float2(g.x, g.y));
+                mx = fmaxf(mx, g.z);
+                flag = fmaxf(flag, g.w);
+            }
+            acc = ff_norm(acc);
+            s_bcast = make_float4(acc.x, acc.y, mx, flag);
+            if (*((volatile int *)a.status) != 0) s_fail = 1;
         }
         __syncthreads();
         return s_bcast;
@@ -1103,26 +1102,44 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     // exchange words of epoch ep (bounded polls); a block barrier, then a
     // block-uniform false on timeout
     auto load_ring_ll = [&](float *dst, const unsigned long long *src, unsigned ep) -> bool {
+        // two cells per thread per round, both loads issued before either is
+        // polled, so a thread with two ring cells waits one round trip
         const int n = 4 * w2 + 4 * ti;
-        for (int k = threadIdx.x; k < n; k += blockDim.x) {
-            int r, q;
-            ring_cell(k, ti, tj, r, q);
-            const int gi = ti0 + r, gj = tj0 + q;
-            float v = 0.f;
-            if (gi >= 0 && gi < NI && gj >= 0 && gj < NJ) {
-                const unsigned long long *p = src + (size_t)gi * NJ + gj;
-                unsigned long long w = ld_ll(p);
-                long long spins = 0;
-                while (ll_epoch(w) != ep) {
-                    if (++spins > lim || ((spins & 255) == 0 && *((volatile int *)a.status) != 0)) {
-                        atomicExch(a.status, 1);
-                        break;
-                    }
-                    w = ld_ll(p);
+        const int nt = (int)blockDim.x;
+        for (int k0 = threadIdx.x; k0 < n; k0 += 2 * nt) {
+            const unsigned long long *p[2] = {nullptr, nullptr};
+            int cell[2] = {-1, -1};
+            unsigned long long w[2] = {0ull, 0ull};
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int k = k0 + h * nt;
+                if (k >= n) continue;
+                int r, q;
+                ring_cell(k, ti, tj, r, q);
+                cell[h] = (r + 2) * w2 + (q + 2);
+                const int gi = ti0 + r, gj = tj0 + q;
+                if (gi >= 0 && gi < NI && gj >= 0 && gj < NJ) {
+                    p[h] = src + (size_t)gi * NJ + gj;
+                    w[h] = ld_ll(p[h]);
                 }
-                v = __uint_as_float((unsigned)w);
             }
-            dst[(r + 2) * w2 + (q + 2)] = v;
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                if (cell[h] < 0) continue;
+                float v = 0.f;
+                if (p[h]) {
+                    long long spins = 0;
+                    while (ll_epoch(w[h]) != ep) {
+                        if (++spins > lim || ((spins & 255) == 0 && *((volatile int *)a.status) != 0)) {
+                            atomicExch(a.status, 1);
+                            break;
+                        }
+                        w[h] = ld_ll(p[h]);
+                    }
+                    v = __uint_as_float((unsigned)w[h]);
+                }
+                dst[cell[h]] = v;
+            }
         }
         return ok();
     };
