@@ -20,10 +20,14 @@ downloaded every step; `roofline` is for the PCG kernel, which dominates the
 substep; `cpu_baseline` is the CPU oracle on this host's cores on a bounded
 sample of the same workload.  `fp64_check` steps the final state once more
 in FP32 and in the FP64 parity mode from identical inputs and reports the
-FP32 error.  `batch` (unless --no-batch) is the batched form
-of the path beside it: 64 scenes of the batched-scenes workload stepped
-together at a 1e-6 pressure residual, and the same scenes one at a time;
-`nbflip` is the same scene stepped by the narrow-band solver (NB-FLIP).
+FP32 error.  Unless --no-batch, sub-objects beside it: `spec_single`, the
+same scene with every solve to a 1e-6 true residual (FS_PCG_SPEC);
+`poisson_2048`, one 2048^2 standalone spec-mode solve; `batch`, the batched
+form of the path: 64 scenes of the batched-scenes workload stepped together
+at a 1e-6 pressure residual, and the same scenes one at a time; `nbflip`,
+the same scene stepped by the narrow-band solver (NB-FLIP); `serve`, 120
+requests of the seeded serving stream (requests/s, p50/p99 latency, worst
+solve residual).
 With --impl reference only the CPU
 implementation is timed (the reference's sources are not present on GPU
 hosts, so its plain-C restatement, pinned bit for bit to it, stands in).
@@ -661,6 +665,20 @@ def gpu_arm(args):
                               "particles": int(r["work"] / 5)}
         except Exception as e:  # reported, never fatal for the main line
             line["nbflip"] = {"error": str(e)}
+    if rank == 0 and world == 1 and not args.no_batch:
+        # the serving loop on a short stretch of the request stream
+        try:
+            r = serve_measure(SERVE_SUBOBJECT_REQUESTS)
+            line["serve"] = {"workload": f"serve_{r['requests']}_requests (Poisson 2000/s, "
+                                         f"{r['scenes']} resident scenes of sides 64-1024, "
+                                         "20 % standalone solves of sides 256-2048)",
+                             "value": r["frame_work"] / r["elapsed_s"], "unit": METRIC,
+                             "requests_per_s": r["requests_per_s"], "latency_ms": r["latency_ms"],
+                             "worst_solve_rel_residual": r["worst_solve_rel_residual"],
+                             "rounds": r["rounds"], "elapsed_s": r["elapsed_s"],
+                             "pcg": "FS_PCG_SPEC, 1e-6 true relative residual"}
+        except Exception as e:  # reported, never fatal for the main line
+            line["serve"] = {"error": str(e)}
     if rank == 0:
         print(json.dumps(line))
     if dist:
@@ -669,6 +687,7 @@ def gpu_arm(args):
 
 
 NB_WARM_FRAMES = 4
+SERVE_SUBOBJECT_REQUESTS = 120
 
 
 def nb_scene(res: int):
@@ -1090,21 +1109,18 @@ def solve_batch_arm(args):
     return 0
 
 
-def serve_arm(args):
-    """Serving loop (--serve R): R requests from a seeded Poisson stream at
-    2000 per second (default_rng(9)), 80 % frame requests to 32 resident
+def serve_measure(n_requests: int, pool: int = 32):
+    """Serves n_requests of the seeded request stream: Poisson arrivals at
+    2000 per second (default_rng(9)), 80 % frame requests to `pool` resident
     scenes with sides log-uniform in [64, 1024] and 20 % standalone solves of
-    sides log-uniform in [256, 2048], served by continuous batching under a
-    150 GB device-memory budget (flipsolver2d_gb300/serve.py).  Every scene
-    first gets one warm-up frame so its creation, seeding and graph capture
-    are outside the measurement.  `value` is frame work served per second of
-    the run (particle-substeps/s); latencies run from arrival to completion."""
+    sides log-uniform in [256, 2048], by continuous batching under a 150 GB
+    device-memory budget (flipsolver2d_gb300/serve.py).  Every scene first
+    gets one warm-up frame, so its creation, seeding and graph capture are
+    outside the measurement.  Latencies run from arrival to completion."""
     import torch
-    from flipsolver2d_gb300 import build, serve
+    from flipsolver2d_gb300 import serve
 
-    build.build()
-    torch.cuda.set_device(0)
-    specs, reqs = serve.serving_workload(args.serve, rate=2000.0, seed=9, pool=32,
+    specs, reqs = serve.serving_workload(n_requests, rate=2000.0, seed=9, pool=pool,
                                          frame_sides=(64, 1024), solve_sides=(256, 2048))
     srv = serve.Server(budget_bytes=150e9)
     for k, sc in specs.items():
@@ -1121,35 +1137,54 @@ def serve_arm(args):
     done = srv.run(reqs)
     elapsed = time.perf_counter() - t0
     clocks = sampler.stop()
-    frame_work = sum(r.work for r in done if r.kind == "frame")
-    solve_work = sum(r.work for r in done if r.kind == "solve")
-    lat = serve.latency_summary(done)
-    worst_rr = max((r.result[2] for r in done if r.kind == "solve"), default=None)
+    out = {
+        "requests": len(reqs), "warm": len(warm), "scenes": len(specs), "elapsed_s": elapsed,
+        "frame_work": sum(r.work for r in done if r.kind == "frame"),
+        "solve_work": sum(r.work for r in done if r.kind == "solve"),
+        "requests_per_s": len(done) / elapsed,
+        "latency_ms": serve.latency_summary(done),
+        "rounds": srv.rounds, "merged_solve_device_ms": srv.batch.timer(0),
+        "worst_solve_rel_residual": max((r.result[2] for r in done if r.kind == "solve"), default=None),
+        "h2d_bytes": sum(r.problem[0].nbytes + r.problem[1].nbytes for r in done if r.kind == "solve"),
+        "d2h_bytes": sum(r.problem[1].nbytes for r in done if r.kind == "solve"),
+        "clocks": clocks,
+    }
+    srv.close()
+    return out
+
+
+def serve_arm(args):
+    """Serving loop (--serve R): R requests of the seeded request stream
+    (serve_measure).  `value` is frame work served per second of the run
+    (particle-substeps/s)."""
+    import torch
+    from flipsolver2d_gb300 import build
+
+    build.build()
+    torch.cuda.set_device(0)
+    r = serve_measure(args.serve)
+    n = r["requests"]
     line = {
-        "metric": METRIC, "value": frame_work / elapsed, "unit": METRIC, "n_gpus": 1,
-        "steps": len(reqs), "warmup": len(warm), "ms_per_step": 1e3 * elapsed / len(reqs),
+        "metric": METRIC, "value": r["frame_work"] / r["elapsed_s"], "unit": METRIC, "n_gpus": 1,
+        "steps": n, "warmup": r["warm"], "ms_per_step": 1e3 * r["elapsed_s"] / n,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded request stream, random scenes and star masks)",
-        "config": {"workload": f"serve_{len(reqs)}_requests", "rate_per_s": 2000.0, "seed": 9,
-                   "scenes": len(specs), "frame_sides": [64, 1024], "solve_sides": [256, 2048],
+        "config": {"workload": f"serve_{n}_requests", "rate_per_s": 2000.0, "seed": 9,
+                   "scenes": r["scenes"], "frame_sides": [64, 1024], "solve_sides": [256, 2048],
                    "solve_fraction": 0.2, "budget_bytes": 150e9,
                    "pcg": "FS_PCG_SPEC, 1e-6 true relative residual",
                    "step": "one request", "parallelism": "single GPU"},
-        "requests_per_s": len(done) / elapsed,
-        "solve_cell_iter_per_s": solve_work / elapsed,
-        "latency_ms": lat,
-        "rounds": srv.rounds, "merged_solve_device_ms": srv.batch.timer(0),
-        "worst_solve_rel_residual": worst_rr,
-        "e2e": {"value": frame_work / elapsed, "unit": METRIC,
-                "h2d_bytes_per_step": int(sum(r.problem[0].nbytes + r.problem[1].nbytes
-                                              for r in done if r.kind == "solve") / len(done)),
-                "d2h_bytes_per_step": int(sum(r.problem[1].nbytes for r in done if r.kind == "solve")
-                                          / len(done)),
+        "requests_per_s": r["requests_per_s"],
+        "solve_cell_iter_per_s": r["solve_work"] / r["elapsed_s"],
+        "latency_ms": r["latency_ms"],
+        "rounds": r["rounds"], "merged_solve_device_ms": r["merged_solve_device_ms"],
+        "worst_solve_rel_residual": r["worst_solve_rel_residual"],
+        "e2e": {"value": r["frame_work"] / r["elapsed_s"], "unit": METRIC,
+                "h2d_bytes_per_step": int(r["h2d_bytes"] / n), "d2h_bytes_per_step": int(r["d2h_bytes"] / n),
                 "path": "value itself is host-timed around the serving loop on the public API"},
-        "clocks": clocks,
+        "clocks": r["clocks"],
     }
     print(json.dumps(line))
-    srv.close()
     return 0
 
 
