@@ -898,19 +898,16 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     const long long lim = a.spin_limit > 0 ? a.spin_limit : kSpinLimit;
     extern __shared__ unsigned char smem_dyn[];
     __shared__ float smf[64];
-    __shared__ float4 s_bcast;
     __shared__ float4 s_gw[8]; // per-warp sums of a reduction's records
-    __shared__ int s_flag, s_fail;
+    __shared__ int s_gwf[8];   // and whether that warp's wait gave up
+    __shared__ int s_flag;
     __shared__ float inv[8];
     __shared__ int s_cmax, s_cscan;
     __shared__ int s_nown;           // chunks whose last unit row is in this tile
     __shared__ int2 s_own[kMaxOwnedChunks]; // (chunk, Rb index)
     if (a.mode == 1 && *a.wrap_flag == 0) return;
     if (a.mode == 2 && *a.wrap_flag != 0) return;
-    if (threadIdx.x == 0) { // ordered before their use by the set-up barriers
-        s_nown = 0;
-        s_fail = 0;
-    }
+    if (threadIdx.x == 0) s_nown = 0; // ordered before its use by the set-up barriers
     // no TMA here, so the 16-byte alignment of dynamic shared memory is
     // enough; indexing smem_dyn directly keeps the accesses in the shared
     // window (32-bit addresses, LDS/STS)
@@ -961,12 +958,13 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
         }
         nred++;
     };
+    bool gfail = false; // the last wait_sum gave up (the same in every thread)
     // completes the last reduction published: warp w gathers records
     // 32 w .. 32 w + 31 (one per lane; the G <= 256 records take at most 8
     // warps, whose loads are all in flight at once), sums them in a fixed
     // order (a shuffle tree per warp, then the warps in order), so every
     // block obtains the same scalars: (pair hi, lo, max, flag) in every
-    // thread.  s_fail, read after it, is block-uniform: 1 after a timeout.
+    // thread.  gfail, read after it, is block-uniform: true after a timeout.
     // (One warp polling all G records, several per lane, took 4-5 us from
     // the last block's publish to completion at 1024^2; a lane per record
     // and a warp per 32 records take under 1 us.)
@@ -1006,25 +1004,26 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
             failed = __any_sync(0xffffffffu, failed);
             if (lane == 0) {
                 s_gw[warp] = make_float4(acc.x, acc.y, mx, flag ? 1.f : 0.f);
-                if (failed) s_fail = 1;
+                s_gwf[warp] = (failed || *((volatile int *)a.status) != 0) ? 1 : 0;
             }
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            float2 acc = make_float2(0.f, 0.f);
-            float mx = 0.f, flag = 0.f;
-            for (int w = 0; w < ngw; w++) {
-                const float4 g = s_gw[w];
-                acc = ff_acc(acc, make_float2(g.x, g.y));
-                mx = fmaxf(mx, g.z);
-                flag = fmaxf(flag, g.w);
-            }
-            acc = ff_norm(acc);
-            s_bcast = make_float4(acc.x, acc.y, mx, flag);
-            if (*((volatile int *)a.status) != 0) s_fail = 1;
+        // every thread adds the warps' sums in the same fixed order: the same
+        // bits everywhere, with no second barrier.  (The next writes of s_gw
+        // come after at least one more block barrier.)
+        float2 acc = make_float2(0.f, 0.f);
+        float mx = 0.f, flag = 0.f;
+        int failed = 0;
+        for (int w = 0; w < ngw; w++) {
+            const float4 g = s_gw[w];
+            acc = ff_acc(acc, make_float2(g.x, g.y));
+            mx = fmaxf(mx, g.z);
+            flag = fmaxf(flag, g.w);
+            failed |= s_gwf[w];
         }
-        __syncthreads();
-        return s_bcast;
+        gfail = failed != 0;
+        acc = ff_norm(acc);
+        return make_float4(acc.x, acc.y, mx, flag);
     };
     // block-uniform: no wait of this launch has timed out (a block barrier)
     auto ok = [&]() { return __syncthreads_or(*((volatile int *)a.status) != 0) == 0; };
@@ -1093,7 +1092,7 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
         const int anynz = __syncthreads_or(nz);
         publish(part, anynz ? 0x80000000u : 0u); // the flag: b has a nonzero
         const float4 s0 = wait_sum();
-        if (s_fail) return;
+        if (gfail) return;
         sigma = make_float2(s0.x, s0.y);
         zero = s0.w == 0.f;
     }
@@ -1229,6 +1228,29 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     auto edge_cell = [&](int e) { return ((e >> 1) + 1) * w2 + ((e & 1) ? w1 : 1); };
     auto edge_op = [&](int e) { return Op[(e >> 1) * w1 + ((e & 1) ? w1 - 1 : 0)]; };
 
+    // |r_{it+1}| at each chunk's last unit row, from the tile holding it (Rb
+    // holds r_{it+1} on the tile); the block barrier of the z.r sum orders
+    // s_cmax / s_cscan before thread 0 publishes them
+    auto chunk_ends = [&]() {
+        auto chunk_end_value = [&](int k, float v) {
+            reinterpret_cast<float *>(a.chunk_val)[k] = v != 0.f ? fabsf(v) : -1.f;
+            if (v != 0.f) atomicMax(&s_cmax, __float_as_int(fabsf(v))); // order of non-negative floats
+            else s_cscan = 1;
+        };
+        if (s_nown <= kMaxOwnedChunks) {
+            for (int j = threadIdx.x; j < s_nown; j += blockDim.x)
+                chunk_end_value(s_own[j].x, Rb[s_own[j].y]);
+        } else {
+            for (int k = threadIdx.x; k < a.nchunks; k += blockDim.x) {
+                const int idx = a.chunk_last_unit[k];
+                if (idx < 0) continue;
+                const int gi = idx / NJ, gj = idx - gi * NJ;
+                if (gi < ti0 || gi >= ti0 + ti || gj < tj0 || gj >= tj0 + tj) continue;
+                chunk_end_value(k, Rb[(gi - ti0 + 2) * w2 + (gj - tj0 + 2)]);
+            }
+        }
+    };
+
     float fb = 0.f, fa_prev = 0.f;
     int result = zero ? 0 : a.iter_limit;
     for (int it = 0; !zero && a.iter_limit > 0; it++) {
@@ -1277,7 +1299,7 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
             }
             // end of iteration it - 1: beta and the stopping test
             const float4 rec = wait_sum();
-            if (s_fail) return;
+            if (gfail) return;
             const float2 newSigma = make_float2(rec.x, rec.y);
             // a zero at a chunk-end unit row needs the backward scan; otherwise
             // the largest |r| over the blocks decides
@@ -1393,7 +1415,7 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
             });
         }
         const float4 qsum = wait_sum();
-        if (s_fail) return;
+        if (gfail) return;
         const float fa = ff_div(sigma, ff_add(make_float2(qsum.x, qsum.y), eps8));
         fa_prev = fa;
         // r_{it+1} = r_it - alpha A s_it (x += alpha s_it on the tile comes at
@@ -1416,6 +1438,8 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
         __syncthreads();
         float zr = 0.f;
         if constexpr (RPS > 0) {
+            // r_{it+1} is in Rb since the barrier above: no barrier of its own
+            chunk_ends();
             const int gj = tj0 + qb - 1;
 #pragma unroll
             for (int rr = 0; rr < kR; rr++) {
@@ -1452,24 +1476,9 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
                 }
             }
         }
-        __syncthreads();
-        // |r_{it+1}| at each chunk's last unit row, from the tile holding it
-        auto chunk_end_value = [&](int k, float v) {
-            reinterpret_cast<float *>(a.chunk_val)[k] = v != 0.f ? fabsf(v) : -1.f;
-            if (v != 0.f) atomicMax(&s_cmax, __float_as_int(fabsf(v))); // order of non-negative floats
-            else s_cscan = 1;
-        };
-        if (s_nown <= kMaxOwnedChunks) {
-            for (int j = threadIdx.x; j < s_nown; j += blockDim.x)
-                chunk_end_value(s_own[j].x, Rb[s_own[j].y]);
-        } else {
-            for (int k = threadIdx.x; k < a.nchunks; k += blockDim.x) {
-                const int idx = a.chunk_last_unit[k];
-                if (idx < 0) continue;
-                const int gi = idx / NJ, gj = idx - gi * NJ;
-                if (gi < ti0 || gi >= ti0 + ti || gj < tj0 || gj >= tj0 + tj) continue;
-                chunk_end_value(k, Rb[(gi - ti0 + 2) * w2 + (gj - tj0 + 2)]);
-            }
+        if constexpr (RPS == 0) {
+            __syncthreads(); // the sweep above stored r_{it+1} in Rb
+            chunk_ends();
         }
         {
             const float2 part = bsum0(zr, smf); // its barrier also orders s_cmax / s_cscan
