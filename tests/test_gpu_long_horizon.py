@@ -12,9 +12,12 @@ the first frame, measures that: by frame 50 a one-ulp change moves the
 particle count by about 40 % and the kinetic energy by more than 100 %.  So
 the bars are:
 
-* early frames (2-6, before the trajectories separate): each statistic of
-  the GPU within EARLY_FACTOR times the ensemble's largest deviation from the
-  unperturbed run, plus EARLY_FLOOR relative;
+* early frames (2-6, before the trajectories separate): the GPU's particle
+  count and fluid volume within EARLY_FACTOR times the ensemble's largest
+  deviation from the unperturbed run, plus EARLY_FLOOR relative.  The
+  kinetic energy is left to the mean bar: a one-ulp perturbation moves it by
+  up to 40 % as early as frame 5, so a per-frame bar would need a far larger
+  ensemble to mean anything;
 * the whole run: the GPU's mean over frames 20-60 of each statistic within
   MEAN_SIGMAS ensemble standard deviations (of the members' own means) of the
   ensemble mean, plus MEAN_FLOOR relative.
@@ -36,6 +39,7 @@ LATE = slice(19, FRAMES)  # frames 20-60
 EARLY_FACTOR, EARLY_FLOOR = 3.0, 0.01
 MEAN_SIGMAS, MEAN_FLOOR = 3.0, 0.05
 NAMES = ("particles", "kinetic energy", "fluid cells")
+EARLY_STATS = (0, 2)  # particle count and fluid volume
 
 
 def stats(particles, material):
@@ -80,10 +84,12 @@ def test_c1_sixty_frames_statistics(gpu_lib, ensemble, precision):
     spread = np.max(np.abs(ensemble[1:] - base), axis=0)  # per frame, per statistic
     tag = "FP32" if precision == gpu.FS_PCG_FP32 else "FP64"
     for f in EARLY:
-        for k, name in enumerate(NAMES):
+        print(f"\n{tag} frame {f + 1}: GPU {g[f].tolist()} oracle {base[f].tolist()} "
+              f"ensemble spread {spread[f].tolist()}")
+        for k in EARLY_STATS:
             bar = EARLY_FACTOR * spread[f, k] + EARLY_FLOOR * abs(base[f, k])
             dev = abs(g[f, k] - base[f, k])
-            assert dev <= bar, f"{tag} frame {f + 1} {name}: {g[f, k]} vs oracle {base[f, k]} (bar {bar})"
+            assert dev <= bar, f"{tag} frame {f + 1} {NAMES[k]}: {g[f, k]} vs oracle {base[f, k]} (bar {bar})"
     member_means = ensemble[:, LATE, :].mean(axis=1)  # ENSEMBLE x 3
     mu, sd = member_means.mean(axis=0), member_means.std(axis=0, ddof=1)
     gm = g[LATE].mean(axis=0)
