@@ -968,9 +968,20 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     // (One warp polling all G records, several per lane, took 4-5 us from
     // the last block's publish to completion at 1024^2; a lane per record
     // and a warp per 32 records take under 1 us.)
-    auto wait_sum = [&]() -> float4 {
+    float fa_prev = 0.f; // alpha of the last iteration
+    auto wait_sum = [&](bool with_x) -> float4 {
         const unsigned k = nred - 1, ep = ep0 + nred;
         const int ngw = (G + 31) >> 5;
+        if (warp >= ngw && with_x) {
+            if constexpr (RPS > 0) {
+                // x += alpha s of the last iteration (s is still in Sb): the
+                // warps that gather no records do it while the others poll
+                const int nx = nw - ngw;
+                for (int r = warp - ngw; r < ti; r += nx)
+                    for (int q = lane; q < tj; q += 32)
+                        Xt[r * tj + q] = fmaf(Sb[(r + 2) * w2 + (q + 2)], fa_prev, Xt[r * tj + q]);
+            }
+        }
         if (warp < ngw) {
             const unsigned long long *base = recs + (size_t)(k & 1) * G * kRecWords;
             const int b = warp * 32 + lane;
@@ -1091,7 +1102,7 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
         const float2 part = bsum0(bb, smf); // its block barrier also retires Ib
         const int anynz = __syncthreads_or(nz);
         publish(part, anynz ? 0x80000000u : 0u); // the flag: b has a nonzero
-        const float4 s0 = wait_sum();
+        const float4 s0 = wait_sum(false);
         if (gfail) return;
         sigma = make_float2(s0.x, s0.y);
         zero = s0.w == 0.f;
@@ -1251,7 +1262,7 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
         }
     };
 
-    float fb = 0.f, fa_prev = 0.f;
+    float fb = 0.f;
     int result = zero ? 0 : a.iter_limit;
     for (int it = 0; !zero && a.iter_limit > 0; it++) {
         const bool first = it == 0;
@@ -1260,18 +1271,6 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
 
         // ---- sweep 1 -------------------------------------------------------
         if (!first) {
-            if constexpr (RPS > 0) {
-                // x += alpha s of the last iteration (s is still in Sb, alpha
-                // known): done here, in the time the neighbours take to
-                // publish, rather than on the path of the last sweep
-#pragma unroll
-                for (int rr = 0; rr < kR; rr++) {
-                    if (on_tile(rr)) {
-                        float *xp = Xt + (row0 + rr - 1) * tj + (qb - 1);
-                        *xp = fmaf(Sb[cbase + rr * w2], fa_prev, *xp);
-                    }
-                }
-            }
             const bool more = it < a.iter_limit;
             if (more) {
                 // z_it = M r_it on the tile and its 1-halo while the grid
@@ -1298,7 +1297,7 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
                 }
             }
             // end of iteration it - 1: beta and the stopping test
-            const float4 rec = wait_sum();
+            const float4 rec = wait_sum(true); // and x += alpha s_{it-1}
             if (gfail) return;
             const float2 newSigma = make_float2(rec.x, rec.y);
             // a zero at a chunk-end unit row needs the backward scan; otherwise
@@ -1414,12 +1413,12 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
                 B1[r * w1 + q] = apply_a(Op[r * w1 + q], Sb, (r + 1) * w2 + (q + 1), w2);
             });
         }
-        const float4 qsum = wait_sum();
+        const float4 qsum = wait_sum(false);
         if (gfail) return;
         const float fa = ff_div(sigma, ff_add(make_float2(qsum.x, qsum.y), eps8));
         fa_prev = fa;
-        // r_{it+1} = r_it - alpha A s_it (x += alpha s_it on the tile comes at
-        // the start of the next iteration)
+        // r_{it+1} = r_it - alpha A s_it (x += alpha s_it on the tile comes
+        // during the next iteration's beta reduction)
         if constexpr (RPS > 0) {
 #pragma unroll
             for (int rr = 0; rr < kR; rr++) Rr[rr] = fmaf(-Sr[rr], fa, Rr[rr]);
