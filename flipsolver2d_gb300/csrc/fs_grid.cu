@@ -562,11 +562,17 @@ __device__ __forceinline__ float bfs_layer_value(const int *nm, const float *val
             if (add == 0 && s == 0.f && eh == 0.f && el == 0.f) return 0.f;
         }
     }
+    // f is the reference's float when the double result D lies strictly
+    // inside f's rounding interval (half the smaller spacing either side):
+    // |D - f| <= |h + l - f| + bound, and h + l - f = d within one rounding
+    // of d (h - f is exact).  The factor 1.0001 covers the float roundings of
+    // this test itself; a cell whose value sits closer to a rounding
+    // boundary than that (about 1 in 10^4) takes the double path below.
     const float d = (h - f) + l;
     const float bound = (m + 1.f) * 0x1p-44f;
     const float gap = 0.5f * fminf(nextafterf(f, INFINITY) - f, f - nextafterf(f, -INFINITY));
     if (count > 0 && isfinite(f) && isfinite(m) && fabsf(f) >= 0x1p-100f &&
-        fabsf(d) + bound < 0.99f * gap)
+        (fabsf(d) + bound) * 1.0001f < gap)
         return f;
     const double avg = bfs_avg<W>(nm, val, r, q, k, count);
     // dividing by 1, 2, 4 or 8 is an exact scaling, the same as multiplying
@@ -637,10 +643,13 @@ __device__ __forceinline__ void bfs_layers(int *mark, float *val, short *fa, sho
         for (int b = 0; b < 9; b++)
             if (got & (1u << b)) out[slot++] = (short)((r + b / 3 - 1) * W + (q + b % 3 - 1));
     };
-    // layer k0 (final from earlier passes) discovers layer k0 + 1
+    // layer k0 (final from earlier passes) discovers layer k0 + 1; a warp
+    // with no layer-k0 cell in this round skips the expansion (its append
+    // would add nothing)
     for (int e0 = 0; e0 < W * W; e0 += blockDim.x) {
         const int e = e0 + (int)threadIdx.x;
         const bool live = e < W * W && mark[e] == k0;
+        if (!__any_sync(0xffffffffu, live)) continue;
         int nm[8];
         if (live) bfs_marks<W>(mark, e / W, e - (e / W) * W, nm);
         expand(live, e, nm, k0, fa, &cnt[(k0 + 1) % 3]);
@@ -659,6 +668,7 @@ __device__ __forceinline__ void bfs_layers(int *mark, float *val, short *fa, sho
         for (int f0 = 0; f0 < ncur; f0 += blockDim.x) {
             const int f = f0 + (int)threadIdx.x;
             const bool live = f < ncur;
+            if (f0 + (int)(threadIdx.x & ~31u) >= ncur) continue; // a warp past the list
             int e = 0;
             int nm[8];
             if (live) {
