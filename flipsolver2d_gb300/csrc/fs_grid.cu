@@ -555,7 +555,9 @@ __device__ __forceinline__ float bfs_layer_value(const int *nm, const float *val
         const int ea = qh != 0.f ? ilogbf(qh) : -1000;
         const int lsb = min(qh != 0.f ? ilogbf(qh) - 23 : INT_MAX, ql != 0.f ? ilogbf(ql) - 23 : INT_MAX);
         // qh + ql (the quotient) must fit a double, and so must it minus one
-        const bool sub_exact = add != 0 ? (max(ea, 0) + 1 - min(lsb, 0) <= 52) : (ea - lsb <= 51);
+        // (a zero quotient, qh = ql = 0, is exact; lsb is INT_MAX then)
+        const bool sub_exact = (qh == 0.f && ql == 0.f) ||
+                               (add != 0 ? (max(ea, 0) + 1 - min(lsb, 0) <= 52) : (ea - lsb <= 51));
         if (sum_exact && sub_exact) {
             if (f != 0.f && isfinite(f)) return f;
             // an exact zero sum: the reference's double sum is +0 as well
