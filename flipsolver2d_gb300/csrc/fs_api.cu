@@ -554,6 +554,16 @@ static fs_status create_impl(const fs_params *p, const fs_exec_params *exec, boo
         A(dalloc(s, &rpart, (size_t)kSpecResBlocks));
         A(dalloc(s, &count, 1));
         A(dalloc(s, &ctl, 1));
+        // inner solves on the resident kernel where the grid fits it (the
+        // handle's exchange words, unused by the FP32 path in this mode)
+        int rti = 0, rtj = 0;
+        const bool res = spec_resident_shape(d.ni, d.nj, &rti, &rtj);
+        if (res) {
+            s->ll.words = n;
+            A(dalloc(s, &s->ll.r, n));
+            A(dalloc(s, &s->ll.s, n));
+            A(dalloc(s, &s->ll.rec, kLlRecWords));
+        }
         for (int k = 0; k < 2; k++) {
             SpecSolve &c = s->spec_chain[k];
             c.ni = d.ni;
@@ -579,6 +589,12 @@ static fs_status create_impl(const fs_params *p, const fs_exec_params *exec, boo
             c.tol = kSpecRelTol;
             c.max_iter = kSpecMaxIter;
             c.max_outer = kSpecMaxOuter;
+            if (res) {
+                c.res_ti = rti;
+                c.res_tj = rtj;
+                c.ll = &s->ll;
+                c.wrap_flag = &s->sc->wrap_units;
+            }
         }
     } else if (s->prec == FS_PCG_SPEC) {
         A(dalloc(s, &s->spec_sys, 2));
@@ -1101,7 +1117,7 @@ static fs_status run_pcg(fs_solver *s, const void *b, void *x, int *iters)
         e = launch_pcg<double>(pcg_args<double>(s, b, x, iters), s->st, &launched);
     } else if (s->prec == FS_PCG_SPEC && s->spec_large) {
         e = launch_spec_chain(s->spec_chain[slot], s->st);
-        launched = 4 * kSpecMaxOuter + 2;
+        launched = spec_chain_kernels(s->spec_chain[slot]);
     } else if (s->prec == FS_PCG_SPEC) {
         e = launch_pcg_cluster(s->spec_sys + slot, 1, s->spec_plan, spec_params(), s->st);
         launched = 1;
@@ -1926,6 +1942,7 @@ struct BatchSolve {
     bool large = false; // above the on-chip limit: a chained solve
     SpecSolve chain{};
     void *chain_mem = nullptr;
+    LlBuffers ll; // its resident inner solves' exchange words (in chain_mem)
 };
 
 struct fs_batch {
@@ -1976,7 +1993,7 @@ static fs_status batch_capture(fs_batch *b, BatchScene &bs, int parity)
                 if (s->spec_large) { // its own chained solve, not a merged one
                     if (launch_spec_chain(s->spec_chain[0], q) != cudaSuccess)
                         st = fail(FS_ERR_CUDA, "fs_batch: capture of a chained solve");
-                    g_kernel_launches += 4 * kSpecMaxOuter + 2;
+                    g_kernel_launches += spec_chain_kernels(s->spec_chain[0]);
                 }
             }
         } else if (seg == 1) {
@@ -1994,7 +2011,7 @@ static fs_status batch_capture(fs_batch *b, BatchScene &bs, int parity)
                 if (st == FS_OK && s->spec_large) {
                     if (launch_spec_chain(s->spec_chain[1], q) != cudaSuccess)
                         st = fail(FS_ERR_CUDA, "fs_batch: capture of a chained solve");
-                    g_kernel_launches += 4 * kSpecMaxOuter + 2;
+                    g_kernel_launches += spec_chain_kernels(s->spec_chain[1]);
                 }
             }
         } else {
@@ -2257,7 +2274,10 @@ extern "C" fs_status fs_batch_submit_solve(fs_batch *b, const fs_poisson_system 
         // the chained cooperative solve's vectors and control block
         const size_t fb = ((N * 4 + 255) & ~(size_t)255);
         const size_t pb = (((size_t)spec_partials_needed() * sizeof(float2) + 255) & ~(size_t)255);
-        const size_t cbytes = 5 * fb + pb + (size_t)kSpecResBlocks * 8 + 256;
+        int rti = 0, rtj = 0;
+        const bool res = spec_resident_shape(q->ni, q->nj, &rti, &rtj);
+        const size_t lb = res ? 2 * N * 8 + kLlRecWords * 8 : 0; // exchange words
+        const size_t cbytes = 5 * fb + pb + (size_t)kSpecResBlocks * 8 + 256 + lb;
         cudaError_t ec = cudaMalloc(&v.chain_mem, cbytes);
         if (ec != cudaSuccess)
             return fail(ec == cudaErrorMemoryAllocation ? FS_ERR_OOM : FS_ERR_CUDA,
@@ -2274,6 +2294,18 @@ extern "C" fs_status fs_batch_submit_solve(fs_batch *b, const fs_poisson_system 
         v.chain.ctl = reinterpret_cast<SpecCtl *>(t);
         v.chain.count = reinterpret_cast<unsigned *>(t + 64);
         v.chain.status = reinterpret_cast<int *>(t + 128);
+        if (res) {
+            // its own copy of the decomposition's j-edge flag (the batch's
+            // scalars serve every submission)
+            v.chain.wrap_flag = reinterpret_cast<const int *>(t + 192);
+            v.chain.res_ti = rti;
+            v.chain.res_tj = rtj;
+            unsigned long long *w = reinterpret_cast<unsigned long long *>(t + 256);
+            v.ll.r = w;
+            v.ll.s = w + N;
+            v.ll.rec = w + 2 * N;
+            v.ll.words = N;
+        }
         if ((ec = cudaMemset(t + 128, 0, sizeof(int))) != cudaSuccess) {
             cudaFree(v.chain_mem);
             return fail(FS_ERR_CUDA, "fs_batch_submit_solve: %s", cudaGetErrorString(ec));
@@ -2297,6 +2329,7 @@ extern "C" fs_status fs_batch_submit_solve(fs_batch *b, const fs_poisson_system 
     cudaStream_t st = b->bst;
     auto bail = [&](cudaError_t err) {
         cudaFree(v.mem);
+        if (v.chain_mem) cudaFree(v.chain_mem);
         return fail(FS_ERR_CUDA, "fs_batch_submit_solve: %s", cudaGetErrorString(err));
     };
     if ((e = cudaMemcpyAsync(mat, q->material, N, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
@@ -2310,6 +2343,10 @@ extern "C" fs_status fs_batch_submit_solve(fs_batch *b, const fs_poisson_system 
     launch_decomposition(gd, G, b->chunk_last, 1, (long long)N, 0, b->dsc, st);
     g_kernel_launches += 1;
     if ((e = cudaGetLastError()) != cudaSuccess) return bail(e);
+    if (v.chain.wrap_flag &&
+        (e = cudaMemcpyAsync(const_cast<int *>(v.chain.wrap_flag), &b->dsc->wrap_units, sizeof(int),
+                             cudaMemcpyDeviceToDevice, st)) != cudaSuccess)
+        return bail(e);
     // the host arrays may be reused once this returns
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return bail(e);
     v.ticket = b->next_ticket++;
@@ -2451,8 +2488,10 @@ static fs_status batch_solve(fs_batch *b, const std::vector<int> &act, const std
         for (int k : act) CK(cudaStreamWaitEvent(b->bst, b->sc[k].ev, 0));
         for (int k : extra)
             if (b->solves[k].large) {
-                CK(launch_spec_chain(b->solves[k].chain, b->bst));
-                g_kernel_launches += 4 * kSpecMaxOuter + 2;
+                BatchSolve &v = b->solves[k];
+                v.chain.ll = v.chain.res_ti > 0 ? &v.ll : nullptr; // the vector may have moved it
+                CK(launch_spec_chain(v.chain, b->bst));
+                g_kernel_launches += spec_chain_kernels(v.chain);
             }
     }
     if (ent.empty()) {
@@ -3024,8 +3063,21 @@ extern "C" fs_status fs_pcg_solve_spec(int ni, int nj, const int8_t *material, f
     p.tol = rel_tol;
     p.max_iter = max_iter;
     p.max_outer = kSpecMaxOuter;
+    // inner solves on the resident kernel where the grid fits it
+    LlBuffers ll;
+    int rti = 0, rtj = 0;
+    if (spec_resident_shape(ni, nj, &rti, &rtj)) {
+        TRY(dalloc_tmp((void **)&ll.r, N * 8));
+        TRY(dalloc_tmp((void **)&ll.s, N * 8));
+        TRY(dalloc_tmp((void **)&ll.rec, kLlRecWords * 8));
+        ll.words = N;
+        p.res_ti = rti;
+        p.res_tj = rtj;
+        p.ll = &ll;
+        p.wrap_flag = &sc->wrap_units;
+    }
     TRY(check(launch_spec_chain(p, st), "solve"));
-    g_kernel_launches += 4 * kSpecMaxOuter + 2;
+    g_kernel_launches += spec_chain_kernels(p);
     int h_status = 0, it = 0;
     double rel = 0.0;
     TRY(check(cudaMemcpyAsync(&h_status, &sc->pcg_status, sizeof(int), cudaMemcpyDeviceToHost, st), "readback"));

@@ -46,6 +46,12 @@ template <typename T> struct PcgArgs {
     const int *wrap_flag;      // set by the decomposition when a unit row sits on
                                // the j = 0 or j = NJ-1 edge (linear-index wrap)
     int mode;                  // 0 run, 1 run only if *wrap_flag, 2 only if !*wrap_flag
+    // spec-mode inner solves (the resident kernel with the K K^T
+    // preconditioner): the chained solve's control block (skip when done,
+    // inner tolerance and iterations left from it, totals back to it) and
+    // the device dt the operator's scale comes from
+    struct SpecCtl *spec_ctl;
+    const float *spec_dt;
 };
 
 // Owner of a set of exchange-word buffers (a solver handle, the per-device

@@ -29,6 +29,7 @@
 #include "fs_device.h"
 #include "fs_pcg.h"
 #include "fs_pcg_tma.h"
+#include "fs_spec.h"
 
 namespace fsg {
 
@@ -794,6 +795,40 @@ __device__ __forceinline__ float2 bsum0(float v, float *sm)
     return x;
 }
 
+// bsum0 of two values at once (sm: 4 floats a warp, at most 16 warps)
+__device__ __forceinline__ void bsum0_2(float v0, float v1, float *sm, float2 &o0, float2 &o1)
+{
+    float2 a0 = make_float2(v0, 0.f), a1 = make_float2(v1, 0.f);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a0 = ff_acc(a0, ff_shfl_down(a0, o));
+        a1 = ff_acc(a1, ff_shfl_down(a1, o));
+    }
+    a0 = ff_norm(a0);
+    a1 = ff_norm(a1);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) {
+        sm[4 * w] = a0.x;
+        sm[4 * w + 1] = a0.y;
+        sm[4 * w + 2] = a1.x;
+        sm[4 * w + 3] = a1.y;
+    }
+    __syncthreads();
+    o0 = o1 = make_float2(0.f, 0.f);
+    if (w == 0) {
+        const bool in = lane < (int)(blockDim.x >> 5);
+        float2 x0 = in ? make_float2(sm[4 * lane], sm[4 * lane + 1]) : make_float2(0.f, 0.f);
+        float2 x1 = in ? make_float2(sm[4 * lane + 2], sm[4 * lane + 3]) : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            x0 = ff_acc(x0, ff_shfl_down(x0, o));
+            x1 = ff_acc(x1, ff_shfl_down(x1, o));
+        }
+        o0 = ff_norm(x0);
+        o1 = ff_norm(x1);
+    }
+}
+
 __device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned *p)
 {
     unsigned v;
@@ -858,6 +893,43 @@ __device__ __forceinline__ float ipp_apply(unsigned p, const float *inv, float v
     return (p & 0x80) ? acc : vc;
 }
 
+// z = K K^T v at one cell, the textbook incomplete-Poisson preconditioner of
+// the spec-mode solve (inversepoissonpreconditioner.h:45-79: K = I - L D^-1,
+// L the strictly lower part of the pressure matrix, D its diagonal), from
+// the cell's value and six neighbours' (down, right, up, up-right, left,
+// down-left).  y = K^T v at the cell and at its upper and left neighbours,
+// then z = K y, each combined in the order the linear-index form evaluates
+// it.  Operator word p (the spec packing):
+//   bits 0-7   the cell's own operator byte
+//   bit 8      the cell below is a unit row whose upper neighbour is fluid
+//   bit 9      the cell to the right is a unit row whose left neighbour is fluid
+//   bits 10-12 K code of the upper neighbour, bit 13 its bit 9
+//   bits 14-16 K code of the left neighbour, bit 17 its bit 8
+// K code: the non-solid count of a unit row with one, else 0; kk[code] is
+// 1 / count, or the operator's scale for code 0 (Eigen's zero-diagonal rule
+// on an identity row).
+__device__ __forceinline__ float kkt_apply(unsigned p, const float *kk, float vc, float dn, float rt,
+                                           float up, float ur, float lf, float dl)
+{
+    const float kc = kk[(p & 0x80) ? ((p >> 4) & 7) : 0];
+    const float ku = kk[(p >> 10) & 7], kl = kk[(p >> 14) & 7];
+    const bool up_in = (p & 0x81) == 0x81; // unit row, upper neighbour fluid
+    const bool lf_in = (p & 0x84) == 0x84; // unit row, left neighbour fluid
+    float yc = vc;
+    yc = (p & 0x100) ? fmaf(kc, dn, yc) : yc;
+    yc = (p & 0x200) ? fmaf(kc, rt, yc) : yc;
+    float yu = up;
+    yu = up_in ? fmaf(ku, vc, yu) : yu;
+    yu = (p & 0x2000) ? fmaf(ku, ur, yu) : yu;
+    float yl = lf;
+    yl = (p & 0x20000) ? fmaf(kl, dl, yl) : yl;
+    yl = lf_in ? fmaf(kl, vc, yl) : yl;
+    float z = yc;
+    z = up_in ? fmaf(ku, yu, z) : z;
+    z = lf_in ? fmaf(kl, yl, z) : z;
+    return z;
+}
+
 // (A v) at one cell (the pressure matrix row; identity on non-unit rows)
 __device__ __forceinline__ float op_apply(unsigned p, float scale, float vc, float up, float dn,
                                           float lf, float rt)
@@ -891,10 +963,11 @@ __device__ __forceinline__ float op_apply(unsigned p, float scale, float vc, flo
 // or halo, goes through the same ipp_apply / op_apply, so values that two
 // tiles both compute agree bit for bit.
 // ---------------------------------------------------------------------------
-template <int RPS>
+template <int RPS, bool SPEC>
 __global__ void __launch_bounds__(RPS > 0 ? kStripThreads : kThreads, 1)
 k_pcg_resident(PcgArgs<float> a, int ti, int tj)
 {
+    static_assert(!SPEC || RPS > 0, "spec-mode solves run on register strips");
     const long long lim = a.spin_limit > 0 ? a.spin_limit : kSpinLimit;
     extern __shared__ unsigned char smem_dyn[];
     __shared__ float smf[64];
@@ -907,6 +980,16 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     __shared__ int2 s_own[kMaxOwnedChunks]; // (chunk, Rb index)
     if (a.mode == 1 && *a.wrap_flag == 0) return;
     if (a.mode == 2 && *a.wrap_flag != 0) return;
+    // spec mode: the chained solve's state, read by every block before any
+    // block publishes (block 0 writes the totals back only after the last
+    // reduction, which every block has joined)
+    int iter_limit = a.iter_limit;
+    float eps_in = 0.f;
+    if constexpr (SPEC) {
+        if (*((volatile const int *)&a.spec_ctl->done)) return;
+        eps_in = *((volatile const float *)&a.spec_ctl->eps_in);
+        iter_limit = a.iter_limit - *((volatile const int *)&a.spec_ctl->total);
+    }
     if (threadIdx.x == 0) s_nown = 0; // ordered before its use by the set-up barriers
     // no TMA here, so the 16-byte alignment of dynamic shared memory is
     // enough; indexing smem_dyn directly keeps the accesses in the shared
@@ -933,7 +1016,7 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     unsigned long long *recs = a.ll_rec;
     const unsigned ep0 = a.ll_base;
     unsigned nred = 0;                // reductions published so far
-    unsigned *count = &a.bar->count;  // arrivals at the rare fenced barrier
+    unsigned *count = SPEC ? nullptr : &a.bar->count; // arrivals at the rare fenced barrier
     unsigned nfenced = 0;
     // chunks without a unit row report DBL_MIN (VOps::maxAbs) on every iteration
     int has_min_static = 0;
@@ -941,20 +1024,31 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     const TolTest tt = tol_test(a.tol);
     const float2 eps8 = make_float2((float)1e-8, (float)(1e-8 - (double)(float)1e-8));
 
-    const double scale_d = pcg_scale(a);
+    const double scale_d = SPEC ? (double)*a.spec_dt / (a.density * a.dx * a.dx) : pcg_scale(a);
     const float scale = (float)scale_d;
-    if (threadIdx.x < 8)
-        inv[threadIdx.x] = (threadIdx.x >= 1 && threadIdx.x <= 4) ? (float)(1.0 / (threadIdx.x * scale_d)) : 0.f;
+    // the preconditioner's coefficients by neighbour count: IPP 1 / (n
+    // scale); spec mode the K table (1 / n, the scale for code 0)
+    if (threadIdx.x < 8) {
+        const int n = (int)threadIdx.x;
+        if constexpr (SPEC)
+            inv[n] = n == 0 ? scale : (n <= 4 ? 1.f / (float)n : 0.f);
+        else
+            inv[n] = (n >= 1 && n <= 4) ? (float)(1.0 / (n * scale_d)) : 0.f;
+    }
 
     // thread 0, holding the block's partial (hi, lo) and the extra word:
     // publish them as this block's record of the next reduction.  Every
     // thread counts the reduction.
-    auto publish = [&](float2 part, unsigned extra) {
+    // (Spec mode: a second pair, r.r, in the last two words.)
+    auto publish = [&](float2 part, unsigned extra, float2 part2 = make_float2(0.f, 0.f)) {
         if (threadIdx.x == 0) {
             const unsigned ep = ep0 + 1 + nred;
             unsigned long long *r = recs + ((size_t)(nred & 1) * G + blockIdx.x) * kRecWords;
             st_ll2(r, ll_pack(__float_as_uint(part.x), ep), ll_pack(__float_as_uint(part.y), ep));
-            st_ll(r + 2, ll_pack(extra, ep));
+            if constexpr (SPEC)
+                st_ll2(r + 2, ll_pack(__float_as_uint(part2.x), ep), ll_pack(__float_as_uint(part2.y), ep));
+            else
+                st_ll(r + 2, ll_pack(extra, ep));
         }
         nred++;
     };
@@ -985,36 +1079,52 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
         if (warp < ngw) {
             const unsigned long long *base = recs + (size_t)(k & 1) * G * kRecWords;
             const int b = warp * 32 + lane;
-            unsigned long long w0 = 0ull, w1 = 0ull, w2 = 0ull;
+            unsigned long long w0 = 0ull, w1 = 0ull, w2 = 0ull, w3 = 0ull;
             bool failed = false;
             if (b < G) {
                 const unsigned long long *rp = base + (size_t)b * kRecWords;
-                ld_ll2(rp, w0, w1);
-                w2 = ld_ll(rp + 2);
+                auto load = [&]() {
+                    ld_ll2(rp, w0, w1);
+                    if constexpr (SPEC) ld_ll2(rp + 2, w2, w3);
+                    else w2 = ld_ll(rp + 2);
+                };
+                load();
                 long long spins = 0;
-                while (ll_epoch(w0) != ep || ll_epoch(w1) != ep || ll_epoch(w2) != ep) {
+                while (ll_epoch(w0) != ep || ll_epoch(w1) != ep || ll_epoch(w2) != ep ||
+                       (SPEC && ll_epoch(w3) != ep)) {
                     if (++spins > lim || ((spins & 255) == 0 && *((volatile int *)a.status) != 0)) {
                         atomicExch(a.status, 1);
                         failed = true;
                         break;
                     }
-                    ld_ll2(rp, w0, w1);
-                    w2 = ld_ll(rp + 2);
+                    load();
                 }
             }
             // records past G are zeros: adding them changes nothing
             float2 acc = make_float2(__uint_as_float((unsigned)w0), __uint_as_float((unsigned)w1));
-            float mx = __uint_as_float((unsigned)w2 & 0x7fffffffu);
-            unsigned flag = (unsigned)w2 >> 31;
+            float4 gw;
+            if constexpr (SPEC) {
+                float2 acc2 = make_float2(__uint_as_float((unsigned)w2), __uint_as_float((unsigned)w3));
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                acc = ff_acc(acc, ff_shfl_down(acc, o));
-                mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
-                flag |= __shfl_down_sync(0xffffffffu, flag, o);
+                for (int o = 16; o > 0; o >>= 1) {
+                    acc = ff_acc(acc, ff_shfl_down(acc, o));
+                    acc2 = ff_acc(acc2, ff_shfl_down(acc2, o));
+                }
+                gw = make_float4(acc.x, acc.y, acc2.x, acc2.y);
+            } else {
+                float mx = __uint_as_float((unsigned)w2 & 0x7fffffffu);
+                unsigned flag = (unsigned)w2 >> 31;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    acc = ff_acc(acc, ff_shfl_down(acc, o));
+                    mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
+                    flag |= __shfl_down_sync(0xffffffffu, flag, o);
+                }
+                gw = make_float4(acc.x, acc.y, mx, flag ? 1.f : 0.f);
             }
             failed = __any_sync(0xffffffffu, failed);
             if (lane == 0) {
-                s_gw[warp] = make_float4(acc.x, acc.y, mx, flag ? 1.f : 0.f);
+                s_gw[warp] = gw;
                 s_gwf[warp] = (failed || *((volatile int *)a.status) != 0) ? 1 : 0;
             }
         }
@@ -1022,18 +1132,26 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
         // every thread adds the warps' sums in the same fixed order: the same
         // bits everywhere, with no second barrier.  (The next writes of s_gw
         // come after at least one more block barrier.)
-        float2 acc = make_float2(0.f, 0.f);
+        float2 acc = make_float2(0.f, 0.f), acc2 = make_float2(0.f, 0.f);
         float mx = 0.f, flag = 0.f;
         int failed = 0;
         for (int w = 0; w < ngw; w++) {
             const float4 g = s_gw[w];
             acc = ff_acc(acc, make_float2(g.x, g.y));
-            mx = fmaxf(mx, g.z);
-            flag = fmaxf(flag, g.w);
+            if constexpr (SPEC) {
+                acc2 = ff_acc(acc2, make_float2(g.z, g.w));
+            } else {
+                mx = fmaxf(mx, g.z);
+                flag = fmaxf(flag, g.w);
+            }
             failed |= s_gwf[w];
         }
         gfail = failed != 0;
         acc = ff_norm(acc);
+        if constexpr (SPEC) {
+            acc2 = ff_norm(acc2);
+            return make_float4(acc.x, acc.y, acc2.x, acc2.y); // the two pairs
+        }
         return make_float4(acc.x, acc.y, mx, flag);
     };
     // block-uniform: no wait of this launch has timed out (a block barrier)
@@ -1089,16 +1207,48 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     // (bits 0-7) and the cell counts of its four neighbours (3 bits each:
     // i-1 at 8, i+1 at 11, j-1 at 14, j+1 at 17), which select the IPP
     // coefficients
+    // (spec mode: the K K^T packing of kkt_apply instead)
     for (int e = threadIdx.x; e < L.hp * w1; e += blockDim.x) {
         const int r = e / w1, q = e - r * w1;
         const int c2 = (r + 1) * w2 + (q + 1);
-        Op[e] = (unsigned)Ib[c2] | ((unsigned)((Ib[c2 - w2] >> 4) & 7) << 8) |
-                ((unsigned)((Ib[c2 + w2] >> 4) & 7) << 11) |
-                ((unsigned)((Ib[c2 - 1] >> 4) & 7) << 14) | ((unsigned)((Ib[c2 + 1] >> 4) & 7) << 17);
+        if constexpr (SPEC) {
+            auto kcode = [](unsigned b) { return (b & 0x80) ? ((b >> 4) & 7u) : 0u; };
+            auto dn_in = [](unsigned b) { return (b & 0x81) == 0x81 ? 1u : 0u; }; // its upper neighbour
+            auto rt_in = [](unsigned b) { return (b & 0x84) == 0x84 ? 1u : 0u; }; // its left neighbour
+            Op[e] = (unsigned)Ib[c2] | (dn_in(Ib[c2 + w2]) << 8) | (rt_in(Ib[c2 + 1]) << 9) |
+                    (kcode(Ib[c2 - w2]) << 10) | (rt_in(Ib[c2 - w2 + 1]) << 13) | (kcode(Ib[c2 - 1]) << 14) |
+                    (dn_in(Ib[c2 + w2 - 1]) << 17);
+        } else {
+            Op[e] = (unsigned)Ib[c2] | ((unsigned)((Ib[c2 - w2] >> 4) & 7) << 8) |
+                    ((unsigned)((Ib[c2 + w2] >> 4) & 7) << 11) |
+                    ((unsigned)((Ib[c2 - 1] >> 4) & 7) << 14) | ((unsigned)((Ib[c2 + 1] >> 4) & 7) << 17);
+        }
     }
     float2 sigma;
     bool zero;
-    {
+    float stop = 0.f; // spec mode: r.r at which the inner solve stops
+    if constexpr (SPEC) {
+        // z_0 = K K^T r_0 on the tile and its 1-halo (r_0 = b is known on the
+        // 2-halo) becomes s_0 there; sigma = r.z and r.r over the tile
+        __syncthreads();
+        float rz = 0.f;
+        for (int e = threadIdx.x; e < h1 * w1; e += blockDim.x) {
+            const int r = e / w1, q = e - r * w1;
+            const int c = (r + 1) * w2 + (q + 1);
+            const float z = kkt_apply(Op[e], inv, Rb[c], Rb[c + w2], Rb[c + 1], Rb[c - w2], Rb[c - w2 + 1],
+                                      Rb[c - 1], Rb[c + w2 - 1]);
+            Sb[c] = z;
+            if (r >= 1 && r <= ti && q >= 1 && q <= tj) rz = fmaf(Rb[c], z, rz);
+        }
+        float2 prz, prr;
+        bsum0_2(rz, bb, smf, prz, prr);
+        publish(prz, 0u, prr);
+        const float4 s0 = wait_sum(false);
+        if (gfail) return;
+        sigma = make_float2(s0.x, s0.y);
+        zero = !(s0.z > 0.f);
+        stop = eps_in * eps_in * s0.z;
+    } else {
         const float2 part = bsum0(bb, smf); // its block barrier also retires Ib
         const int anynz = __syncthreads_or(nz);
         publish(part, anynz ? 0x80000000u : 0u); // the flag: b has a nonzero
@@ -1154,6 +1304,57 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
         return ok();
     };
 
+    // strips: the neighbours' values on the 1-deep ring around the tile (the
+    // tile's 1-halo), from their exchange words of epoch ep, into dst (the
+    // tile-plus-1-halo layout, pitch w1); two cells per thread per round,
+    // both loads issued before either is polled.  A block barrier, then a
+    // block-uniform false on timeout.
+    auto load_ring1 = [&](float *dst, const unsigned long long *src, unsigned ep) -> bool {
+        const int n = 2 * w1 + 2 * ti;
+        const int nt = (int)blockDim.x;
+        for (int k0 = threadIdx.x; k0 < n; k0 += 2 * nt) {
+            int g[2] = {-1, -1}, cell[2] = {-1, -1};
+            unsigned long long w[2] = {0ull, 0ull};
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int k = k0 + h * nt;
+                if (k >= n) continue;
+                int hr, hq;
+                if (k < 2 * w1) {
+                    hr = k < w1 ? 0 : h1 - 1;
+                    hq = k < w1 ? k : k - w1;
+                } else {
+                    hr = 1 + ((k - 2 * w1) >> 1);
+                    hq = ((k - 2 * w1) & 1) ? w1 - 1 : 0;
+                }
+                cell[h] = hr * w1 + hq;
+                const int gi = ti0 + hr - 1, gj = tj0 + hq - 1;
+                if (gi >= 0 && gi < NI && gj >= 0 && gj < NJ) {
+                    g[h] = gi * NJ + gj;
+                    w[h] = ld_ll(src + g[h]);
+                }
+            }
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                if (cell[h] < 0) continue;
+                float v = 0.f;
+                if (g[h] >= 0) {
+                    long long spins = 0;
+                    while (ll_epoch(w[h]) != ep) {
+                        if (++spins > lim || ((spins & 255) == 0 && *((volatile int *)a.status) != 0)) {
+                            atomicExch(a.status, 1);
+                            break;
+                        }
+                        w[h] = ld_ll(src + g[h]);
+                    }
+                    v = __uint_as_float((unsigned)w[h]);
+                }
+                dst[cell[h]] = v;
+            }
+        }
+        return ok();
+    };
+
     // the stencils on a row-major shared array of pitch w, centred at c
     auto precond = [&](unsigned p, const float *v, int c, int w) -> float {
         return ipp_apply(p, inv, v[c], v[c - w], v[c + w], v[c - 1], v[c + 1]);
@@ -1178,7 +1379,7 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
 #pragma unroll
         for (int rr = 0; rr < kR; rr++) {
             Rr[rr] = Rb[cbase + rr * w2];
-            Sr[rr] = Rr[rr];
+            Sr[rr] = SPEC ? Sb[cbase + rr * w2] : Rr[rr]; // s_0: z_0 in spec mode, else b
         }
     }
     auto live = [&](int rr) { return row0 + rr < h1; };                     // stored rows
@@ -1192,39 +1393,34 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
         return rr > 0 ? reg[rr > 0 ? rr - 1 : 0] : arr[c - w2];
     };
     // tile cells within two of the tile border (what a neighbour's ring reads)
+    // tile cells on the tile's border: neighbours read them as their 1-halo
+    // ring (z after the z sweep, A s after the A s sweep)
     const int tcol = qb - 1;
-    const bool col_band = tcol < 2 || tcol >= tj - 2;
+    const bool col_band = tcol == 0 || tcol == tj - 1;
     auto in_band = [&](int rr) {
         const int tr = row0 + rr - 1;
-        return col_band || tr < 2 || tr >= ti - 2;
+        return col_band || tr == 0 || tr == ti - 1;
     };
-    // all of the tile's r (in Rb) as exchange words of epoch ep
-    auto publish_tile_r = [&](unsigned ep) {
+    // all of the tile's r (in Rb) into r0 (plain stores; the fenced barrier
+    // that follows orders them before any block reads them)
+    auto publish_tile_r = [&]() {
         for (int r = warp; r < ti; r += nw) {
             const int gi = ti0 + r;
             if (gi >= NI) break;
             for (int q = lane; q < tj; q += 32) {
                 const int gj = tj0 + q;
-                if (gj < NJ)
-                    st_ll(a.ll_r + (size_t)gi * NJ + gj,
-                          ll_pack(__float_as_uint(Rb[(r + 2) * w2 + (q + 2)]), ep));
+                if (gj < NJ) a.r0[(size_t)gi * NJ + gj] = Rb[(r + 2) * w2 + (q + 2)];
             }
         }
     };
-    // after a ring load: the register copy of row h1 (the outer ring row)
-    auto refresh_ring_row = [&](float *reg, const float *arr) {
-#pragma unroll
-        for (int rr = 0; rr < kR; rr++)
-            if (row0 + rr == h1) reg[rr] = arr[cbase + rr * w2];
-    };
-    // halo-column cells (1-halo columns 0 and w1 - 1): with strips of 4 rows
+    // halo-column cells (1-halo columns 0 and w1 - 1; their z and A s land in
+    // B1 with the rings): with strips of 4 rows
     // or more, one a thread on the warps whose strips hold no 1-halo row
     // (strips 1 .. smax, which have no halo row of their own to compute) when
     // they are enough; else four a warp, spread over the warps.  (Measured
     // on GB300: the first takes 0.11 ms off a 200-iteration solve at 1024^2
     // and 0.08 ms at 512^2, but adds 0.14 ms at 256^2, where strips are one
     // row high.)
-    float *Ze = B1; // 2 h1 floats of scratch (B1 is unused with strips)
     int edge0 = (threadIdx.x & 7) == 0 ? (int)(threadIdx.x >> 3) : 1 << 30;
     int edge_step = (int)(blockDim.x >> 3);
     if constexpr (RPS >= 4) {
@@ -1237,6 +1433,8 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
         }
     }
     auto edge_cell = [&](int e) { return ((e >> 1) + 1) * w2 + ((e & 1) ? w1 : 1); };
+    // the same halo-column cell in the tile-plus-1-halo layout of B1
+    auto edge_b1 = [&](int e) { return (e >> 1) * w1 + ((e & 1) ? w1 - 1 : 0); };
     auto edge_op = [&](int e) { return Op[(e >> 1) * w1 + ((e & 1) ? w1 - 1 : 0)]; };
 
     // |r_{it+1}| at each chunk's last unit row, from the tile holding it (Rb
@@ -1263,34 +1461,29 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     };
 
     float fb = 0.f;
-    int result = zero ? 0 : a.iter_limit;
-    for (int it = 0; !zero && a.iter_limit > 0; it++) {
+    int result = zero || iter_limit <= 0 ? 0 : iter_limit;
+    for (int it = 0; !zero && iter_limit > 0; it++) {
         const bool first = it == 0;
         const unsigned ep_s = ep0 + 2u * it + 1u; // epoch of s_it's exchange words
         const unsigned ep_r = ep0 + 2u * it + 2u; // epoch of r_{it+1}'s
 
         // ---- sweep 1 -------------------------------------------------------
         if (!first) {
-            const bool more = it < a.iter_limit;
+            const bool more = it < iter_limit;
             if (more) {
-                // z_it = M r_it on the tile and its 1-halo while the grid
-                // barrier of the last sweep completes
-                if (!load_ring_ll(Rb, a.ll_r, ep0 + 2u * it)) return;
                 if constexpr (RPS > 0) {
-                    refresh_ring_row(Rr, Rb);
-                    // z on the tile rows came with the last sweep's z.r (step F);
-                    // only the 1-halo rows need the ring
+                    // z_it on the tile's 1-halo as the neighbours computed it on
+                    // their border (their z sweep published it); z on the tile
+                    // rows came with the last sweep's z.r.  Halo columns read it
+                    // from B1 in the s update.
+                    if (!load_ring1(B1, a.ll_r, ep0 + 2u * it)) return;
 #pragma unroll
-                    for (int rr = 0; rr < kR; rr++) {
-                        if (!on_tile(rr)) {
-                            const int c = cbase + rr * w2;
-                            Sr[rr] = ipp_apply(Ost[rr * w1], inv, Rr[rr], up_of(Rr, Rb, rr, c),
-                                               dn_of(Rr, Rb, rr, c), Rb[c - 1], Rb[c + 1]);
-                        }
-                    }
-                    for (int ed = edge0; ed < 2 * h1; ed += edge_step)
-                        Ze[ed] = precond(edge_op(ed), Rb, edge_cell(ed), w2);
+                    for (int rr = 0; rr < kR; rr++)
+                        if (live(rr) && !on_tile(rr)) Sr[rr] = B1[(row0 + rr) * w1 + qb];
                 } else {
+                    // z_it = M r_it on the tile and its 1-halo while the grid
+                    // barrier of the last sweep completes
+                    if (!load_ring_ll(Rb, a.ll_r, ep0 + 2u * it)) return;
                     for_halo1(h1, w1, [&](int r, int q) {
                         B1[r * w1 + q] = precond(Op[r * w1 + q], Rb, (r + 1) * w2 + (q + 1), w2);
                     });
@@ -1300,26 +1493,32 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
             const float4 rec = wait_sum(true); // and x += alpha s_{it-1}
             if (gfail) return;
             const float2 newSigma = make_float2(rec.x, rec.y);
-            // a zero at a chunk-end unit row needs the backward scan; otherwise
-            // the largest |r| over the blocks decides
-            if (rec.w != 0.f) {
-                // the scan reads r anywhere in a chunk: every tile publishes
-                // all of r_it (still intact in Rb) and the grid meets at a
-                // fenced barrier
-                publish_tile_r(ep0 + 2u * it);
-                if (!fenced_barrier()) return;
+            if constexpr (SPEC) {
+                // spec mode: r.r against the inner tolerance (k_pcg_spec's rule)
+                if (rec.z <= stop || !more) {
+                    result = it;
+                    break;
+                }
+            } else {
+                // a zero at a chunk-end unit row needs the backward scan;
+                // otherwise the largest |r| over the blocks decides
+                if (rec.w != 0.f) {
+                    // the scan reads r anywhere in a chunk: every tile
+                    // publishes all of r_it (still intact in Rb) and the grid
+                    // meets at a fenced barrier
+                    publish_tile_r();
+                    if (!fenced_barrier()) return;
+                }
+                const bool done =
+                    rec.w != 0.f
+                        ? chunk_converged(a, [&](long long e) { return __ldcg(a.r0 + e); }, tt, &s_flag)
+                        : tol_met(tt, rec.z, has_min_static);
+                if (done) {
+                    result = it - 1;
+                    break;
+                }
+                if (!more) break;
             }
-            const bool done =
-                rec.w != 0.f
-                    ? chunk_converged(
-                          a, [&](long long e) { return __uint_as_float((unsigned)__ldcg(a.ll_r + e)); },
-                          tt, &s_flag)
-                    : tol_met(tt, rec.z, has_min_static);
-            if (done) {
-                result = it - 1;
-                break;
-            }
-            if (!more) break;
             fb = ff_div(newSigma, sigma);
             sigma = newSigma;
             // s_it = z_it + beta s_{it-1}
@@ -1334,7 +1533,7 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
                     if (live(rr)) Sb[cbase + rr * w2] = Sr[rr];
                 for (int ed = edge0; ed < 2 * h1; ed += edge_step) {
                     const int c = edge_cell(ed);
-                    Sb[c] = fmaf(Sb[c], fb, Ze[ed]);
+                    Sb[c] = fmaf(Sb[c], fb, B1[edge_b1(ed)]); // z from the ring
                 }
             } else {
                 for_halo1(h1, w1, [&](int r, int q) {
@@ -1363,14 +1562,15 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
                 Sr[rr] = on_tile(rr) ? q : cur;
                 prev = cur;
             }
-            // only the 2-cell band along the tile's border is published: it
-            // is all that neighbours' rings read
-            if (!first && gj < NJ) {
+            // A s on the tile's border: the neighbours' 1-halo ring in their
+            // sweep 2 (iteration 0 computes it from s_0 = b instead, except in
+            // spec mode, where s_0 = z_0 is known on the 1-halo only)
+            if ((SPEC || !first) && gj < NJ) {
 #pragma unroll
                 for (int rr = 0; rr < kR; rr++) {
                     const int gi = ti0 + row0 + rr - 1;
                     if (on_tile(rr) && in_band(rr) && gi < NI)
-                        st_ll(a.ll_s + (size_t)gi * NJ + gj, ll_pack(__float_as_uint(Sb[cbase + rr * w2]), ep_s));
+                        st_ll(a.ll_s + (size_t)gi * NJ + gj, ll_pack(__float_as_uint(Sr[rr]), ep_s));
                 }
             }
         } else {
@@ -1399,23 +1599,36 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
         }
 
         // ---- sweep 2 -------------------------------------------------------
-        if (!first && !load_ring_ll(Sb, a.ll_s, ep_s)) return; // neighbours' s_it
-        // A s_it on the tile and its 1-halo while the grid barrier completes
+        // A s_it on the tile's 1-halo while the grid barrier completes; the
+        // tile rows' A s came with s.As
         if constexpr (RPS > 0) {
-            // the tile rows' A s came with s.As (step C); the 1-halo rows read
-            // the ring, all from Sb (s_it itself stays there)
+            if (first && !SPEC) {
+                // s_0 = b is known on the 2-halo since the set-up: A s_0 on the
+                // 1-halo from Sb (its 1-halo rows into registers, its halo
+                // columns into B1 where later iterations' rings land)
 #pragma unroll
-            for (int rr = 0; rr < kR; rr++)
-                if (!on_tile(rr)) Sr[rr] = apply_a(Ost[rr * w1], Sb, cbase + rr * w2, w2);
-            for (int ed = edge0; ed < 2 * h1; ed += edge_step) Ze[ed] = apply_a(edge_op(ed), Sb, edge_cell(ed), w2);
+                for (int rr = 0; rr < kR; rr++)
+                    if (!on_tile(rr)) Sr[rr] = apply_a(Ost[rr * w1], Sb, cbase + rr * w2, w2);
+                for (int ed = edge0; ed < 2 * h1; ed += edge_step)
+                    B1[edge_b1(ed)] = apply_a(edge_op(ed), Sb, edge_cell(ed), w2);
+            } else {
+                // as the neighbours computed it on their border
+                if (!load_ring1(B1, a.ll_s, ep_s)) return;
+#pragma unroll
+                for (int rr = 0; rr < kR; rr++)
+                    if (live(rr) && !on_tile(rr)) Sr[rr] = B1[(row0 + rr) * w1 + qb];
+            }
         } else {
+            if (!first && !load_ring_ll(Sb, a.ll_s, ep_s)) return; // neighbours' s_it
             for_halo1(h1, w1, [&](int r, int q) {
                 B1[r * w1 + q] = apply_a(Op[r * w1 + q], Sb, (r + 1) * w2 + (q + 1), w2);
             });
         }
         const float4 qsum = wait_sum(false);
         if (gfail) return;
-        const float fa = ff_div(sigma, ff_add(make_float2(qsum.x, qsum.y), eps8));
+        // (the reference adds 1e-8 to s.As; the spec-mode solve does not)
+        const float fa = SPEC ? ff_div(sigma, make_float2(qsum.x, qsum.y))
+                              : ff_div(sigma, ff_add(make_float2(qsum.x, qsum.y), eps8));
         fa_prev = fa;
         // r_{it+1} = r_it - alpha A s_it (x += alpha s_it on the tile comes
         // during the next iteration's beta reduction)
@@ -1427,7 +1640,7 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
                 if (live(rr)) Rb[cbase + rr * w2] = Rr[rr];
             for (int ed = edge0; ed < 2 * h1; ed += edge_step) {
                 const int c = edge_cell(ed);
-                Rb[c] = fmaf(-Ze[ed], fa, Rb[c]);
+                Rb[c] = fmaf(-B1[edge_b1(ed)], fa, Rb[c]); // A s on the halo column
             }
         } else {
             for_halo1(h1, w1, [&](int r, int q) {
@@ -1435,28 +1648,36 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
             });
         }
         __syncthreads();
-        float zr = 0.f;
+        float zr = 0.f, rr2 = 0.f;
         if constexpr (RPS > 0) {
             // r_{it+1} is in Rb since the barrier above: no barrier of its own
-            chunk_ends();
+            if constexpr (!SPEC) chunk_ends();
             const int gj = tj0 + qb - 1;
 #pragma unroll
             for (int rr = 0; rr < kR; rr++) {
                 const int c = cbase + rr * w2;
-                const float z = ipp_apply(Ost[rr * w1], inv, Rr[rr], up_of(Rr, Rb, rr, c), dn_of(Rr, Rb, rr, c),
-                                          Rb[c - 1], Rb[c + 1]);
+                float z;
+                if constexpr (SPEC) {
+                    z = kkt_apply(Ost[rr * w1], inv, Rr[rr], dn_of(Rr, Rb, rr, c), Rb[c + 1], up_of(Rr, Rb, rr, c),
+                                  Rb[c - w2 + 1], Rb[c - 1], Rb[c + w2 - 1]);
+                    rr2 = on_tile(rr) ? fmaf(Rr[rr], Rr[rr], rr2) : rr2;
+                } else {
+                    z = ipp_apply(Ost[rr * w1], inv, Rr[rr], up_of(Rr, Rb, rr, c), dn_of(Rr, Rb, rr, c),
+                                  Rb[c - 1], Rb[c + 1]);
+                }
                 zr = on_tile(rr) ? fmaf(z, Rr[rr], zr) : zr;
                 // z on the tile rows is the next sweep's z there too
                 Sr[rr] = on_tile(rr) ? z : Sr[rr];
             }
-            // the band only, as for s; the rare backward max-abs scan gets the
-            // whole tile published on demand (publish_tile_r)
+            // z on the tile's border: the neighbours' 1-halo ring in their next
+            // sweep 1; the rare backward max-abs scan gets the tile's whole r
+            // on demand (publish_tile_r)
             if (gj < NJ) {
 #pragma unroll
                 for (int rr = 0; rr < kR; rr++) {
                     const int gi = ti0 + row0 + rr - 1;
                     if (on_tile(rr) && in_band(rr) && gi < NI)
-                        st_ll(a.ll_r + (size_t)gi * NJ + gj, ll_pack(__float_as_uint(Rr[rr]), ep_r));
+                        st_ll(a.ll_r + (size_t)gi * NJ + gj, ll_pack(__float_as_uint(Sr[rr]), ep_r));
                 }
             }
         } else {
@@ -1479,7 +1700,11 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
             __syncthreads(); // the sweep above stored r_{it+1} in Rb
             chunk_ends();
         }
-        {
+        if constexpr (SPEC) {
+            float2 pzr, prr;
+            bsum0_2(zr, rr2, smf, pzr, prr);
+            publish(pzr, 0u, prr);
+        } else {
             const float2 part = bsum0(zr, smf); // its barrier also orders s_cmax / s_cscan
             publish(part, (unsigned)s_cmax | (s_cscan ? 0x80000000u : 0u));
         }
@@ -1493,7 +1718,13 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
             if (gj < NJ) a.x[(size_t)gi * NJ + gj] = Xt[r * tj + q];
         }
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) *a.iters_out = result;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (a.iters_out) *a.iters_out = result;
+        if constexpr (SPEC) {
+            a.spec_ctl->total += result;
+            a.spec_ctl->last_it = result;
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1634,20 +1865,20 @@ bool resident_tile_shape(int ni, int nj, int *ti, int *tj)
     return best >= 0;
 }
 
-template <int RPS>
+template <int RPS, bool SPEC = false>
 static cudaError_t launch_resident_rps(const PcgArgs<float> &a, int ti, int tj, int grid,
                                        cudaStream_t st)
 {
     const int nstrips = (RPS > 0 ? kStripThreads : kThreads) / 32 / (tj / 32);
     const size_t smem = res_layout(ti, tj, RPS > 0 ? nstrips * RPS : 0).bytes;
-    cudaError_t e = cudaFuncSetAttribute((const void *)k_pcg_resident<RPS>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const void *fn = (const void *)k_pcg_resident<RPS, SPEC>;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     PcgArgs<float> args = a;
     int vti = ti, vtj = tj;
     void *kargs[] = {&args, &vti, &vtj};
-    return cudaLaunchCooperativeKernel((const void *)k_pcg_resident<RPS>, dim3(grid),
-                                       dim3(RPS > 0 ? kStripThreads : kThreads), kargs, smem, st);
+    return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(RPS > 0 ? kStripThreads : kThreads), kargs, smem,
+                                       st);
 }
 
 cudaError_t launch_pcg_resident(const PcgArgs<float> &a0, int ti, int tj, cudaStream_t st,
@@ -1693,6 +1924,38 @@ cudaError_t launch_pcg_resident(const PcgArgs<float> &a0, int ti, int tj, cudaSt
     case 14: return launch_resident_rps<14>(a, ti, tj, grid, st);
     case 16: return launch_resident_rps<16>(a, ti, tj, grid, st);
     default: return launch_resident_rps<0>(a, ti, tj, grid, st);
+    }
+}
+
+bool spec_resident_shape(int ni, int nj, int *ti, int *tj)
+{
+    int a = 0, b = 0;
+    if (!resident_tile_shape(ni, nj, &a, &b) || strip_rows(a, b) == 0) return false;
+    *ti = a;
+    *tj = b;
+    return true;
+}
+
+unsigned long long spec_resident_epochs(int max_iter)
+{
+    return 2ull * (unsigned long long)(max_iter > 0 ? max_iter : 0) + 8ull;
+}
+
+cudaError_t launch_spec_resident(const PcgArgs<float> &a, int ti, int tj, cudaStream_t st)
+{
+    const int grid = ((a.ni + ti - 1) / ti) * ((a.nj + tj - 1) / tj);
+    if (!a.ll_r || !a.ll_s || !a.ll_rec || !a.spec_ctl || !a.spec_dt || grid > 256) return cudaErrorInvalidValue;
+    switch (strip_rows(ti, tj)) {
+    case 1: return launch_resident_rps<1, true>(a, ti, tj, grid, st);
+    case 2: return launch_resident_rps<2, true>(a, ti, tj, grid, st);
+    case 4: return launch_resident_rps<4, true>(a, ti, tj, grid, st);
+    case 6: return launch_resident_rps<6, true>(a, ti, tj, grid, st);
+    case 8: return launch_resident_rps<8, true>(a, ti, tj, grid, st);
+    case 10: return launch_resident_rps<10, true>(a, ti, tj, grid, st);
+    case 12: return launch_resident_rps<12, true>(a, ti, tj, grid, st);
+    case 14: return launch_resident_rps<14, true>(a, ti, tj, grid, st);
+    case 16: return launch_resident_rps<16, true>(a, ti, tj, grid, st);
+    default: return cudaErrorInvalidValue;
     }
 }
 

@@ -31,5 +31,13 @@ bool resident_tile_shape(int ni, int nj, int *ti, int *tj);
 // (a.ll_r / a.ll_s are taken from it) and their epoch counter.
 cudaError_t launch_pcg_resident(const PcgArgs<float> &a, int ti, int tj, cudaStream_t st,
                                 LlBuffers *ll);
+// Spec mode: the resident kernel as the inner FP32 solve of a chained
+// spec-mode solve (K K^T preconditioner, r.r stopping rule, a.spec_ctl).
+// The caller assigns the launch its exchange-word epochs: a.ll_base and the
+// spec_resident_epochs(a.iter_limit) that follow.  False from the shape
+// query when the grid does not fit register strips one tile per SM.
+bool spec_resident_shape(int ni, int nj, int *ti, int *tj);
+unsigned long long spec_resident_epochs(int max_iter);
+cudaError_t launch_spec_resident(const PcgArgs<float> &a, int ti, int tj, cudaStream_t st);
 
 } // namespace fsg

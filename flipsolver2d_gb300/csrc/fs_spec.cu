@@ -30,6 +30,7 @@
 
 #include "fs_device.h"
 #include "fs_pcg.h"
+#include "fs_pcg_tma.h"
 #include "fs_spec.h"
 
 namespace fsg {
@@ -259,6 +260,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2) k_pcg_spec(SpecArgs a)
     float *__restrict__ z = a.z, *__restrict__ d = a.d;
     float2 *pA = a.partials, *pB = a.partials + G, *pC = a.partials + 2 * G;
     SpecGrid g{a.count, a.status, 0u};
+    if (a.mode == 1 && *a.wrap_flag == 0) return; // the resident kernel solved it
     float eps_in = a.eps_in;
     int max_iter = a.max_iter;
     if (a.ctl) {
@@ -392,6 +394,12 @@ static int spec_grid()
 
 int spec_partials_needed() { return 3 * spec_grid() + 8; }
 
+int spec_chain_kernels(const SpecSolve &p)
+{
+    const bool res = p.res_ti > 0 && p.ll && p.wrap_flag;
+    return (res ? 5 : 4) * p.max_outer + 2;
+}
+
 cudaError_t launch_spec_residual(const uint8_t *info, const double *b, const double *x, float *r32,
                                  long long N, int NJ, double scale, double *partial, int nblocks,
                                  cudaStream_t st)
@@ -427,6 +435,47 @@ cudaError_t launch_spec_chain(const SpecSolve &p, cudaStream_t st)
     cudaError_t e = cudaMemsetAsync(p.ctl, 0, sizeof(SpecCtl), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(p.x, 0, (size_t)N * 8, st);
     if (e != cudaSuccess) return e;
+    // the resident inner solves: one range of exchange-word epochs per
+    // round, all taken now (a captured chain replays with the same epochs,
+    // so it clears the words inside the capture and leaves them to be
+    // cleared again before the next launch outside it)
+    const bool res = p.res_ti > 0 && p.ll && p.wrap_flag;
+    PcgArgs<float> ra{};
+    const unsigned long long span = spec_resident_epochs(p.max_iter);
+    if (res) {
+        LlBuffers *ll = p.ll;
+        if (!ll->r || !ll->s || !ll->rec || ll->words < (size_t)N) return cudaErrorInvalidValue;
+        const unsigned long long need = span * (unsigned long long)(p.max_outer + 1);
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if ((e = cudaStreamIsCapturing(st, &cs)) != cudaSuccess) return e;
+        const bool capturing = cs != cudaStreamCaptureStatusNone;
+        if (capturing || ll->next == 0 || (unsigned long long)ll->next + need > 0xfffffff0ull) {
+            e = cudaMemsetAsync(ll->r, 0, ll->words * sizeof(unsigned long long), st);
+            if (e == cudaSuccess) e = cudaMemsetAsync(ll->s, 0, ll->words * sizeof(unsigned long long), st);
+            if (e == cudaSuccess) e = cudaMemsetAsync(ll->rec, 0, kLlRecWords * sizeof(unsigned long long), st);
+            if (e != cudaSuccess) return e;
+            ll->next = 1;
+        }
+        ra.ni = p.ni;
+        ra.nj = p.nj;
+        ra.N = N;
+        ra.info = p.info;
+        ra.b = p.r;
+        ra.x = p.d;
+        ra.ll_r = ll->r;
+        ra.ll_s = ll->s;
+        ra.ll_rec = ll->rec;
+        ra.ll_base = ll->next;
+        ra.density = p.density;
+        ra.dx = p.dx;
+        ra.iter_limit = p.max_iter;
+        ra.status = p.status;
+        ra.wrap_flag = p.wrap_flag;
+        ra.mode = 2; // unless a unit row touches a j edge
+        ra.spec_ctl = p.ctl;
+        ra.spec_dt = p.dt;
+        ll->next = capturing ? 0u : (unsigned)(ll->next + need);
+    }
     const int ublocks = (int)((N + 255) / 256 < 4096 ? (N + 255) / 256 : 4096);
     SpecArgs a{};
     a.ni = p.ni;
@@ -446,6 +495,8 @@ cudaError_t launch_spec_chain(const SpecSolve &p, cudaStream_t st)
     a.eps_in = 1e-4f;
     a.max_iter = p.max_iter;
     a.ctl = p.ctl;
+    a.wrap_flag = p.wrap_flag;
+    a.mode = res ? 1 : 0;
     for (int round = 0;; round++) {
         k_spec_residual<<<kSpecResBlocks, 256, 0, st>>>(p.info, p.b, p.x, p.r, N, p.nj, 0.0, p.rpart, p.ctl,
                                                         p.dt, p.density, p.dx);
@@ -456,7 +507,11 @@ cudaError_t launch_spec_chain(const SpecSolve &p, cudaStream_t st)
         a.dt = p.dt; // the scale from the device dt, like the residual
         a.density = p.density;
         a.dx = p.dx;
-        e = launch_spec_pcg(a, st);
+        if (res) {
+            e = launch_spec_resident(ra, p.res_ti, p.res_tj, st);
+            ra.ll_base += (unsigned)span;
+        }
+        if (e == cudaSuccess) e = launch_spec_pcg(a, st);
         if (e != cudaSuccess) return e;
         k_spec_update<<<ublocks > 0 ? ublocks : 1, 256, 0, st>>>(p.x, p.d, N, p.ctl);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;

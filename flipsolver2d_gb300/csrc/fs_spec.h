@@ -4,6 +4,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "fs_pcg.h"
+
 namespace fsg {
 
 // the state of one chained solve on the device (launch_spec_chain): the
@@ -37,6 +39,8 @@ struct SpecArgs {
                          // remaining iterations from here, totals back here
     const float *dt;     // when set: scale = *dt / (density dx^2) on the device
     double density, dx;
+    const int *wrap_flag; // with mode 1: run only when a unit row touches a j edge
+    int mode;             // 0 always, 1 only if *wrap_flag
 };
 
 // one whole spec-mode solve of A x = b enqueued on a stream with no host
@@ -61,8 +65,19 @@ struct SpecSolve {
     double *rel_out;  // optional: final relative residual
     double tol;
     int max_iter, max_outer;
+    // Inner solves on the shared-memory-resident kernel when the grid fits
+    // one tile per SM (res_ti > 0, tile res_ti x res_tj, exchange words in
+    // *ll).  Its tiles treat cells outside the grid as absent, the linear
+    // index wraps j edges into the next row, so on a grid whose unit rows
+    // touch a j edge (*wrap_flag, set by the decomposition) the streaming
+    // kernel runs instead; the choice is made on the device.
+    int res_ti, res_tj;
+    LlBuffers *ll;
+    const int *wrap_flag;
 };
 cudaError_t launch_spec_chain(const SpecSolve &p, cudaStream_t st);
+// kernels one launch_spec_chain enqueues
+int spec_chain_kernels(const SpecSolve &p);
 
 int spec_partials_needed();
 cudaError_t launch_spec_residual(const uint8_t *info, const double *b, const double *x, float *r32,

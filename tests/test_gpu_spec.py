@@ -93,3 +93,84 @@ def test_spec_mixed_precision_configuration(port_lib, gpu_lib, monkeypatch):
     true_rr = _true_rel_residual(m, b, x_c, dx)
     assert rr_c <= REL_TOL and true_rr <= 1.01 * REL_TOL, (rr_c, true_rr)
     assert np.linalg.norm(x_c - x64) / np.linalg.norm(x64) <= SOL_TOL_2048
+
+
+def _apply_a_linear(m, x, dt, density, dx):
+    """apply_a with the reference's linear-index neighbours: on a unit row
+    at j = 0 or j = NJ - 1 the j neighbour is the previous or next row's end
+    cell (linearindexable2d.h:103-106), which the 2-D form zero-pads."""
+    ni, nj = m.shape
+    n = ni * nj
+    scale = np.float64(np.float32(dt)) / (density * dx * dx)
+    fl = (m & 0x40) != 0
+    pad_s = np.pad((m & 0x20) != 0, 1, mode="edge")
+    pad_f = np.pad(fl, 1, mode="edge")
+    xf = x.ravel()
+    cnt = np.zeros(n)
+    acc = np.zeros(n)
+    for (di, dj), off in (((-1, 0), -nj), ((1, 0), nj), ((0, -1), -1), ((0, 1), 1)):
+        ns = ~pad_s[1 + di:ni + 1 + di, 1 + dj:nj + 1 + dj]
+        nf = pad_f[1 + di:ni + 1 + di, 1 + dj:nj + 1 + dj].ravel()
+        cnt += ns.ravel()
+        idx = np.arange(n) + off
+        ok = nf & (idx >= 0) & (idx < n)
+        acc[ok] += xf[idx[ok]]
+    out = xf.copy()
+    f = fl.ravel()
+    out[f] = (scale * (cnt * xf - acc))[f]
+    return out.reshape(ni, nj)
+
+
+def _mask(ni, nj, seed):
+    """random_mask cropped to ni x nj, with its solid border restored."""
+    m = random_mask(max(ni, nj), seed)[:ni, :nj].copy()
+    m[0, :] = m[-1, :] = m[:, 0] = m[:, -1] = 0x20
+    return m
+
+
+def _oracle_bar(m, b, dx):
+    """3 x the FP64 oracle's own error at a 1e-6 stop (against its 1e-8
+    solution), floor 1e-4: what a correct 1e-6 solve may differ by."""
+    _, x8, rr8 = fo.spec_solve(m, b, DT, DENSITY, dx, 1e-8)
+    assert rr8 <= 1e-8
+    _, x6, _ = fo.spec_solve(m, b, DT, DENSITY, dx, REL_TOL)
+    return x8, max(3.0 * np.linalg.norm(x6 - x8) / np.linalg.norm(x8), 1e-4)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ni,nj,seed", [(600, 600, 11), (613, 797, 12), (1024, 1024, 13)])
+def test_spec_resident_inner_solves(port_lib, gpu_lib, monkeypatch, ni, nj, seed):
+    """Grids above the cluster solve's on-chip limit that fit one tile per
+    SM: the chained solve's inner FP32 solves run on the resident kernel
+    (K K^T preconditioner in shared memory, r.r stopping rule).  They reach
+    the 1e-6 true residual, recomputed here in FP64, and agree with the FP64
+    oracle."""
+    monkeypatch.setenv("FSO_HOST_THREADS", str(os.cpu_count() or 1))
+    m = _mask(ni, nj, seed)
+    b = rhs_for(m, seed)
+    dx = 1.0 / max(ni, nj)
+    x8, bar = _oracle_bar(m, b, dx)
+    it, x, rr = gpu.pcg_solve_spec(m, b, DT, DENSITY, dx, REL_TOL)
+    true_rr = _true_rel_residual(m, b, x, dx)
+    assert rr <= REL_TOL and true_rr <= 1.01 * REL_TOL, (rr, true_rr)
+    err = np.linalg.norm(x - x8) / np.linalg.norm(x8)
+    assert err <= bar, f"error against the FP64 oracle {err} (bar {bar})"
+
+
+@pytest.mark.gpu
+def test_spec_wrapping_grid_falls_back(port_lib, gpu_lib, monkeypatch):
+    """Fluid on the j = 0 and j = NJ - 1 columns: the linear index wraps
+    those rows' j neighbours into the next row, which the resident kernel's
+    tiles do not, so the streaming inner solve runs instead -- and the solve
+    still meets the residual and the oracle."""
+    monkeypatch.setenv("FSO_HOST_THREADS", str(os.cpu_count() or 1))
+    m = _mask(600, 600, 14)
+    m[200:400, 0] = 0x40
+    m[250:350, -1] = 0x40
+    b = rhs_for(m, 14)
+    dx = 1.0 / 600
+    x8, bar = _oracle_bar(m, b, dx)
+    it, x, rr = gpu.pcg_solve_spec(m, b, DT, DENSITY, dx, REL_TOL)
+    true_rr = np.linalg.norm(b - _apply_a_linear(m, x, DT, DENSITY, dx)) / np.linalg.norm(b)
+    assert rr <= REL_TOL and true_rr <= 1.01 * REL_TOL, (rr, true_rr)
+    assert np.linalg.norm(x - x8) / np.linalg.norm(x8) <= bar
