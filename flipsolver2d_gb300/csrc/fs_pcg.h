@@ -65,9 +65,14 @@ struct LlBuffers {
     size_t words = 0;
     unsigned next = 0; // first epoch of the next launch; 0: clear first
 };
-// the partial records: two sets of at most 256 blocks (the resident kernel's
-// tile limit) of four words
-constexpr size_t kLlRecWords = 2 * 256 * 4;
+// The resident kernel's small exchange-word regions, one allocation: the
+// partial records (two sets of at most 256 blocks, its tile limit, of four
+// words), then per chunk of the max-abs test the index of its last live unit
+// row (at most kLlMaxChunks chunks)
+constexpr size_t kLlRecSets = 2 * 256 * 4;
+constexpr size_t kLlEffOff = kLlRecSets;
+constexpr size_t kLlMaxChunks = 4096;
+constexpr size_t kLlRecWords = kLlEffOff + kLlMaxChunks;
 
 // scale = dt / (density dx^2) of the pressure operator (flipsolver2d.cpp:797-887)
 template <typename T> __device__ __forceinline__ double pcg_scale(const PcgArgs<T> &a)

@@ -254,9 +254,10 @@ __device__ __forceinline__ bool gsync(GridBarrier *gb, unsigned nblocks, int *st
 // VOps::maxAbs (vmath.cpp:100-136) with the reference's chunking, then the
 // stopping test: the value of a chunk is |r| at its last nonzero entry.  The
 // owner tile of each chunk's last unit row stored |r| there in chunk_val (or
-// -1 when it is zero, then the chunk is scanned backwards here).
-template <typename Load>
-__device__ __forceinline__ bool chunk_converged(const PcgArgs<float> &a, Load rn,
+// -1 when it is zero, then the chunk is scanned backwards here).  lastl(k):
+// the last unit row of chunk k that r can reach (-1: none).
+template <typename Load, typename LastLoad>
+__device__ __forceinline__ bool chunk_converged(const PcgArgs<float> &a, Load rn, LastLoad lastl,
                                                 const TolTest &tt, int *s_flag)
 {
     __shared__ float s_mx[32];
@@ -268,7 +269,7 @@ __device__ __forceinline__ bool chunk_converged(const PcgArgs<float> &a, Load rn
     int has_min = 0;
     for (int k = warp; k < a.nchunks; k += nw) {
         const long long start = k == 0 ? 0 : a.chunk_end[k - 1];
-        const int last = a.chunk_last_unit[k];
+        const int last = lastl(k);
         if (last < 0) {
             has_min = 1;
             continue;
@@ -619,7 +620,9 @@ k_pcg_tma(PcgArgs<float> a, const __grid_constant__ TmaMaps m, int ti, int tj)
         if (!gsync(a.bar, G, a.status, lim)) return;
         const float *rn = (it & 1) ? a.r0 : a.r1;
         const float2 newSigma = psum(pB, G, sm);
-        if (chunk_converged(a, [&](long long e) { return __ldcg(rn + e); }, tt, &s_flag)) {
+        if (chunk_converged(
+                a, [&](long long e) { return __ldcg(rn + e); }, [&](int k) { return a.chunk_last_unit[k]; }, tt,
+                &s_flag)) {
             result = it;
             break;
         }
@@ -752,7 +755,7 @@ __device__ __forceinline__ void ld_ll2(const unsigned long long *p, unsigned lon
 constexpr int kRecWords = 4;
 
 // reduction k of a launch uses set k & 1 of two sets of G records
-static_assert(kRecWords * 2 * 256 == (int)kLlRecWords, "record buffer");
+static_assert(kRecWords * 2 * 256 == (int)kLlRecSets, "record buffer");
 
 // float-pair accumulation without renormalising: hi carries the running
 // sum, lo the rounding errors of the additions and the low parts
@@ -1021,6 +1024,21 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     // chunks without a unit row report DBL_MIN (VOps::maxAbs) on every iteration
     int has_min_static = 0;
     for (int k = 0; k < a.nchunks; k++) has_min_static |= a.chunk_last_unit[k] < 0;
+    // Live chunk ends: a unit row whose b is zero and whose fluid neighbours
+    // are none, or one that has no other (a one- or two-cell droplet), keeps
+    // r exactly zero through every iteration (A s, z = M r and s there only
+    // combine zeros).  The max-abs value of a chunk -- |r| at its last nonzero
+    // entry -- therefore never comes from such a row, and its last live unit
+    // row serves as the chunk's end: a flying droplet at the end of a chunk
+    // no longer sends every iteration to the backward search.  Per launch,
+    // the largest live index per chunk as (epoch << 32 | index + 1).
+    unsigned long long *effw = a.ll_rec + kLlEffOff;
+    const bool eff = !SPEC && a.nchunks > 0 && a.nchunks <= (int)kLlMaxChunks;
+    auto last_unit = [&](int k) -> int {
+        if (!eff) return a.chunk_last_unit[k];
+        const unsigned long long w = __ldcg(effw + k);
+        return (unsigned)(w >> 32) == ep0 ? (int)(unsigned)w - 1 : -1;
+    };
     const TolTest tt = tol_test(a.tol);
     const float2 eps8 = make_float2((float)1e-8, (float)(1e-8 - (double)(float)1e-8));
 
@@ -1195,13 +1213,79 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     __syncthreads();
     // the chunk ends this tile owns, listed once (more than kMaxOwnedChunks,
     // possible only with tiny chunks, falls back to a scan of all chunks)
-    for (int k = threadIdx.x; k < a.nchunks; k += blockDim.x) {
-        const int idx = a.chunk_last_unit[k];
-        if (idx < 0) continue;
-        const int gi = idx / NJ, gj = idx - gi * NJ;
-        if (gi < ti0 || gi >= ti0 + ti || gj < tj0 || gj >= tj0 + tj) continue;
-        const int slot = atomicAdd(&s_nown, 1);
-        if (slot < kMaxOwnedChunks) s_own[slot] = make_int2(k, (gi - ti0 + 2) * w2 + (gj - tj0 + 2));
+    auto list_owned = [&]() {
+        for (int k = threadIdx.x; k < a.nchunks; k += blockDim.x) {
+            const int idx = last_unit(k);
+            if (idx < 0) continue;
+            const int gi = idx / NJ, gj = idx - gi * NJ;
+            if (gi < ti0 || gi >= ti0 + ti || gj < tj0 || gj >= tj0 + tj) continue;
+            const int slot = atomicAdd(&s_nown, 1);
+            if (slot < kMaxOwnedChunks) s_own[slot] = make_int2(k, (gi - ti0 + 2) * w2 + (gj - tj0 + 2));
+        }
+    };
+    if (!eff) {
+        list_owned();
+    } else {
+        // this tile's live unit rows: per row segment, the highest live
+        // lane of each chunk; a warp keeps its running maximum per chunk and
+        // folds it into the chunk's word when the chunk changes
+        auto chunk_index = [&](long long e) { // the first chunk whose end exceeds e
+            int lo = 0, hi = a.nchunks - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (a.chunk_end[mid] > e) hi = mid;
+                else lo = mid + 1;
+            }
+            return lo;
+        };
+        const unsigned long long tag = (unsigned long long)ep0 << 32;
+        unsigned long long wbest = 0ull;
+        int wk = -1;
+        for (int r = warp; r < ti; r += nw) {
+            const int gi = ti0 + r;
+            if (gi >= NI) break;
+            for (int q0 = 0; q0 < tj && tj0 + q0 < NJ; q0 += 32) {
+                const int q = q0 + lane, gj = tj0 + q;
+                bool live = false;
+                if (q < tj && gj < NJ) {
+                    const int c = (r + 2) * w2 + (q + 2);
+                    const unsigned p = Ib[c];
+                    const unsigned msk = p & 0xfu;
+                    const int nf = __popc(msk);
+                    if ((p & 0x80u) && (Rb[c] != 0.f || nf > 1)) {
+                        live = true;
+                    } else if ((p & 0x80u) && nf == 1) {
+                        const int cn = c + ((msk & 1u) ? -w2 : (msk & 2u) ? w2 : (msk & 4u) ? -1 : 1);
+                        live = !(Rb[cn] == 0.f && __popc(Ib[cn] & 0xfu) == 1);
+                    }
+                }
+                unsigned lv = __ballot_sync(0xffffffffu, live);
+                if (!lv) continue;
+                // the chunk of each lane's cell: one search for the segment,
+                // one a lane only where a chunk boundary falls inside it
+                const long long e0 = (long long)gi * NJ + tj0 + q0, e = e0 + lane;
+                const int seg_last = min(31, min(tj, NJ - tj0) - 1 - q0);
+                int k0 = 0;
+                if (lane == 0) k0 = chunk_index(e0);
+                k0 = __shfl_sync(0xffffffffu, k0, 0);
+                const bool one = e0 + seg_last < a.chunk_end[k0];
+                const int kl = one ? k0 : (lane <= seg_last ? chunk_index(e) : k0);
+                while (lv) {
+                    const int h = 31 - __clz((int)lv);
+                    const int kh = __shfl_sync(0xffffffffu, kl, h);
+                    const unsigned long long ph = tag | (unsigned long long)(e0 + h + 1);
+                    lv &= ~__ballot_sync(0xffffffffu, kl == kh);
+                    if (kh != wk) {
+                        if (wk >= 0 && lane == 0) atomicMax(effw + wk, wbest);
+                        wk = kh;
+                        wbest = ph;
+                    } else if (ph > wbest) {
+                        wbest = ph;
+                    }
+                }
+            }
+        }
+        if (wk >= 0 && lane == 0) atomicMax(effw + wk, wbest);
     }
     // packed operator word of each tile-plus-1-halo cell: its own row byte
     // (bits 0-7) and the cell counts of its four neighbours (3 bits each:
@@ -1251,11 +1335,22 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     } else {
         const float2 part = bsum0(bb, smf); // its block barrier also retires Ib
         const int anynz = __syncthreads_or(nz);
+        // the live-end maxima of every thread of the block are ordered before
+        // the record (release); the gathering lanes acquire after it
+        if (eff && threadIdx.x == 0) fence_acq_rel_gpu();
         publish(part, anynz ? 0x80000000u : 0u); // the flag: b has a nonzero
         const float4 s0 = wait_sum(false);
         if (gfail) return;
         sigma = make_float2(s0.x, s0.y);
         zero = s0.w == 0.f;
+        if (eff) {
+            if (warp < ((G + 31) >> 5)) fence_acq_rel_gpu();
+            __syncthreads();
+            list_owned();
+            int hm = 0;
+            for (int k = threadIdx.x; k < a.nchunks; k += blockDim.x) hm |= last_unit(k) < 0;
+            has_min_static = __syncthreads_or(hm);
+        }
     }
 
     // the neighbours' values on the 2-deep ring around the tile, from their
@@ -1437,7 +1532,7 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     auto edge_b1 = [&](int e) { return (e >> 1) * w1 + ((e & 1) ? w1 - 1 : 0); };
     auto edge_op = [&](int e) { return Op[(e >> 1) * w1 + ((e & 1) ? w1 - 1 : 0)]; };
 
-    // |r_{it+1}| at each chunk's last unit row, from the tile holding it (Rb
+    // |r_{it+1}| at each chunk's last (live) unit row, from the tile holding it (Rb
     // holds r_{it+1} on the tile); the block barrier of the z.r sum orders
     // s_cmax / s_cscan before thread 0 publishes them
     auto chunk_ends = [&]() {
@@ -1451,7 +1546,7 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
                 chunk_end_value(s_own[j].x, Rb[s_own[j].y]);
         } else {
             for (int k = threadIdx.x; k < a.nchunks; k += blockDim.x) {
-                const int idx = a.chunk_last_unit[k];
+                const int idx = last_unit(k);
                 if (idx < 0) continue;
                 const int gi = idx / NJ, gj = idx - gi * NJ;
                 if (gi < ti0 || gi >= ti0 + ti || gj < tj0 || gj >= tj0 + tj) continue;
@@ -1511,7 +1606,7 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
                 }
                 const bool done =
                     rec.w != 0.f
-                        ? chunk_converged(a, [&](long long e) { return __ldcg(a.r0 + e); }, tt, &s_flag)
+                        ? chunk_converged(a, [&](long long e) { return __ldcg(a.r0 + e); }, last_unit, tt, &s_flag)
                         : tol_met(tt, rec.z, has_min_static);
                 if (done) {
                     result = it - 1;
