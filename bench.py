@@ -679,6 +679,21 @@ def gpu_arm(args):
                              "pcg": "FS_PCG_SPEC, 1e-6 true relative residual"}
         except Exception as e:  # reported, never fatal for the main line
             line["serve"] = {"error": str(e)}
+        # the device-resident request loop on solve requests
+        try:
+            r = serve_device_measure(SERVE_DEVICE_REQUESTS)
+            line["serve_device"] = {
+                "workload": f"serve_device_{r['requests']}_solves (Poisson 2000/s, sides 64-512, "
+                            "masks of the Poisson case)",
+                "value": r["requests_per_s"], "unit": "requests/s", "latency_ms": r["latency_ms"],
+                "cell_iter_per_s": r["cell_iter_per_s"], "clusters": r["clusters"],
+                "worst_rel_residual": r["worst_rel_residual"], "elapsed_s": r["elapsed_s"],
+                "h2d_bytes": r["h2d_bytes"], "d2h_bytes": r["d2h_bytes"],
+                "path": "fs_server_submit / fs_server_poll / fs_server_take: one persistent cluster-solve "
+                        "launch fed from a ring in mapped pinned memory",
+                "pcg": "FS_PCG_SPEC cluster solve, 1e-6 true relative residual"}
+        except Exception as e:  # reported, never fatal for the main line
+            line["serve_device"] = {"error": str(e)}
     if rank == 0:
         print(json.dumps(line))
     if dist:
@@ -688,6 +703,67 @@ def gpu_arm(args):
 
 NB_WARM_FRAMES = 4
 SERVE_SUBOBJECT_REQUESTS = 120
+SERVE_DEVICE_REQUESTS = 400
+
+
+def serve_device_measure(n_requests: int, rate: float = 2000.0, sides=(64, 512), slots: int = 256):
+    """Serves n_requests spec-mode solve requests through the device-resident
+    loop (fs_server_*): Poisson arrivals at `rate` per second
+    (default_rng(19)), sides log-uniform in `sides`, the masks and
+    right-hand sides of scenes.poisson_case.  The problems are built before
+    the clock starts; a request is submitted at its arrival time (or when a
+    slot frees), and completes when its result is back in host memory.
+    Latencies run from arrival to that point."""
+    import math
+    from flipsolver2d_gb300 import gpu, scenes
+
+    rng = np.random.default_rng(19)
+    reqs, t = [], 0.0
+    for _ in range(n_requests):
+        t += rng.exponential(1.0 / rate)
+        side = int(round(math.exp(rng.uniform(math.log(sides[0]), math.log(sides[1])))))
+        side = max(sides[0], min(sides[1], side))
+        m, b, dx = scenes.poisson_case(side, seed=int(rng.integers(1 << 30)))
+        reqs.append({"arrival": t, "m": m, "b": b, "dx": dx})
+    srv = gpu.Server(sides[1], sides[1], slots=slots)
+    # warm-up: the first launch and its module load stay outside the clock
+    w = [srv.submit(reqs[k]["m"], reqs[k]["b"], 1.0 / 30, 1000.0, reqs[k]["dx"]) for k in range(4)]
+    while not all(srv.poll(x) for x in w):
+        time.sleep(0.0002)
+    for x in w:
+        srv.take(x)
+    pending, inflight, done = 0, {}, []
+    t0 = time.perf_counter()
+    while len(done) < len(reqs):
+        now = time.perf_counter() - t0
+        while pending < len(reqs) and reqs[pending]["arrival"] <= now:
+            q = reqs[pending]
+            try:
+                inflight[srv.submit(q["m"], q["b"], 1.0 / 30, 1000.0, q["dx"])] = q
+            except gpu.FsError as e:
+                if e.status != 6:  # every slot busy: submit it after the next take
+                    raise
+                break
+            pending += 1
+        for tk in [x for x in inflight if srv.poll(x)]:
+            it, x, rel = srv.take(tk)
+            q = inflight.pop(tk)
+            q.update(done=time.perf_counter() - t0, it=it, rel=rel)
+            done.append(q)
+        if now > 120.0:
+            raise RuntimeError("device serving did not finish within 120 s")
+    elapsed = time.perf_counter() - t0
+    clusters = srv.clusters()
+    srv.close()
+    lat = [1e3 * (q["done"] - q["arrival"]) for q in done]
+    return {
+        "requests": len(done), "elapsed_s": elapsed, "requests_per_s": len(done) / elapsed,
+        "latency_ms": {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))},
+        "cell_iter_per_s": sum(q["m"].size * q["it"] for q in done) / elapsed,
+        "worst_rel_residual": max(q["rel"] for q in done), "clusters": clusters,
+        "h2d_bytes": sum(q["m"].nbytes + q["b"].nbytes for q in done),
+        "d2h_bytes": sum(q["b"].nbytes for q in done),
+    }
 
 
 def nb_scene(res: int):

@@ -3351,6 +3351,270 @@ extern "C" fs_status fs_cluster_autotune(int ni, int nj, int objective, int devi
 }
 
 // ---------------------------------------------------------------------------
+// fs_server_*: the device-resident request loop (no reference counterpart).
+// One persistent launch of the cluster solve (launch_serve, fs_cluster.cu)
+// whose clusters take requests from a ring in mapped pinned memory: the host
+// copies a request's material, right-hand side and dt into a free slot,
+// writes the slot into the ring and advances the tail; a cluster claims it,
+// builds the operator, solves, and flags the slot done in mapped memory.  The
+// host never waits for the device to accept a request.  The launch leaves
+// when the ring stays empty for about 50 ms (or on destroy); a submit or a
+// poll that finds unclaimed requests and no launch running starts another.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr unsigned kServeRing = 1u << 16; // ring entries; requests in flight never exceed the slots
+constexpr long long kServeIdlePolls = 25000;
+constexpr size_t kServeHead = 64; // tail, stop
+} // namespace
+
+struct fs_server {
+    int device = 0;
+    int max_ni = 0, max_nj = 0, slots = 0;
+    ClusterPlan plan{};
+    ClusterParams params{};
+    cudaStream_t kst = nullptr, cst = nullptr; // the server launch; copies
+    cudaEvent_t ev = nullptr;                  // recorded after each server launch
+    bool launched = false;
+    int clusters = 0;
+    unsigned char *host = nullptr, *mapped = nullptr; // control block: host / device address
+    ServeSlot *d_slots = nullptr;
+    unsigned *d_claimed = nullptr;
+    void *slot_mem = nullptr;
+    size_t slot_bytes = 0, cells = 0;
+    std::vector<int> free_slots;
+    struct Req {
+        unsigned k;
+        int slot, ni, nj;
+    };
+    std::vector<std::pair<unsigned long long, Req>> reqs;
+    unsigned next_k = 0;
+    unsigned long long next_ticket = 1;
+    std::mutex mu;
+
+    volatile unsigned *tail() { return reinterpret_cast<volatile unsigned *>(host); }
+    volatile int *stop() { return reinterpret_cast<volatile int *>(host + 4); }
+    volatile unsigned *ring() { return reinterpret_cast<volatile unsigned *>(host + kServeHead); }
+    volatile unsigned *started() { return ring() + kServeRing; }
+    volatile unsigned *done() { return started() + slots; }
+    // a slot's buffers: material, operator bytes, b, x, then dt, iterations, residual
+    unsigned char *slot_base(int k) { return static_cast<unsigned char *>(slot_mem) + (size_t)k * slot_bytes; }
+    size_t a256(size_t x) const { return (x + 255) & ~(size_t)255; }
+    int8_t *mat(int k) { return reinterpret_cast<int8_t *>(slot_base(k)); }
+    uint8_t *info(int k) { return slot_base(k) + a256(cells); }
+    double *b(int k) { return reinterpret_cast<double *>(slot_base(k) + 2 * a256(cells)); }
+    double *x(int k) { return b(k) + cells; }
+    unsigned char *tailb(int k) { return reinterpret_cast<unsigned char *>(x(k) + cells); }
+    float *dt(int k) { return reinterpret_cast<float *>(tailb(k)); }
+    int *iters(int k) { return reinterpret_cast<int *>(tailb(k) + 16); }
+    double *rel(int k) { return reinterpret_cast<double *>(tailb(k) + 32); }
+};
+
+static void server_free(fs_server *s)
+{
+    if (s->kst) cudaStreamDestroy(s->kst);
+    if (s->cst) cudaStreamDestroy(s->cst);
+    if (s->ev) cudaEventDestroy(s->ev);
+    if (s->host) cudaFreeHost(s->host);
+    if (s->d_slots) cudaFree(s->d_slots);
+    if (s->d_claimed) cudaFree(s->d_claimed);
+    if (s->slot_mem) cudaFree(s->slot_mem);
+    delete s;
+}
+
+// a server launch is running, or one is started; FS_ERR_CUDA if the last
+// launch failed
+static fs_status server_running(fs_server *s)
+{
+    if (s->launched) {
+        const cudaError_t q = cudaEventQuery(s->ev);
+        if (q == cudaErrorNotReady) return FS_OK;
+        if (q != cudaSuccess) return fail(FS_ERR_CUDA, "fs_server: the server launch failed: %s", cudaGetErrorString(q));
+    }
+    ServeQueue q{};
+    q.slots = s->d_slots;
+    q.tail = reinterpret_cast<const unsigned *>(s->mapped);
+    q.stop = reinterpret_cast<const int *>(s->mapped + 4);
+    q.ring = reinterpret_cast<const unsigned *>(s->mapped + kServeHead);
+    q.ring_size = kServeRing;
+    q.claimed = s->d_claimed;
+    q.started = reinterpret_cast<unsigned *>(s->mapped + kServeHead) + kServeRing;
+    q.done = q.started + s->slots;
+    q.idle_polls = kServeIdlePolls;
+    cudaError_t e = launch_serve(q, s->plan, s->params, s->kst, &s->clusters);
+    if (e == cudaSuccess) e = cudaEventRecord(s->ev, s->kst);
+    if (e != cudaSuccess) return fail(FS_ERR_CUDA, "fs_server: launch: %s", cudaGetErrorString(e));
+    s->launched = true;
+    g_kernel_launches += 1;
+    return FS_OK;
+}
+
+extern "C" fs_status fs_server_create(int device, int max_ni, int max_nj, int slots, double rel_tol,
+                                      int max_iter, fs_server **out)
+{
+    if (!out || max_ni < 1 || max_nj < 1 || slots < 1 || slots > 4096 || !(rel_tol > 0.0) || max_iter < 1)
+        return fail(FS_ERR_BAD_ARG, "fs_server_create: invalid argument");
+    *out = nullptr;
+    if (cudaSetDevice(device) != cudaSuccess) return fail(FS_ERR_CUDA, "fs_server_create: no device %d", device);
+    fs_server *s = new fs_server();
+    s->device = device;
+    s->max_ni = max_ni;
+    s->max_nj = max_nj;
+    s->slots = slots;
+    if (!cluster_plan(max_ni, max_nj, &s->plan)) {
+        delete s;
+        return fail(FS_ERR_BAD_ARG, "fs_server_create: %d x %d exceeds the on-chip limit of the cluster solve",
+                    max_ni, max_nj);
+    }
+    s->params = spec_params();
+    s->params.tol = rel_tol;
+    s->params.max_iter = max_iter;
+    s->cells = (size_t)max_ni * max_nj;
+    s->slot_bytes = s->a256(2 * s->a256(s->cells) + 16 * s->cells + 64);
+    const size_t hbytes = kServeHead + 4 * ((size_t)kServeRing + 2 * (size_t)slots);
+    cudaError_t e = cudaStreamCreateWithFlags(&s->kst, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cst, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaHostAlloc((void **)&s->host, hbytes, cudaHostAllocMapped);
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer((void **)&s->mapped, s->host, 0);
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_slots, (size_t)slots * sizeof(ServeSlot));
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_claimed, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc(&s->slot_mem, (size_t)slots * s->slot_bytes);
+    if (e == cudaSuccess) e = cudaMemset(s->d_claimed, 0, sizeof(unsigned));
+    if (e != cudaSuccess) {
+        server_free(s);
+        return fail(e == cudaErrorMemoryAllocation ? FS_ERR_OOM : FS_ERR_CUDA, "fs_server_create: %s",
+                    cudaGetErrorString(e));
+    }
+    memset(s->host, 0, hbytes);
+    for (int k = slots - 1; k >= 0; k--) s->free_slots.push_back(k);
+    *out = s;
+    return FS_OK;
+}
+
+extern "C" fs_status fs_server_submit(fs_server *s, const fs_poisson_system *q, unsigned long long *ticket)
+{
+    if (!s || !q || !ticket || q->ni < 1 || q->nj < 1 || !q->material || !q->rhs)
+        return fail(FS_ERR_BAD_ARG, "fs_server_submit: invalid argument");
+    if (q->ni > s->max_ni || q->nj > s->max_nj)
+        return fail(FS_ERR_BAD_ARG, "fs_server_submit: %d x %d exceeds the server's %d x %d", q->ni, q->nj, s->max_ni,
+                    s->max_nj);
+    const size_t N = (size_t)q->ni * q->nj;
+    if (!valid_material(q->material, N)) return fail(FS_ERR_BAD_ARG, "fs_server_submit: unknown material code");
+    std::lock_guard<std::mutex> lock(s->mu);
+    if (s->free_slots.empty()) return fail(FS_ERR_STATE, "fs_server_submit: every slot holds a request not yet taken");
+    CK(cudaSetDevice(s->device));
+    const int k = s->free_slots.back();
+    ServeSlot h{};
+    h.sys.ni = q->ni;
+    h.sys.nj = q->nj;
+    h.sys.info = s->info(k);
+    h.sys.b = s->b(k);
+    h.sys.x = s->x(k);
+    h.sys.dt = s->dt(k);
+    h.sys.density = q->density;
+    h.sys.dx = q->dx;
+    h.sys.iters = s->iters(k);
+    h.sys.rel_res = s->rel(k);
+    h.material = s->mat(k);
+    h.info = s->info(k);
+    cudaError_t e = cudaMemcpyAsync(s->mat(k), q->material, N, cudaMemcpyHostToDevice, s->cst);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s->b(k), q->rhs, N * 8, cudaMemcpyHostToDevice, s->cst);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s->dt(k), &q->dt, sizeof(float), cudaMemcpyHostToDevice, s->cst);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_slots + k, &h, sizeof(h), cudaMemcpyHostToDevice, s->cst);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->cst); // in device memory before the ring names it
+    if (e != cudaSuccess) return fail(FS_ERR_CUDA, "fs_server_submit: %s", cudaGetErrorString(e));
+    s->free_slots.pop_back();
+    const unsigned rk = s->next_k++;
+    s->started()[k] = 0u;
+    s->done()[k] = 0u;
+    s->ring()[rk % kServeRing] = (unsigned)k;
+    std::atomic_thread_fence(std::memory_order_seq_cst);
+    *s->tail() = rk + 1;
+    std::atomic_thread_fence(std::memory_order_seq_cst);
+    *ticket = s->next_ticket++;
+    s->reqs.push_back({*ticket, fs_server::Req{rk, k, q->ni, q->nj}});
+    return server_running(s);
+}
+
+static fs_server::Req *server_find(fs_server *s, unsigned long long ticket, size_t *at)
+{
+    for (size_t i = 0; i < s->reqs.size(); i++)
+        if (s->reqs[i].first == ticket) {
+            if (at) *at = i;
+            return &s->reqs[i].second;
+        }
+    return nullptr;
+}
+
+extern "C" fs_status fs_server_poll(fs_server *s, unsigned long long ticket, int *done)
+{
+    if (!s || !done) return fail(FS_ERR_BAD_ARG, "fs_server_poll: invalid argument");
+    std::lock_guard<std::mutex> lock(s->mu);
+    fs_server::Req *r = server_find(s, ticket, nullptr);
+    if (!r) return fail(FS_ERR_BAD_ARG, "fs_server_poll: unknown ticket");
+    *done = s->done()[r->slot] == r->k + 1 ? 1 : 0;
+    std::atomic_thread_fence(std::memory_order_seq_cst);
+    if (*done) return FS_OK;
+    CK(cudaSetDevice(s->device));
+    // a request not yet claimed needs a launch to claim it (one that left
+    // for lack of work is started again); a claimed one is being solved
+    return server_running(s);
+}
+
+extern "C" fs_status fs_server_take(fs_server *s, unsigned long long ticket, double *result, int *iterations,
+                                    double *rel_residual)
+{
+    if (!s || !result) return fail(FS_ERR_BAD_ARG, "fs_server_take: invalid argument");
+    std::lock_guard<std::mutex> lock(s->mu);
+    size_t at = 0;
+    fs_server::Req *r = server_find(s, ticket, &at);
+    if (!r) return fail(FS_ERR_BAD_ARG, "fs_server_take: unknown ticket");
+    if (s->done()[r->slot] != r->k + 1) return fail(FS_ERR_STATE, "fs_server_take: the request is not done");
+    std::atomic_thread_fence(std::memory_order_seq_cst);
+    CK(cudaSetDevice(s->device));
+    const int k = r->slot;
+    const size_t N = (size_t)r->ni * r->nj;
+    int it = 0;
+    double rel = 0.0;
+    cudaError_t e = cudaMemcpyAsync(result, s->x(k), N * 8, cudaMemcpyDeviceToHost, s->cst);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&it, s->iters(k), sizeof(int), cudaMemcpyDeviceToHost, s->cst);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&rel, s->rel(k), sizeof(double), cudaMemcpyDeviceToHost, s->cst);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->cst);
+    if (e != cudaSuccess) return fail(FS_ERR_CUDA, "fs_server_take: %s", cudaGetErrorString(e));
+    if (iterations) *iterations = it;
+    if (rel_residual) *rel_residual = rel;
+    s->free_slots.push_back(k);
+    s->reqs.erase(s->reqs.begin() + (long)at);
+    return FS_OK;
+}
+
+extern "C" fs_status fs_server_clusters(fs_server *s, int *clusters)
+{
+    if (!s || !clusters) return fail(FS_ERR_BAD_ARG, "fs_server_clusters: invalid argument");
+    std::lock_guard<std::mutex> lock(s->mu);
+    *clusters = s->clusters;
+    return FS_OK;
+}
+
+extern "C" fs_status fs_server_destroy(fs_server *s)
+{
+    if (!s) return FS_OK;
+    fs_status st = FS_OK;
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        cudaSetDevice(s->device);
+        *s->stop() = 1;
+        std::atomic_thread_fence(std::memory_order_seq_cst);
+        // the launch leaves after the requests its clusters hold (each bounded
+        // by the inner iteration limit); requests not yet claimed are dropped
+        if (s->launched && cudaEventSynchronize(s->ev) != cudaSuccess)
+            st = fail(FS_ERR_CUDA, "fs_server_destroy: the server launch failed");
+    }
+    server_free(s);
+    return st;
+}
+
+// ---------------------------------------------------------------------------
 // fs_pcg_solve_device_noalloc: the FP32 device-pointer solve with all of its
 // scratch in one fixed device array (no counterpart in the reference).
 //

@@ -42,6 +42,7 @@
 #include <vector>
 
 #include "fs_cluster.h"
+#include "fs_common.cuh"
 #include "fs_device.h"
 
 namespace cg = cooperative_groups;
@@ -100,33 +101,42 @@ __device__ __forceinline__ float cl_div(float2 a, float2 b)
 //   bit 9      (K^T r)(c) takes r(c + 1): the same for the left neighbour
 //   bits 10-12 k(c) = scale / A(c, c): the count of a unit row (k = 1 / count),
 //              0 otherwise (Eigen's zero-diagonal rule, k = scale)
+// Inputs are read through the read-only cache (__ldg) when they stay fixed
+// for the whole launch; a server launch (FRESH) serves many requests from the
+// same buffers, which the host rewrites between them, so it reads past L1.
+template <bool FRESH, typename T> __device__ __forceinline__ T cl_ro(const T *p)
+{
+    if constexpr (FRESH) return __ldcg(p);
+    else return __ldg(p);
+}
+
+template <bool FRESH = false>
 __device__ __forceinline__ unsigned cl_word(const uint8_t *__restrict__ info, int c, int N, int nj)
 {
     if (c < 0 || c >= N) return 0u;
-    const unsigned p = __ldg(info + c);
+    const unsigned p = cl_ro<FRESH>(info + c);
     unsigned m = p & 0xFu;
     if (c - nj < 0) m &= ~1u;
     if (c + nj >= N) m &= ~2u;
     if (c - 1 < 0) m &= ~4u;
     if (c + 1 >= N) m &= ~8u;
     unsigned w = (p & 0xF0u) | m;
-    if (c + nj < N && (__ldg(info + c + nj) & 0x81) == 0x81) w |= 0x100u;
-    if (c + 1 < N && (__ldg(info + c + 1) & 0x84) == 0x84) w |= 0x200u;
+    if (c + nj < N && (cl_ro<FRESH>(info + c + nj) & 0x81) == 0x81) w |= 0x100u;
+    if (c + 1 < N && (cl_ro<FRESH>(info + c + 1) & 0x84) == 0x84) w |= 0x200u;
     const unsigned cnt = (p >> 4) & 7u;
     if ((p & 0x80u) && cnt > 0) w |= cnt << 10;
     return w;
 }
 
+// One system's whole solve by the calling thread-block cluster.
 // K = template cells per thread: the own cells of a CTA are
 // tid + k * kClThreads, k < K; d and the per-cell q or z stay in registers
-template <int K>
-__global__ void __launch_bounds__(kClThreads, K >= 16 ? 1 : 2)
-k_pcg_cluster(const ClusterSystem *__restrict__ systems, ClusterParams P)
+template <int K, bool FRESH = false>
+__device__ __forceinline__ void cluster_solve(const ClusterSystem S, const ClusterParams &P)
 {
     cg::cluster_group cl = cg::this_cluster();
     const int C = (int)cl.num_blocks();
     const int rank = (int)cl.block_rank();
-    const ClusterSystem S = systems[blockIdx.x / C];
     const int ni = S.ni, nj = S.nj;
     const int N = ni * nj; // at most the on-chip limit, far below 2^31
     const int i0 = (int)((long long)rank * ni / C);
@@ -154,7 +164,7 @@ k_pcg_cluster(const ClusterSystem *__restrict__ systems, ClusterParams P)
     double *dwsum = reinterpret_cast<double *>(wsum + 64); // [32]
     float *ktab = reinterpret_cast<float *>(dwsum + 32);   // [8] k by word code
 
-    const double scale_d = (double)*S.dt / (S.density * S.dx * S.dx);
+    const double scale_d = (double)cl_ro<FRESH>(S.dt) / (S.density * S.dx * S.dx);
     const float scale = (float)scale_d;
     if (tid < 8) ktab[tid] = (tid >= 1 && tid <= 4) ? 1.f / (float)tid : scale;
 
@@ -246,7 +256,7 @@ k_pcg_cluster(const ClusterSystem *__restrict__ systems, ClusterParams P)
             if (w & 8u) nb += __ldcg(S.x + c + 1);
             ax = scale_d * ((double)((w >> 4) & 7u) * xc - nb);
         }
-        return __ldg(S.b + c) - ax;
+        return cl_ro<FRESH>(S.b + c) - ax;
     };
     // (A s) at own index m
     auto a32 = [&](int m) -> float {
@@ -312,13 +322,14 @@ k_pcg_cluster(const ClusterSystem *__restrict__ systems, ClusterParams P)
 
     // operator words of the own and halo rows (zero outside the grid); halo
     // rows outside the grid are never read, clear them anyway
-    for (int l = -nj + tid; l < nown + nj; l += kClThreads) wd[l + nj] = (uint16_t)cl_word(S.info, cb + l, N, nj);
+    for (int l = -nj + tid; l < nown + nj; l += kClThreads)
+        wd[l + nj] = (uint16_t)cl_word<FRESH>(S.info, cb + l, N, nj);
     for (int j = tid; j < nj; j += kClThreads) r_up[j] = r_dn[j] = s_up[j] = s_dn[j] = 0.f;
     // x = 0 (the reference clears the result) and ||b||^2
     double bsq = 0.0;
     for (int l = tid; l < nown; l += kClThreads) {
         S.x[cb + l] = 0.0;
-        const double bv = __ldg(S.b + cb + l);
+        const double bv = cl_ro<FRESH>(S.b + cb + l);
         bsq = fma(bv, bv, bsq);
     }
     const double bb = cluster_dsum(bsq, 0);
@@ -418,6 +429,112 @@ k_pcg_cluster(const ClusterSystem *__restrict__ systems, ClusterParams P)
         *S.rel_res = bb > 0.0 ? sqrt(rrt / bb) : 0.0;
     }
     cl.sync(); // no CTA leaves while another may still read its shared memory
+}
+
+template <int K>
+__global__ void __launch_bounds__(kClThreads, K >= 16 ? 1 : 2)
+k_pcg_cluster(const ClusterSystem *__restrict__ systems, ClusterParams P)
+{
+    cluster_solve<K>(systems[blockIdx.x / cg::this_cluster().num_blocks()], P);
+}
+
+// ---------------------------------------------------------------------------
+// The device-resident server (fs_server_*): a persistent launch whose
+// clusters take requests from a ring the host fills in mapped pinned memory.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned sv_ld_acquire_sys(const unsigned *p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void sv_st_release_sys(unsigned *p, unsigned v)
+{
+    asm volatile("st.release.sys.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// The packed operator byte of k_decomposition (fs_grid.cu) for one cell:
+// non-solid neighbour count at bits 4-6, and for a fluid cell the unit bit
+// and the fluid-neighbour mask with the linear-index bounds of
+// getPressureProjectionMatrix (flipsolver2d.cpp:797-887); neighbours outside
+// the grid read as the cell's nearest edge cell (OOB_EXTEND).
+__device__ __forceinline__ uint8_t sv_operator_byte(const int8_t *__restrict__ m, int ni, int nj, int c)
+{
+    const int i = c / nj, j = c - i * nj;
+    auto at = [&](int a, int b) { return __ldcg(m + (size_t)clampi(a, 0, ni - 1) * nj + clampi(b, 0, nj - 1)); };
+    const int8_t mim = at(i - 1, j), mip = at(i + 1, j);
+    const int8_t mjm = at(i, j - 1), mjp = at(i, j + 1);
+    const int nsc = !t_solid(mim) + !t_solid(mip) + !t_solid(mjm) + !t_solid(mjp);
+    uint8_t b = (uint8_t)(nsc << 4);
+    const int N = ni * nj;
+    if (t_fluid(__ldcg(m + c))) {
+        b |= 0x80;
+        if (t_fluid(mim) && c - nj >= 0) b |= 1;
+        if (t_fluid(mip) && c + nj < N) b |= 2;
+        if (t_fluid(mjm) && c - 1 >= 0) b |= 4;
+        if (t_fluid(mjp) && c + 1 < N) b |= 8;
+    }
+    return b;
+}
+
+// rank 0 thread 0 of a cluster: the slot of the next request, or -1 when the
+// host asked the server to stop or nothing arrived for q.idle_polls polls
+__device__ int sv_claim(const ServeQueue &q)
+{
+    long long idle = 0;
+    for (;;) {
+        if (*((volatile const int *)q.stop)) return -1;
+        const unsigned tail = sv_ld_acquire_sys(q.tail);
+        const unsigned c = *((volatile unsigned *)q.claimed);
+        if ((int)(tail - c) > 0) {
+            if (atomicCAS(q.claimed, c, c + 1) == c) {
+                const int slot = (int)*((volatile const unsigned *)(q.ring + (c % q.ring_size)));
+                sv_st_release_sys(q.started + slot, c + 1);
+                return slot;
+            }
+            continue; // another cluster took request c
+        }
+        if (++idle > q.idle_polls) return -1;
+        __nanosleep(2000);
+    }
+}
+
+template <int K>
+__global__ void __launch_bounds__(kClThreads, K >= 16 ? 1 : 2) k_serve(ServeQueue q, ClusterParams P)
+{
+    cg::cluster_group cl = cg::this_cluster();
+    const int C = (int)cl.num_blocks(), rank = (int)cl.block_rank();
+    __shared__ int s_slot;
+    for (;;) {
+        if (rank == 0 && threadIdx.x == 0) s_slot = sv_claim(q);
+        cl.sync();
+        const int slot = *cl.map_shared_rank(&s_slot, 0);
+        cl.sync(); // every CTA has its copy before rank 0 claims again
+        if (slot < 0) break;
+        // the slot as the host last wrote it (read past L1: the same slot
+        // served other requests earlier in this launch)
+        ServeSlot sl;
+        {
+            const unsigned long long *src = reinterpret_cast<const unsigned long long *>(q.slots + slot);
+            unsigned long long *dst = reinterpret_cast<unsigned long long *>(&sl);
+#pragma unroll
+            for (int w = 0; w < (int)(sizeof(ServeSlot) / 8); w++) dst[w] = __ldcg(src + w);
+        }
+        const ClusterSystem S = sl.sys;
+        // the operator bytes of the request's material, split over the CTAs
+        const int N = S.ni * S.nj;
+        const int c0 = (int)((long long)rank * N / C), c1 = (int)((long long)(rank + 1) * N / C);
+        for (int c = c0 + (int)threadIdx.x; c < c1; c += blockDim.x)
+            sl.info[c] = sv_operator_byte(sl.material, S.ni, S.nj, c);
+        cl.sync(); // the whole operator before any CTA reads its halo rows
+        cluster_solve<K, true>(S, P);
+        if (rank == 0 && threadIdx.x == 0) {
+            // x, the iterations and the residual are written (the solve's
+            // last cluster barrier); make them visible to the host's copies
+            __threadfence_system();
+            sv_st_release_sys(q.done + slot, *((volatile unsigned *)(q.started + slot)));
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -575,6 +692,49 @@ static cudaError_t launch_k(const ClusterSystem *systems_dev, int n, int C, size
     cfg.numAttrs = 1;
     ClusterParams pp = p;
     return cudaLaunchKernelEx(&cfg, k_pcg_cluster<K>, systems_dev, pp);
+}
+
+template <int K> static cudaError_t launch_serve_k(const ServeQueue &q, const ClusterPlan &plan,
+                                                  const ClusterParams &p, cudaStream_t st, int *clusters)
+{
+    const void *fn = (const void *)k_serve<K>;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.blockDim = dim3(kClThreads);
+    cfg.dynamicSmemBytes = plan.smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)plan.C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    // as many clusters as fit at once: each loops over requests
+    cfg.gridDim = dim3((unsigned)plan.C);
+    int nc = 0;
+    if ((e = cudaOccupancyMaxActiveClusters(&nc, fn, &cfg)) != cudaSuccess) return e;
+    if (nc < 1) return cudaErrorInvalidConfiguration;
+    cfg.gridDim = dim3((unsigned)(nc * plan.C));
+    *clusters = nc;
+    ServeQueue qq = q;
+    ClusterParams pp = p;
+    return cudaLaunchKernelEx(&cfg, k_serve<K>, qq, pp);
+}
+
+cudaError_t launch_serve(const ServeQueue &q, const ClusterPlan &plan, const ClusterParams &p, cudaStream_t st,
+                         int *clusters)
+{
+    const ClDevice D = cl_init();
+    if (plan.C < 1 || plan.C > D.max_cluster || plan.smem > D.smem_limit) return cudaErrorInvalidValue;
+    switch (plan.K) {
+    case 8: return launch_serve_k<8>(q, plan, p, st, clusters);
+    case 16: return launch_serve_k<16>(q, plan, p, st, clusters);
+    case 32: return launch_serve_k<32>(q, plan, p, st, clusters);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 cudaError_t launch_pcg_cluster(const ClusterSystem *systems_dev, int n, const ClusterPlan &plan,

@@ -46,6 +46,34 @@ void cluster_set_tuned(int ni, int nj, const ClusterPlan &plan);
 // the most cells a system may have
 long long cluster_max_cells();
 
+// One request slot of the device-resident server: the request's material
+// (copied in by the host), its operator bytes (written by the server before
+// the solve) and the system it solves (sys.info == info).
+struct ServeSlot {
+    ClusterSystem sys;
+    const int8_t *material;
+    uint8_t *info;
+};
+// The request ring of the device-resident server.  The host writes the slot
+// of request k at ring[k % ring_size] and then advances *tail (both in mapped
+// pinned memory); the clusters of the server launch claim requests in order
+// through *claimed (device memory), set started[slot] = k + 1 when they take
+// request k and done[slot] = k + 1 when its result is in device memory.
+struct ServeQueue {
+    const ServeSlot *slots;    // device, one per slot
+    const unsigned *tail;      // mapped: requests published
+    const unsigned *ring;      // mapped
+    unsigned ring_size;
+    unsigned *claimed;         // device: requests taken
+    unsigned *started, *done;  // mapped, one per slot
+    const int *stop;           // mapped: 1 = leave after the current request
+    long long idle_polls;      // polls of an empty ring (about 2 us each) before leaving
+};
+// Launches the server (as many clusters of `plan` as fit at once, each
+// looping over requests); *clusters receives that number.
+cudaError_t launch_serve(const ServeQueue &q, const ClusterPlan &plan, const ClusterParams &p, cudaStream_t st,
+                         int *clusters);
+
 // solves systems[0 .. n) (device array), all with the same C and K; smem =
 // the largest of their needs
 cudaError_t launch_pcg_cluster(const ClusterSystem *systems_dev, int n, const ClusterPlan &plan,

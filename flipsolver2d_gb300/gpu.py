@@ -131,6 +131,14 @@ _SIGS = {
     "fs_batch_timer": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "fs_pcg_solve_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                           ctypes.c_void_p]),
+    "fs_server_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_double, ctypes.c_int, ctypes.c_void_p]),
+    "fs_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_server_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_ulonglong, ctypes.c_void_p]),
+    "fs_server_take": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_ulonglong, ctypes.c_void_p,
+                                      ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_server_clusters": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "fs_server_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "fs_pcg_solve_device_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                                    ctypes.c_float, ctypes.c_double, ctypes.c_double,
                                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
@@ -420,6 +428,64 @@ def pcg_solve_operator(cell_info: np.ndarray, rhs: np.ndarray, scale: float, ite
     _check(lib.fs_pcg_solve_operator(ni, nj, _ptr(info), scale, _ptr(b), _ptr(x), iter_limit, tol,
                                      ctypes.byref(ex), ctypes.byref(it)), "fs_pcg_solve_operator")
     return int(it.value), x
+
+
+class Server:
+    """fs_server: the device-resident request loop for spec-mode solves (a
+    persistent launch that takes requests from a ring in mapped memory)."""
+
+    def __init__(self, max_ni: int, max_nj: int, slots: int = 64, rel_tol: float = 1e-6,
+                 max_iter: int = 100000, device: int = 0):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        _check(self.lib.fs_server_create(int(device), int(max_ni), int(max_nj), int(slots), float(rel_tol),
+                                         int(max_iter), ctypes.byref(h)), "fs_server_create")
+        self.h = h
+        self._shapes = {}
+
+    def submit(self, material, rhs, dt, density, dx) -> int:
+        ni, nj = material.shape
+        m = np.ascontiguousarray(material, np.int8)
+        b = np.ascontiguousarray(rhs, np.float64).reshape(ni, nj)
+        sysd = PoissonSystem(ni, nj, m.ctypes.data, float(dt), float(density), float(dx),
+                             b.ctypes.data, None, 0, 0.0)
+        t = ctypes.c_ulonglong()
+        _check(self.lib.fs_server_submit(self.h, ctypes.byref(sysd), ctypes.byref(t)), "fs_server_submit")
+        self._shapes[int(t.value)] = (ni, nj)
+        return int(t.value)
+
+    def poll(self, ticket: int) -> bool:
+        x = ctypes.c_int()
+        _check(self.lib.fs_server_poll(self.h, ctypes.c_ulonglong(ticket), ctypes.byref(x)), "fs_server_poll")
+        return bool(x.value)
+
+    def take(self, ticket: int):
+        """(inner iterations, solution float64 [ni, nj], relative residual)."""
+        ni, nj = self._shapes.get(ticket, (1, 1))  # an unknown ticket: the library reports it
+        x = np.zeros((ni, nj), np.float64)
+        it = ctypes.c_int()
+        rr = ctypes.c_double()
+        _check(self.lib.fs_server_take(self.h, ctypes.c_ulonglong(ticket), x.ctypes.data, ctypes.byref(it),
+                                       ctypes.byref(rr)), "fs_server_take")
+        del self._shapes[ticket]
+        return int(it.value), x, float(rr.value)
+
+    def clusters(self) -> int:
+        x = ctypes.c_int()
+        _check(self.lib.fs_server_clusters(self.h, ctypes.byref(x)), "fs_server_clusters")
+        return int(x.value)
+
+    def close(self):
+        if getattr(self, "h", None):
+            st = self.lib.fs_server_destroy(self.h)
+            self.h = None
+            _check(st, "fs_server_destroy")
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Batch:

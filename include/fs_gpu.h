@@ -394,6 +394,40 @@ fs_status fs_batch_destroy(fs_batch *batch);
  * writes 0). */
 fs_status fs_batch_timer(fs_batch *batch, int which, double *value);
 
+/* A device-resident request loop for spec-mode solves (no reference
+ * counterpart; each request is the problem of fs_pcg_solve_spec, solved by the
+ * cluster solve of fs_pcg_solve_batch).  One persistent launch keeps running
+ * while requests arrive: its thread-block clusters take requests from a ring
+ * the host fills in mapped pinned memory and flag each result there, so a
+ * request needs no launch and no host synchronisation with the device.  The
+ * launch leaves after about 50 ms without requests; the next submit or poll
+ * starts another.  While it runs it holds the SMs its clusters fit on, so
+ * other work on the device waits for it to leave.
+ *   fs_server_create: systems up to max_ni x max_nj (within the on-chip limit
+ *     of fs_pcg_solve_batch, else FS_ERR_BAD_ARG), `slots` requests in flight,
+ *     every solve to rel_tol within max_iter inner iterations.
+ *   fs_server_submit: copies the system's material, rhs and dt to a free slot
+ *     and queues it; FS_ERR_STATE when every slot holds a request not yet
+ *     taken.  system->result is not used; the call returns a ticket.
+ *   fs_server_poll: *done = 1 once the ticket's result is in device memory.
+ *   fs_server_take: copies the result, the inner iterations and the final
+ *     relative residual (any may be NULL but result) and frees the slot;
+ *     FS_ERR_STATE before the request is done.
+ *   fs_server_clusters: clusters of the last launch (requests solved at once).
+ *   fs_server_destroy: stops the loop after the requests being solved; requests
+ *     not yet taken by a cluster are dropped.
+ * Calls on one server are serialised by a lock; results do not depend on the
+ * other requests or on the order of arrival. */
+typedef struct fs_server fs_server;
+fs_status fs_server_create(int device, int max_ni, int max_nj, int slots, double rel_tol, int max_iter,
+                           fs_server **server);
+fs_status fs_server_submit(fs_server *server, const fs_poisson_system *system, unsigned long long *ticket);
+fs_status fs_server_poll(fs_server *server, unsigned long long ticket, int *done);
+fs_status fs_server_take(fs_server *server, unsigned long long ticket, double *result, int *iterations,
+                         double *rel_residual);
+fs_status fs_server_clusters(fs_server *server, int *clusters);
+fs_status fs_server_destroy(fs_server *server);
+
 /* Autotuner of the cluster solve (no reference counterpart): times every
  * cluster size that fits an ni x nj system (64 inner iterations on a
  * synthetic fluid-in-a-box system, CUDA events) and records the best for

@@ -27,3 +27,6 @@ def test_bad_arguments_rejected_without_device(gpu_lib):
     assert gpu_lib.fs_create(None, None, ctypes.byref(h)) == 1
     assert gpu_lib.fs_pcg_solve(0, 0, None, 0.0, 1.0, 1.0, None, None, 1, 1e-2, None, None) == 1
     assert b"invalid" in gpu_lib.fs_last_error()
+    srv = ctypes.c_void_p()
+    assert gpu_lib.fs_server_create(0, 0, 64, 4, ctypes.c_double(1e-6), 100, ctypes.byref(srv)) == 1
+    assert gpu_lib.fs_server_submit(None, None, None) == 1
