@@ -3351,6 +3351,86 @@ extern "C" fs_status fs_cluster_autotune(int ni, int nj, int objective, int devi
 }
 
 // ---------------------------------------------------------------------------
+// fs_resident_autotune: times every resident tile shape of the FP32 solve for
+// a grid shape (200 iterations of a synthetic system through
+// fs_pcg_solve_device, the best of three per shape) and records the fastest
+// for later handles and solves of that shape in this process.
+// ---------------------------------------------------------------------------
+extern "C" fs_status fs_resident_autotune(int ni, int nj, int device, int *tile_rows, int *tile_cols,
+                                          float *us_per_iteration)
+{
+    if (ni < 1 || nj < 1) return fail(FS_ERR_BAD_ARG, "fs_resident_autotune: invalid argument");
+    CK(cudaSetDevice(device));
+    std::vector<std::pair<int, int>> cand;
+    resident_candidates(ni, nj, &cand);
+    if (cand.empty())
+        return fail(FS_ERR_BAD_ARG, "fs_resident_autotune: %d x %d needs more tiles than SMs", ni, nj);
+    // fluid inside a one-cell solid wall, a seeded right-hand side on the fluid
+    const size_t N = (size_t)ni * nj;
+    std::vector<int8_t> mat(N, (int8_t)M_FLUID);
+    std::vector<float> rhs(N, 0.f);
+    unsigned long long rng = 0x9E3779B97F4A7C15ull;
+    for (int i = 0; i < ni; i++)
+        for (int j = 0; j < nj; j++) {
+            const size_t c = (size_t)i * nj + j;
+            if (i == 0 || j == 0 || i == ni - 1 || j == nj - 1) {
+                mat[c] = (int8_t)M_SOLID;
+            } else {
+                rng = rng * 6364136223846793005ull + 1442695040888963407ull;
+                rhs[c] = (float)((rng >> 11) * (1.0 / 9007199254740992.0)) - 0.5f;
+            }
+        }
+    int8_t *dm = nullptr;
+    float *db = nullptr, *dres = nullptr;
+    auto release = [&]() {
+        if (dm) cudaFree(dm);
+        if (db) cudaFree(db);
+        if (dres) cudaFree(dres);
+    };
+    cudaError_t e = cudaMalloc(&dm, N);
+    if (e == cudaSuccess) e = cudaMalloc(&db, N * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&dres, N * 4);
+    if (e == cudaSuccess) e = cudaMemcpy(dm, mat.data(), N, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(db, rhs.data(), N * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        release();
+        return fail(e == cudaErrorMemoryAllocation ? FS_ERR_OOM : FS_ERR_CUDA, "fs_resident_autotune: %s",
+                    cudaGetErrorString(e));
+    }
+    fs_exec_params ex{FS_PCG_FP32, 1, device, 0, {0, 0, 0, 0}};
+    double best_us = -1.0;
+    size_t best = 0;
+    for (size_t k = 0; k < cand.size(); k++) {
+        resident_set_tuned(ni, nj, cand[k].first, cand[k].second);
+        double t_min = -1.0;
+        for (int rep = 0; rep < 4; rep++) {
+            int its = 0;
+            const auto t0 = std::chrono::steady_clock::now();
+            // tolerance 0: every solve runs its 200 iterations
+            const fs_status st = fs_pcg_solve_device(ni, nj, dm, 1.0f / 60.0f, 1000.0, 1.0 / ni, db, dres, 200, 0.0,
+                                                     &ex, &its);
+            const double us = std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now() - t0).count();
+            if (st != FS_OK) {
+                resident_set_tuned(ni, nj, 0, 0);
+                release();
+                return st;
+            }
+            if (rep > 0 && (t_min < 0.0 || us < t_min)) t_min = us; // the first is a warm-up
+        }
+        if (best_us < 0.0 || t_min < best_us) {
+            best_us = t_min;
+            best = k;
+        }
+    }
+    release();
+    resident_set_tuned(ni, nj, cand[best].first, cand[best].second);
+    if (tile_rows) *tile_rows = cand[best].first;
+    if (tile_cols) *tile_cols = cand[best].second;
+    if (us_per_iteration) *us_per_iteration = (float)(best_us / 200.0);
+    return FS_OK;
+}
+
+// ---------------------------------------------------------------------------
 // fs_server_*: the device-resident request loop (no reference counterpart).
 // One persistent launch of the cluster solve (launch_serve, fs_cluster.cu)
 // whose clusters take requests from a ring in mapped pinned memory: the host

@@ -22,6 +22,10 @@
 // the loading thread fences again before issuing the next TMA loads.
 #include <cfloat>
 #include <initializer_list>
+#include <map>
+#include <mutex>
+#include <utility>
+#include <vector>
 #include <cstdio>
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -1933,13 +1937,13 @@ static size_t resident_smem(int ti, int tj)
     return res_layout(ti, tj, nstrips * rps).bytes;
 }
 
-bool resident_tile_shape(int ni, int nj, int *ti, int *tj)
+// every tile shape of width 32 .. 256 with at most one tile per SM (and no
+// more tiles than the grid reduction reads partials for) whose shared memory
+// fits: the rows per tile are the fewest that cover the grid in that many
+void resident_candidates(int ni, int nj, std::vector<std::pair<int, int>> *out)
 {
-    // among tile widths 32..256, the shape with the fewest cells per block
-    // including the 1-halo it recomputes, with at most one tile per SM (and
-    // no more tiles than the grid reduction reads partials for)
+    out->clear();
     const int blocks = min(sm_count(), 32 * kPartRounds);
-    long long best = -1;
     for (int w = 32; w <= 256; w *= 2) {
         const long long tiles_j = (nj + w - 1) / w;
         if (tiles_j > blocks) continue;
@@ -1949,13 +1953,45 @@ bool resident_tile_shape(int ni, int nj, int *ti, int *tj)
         const long long ntiles = ((ni + h - 1) / h) * tiles_j;
         if (ntiles > blocks) continue;
         if (resident_smem((int)h, w) > kMaxResidentSmem) continue;
-        const long long cost = (h + 2) * (w + 2);
+        out->push_back({(int)h, w});
+        if (w >= nj) break; // wider tiles only add empty columns
+    }
+}
+
+// shapes chosen by the autotuner, by grid shape (this process)
+static std::mutex g_res_mu;
+static std::map<std::pair<int, int>, std::pair<int, int>> g_res_tuned;
+
+void resident_set_tuned(int ni, int nj, int ti, int tj)
+{
+    std::lock_guard<std::mutex> lock(g_res_mu);
+    if (ti > 0) g_res_tuned[{ni, nj}] = {ti, tj};
+    else g_res_tuned.erase({ni, nj});
+}
+
+bool resident_tile_shape(int ni, int nj, int *ti, int *tj)
+{
+    {
+        std::lock_guard<std::mutex> lock(g_res_mu);
+        auto it = g_res_tuned.find({ni, nj});
+        if (it != g_res_tuned.end()) {
+            *ti = it->second.first;
+            *tj = it->second.second;
+            return true;
+        }
+    }
+    // the default: the candidate with the fewest cells per block including
+    // the 1-halo around its tile
+    std::vector<std::pair<int, int>> cand;
+    resident_candidates(ni, nj, &cand);
+    long long best = -1;
+    for (const auto &c : cand) {
+        const long long cost = (long long)(c.first + 2) * (c.second + 2);
         if (best < 0 || cost < best) {
             best = cost;
-            *ti = (int)h;
-            *tj = w;
+            *ti = c.first;
+            *tj = c.second;
         }
-        if (w >= nj) break; // wider tiles only add empty columns
     }
     return best >= 0;
 }

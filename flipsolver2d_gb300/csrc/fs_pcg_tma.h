@@ -3,6 +3,8 @@
 
 #include <cuda.h>
 #include <cuda_runtime.h>
+#include <utility>
+#include <vector>
 
 #include "fs_pcg.h"
 
@@ -27,6 +29,10 @@ cudaError_t launch_pcg_tma(const PcgArgs<float> &a, const TmaMaps &maps, int ti,
 // one tile per block resident in shared memory for the whole solve; false
 // when the grid needs more tiles than there are SMs
 bool resident_tile_shape(int ni, int nj, int *ti, int *tj);
+// every feasible resident tile shape (rows, columns) of a grid, and the
+// autotuner's record of the one to use for a grid shape (ti <= 0 clears it)
+void resident_candidates(int ni, int nj, std::vector<std::pair<int, int>> *out);
+void resident_set_tuned(int ni, int nj, int ti, int tj);
 // The shared-memory-resident FP32 solve; `ll` owns the exchange-word buffers
 // (a.ll_r / a.ll_s are taken from it) and their epoch counter.
 cudaError_t launch_pcg_resident(const PcgArgs<float> &a, int ti, int tj, cudaStream_t st,

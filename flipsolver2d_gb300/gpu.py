@@ -131,6 +131,8 @@ _SIGS = {
     "fs_batch_timer": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "fs_pcg_solve_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                           ctypes.c_void_p]),
+    "fs_resident_autotune": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                            ctypes.c_void_p, ctypes.c_void_p]),
     "fs_server_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_double, ctypes.c_int, ctypes.c_void_p]),
     "fs_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
@@ -428,6 +430,16 @@ def pcg_solve_operator(cell_info: np.ndarray, rhs: np.ndarray, scale: float, ite
     _check(lib.fs_pcg_solve_operator(ni, nj, _ptr(info), scale, _ptr(b), _ptr(x), iter_limit, tol,
                                      ctypes.byref(ex), ctypes.byref(it)), "fs_pcg_solve_operator")
     return int(it.value), x
+
+
+def resident_autotune(ni: int, nj: int, device: int = 0):
+    """fs_resident_autotune: (tile rows, tile columns, us per iteration) of
+    the fastest resident tile shape, recorded for this grid shape."""
+    lib = load()
+    r, c, us = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+    _check(lib.fs_resident_autotune(int(ni), int(nj), int(device), ctypes.byref(r), ctypes.byref(c),
+                                    ctypes.byref(us)), "fs_resident_autotune")
+    return int(r.value), int(c.value), float(us.value)
 
 
 class Server:

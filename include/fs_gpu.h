@@ -394,6 +394,18 @@ fs_status fs_batch_destroy(fs_batch *batch);
  * writes 0). */
 fs_status fs_batch_timer(fs_batch *batch, int which, double *value);
 
+/* Autotuner of the FP32 solve's resident tile shape (no reference
+ * counterpart): times every shape of one tile per SM for an ni x nj grid
+ * (200 iterations of a synthetic fluid-in-a-box system, the best of three
+ * host-timed solves) and records the fastest for this grid shape in the
+ * process; handles created and FP32 solves run afterwards use it.  Results
+ * depend on the tile shape in the last bits (the order of the sums), so a
+ * process that needs reproducible FP32 bits tunes once, before its first
+ * handle, or not at all.  Without a call the shape is the one with the
+ * fewest cells per block including its ring.  Any output may be NULL. */
+fs_status fs_resident_autotune(int ni, int nj, int device, int *tile_rows, int *tile_cols,
+                               float *us_per_iteration);
+
 /* A device-resident request loop for spec-mode solves (no reference
  * counterpart; each request is the problem of fs_pcg_solve_spec, solved by the
  * cluster solve of fs_pcg_solve_batch).  One persistent launch keeps running

@@ -230,3 +230,32 @@ def test_operator_entry_point_matches_material_solve(gpu_lib, precision):
                                        precision=precision, pool_threads=POOL_THREADS)
     assert it_o == it_m
     assert np.array_equal(x_o, x_m)
+
+
+def test_resident_autotune(gpu_lib, tmp_path):
+    """fs_resident_autotune times every resident tile shape of a grid and
+    records the fastest; FP32 solves of that shape then use it and stay
+    within the FP32 bar of the FP64 mode.  Run in a child process: the
+    recorded shape lasts for the process and changes FP32 bits."""
+    import subprocess
+    import sys
+    m = random_mask(256, 21)
+    np.savez(tmp_path / "sys.npz", m=m, b=rhs_for(m, 21))
+    code = r"""
+import sys, numpy as np
+from flipsolver2d_gb300 import gpu
+rows, cols, us = gpu.resident_autotune(256, 256)
+assert cols in (32, 64, 128, 256) and rows >= 1 and us > 0, (rows, cols, us)
+assert -(-256 // rows) * -(-256 // cols) <= 256
+d = np.load(sys.argv[1])
+_, x32 = gpu.pcg_solve(d["m"], d["b"], 1 / 30, 1000.0, 1 / 256, 200, 1e-2, precision=gpu.FS_PCG_FP32)
+_, x64 = gpu.pcg_solve(d["m"], d["b"], 1 / 30, 1000.0, 1 / 256, 200, 1e-2, precision=gpu.FS_PCG_FP64)
+err = np.linalg.norm(x32 - x64) / np.linalg.norm(x64)
+print(rows, cols, us, err)
+assert err <= 1e-2, err
+"""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", code, str(tmp_path / "sys.npz")], cwd=root, capture_output=True,
+                       text=True, timeout=600)
+    print(r.stdout, r.stderr[-2000:])
+    assert r.returncode == 0
