@@ -66,10 +66,10 @@ struct LlBuffers {
     unsigned next = 0; // first epoch of the next launch; 0: clear first
 };
 // The resident kernel's small exchange-word regions, one allocation: the
-// partial records (two sets of at most 256 blocks, its tile limit, of four
-// words), then per chunk of the max-abs test the index of its last live unit
-// row (at most kLlMaxChunks chunks)
-constexpr size_t kLlRecSets = 2 * 256 * 4;
+// partial records (two sets of at most 256 blocks, its tile limit, of one
+// 128-byte line each), then per chunk of the max-abs test the index of its
+// last live unit row (at most kLlMaxChunks chunks)
+constexpr size_t kLlRecSets = 2 * 256 * 16;
 constexpr size_t kLlEffOff = kLlRecSets;
 constexpr size_t kLlMaxChunks = 4096;
 constexpr size_t kLlRecWords = kLlEffOff + kLlMaxChunks;

@@ -755,8 +755,13 @@ __device__ __forceinline__ void ld_ll2(const unsigned long long *p, unsigned lon
 
 // words of one block's partial record: hi, lo of a float-pair sum, then a
 // word whose low 31 bits are a non-negative float (a max) and whose top bit
-// is a flag (an OR), then one unused word -- 32 bytes, one sector
-constexpr int kRecWords = 4;
+// is a flag (an OR), then one unused word (spec mode: a second pair).  Each
+// record has a 128-byte line to itself: every block polls every record, and
+// with four records a line (32 bytes each) the polls of a line's four
+// readers-by-152 slowed the publishes into it -- measured on GB300, the
+// padded layout took the 1024^2 solves from 4.95 to 4.51 ms per substep and
+// the 256^2 ones from 3.43 to 2.5 ms, bit-identical
+constexpr int kRecWords = 16;
 
 // reduction k of a launch uses set k & 1 of two sets of G records
 static_assert(kRecWords * 2 * 256 == (int)kLlRecSets, "record buffer");
