@@ -57,7 +57,7 @@ WORKLOAD = "dam_break_1024_obstacle"
 # by ncu (dram__bytes_read.sum + dram__bytes_write.sum) on this workload; the
 # solve keeps its vectors on chip, so this is little more than b and the
 # operator in, x out
-PCG_TRAFFIC_BYTES = 9051456
+PCG_TRAFFIC_BYTES = 9078784
 
 
 def set_resolution(res: int):
