@@ -1243,20 +1243,20 @@ static fs_status stage(fs_solver *s, int which, bool in_step)
         }
         break;
     case FS_STAGE_LEVELSET_OUTSIDE:
-        launch_levelset(d, s->G, true, q);
-        g_kernel_launches += 1 + levelset_max_passes(d);
+        launch_levelset(d, s->G, true, q, &s->sc->pcg_status, s->ex.wait_polls);
+        g_kernel_launches += levelset_launches(d, true);
         break;
     case FS_STAGE_LEVELSET:
         if (in_step && !s->nb) {
             CK(cudaEventRecord(s->ev_p2g, q));
             CK(cudaStreamWaitEvent(s->side, s->ev_p2g, 0));
-            launch_levelset(d, s->G, false, s->side);
+            launch_levelset(d, s->G, false, s->side, &s->sc->pcg_status, s->ex.wait_polls);
             CK(cudaEventRecord(s->ev_levelset, s->side));
             s->levelset_pending = true;
         } else {
-            launch_levelset(d, s->G, false, q);
+            launch_levelset(d, s->G, false, q, &s->sc->pcg_status, s->ex.wait_polls);
         }
-        g_kernel_launches += 1 + levelset_max_passes(d);
+        g_kernel_launches += levelset_launches(d, true);
         break;
     case FS_STAGE_VEL_EXTRAP:
         launch_vel_extrapolate(d, s->G, s->sp, s->sc, false, q);

@@ -813,14 +813,14 @@ __global__ void k_levelset_init(GridDims d, const float *__restrict__ sdf,
         cells[c] = ls_pack(seed ? 0 : kMarkInf, v);
     }
     if (c < 3LL * ntiles) act[c] = 0;
-    if (c < passes) active[c] = 0;
+    if (c <= passes) active[c] = 0; // active[passes]: the one-launch form's barrier counter
 }
 
+// one BFS pass of a tile (the block); every thread of the block takes the
+// same exits
 template <class S>
-__global__ void __launch_bounds__(1024, 1) k_levelset_pass(GridDims d, float *__restrict__ sdf,
-                                                       unsigned long long *__restrict__ cells,
-                                                       uint8_t *__restrict__ act,
-                                                       int *__restrict__ active, int pass, int add)
+__device__ __forceinline__ void ls_pass(GridDims d, float *__restrict__ sdf, unsigned long long *__restrict__ cells,
+                                        uint8_t *__restrict__ act, int *__restrict__ active, int pass, int add)
 {
     extern __shared__ int ls_smem[];
     constexpr int W = S::kW;
@@ -905,6 +905,56 @@ __global__ void __launch_bounds__(1024, 1) k_levelset_pass(GridDims d, float *__
     }
 }
 
+template <class S>
+__global__ void __launch_bounds__(1024, 1) k_levelset_pass(GridDims d, float *__restrict__ sdf,
+                                                       unsigned long long *__restrict__ cells,
+                                                       uint8_t *__restrict__ act,
+                                                       int *__restrict__ active, int pass, int add)
+{
+    ls_pass<S>(d, sdf, cells, act, active, pass, add);
+}
+
+// All passes in one cooperative launch when every tile is resident at once
+// (one tile per SM): a grid barrier between passes instead of a kernel
+// boundary, and the launch ends after the first pass that assigns nothing,
+// instead of the remaining launches each returning at once.  The barrier is
+// an arrival counter (active[passes], zeroed by k_levelset_init): release
+// fence and relaxed add, then bounded acquire polls by thread 0 of a block;
+// a timeout sets *status (reported like a PCG wait) and the blocks leave.
+template <class S>
+__global__ void __launch_bounds__(1024, 1) k_levelset_all(GridDims d, float *__restrict__ sdf,
+                                                      unsigned long long *__restrict__ cells,
+                                                      uint8_t *__restrict__ act, int *__restrict__ active,
+                                                      int passes, int add, int *__restrict__ status,
+                                                      long long lim)
+{
+    unsigned *count = reinterpret_cast<unsigned *>(active + passes);
+    const unsigned nb = gridDim.x * gridDim.y;
+    for (int pass = 0; pass < passes; pass++) {
+        if (pass > 0 && ((volatile int *)active)[pass - 1] == 0) break; // the same in every block
+        ls_pass<S>(d, sdf, cells, act, active, pass, add);
+        __syncthreads();
+        int gave_up = 0;
+        if (threadIdx.x == 0) {
+            asm volatile("fence.acq_rel.gpu;" ::: "memory");
+            asm volatile("red.relaxed.gpu.global.add.u32 [%0], 1;" ::"l"(count) : "memory");
+            const unsigned target = (unsigned)(pass + 1) * nb;
+            long long spins = 0;
+            for (;;) {
+                unsigned v;
+                asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(count) : "memory");
+                if ((int)(v - target) >= 0) break;
+                if (++spins > lim || ((spins & 1023) == 0 && *((volatile int *)status) != 0)) {
+                    atomicExch(status, 1);
+                    gave_up = 1;
+                    break;
+                }
+            }
+        }
+        if (__syncthreads_or(gave_up)) return;
+    }
+}
+
 // waves per BFS layer: a pass of H layers plus the tile load (about five
 // layers' time) runs its tiles in ceil(tiles / SMs) waves
 static bool ls_wide(const GridDims &d)
@@ -923,7 +973,28 @@ int levelset_max_passes(const GridDims &d)
     return m / (ls_wide(d) ? LsWide::kHalo : LsNarrow::kHalo) + 2;
 }
 
-template <class S> static void launch_levelset_shape(const GridDims &d, Grids &G, bool outside, cudaStream_t st)
+// whether every tile of shape S fits on the device at once (one launch)
+template <class S> static bool ls_one_launch(const GridDims &d)
+{
+    const long long tiles = (long long)nblk(d.nj, S::kTile) * nblk(d.ni, S::kTile);
+    static std::atomic<int> slots[kMaxDevices];
+    const int per_sm = device_cached(slots, [] {
+        cudaFuncSetAttribute((const void *)k_levelset_all<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)S::kSmem);
+        int nb = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void *)k_levelset_all<S>, 1024, S::kSmem) !=
+            cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+        return nb;
+    });
+    return per_sm > 0 && tiles <= (long long)per_sm * device_sm_count();
+}
+
+template <class S>
+static void launch_levelset_shape(const GridDims &d, Grids &G, bool outside, cudaStream_t st, int *status,
+                                  long long spin_limit)
 {
     constexpr int kLsTile = S::kTile;
     const int passes = levelset_max_passes(d);
@@ -931,12 +1002,28 @@ template <class S> static void launch_levelset_shape(const GridDims &d, Grids &G
     const int ntiles = grid.x * grid.y;
     const long long n = (long long)d.ni * d.nj;
     long long init_n = n > 3LL * ntiles ? n : 3LL * ntiles;
-    if (init_n < passes) init_n = passes;
+    if (init_n < passes + 1) init_n = passes + 1;
     unsigned long long *cells = reinterpret_cast<unsigned long long *>(G.levelset_cells);
     k_levelset_init<<<nblk(init_n, kThreads), kThreads, 0, st>>>(d, G.fluid_sdf, cells,
                                                                G.levelset_act, ntiles,
                                                                G.levelset_active, passes,
                                                                outside ? 1 : 0);
+    if (status && ls_one_launch<S>(d)) {
+        cudaFuncSetAttribute((const void *)k_levelset_all<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)S::kSmem);
+        GridDims dd = d;
+        float *sdf = G.fluid_sdf;
+        uint8_t *act = G.levelset_act;
+        int *active = G.levelset_active;
+        int np = passes, add = outside ? 1 : -1;
+        int *stp = status;
+        long long lim = spin_limit > 0 ? spin_limit : (1LL << 25);
+        void *args[] = {&dd, &sdf, &cells, &act, &active, &np, &add, &stp, &lim};
+        if (cudaLaunchCooperativeKernel((const void *)k_levelset_all<S>, grid, dim3(1024), args, S::kSmem, st) ==
+            cudaSuccess)
+            return;
+        cudaGetLastError(); // not launched: the passes one launch each
+    }
     cudaFuncSetAttribute((const void *)k_levelset_pass<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)S::kSmem);
     for (int p = 0; p < passes; p++)
@@ -944,10 +1031,16 @@ template <class S> static void launch_levelset_shape(const GridDims &d, Grids &G
                                                           G.levelset_active, p, outside ? 1 : -1);
 }
 
-void launch_levelset(const GridDims &d, Grids &G, bool outside, cudaStream_t st)
+void launch_levelset(const GridDims &d, Grids &G, bool outside, cudaStream_t st, int *status, long long spin_limit)
 {
-    if (ls_wide(d)) launch_levelset_shape<LsWide>(d, G, outside, st);
-    else launch_levelset_shape<LsNarrow>(d, G, outside, st);
+    if (ls_wide(d)) launch_levelset_shape<LsWide>(d, G, outside, st, status, spin_limit);
+    else launch_levelset_shape<LsNarrow>(d, G, outside, st, status, spin_limit);
+}
+
+int levelset_launches(const GridDims &d, bool with_status)
+{
+    const bool one = with_status && (ls_wide(d) ? ls_one_launch<LsWide>(d) : ls_one_launch<LsNarrow>(d));
+    return one ? 2 : 1 + levelset_max_passes(d);
 }
 
 // ---------------------------------------------------------------------------

@@ -167,7 +167,12 @@ void launch_density_grid(const GridDims &d, const SceneParams &sp, const Particl
 void launch_p2g_sdf_materials(const GridDims &d, const SceneParams &sp, const Particles &P,
                               const Grids &G, bool nb, cudaStream_t st);
 // extrapolateLevelsetInside, or with `outside` extrapolateLevelsetOutside
-void launch_levelset(const GridDims &d, Grids &G, bool outside, cudaStream_t st);
+// status (may be null): with it, and when every tile fits on the device at
+// once, all passes run in one cooperative launch whose grid-barrier timeouts
+// set *status; spin_limit: polls before a barrier wait gives up (0: default)
+void launch_levelset(const GridDims &d, Grids &G, bool outside, cudaStream_t st, int *status = nullptr,
+                     long long spin_limit = 0);
+int levelset_launches(const GridDims &d, bool with_status); // kernels one launch_levelset enqueues
 void launch_vel_extrapolate(const GridDims &d, Grids &G, const SceneParams &sp,
                             const Scalars *sc, bool save_and_gravity, cudaStream_t st);
 void launch_pressure_rhs(const GridDims &d, const Grids &G, void *rhs, int rhs_is_double,
