@@ -1033,10 +1033,10 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     // chunks without a unit row report DBL_MIN (VOps::maxAbs) on every iteration
     int has_min_static = 0;
     for (int k = 0; k < a.nchunks; k++) has_min_static |= a.chunk_last_unit[k] < 0;
-    // Live chunk ends: a unit row whose b is zero and whose fluid neighbours
-    // are none, or one that has no other (a one- or two-cell droplet), keeps
-    // r exactly zero through every iteration (A s, z = M r and s there only
-    // combine zeros).  The max-abs value of a chunk -- |r| at its last nonzero
+    // Live chunk ends: a unit row whose b is zero, in a fluid component of
+    // at most four cells that all have b = 0 and whose non-fluid neighbours
+    // have b = 0 (a small droplet), keeps r exactly zero through every
+    // iteration (A s, z = M r and s there only combine zeros).  The max-abs value of a chunk -- |r| at its last nonzero
     // entry -- therefore never comes from such a row, and its last live unit
     // row serves as the chunk's end: a flying droplet at the end of a chunk
     // no longer sends every iteration to the backward search.  Per launch,
@@ -1247,6 +1247,40 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
             }
             return lo;
         };
+        // A unit row with b = 0 whose fluid component has at most kDeadCells
+        // cells, all with b = 0, and whose non-fluid neighbours hold b = 0 as
+        // well: r, s and z stay exactly zero there (the operator couples it
+        // only to the component; M also reads the non-fluid neighbours, whose
+        // identity rows keep r = b = 0).  A small flood over the operator
+        // bytes and b in global memory (set-up only).
+        constexpr int kDeadCells = 4;
+        auto dead_unit = [&](int e0) -> bool {
+            int comp[kDeadCells];
+            int n = 0;
+            comp[n++] = e0;
+            for (int k = 0; k < n; k++) {
+                const int e = comp[k];
+                const int ei = e / NJ, ej = e - ei * NJ;
+                const unsigned p = __ldg(a.info + e);
+                const int nbr[4] = {e - NJ, e + NJ, e - 1, e + 1};
+                const bool in[4] = {ei > 0, ei < NI - 1, ej > 0, ej < NJ - 1};
+#pragma unroll
+                for (int t = 0; t < 4; t++) {
+                    if (!in[t]) continue;
+                    const int f = nbr[t];
+                    if (p & (1u << t)) { // a fluid neighbour: part of the component
+                        bool seen = false;
+                        for (int u = 0; u < n; u++) seen |= comp[u] == f;
+                        if (seen) continue;
+                        if (n == kDeadCells || __ldg(a.b + f) != 0.f) return false;
+                        comp[n++] = f;
+                    } else if (__ldg(a.b + f) != 0.f) {
+                        return false;
+                    }
+                }
+            }
+            return true;
+        };
         const unsigned long long tag = (unsigned long long)ep0 << 32;
         unsigned long long wbest = 0ull;
         int wk = -1;
@@ -1258,15 +1292,7 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
                 bool live = false;
                 if (q < tj && gj < NJ) {
                     const int c = (r + 2) * w2 + (q + 2);
-                    const unsigned p = Ib[c];
-                    const unsigned msk = p & 0xfu;
-                    const int nf = __popc(msk);
-                    if ((p & 0x80u) && (Rb[c] != 0.f || nf > 1)) {
-                        live = true;
-                    } else if ((p & 0x80u) && nf == 1) {
-                        const int cn = c + ((msk & 1u) ? -w2 : (msk & 2u) ? w2 : (msk & 4u) ? -1 : 1);
-                        live = !(Rb[cn] == 0.f && __popc(Ib[cn] & 0xfu) == 1);
-                    }
+                    if (Ib[c] & 0x80u) live = Rb[c] != 0.f || !dead_unit(gi * NJ + gj);
                 }
                 unsigned lv = __ballot_sync(0xffffffffu, live);
                 if (!lv) continue;
