@@ -637,14 +637,16 @@ def gpu_arm(args):
         except Exception as e:  # reported, never fatal for the main line
             line["poisson_2048"] = {"error": str(e)}
     if rank == 0 and world == 1 and not args.no_batch:
-        # the batched form of the same path beside the single-scene line: 64
-        # scenes of the batched-scenes workload stepped together, and 16 of
-        # them one at a time, both at a 1e-6 pressure residual
+        # the batched form of the same path beside the single-scene line: the
+        # batched-scenes workload at its configured size, 256 scenes stepped
+        # together, and 16 of them one at a time, both at a 1e-6 pressure
+        # residual
         try:
-            r = batch_measure(64, 2, 3, 16)
+            r = batch_measure(BATCH_SCENES, 2, 3, 16)
             bv = r["work"] / (r["total_ms"] / 1e3)
             ss = line.get("spec_single", {}).get("value")
-            line["batch"] = {"workload": "batch_64_scenes (sides 64-512, seeds 1000..1063)",
+            line["batch"] = {"workload": f"batch_{BATCH_SCENES}_scenes (sides 64-512, seeds "
+                                         f"1000..{1000 + BATCH_SCENES - 1})",
                              "value": bv, "unit": METRIC, "frames": 3,
                              "vs_spec_single_1024": bv / ss if ss else None,
                              "ms_per_frame": r["total_ms"] / 3,
@@ -702,6 +704,7 @@ def gpu_arm(args):
 
 
 NB_WARM_FRAMES = 4
+BATCH_SCENES = 256
 SERVE_SUBOBJECT_REQUESTS = 120
 SERVE_DEVICE_REQUESTS = 400
 
