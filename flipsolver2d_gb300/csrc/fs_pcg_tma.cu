@@ -1440,13 +1440,24 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
     // both loads issued before either is polled.  A block barrier, then a
     // block-uniform false on timeout.
     auto load_ring1 = [&](float *dst, const unsigned long long *src, unsigned ep) -> bool {
+        // strips of one or two rows (small grids): a quarter of the threads
+        // poll, four cells each -- fewer pollers at once (256^2: 2.27
+        // against 2.6 ms of PCG per substep on GB300; at 1024^2 the same
+        // cost 6 %, so taller strips keep two cells a thread on every thread)
+        constexpr int kC = RPS <= 2 ? 4 : 2;
         const int n = 2 * w1 + 2 * ti;
-        const int nt = (int)blockDim.x;
-        for (int k0 = threadIdx.x; k0 < n; k0 += 2 * nt) {
-            int g[2] = {-1, -1}, cell[2] = {-1, -1};
-            unsigned long long w[2] = {0ull, 0ull};
+        const int nt = kC == 4 ? (int)blockDim.x / 4 : (int)blockDim.x;
+        for (int k0 = threadIdx.x; k0 < n && (int)threadIdx.x < nt; k0 += kC * nt) {
+            int g[kC], cell[kC];
+            unsigned long long w[kC];
 #pragma unroll
-            for (int h = 0; h < 2; h++) {
+            for (int h = 0; h < kC; h++) {
+                g[h] = -1;
+                cell[h] = -1;
+                w[h] = 0ull;
+            }
+#pragma unroll
+            for (int h = 0; h < kC; h++) {
                 const int k = k0 + h * nt;
                 if (k >= n) continue;
                 int hr, hq;
@@ -1465,7 +1476,7 @@ k_pcg_resident(PcgArgs<float> a, int ti, int tj)
                 }
             }
 #pragma unroll
-            for (int h = 0; h < 2; h++) {
+            for (int h = 0; h < kC; h++) {
                 if (cell[h] < 0) continue;
                 float v = 0.f;
                 if (g[h] >= 0) {
